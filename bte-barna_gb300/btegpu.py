@@ -1,0 +1,267 @@
+"""Python host interface of the GB300 engine (ctypes over libbtegpu.so).
+
+Mirrors the reference's run interface for the RTA particle loop: load a mode
+table and a geometry, then run with the <RTA_MC2d> parameters (T0, dt,
+maxtime, N, ballistic) and read back the temperature / jx / jy arrays that
+RTAMC2D writes to temperature_*.csv, jx_*.csv and jy_*.csv
+(src/RTA_MC2D.cpp:2437-2471).  Errors raise BteError carrying the status code
+that maps to the reference's exception types (include/exceptions.hpp).
+
+The CUDA library is the only compute path: if it cannot be loaded this module
+raises instead of falling back to anything else.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libbtegpu.so")
+
+BTE_OK, BTE_ERR_INPUT, BTE_ERR_VALUE, BTE_ERR_GEOMETRY, BTE_ERR_LIMIT, BTE_ERR_CUDA, BTE_ERR_STATE = range(7)
+STATUS_NAMES = {0: "ok", 1: "input_error", 2: "value_error", 3: "geometry_error",
+                4: "limit", 5: "cuda_error", 6: "state_error"}
+MODE_REPLAY, MODE_PRODUCTION = 0, 1
+SOURCE_WALLS, SOURCE_INITIAL = 0, 1
+
+# Exported symbols declared in include/btegpu.h.
+PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
+                  "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
+                  "bte_version"]
+
+
+class BteError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class DeviceOpts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("verbose", C.c_int32)]
+
+
+class ModeTable(C.Structure):
+    _fields_ = [("nq", C.c_int32), ("nb", C.c_int32), ("grid", C.c_int32 * 3),
+                ("omega", C.POINTER(C.c_double)), ("vg", C.POINTER(C.c_double)),
+                ("w", C.POINTER(C.c_double)), ("dq", C.POINTER(C.c_double)),
+                ("V", C.c_double), ("c_lat", C.c_double)]
+
+
+class Geometry(C.Structure):
+    _fields_ = [("nboxes", C.c_int32), ("npoints", C.POINTER(C.c_int32)),
+                ("vertices", C.POINTER(C.c_double)), ("Teq", C.POINTER(C.c_double)),
+                ("Tinit", C.POINTER(C.c_double)), ("reservoir", C.POINTER(C.c_int32)),
+                ("thickness", C.c_double)]
+
+
+class RtaParams(C.Structure):
+    _fields_ = [("T0", C.c_double), ("dt", C.c_double), ("maxtime", C.c_double),
+                ("nparticles", C.c_int64), ("seed", C.c_uint64), ("mode", C.c_int32),
+                ("source", C.c_int32), ("ballistic", C.c_int32), ("reserved0", C.c_int32),
+                ("specularity", C.c_double), ("particle_begin", C.c_int64),
+                ("particle_end", C.c_int64)]
+
+
+class RtaResult(C.Structure):
+    _fields_ = [("nboxes", C.c_int32), ("nbins", C.c_int32),
+                ("gz", C.POINTER(C.c_double)), ("gz_jx", C.POINTER(C.c_double)),
+                ("gz_jy", C.POINTER(C.c_double)), ("temperature", C.POINTER(C.c_double)),
+                ("jx", C.POINTER(C.c_double)), ("jy", C.POINTER(C.c_double)),
+                ("exact", C.POINTER(C.c_int64)), ("Eeff", C.c_double),
+                ("energy_rate", C.c_double), ("events", C.c_int64), ("wall_hits", C.c_int64),
+                ("crossings", C.c_int64), ("absorbed", C.c_int64),
+                ("specular_hits", C.c_int64), ("tally_updates", C.c_int64),
+                ("kernel_ms", C.c_double)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
+                ("smem_tally", C.c_int32), ("smem_alias", C.c_int32)]
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def mode_struct(m: dict):
+    """ModeTable over the arrays of a synth.mode_table dict (keeps refs)."""
+    keep = {k: np.ascontiguousarray(m[k], dtype=np.float64) for k in ("omega", "vg", "w", "dq")}
+    s = ModeTable()
+    s.nq, s.nb = int(m["nq"]), int(m["nb"])
+    for i in range(3):
+        s.grid[i] = int(m["grid"][i])
+    s.omega, s.vg, s.w, s.dq = (_dptr(keep[k]) for k in ("omega", "vg", "w", "dq"))
+    s.V, s.c_lat = float(m["V"]), float(m["c_lat"])
+    return s, keep
+
+
+def geom_struct(g: dict):
+    keep = {"npoints": np.ascontiguousarray(g["npoints"], dtype=np.int32),
+            "vertices": np.ascontiguousarray(g["vertices"], dtype=np.float64),
+            "Teq": np.ascontiguousarray(g["Teq"], dtype=np.float64),
+            "Tinit": np.ascontiguousarray(g.get("Tinit", g["Teq"]), dtype=np.float64),
+            "reservoir": np.ascontiguousarray(g["reservoir"], dtype=np.int32)}
+    s = Geometry()
+    s.nboxes = int(g["nboxes"])
+    s.npoints = _iptr(keep["npoints"])
+    s.vertices = _dptr(keep["vertices"])
+    s.Teq = _dptr(keep["Teq"])
+    s.Tinit = _dptr(keep["Tinit"])
+    s.reservoir = _iptr(keep["reservoir"])
+    s.thickness = float(g["thickness"])
+    return s, keep
+
+
+def params_struct(T0, dt, maxtime, N, seed=1, mode=MODE_PRODUCTION, source=SOURCE_WALLS,
+                  ballistic=False, specularity=0.0, begin=0, end=0):
+    p = RtaParams()
+    p.T0, p.dt, p.maxtime, p.nparticles, p.seed = float(T0), float(dt), float(maxtime), int(N), int(seed)
+    p.mode, p.source, p.ballistic = int(mode), int(source), int(bool(ballistic))
+    p.specularity, p.particle_begin, p.particle_end = float(specularity), int(begin), int(end)
+    return p
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libbtegpu.so (raises OSError when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError(f"{path} is missing: run __graft_entry__.build() first")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    lib.bte_create.argtypes = [C.POINTER(vp), C.POINTER(DeviceOpts)]
+    lib.bte_destroy.argtypes = [vp]
+    lib.bte_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    lib.bte_load_modes.argtypes = [vp, C.POINTER(ModeTable)]
+    lib.bte_load_geometry.argtypes = [vp, C.POINTER(Geometry)]
+    lib.bte_rta_run.argtypes = [vp, C.POINTER(RtaParams), C.POINTER(RtaResult)]
+    lib.bte_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    lib.bte_query_sizes.argtypes = [vp, C.POINTER(RtaParams), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    lib.bte_version.restype = C.c_int32
+    for f in ("bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
+              "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes"):
+        getattr(lib, f).restype = C.c_int
+    lib.btegpu_debug_geometry.argtypes = [C.POINTER(Geometry), C.POINTER(C.c_double), C.c_longlong]
+    lib.btegpu_debug_geometry.restype = C.c_longlong
+    lib.btegpu_debug_grid.argtypes = [C.POINTER(Geometry), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.btegpu_debug_lambert.argtypes = [C.POINTER(ModeTable), C.POINTER(Geometry),
+                                         C.POINTER(C.c_longlong), C.c_int]
+    lib.btegpu_debug_lambert.restype = C.c_longlong
+    lib.btegpu_debug_log.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong]
+    _lib = lib
+    return lib
+
+
+class Engine:
+    """One engine context on one CUDA device."""
+
+    def __init__(self, device: int = 0, verbose: bool = False):
+        self.lib = load_library()
+        self.ctx = C.c_void_p()
+        opts = DeviceOpts(device, int(verbose))
+        st = self.lib.bte_create(C.byref(self.ctx), C.byref(opts))
+        if st != BTE_OK:
+            buf = C.create_string_buffer(512)
+            self.lib.bte_last_error(None, buf, 512)
+            raise BteError(st, buf.value.decode())
+        self._keep = {}
+
+    def close(self):
+        if self.ctx:
+            self.lib.bte_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != BTE_OK:
+            buf = C.create_string_buffer(1024)
+            self.lib.bte_last_error(self.ctx, buf, 1024)
+            raise BteError(st, buf.value.decode())
+
+    def load_modes(self, m: dict):
+        s, keep = mode_struct(m)
+        self._check(self.lib.bte_load_modes(self.ctx, C.byref(s)))
+        self._keep["modes"] = keep
+
+    def load_geometry(self, g: dict):
+        s, keep = geom_struct(g)
+        self._check(self.lib.bte_load_geometry(self.ctx, C.byref(s)))
+        self._keep["geom"] = keep
+        self.nboxes = int(g["nboxes"])
+
+    def set_tuning(self, block_threads=0, blocks_per_sm=0, smem_tally=1, smem_alias=0):
+        t = Tuning(block_threads, blocks_per_sm, smem_tally, smem_alias)
+        self._check(self.lib.bte_set_tuning(self.ctx, C.byref(t)))
+
+    def rta_run(self, T0, dt, maxtime, N, seed=1, mode=MODE_PRODUCTION, source=SOURCE_WALLS,
+                ballistic=False, specularity=0.0, begin=0, end=0, raw=True, exact=False):
+        p = params_struct(T0, dt, maxtime, N, seed, mode, source, ballistic, specularity, begin, end)
+        nbx, nbn, nm = C.c_int32(), C.c_int32(), C.c_int64()
+        self._check(self.lib.bte_query_sizes(self.ctx, C.byref(p), C.byref(nbx), C.byref(nbn), C.byref(nm)))
+        shape = (nbx.value, nbn.value)
+        out = {k: np.zeros(shape) for k in ("temperature", "jx", "jy")}
+        r = RtaResult()
+        r.temperature, r.jx, r.jy = (_dptr(out[k]) for k in ("temperature", "jx", "jy"))
+        if raw:
+            for k in ("gz", "gz_jx", "gz_jy"):
+                out[k] = np.zeros(shape)
+            r.gz, r.gz_jx, r.gz_jy = (_dptr(out[k]) for k in ("gz", "gz_jx", "gz_jy"))
+        if exact:
+            out["exact"] = np.zeros(shape + (3, 2), dtype=np.int64)
+            r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
+        self._check(self.lib.bte_rta_run(self.ctx, C.byref(p), C.byref(r)))
+        for k in ("Eeff", "energy_rate", "events", "wall_hits", "crossings", "absorbed",
+                  "specular_hits", "tally_updates", "kernel_ms"):
+            out[k] = getattr(r, k)
+        return out
+
+
+def debug_geometry(g: dict) -> np.ndarray:
+    lib = load_library()
+    s, keep = geom_struct(g)
+    n = lib.btegpu_debug_geometry(C.byref(s), None, 0)
+    if n < 0:
+        raise BteError(BTE_ERR_GEOMETRY, "geometry build failed")
+    out = np.zeros(n)
+    lib.btegpu_debug_geometry(C.byref(s), _dptr(out), n)
+    return out
+
+
+def debug_grid(g: dict):
+    lib = load_library()
+    s, keep = geom_struct(g)
+    nx, ny = C.c_int(), C.c_int()
+    r = lib.btegpu_debug_grid(C.byref(s), C.byref(nx), C.byref(ny))
+    return r, nx.value, ny.value
+
+
+def debug_lambert(m: dict, g: dict, maxclass: int = 16):
+    lib = load_library()
+    ms, k1 = mode_struct(m)
+    gs, k2 = geom_struct(g)
+    nnz = np.zeros(maxclass, dtype=np.int64)
+    tot = lib.btegpu_debug_lambert(C.byref(ms), C.byref(gs),
+                                   nnz.ctypes.data_as(C.POINTER(C.c_longlong)), maxclass)
+    return tot, nnz
+
+
+def debug_log(x: np.ndarray) -> np.ndarray:
+    lib = load_library()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    lib.btegpu_debug_log(_dptr(x), _dptr(y), x.size)
+    return y

@@ -1,0 +1,652 @@
+// capi.cu - the C ABI of include/btegpu.h: context, device tables, run
+// orchestration and the post-processing of src/RTA_MC2D.cpp:2326-2435.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/btegpu.h"
+#include "btegpu_debug.h"
+#include "kernels.h"
+#include "tables.hpp"
+
+using bte::Error;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess)
+        throw Error(BTE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Owned device allocation.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void alloc(size_t n) {
+        if (n == 0) n = 16;
+        if (p && bytes >= n) return;
+        release();
+        ck(cudaMalloc(&p, n), "cudaMalloc");
+        bytes = n;
+    }
+    template <class T>
+    void upload(const std::vector<T>& v, cudaStream_t s) {
+        alloc(v.size() * sizeof(T));
+        if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+int hw_threads() {
+    unsigned n = std::thread::hardware_concurrency();
+    return n ? int(std::min(n, 64u)) : 4;
+}
+
+}  // namespace
+
+struct bte_ctx {
+    int device = 0;
+    int nsm = 0;
+    int verbose = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    bte::ProdTuning tune{0, 0, 1, 0};
+
+    bool have_modes = false, have_geom = false;
+    bte::HostModes modes;
+    bte::HostGeometry geom;
+
+    // static tables
+    bool modes_dev = false, geom_dev = false, lambert_dev = false;
+    DBuf d_vxc, d_vyc, d_w, d_tau, d_mv;
+    DBuf d_boxes, d_hull, d_borders, d_contacts;
+    DBuf d_gx, d_gy, d_gcell, d_boxcell;
+    DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;
+    int nclass = 0;
+    bool have_mirror = false;
+    // per-T0 resampling
+    double resample_T0 = -1;
+    DBuf d_rcdf, d_rprob, d_ralt;
+    // generators
+    int gen_key_source = -1;
+    long long gen_key_n = -1;
+    unsigned long long gen_key_seed = 0;
+    bte::Generators gens;
+    double gen_Eeff = 0;
+    DBuf d_gcdf, d_gprob, d_galt, d_walls, d_wcum, d_ifirst, d_ibox, d_isign;
+    // run buffers
+    DBuf d_time, d_tally, d_counters, d_err, d_work;
+    std::vector<double> h_time;
+};
+
+namespace {
+
+void sync(bte_ctx* c) { ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"); }
+
+void ensure_static(bte_ctx* c) {
+    const bte::HostModes& m = c->modes;
+    const bte::HostGeometry& g = c->geom;
+    const std::size_t n = m.n();
+    if (!c->modes_dev) {
+        std::vector<double> tau(n);
+        std::vector<bte::ModeVel> mv(n);
+        for (std::size_t k = 0; k < n; ++k) {
+            tau[k] = m.w[k] > 0. ? 1.0 / m.w[k] : 0.;
+            mv[k].vx = m.vxc[k];
+            mv[k].vy = m.vyc[k];
+            mv[k].ivx = m.vxc[k] != 0. ? 1.0 / m.vxc[k] : 0.;
+            mv[k].ivy = m.vyc[k] != 0. ? 1.0 / m.vyc[k] : 0.;
+        }
+        c->d_vxc.upload(m.vxc, c->stream);
+        c->d_vyc.upload(m.vyc, c->stream);
+        c->d_w.upload(m.w, c->stream);
+        c->d_tau.upload(tau, c->stream);
+        c->d_mv.upload(mv, c->stream);
+        sync(c);
+        c->modes_dev = true;
+    }
+    if (!c->geom_dev) {
+        c->d_boxes.upload(g.boxes, c->stream);
+        c->d_hull.upload(g.hull, c->stream);
+        c->d_borders.upload(g.borders, c->stream);
+        c->d_contacts.upload(g.contacts, c->stream);
+        if (g.rect_grid) {
+            c->d_gx.upload(g.gx, c->stream);
+            c->d_gy.upload(g.gy, c->stream);
+            c->d_gcell.upload(g.gcell, c->stream);
+            std::vector<int2> bc(g.boxes.size(), make_int2(-1, -1));
+            for (int i = 0; i < g.gnx; ++i)
+                for (int j = 0; j < g.gny; ++j) {
+                    int v = g.gcell[std::size_t(i) * g.gny + j];
+                    int b = v >= 0 ? v : (v <= -2 ? -2 - v : -1);
+                    if (b >= 0) bc[std::size_t(b)] = make_int2(i, j);
+                }
+            c->d_boxcell.upload(bc, c->stream);
+        }
+        sync(c);
+        c->geom_dev = true;
+    }
+    if (!c->lambert_dev) {
+        bte::LambertTable L = bte::build_lambert(m, g, hw_threads());
+        c->nclass = L.nclass;
+        c->d_row_ptr.upload(L.row_ptr, c->stream);
+        c->d_lcol.upload(L.col, c->stream);
+        c->d_lcdf.upload(L.cdf, c->stream);
+        c->d_lalias.upload(L.alias, c->stream);
+        std::vector<int> mir = bte::build_mirror(m, g);
+        c->have_mirror = std::any_of(mir.begin(), mir.end(), [](int x) { return x >= 0; });
+        c->d_mirror.upload(mir, c->stream);
+        sync(c);
+        c->lambert_dev = true;
+        if (c->verbose)
+            std::printf("#Diffusive table: %d wall normals, %zu entries\n", L.nclass, L.col.size());
+    }
+}
+
+void ensure_resample(bte_ctx* c, double T0) {
+    if (c->resample_T0 == T0) return;
+    std::vector<double> cdf;
+    std::vector<bte::Alias> al;
+    bte::build_resample(c->modes, T0, cdf, al);
+    std::vector<float> prob(al.size());
+    std::vector<int> alt(al.size());
+    for (std::size_t i = 0; i < al.size(); ++i) {
+        prob[i] = al[i].prob;
+        alt[i] = al[i].alt;
+    }
+    c->d_rcdf.upload(cdf, c->stream);
+    c->d_rprob.upload(prob, c->stream);
+    c->d_ralt.upload(alt, c->stream);
+    sync(c);
+    c->resample_T0 = T0;
+}
+
+void ensure_generators(bte_ctx* c, const bte_rta_params* p) {
+    if (c->gen_key_source == p->source) {
+        if (p->source == BTE_SOURCE_INITIAL &&
+            (c->gen_key_n != p->nparticles || c->gen_key_seed != p->seed)) {
+            c->gen_Eeff = bte::initial_counts(c->gens, p->nparticles, p->seed);
+            c->d_ifirst.upload(c->gens.init_first, c->stream);
+            sync(c);
+            c->gen_key_n = p->nparticles;
+            c->gen_key_seed = p->seed;
+        }
+        return;
+    }
+    if (p->source == BTE_SOURCE_WALLS) {
+        c->gens = bte::build_wall_generators(c->modes, c->geom);
+    } else {
+        c->gens = bte::build_initial_generators(c->modes, c->geom);
+        c->gen_Eeff = bte::initial_counts(c->gens, p->nparticles, p->seed);
+    }
+    std::vector<float> prob(c->gens.alias.size());
+    std::vector<int> alt(c->gens.alias.size());
+    for (std::size_t i = 0; i < prob.size(); ++i) {
+        prob[i] = c->gens.alias[i].prob;
+        alt[i] = c->gens.alias[i].alt;
+    }
+    c->d_gcdf.upload(c->gens.cdf, c->stream);
+    c->d_gprob.upload(prob, c->stream);
+    c->d_galt.upload(alt, c->stream);
+    std::vector<bte::WallGenDev> wd;
+    for (auto& W : c->gens.walls) {
+        bte::WallGenDev d;
+        d.p1 = W.p1;
+        d.nd = W.nd;
+        d.sa = W.sa;
+        d.sb = W.sb;
+        d.box = W.box;
+        d.sign = W.sign;
+        wd.push_back(d);
+    }
+    c->d_walls.upload(wd, c->stream);
+    c->d_wcum.upload(c->gens.wall_cum, c->stream);
+    c->d_ifirst.upload(c->gens.init_first, c->stream);
+    c->d_ibox.upload(c->gens.init_box, c->stream);
+    c->d_isign.upload(c->gens.init_sign, c->stream);
+    sync(c);
+    c->gen_key_source = p->source;
+    c->gen_key_n = p->nparticles;
+    c->gen_key_seed = p->seed;
+}
+
+bte_status fail(bte_ctx* c, const Error& e) {
+    c->err = e.what();
+    return e.code;
+}
+
+void validate(const bte_rta_params* p) {
+    if (!p) throw Error(BTE_ERR_INPUT, "null parameters");
+    if (!(p->dt > 0.) || !(p->maxtime > 0.) || !std::isfinite(p->dt) || !std::isfinite(p->maxtime))
+        throw Error(BTE_ERR_INPUT, "time dt and maxtime must be positive");
+    if (p->maxtime / p->dt > 1.0e7) throw Error(BTE_ERR_INPUT, "too many time bins");
+    if (p->nparticles < 1) throw Error(BTE_ERR_INPUT, "particles N must be >= 1");
+    if (p->mode != BTE_MODE_REPLAY && p->mode != BTE_MODE_PRODUCTION)
+        throw Error(BTE_ERR_INPUT, "unknown mode");
+    if (p->source != BTE_SOURCE_WALLS && p->source != BTE_SOURCE_INITIAL)
+        throw Error(BTE_ERR_INPUT, "unknown particle source");
+    if (!(p->specularity >= 0. && p->specularity <= 1.))
+        throw Error(BTE_ERR_INPUT, "specularity must lie in [0, 1]");
+    if (!(p->T0 > 0.)) throw Error(BTE_ERR_INPUT, "T0 must be positive");
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t bte_version(void) { return BTEGPU_VERSION; }
+
+bte_status bte_create(bte_ctx** out, const bte_device_opts* opts) {
+    if (!out) return BTE_ERR_INPUT;
+    *out = nullptr;
+    try {
+        std::unique_ptr<bte_ctx> c(new bte_ctx());
+        c->device = opts ? opts->device : 0;
+        c->verbose = opts ? opts->verbose : 0;
+        int ndev = 0;
+        ck(cudaGetDeviceCount(&ndev), "cudaGetDeviceCount");
+        if (c->device < 0 || c->device >= ndev) throw Error(BTE_ERR_INPUT, "no such CUDA device");
+        ck(cudaSetDevice(c->device), "cudaSetDevice");
+        ck(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device), "attribute");
+        ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaEventCreate(&c->ev0), "cudaEventCreate");
+        ck(cudaEventCreate(&c->ev1), "cudaEventCreate");
+        *out = c.release();
+        return BTE_OK;
+    } catch (const Error& e) {
+        g_create_error = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return BTE_ERR_CUDA;
+    }
+}
+
+bte_status bte_destroy(bte_ctx* c) {
+    if (!c) return BTE_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    cudaStream_t s = c->stream;
+    delete c;
+    if (s) cudaStreamDestroy(s);
+    return BTE_OK;
+}
+
+bte_status bte_last_error(const bte_ctx* c, char* buf, size_t size) {
+    if (!buf || size == 0) return BTE_ERR_INPUT;
+    const std::string& m = c ? c->err : g_create_error;
+    std::snprintf(buf, size, "%s", m.c_str());
+    return BTE_OK;
+}
+
+bte_status bte_set_tuning(bte_ctx* c, const bte_tuning* t) {
+    if (!c) return BTE_ERR_INPUT;
+    if (!t) {
+        c->tune = bte::ProdTuning{0, 0, 1, 0};
+        return BTE_OK;
+    }
+    if (t->block_threads < 0 || t->block_threads > 256 || (t->block_threads % 32) != 0) {
+        c->err = "block_threads must be a multiple of 32 in [32, 256] (0 = default)";
+        return BTE_ERR_INPUT;
+    }
+    c->tune.block_threads = t->block_threads;
+    c->tune.blocks_per_sm = t->blocks_per_sm;
+    c->tune.smem_tally = t->smem_tally;
+    c->tune.smem_alias = t->smem_alias;
+    return BTE_OK;
+}
+
+bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
+    if (!c) return BTE_ERR_INPUT;
+    try {
+        ck(cudaSetDevice(c->device), "cudaSetDevice");
+        c->modes = bte::build_modes(mt);
+        c->have_modes = true;
+        c->modes_dev = false;
+        c->lambert_dev = false;
+        c->resample_T0 = -1;
+        c->gen_key_source = -1;
+        return BTE_OK;
+    } catch (const Error& e) {
+        return fail(c, e);
+    }
+}
+
+bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
+    if (!c) return BTE_ERR_INPUT;
+    try {
+        ck(cudaSetDevice(c->device), "cudaSetDevice");
+        c->geom = bte::build_geometry(g);
+        c->have_geom = true;
+        c->geom_dev = false;
+        c->lambert_dev = false;
+        c->gen_key_source = -1;
+        return BTE_OK;
+    } catch (const Error& e) {
+        return fail(c, e);
+    }
+}
+
+bte_status bte_query_sizes(const bte_ctx* c, const bte_rta_params* p, int32_t* nboxes,
+                           int32_t* nbins, int64_t* nmodes) {
+    if (!c || !p) return BTE_ERR_INPUT;
+    if (nboxes) *nboxes = int32_t(c->geom.boxes.size());
+    if (nbins) *nbins = p->dt > 0 ? int32_t(std::floor(p->maxtime / p->dt + 1.0e-6)) : 0;
+    if (nmodes) *nmodes = int64_t(c->modes.n());
+    return BTE_OK;
+}
+
+bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out) {
+    if (!c || !out) return BTE_ERR_INPUT;
+    try {
+        validate(p);
+        if (!c->have_modes || !c->have_geom)
+            throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
+        ck(cudaSetDevice(c->device), "cudaSetDevice");
+        for (std::size_t b = 0; b < c->geom.boxes.size(); ++b)
+            if (!c->geom.reservoir[b] && !bte::almost_equal(c->geom.Teq[b], p->T0) &&
+                c->geom.Teq[b] != p->T0)
+                throw Error(BTE_ERR_INPUT, "Tref in xml is different from provided T0");
+        ensure_static(c);
+        if (p->specularity > 0. && !c->have_mirror)
+            throw Error(BTE_ERR_INPUT, "specular walls need an axis-aligned q grid with mirror images");
+        ensure_resample(c, p->T0);
+        ensure_generators(c, p);
+        const bte::HostModes& m = c->modes;
+        const bte::HostGeometry& g = c->geom;
+        // time grid, src/RTA_MC2D.cpp:2118-2124
+        const std::size_t ntime = std::size_t(std::floor(p->maxtime / p->dt + 1.0e-6)) + 1;
+        if (ntime < 2) throw Error(BTE_ERR_INPUT, "maxtime shorter than one time bin");
+        const double maxtime = double(ntime - 1) * p->dt;
+        c->h_time.resize(ntime);
+        const double step = (maxtime - 0.0) / double(ntime - 1);
+        for (std::size_t i = 0; i < ntime; ++i)
+            c->h_time[i] = (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
+        c->d_time.upload(c->h_time, c->stream);
+        const int nbins = int(ntime - 1);
+        const int nbx = int(g.boxes.size());
+        const std::size_t nk = std::size_t(nbx) * std::size_t(nbins);
+        const bool replay = p->mode == BTE_MODE_REPLAY;
+        const std::size_t tally_bytes = replay ? nk * 6 * sizeof(unsigned long long) : nk * 3 * sizeof(double);
+        c->d_tally.alloc(tally_bytes);
+        c->d_counters.alloc(8 * sizeof(unsigned long long));
+        c->d_err.alloc(4 * sizeof(int));
+        c->d_work.alloc(sizeof(unsigned long long));
+        ck(cudaMemsetAsync(c->d_tally.p, 0, tally_bytes, c->stream), "memset");
+        ck(cudaMemsetAsync(c->d_counters.p, 0, 8 * sizeof(unsigned long long), c->stream), "memset");
+        ck(cudaMemsetAsync(c->d_err.p, 0, 4 * sizeof(int), c->stream), "memset");
+        ck(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long), c->stream), "memset");
+
+        // Eeff (src/RTA_MC2D.cpp:2177) and the particle range
+        double Eeff;
+        long long total;
+        if (p->source == BTE_SOURCE_WALLS) {
+            Eeff = c->gens.total_energy / double(p->nparticles);
+            total = p->nparticles;
+        } else {
+            Eeff = c->gen_Eeff;
+            total = c->gens.init_first.back();
+        }
+        long long pbeg = std::max<long long>(0, p->particle_begin);
+        long long pend = p->particle_end > 0 ? std::min<long long>(p->particle_end, total) : total;
+        if (pend < pbeg) pend = pbeg;
+
+        bte::DevTables T{};
+        T.n = int(m.n());
+        T.nb = m.nb;
+        T.vxc = c->d_vxc.as<double>();
+        T.vyc = c->d_vyc.as<double>();
+        T.w = c->d_w.as<double>();
+        T.tau = c->d_tau.as<double>();
+        T.resample_cdf = c->d_rcdf.as<double>();
+        T.resample_prob = c->d_rprob.as<float>();
+        T.resample_alt = c->d_ralt.as<int>();
+        T.nboxes = nbx;
+        T.boxes = c->d_boxes.as<bte::GBox>();
+        T.hull = c->d_hull.as<bte::V2>();
+        T.borders = c->d_borders.as<bte::GBorder>();
+        T.contacts = c->d_contacts.as<bte::GContact>();
+        T.nclass = c->nclass;
+        T.row_ptr = c->d_row_ptr.as<long long>();
+        T.lcol = c->d_lcol.as<int>();
+        T.lcdf = c->d_lcdf.as<double>();
+        T.lalias = c->d_lalias.as<int4>();
+        T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
+        T.ntime = int(ntime);
+        T.timegrid = c->d_time.as<double>();
+        T.maxtime = maxtime;
+        T.inv_dt = 1.0 / step;
+        T.source = p->source;
+        T.ngen = p->source == BTE_SOURCE_WALLS ? int(c->gens.walls.size()) : int(c->gens.init_box.size());
+        T.gen_cdf = c->d_gcdf.as<double>();
+        T.gen_prob = c->d_gprob.as<float>();
+        T.gen_alt = c->d_galt.as<int>();
+        T.walls = c->d_walls.as<bte::WallGenDev>();
+        T.wall_cum = c->d_wcum.as<double>();
+        T.init_first = c->d_ifirst.as<long long>();
+        T.init_box = c->d_ibox.as<int>();
+        T.init_sign = c->d_isign.as<int>();
+        T.seed = p->seed;
+        T.ballistic = p->ballistic;
+        T.specularity = p->specularity;
+        T.pbegin = pbeg;
+        T.pend = pend;
+        T.nbins = nbins;
+
+        auto* counters = c->d_counters.as<unsigned long long>();
+        auto* err = c->d_err.as<int>();
+        ck(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
+        if (replay) {
+            bte::launch_replay(T, c->d_tally.as<unsigned long long>(), counters, err, c->nsm, c->stream);
+        } else if (g.rect_grid) {
+            bte::GridArgs A{};
+            A.G.nx = g.gnx;
+            A.G.ny = g.gny;
+            A.G.gx = c->d_gx.as<double>();
+            A.G.gy = c->d_gy.as<double>();
+            A.G.cell = c->d_gcell.as<int>();
+            A.boxcell = c->d_boxcell.as<int2>();
+            A.mv = c->d_mv.as<bte::ModeVel>();
+            const bte::V2 want[4] = {bte::v2(1, 0), bte::v2(-1, 0), bte::v2(0, 1), bte::v2(0, -1)};
+            for (int w = 0; w < 4; ++w) {
+                A.cls[w] = -1;
+                for (std::size_t k = 0; k < g.normals.size(); ++k)
+                    if (g.normals[k].x == want[w].x && g.normals[k].y == want[w].y) A.cls[w] = int(k);
+            }
+            if (!bte::launch_prod_grid(T, A, c->d_tally.as<double>(), counters, err,
+                                       c->d_work.as<unsigned long long>(), c->tune, c->nsm, c->stream))
+                throw Error(BTE_ERR_INPUT, "tuning not supported by the grid kernel");
+        } else {
+            bte::launch_prod_general(T, c->d_tally.as<double>(), counters, err, c->nsm, c->stream);
+        }
+        ck(cudaGetLastError(), "kernel launch");
+        ck(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
+        std::vector<unsigned long long> hc(8);
+        int herr[4];
+        std::vector<unsigned long long> hex;
+        std::vector<double> htal;
+        if (replay) {
+            hex.resize(nk * 6);
+            ck(cudaMemcpyAsync(hex.data(), c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
+        } else {
+            htal.resize(nk * 3);
+            ck(cudaMemcpyAsync(htal.data(), c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
+        }
+        ck(cudaMemcpyAsync(hc.data(), counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream), "d2h");
+        ck(cudaMemcpyAsync(herr, err, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream), "d2h");
+        sync(c);
+        float ms = 0;
+        ck(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "cudaEventElapsedTime");
+        out->kernel_ms = ms;
+        if (herr[0] != 0) {
+            const long long pid = (long long)herr[1] | ((long long)herr[2] << 31);
+            char msg[160];
+            std::snprintf(msg, sizeof msg, "particle %lld: %s", pid,
+                          herr[0] == BTE_ERR_VALUE ? "invalid scattering rate"
+                          : herr[0] == BTE_ERR_LIMIT ? "iteration cap reached"
+                                                      : "geometry error");
+            throw Error(bte_status(herr[0]), msg);
+        }
+        // raw tallies
+        std::vector<double> gz(nk), jx(nk), jy(nk);
+        if (replay) {
+            for (std::size_t k = 0; k < nk; ++k) {
+                double* dst[3] = {&gz[k], &jx[k], &jy[k]};
+                for (int q = 0; q < 3; ++q) {
+                    const unsigned long long hi = hex[6 * k + 2 * q], lo = hex[6 * k + 2 * q + 1];
+                    const __int128 v = (__int128)(((unsigned __int128)hi << 64) | lo);
+                    *dst[q] = double(v) / bte::FIX_SCALE;
+                }
+            }
+            if (out->exact) std::memcpy(out->exact, hex.data(), nk * 6 * sizeof(long long));
+        } else {
+            for (std::size_t k = 0; k < nk; ++k) {
+                gz[k] = htal[3 * k];
+                jx[k] = htal[3 * k + 1];
+                jy[k] = htal[3 * k + 2];
+            }
+        }
+        out->nboxes = nbx;
+        out->nbins = nbins;
+        out->Eeff = Eeff;
+        out->energy_rate = c->gens.total_energy;
+        out->events = (int64_t)hc[0];
+        out->wall_hits = (int64_t)hc[1];
+        out->crossings = (int64_t)hc[2];
+        out->absorbed = (int64_t)hc[3];
+        out->specular_hits = (int64_t)hc[4];
+        out->tally_updates = (int64_t)hc[7];
+        if (out->gz) std::copy(gz.begin(), gz.end(), out->gz);
+        if (out->gz_jx) std::copy(jx.begin(), jx.end(), out->gz_jx);
+        if (out->gz_jy) std::copy(jy.begin(), jy.end(), out->gz_jy);
+        // post-processing, src/RTA_MC2D.cpp:2336-2435
+        for (int ir = 0; ir < nbx; ++ir) {
+            const double vbox = g.boxes[std::size_t(ir)].area * g.thickness;
+            for (int i = 0; i < nbins; ++i) {
+                const std::size_t k = std::size_t(ir) * nbins + i;
+                gz[k] /= vbox;
+                jx[k] /= vbox;
+                jy[k] /= vbox;
+            }
+        }
+        for (auto& x : gz) x *= Eeff;
+        for (auto& x : jx) x *= Eeff * 1e12 * 1e9 * 1e9;
+        for (auto& x : jy) x *= Eeff * 1e12 * 1e9 * 1e9;
+        if (p->source == BTE_SOURCE_WALLS) {
+            // step response: integrate in time
+            for (int ir = 0; ir < nbx; ++ir)
+                for (int i = 1; i < nbins; ++i) {
+                    const std::size_t k = std::size_t(ir) * nbins + i;
+                    gz[k] += gz[k - 1];
+                    jx[k] += jx[k - 1];
+                    jy[k] += jy[k - 1];
+                }
+        } else {
+            // relaxation of an initial deviation: bin averages
+            for (std::size_t k = 0; k < nk; ++k) {
+                gz[k] /= step;
+                jx[k] /= step;
+                jy[k] /= step;
+            }
+        }
+        const double cv = bte::calc_cv(m, p->T0);
+        const double vcorr = g.thickness / m.c;
+        if (out->temperature)
+            for (std::size_t k = 0; k < nk; ++k) out->temperature[k] = gz[k] / (cv / vcorr) + p->T0;
+        if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
+        if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
+        return BTE_OK;
+    } catch (const Error& e) {
+        return fail(c, e);
+    } catch (const std::exception& e) {
+        c->err = e.what();
+        return BTE_ERR_CUDA;
+    }
+}
+
+// ------------------------------------------------------------------ debug
+// Host-only views of the tables for the CPU tests (no GPU needed).
+
+long long btegpu_debug_geometry(const bte_geometry* gm, double* out, long long cap) {
+    try {
+        bte::HostGeometry g = bte::build_geometry(gm);
+        long long k = 0;
+        auto put = [&](double x) {
+            if (k < cap) out[k] = x;
+            k++;
+        };
+        for (std::size_t b = 0; b < g.boxes.size(); ++b) {
+            const bte::GBox& B = g.boxes[b];
+            put(double(B.nborders));
+            for (int i = 0; i < B.nborders; ++i) {
+                const bte::GBorder& br = g.borders[std::size_t(B.border_off + i)];
+                put(br.p1.x); put(br.p1.y); put(br.p2.x); put(br.p2.y);
+                put(br.np.x); put(br.np.y);
+            }
+            put(double(B.ncontacts));
+            for (int i = 0; i < B.ncontacts; ++i) {
+                const bte::GContact& ct = g.contacts[std::size_t(B.contact_off + i)];
+                put(double(ct.id)); put(ct.np.x); put(ct.np.y);
+            }
+            put(B.center.x); put(B.center.y); put(B.area);
+        }
+        return k;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+int btegpu_debug_grid(const bte_geometry* gm, int* nx, int* ny) {
+    try {
+        bte::HostGeometry g = bte::build_geometry(gm);
+        *nx = g.gnx;
+        *ny = g.gny;
+        return g.rect_grid ? 1 : 0;
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+long long btegpu_debug_lambert(const bte_mode_table* mt, const bte_geometry* gm, long long* nnz_per_class,
+                               int maxclass) {
+    try {
+        bte::HostModes m = bte::build_modes(mt);
+        bte::HostGeometry g = bte::build_geometry(gm);
+        bte::LambertTable L = bte::build_lambert(m, g, hw_threads());
+        const std::size_t n = m.n();
+        for (int c = 0; c < L.nclass && c < maxclass; ++c)
+            nnz_per_class[c] = L.row_ptr[std::size_t(c) * (n + 1) + n] - L.row_ptr[std::size_t(c) * (n + 1)];
+        return (long long)L.col.size();
+    } catch (const std::exception&) {
+        return -1;
+    }
+}
+
+int btegpu_debug_log(const double* x, double* y, long long n) {
+    for (long long i = 0; i < n; ++i) y[i] = bte::bte_log(x[i]);
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,338 @@
+// cli_rtamc2d.cpp - rtamc2d_gpu, the drop-in for the RTAMC2D executable.
+//
+//   rtamc2d_gpu <inputfile.xml> nthreads [nruns]        (src/RTA_MC2D.cpp:2085-2101)
+//
+// Reads the <RTA_MC2d> XML (src/RTA_MC2D.cpp:1806-2055) and the geometry XML
+// (src/geometry_2d.cpp:408-522), runs the particle loop on the GPU through
+// the C ABI and writes temperature_/jx_/jy_{T0}K_run_{i}.csv with rows
+// [t_mid, box0, box1, ...] (src/RTA_MC2D.cpp:2437-2471).  `nthreads` is
+// accepted and ignored.  The material database is the engine's binary mode
+// table (magic BTEMODE1); almaBTE HDF5 files need libhdf5, which this build
+// does not link.  Extensions live in an <engine .../> element:
+//   mode="replay|production" seed="N" specularity="p" source="walls|initial"
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/btegpu.h"
+
+namespace {
+
+struct Node {
+    std::string name, text;
+    std::map<std::string, std::string> attr;
+    std::vector<std::unique_ptr<Node>> kids;
+    const Node* child(const std::string& n) const {
+        for (auto& k : kids)
+            if (k->name == n) return k.get();
+        return nullptr;
+    }
+    std::string get(const std::string& a) const {
+        auto it = attr.find(a);
+        if (it == attr.end()) throw std::runtime_error("missing attribute " + a + " in <" + name + ">");
+        return it->second;
+    }
+    bool has(const std::string& a) const { return attr.count(a) != 0; }
+};
+
+// Minimal XML reader: elements, attributes, text; skips <? ?>, <!-- -->.
+struct XmlReader {
+    std::string s;
+    std::size_t i = 0;
+    void ws() {
+        while (i < s.size() && std::isspace((unsigned char)s[i])) ++i;
+    }
+    void skip_misc() {
+        for (;;) {
+            ws();
+            if (s.compare(i, 4, "<!--") == 0) {
+                std::size_t e = s.find("-->", i);
+                if (e == std::string::npos) throw std::runtime_error("unterminated comment");
+                i = e + 3;
+            } else if (s.compare(i, 2, "<?") == 0) {
+                std::size_t e = s.find("?>", i);
+                if (e == std::string::npos) throw std::runtime_error("unterminated declaration");
+                i = e + 2;
+            } else {
+                return;
+            }
+        }
+    }
+    std::string name() {
+        std::size_t b = i;
+        while (i < s.size() && (std::isalnum((unsigned char)s[i]) || s[i] == '_' || s[i] == '-' || s[i] == ':' || s[i] == '.')) ++i;
+        if (b == i) throw std::runtime_error("bad XML name");
+        return s.substr(b, i - b);
+    }
+    std::unique_ptr<Node> element() {
+        skip_misc();
+        if (i >= s.size() || s[i] != '<') throw std::runtime_error("expected an element");
+        ++i;
+        auto n = std::make_unique<Node>();
+        n->name = name();
+        for (;;) {
+            ws();
+            if (s.compare(i, 2, "/>") == 0) {
+                i += 2;
+                return n;
+            }
+            if (s[i] == '>') {
+                ++i;
+                break;
+            }
+            std::string a = name();
+            ws();
+            if (s[i] != '=') throw std::runtime_error("expected = in attribute");
+            ++i;
+            ws();
+            char q = s[i++];
+            std::size_t e = s.find(q, i);
+            if (e == std::string::npos) throw std::runtime_error("unterminated attribute");
+            n->attr[a] = s.substr(i, e - i);
+            i = e + 1;
+        }
+        for (;;) {
+            std::size_t b = i;
+            while (i < s.size() && s[i] != '<') ++i;
+            n->text += s.substr(b, i - b);
+            if (i >= s.size()) throw std::runtime_error("unterminated element " + n->name);
+            if (s.compare(i, 4, "<!--") == 0) {
+                skip_misc();
+                continue;
+            }
+            if (s.compare(i, 2, "</") == 0) {
+                i += 2;
+                std::string e = name();
+                if (e != n->name) throw std::runtime_error("mismatched </" + e + ">");
+                ws();
+                ++i;  // '>'
+                return n;
+            }
+            n->kids.push_back(element());
+        }
+    }
+};
+
+std::unique_ptr<Node> read_xml(const std::string& path) {
+    std::ifstream f(path);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    XmlReader r;
+    r.s = ss.str();
+    return r.element();
+}
+
+std::string dir_of(const std::string& p) {
+    std::size_t k = p.find_last_of('/');
+    return k == std::string::npos ? std::string() : p.substr(0, k + 1);
+}
+
+std::string resolve(const std::string& base, const std::string& f) {
+    if (!f.empty() && f[0] == '/') return f;
+    std::ifstream t(f);
+    if (t) return f;
+    return base + f;
+}
+
+struct ModesFile {
+    int32_t head[5];
+    double V, c, dq[9];
+    std::vector<double> omega, vg, w;
+};
+
+ModesFile read_modes(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open database " + path);
+    char magic[8];
+    f.read(magic, 8);
+    if (std::string(magic, 8) != "BTEMODE1")
+        throw std::runtime_error(path + " is not a BTEMODE1 mode table (HDF5 databases need libhdf5)");
+    ModesFile m;
+    f.read(reinterpret_cast<char*>(m.head), sizeof m.head);
+    f.read(reinterpret_cast<char*>(&m.V), 8);
+    f.read(reinterpret_cast<char*>(&m.c), 8);
+    f.read(reinterpret_cast<char*>(m.dq), sizeof m.dq);
+    const std::size_t n = std::size_t(m.head[0]) * std::size_t(m.head[1]);
+    m.omega.resize(n);
+    m.vg.resize(3 * n);
+    m.w.resize(n);
+    f.read(reinterpret_cast<char*>(m.omega.data()), std::streamsize(n * 8));
+    f.read(reinterpret_cast<char*>(m.vg.data()), std::streamsize(3 * n * 8));
+    f.read(reinterpret_cast<char*>(m.w.data()), std::streamsize(n * 8));
+    if (!f) throw std::runtime_error("truncated mode table " + path);
+    return m;
+}
+
+std::string fmt_g(double x) {
+    char b[64];
+    std::snprintf(b, sizeof b, "%g", x);
+    return b;
+}
+
+void write_csv(const std::string& fn, const std::vector<double>& data, int nboxes, int nbins, double dt) {
+    std::ofstream o(fn);
+    if (!o) throw std::runtime_error("cannot write " + fn);
+    for (int i = 0; i < nbins; ++i) {
+        o << (i + 0.5) * dt;
+        for (int b = 0; b < nboxes; ++b) o << ',' << data[std::size_t(b) * nbins + i];
+        o << '\n';
+    }
+}
+
+void check(bte_ctx* ctx, bte_status s, const char* what) {
+    if (s != BTE_OK) {
+        char buf[512];
+        bte_last_error(ctx, buf, sizeof buf);
+        throw std::runtime_error(std::string(what) + ": " + buf);
+    }
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    auto tA = std::chrono::high_resolution_clock::now();
+    std::cout << "********************************************\n"
+              << "This is rtamc2d_gpu (GB300 engine, C ABI v" << bte_version() << ")\n"
+              << "********************************************" << std::endl;
+    if (argc != 3 && argc != 4) {
+        std::cerr << "Usage: " << argv[0] << " <inputfile.xml> nthreads nruns" << std::endl;
+        return 1;
+    }
+    const long nruns = argc == 4 ? std::atol(argv[3]) : 1;
+    try {
+        const std::string input = argv[1];
+        auto root = read_xml(input);
+        if (root->name != "RTA_MC2d") throw std::runtime_error("root element must be <RTA_MC2d>");
+        const std::string base = dir_of(input);
+        std::string gfile, dbfile;
+        double dt = 0, maxtime = 0, thickness = 0, T0 = -1, p = 0;
+        long long N = 0;
+        unsigned long long seed = 20261203ULL;
+        int mode = BTE_MODE_PRODUCTION, source = BTE_SOURCE_WALLS, ballistic = 0;
+        for (auto& k : root->kids) {
+            if (k->name == "geometry") gfile = k->get("file");
+            if (k->name == "time") {
+                dt = std::stod(k->get("dt"));
+                maxtime = std::stod(k->get("maxtime"));
+            }
+            if (k->name == "material") {
+                dbfile = k->get("database");
+                thickness = std::stod(k->get("thickness"));
+                T0 = std::stod(k->get("T0"));
+            }
+            if (k->name == "particles") N = std::stoll(k->get("N"));
+            if (k->name == "ballistic") ballistic = 1;
+            if (k->name == "gradient") throw std::runtime_error("<gradient> (periodic steady state) is not supported yet");
+            if (k->name == "layer" || k->name == "layers_connection")
+                throw std::runtime_error("multi-material layers are not supported");
+            if (k->name == "engine") {
+                if (k->has("mode")) mode = k->get("mode") == "replay" ? BTE_MODE_REPLAY : BTE_MODE_PRODUCTION;
+                if (k->has("seed")) seed = std::stoull(k->get("seed"));
+                if (k->has("specularity")) p = std::stod(k->get("specularity"));
+                if (k->has("source")) source = k->get("source") == "initial" ? BTE_SOURCE_INITIAL : BTE_SOURCE_WALLS;
+            }
+        }
+        // geometry
+        auto groot = read_xml(resolve(base, gfile));
+        std::vector<int32_t> npts, res;
+        std::vector<double> verts, teq, tinit;
+        for (auto& b : groot->kids) {
+            if (b->name != "Box") continue;
+            const Node* v = b->child("Vertices");
+            if (!v) throw std::runtime_error("<Box> without <Vertices>");
+            const int rows = std::stoi(v->get("dim")), cols = std::stoi(v->get("npoints"));
+            if (rows != 2) throw std::runtime_error("Error in provided vertices, bad dimension");
+            std::stringstream ds(v->text);
+            for (int i = 0; i < rows * cols; ++i) {
+                double x;
+                ds >> x;
+                verts.push_back(x);
+            }
+            npts.push_back(cols);
+            const Node* ic = b->child("initCnd");
+            double te = ic ? std::stod(ic->get("Teq")) : -1.;
+            teq.push_back(te);
+            tinit.push_back(ic && ic->has("Tinit") ? std::stod(ic->get("Tinit")) : te);
+            res.push_back(b->child("Reservoir") ? 1 : 0);
+            if (b->child("Translate_to")) throw std::runtime_error("periodic boxes are not supported yet");
+        }
+        ModesFile mf = read_modes(resolve(base, dbfile));
+        bte_ctx* ctx = nullptr;
+        bte_device_opts opts{0, 1};
+        if (bte_create(&ctx, &opts) != BTE_OK) {
+            char buf[256];
+            bte_last_error(nullptr, buf, sizeof buf);
+            throw std::runtime_error(std::string("bte_create: ") + buf);
+        }
+        std::unique_ptr<bte_ctx, bte_status (*)(bte_ctx*)> guard(ctx, bte_destroy);
+        bte_mode_table mt{};
+        mt.nq = mf.head[0];
+        mt.nb = mf.head[1];
+        for (int i = 0; i < 3; ++i) mt.grid[i] = mf.head[2 + i];
+        mt.omega = mf.omega.data();
+        mt.vg = mf.vg.data();
+        mt.w = mf.w.data();
+        mt.dq = mf.dq;
+        mt.V = mf.V;
+        mt.c_lat = mf.c;
+        check(ctx, bte_load_modes(ctx, &mt), "load modes");
+        bte_geometry gm{};
+        gm.nboxes = int32_t(npts.size());
+        gm.npoints = npts.data();
+        gm.vertices = verts.data();
+        gm.Teq = teq.data();
+        gm.Tinit = tinit.data();
+        gm.reservoir = res.data();
+        gm.thickness = thickness;
+        check(ctx, bte_load_geometry(ctx, &gm), "load geometry");
+        auto tB = std::chrono::high_resolution_clock::now();
+        std::cout << "#Init variables -> Done (" << std::chrono::duration<double>(tB - tA).count() << " s )\n";
+        for (long irun = 0; irun < nruns; ++irun) {
+            bte_rta_params rp{};
+            rp.T0 = T0;
+            rp.dt = dt;
+            rp.maxtime = maxtime;
+            rp.nparticles = N;
+            rp.seed = seed + (unsigned long long)irun;
+            rp.mode = mode;
+            rp.source = source;
+            rp.ballistic = ballistic;
+            rp.specularity = p;
+            int32_t nbx = 0, nbn = 0;
+            int64_t nm = 0;
+            bte_query_sizes(ctx, &rp, &nbx, &nbn, &nm);
+            std::vector<double> T(std::size_t(nbx) * nbn), jx(T.size()), jy(T.size());
+            bte_rta_result out{};
+            out.temperature = T.data();
+            out.jx = jx.data();
+            out.jy = jy.data();
+            std::cout << "#Run: " << irun << std::endl;
+            auto t0 = std::chrono::high_resolution_clock::now();
+            check(ctx, bte_rta_run(ctx, &rp, &out), "run");
+            auto t1 = std::chrono::high_resolution_clock::now();
+            std::cout << "#|E| =" << out.energy_rate << " J/ps\n#Eeff = " << out.Eeff << "\n"
+                      << "#MC loop -> Done ( " << std::chrono::duration<double>(t1 - t0).count()
+                      << " s ), kernel " << out.kernel_ms << " ms, " << out.events << " flight events ("
+                      << double(out.events) / (out.kernel_ms * 1e-3) << " /s)" << std::endl;
+            const std::string tag = fmt_g(T0) + "K_run_" + std::to_string(irun) + ".csv";
+            write_csv("temperature_" + tag, T, nbx, nbn, dt);
+            write_csv("jx_" + tag, jx, nbx, nbn, dt);
+            write_csv("jy_" + tag, jy, nbx, nbn, dt);
+        }
+    } catch (const std::exception& e) {
+        std::cerr << "error: " << e.what() << std::endl;
+        return 2;
+    }
+    return 0;
+}

@@ -1,0 +1,52 @@
+// kernels.h - launch wrappers of the particle-loop kernels (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "rta_flight.cuh"
+
+namespace bte {
+
+// Grid description of the axis-aligned fast path (production mode).
+struct DevGrid {
+    int nx, ny;
+    const double* gx;   // nx + 1 grid lines
+    const double* gy;   // ny + 1 grid lines
+    const int* cell;    // [nx*ny] box id, -1 void, -2 - b reservoir box b
+};
+
+struct ProdTuning {
+    int block_threads;
+    int blocks_per_sm;
+    int smem_tally;
+    int smem_alias;
+};
+
+void launch_replay(const DevTables& T, unsigned long long* ex, unsigned long long* counters,
+                   int* err, int nsm, cudaStream_t s);
+
+// General convex-box production kernel (any geometry).
+void launch_prod_general(const DevTables& T, double* tally, unsigned long long* counters,
+                         int* err, int nsm, cudaStream_t s);
+
+// Per-mode velocity record of the grid path.
+struct __align__(32) ModeVel {
+    double vx, vy;    // get_v velocities, nm/ps
+    double ivx, ivy;  // their inverses (0 where the component is 0)
+};
+
+// Grid-path kernel parameters beyond the tables.
+struct GridArgs {
+    DevGrid G;
+    const int2* boxcell;     // box -> (i, j)
+    const ModeVel* mv;       // per mode velocities and inverses
+    int cls[4];              // normal classes of the +x, -x, +y, -y walls (-1: none)
+};
+
+// Axis-aligned grid production kernel (persistent, warp-refilled work).
+// Returns false when the tuning cannot be honoured (e.g. smem too small).
+bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
+                      unsigned long long* counters, int* err, unsigned long long* work,
+                      const ProdTuning& tune, int nsm, cudaStream_t s);
+
+}  // namespace bte

@@ -1,0 +1,457 @@
+// rta_flight.cuh - the RTA particle life on the device, for general convex
+// boxes.  One thread carries one particle from its generation to absorption
+// or maxtime.  The logic follows, step for step:
+//   per-particle loop     src/RTA_MC2D.cpp:2262-2316
+//   evolparticle          src/RTA_MC2D.cpp:990-1386 (transient, one material)
+//   get_inter_side        src/geometry_2d.cpp:160-293
+//   in_corner3            src/geometry_2d.cpp:388-406
+//   correct_corner_problem include/geometry_2d.hpp:524-561
+//   Init_generator        src/RTA_MC2D.cpp:421-511 (walls)
+//   init_particles        src/beyondRTA_MC2d.cpp:211-269 (initial deviation)
+// The policy P supplies the random draws, the samplers and the tally, so the
+// same code serves the bit-exact replay mode and the production mode.
+#pragma once
+
+#include "bte_device.cuh"
+
+namespace bte {
+
+constexpr int MAXB = 16;        // borders per box
+constexpr int MAXC = 32;        // candidate boxes at one crossing
+constexpr int FLIGHT_CAP = 1 << 20;  // evolparticle calls per free flight
+constexpr int NUDGE_CAP = 64;   // consecutive geometry nudges
+
+// Error codes written to the device error word (bte_status values).
+constexpr int E_VALUE = 2, E_GEOM = 3, E_LIMIT = 4;
+
+struct WallGenDev {
+    V2 p1, nd, sa, sb;
+    int box, sign;
+};
+
+struct DevTables {
+    // modes
+    int n, nb;
+    const double* vxc;
+    const double* vyc;
+    const double* w;
+    const double* tau;
+    const double* resample_cdf;
+    const float* resample_prob;
+    const int* resample_alt;
+    // geometry
+    int nboxes;
+    const GBox* boxes;
+    const V2* hull;
+    const GBorder* borders;
+    const GContact* contacts;
+    int nclass;
+    // Lambert rows
+    const long long* row_ptr;
+    const int* lcol;
+    const double* lcdf;
+    const int4* lalias;   // {prob bits, keep, alt, pad}
+    const int* mirror;    // [nclass][n] or null
+    // time grid
+    int ntime;
+    const double* timegrid;
+    double maxtime;
+    double inv_dt;        // 1 / bin width (production)
+    // generators
+    int source, ngen;
+    const double* gen_cdf;
+    const float* gen_prob;
+    const int* gen_alt;
+    const WallGenDev* walls;
+    const double* wall_cum;
+    const long long* init_first;
+    const int* init_box;
+    const int* init_sign;
+    // run
+    unsigned long long seed;
+    int ballistic;
+    double specularity;
+    long long pbegin, pend;
+    int nbins;
+};
+
+struct Counters {
+    unsigned long long events, wall_hits, crossings, absorbed, specular, nudges, quirks, tallies;
+};
+
+struct Particle {
+    V2 pos;
+    int mode;
+    int sign;
+    double t;
+    int box;
+};
+
+// std::lower_bound over a sorted double array: first index with a[i] >= u.
+__device__ __forceinline__ int lower_bound_d(const double* a, int n, double u) {
+    int lo = 0, cnt = n;
+    while (cnt > 0) {
+        const int step = cnt >> 1;
+        const int it = lo + step;
+        if (a[it] < u) {
+            lo = it + 1;
+            cnt -= step + 1;
+        } else {
+            cnt = step;
+        }
+    }
+    return lo;
+}
+
+__device__ __forceinline__ bool box_inside(const DevTables& T, int b, V2 p) {
+    const GBox& B = T.boxes[b];
+    return inside_hull(T.hull + B.hull_off, B.nhull, p);
+}
+
+struct HitD {
+    double time;
+    V2 rf;
+    int nb;
+    int bids[MAXB];
+};
+
+// get_inter_side: returns false on the reference's geometry_error.
+static __device__ __noinline__ bool get_inter_side(const DevTables& T, int box, V2 r0, V2 v, double dt, HitD& h) {
+    const GBox& B = T.boxes[box];
+    const V2 pf = v2(r0.x + dt * v.x, r0.y + dt * v.y);
+    double time = 1.0e+7;
+    V2 rf = v2(0., 0.);
+    h.nb = 0;
+    bool already_there = true;
+    for (int id = 0; id < B.nborders; ++id) {
+        const GBorder& b = T.borders[B.border_off + id];
+        V2 rin;
+        if (seg_intersect(r0, pf, b.la, b.lb, rin) && !on_segment(r0, b.la, b.lb)) {
+            if (dot(b.np, v) > 0.) {
+                const double tx = (__builtin_fabs(v.x) < 1.0e-6) ? -1 : (rin.x - r0.x) / v.x;
+                const double ty = (__builtin_fabs(v.y) < 1.0e-6) ? -1 : (rin.y - r0.y) / v.y;
+                const double newtime = tx > ty ? tx : ty;
+                if (newtime == time && h.nb < MAXB) h.bids[h.nb++] = id;
+                if (newtime < time) {
+                    h.nb = 0;
+                    rf = rin;
+                    time = newtime;
+                    already_there = false;
+                    h.bids[h.nb++] = id;
+                }
+            }
+        }
+    }
+    if (already_there) {
+        const V2 p0p = v2(r0.x - 1.0e-6 * v.x, r0.y - 1.0e-6 * v.y);
+        for (int id = 0; id < B.nborders; ++id) {
+            const GBorder& b = T.borders[B.border_off + id];
+            V2 rin;
+            if (seg_intersect(p0p, pf, b.la, b.lb, rin)) {
+                if (dot(b.np, v) > 0.) {
+                    const double tx = (__builtin_fabs(v.x) < 1.0e-6) ? -1.0e+8 : (rin.x - r0.x) / v.x;
+                    const double ty = (__builtin_fabs(v.y) < 1.0e-6) ? -1.0e+8 : (rin.y - r0.y) / v.y;
+                    const double newtime = tx > ty ? tx : ty;
+                    if (newtime == time && h.nb < MAXB) h.bids[h.nb++] = id;
+                    if (__builtin_fabs(newtime) < time) {
+                        h.nb = 0;
+                        rf = rin;
+                        time = newtime;
+                        h.bids[h.nb++] = id;
+                    }
+                }
+            }
+        }
+        if (time > 1.0e+6) return false;
+    }
+    if (almost_equal(time, 0.)) time = 0.;
+    if (time < 0.) return false;
+    h.time = time;
+    h.rf = rf;
+    return true;
+}
+
+// Contact normal of `box` towards neighbour `test` (contacts sorted by id).
+__device__ __forceinline__ int contact_index(const DevTables& T, int box, int test) {
+    const GBox& B = T.boxes[box];
+    for (int i = 0; i < B.ncontacts; ++i)
+        if (T.contacts[B.contact_off + i].id == test) return B.contact_off + i;
+    return -1;
+}
+
+template <class P>
+__device__ int correct_corner_problem(const DevTables& T, P& pol, V2 rf, V2 v, const int* cand,
+                                      int ncand, int& winner) {
+    int fin[MAXC];
+    int nf = 0;
+    for (int i = 0; i < ncand; ++i) {
+        const GBox& B = T.boxes[cand[i]];
+        int nbrd = 0;
+        for (int k = 0; k < B.nborders; ++k) {
+            const GBorder& b = T.borders[B.border_off + k];
+            if (on_segment(rf, b.la, b.lb) && dot(b.np, v) > 0.) nbrd++;
+        }
+        if (nbrd <= 1) fin[nf++] = cand[i];
+    }
+    if (nf == 0) return E_GEOM;
+    winner = fin[pol.choose(nf)];
+    return 0;
+}
+
+// evolparticle (transient).  Returns 0 or an error code.
+template <class P>
+__device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, double& dt,
+                            Counters& c, int& nudges) {
+    const V2 opos = p.pos;
+    const GBox& box = T.boxes[p.box];
+    if (box.reservoir) {
+        p.mode = 0;
+        dt = 0.;
+        c.absorbed++;
+        return 0;
+    }
+    V2 rnew = v2(p.pos.x + dt * v.x, p.pos.y + dt * v.y);
+    if (inside_hull(T.hull + box.hull_off, box.nhull, rnew)) {
+        p.pos = rnew;
+        int e = pol.tally(T, p.box, p.t, p.t + dt, p.sign, v);
+        if (e) return e;
+        p.t += dt;
+        if (!T.ballistic) p.mode = pol.resample(T);
+        dt = 0.;
+        nudges = 0;
+        return 0;
+    }
+    HitD mru;
+    if (!get_inter_side(T, p.box, p.pos, v, dt, mru)) {
+        const V2 d = sub(box.center, opos);
+        p.pos = add(p.pos, divs(scal(1.0e-6, d), norm(d)));
+        c.nudges++;
+        if (++nudges > NUDGE_CAP) return E_LIMIT;
+        return 0;
+    }
+    nudges = 0;
+    double left_time = dt - mru.time;
+    const double tf = mru.time;
+    if (almost_equal(left_time, 0.)) left_time = 0.;
+    dt = left_time;
+    rnew = mru.rf;
+    const V2 reps = add(rnew, divs(scal(1.0e-6, v), norm(v)));
+    // candidate boxes among the contacts (ascending id)
+    int pboxes[MAXC];
+    int np = 0;
+    for (int i = 0; i < box.ncontacts; ++i) {
+        const GContact& gc = T.contacts[box.contact_off + i];
+        const int test = gc.id;
+        if (test == p.box) continue;
+        const double npv = dot(gc.np, v);
+        const bool parallel = almost_equal(npv, 0.);
+        const bool oriented = npv > 0.;
+        if ((box_inside(T, test, rnew) || box_inside(T, test, reps)) && !parallel && oriented) {
+            if (np == MAXC) return E_LIMIT;
+            pboxes[np++] = test;
+        }
+    }
+    if (np == 0) {
+        int e = pol.tally(T, p.box, p.t, p.t + tf, p.sign, v);
+        if (e) return e;
+        p.t += tf;
+        // in_corner3 over the boxes that can cover a border point: this box
+        // and its contacts, in ascending id order
+        int ids[MAXC + 1];
+        int ni = 0;
+        {
+            const int self = p.box;
+            bool self_added = false;
+            for (int i = 0; i < box.ncontacts; ++i) {
+                const int cand = T.contacts[box.contact_off + i].id;
+                if (!self_added && self < cand) {
+                    if (box_inside(T, self, rnew)) ids[ni++] = self;
+                    self_added = true;
+                }
+                if (ni >= MAXC) return E_LIMIT;
+                if (box_inside(T, cand, rnew)) ids[ni++] = cand;
+            }
+            if (!self_added && box_inside(T, self, rnew)) ids[ni++] = self;
+        }
+        if (ni > 2) {
+            int winner;
+            int e2 = correct_corner_problem(T, pol, rnew, v, ids, ni, winner);
+            if (e2) return e2;
+            p.box = winner;
+            const V2 corr = sub(T.boxes[winner].center, rnew);
+            const V2 cpos = add(rnew, divs(scal(1.0e-6, corr), norm(corr)));
+            if (!get_inter_side(T, winner, cpos, v, 1.0e+18, mru)) return E_GEOM;
+            rnew = mru.rf;
+        }
+        const GBox& cur = T.boxes[p.box];
+        int iborder;
+        if (mru.nb > 1) {
+            int vb[MAXB];
+            int nv = 0;
+            for (int i = 0; i < mru.nb; ++i) {
+                const GBorder& mb = T.borders[cur.border_off + mru.bids[i]];
+                const V2 rc = add(rnew, scal(1.0e-4, mb.np));
+                bool isvoid = true;
+                for (int j = 0; j < box.ncontacts; ++j)
+                    if (box_inside(T, T.contacts[box.contact_off + j].id, rc)) {
+                        isvoid = false;
+                        break;
+                    }
+                if (isvoid) vb[nv++] = mru.bids[i];
+            }
+            if (nv == 0) return E_GEOM;
+            // uniform_int_distribution(0, size): inclusive bound of the
+            // reference; the out-of-range draw is counted and clamped
+            int idx = pol.choose(nv + 1);
+            if (idx == nv) {
+                c.quirks++;
+                idx--;
+            }
+            iborder = vb[idx];
+        } else {
+            iborder = mru.bids[0];
+        }
+        const GBorder& wb = T.borders[cur.border_off + iborder];
+        int nm = -1;
+        if (T.specularity > 0.) {
+            if (pol.u() < T.specularity) {
+                const int mm = T.mirror ? T.mirror[wb.ncls * T.n + p.mode] : -1;
+                if (mm >= 0) {
+                    nm = mm;
+                    c.specular++;
+                }
+            }
+        }
+        if (nm < 0) {
+            nm = pol.bounce(T, wb.ncls, p.mode);
+            if (nm < 0) return E_GEOM;
+        }
+        p.pos = rnew;
+        p.mode = nm;
+        dt = 0.;
+        c.wall_hits++;
+        return 0;
+    } else if (np == 1) {
+        p.pos = rnew;
+        int e = pol.tally(T, p.box, p.t, p.t + tf, p.sign, v);
+        if (e) return e;
+        p.t += tf;
+        p.box = pboxes[0];
+        c.crossings++;
+        return 0;
+    } else {
+        int e = pol.tally(T, p.box, p.t, p.t + tf, p.sign, v);
+        if (e) return e;
+        p.t += tf;
+        p.pos = rnew;
+        int pbox2[MAXC];
+        int n2 = 0;
+        const V2 rcheck = add(rnew, scal(1.0e-6, v));
+        for (int i = 0; i < np; ++i)
+            if (box_inside(T, pboxes[i], rcheck)) pbox2[n2++] = pboxes[i];
+        int newid;
+        if (n2 == 0) {
+            newid = pboxes[pol.choose(np)];
+            const V2 d = sub(T.boxes[newid].center, rnew);
+            p.pos = add(p.pos, divs(scal(1.0e-6, d), norm(d)));
+        } else {
+            newid = pbox2[pol.choose(n2)];
+        }
+        p.box = newid;
+        c.crossings++;
+        return 0;
+    }
+}
+
+// Particle generation.  Returns 0 or an error code; `skip` is set when the
+// particle index has no particle (initial source beyond the generated count).
+template <class P>
+__device__ int generate(const DevTables& T, P& pol, long long pid, Particle& p) {
+    if (T.source == 0) {
+        const double selectGenR = pol.u();
+        (void)selectGenR;  // without a gradient source every particle comes from a wall
+        const double whereGenR = pol.u();
+        int g = lower_bound_d(T.wall_cum, T.ngen, whereGenR);
+        if (g >= T.ngen) g = T.ngen - 1;
+        const WallGenDev W = T.walls[g];
+        V2 ppos;
+        int tries = 0;
+        for (;;) {
+            if (++tries > 1000) return E_LIMIT;
+            ppos = add(W.p1, scal(pol.u(), W.nd));
+            if (on_segment(ppos, W.sa, W.sb)) break;
+        }
+        if (!box_inside(T, W.box, ppos)) {
+            const V2 d = sub(T.boxes[W.box].center, ppos);
+            ppos = add(ppos, divs(scal(1.0e-6, d), norm(d)));
+            if (!box_inside(T, W.box, ppos)) return E_GEOM;
+        }
+        p.mode = pol.gen_mode(T, g);
+        p.pos = ppos;
+        p.sign = W.sign;
+        p.t = 0.;
+        p.box = W.box;
+        return 0;
+    }
+    // initial deviation: particle -> box by the prefix of generated counts
+    int lo = 0, hi = T.ngen;  // find g with init_first[g] <= pid < init_first[g+1]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (T.init_first[mid] <= pid) lo = mid; else hi = mid;
+    }
+    const int g = lo;
+    const int b = T.init_box[g];
+    const GBox& B = T.boxes[b];
+    const V2* h = T.hull + B.hull_off;
+    double x0 = h[0].x, x1 = h[0].x, y0 = h[0].y, y1 = h[0].y;
+    for (int i = 1; i < B.nhull; ++i) {
+        x0 = fmin(x0, h[i].x);
+        x1 = fmax(x1, h[i].x);
+        y0 = fmin(y0, h[i].y);
+        y1 = fmax(y1, h[i].y);
+    }
+    V2 r;
+    int tries = 0;
+    for (;;) {
+        if (++tries > 100000) return E_LIMIT;
+        r.x = x0 + pol.u() * (x1 - x0);
+        r.y = y0 + pol.u() * (y1 - y0);
+        if (inside_hull(h, B.nhull, r)) break;
+    }
+    p.mode = pol.gen_mode(T, g);
+    p.pos = r;
+    p.sign = T.init_sign[g];
+    p.t = 0.;
+    p.box = b;
+    return 0;
+}
+
+// A whole particle life.  Returns 0 or an error code.
+template <class P>
+__device__ int run_particle(const DevTables& T, P& pol, long long pid, Counters& c) {
+    Particle p;
+    int e = generate(T, pol, pid, p);
+    if (e) return e;
+    double time = 0.;
+    int nudges = 0;
+    while (time < T.maxtime) {
+        const int k = p.mode;
+        const V2 v = v2(T.vxc[k], T.vyc[k]);
+        const double w = T.w[k];
+        if (w == 0.) return E_VALUE;
+        double dt = pol.flight(T, k);
+        c.events++;
+        if (time + dt > T.maxtime) dt = T.maxtime - time + 1.0e-8;
+        int guard = 0;
+        while (!almost_equal(dt, 0.)) {
+            if (++guard > FLIGHT_CAP) return E_LIMIT;
+            e = evolparticle(T, pol, p, v, dt, c, nudges);
+            if (e) return e;
+        }
+        if (p.mode == 0) break;
+        time = p.t;
+    }
+    return 0;
+}
+
+}  // namespace bte

@@ -1,0 +1,703 @@
+// tables.cpp - host construction of the device tables (see tables.hpp).
+//
+// The formulas and their operation order follow the reference so that the
+// replay mode reproduces the CPU restatement bit for bit:
+//   geometry_2d ctor / get_sides      src/geometry_2d.cpp:51-153
+//   calculate_contacts                src/geometry_2d.cpp:295-381
+//   BE_derivative_distribution        src/sampling.cpp:47-68
+//   Isothermal_wall_distribution      src/sampling.cpp:189-269
+//   outTref_distribution              src/sampling.cpp:271-330
+//   fill_cumulative                   src/sampling.cpp:26-44
+//   diffusive_bouncing table + bounce src/RTA_MC2D.cpp:556-678
+//   Init_generator weights            src/RTA_MC2D.cpp:289-418
+//   calc_cv                           include/bulk_properties.hpp:32-47
+#include "tables.hpp"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <numeric>
+#include <thread>
+
+namespace bte {
+
+namespace {
+constexpr double kB = 1.3806488e-23;
+constexpr double hbar = 1.054571726e-34;
+constexpr double nsigma = 2.828427124746190097603377448419396157138;
+constexpr double PI = 3.1415926535897932384626433832795028841953;
+
+V2 vneg(V2 a) { return v2(-1. * a.x, -1. * a.y); }
+
+std::vector<V2> convex_hull(std::vector<V2> pts) {
+    std::sort(pts.begin(), pts.end(),
+              [](V2 a, V2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
+    pts.erase(std::unique(pts.begin(), pts.end(),
+                          [](V2 a, V2 b) { return a.x == b.x && a.y == b.y; }),
+              pts.end());
+    if (pts.size() < 3) throw Error(BTE_ERR_INPUT, "a box needs three distinct vertices");
+    std::vector<V2> h(2 * pts.size());
+    std::size_t k = 0;
+    for (std::size_t i = 0; i < pts.size(); ++i) {
+        while (k >= 2 && cross(sub(h[k - 1], h[k - 2]), sub(pts[i], h[k - 2])) <= 0.) --k;
+        h[k++] = pts[i];
+    }
+    for (std::size_t i = pts.size() - 1, t = k + 1; i > 0; --i) {
+        while (k >= t && cross(sub(h[k - 1], h[k - 2]), sub(pts[i - 1], h[k - 2])) <= 0.) --k;
+        h[k++] = pts[i - 1];
+    }
+    h.resize(k - 1);
+    return h;
+}
+
+struct BoxBuild {
+    std::vector<V2> hull;
+    V2 center;
+    double area;
+    std::vector<GBorder> borders;
+    std::map<int, GBorder> contacts;  // neighbour -> contact border (seen from here)
+};
+
+BoxBuild make_box(const std::vector<V2>& verts) {
+    BoxBuild b;
+    b.hull = convex_hull(verts);
+    const std::size_t n = b.hull.size();
+    double a2 = 0, cx = 0, cy = 0;
+    const V2 o = b.hull[0];
+    for (std::size_t i = 0; i < n; ++i) {
+        V2 p = sub(b.hull[i], o), q = sub(b.hull[(i + 1) % n], o);
+        double c = cross(p, q);
+        a2 += c;
+        cx += (p.x + q.x) * c;
+        cy += (p.y + q.y) * c;
+    }
+    b.area = 0.5 * a2;
+    b.center = v2(o.x + cx / (3. * a2), o.y + cy / (3. * a2));
+    for (std::size_t i = 0; i < verts.size(); ++i) {
+        V2 p1 = verts[i];
+        for (std::size_t j = i; j < verts.size(); ++j) {
+            V2 p2 = verts[j];
+            if (norm(sub(p1, p2)) < 1.0e-6) continue;
+            V2 sc = v2((p1.x + p2.x) / 2., (p1.y + p2.y) / 2.);
+            V2 ncsc = sub(sc, b.center);
+            if (norm(ncsc) == 0.) continue;
+            double nc = 1. / norm(ncsc);
+            ncsc.x *= 1.0e-4 * nc;
+            ncsc.y *= 1.0e-4 * nc;
+            V2 fp = add(ncsc, sc);
+            if (inside_hull(b.hull.data(), int(b.hull.size()), fp)) continue;
+            GBorder br{};
+            br.p1 = p1;
+            br.p2 = p2;
+            br.nd = sub(p2, p1);
+            V2 npt = v2(br.nd.y, -br.nd.x);
+            if (dot(npt, ncsc) < 0.) npt = vneg(npt);
+            br.np = divs(npt, norm(npt));
+            br.la = sub(p1, scal(1.0e-6, br.nd));
+            br.lb = add(p2, scal(1.0e-6, br.nd));
+            bool dup = false;
+            for (auto& o2 : b.borders)
+                if (norm(sub(o2.np, br.np)) < 1.0e-6) dup = true;
+            if (!dup) b.borders.push_back(br);
+            if (b.borders.size() > verts.size()) throw Error(BTE_ERR_GEOMETRY, "To much borders");
+        }
+    }
+    return b;
+}
+
+std::vector<V2> touching_points(const BoxBuild& A, const BoxBuild& B) {
+    std::vector<V2> pts;
+    auto addp = [&](V2 p) {
+        for (auto& q : pts)
+            if (q.x == p.x && q.y == p.y) return;
+        pts.push_back(p);
+    };
+    const std::size_t na = A.hull.size(), nb = B.hull.size();
+    for (std::size_t i = 0; i < na; ++i) {
+        V2 a0 = A.hull[i], a1 = A.hull[(i + 1) % na];
+        for (std::size_t j = 0; j < nb; ++j) {
+            V2 b0 = B.hull[j], b1 = B.hull[(j + 1) % nb];
+            if (on_segment(b0, a0, a1)) addp(b0);
+            if (on_segment(b1, a0, a1)) addp(b1);
+            if (on_segment(a0, b0, b1)) addp(a0);
+            if (on_segment(a1, b0, b1)) addp(a1);
+        }
+    }
+    if (pts.size() > 2) throw Error(BTE_ERR_GEOMETRY, "overlapping boxes are not supported");
+    std::sort(pts.begin(), pts.end(),
+              [](V2 a, V2 b) { return a.x < b.x || (a.x == b.x && a.y < b.y); });
+    return pts;
+}
+
+std::vector<double> fill_cumulative(const std::vector<double>& p) {
+    if (*std::min_element(p.begin(), p.end()) < 0.)
+        throw Error(BTE_ERR_VALUE, "probabilities must be >= 0.");
+    std::vector<double> c;
+    c.reserve(p.size());
+    std::partial_sum(p.begin(), p.end(), std::back_inserter(c));
+    const double last = c.back();
+    if (!(last > 0.)) throw Error(BTE_ERR_VALUE, "distribution with zero total weight");
+    for (auto& x : c) x /= last;
+    return c;
+}
+
+// Axis-aligned rectangle check: returns true and its bounds.
+bool as_rect(const std::vector<V2>& hull, double& x0, double& y0, double& x1, double& y1) {
+    if (hull.size() != 4) return false;
+    x0 = x1 = hull[0].x;
+    y0 = y1 = hull[0].y;
+    for (auto& p : hull) {
+        x0 = std::min(x0, p.x);
+        x1 = std::max(x1, p.x);
+        y0 = std::min(y0, p.y);
+        y1 = std::max(y1, p.y);
+    }
+    for (auto& p : hull)
+        if (!((p.x == x0 || p.x == x1) && (p.y == y0 || p.y == y1))) return false;
+    return true;
+}
+
+void detect_grid(HostGeometry& G, const std::vector<BoxBuild>& bb) {
+    std::vector<double> xs, ys;
+    std::vector<std::array<double, 4>> r(bb.size());
+    for (std::size_t i = 0; i < bb.size(); ++i) {
+        if (!as_rect(bb[i].hull, r[i][0], r[i][1], r[i][2], r[i][3])) return;
+        xs.push_back(r[i][0]);
+        xs.push_back(r[i][2]);
+        ys.push_back(r[i][1]);
+        ys.push_back(r[i][3]);
+    }
+    std::sort(xs.begin(), xs.end());
+    xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
+    std::sort(ys.begin(), ys.end());
+    ys.erase(std::unique(ys.begin(), ys.end()), ys.end());
+    const int nx = int(xs.size()) - 1, ny = int(ys.size()) - 1;
+    if (nx < 1 || ny < 1 || double(nx) * ny > 5.0e7) return;
+    std::vector<int> cell(std::size_t(nx) * ny, -1);
+    for (std::size_t b = 0; b < bb.size(); ++b) {
+        int i0 = int(std::lower_bound(xs.begin(), xs.end(), r[b][0]) - xs.begin());
+        int i1 = int(std::lower_bound(xs.begin(), xs.end(), r[b][2]) - xs.begin());
+        int j0 = int(std::lower_bound(ys.begin(), ys.end(), r[b][1]) - ys.begin());
+        int j1 = int(std::lower_bound(ys.begin(), ys.end(), r[b][3]) - ys.begin());
+        if (i1 != i0 + 1 || j1 != j0 + 1) return;  // a box spanning several cells
+        int& c = cell[std::size_t(i0) * ny + j0];
+        if (c != -1) return;
+        c = G.reservoir[b] ? -2 - int(b) : int(b);
+    }
+    G.rect_grid = true;
+    G.gnx = nx;
+    G.gny = ny;
+    G.gx = xs;
+    G.gy = ys;
+    G.gcell = std::move(cell);
+}
+}  // namespace
+
+double bose_einstein(double omega, double T) {
+    constexpr double prefactor = 1e12 * hbar / kB;
+    return 1. / (std::exp(prefactor * omega / T) - 1.);
+}
+
+double bose_einstein_kernel(double omega, double T) {
+    constexpr double prefactor = 0.5 * 1e12 * hbar / kB;
+    double x = prefactor * omega / T;
+    if (x < 1e-320) return 1.;
+    if (x > 300.) return 0.;
+    double s = x / std::sinh(x);
+    return s * s;
+}
+
+double calc_cv(const HostModes& m, double T) {
+    double cv = 0.;
+    for (std::size_t k = 0; k < m.n(); ++k) cv += bose_einstein_kernel(m.omega[k], T);
+    cv *= kB / double(m.nq) / m.V;
+    return cv;
+}
+
+HostModes build_modes(const bte_mode_table* mt) {
+    if (!mt || mt->nq < 2 || mt->nb < 1 || !mt->omega || !mt->vg || !mt->w || !mt->dq)
+        throw Error(BTE_ERR_INPUT, "incomplete mode table");
+    if (!(mt->V > 0.) || !(mt->c_lat > 0.)) throw Error(BTE_ERR_INPUT, "bad unit cell");
+    HostModes m;
+    m.nq = mt->nq;
+    m.nb = mt->nb;
+    for (int i = 0; i < 3; ++i) m.grid[i] = mt->grid[i];
+    const std::size_t n = m.n();
+    if (n > (std::size_t(1) << 30)) throw Error(BTE_ERR_INPUT, "too many modes");
+    m.omega.assign(mt->omega, mt->omega + n);
+    m.w.assign(mt->w, mt->w + n);
+    m.vx.resize(n);
+    m.vy.resize(n);
+    m.vz.resize(n);
+    m.vxc.resize(n);
+    m.vyc.resize(n);
+    for (std::size_t k = 0; k < n; ++k) {
+        m.vx[k] = mt->vg[3 * k];
+        m.vy[k] = mt->vg[3 * k + 1];
+        m.vz[k] = mt->vg[3 * k + 2];
+        m.vxc[k] = almost_equal(m.vx[k], 0.) ? 0. : m.vx[k];
+        m.vyc[k] = almost_equal(m.vy[k], 0.) ? 0. : m.vy[k];
+        if (!std::isfinite(m.omega[k]) || !std::isfinite(m.w[k]) || m.w[k] < 0.)
+            throw Error(BTE_ERR_VALUE, "non-finite or negative mode data");
+    }
+    std::memcpy(m.dq, mt->dq, sizeof(m.dq));
+    m.V = mt->V;
+    m.c = mt->c_lat;
+    return m;
+}
+
+HostGeometry build_geometry(const bte_geometry* g) {
+    if (!g || g->nboxes < 1 || !g->npoints || !g->vertices || !g->Teq || !g->reservoir)
+        throw Error(BTE_ERR_INPUT, "incomplete geometry");
+    if (!(g->thickness > 0.)) throw Error(BTE_ERR_INPUT, "material thickness must be > 0");
+    HostGeometry G;
+    G.thickness = g->thickness;
+    std::vector<BoxBuild> bb;
+    std::size_t off = 0;
+    for (int i = 0; i < g->nboxes; ++i) {
+        std::vector<V2> verts;
+        if (g->npoints[i] < 3) throw Error(BTE_ERR_INPUT, "a box needs at least three vertices");
+        for (int j = 0; j < g->npoints[i]; ++j, ++off)
+            verts.push_back(v2(g->vertices[2 * off], g->vertices[2 * off + 1]));
+        bb.push_back(make_box(verts));
+        G.Teq.push_back(g->Teq[i]);
+        G.Tinit.push_back(g->Tinit ? g->Tinit[i] : g->Teq[i]);
+        G.reservoir.push_back(g->reservoir[i] != 0);
+    }
+    const int nbx = g->nboxes;
+    std::vector<std::array<double, 4>> bx(static_cast<std::size_t>(nbx));
+    for (int a = 0; a < nbx; ++a) {
+        const auto& h = bb[std::size_t(a)].hull;
+        double x0 = h[0].x, x1 = x0, y0 = h[0].y, y1 = y0;
+        for (auto& p : h) {
+            x0 = std::min(x0, p.x); x1 = std::max(x1, p.x);
+            y0 = std::min(y0, p.y); y1 = std::max(y1, p.y);
+        }
+        bx[std::size_t(a)] = {x0, y0, x1, y1};
+    }
+    for (int a = 0; a < nbx; ++a) {
+        for (int b = 0; b < nbx; ++b) {
+            if (a == b) continue;
+            const auto& A = bx[std::size_t(a)];
+            const auto& B = bx[std::size_t(b)];
+            if (B[0] > A[2] || A[0] > B[2] || B[1] > A[3] || A[1] > B[3]) continue;  // apart
+            auto pinter = touching_points(bb[std::size_t(a)], bb[std::size_t(b)]);
+            if (pinter.empty()) continue;
+            GBorder cb{};
+            const BoxBuild& me = bb[std::size_t(a)];
+            if (pinter.size() == 1 || norm(sub(pinter[1], pinter[0])) < 1.0e-6) {
+                cb.p1 = cb.p2 = pinter[0];
+                cb.np = divs(sub(cb.p1, me.center), norm(sub(cb.p1, me.center)));
+                bb[std::size_t(a)].contacts[b] = cb;
+                continue;
+            }
+            cb.p1 = pinter[0];
+            cb.p2 = pinter[1];
+            cb.nd = sub(cb.p2, cb.p1);
+            V2 sc = v2((cb.p1.x + cb.p2.x) / 2., (cb.p1.y + cb.p2.y) / 2.);
+            V2 ncsc = sub(sc, me.center);
+            V2 npt = v2(cb.nd.y, -cb.nd.x);
+            if (dot(npt, ncsc) < 0.) npt = vneg(npt);
+            cb.np = divs(npt, norm(npt));
+            cb.la = sub(cb.p1, divs(scal(1.0e-6, cb.nd), norm(cb.nd)));
+            cb.lb = add(cb.p2, divs(scal(1.0e-6, cb.nd), norm(cb.nd)));
+            bb[std::size_t(a)].contacts[b] = cb;
+        }
+        if (bb[std::size_t(a)].contacts.empty() && nbx > 1)
+            throw Error(BTE_ERR_GEOMETRY, "There are unconnected boxes");
+    }
+    for (int a = 0; a < nbx; ++a) {
+        const BoxBuild& me = bb[std::size_t(a)];
+        GBox box{};
+        box.center = me.center;
+        box.area = me.area;
+        box.hull_off = int(G.hull.size());
+        box.nhull = int(me.hull.size());
+        for (auto& p : me.hull) G.hull.push_back(p);
+        box.border_off = int(G.borders.size());
+        box.nborders = int(me.borders.size());
+        for (auto br : me.borders) {
+            int cls = -1;
+            for (std::size_t c = 0; c < G.normals.size(); ++c)
+                if (G.normals[c].x == br.np.x && G.normals[c].y == br.np.y) cls = int(c);
+            if (cls < 0) {
+                cls = int(G.normals.size());
+                G.normals.push_back(br.np);
+            }
+            br.ncls = cls;
+            G.borders.push_back(br);
+        }
+        box.contact_off = int(G.contacts.size());
+        box.ncontacts = int(me.contacts.size());
+        for (auto& [id, cb] : me.contacts) {
+            GContact c{};
+            c.id = id;
+            c.np = cb.np;
+            G.contacts.push_back(c);
+            G.contact_borders.push_back(cb);
+        }
+        box.reservoir = G.reservoir[std::size_t(a)];
+        G.boxes.push_back(box);
+    }
+    detect_grid(G, bb);
+    return G;
+}
+
+void alias_table(const double* w, int n, Alias* out) {
+    // Vose's alias method on weights scaled to mean 1.
+    double sum = 0.;
+    for (int i = 0; i < n; ++i) sum += w[i];
+    std::vector<double> p(static_cast<std::size_t>(n));
+    std::vector<int> small, large;
+    for (int i = 0; i < n; ++i) {
+        p[std::size_t(i)] = sum > 0. ? w[i] * n / sum : 0.;
+        (p[std::size_t(i)] < 1.0 ? small : large).push_back(i);
+        out[i].alt = i;
+        out[i].prob = 1.0f;
+    }
+    while (!small.empty() && !large.empty()) {
+        int s = small.back(), l = large.back();
+        small.pop_back();
+        out[s].prob = float(p[std::size_t(s)]);
+        out[s].alt = l;
+        p[std::size_t(l)] = (p[std::size_t(l)] + p[std::size_t(s)]) - 1.0;
+        if (p[std::size_t(l)] < 1.0) {
+            large.pop_back();
+            small.push_back(l);
+        }
+    }
+    // leftovers (rounding) keep themselves
+    for (int s : small) {
+        out[s].prob = 1.0f;
+        out[s].alt = s;
+    }
+    for (int l : large) {
+        out[l].prob = 1.0f;
+        out[l].alt = l;
+    }
+    // a zero-weight slot must never be kept
+    for (int i = 0; i < n; ++i)
+        if (w[i] <= 0. && out[i].alt == i) {
+            // point it to any positive slot
+            for (int j = 0; j < n; ++j)
+                if (w[j] > 0.) {
+                    out[i].alt = j;
+                    out[i].prob = 0.f;
+                    break;
+                }
+        } else if (w[i] <= 0.) {
+            out[i].prob = 0.f;
+        }
+}
+
+void build_resample(const HostModes& m, double T0, std::vector<double>& cdf,
+                    std::vector<Alias>& alias) {
+    std::vector<double> pmf(m.n());
+    for (std::size_t k = 0; k < m.n(); ++k)
+        pmf[k] = m.omega[k] <= 0. ? 0. : bose_einstein_kernel(m.omega[k], T0) * m.w[k];
+    cdf = fill_cumulative(pmf);
+    alias.resize(m.n());
+    alias_table(pmf.data(), int(m.n()), alias.data());
+}
+
+LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthreads) {
+    const std::size_t nq = std::size_t(m.nq), nb = std::size_t(m.nb), n = m.n();
+    // broadening per mode, Gamma_grid::base_sigma (include/qpoint_grid.hpp:179-181)
+    std::vector<double> sig(n);
+    for (std::size_t k = 0; k < n; ++k) {
+        const double v[3] = {m.vx[k], m.vy[k], m.vz[k]};
+        double r[3];
+        for (int j = 0; j < 3; ++j)
+            r[j] = v[0] * m.dq[0 + 3 * j] + v[1] * m.dq[1 + 3 * j] + v[2] * m.dq[2 + 3 * j];
+        sig[k] = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) / std::sqrt(12.);
+    }
+    {
+        std::vector<double> ls(n);
+        for (std::size_t k = 0; k < n; ++k)
+            ls[k] = sig[k] == 0. ? std::numeric_limits<double>::lowest() : std::log(sig[k]);
+        std::sort(ls.begin(), ls.end());
+        const double p25 = ls[25 * n / 100], p75 = ls[75 * n / 100];
+        const double lbound = std::exp(p25 - 1.5 * (p75 - p25));
+        for (auto& s : sig)
+            if (s < lbound) s = lbound;
+    }
+    const double root_two_pi = std::sqrt(2. * PI);
+    // candidate modes (not Gamma, omega not ~0), sorted by omega for windows
+    std::vector<int> cand;
+    double smax = 0.;
+    for (std::size_t k = 0; k < n; ++k)
+        if (k / nb >= 1 && !almost_equal(0., m.omega[k])) {
+            cand.push_back(int(k));
+            smax = std::max(smax, sig[k]);
+        }
+    std::vector<int> byw = cand;
+    std::sort(byw.begin(), byw.end(), [&](int a, int b) {
+        return m.omega[std::size_t(a)] < m.omega[std::size_t(b)] || (m.omega[std::size_t(a)] == m.omega[std::size_t(b)] && a < b);
+    });
+    std::vector<double> wsorted(byw.size());
+    for (std::size_t i = 0; i < byw.size(); ++i) wsorted[i] = m.omega[std::size_t(byw[i])];
+    // rows of (outgoing mode, pdf) for every incoming mode
+    std::vector<std::vector<std::pair<int, double>>> rows(n);
+    auto work = [&](std::size_t lo, std::size_t hi) {
+        std::vector<std::pair<int, double>> tmp;
+        for (std::size_t ci = lo; ci < hi; ++ci) {
+            const std::size_t k1 = std::size_t(cand[ci]);
+            const double w1 = m.omega[k1];
+            // hypot(a, b) <= a + b: a window of half-width nsigma (s1 + smax)
+            // (with a margin) contains every accepted partner.
+            const double half = nsigma * (sig[k1] + smax) * (1.0 + 1e-9) + 1e-300;
+            auto a = std::lower_bound(wsorted.begin(), wsorted.end(), w1 - half);
+            auto b = std::upper_bound(wsorted.begin(), wsorted.end(), w1 + half);
+            tmp.clear();
+            for (auto it = a; it != b; ++it) {
+                const std::size_t k2 = std::size_t(byw[std::size_t(it - wsorted.begin())]);
+                const double sigma = std::hypot(sig[k1], sig[k2]);
+                const double delta = std::fabs(m.omega[k1] - m.omega[k2]);
+                if (delta <= nsigma * sigma) {
+                    double e = delta;
+                    e *= -e;
+                    e /= 2 * sigma * sigma;
+                    double pdf = std::exp(e);
+                    pdf /= sigma * root_two_pi;
+                    tmp.push_back({int(k2), pdf});
+                }
+            }
+            std::sort(tmp.begin(), tmp.end());
+            rows[k1] = tmp;
+        }
+    };
+    if (nthreads < 1) nthreads = 1;
+    {
+        std::vector<std::thread> th;
+        const std::size_t nc = cand.size();
+        for (int t = 0; t < nthreads; ++t)
+            th.emplace_back(work, nc * std::size_t(t) / std::size_t(nthreads),
+                            nc * std::size_t(t + 1) / std::size_t(nthreads));
+        for (auto& t : th) t.join();
+    }
+    (void)nq;
+    // per wall-normal class: filter by outgoing direction and build the
+    // cumulative values of bounce() and an alias table
+    LambertTable L;
+    L.nclass = int(g.normals.size());
+    L.row_ptr.assign(std::size_t(L.nclass) * (n + 1), 0);
+    std::vector<std::vector<int>> ccol(std::size_t(L.nclass));
+    std::vector<std::vector<double>> ccdf(std::size_t(L.nclass));
+    std::vector<std::vector<AliasRow>> cal(std::size_t(L.nclass));
+    auto cwork = [&](int c) {
+        const V2 np = g.normals[std::size_t(c)];
+        auto& col = ccol[std::size_t(c)];
+        auto& cdf = ccdf[std::size_t(c)];
+        auto& al = cal[std::size_t(c)];
+        long long* rp = &L.row_ptr[std::size_t(c) * (n + 1)];
+        std::vector<std::pair<int, double>> states;
+        std::vector<double> wts;
+        std::vector<Alias> atmp;
+        for (std::size_t k = 0; k < n; ++k) {
+            rp[k] = (long long)col.size();
+            states.clear();
+            double cum = 0.;
+            for (auto& [imf, econ] : rows[k]) {
+                const double vx = m.vxc[std::size_t(imf)], vy = m.vyc[std::size_t(imf)];
+                const double vn = -(np.x * vx + np.y * vy);
+                if (vn < 0. || almost_equal(vn, 0.)) continue;
+                cum += vn * econ;
+                states.push_back({imf, vn * econ});
+            }
+            // std::map<double, size_t> semantics: a repeated key keeps the
+            // later mode
+            const std::size_t start = col.size();
+            double cum2 = 0;
+            wts.clear();
+            for (auto& [imf, tran] : states) {
+                cum2 += tran / cum;
+                if (col.size() > start && cdf.back() == cum2) {
+                    col.back() = imf;
+                    wts.back() += tran;
+                } else {
+                    col.push_back(imf);
+                    cdf.push_back(cum2);
+                    wts.push_back(tran);
+                }
+            }
+            const int len = int(col.size() - start);
+            atmp.resize(std::size_t(len));
+            if (len > 0) alias_table(wts.data(), len, atmp.data());
+            for (int j = 0; j < len; ++j) {
+                AliasRow r;
+                r.prob = atmp[std::size_t(j)].prob;
+                r.keep = col[start + std::size_t(j)];
+                r.alt = col[start + std::size_t(atmp[std::size_t(j)].alt)];
+                r.pad = 0;
+                al.push_back(r);
+            }
+        }
+        rp[n] = (long long)col.size();
+    };
+    {
+        std::vector<std::thread> th;
+        for (int c = 0; c < L.nclass; ++c) th.emplace_back(cwork, c);
+        for (auto& t : th) t.join();
+    }
+    long long base = 0;
+    for (int c = 0; c < L.nclass; ++c) {
+        long long* rp = &L.row_ptr[std::size_t(c) * (n + 1)];
+        for (std::size_t k = 0; k <= n; ++k) rp[k] += base;
+        base += (long long)ccol[std::size_t(c)].size();
+        L.col.insert(L.col.end(), ccol[std::size_t(c)].begin(), ccol[std::size_t(c)].end());
+        L.cdf.insert(L.cdf.end(), ccdf[std::size_t(c)].begin(), ccdf[std::size_t(c)].end());
+        L.alias.insert(L.alias.end(), cal[std::size_t(c)].begin(), cal[std::size_t(c)].end());
+    }
+    return L;
+}
+
+Generators build_wall_generators(const HostModes& m, const HostGeometry& g) {
+    Generators R;
+    const std::size_t n = m.n();
+    const double vuc = m.V * g.thickness / m.c;
+    const int nbx = int(g.boxes.size());
+    std::vector<double> pmf(n);
+    for (int s = 0; s < nbx; ++s) {
+        if (!g.reservoir[std::size_t(s)]) continue;
+        const GBox& rb = g.boxes[std::size_t(s)];
+        for (int ci = 0; ci < rb.ncontacts; ++ci) {
+            const int c = g.contacts[std::size_t(rb.contact_off + ci)].id;
+            if (g.reservoir[std::size_t(c)]) continue;
+            const GBorder& b = g.contact_borders[std::size_t(rb.contact_off + ci)];
+            if (almost_equal(norm(sub(b.p2, b.p1)), 0.)) continue;
+            const double Tw = g.Teq[std::size_t(s)], Te = g.Teq[std::size_t(c)];
+            if (almost_equal(Tw, Te)) continue;
+            for (std::size_t k = 0; k < n; ++k) {
+                const double vn = b.np.x * m.vx[k] + b.np.y * m.vy[k] + 0. * m.vz[k];
+                if (vn <= 0. || almost_equal(0., m.omega[k]))
+                    pmf[k] = 0.;
+                else
+                    pmf[k] = vn * m.omega[k] *
+                             std::fabs(bose_einstein(m.omega[k], Tw) - bose_einstein(m.omega[k], Te));
+            }
+            const double cumulsum = 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+            WallGenerator W{};
+            W.res = s;
+            W.box = c;
+            W.sign = (Tw - Te) >= 0 ? 1 : -1;
+            W.p1 = b.p1;
+            W.nd = b.nd;
+            W.sa = b.p1;
+            W.sb = b.p2;
+            W.flux = W.sign * (cumulsum / (double(m.nq) * vuc));
+            auto cdf = fill_cumulative(pmf);
+            R.cdf.insert(R.cdf.end(), cdf.begin(), cdf.end());
+            std::vector<Alias> al(n);
+            alias_table(pmf.data(), int(n), al.data());
+            R.alias.insert(R.alias.end(), al.begin(), al.end());
+            R.walls.push_back(W);
+        }
+    }
+    if (R.walls.empty())
+        throw Error(BTE_ERR_INPUT, "no isothermal wall generator (no reservoir with a different Teq)");
+    std::vector<double> ws;
+    double total = 0;
+    for (auto& W : R.walls) {
+        const double Lb = norm(sub(W.sb, W.sa));
+        W.energy = std::fabs(W.flux) * Lb * g.thickness;
+        total += W.energy;
+        ws.push_back(W.energy);
+    }
+    const double wnorm = std::accumulate(ws.begin(), ws.end(), 0.);
+    double cum = 0;
+    for (double w : ws) {
+        cum += w / wnorm;
+        R.wall_cum.push_back(cum);
+    }
+    R.total_energy = total;
+    return R;
+}
+
+Generators build_initial_generators(const HostModes& m, const HostGeometry& g) {
+    Generators R;
+    const std::size_t n = m.n();
+    const double vuc = m.V * g.thickness / m.c;
+    std::vector<double> pmf(n);
+    for (std::size_t s = 0; s < g.boxes.size(); ++s) {
+        if (g.reservoir[s]) continue;
+        const double Tr = g.Tinit[s], Te = g.Teq[s];
+        if (almost_equal(Te, Tr)) continue;
+        if (Tr <= 0 || Te <= 0) throw Error(BTE_ERR_VALUE, "Invalid temperature value");
+        for (std::size_t k = 0; k < n; ++k) {
+            const double om = m.omega[k];
+            pmf[k] = almost_equal(om, 0.)
+                         ? 0.
+                         : om * std::fabs(bose_einstein(om, Tr) - bose_einstein(om, Te));
+        }
+        const double cumulsum = 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+        const double vol = g.boxes[s].area * g.thickness / vuc;
+        R.init_box.push_back(int(s));
+        R.init_sign.push_back((Tr - Te) >= 0 ? 1 : -1);
+        R.init_energy.push_back(vol * cumulsum / double(m.nq));
+        auto cdf = fill_cumulative(pmf);
+        R.cdf.insert(R.cdf.end(), cdf.begin(), cdf.end());
+        std::vector<Alias> al(n);
+        alias_table(pmf.data(), int(n), al.data());
+        R.alias.insert(R.alias.end(), al.begin(), al.end());
+    }
+    if (R.init_box.empty()) throw Error(BTE_ERR_INPUT, "no box with Tinit different from Teq");
+    double total = 0;
+    for (double e : R.init_energy) total += e;
+    R.total_energy = total;
+    return R;
+}
+
+double initial_counts(Generators& R, int64_t nparticles, uint64_t seed) {
+    if (nparticles < 1) throw Error(BTE_ERR_INPUT, "nparticles must be >= 1");
+    const double Eeff = R.total_energy / double(nparticles);
+    R.init_first.clear();
+    // Ntogenerate: floor(E_box / Eeff) plus one with probability equal to the
+    // fraction (src/sampling.cpp:310-326), drawn from pcg64(seed, 2^63 + box)
+    long long first = 0;
+    for (std::size_t b = 0; b < R.init_box.size(); ++b) {
+        R.init_first.push_back(first);
+        const double gen = R.init_energy[b] / Eeff;
+        long long np = (long long)gen;
+        const double rem = gen - std::floor(gen);
+        Pcg64 r;
+        r.seed(seed, (uint64_t(1) << 63) + uint64_t(R.init_box[b]));
+        if (canonical_from(r.next()) <= rem) np++;
+        first += np;
+    }
+    R.init_first.push_back(first);
+    return Eeff;
+}
+
+std::vector<int> build_mirror(const HostModes& m, const HostGeometry& g) {
+    const std::size_t n = m.n();
+    const int nc = int(g.normals.size());
+    std::vector<int> mir(std::size_t(nc) * n, -1);
+    const int n1 = m.grid[0], n2 = m.grid[1];
+    if (n1 < 1 || n2 < 1 || std::size_t(n1) * std::size_t(n2) != std::size_t(m.nq)) return mir;
+    for (int c = 0; c < nc; ++c) {
+        const V2 np = g.normals[std::size_t(c)];
+        const bool ny = (np.x == 0. && std::fabs(np.y) == 1.);
+        const bool nx = (np.y == 0. && std::fabs(np.x) == 1.);
+        if (!nx && !ny) continue;
+        for (std::size_t k = 0; k < n; ++k) {
+            const int iq = int(k / std::size_t(m.nb)), ib = int(k % std::size_t(m.nb));
+            int i = iq / n2, j = iq % n2;
+            if (ny) j = (n2 - j) % n2;
+            if (nx) i = (n1 - i) % n1;
+            const std::size_t k2 = std::size_t(i * n2 + j) * std::size_t(m.nb) + std::size_t(ib);
+            // the image must carry the reflected velocity
+            const double vn_in = np.x * m.vxc[k] + np.y * m.vyc[k];
+            const double vn_out = np.x * m.vxc[k2] + np.y * m.vyc[k2];
+            const double vt_in = nx ? m.vyc[k] : m.vxc[k];
+            const double vt_out = nx ? m.vyc[k2] : m.vxc[k2];
+            if (vn_out == -vn_in && vt_out == vt_in && m.omega[k2] > 0.)
+                mir[std::size_t(c) * n + k] = int(k2);
+        }
+    }
+    return mir;
+}
+
+}  // namespace bte

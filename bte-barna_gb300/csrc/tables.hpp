@@ -1,0 +1,125 @@
+// tables.hpp - host construction of the device-side tables of the particle
+// loop: geometry records, sampling distributions (CDF for replay, alias for
+// production), the energy-conserving Lambert wall table and the particle
+// generators.
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/btegpu.h"
+#include "bte_device.cuh"
+
+namespace bte {
+
+// Status-carrying exception used inside the library only; the C ABI turns
+// it into a bte_status and a message.
+struct Error : std::runtime_error {
+    bte_status code;
+    Error(bte_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+struct HostModes {
+    int nq = 0, nb = 0, grid[3] = {0, 0, 0};
+    std::vector<double> omega, vx, vy, vz, w;
+    std::vector<double> vxc, vyc;  // get_v: components almost equal to 0 set to 0
+    double dq[9] = {0};
+    double V = 0, c = 0;
+    std::size_t n() const { return std::size_t(nq) * std::size_t(nb); }
+};
+
+struct HostGeometry {
+    std::vector<GBox> boxes;
+    std::vector<V2> hull;
+    std::vector<GBorder> borders;
+    std::vector<GContact> contacts;
+    std::vector<GBorder> contact_borders;  // host copy of each contact border
+    std::vector<V2> normals;  // distinct border normals; GBorder::ncls indexes it
+    std::vector<double> Teq, Tinit;
+    std::vector<int> reservoir;
+    double thickness = 0;
+    // axis-aligned grid description (production fast path); valid when
+    // rect_grid is true: cell (i, j) -> box id or -1 (void / pore),
+    // -2 - r for reservoir r.
+    bool rect_grid = false;
+    int gnx = 0, gny = 0;
+    std::vector<double> gx, gy;    // grid lines, gnx+1 and gny+1 values
+    std::vector<int> gcell;        // [gnx * gny], i-major
+};
+
+// Alias entry of a Lambert row: pick slot j, keep its mode with probability
+// prob, else take alt (Walker / Vose).
+struct AliasRow {
+    float prob;
+    int keep;
+    int alt;
+    int pad;
+};
+// Alias entry of a mode distribution: keep = the slot itself.
+struct Alias {
+    float prob;
+    int alt;
+};
+
+struct LambertTable {
+    int nclass = 0;
+    std::vector<long long> row_ptr;  // [nclass][n + 1]
+    std::vector<int> col;            // outgoing mode of each entry
+    std::vector<double> cdf;         // replay: cumulative values (std::map semantics)
+    std::vector<AliasRow> alias;     // production
+};
+
+struct WallGenerator {
+    int res, box, sign;
+    V2 p1, nd, sa, sb;  // contact border seen from the reservoir
+    double flux;        // J nm^-2 ps^-1
+    double energy;      // J / ps (|flux| * length * thickness)
+};
+
+struct Generators {
+    // BTE_SOURCE_WALLS
+    std::vector<WallGenerator> walls;
+    std::vector<double> wall_cum;  // cumulative weights of the walls
+    // BTE_SOURCE_INITIAL
+    std::vector<int> init_box;            // boxes with Tinit != Teq
+    std::vector<int> init_sign;
+    std::vector<long long> init_first;    // first particle of each box (prefix)
+    std::vector<double> init_energy;      // J per box
+    // distributions: one row of n modes per generator (walls or init boxes)
+    std::vector<double> cdf;              // [ngen][n]
+    std::vector<Alias> alias;             // [ngen][n]
+    double total_energy = 0;              // J/ps (walls) or J (initial)
+};
+
+HostModes build_modes(const bte_mode_table* mt);
+HostGeometry build_geometry(const bte_geometry* g);
+
+// Resampling distribution after an RTA scattering: pmf ~ C(omega, T) w.
+void build_resample(const HostModes& m, double T0, std::vector<double>& cdf,
+                    std::vector<Alias>& alias);
+
+// Lambert table rows per (wall-normal class, incoming mode).
+LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthreads);
+
+Generators build_wall_generators(const HostModes& m, const HostGeometry& g);
+// Distributions of the initial deviation per box (no particle counts).
+Generators build_initial_generators(const HostModes& m, const HostGeometry& g);
+// Particle counts per box for N particles (Ntogenerate stochastic rounding):
+// fills init_first and returns Eeff.
+double initial_counts(Generators& G, int64_t nparticles, uint64_t seed);
+
+// Walker/Vose alias table of unnormalised non-negative weights.
+void alias_table(const double* w, int n, Alias* out);
+
+// Mode-mirror maps for specular reflection on the q grid: for each wall
+// normal class, the mode with v_n reversed (or -1 when the class is not
+// axis-aligned or the grid has no mirror image).
+std::vector<int> build_mirror(const HostModes& m, const HostGeometry& g);
+
+double calc_cv(const HostModes& m, double T);
+double bose_einstein(double omega, double T);
+double bose_einstein_kernel(double omega, double T);
+
+}  // namespace bte

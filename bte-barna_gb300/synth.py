@@ -1,0 +1,229 @@
+"""Seeded synthetic inputs for the RTA / beyond-RTA particle loop.
+
+The reference reads almaBTE HDF5 databases (src/bulk_hdf5.cpp:443-686) and
+geometry XMLs (src/geometry_2d.cpp:408-522).  No database exists here, so the
+workloads run on synthetic 2D-material mode tables with the shapes, sizes and
+value distributions of the benchmark configurations:
+
+  * square lattice a = 0.25 nm, out-of-plane c = thickness = 0.335 nm;
+  * Gamma-centred n x n q-grid, q index iq = i*n + j, iq = 0 is Gamma;
+  * acoustic branches omega = W_b sin(pi s / 2), s = 2|q| (reduced units, s = 1
+    at the zone boundary along the axes), W_b ~ 2 pi U[5, 15] THz;
+  * flat optical branches 2 pi U[15, 30] THz, each mode x (1 + U[-0.05, 0.05]);
+  * group velocity = the analytic gradient (0 for flat branches);
+  * tau = A (omega / omega_max,b)^-2 exp(-Theta / 3T) / exp(-Theta / 900),
+    A log-uniform in [1, 100] ps per mode, Theta = hbar max(omega) / kB, so
+    that tau(300 K) = A at omega = omega_max,b; Gamma acoustic modes get w = 0.
+
+All randomness comes from numpy SeedSequence((master, config, purpose)).
+"""
+import math
+import os
+
+import numpy as np
+
+MASTER_SEED = 20261203
+KB = 1.3806488e-23
+HBAR = 1.054571726e-34
+A_LAT = 0.25
+C_LAT = 0.335
+
+
+def _rng(config: int, purpose: int) -> np.random.Generator:
+    return np.random.default_rng(np.random.SeedSequence((MASTER_SEED, config, purpose)))
+
+
+def mode_table(n: int = 32, n_acoustic: int = 3, n_optical: int = 3, T: float = 300.0,
+               config: int = 0) -> dict:
+    """Mode table as a dict of numpy arrays (keys mirror bte_mode_table)."""
+    rng = _rng(config, 1)
+    nb = n_acoustic + n_optical
+    idx = np.arange(n)
+    qred = ((idx + n // 2) % n - n // 2) / n          # wrapped to [-1/2, 1/2)
+    qx = np.repeat(qred, n)                            # iq = i*n + j
+    qy = np.tile(qred, n)
+    qn = np.sqrt(qx * qx + qy * qy)
+    s = 2.0 * qn
+    nq = n * n
+    omega = np.zeros((nq, nb))
+    vg = np.zeros((nq, nb, 3))
+    wmax_b = np.zeros(nb)
+    W = 2 * math.pi * rng.uniform(5.0, 15.0, n_acoustic)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ux = np.where(qn > 0, qx / np.where(qn > 0, qn, 1), 0.0)
+        uy = np.where(qn > 0, qy / np.where(qn > 0, qn, 1), 0.0)
+    for b in range(n_acoustic):
+        omega[:, b] = W[b] * np.sin(math.pi * s / 2)
+        dwds = W[b] * np.cos(math.pi * s / 2) * (math.pi / 2)
+        # ds/dk = 2 (q/|q|) a / (2 pi) per unit k = (2 pi / a) q
+        vg[:, b, 0] = dwds * 2.0 * ux * A_LAT / (2 * math.pi)
+        vg[:, b, 1] = dwds * 2.0 * uy * A_LAT / (2 * math.pi)
+        wmax_b[b] = W[b]
+    omega[0, :n_acoustic] = 0.0
+    vg[0, :n_acoustic, :] = 0.0
+    Om = 2 * math.pi * rng.uniform(15.0, 30.0, n_optical)
+    for k in range(n_optical):
+        b = n_acoustic + k
+        omega[:, b] = Om[k] * (1.0 + rng.uniform(-0.05, 0.05, nq))
+        wmax_b[b] = omega[:, b].max()
+    A = np.exp(rng.uniform(math.log(1.0), math.log(100.0), (nq, nb)))
+    theta = HBAR * 1e12 * omega.max() / KB
+    ratio = np.where(omega > 0, omega / wmax_b[None, :], 1.0)
+    tau = A * ratio ** -2 * math.exp(-theta / (3 * T)) / math.exp(-theta / 900.0)
+    w = np.where(omega > 0, 1.0 / tau, 0.0)
+    dq = np.zeros((3, 3))
+    dq[0, 0] = 2 * math.pi / (A_LAT * n)
+    dq[1, 1] = 2 * math.pi / (A_LAT * n)
+    dq[2, 2] = 2 * math.pi / C_LAT
+    return {
+        "nq": nq, "nb": nb, "grid": (n, n, 1),
+        "omega": np.ascontiguousarray(omega.reshape(-1)),
+        "vg": np.ascontiguousarray(vg.reshape(-1)),
+        "w": np.ascontiguousarray(w.reshape(-1)),
+        "dq": np.ascontiguousarray(dq.reshape(-1, order="F")),
+        "V": A_LAT * A_LAT * C_LAT, "c_lat": C_LAT, "T": T,
+    }
+
+
+def _rect(x0, y0, x1, y1):
+    # vertex order of the reference's examples: (x0,y0) (x0,y1) (x1,y1) (x1,y0)
+    return [(x0, y0), (x0, y1), (x1, y1), (x1, y0)]
+
+
+def ribbon_geometry(length: float = 1000.0, width: float = 100.0, ncells: int = 50,
+                    T_hot: float = 301.0, T_cold: float = 299.0, T0: float = 300.0,
+                    thickness: float = C_LAT, reservoir_depth: float = 20.0) -> dict:
+    """Ribbon of `ncells` boxes along x between two isothermal reservoirs."""
+    boxes, Teq, res = [], [], []
+    dx = length / ncells
+    for i in range(ncells):
+        boxes.append(_rect(i * dx, 0.0, (i + 1) * dx, width))
+        Teq.append(T0)
+        res.append(0)
+    boxes.append(_rect(-reservoir_depth, 0.0, 0.0, width))
+    Teq.append(T_hot)
+    res.append(1)
+    boxes.append(_rect(length, 0.0, length + reservoir_depth, width))
+    Teq.append(T_cold)
+    res.append(1)
+    return _pack(boxes, Teq, list(Teq), res, thickness)
+
+
+def grid_geometry(lx: float, ly: float, nx: int, ny: int, T0: float = 300.0,
+                  pore_center=None, pore_diameter: float = 0.0,
+                  hot_center=None, hot_sigma: float = 50.0, hot_dT: float = 0.0,
+                  thickness: float = C_LAT) -> dict:
+    """Rectangle of nx x ny cells; cells whose centre lies inside the pore
+    circle are removed (a staircase pore); optional Gaussian initial hot spot
+    sets Tinit per cell."""
+    boxes, Teq, Tinit, res = [], [], [], []
+    dx, dy = lx / nx, ly / ny
+    for i in range(nx):
+        for j in range(ny):
+            cx, cy = (i + 0.5) * dx, (j + 0.5) * dy
+            if pore_center is not None:
+                if math.hypot(cx - pore_center[0], cy - pore_center[1]) < pore_diameter / 2:
+                    continue
+            boxes.append(_rect(i * dx, j * dy, (i + 1) * dx, (j + 1) * dy))
+            Teq.append(T0)
+            if hot_center is not None and hot_dT != 0.0:
+                r2 = (cx - hot_center[0]) ** 2 + (cy - hot_center[1]) ** 2
+                Tinit.append(T0 + hot_dT * math.exp(-r2 / (2 * hot_sigma ** 2)))
+            else:
+                Tinit.append(T0)
+            res.append(0)
+    return _pack(boxes, Teq, Tinit, res, thickness)
+
+
+def _pack(boxes, Teq, Tinit, res, thickness):
+    npts = np.array([len(b) for b in boxes], dtype=np.int32)
+    verts = np.array([c for b in boxes for p in b for c in p], dtype=np.float64)
+    return {
+        "nboxes": len(boxes), "npoints": npts, "vertices": verts,
+        "Teq": np.array(Teq, dtype=np.float64), "Tinit": np.array(Tinit, dtype=np.float64),
+        "reservoir": np.array(res, dtype=np.int32), "thickness": float(thickness),
+    }
+
+
+def write_geometry_xml(path: str, geom: dict, material: str = "synthetic") -> None:
+    """Geometry XML in the schema of read_geometry_XML (src/geometry_2d.cpp:408-522)."""
+    lines = ["<Geometry>", f'    <number_of_boxes Ngeom="{geom["nboxes"]}"/>']
+    off = 0
+    for i in range(geom["nboxes"]):
+        n = int(geom["npoints"][i])
+        lines.append("    <Box>")
+        lines.append(f'        <BoxID id="{i}"/>')
+        lines.append(f'        <MaterialID name="{material}"/>')
+        lines.append(f'        <Vertices dim="2" npoints="{n}">')
+        for k in range(n):
+            x, y = geom["vertices"][2 * (off + k)], geom["vertices"][2 * (off + k) + 1]
+            lines.append(f"           {x!r} {y!r}")
+        lines.append("        </Vertices>")
+        off += n
+        teq, tin = geom["Teq"][i], geom["Tinit"][i]
+        if tin != teq:
+            lines.append(f'        <initCnd Teq="{teq!r}" Tinit="{tin!r}"/>')
+        else:
+            lines.append(f'        <initCnd Teq="{teq!r}"/>')
+        if geom["reservoir"][i]:
+            lines.append("        <Reservoir/>")
+        lines.append("    </Box>")
+    lines.append("</Geometry>")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+MODES_MAGIC = b"BTEMODE1"
+
+
+def write_modes_file(path: str, m: dict) -> None:
+    """Binary mode table read by the rtamc2d_gpu drop-in in place of the HDF5
+    database: magic, int32 nq, nb, grid[3], float64 V, c_lat, dq[9], then
+    omega[nq*nb], vg[nq*nb*3], w[nq*nb] (little endian)."""
+    with open(path, "wb") as f:
+        f.write(MODES_MAGIC)
+        np.array([m["nq"], m["nb"], *m["grid"]], dtype="<i4").tofile(f)
+        np.array([m["V"], m["c_lat"]], dtype="<f8").tofile(f)
+        np.asarray(m["dq"], dtype="<f8").tofile(f)
+        np.asarray(m["omega"], dtype="<f8").tofile(f)
+        np.asarray(m["vg"], dtype="<f8").tofile(f)
+        np.asarray(m["w"], dtype="<f8").tofile(f)
+
+
+# ------------------------------------------------------------------ configs
+def config0(n_particles: int = 1_000_000) -> dict:
+    """Plain RTA ribbon: 32x32x6 modes, 1 um x 100 nm, 50 cells, 301/299 K
+    reservoirs, diffuse walls, 100 bins of 10 ps."""
+    return {"modes": mode_table(32, 3, 3, 300.0, config=0),
+            "geom": ribbon_geometry(1000.0, 100.0, 50),
+            "T0": 300.0, "dt": 10.0, "maxtime": 1000.0, "N": n_particles,
+            "specularity": 0.0, "source": "walls"}
+
+
+def config1(n_particles: int = 100_000_000) -> dict:
+    """Transient RTA at scale: 64x64x9 modes, 2 um x 500 nm, 100x25 cells of
+    20 nm, 200 nm-diameter staircase pore at the centre, p = 0.3, 1 K Gaussian
+    hot spot (sigma 50 nm) at (500, 250) nm, 200 bins to 10 ns."""
+    return {"modes": mode_table(64, 3, 6, 300.0, config=1),
+            "geom": grid_geometry(2000.0, 500.0, 100, 25, 300.0,
+                                  pore_center=(1000.0, 250.0), pore_diameter=200.0,
+                                  hot_center=(500.0, 250.0), hot_sigma=50.0, hot_dT=1.0),
+            "T0": 300.0, "dt": 50.0, "maxtime": 10000.0, "N": n_particles,
+            "specularity": 0.3, "source": "initial"}
+
+
+def small_case(n: int = 8, ncells: int = 5, n_particles: int = 2000, maxtime: float = 200.0,
+               dt: float = 10.0, width: float = 50.0, length: float = 200.0) -> dict:
+    """A parity-sized ribbon the oracle finishes in well under a second."""
+    return {"modes": mode_table(n, 3, 3, 300.0, config=100),
+            "geom": ribbon_geometry(length, width, ncells),
+            "T0": 300.0, "dt": dt, "maxtime": maxtime, "N": n_particles,
+            "specularity": 0.0, "source": "walls"}
+
+
+if __name__ == "__main__":
+    m = mode_table()
+    print(m["nq"], m["nb"], float(np.max(np.abs(m["vg"]))), float(np.max(m["omega"])))
+    w = m["w"][m["w"] > 0]
+    print("tau range ps", 1 / w.max(), 1 / w.min())
+    os.makedirs("/tmp/bte", exist_ok=True)

@@ -1,0 +1,195 @@
+/*
+ * btegpu.h - C ABI of the GB300 deviational Monte Carlo engine for the
+ * RTAMC2D / beRTAMC2D particle loop of BTE-Barna.
+ *
+ * The reference has no library or plugin interface: its boundary is the
+ * executable plus files (src/RTA_MC2D.cpp:2085-2101 argv, :1806-2055 XML,
+ * src/bulk_hdf5.cpp:443 mode table, :2437-2471 CSV outputs).  Each entry point
+ * below replaces one step of that pipeline; the citation on each names the
+ * reference code whose role it takes.
+ *
+ * Conventions
+ *  - Plain C types only; caller-owned host buffers are copied in, results go
+ *    to caller-allocated host buffers, device memory is owned by the context.
+ *  - No exception crosses the ABI: every call returns a bte_status, and
+ *    bte_last_error() gives the message of the last failing call.
+ *  - One context per host thread; calls on one context are serialised; the
+ *    context owns one CUDA stream and results are valid when a call returns.
+ *  - Mode index = iq * nb + ib (src/RTA_MC2D.cpp:1250-1254).
+ *  - Units follow the reference: omega rad/ps, velocities nm/ps, lengths nm,
+ *    times ps, energies J (include/constants.hpp:27-56).
+ */
+#ifndef BTEGPU_H
+#define BTEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BTEGPU_VERSION 1
+
+/* Status codes.  The first three mirror the reference's exception types
+ * (include/exceptions.hpp:25-55). */
+typedef enum bte_status {
+    BTE_OK = 0,
+    BTE_ERR_INPUT = 1,    /* alma::input_error: malformed or unsupported input */
+    BTE_ERR_VALUE = 2,    /* alma::value_error: e.g. a zero scattering rate   */
+    BTE_ERR_GEOMETRY = 3, /* alma::geometry_error: inconsistent geometry      */
+    BTE_ERR_LIMIT = 4,    /* a device loop reached its iteration cap          */
+    BTE_ERR_CUDA = 5,     /* CUDA runtime failure                             */
+    BTE_ERR_STATE = 6     /* wrong call order (e.g. run before load)          */
+} bte_status;
+
+/* Run modes. */
+enum {
+    /* Deterministic replay: one pcg64 stream per particle (seed, stream =
+     * particle index), CDF inversion by lower_bound, FP64 everywhere, exact
+     * fixed-point tallies.  Bit-identical to the CPU restatement in oracle/. */
+    BTE_MODE_REPLAY = 0,
+    /* Production: counter-based Philox4x32-10 streams keyed by (seed,
+     * particle), alias tables, FP64 position/time/tallies with FP64 atomics. */
+    BTE_MODE_PRODUCTION = 1
+};
+
+/* Particle sources of an RTA run. */
+enum {
+    /* Isothermal reservoir walls inject at t=0; the tally is integrated in
+     * time into a step response (src/RTA_MC2D.cpp:272-449, :2380-2384). */
+    BTE_SOURCE_WALLS = 0,
+    /* Initial deviation Tinit - Teq per box (outTref_distribution,
+     * src/sampling.cpp:271-330); tallies are bin averages, not integrated. */
+    BTE_SOURCE_INITIAL = 1
+};
+
+typedef struct bte_ctx bte_ctx;
+
+typedef struct bte_device_opts {
+    int32_t device;  /* CUDA device ordinal */
+    int32_t verbose; /* 0 = silent, 1 = banners like the reference's stdout */
+} bte_device_opts;
+
+/* Phonon mode table of one material (replaces alma::Gamma_grid +
+ * Crystal_structure as loaded by load_bulk_hdf5, src/bulk_hdf5.cpp:443-686,
+ * and the RTA rates of calc_w0_threeph + calc_w0_twoph,
+ * src/RTA_MC2D.cpp:1899-1907).  iq = 0 must be the Gamma point. */
+typedef struct bte_mode_table {
+    int32_t nq;            /* number of q points                                */
+    int32_t nb;            /* branches per q point                              */
+    int32_t grid[3];       /* q-grid divisions; q index iq = i*grid[1] + j     */
+    const double* omega;   /* [nq*nb] angular frequency, rad/ps                */
+    const double* vg;      /* [nq*nb*3] group velocity (vx,vy,vz), nm/ps       */
+    const double* w;       /* [nq*nb] RTA scattering rate 1/tau, 1/ps          */
+    const double* dq;      /* [9] column-major q-grid steps, nm^-1
+                              (Gamma_grid::dq, include/qpoint_grid.hpp:45)      */
+    double V;              /* unit-cell volume, nm^3 (Crystal_structure::V)     */
+    double c_lat;          /* out-of-plane lattice vector lattvec(2,2), nm      */
+} bte_mode_table;
+
+/* Convex boxes of a geometry XML (replaces read_geometry_XML,
+ * src/geometry_2d.cpp:408-522, and the geometry_2d constructor :127-153). */
+typedef struct bte_geometry {
+    int32_t nboxes;
+    const int32_t* npoints;   /* [nboxes] vertices per box                     */
+    const double* vertices;   /* (x,y) pairs of all boxes, concatenated, nm     */
+    const double* Teq;        /* [nboxes] initCnd Teq, K                        */
+    const double* Tinit;      /* [nboxes] initCnd Tinit (= Teq when absent), K  */
+    const int32_t* reservoir; /* [nboxes] 1 for <Reservoir/>                    */
+    double thickness;         /* material thickness, nm (<material thickness>)  */
+} bte_geometry;
+
+/* Parameters of one RTA run (the <RTA_MC2d> XML of src/RTA_MC2D.cpp:1818-1947
+ * plus the knobs of this engine). */
+typedef struct bte_rta_params {
+    double T0;               /* reference temperature, K                        */
+    double dt;               /* width of a time bin, ps                         */
+    double maxtime;          /* simulated time, ps                              */
+    int64_t nparticles;      /* N: sets Eeff = |E|/N                            */
+    uint64_t seed;           /* master seed of all particle streams             */
+    int32_t mode;            /* BTE_MODE_*                                      */
+    int32_t source;          /* BTE_SOURCE_*                                    */
+    int32_t ballistic;       /* 1: no intrinsic scattering (<ballistic/>)       */
+    int32_t reserved0;
+    double specularity;      /* p of void walls; 0 = the reference's diffuse    */
+    int64_t particle_begin;  /* simulate particles [begin, end) of the N;      */
+    int64_t particle_end;    /*   end <= 0 means N                              */
+} bte_rta_params;
+
+/* Results of one RTA run.  Every array pointer may be NULL (not written).
+ * Arrays are row-major [nboxes][nbins]. */
+typedef struct bte_rta_result {
+    int32_t nboxes;          /* out */
+    int32_t nbins;           /* out: ntime - 1                                   */
+    double* gz;              /* raw sign-weighted particle time per box and bin  */
+    double* gz_jx;           /* raw vx-weighted tally                            */
+    double* gz_jy;           /* raw vy-weighted tally                            */
+    double* temperature;     /* K, as written to temperature_*.csv               */
+    double* jx;              /* J m^-2 s^-1, as written to jx_*.csv              */
+    double* jy;              /* J m^-2 s^-1, as written to jy_*.csv              */
+    int64_t* exact;          /* replay mode: [nboxes][nbins][3][2] 128-bit
+                                fixed-point sums (hi, lo) scaled by 2^44       */
+    double Eeff;             /* energy per particle, J/ps (src/RTA_MC2D.cpp:2177) */
+    double energy_rate;      /* |E| injected per ps or initial energy, J         */
+    int64_t events;          /* free-flight draws (random_dt calls)              */
+    int64_t wall_hits;       /* void-wall reflections                            */
+    int64_t crossings;       /* box-to-box transfers                             */
+    int64_t absorbed;        /* particles that reached a reservoir               */
+    int64_t specular_hits;   /* specular reflections (p > 0)                     */
+    int64_t tally_updates;   /* (box, time-bin) contributions made               */
+    double kernel_ms;        /* device time of the particle loop                 */
+} bte_rta_result;
+
+/* Tuning knobs of the production kernels (project-written autotuner picks
+ * them; 0 selects the built-in default). */
+typedef struct bte_tuning {
+    int32_t block_threads;   /* threads per block                              */
+    int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid  */
+    int32_t smem_tally;      /* 1: privatise tallies in shared memory           */
+    int32_t smem_alias;      /* 1: stage the resampling alias table in smem     */
+} bte_tuning;
+
+/* ------------------------------------------------------------------------ */
+
+/* Create a context on a device (replaces the start of main,
+ * src/RTA_MC2D.cpp:2061-2118). */
+bte_status bte_create(bte_ctx** ctx, const bte_device_opts* opts);
+
+/* Release all device memory and the stream of a context. */
+bte_status bte_destroy(bte_ctx* ctx);
+
+/* Copy the last error message of ctx (or of bte_create when ctx is NULL). */
+bte_status bte_last_error(const bte_ctx* ctx, char* buf, size_t size);
+
+/* Load the mode table of the (single) material and build the device tables:
+ * resampling CDF/alias (BE_derivative_distribution, src/sampling.cpp:47-68)
+ * and the energy-conserving Lambert wall table
+ * (generators::diffusive_bouncing, src/RTA_MC2D.cpp:556-626). */
+bte_status bte_load_modes(bte_ctx* ctx, const bte_mode_table* modes);
+
+/* Load the boxes and build borders and contacts (geometry_2d::get_sides and
+ * calculate_contacts, src/geometry_2d.cpp:51-124, :295-381). */
+bte_status bte_load_geometry(bte_ctx* ctx, const bte_geometry* geom);
+
+/* Run the RTA particle loop for one run and fill `out` (replaces one
+ * iteration of the run loop of src/RTA_MC2D.cpp:2188-2543: generation,
+ * the parallel_for over evolparticle, and the post-processing). */
+bte_status bte_rta_run(bte_ctx* ctx, const bte_rta_params* params,
+                       bte_rta_result* out);
+
+/* Set the production-kernel tuning; NULL restores the defaults. */
+bte_status bte_set_tuning(bte_ctx* ctx, const bte_tuning* tuning);
+
+/* Number of modes and boxes loaded; sizes of the result arrays. */
+bte_status bte_query_sizes(const bte_ctx* ctx, const bte_rta_params* params,
+                           int32_t* nboxes, int32_t* nbins, int64_t* nmodes);
+
+/* Library version (BTEGPU_VERSION). */
+int32_t bte_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BTEGPU_H */

@@ -1,0 +1,153 @@
+"""ctypes binding of the CPU restatement (oracle/rta_oracle.cpp).
+
+Test infrastructure: used by tests/, __graft_entry__.smoke() and the
+cpu_baseline leg of bench.py only.
+"""
+import ctypes as C
+import importlib.util
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+
+if "btegpu" in sys.modules:
+    _bt = sys.modules["btegpu"]
+else:  # share the struct definitions of the engine's host module
+    _spec = importlib.util.spec_from_file_location(
+        "btegpu", os.path.join(REPO, "bte-barna_gb300", "btegpu.py"))
+    _bt = importlib.util.module_from_spec(_spec)
+    sys.modules["btegpu"] = _bt
+    _spec.loader.exec_module(_bt)
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    bspec = importlib.util.spec_from_file_location("bte_oracle_build", os.path.join(HERE, "build.py"))
+    bmod = importlib.util.module_from_spec(bspec)
+    bspec.loader.exec_module(bmod)
+    path = bmod.build_oracle()
+    lib = C.CDLL(path)
+    lib.oracle_last_error.restype = C.c_char_p
+    lib.oracle_rta_run.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
+                                   C.POINTER(_bt.RtaParams), C.c_int, C.c_int,
+                                   C.POINTER(_bt.RtaResult), C.POINTER(C.c_int64)]
+    lib.oracle_rta_run.restype = C.c_int
+    lib.oracle_geometry_dump.argtypes = [C.c_void_p, C.POINTER(_bt.Geometry),
+                                         C.POINTER(C.c_double), C.c_longlong]
+    lib.oracle_geometry_dump.restype = C.c_longlong
+    lib.oracle_inter_side.argtypes = [C.POINTER(_bt.Geometry), C.c_int] + [C.c_double] * 5 + [
+        C.POINTER(C.c_double)]
+    lib.oracle_inter_side.restype = C.c_int
+    lib.oracle_pcg64.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
+    lib.oracle_log.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int]
+    lib.oracle_be.argtypes = [C.POINTER(C.c_double), C.c_longlong, C.c_double,
+                              C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.oracle_lambert_nnz.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
+                                       C.POINTER(C.c_longlong)]
+    lib.oracle_timegrid.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int]
+    lib.oracle_timegrid.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def timegrid(dt, maxtime):
+    lib = load()
+    n = lib.oracle_timegrid(dt, maxtime, None, 0)
+    out = np.zeros(n)
+    lib.oracle_timegrid(dt, maxtime, out.ctypes.data_as(C.POINTER(C.c_double)), n)
+    return out
+
+
+def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,
+            source=None, specularity=None):
+    """Run the restatement on a synth case dict; returns arrays and counters."""
+    if source is None:
+        source = _bt.SOURCE_INITIAL if case.get("source") == "initial" else _bt.SOURCE_WALLS
+    if specularity is None:
+        specularity = case.get("specularity", 0.0)
+    lib = load()
+    ms, k1 = _bt.mode_struct(case["modes"])
+    gs, k2 = _bt.geom_struct(case["geom"])
+    N = case["N"] if N is None else N
+    p = _bt.params_struct(case["T0"], case["dt"], case["maxtime"], N, seed, _bt.MODE_REPLAY,
+                          source, ballistic, specularity, begin, end)
+    nbins = int(np.floor(case["maxtime"] / case["dt"] + 1e-6))
+    shape = (int(case["geom"]["nboxes"]), nbins)
+    out = {k: np.zeros(shape) for k in ("gz", "gz_jx", "gz_jy", "temperature", "jx", "jy")}
+    out["exact"] = np.zeros(shape + (3, 2), dtype=np.int64)
+    r = _bt.RtaResult()
+    for k in ("gz", "gz_jx", "gz_jy", "temperature", "jx", "jy"):
+        setattr(r, k, out[k].ctypes.data_as(C.POINTER(C.c_double)))
+    r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
+    cnt = np.zeros(6, dtype=np.int64)
+    st = lib.oracle_rta_run(C.byref(ms), C.byref(gs), C.byref(p), int(nthreads), int(log_impl),
+                            C.byref(r), cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    out.update(Eeff=r.Eeff, energy_rate=r.energy_rate, events=int(cnt[0]), wall_hits=int(cnt[1]),
+               crossings=int(cnt[2]), absorbed=int(cnt[3]), nudges=int(cnt[4]), quirks=int(cnt[5]),
+               specular_hits=int(r.specular_hits))
+    return out
+
+
+def geometry_dump(g: dict) -> np.ndarray:
+    lib = load()
+    gs, keep = _bt.geom_struct(g)
+    n = lib.oracle_geometry_dump(None, C.byref(gs), None, 0)
+    if n < 0:
+        raise _bt.BteError(3, lib.oracle_last_error().decode())
+    out = np.zeros(n)
+    lib.oracle_geometry_dump(None, C.byref(gs), out.ctypes.data_as(C.POINTER(C.c_double)), n)
+    return out
+
+
+def inter_side(g: dict, box, x, y, vx, vy, dt):
+    lib = load()
+    gs, keep = _bt.geom_struct(g)
+    out = np.zeros(12)
+    st = lib.oracle_inter_side(C.byref(gs), box, x, y, vx, vy, dt,
+                               out.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        return None
+    nb = int(out[3])
+    return out[0], (out[1], out[2]), [int(b) for b in out[4:4 + nb]]
+
+
+def pcg64(seed, stream, n, int_hi=6):
+    lib = load()
+    raw = np.zeros(n, dtype=np.uint64)
+    can = np.zeros(n)
+    ints = np.zeros(n, dtype=np.int32)
+    lib.oracle_pcg64(seed, stream, n, raw.ctypes.data_as(C.POINTER(C.c_uint64)),
+                     can.ctypes.data_as(C.POINTER(C.c_double)),
+                     ints.ctypes.data_as(C.POINTER(C.c_int)), int_hi)
+    return raw, can, ints
+
+
+def log(x, impl=0):
+    lib = load()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros_like(x)
+    lib.oracle_log(x.ctypes.data_as(C.POINTER(C.c_double)), y.ctypes.data_as(C.POINTER(C.c_double)),
+                   x.size, impl)
+    return y
+
+
+def lambert_nnz(case: dict) -> np.ndarray:
+    lib = load()
+    ms, k1 = _bt.mode_struct(case["modes"])
+    gs, k2 = _bt.geom_struct(case["geom"])
+    n = int(case["modes"]["nq"]) * int(case["modes"]["nb"])
+    out = np.zeros(n, dtype=np.int64)
+    st = lib.oracle_lambert_nnz(C.byref(ms), C.byref(gs), out.ctypes.data_as(C.POINTER(C.c_longlong)))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    return out

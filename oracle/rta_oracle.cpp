@@ -1,0 +1,1351 @@
+// rta_oracle.cpp - CPU restatement of BTE-Barna's RTAMC2D transient particle
+// loop.  TEST INFRASTRUCTURE ONLY: it is the checker of the GPU engine and the
+// CPU baseline of bench.py; the engine never links or calls it.
+//
+// Parity status: the reference cannot be built here (Boost, TBB, HDF5, MPI and
+// msgpack-c are absent) and its own tests never exercise this path, so the
+// restatement is pinned only at its leaves: pcg64 outputs, the libstdc++
+// uniform mappings and the time grid are checked against golden vectors made
+// by oracle/build_ref.py from the reference's vendored pcg-cpp / Eigen
+// headers.  Geometry (restated without Boost.Geometry) and the table
+// iteration orders are this restatement's own definitions; parity with the
+// reference is unpinned there.
+//
+// What it follows (file:line of the reference):
+//   src/RTA_MC2D.cpp:272-449      generators::Init_generator (isothermal walls)
+//   src/RTA_MC2D.cpp:556-678      generators::diffusive_bouncing (table, bounce)
+//   src/RTA_MC2D.cpp:133-148      get_bin_index
+//   src/RTA_MC2D.cpp:699-769      process_segment (transient)
+//   src/RTA_MC2D.cpp:843-856      get_v
+//   src/RTA_MC2D.cpp:990-1386     evolparticle (transient, single material)
+//   src/RTA_MC2D.cpp:2118-2124    time grid
+//   src/RTA_MC2D.cpp:2262-2316    per-particle flight loop
+//   src/RTA_MC2D.cpp:2326-2435    merge, scaling, cumulative sum, temperature
+//   src/geometry_2d.cpp:51-158    borders (get_sides), hull, inside
+//   src/geometry_2d.cpp:160-293   get_inter_side
+//   src/geometry_2d.cpp:295-406   calculate_contacts, in_corner3
+//   include/geometry_2d.hpp:114-125,524-561  border point, correct_corner_problem
+//   include/sampling.hpp:40-114   random_dt, Grid_distribution::sample*
+//   src/sampling.cpp:26-68,189-269 fill_cumulative, BE_derivative, isothermal wall
+//   include/utilities.hpp:45-49,214-224,385-417  choose, almost_equal, BE functions
+//   include/bulk_properties.hpp:32-47  calc_cv
+//   src/isotopic_scattering.cpp:31-50  calc_percentiles_log
+//
+// Replay contract (shared with the GPU replay mode): particle i owns the
+// stream pcg64(seed, stream = i); every draw of its life (generation, flight
+// times, resampling, bounces, random choices) comes from that stream in the
+// reference's order.  Uniforms are libstdc++'s generate_canonical<double,53>
+// over a 64-bit engine; integers are libstdc++'s uniform_int_distribution
+// (Lemire's nearly-divisionless method).  -log(u) uses bte_log (log_impl 0),
+// written identically in the engine, or glibc's log (log_impl 1).
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../include/btegpu.h"
+
+namespace orc {
+
+// ---------------------------------------------------------------- numerics
+constexpr double kB = 1.3806488e-23;      // include/constants.hpp:37
+constexpr double hbar = 1.054571726e-34;  // include/constants.hpp:47
+constexpr double nsigma = 2.828427124746190097603377448419396157138;
+constexpr double PI = 3.1415926535897932384626433832795028841953;
+
+struct geometry_error : std::runtime_error { using std::runtime_error::runtime_error; };
+struct value_error : std::runtime_error { using std::runtime_error::runtime_error; };
+struct input_error : std::runtime_error { using std::runtime_error::runtime_error; };
+struct limit_error : std::runtime_error { using std::runtime_error::runtime_error; };
+
+inline bool almost_equal(double a, double b, double abstol = 1e-8,
+                         double reltol = 1e-5) {
+    const double tol = std::fabs(abstol) + std::fabs(reltol * b);
+    return std::fabs(a - b) < tol;
+}
+
+inline double bose_einstein(double omega, double T) {
+    constexpr double prefactor = 1e12 * hbar / kB;
+    return 1. / (std::exp(prefactor * omega / T) - 1.);
+}
+
+inline double bose_einstein_kernel(double omega, double T) {
+    constexpr double prefactor = 0.5 * 1e12 * hbar / kB;
+    double x = prefactor * omega / T;
+    if (x < 1e-320) return 1.;
+    if (x > 300.) return 0.;
+    double s = x / std::sinh(x);
+    return s * s;
+}
+
+// Natural log by Cody-Waite reduction x = 2^e m, m in (1/sqrt2, sqrt2], and
+// the series log m = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...), s = (m-1)/(m+1).
+// The engine carries the same function operation for operation, so both give
+// the same bits when neither contracts a*b+c into an FMA.
+inline double bte_log(double x) {
+    if (!(x > 0.)) return x == 0. ? -HUGE_VAL : std::nan("");
+    if (x == HUGE_VAL) return x;
+    uint64_t bits;
+    std::memcpy(&bits, &x, 8);
+    int e = int((bits >> 52) & 0x7ff);
+    if (e == 0) {  // subnormal: scale by 2^54
+        double y = x * 18014398509481984.0;
+        std::memcpy(&bits, &y, 8);
+        e = int((bits >> 52) & 0x7ff) - 54;
+    }
+    e -= 1023;
+    uint64_t mb = (bits & 0x000fffffffffffffULL) | 0x3ff0000000000000ULL;
+    double m;
+    std::memcpy(&m, &mb, 8);
+    if (m > 1.4142135623730951) {
+        m = m * 0.5;
+        e += 1;
+    }
+    const double f = m - 1.0;
+    const double s = f / (2.0 + f);
+    const double z = s * s;
+    double p = 1.0 / 23.0;
+    p = p * z + 1.0 / 21.0;
+    p = p * z + 1.0 / 19.0;
+    p = p * z + 1.0 / 17.0;
+    p = p * z + 1.0 / 15.0;
+    p = p * z + 1.0 / 13.0;
+    p = p * z + 1.0 / 11.0;
+    p = p * z + 1.0 / 9.0;
+    p = p * z + 1.0 / 7.0;
+    p = p * z + 1.0 / 5.0;
+    p = p * z + 1.0 / 3.0;
+    const double two_s = s + s;
+    const double logm = two_s + two_s * z * p;
+    const double de = double(e);
+    const double LN2_HI = 0.6931471787393093;      // ln 2 with 28 significant bits
+    const double LN2_LO = 1.8206359985041462e-09;  // ln 2 - LN2_HI
+    return de * LN2_HI + (de * LN2_LO + logm);
+}
+
+// ---------------------------------------------------------------- pcg64
+// setseq_xsl_rr_128_64 (external/pcg-cpp-0.98/include/pcg_random.hpp:1592,1675)
+struct Pcg64 {
+    using u128 = unsigned __int128;
+    u128 state, inc;
+    static u128 mult() {
+        return (u128(2549297995355413924ULL) << 64) | u128(4865540595714422341ULL);
+    }
+    Pcg64(uint64_t seed, uint64_t stream) {
+        inc = (u128(stream) << 1) | 1u;
+        state = (u128(seed) + inc) * mult() + inc;
+    }
+    uint64_t operator()() {
+        state = state * mult() + inc;
+        unsigned rot = unsigned(state >> 122) & 63u;
+        uint64_t x = uint64_t(state >> 64) ^ uint64_t(state);
+        return rot ? (x >> rot) | (x << ((64 - rot) & 63)) : x;
+    }
+};
+
+// generate_canonical<double, 53> over a 64-bit engine: one draw, x / 2^64,
+// moved below 1 when it rounds up (libstdc++ bits/random.tcc).
+inline double canonical(Pcg64& g) {
+    double u = double(g()) * 0x1p-64;
+    if (u >= 1.0) u = 0x1.fffffffffffffp-1;
+    return u;
+}
+
+// uniform_int_distribution<int>(a, b) over a 64-bit engine (libstdc++
+// bits/uniform_int_dist.h, Lemire 2019).  b < a is an empty range.
+inline int uniform_int(Pcg64& g, int a, int b) {
+    if (b < a) throw geometry_error("random choice from an empty set");
+    using u128 = unsigned __int128;
+    const uint64_t range = uint64_t(int64_t(b)) - uint64_t(int64_t(a)) + 1u;
+    u128 product = u128(g()) * u128(range);
+    uint64_t low = uint64_t(product);
+    if (low < range) {
+        uint64_t threshold = (0 - range) % range;
+        while (low < threshold) {
+            product = u128(g()) * u128(range);
+            low = uint64_t(product);
+        }
+    }
+    return int(uint64_t(product >> 64) + uint64_t(int64_t(a)));
+}
+
+// ---------------------------------------------------------------- geometry
+struct V2 {
+    double x = 0, y = 0;
+};
+inline V2 operator+(V2 a, V2 b) { return {a.x + b.x, a.y + b.y}; }
+inline V2 operator-(V2 a, V2 b) { return {a.x - b.x, a.y - b.y}; }
+inline V2 operator*(double s, V2 a) { return {s * a.x, s * a.y}; }
+inline V2 operator/(V2 a, double s) { return {a.x / s, a.y / s}; }
+inline double dot(V2 a, V2 b) { return a.x * b.x + a.y * b.y; }
+inline double cross(V2 a, V2 b) { return a.x * b.y - a.y * b.x; }
+inline double norm(V2 a) { return std::sqrt(a.x * a.x + a.y * a.y); }
+
+struct Border {
+    V2 p1, p2, nd, np;  // end points, p2 - p1, outward unit normal
+    V2 sa, sb;          // the segment
+    V2 la, lb;          // the segment lengthened at both ends (sbl)
+};
+
+// Point on a segment, including its end points; a degenerate segment is a point.
+inline bool on_segment(V2 p, V2 a, V2 b) {
+    V2 d = b - a;
+    if (d.x == 0. && d.y == 0.) return p.x == a.x && p.y == a.y;
+    if (cross(d, p - a) != 0.) return false;
+    double t = dot(p - a, d);
+    return t >= 0. && t <= dot(d, d);
+}
+
+// Intersection of segments s0-s1 and l0-l1 (parallel segments never meet);
+// the point is taken on l0-l1 so that it lies exactly on axis-aligned borders.
+inline bool seg_intersect(V2 s0, V2 s1, V2 l0, V2 l1, V2& out) {
+    V2 d1 = s1 - s0, d2 = l1 - l0;
+    double den = cross(d1, d2);
+    if (den == 0.) return false;
+    V2 w = l0 - s0;
+    double t = cross(w, d2) / den;
+    double u = cross(w, d1) / den;
+    if (!(t >= 0. && t <= 1. && u >= 0. && u <= 1.)) return false;
+    out = l0 + u * d2;
+    return true;
+}
+
+struct Box {
+    std::vector<V2> hull;  // counter-clockwise convex hull
+    V2 center;
+    double area = 0;
+    std::vector<Border> borders;
+    std::map<std::size_t, std::vector<Border>> contacts;
+    double Teq = -1, Treal = -1;
+    bool reservoir = false;
+    std::size_t id = 0;
+
+    bool inside(V2 p) const {
+        const std::size_t n = hull.size();
+        for (std::size_t i = 0; i < n; ++i) {
+            V2 a = hull[i], b = hull[(i + 1) % n];
+            if (cross(b - a, p - a) < 0.) return false;
+        }
+        return true;
+    }
+};
+
+inline std::vector<V2> convex_hull(std::vector<V2> pts) {
+    std::sort(pts.begin(), pts.end(), [](V2 a, V2 b) {
+        return a.x < b.x || (a.x == b.x && a.y < b.y);
+    });
+    pts.erase(std::unique(pts.begin(), pts.end(),
+                          [](V2 a, V2 b) { return a.x == b.x && a.y == b.y; }),
+              pts.end());
+    if (pts.size() < 3) throw input_error("a box needs three distinct vertices");
+    std::vector<V2> h(2 * pts.size());
+    std::size_t k = 0;
+    for (std::size_t i = 0; i < pts.size(); ++i) {
+        while (k >= 2 && cross(h[k - 1] - h[k - 2], pts[i] - h[k - 2]) <= 0.) --k;
+        h[k++] = pts[i];
+    }
+    for (std::size_t i = pts.size() - 1, t = k + 1; i > 0; --i) {
+        while (k >= t && cross(h[k - 1] - h[k - 2], pts[i - 1] - h[k - 2]) <= 0.) --k;
+        h[k++] = pts[i - 1];
+    }
+    h.resize(k - 1);
+    return h;
+}
+
+// Box from vertices: hull, area, area centroid, borders in the order of
+// geometry_2d::get_sides (pairs i <= j of the input vertices whose midpoint,
+// pushed 1e-4 away from the centre, falls outside the hull).
+inline Box make_box(const std::vector<V2>& verts) {
+    Box b;
+    b.hull = convex_hull(verts);
+    const std::size_t n = b.hull.size();
+    double a2 = 0, cx = 0, cy = 0;
+    V2 o = b.hull[0];
+    for (std::size_t i = 0; i < n; ++i) {
+        V2 p = b.hull[i] - o, q = b.hull[(i + 1) % n] - o;
+        double c = cross(p, q);
+        a2 += c;
+        cx += (p.x + q.x) * c;
+        cy += (p.y + q.y) * c;
+    }
+    b.area = 0.5 * a2;
+    b.center = {o.x + cx / (3. * a2), o.y + cy / (3. * a2)};
+    for (std::size_t i = 0; i < verts.size(); ++i) {
+        V2 p1 = verts[i];
+        for (std::size_t j = i; j < verts.size(); ++j) {
+            V2 p2 = verts[j];
+            if (norm(p1 - p2) < 1.0e-6) continue;
+            V2 sc = {(p1.x + p2.x) / 2., (p1.y + p2.y) / 2.};
+            V2 ncsc = sc - b.center;
+            if (norm(ncsc) == 0.) continue;
+            double nc = 1. / norm(ncsc);
+            ncsc.x *= 1.0e-4 * nc;
+            ncsc.y *= 1.0e-4 * nc;
+            V2 fp = ncsc + sc;
+            if (b.inside(fp)) continue;
+            Border br;
+            br.p1 = p1;
+            br.p2 = p2;
+            br.nd = p2 - p1;
+            V2 npt = {br.nd.y, -br.nd.x};
+            if (dot(npt, ncsc) < 0.) npt = -1. * npt;
+            br.np = npt / norm(npt);
+            br.sa = p1;
+            br.sb = p2;
+            br.la = p1 - 1.0e-6 * br.nd;
+            br.lb = p2 + 1.0e-6 * br.nd;
+            bool dup = false;
+            for (auto& o2 : b.borders)
+                if (norm(o2.np - br.np) < 1.0e-6) dup = true;
+            if (!dup) b.borders.push_back(br);
+            if (b.borders.size() > verts.size())
+                throw geometry_error("To much borders");
+        }
+    }
+    return b;
+}
+
+// Shared boundary of two touching convex boxes: the end points of the
+// overlap of collinear edges, else a shared point.  Returns 0, 1 or 2 points.
+inline std::vector<V2> touching_points(const Box& A, const Box& B) {
+    std::vector<V2> pts;
+    auto add = [&](V2 p) {
+        for (auto& q : pts)
+            if (q.x == p.x && q.y == p.y) return;
+        pts.push_back(p);
+    };
+    const std::size_t na = A.hull.size(), nb = B.hull.size();
+    for (std::size_t i = 0; i < na; ++i) {
+        V2 a0 = A.hull[i], a1 = A.hull[(i + 1) % na];
+        for (std::size_t j = 0; j < nb; ++j) {
+            V2 b0 = B.hull[j], b1 = B.hull[(j + 1) % nb];
+            if (on_segment(b0, a0, a1)) add(b0);
+            if (on_segment(b1, a0, a1)) add(b1);
+            if (on_segment(a0, b0, b1)) add(a0);
+            if (on_segment(a1, b0, b1)) add(a1);
+        }
+    }
+    if (pts.size() > 2) throw geometry_error("overlapping boxes are not supported");
+    std::sort(pts.begin(), pts.end(), [](V2 a, V2 b) {
+        return a.x < b.x || (a.x == b.x && a.y < b.y);
+    });
+    return pts;
+}
+
+inline bool bboxes_meet(const Box& A, const Box& B) {
+    double ax0 = A.hull[0].x, ax1 = ax0, ay0 = A.hull[0].y, ay1 = ay0;
+    for (auto& p : A.hull) {
+        ax0 = std::min(ax0, p.x); ax1 = std::max(ax1, p.x);
+        ay0 = std::min(ay0, p.y); ay1 = std::max(ay1, p.y);
+    }
+    double bx0 = B.hull[0].x, bx1 = bx0, by0 = B.hull[0].y, by1 = by0;
+    for (auto& p : B.hull) {
+        bx0 = std::min(bx0, p.x); bx1 = std::max(bx1, p.x);
+        by0 = std::min(by0, p.y); by1 = std::max(by1, p.y);
+    }
+    return !(bx0 > ax1 || ax0 > bx1 || by0 > ay1 || ay0 > by1);
+}
+
+inline void calculate_contacts(std::vector<Box>& sys) {
+    for (auto& me : sys) {
+        for (auto& other : sys) {
+            if (other.id == me.id) continue;
+            if (!bboxes_meet(me, other)) continue;  // boxes apart cannot touch
+            auto pinter = touching_points(me, other);
+            if (pinter.empty()) continue;
+            Border cb;
+            if (pinter.size() == 1 || norm(pinter[1] - pinter[0]) < 1.0e-6) {
+                cb.p1 = cb.p2 = pinter[0];
+                cb.sa = cb.sb = pinter[0];
+                cb.np = (cb.p1 - me.center) / norm(cb.p1 - me.center);
+                me.contacts[other.id] = {cb};
+                continue;
+            }
+            cb.p1 = pinter[0];
+            cb.p2 = pinter[1];
+            cb.nd = cb.p2 - cb.p1;
+            V2 sc = {(cb.p1.x + cb.p2.x) / 2., (cb.p1.y + cb.p2.y) / 2.};
+            V2 ncsc = sc - me.center;
+            V2 npt = {cb.nd.y, -cb.nd.x};
+            if (dot(npt, ncsc) < 0.) npt = -1. * npt;
+            cb.np = npt / norm(npt);
+            cb.sa = cb.p1;
+            cb.sb = cb.p2;
+            cb.la = cb.p1 - 1.0e-6 * cb.nd / norm(cb.nd);
+            cb.lb = cb.p2 + 1.0e-6 * cb.nd / norm(cb.nd);
+            me.contacts[other.id] = {cb};
+        }
+        if (me.contacts.empty() && sys.size() > 1)
+            throw geometry_error("There are unconnected boxes");
+    }
+}
+
+struct Hit {
+    double time;
+    V2 rf;
+    std::vector<int> bids;
+};
+
+// geometry_2d::get_inter_side, src/geometry_2d.cpp:160-293.
+inline Hit get_inter_side(const Box& box, V2 r0, V2 v, double dt) {
+    V2 pf = {r0.x + dt * v.x, r0.y + dt * v.y};
+    double time = 1.0e+7;
+    V2 rf;
+    std::vector<int> bids;
+    bool already_there = true;
+    int border_id = 0;
+    for (auto& b : box.borders) {
+        V2 rin;
+        if (seg_intersect(r0, pf, b.la, b.lb, rin) && !on_segment(r0, b.la, b.lb)) {
+            if (dot(b.np, v) > 0.) {
+                double tx = (std::fabs(v.x) < 1.0e-6) ? -1 : (rin.x - r0.x) / v.x;
+                double ty = (std::fabs(v.y) < 1.0e-6) ? -1 : (rin.y - r0.y) / v.y;
+                double newtime = std::max(tx, ty);
+                if (newtime == time) bids.push_back(border_id);
+                if (newtime < time) {
+                    bids.clear();
+                    rf = rin;
+                    time = newtime;
+                    already_there = false;
+                    bids.push_back(border_id);
+                }
+            }
+        }
+        border_id++;
+    }
+    if (already_there) {
+        V2 p0p = {r0.x - 1.0e-6 * v.x, r0.y - 1.0e-6 * v.y};
+        border_id = 0;
+        for (auto& b : box.borders) {
+            V2 rin;
+            if (seg_intersect(p0p, pf, b.la, b.lb, rin)) {
+                if (dot(b.np, v) > 0.) {
+                    double tx = (std::fabs(v.x) < 1.0e-6) ? -1.0e+8 : (rin.x - r0.x) / v.x;
+                    double ty = (std::fabs(v.y) < 1.0e-6) ? -1.0e+8 : (rin.y - r0.y) / v.y;
+                    double newtime = std::max(tx, ty);
+                    if (newtime == time) bids.push_back(border_id);
+                    if (std::fabs(newtime) < time) {
+                        bids.clear();
+                        rf = rin;
+                        time = newtime;
+                        bids.push_back(border_id);
+                    }
+                }
+            }
+            border_id++;
+        }
+        if (time > 1.0e+6) throw geometry_error("Error to huge time");
+    }
+    if (almost_equal(time, 0.)) time = 0.;
+    if (time < 0.) throw geometry_error("Bad time");
+    return {time, rf, bids};
+}
+
+// ---------------------------------------------------------------- distributions
+// Grid_distribution::fill_cumulative, src/sampling.cpp:26-44
+inline std::vector<double> fill_cumulative(const std::vector<double>& p) {
+    if (*std::min_element(p.begin(), p.end()) < 0.)
+        throw value_error("probabilities must be >= 0.");
+    std::vector<double> c;
+    c.reserve(p.size());
+    std::partial_sum(p.begin(), p.end(), std::back_inserter(c));
+    double last = c.back();
+    for (auto& x : c) x /= last;
+    return c;
+}
+
+inline std::size_t lower_bound_idx(const std::vector<double>& c, double u) {
+    return std::size_t(std::lower_bound(c.begin(), c.end(), u) - c.begin());
+}
+
+struct Modes {
+    int nq = 0, nb = 0, grid[3] = {0, 0, 0};
+    std::vector<double> omega, vx, vy, vz, w;
+    double dq[9] = {0};
+    double V = 0, c = 0;
+    std::size_t n() const { return std::size_t(nq) * nb; }
+};
+
+struct WallGen {
+    std::size_t res, box;     // reservoir id, injection box id
+    Border b;                 // contact border seen from the reservoir
+    std::vector<double> cdf;  // Isothermal_wall_distribution
+    int sign;
+    double flux;              // J nm^-2 ps^-1 (get_flux)
+};
+
+struct Sim {
+    Modes m;
+    std::vector<Box> sys;
+    double thickness = 0;
+    // run state
+    std::vector<double> timegrid;
+    std::vector<double> resample_cdf;
+    std::vector<std::vector<std::pair<std::size_t, double>>> lambert;  // rows by ascending mode
+    std::vector<WallGen> gens;
+    std::vector<double> gen_cum;  // cumulative generator weights
+    double Eeff = 0, energy = 0;
+    // initial-deviation source (outTref_distribution per box)
+    std::vector<std::size_t> init_box;
+    std::vector<int> init_sign;
+    std::vector<std::vector<double>> init_cdf;
+    std::vector<long long> init_first;
+};
+
+// generators::diffusive_bouncing constructor, src/RTA_MC2D.cpp:556-626, with
+// trivial q-point symmetry (every q is its own class; class 0 is Gamma).
+inline void build_lambert(Sim& S) {
+    const Modes& m = S.m;
+    const std::size_t nq = m.nq, nb = m.nb;
+    std::vector<double> sig(nq * nb);
+    for (std::size_t iq = 0; iq < nq; ++iq)
+        for (std::size_t im = 0; im < nb; ++im) {
+            std::size_t k = iq * nb + im;
+            double v[3] = {m.vx[k], m.vy[k], m.vz[k]};
+            double r[3];
+            for (int j = 0; j < 3; ++j)
+                r[j] = v[0] * m.dq[0 + 3 * j] + v[1] * m.dq[1 + 3 * j] + v[2] * m.dq[2 + 3 * j];
+            sig[k] = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) / std::sqrt(12.);
+        }
+    // calc_percentiles_log, src/isotopic_scattering.cpp:31-50 (column-major
+    // (nb x nq) order, sorted anyway)
+    std::vector<double> ls(sig.size());
+    for (std::size_t k = 0; k < sig.size(); ++k)
+        ls[k] = sig[k] == 0. ? std::numeric_limits<double>::lowest() : std::log(sig[k]);
+    std::sort(ls.begin(), ls.end());
+    const std::size_t N = ls.size();
+    double p25 = ls[25 * N / 100], p75 = ls[75 * N / 100];
+    double lbound = std::exp(p25 - 1.5 * (p75 - p25));
+    for (auto& s : sig)
+        if (s < lbound) s = lbound;
+    S.lambert.assign(nq * nb, {});
+    const double root_two_pi = std::sqrt(2. * PI);
+    // rows are filled in (iq2, im2) order, i.e. by ascending outgoing mode;
+    // threads own disjoint ranges of iq1
+    auto work = [&](std::size_t q0, std::size_t q1) {
+        for (std::size_t iq1 = q0; iq1 < q1; ++iq1)
+            for (std::size_t iq2 = 1; iq2 < nq; ++iq2)
+                for (std::size_t im1 = 0; im1 < nb; ++im1)
+                    for (std::size_t im2 = 0; im2 < nb; ++im2) {
+                        std::size_t k1 = iq1 * nb + im1, k2 = iq2 * nb + im2;
+                        if (almost_equal(0., m.omega[k1]) || almost_equal(0., m.omega[k2]))
+                            continue;
+                        double sigma = std::hypot(sig[k1], sig[k2]);
+                        double delta = std::fabs(m.omega[k1] - m.omega[k2]);
+                        if (delta <= nsigma * sigma) {
+                            double e = delta;
+                            e *= -e;
+                            e /= 2 * sigma * sigma;
+                            double pdf = std::exp(e);
+                            pdf /= sigma * root_two_pi;
+                            S.lambert[k1].push_back({k2, pdf});
+                        }
+                    }
+    };
+    unsigned nt = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t)
+        th.emplace_back(work, 1 + (nq - 1) * t / nt, 1 + (nq - 1) * (t + 1) / nt);
+    for (auto& t : th) t.join();
+}
+
+inline V2 get_v(const Modes& m, std::size_t k) {
+    V2 v = {m.vx[k], m.vy[k]};
+    if (almost_equal(v.x, 0.)) v.x = 0.;
+    if (almost_equal(v.y, 0.)) v.y = 0.;
+    return v;
+}
+
+// diffusive_bouncing::bounce, src/RTA_MC2D.cpp:635-678.  The weights are
+// summed in ascending outgoing-mode order; a cumulative value that repeats
+// keeps the later mode (std::map assignment); a draw above the last
+// cumulative value takes the last mode.
+inline std::size_t bounce(const Sim& S, V2 npout, std::size_t imode, Pcg64& rng) {
+    const auto& tm = S.lambert[imode];
+    std::vector<std::pair<std::size_t, double>> states;
+    double cum = 0.;
+    for (auto& [imf, econ] : tm) {
+        V2 v = get_v(S.m, imf);
+        double vn = -(npout.x * v.x + npout.y * v.y);
+        if (vn < 0. || almost_equal(vn, 0.)) continue;
+        cum += vn * econ;
+        states.push_back({imf, vn * econ});
+    }
+    std::vector<std::pair<double, std::size_t>> st2;
+    double cum2 = 0;
+    for (auto& [imf, tran] : states) {
+        cum2 += tran / cum;
+        if (!st2.empty() && st2.back().first == cum2)
+            st2.back().second = imf;
+        else
+            st2.push_back({cum2, imf});
+    }
+    double s = canonical(rng);
+    if (st2.empty()) throw geometry_error("diffuse wall without outgoing states");
+    auto it = std::lower_bound(st2.begin(), st2.end(), s,
+                               [](const std::pair<double, std::size_t>& a, double x) {
+                                   return a.first < x;
+                               });
+    if (it == st2.end()) --it;
+    return it->second;
+}
+
+// Generators of Init_generator, src/RTA_MC2D.cpp:289-418, in the order
+// (reservoir id, injection box id).
+inline void build_generators(Sim& S, double /*T0*/) {
+    S.gens.clear();
+    const Modes& m = S.m;
+    const double vuc = m.V * S.thickness / m.c;
+    for (auto& s : S.sys) {
+        if (!s.reservoir) continue;
+        for (auto& [c, bv] : s.contacts) {
+            if (S.sys[c].reservoir) continue;
+            const Border& b = bv[0];
+            if (almost_equal(norm(b.p2 - b.p1), 0.)) continue;
+            if (almost_equal(s.Teq, S.sys[c].Teq)) continue;
+            WallGen g;
+            g.res = s.id;
+            g.box = c;
+            g.b = b;
+            const double Tw = s.Teq, Te = S.sys[c].Teq;
+            std::vector<double> pmf(m.n());
+            for (std::size_t k = 0; k < m.n(); ++k) {
+                double vn = b.np.x * m.vx[k] + b.np.y * m.vy[k] + 0. * m.vz[k];
+                if (vn <= 0. || almost_equal(0., m.omega[k]))
+                    pmf[k] = 0.;
+                else
+                    pmf[k] = vn * m.omega[k] *
+                             std::fabs(bose_einstein(m.omega[k], Tw) - bose_einstein(m.omega[k], Te));
+            }
+            double cumulsum = 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+            g.sign = (Tw - Te) >= 0 ? 1 : -1;
+            g.cdf = fill_cumulative(pmf);
+            g.flux = g.sign * (cumulsum / (double(m.nq) * vuc));
+            S.gens.push_back(std::move(g));
+        }
+    }
+    if (S.gens.empty()) throw input_error("no isothermal wall generator (no reservoir with a different Teq)");
+    std::vector<double> ws;
+    double total = 0;
+    for (auto& g : S.gens) {
+        double Lb = norm(g.b.p2 - g.b.p1);
+        double e = std::fabs(g.flux) * Lb * S.thickness;
+        total += e;
+        ws.push_back(e);
+    }
+    double wnorm = std::accumulate(ws.begin(), ws.end(), 0.);
+    double cum = 0;
+    S.gen_cum.clear();
+    for (double w : ws) {
+        cum += w / wnorm;
+        S.gen_cum.push_back(cum);
+    }
+    S.energy = total;
+}
+
+struct Particle {
+    V2 pos;
+    std::size_t q = 0, alpha = 0;
+    int sign = 1;
+    double t = 0;
+    std::size_t box = 0;
+};
+
+struct Tally {
+    std::size_t nboxes = 0, nbins = 0;
+    std::vector<double> gz, jx, jy;
+    std::vector<__int128> ex;  // [box][bin][3]
+    int64_t events = 0, wall_hits = 0, crossings = 0, absorbed = 0, nudges = 0,
+            quirks = 0, specular = 0;
+    void init(std::size_t nbx, std::size_t nbn) {
+        nboxes = nbx;
+        nbins = nbn;
+        gz.assign(nbx * nbn, 0.);
+        jx = gz;
+        jy = gz;
+        ex.assign(nbx * nbn * 3, 0);
+    }
+};
+
+// Fixed-point quantisation of one contribution (scale 2^44, |x| < 2^18).
+inline __int128 quant(double x) {
+    double y = x * 17592186044416.0;  // 2^44
+    if (!(std::fabs(y) < 4611686018427387904.0))  // 2^62
+        throw limit_error("tally contribution out of fixed-point range");
+    return __int128(std::llrint(y));
+}
+
+inline std::size_t bin_index(const std::vector<double>& g, double t) {
+    long k = long(std::lower_bound(g.begin(), g.end(), t) - g.begin()) - 1;
+    long hi = long(g.size()) - 2;
+    return std::size_t(std::clamp(k, 0L, hi));
+}
+
+// process_segment (transient), src/RTA_MC2D.cpp:699-769, without the
+// spectral decomposition.
+inline void process_segment(const Sim& S, Tally& T, std::size_t ibox, double t0,
+                            double t1, int sign, V2 v) {
+    const auto& g = S.timegrid;
+    std::size_t sb = bin_index(g, t0), eb = bin_index(g, t1);
+    double delta_t = t1 - t0;
+    for (std::size_t i = sb; i <= eb; ++i) {
+        double lo = std::max(g[i] - t0, 0.);
+        double hi = std::min(g[i + 1] - t0, delta_t);
+        double contr = double(sign) * std::max(hi - lo, 0.);
+        std::size_t k = ibox * T.nbins + i;
+        T.gz[k] += contr;
+        T.jx[k] += v.x * contr;
+        T.jy[k] += v.y * contr;
+        T.ex[3 * k + 0] += quant(contr);
+        T.ex[3 * k + 1] += quant(v.x * contr);
+        T.ex[3 * k + 2] += quant(v.y * contr);
+    }
+}
+
+struct Opts {
+    bool ballistic = false;
+    int log_impl = 0;
+    double specularity = 0.;  // p of void walls (this engine's extension)
+};
+
+// Specular image of mode k at a wall of outward normal np on the q grid:
+// q mirrored across the wall, same branch; -1 when the wall is not
+// axis-aligned or the image does not carry the reflected velocity.
+inline long long mirror_mode(const Sim& S, V2 np, std::size_t k) {
+    const Modes& m = S.m;
+    const int n1 = m.grid[0], n2 = m.grid[1];
+    if (n1 < 1 || n2 < 1 || std::size_t(n1) * std::size_t(n2) != std::size_t(m.nq)) return -1;
+    const bool ny = (np.x == 0. && std::fabs(np.y) == 1.);
+    const bool nx = (np.y == 0. && std::fabs(np.x) == 1.);
+    if (!nx && !ny) return -1;
+    const int iq = int(k / std::size_t(m.nb)), ib = int(k % std::size_t(m.nb));
+    int i = iq / n2, j = iq % n2;
+    if (ny) j = (n2 - j) % n2;
+    if (nx) i = (n1 - i) % n1;
+    const std::size_t k2 = std::size_t(i * n2 + j) * std::size_t(m.nb) + std::size_t(ib);
+    const V2 a = get_v(m, k), b = get_v(m, k2);
+    const double vn_in = np.x * a.x + np.y * a.y, vn_out = np.x * b.x + np.y * b.y;
+    const double vt_in = nx ? a.y : a.x, vt_out = nx ? b.y : b.x;
+    if (vn_out == -vn_in && vt_out == vt_in && m.omega[k2] > 0.) return (long long)k2;
+    return -1;
+}
+
+// correct_corner_problem, include/geometry_2d.hpp:524-561: the winner box.
+inline std::size_t correct_corner_problem(const Sim& S, V2 rf, V2 v,
+                                          const std::vector<std::size_t>& cand,
+                                          Pcg64& rng) {
+    std::vector<std::size_t> finalist;
+    for (auto c : cand) {
+        int nb = 0;
+        for (auto& b : S.sys[c].borders)
+            if (on_segment(rf, b.la, b.lb) && dot(b.np, v) > 0.) nb++;
+        if (nb <= 1) finalist.push_back(c);
+    }
+    if (finalist.empty()) throw geometry_error("corner without a candidate box");
+    return finalist[std::size_t(uniform_int(rng, 0, int(finalist.size()) - 1))];
+}
+
+// evolparticle (transient, one material), src/RTA_MC2D.cpp:990-1386.
+inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng,
+                         Tally& T, const Opts& o) {
+    const std::size_t nb = S.m.nb;
+    V2 opos = p.pos;
+    const Box& box = S.sys[p.box];
+    if (box.reservoir) {
+        p.q = 0;
+        p.alpha = 0;
+        dt = 0.;
+        T.absorbed++;
+        return;
+    }
+    V2 rnew = {p.pos.x + dt * v.x, p.pos.y + dt * v.y};
+    if (box.inside(rnew)) {
+        p.pos = rnew;
+        process_segment(S, T, p.box, p.t, p.t + dt, p.sign, v);
+        p.t += dt;
+        if (!o.ballistic) {
+            double u = canonical(rng);
+            std::size_t pos = lower_bound_idx(S.resample_cdf, u);
+            p.q = pos / nb;
+            p.alpha = pos % nb;
+        }
+        dt = 0.;
+        return;
+    }
+    Hit mru;
+    try {
+        mru = get_inter_side(box, p.pos, v, dt);
+    } catch (const geometry_error&) {
+        V2 d = box.center - opos;
+        p.pos = p.pos + (1.0e-6 * d) / norm(d);
+        T.nudges++;
+        return;
+    }
+    double left_time = dt - mru.time;
+    double tf = mru.time;
+    if (almost_equal(left_time, 0.)) left_time = 0.;
+    dt = left_time;
+    rnew = mru.rf;
+    V2 reps = rnew + (1.0e-6 * v) / norm(v);
+    std::vector<std::size_t> cboxes;
+    for (auto& [ibc, bb] : box.contacts) cboxes.push_back(ibc);
+    std::vector<std::size_t> pboxes;
+    for (auto test : cboxes) {
+        if (test == p.box) continue;
+        const Border& bc = box.contacts.at(test)[0];
+        double npv = dot(bc.np, v);
+        bool parallel = almost_equal(npv, 0.);
+        bool oriented = npv > 0.;
+        if ((S.sys[test].inside(rnew) || S.sys[test].inside(reps)) && !parallel && oriented)
+            pboxes.push_back(test);
+    }
+    if (pboxes.empty()) {
+        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v);
+        p.t += tf;
+        // in_corner3, src/geometry_2d.cpp:388-406
+        std::vector<std::size_t> ids;
+        for (auto& g : S.sys)
+            if (g.inside(rnew)) ids.push_back(g.id);
+        if (ids.size() > 2) {
+            p.box = correct_corner_problem(S, rnew, v, ids, rng);
+            V2 corr = S.sys[p.box].center - rnew;
+            V2 cpos = rnew + (1.0e-6 * corr) / norm(corr);
+            mru = get_inter_side(S.sys[p.box], cpos, v, 1.0e+18);
+            rnew = mru.rf;
+        }
+        const Box& cur = S.sys[p.box];
+        std::size_t iborder;
+        if (mru.bids.size() > 1) {
+            std::vector<std::size_t> voidborders;
+            for (int tvb : mru.bids) {
+                const Border& mb = cur.borders[std::size_t(tvb)];
+                V2 rc = rnew + 1.0e-4 * mb.np;
+                bool isvoid = true;
+                for (auto cb : cboxes)
+                    if (S.sys[cb].inside(rc)) {
+                        isvoid = false;
+                        break;
+                    }
+                if (isvoid) voidborders.push_back(std::size_t(tvb));
+            }
+            if (voidborders.empty()) throw geometry_error("Error in void borders");
+            // uniform_int_distribution(0, size) has an inclusive upper bound;
+            // the reference then reads one past the end.  Counted and clamped.
+            int idx = uniform_int(rng, 0, int(voidborders.size()));
+            if (std::size_t(idx) == voidborders.size()) {
+                T.quirks++;
+                idx--;
+            }
+            iborder = voidborders[std::size_t(idx)];
+        } else {
+            iborder = std::size_t(mru.bids.at(0));
+        }
+        V2 u = cur.borders[iborder].np;
+        const std::size_t k0 = p.q * nb + p.alpha;
+        long long nmm = -1;
+        if (o.specularity > 0.) {
+            if (canonical(rng) < o.specularity) {
+                nmm = mirror_mode(S, u, k0);
+                if (nmm >= 0) T.specular++;
+            }
+        }
+        std::size_t nm = nmm >= 0 ? std::size_t(nmm) : bounce(S, u, k0, rng);
+        p.pos = rnew;
+        p.q = nm / nb;
+        p.alpha = nm % nb;
+        dt = 0.;
+        T.wall_hits++;
+        return;
+    } else if (pboxes.size() == 1) {
+        p.pos = rnew;
+        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v);
+        p.t += tf;
+        p.box = pboxes[0];
+        T.crossings++;
+        return;
+    } else {
+        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v);
+        p.t += tf;
+        p.pos = rnew;
+        std::vector<std::size_t> pbox2;
+        V2 rcheck = rnew + 1.0e-6 * v;
+        for (auto PB : pboxes)
+            if (S.sys[PB].inside(rcheck)) pbox2.push_back(PB);
+        std::size_t newid;
+        if (pbox2.empty()) {
+            newid = pboxes[std::size_t(uniform_int(rng, 0, int(pboxes.size()) - 1))];
+            V2 d = S.sys[newid].center - rnew;
+            p.pos = p.pos + (1.0e-6 * d) / norm(d);
+        } else {
+            newid = pbox2[std::size_t(uniform_int(rng, 0, int(pbox2.size()) - 1))];
+        }
+        p.box = newid;
+        T.crossings++;
+        return;
+    }
+}
+
+// One particle of Init_generator (walls), src/RTA_MC2D.cpp:421-511.
+inline Particle generate(const Sim& S, Pcg64& rng) {
+    const std::size_t nb = S.m.nb;
+    double selectGenR = canonical(rng);
+    (void)selectGenR;  // ExGen = {1, 1} without a gradient: always walls
+    double whereGenR = canonical(rng);
+    auto it = std::lower_bound(S.gen_cum.begin(), S.gen_cum.end(), whereGenR);
+    if (it == S.gen_cum.end()) --it;
+    const WallGen& G = S.gens[std::size_t(it - S.gen_cum.begin())];
+    V2 ppos;
+    for (int tries = 0;; ++tries) {
+        if (tries > 1000) throw limit_error("border point rejection loop");
+        ppos = G.b.p1 + canonical(rng) * G.b.nd;
+        if (on_segment(ppos, G.b.sa, G.b.sb)) break;
+    }
+    const Box& inj = S.sys[G.box];
+    if (!inj.inside(ppos)) {
+        V2 d = inj.center - ppos;
+        ppos = ppos + (1.0e-6 * d) / norm(d);
+        if (!inj.inside(ppos)) throw geometry_error("Generated particle out of insertion box");
+    }
+    double u = canonical(rng);
+    std::size_t pos = lower_bound_idx(G.cdf, u);
+    Particle p;
+    p.pos = ppos;
+    p.q = pos / nb;
+    p.alpha = pos % nb;
+    p.sign = G.sign;
+    p.t = 0.;
+    p.box = G.box;
+    return p;
+}
+
+// Initial deviation Tinit - Teq of each box (init_particles,
+// src/beyondRTA_MC2d.cpp:211-269, with outTref_distribution,
+// src/sampling.cpp:271-330): particle pid belongs to the box whose prefix
+// range holds it; uniform position by bounding-box rejection
+// (geometry_2d::get_random_point, include/geometry_2d.hpp:338-356).
+inline Particle generate_initial(const Sim& S, std::size_t pid, Pcg64& rng) {
+    auto it = std::upper_bound(S.init_first.begin(), S.init_first.end(), (long long)pid);
+    const std::size_t g = std::size_t(it - S.init_first.begin()) - 1;
+    const Box& B = S.sys[S.init_box[g]];
+    double x0 = B.hull[0].x, x1 = B.hull[0].x, y0 = B.hull[0].y, y1 = B.hull[0].y;
+    for (auto& h : B.hull) {
+        x0 = std::min(x0, h.x);
+        x1 = std::max(x1, h.x);
+        y0 = std::min(y0, h.y);
+        y1 = std::max(y1, h.y);
+    }
+    V2 r;
+    for (int tries = 0;; ++tries) {
+        if (tries > 100000) throw limit_error("random point rejection loop");
+        r.x = x0 + canonical(rng) * (x1 - x0);
+        r.y = y0 + canonical(rng) * (y1 - y0);
+        if (B.inside(r)) break;
+    }
+    const double u = canonical(rng);
+    const std::size_t pos = lower_bound_idx(S.init_cdf[g], u);
+    Particle p;
+    p.pos = r;
+    p.q = pos / S.m.nb;
+    p.alpha = pos % S.m.nb;
+    p.sign = S.init_sign[g];
+    p.t = 0.;
+    p.box = S.init_box[g];
+    return p;
+}
+
+inline void build_initial(Sim& S, int64_t nparticles, uint64_t seed) {
+    const Modes& m = S.m;
+    const double vuc = m.V * S.thickness / m.c;
+    std::vector<double> pmf(m.n()), energy;
+    for (auto& s : S.sys) {
+        if (s.reservoir) continue;
+        if (almost_equal(s.Teq, s.Treal)) continue;
+        if (s.Treal <= 0 || s.Teq <= 0) throw value_error("Invalid temperature value");
+        for (std::size_t k = 0; k < m.n(); ++k) {
+            const double om = m.omega[k];
+            pmf[k] = almost_equal(om, 0.)
+                         ? 0.
+                         : om * std::fabs(bose_einstein(om, s.Treal) - bose_einstein(om, s.Teq));
+        }
+        const double cumulsum = 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+        const double vol = s.area * S.thickness / vuc;
+        S.init_box.push_back(s.id);
+        S.init_sign.push_back((s.Treal - s.Teq) >= 0 ? 1 : -1);
+        S.init_cdf.push_back(fill_cumulative(pmf));
+        energy.push_back(vol * cumulsum / double(m.nq));
+    }
+    if (S.init_box.empty()) throw input_error("no box with Tinit different from Teq");
+    double total = 0;
+    for (double e : energy) total += e;
+    S.energy = total;
+    S.Eeff = total / double(nparticles);
+    long long first = 0;
+    for (std::size_t b = 0; b < S.init_box.size(); ++b) {
+        S.init_first.push_back(first);
+        const double gen = energy[b] / S.Eeff;
+        long long np = (long long)gen;
+        const double rem = gen - std::floor(gen);
+        Pcg64 r(seed, (uint64_t(1) << 63) + uint64_t(S.init_box[b]));
+        if (canonical(r) <= rem) np++;
+        first += np;
+    }
+    S.init_first.push_back(first);
+}
+
+inline void run_particle(const Sim& S, std::size_t pid, uint64_t seed, double maxtime,
+                         Tally& T, const Opts& o) {
+    Pcg64 rng(seed, pid);
+    Particle p = S.init_first.empty() ? generate(S, rng) : generate_initial(S, pid, rng);
+    const std::size_t nb = S.m.nb;
+    double time = 0.;
+    while (time < maxtime) {
+        std::size_t k = p.q * nb + p.alpha;
+        V2 v = get_v(S.m, k);
+        double w = S.m.w[k];
+        if (w == 0.) throw value_error("invalid scattering rate");
+        double u = canonical(rng);
+        double dt_ = -(o.log_impl == 0 ? bte_log(u) : std::log(u)) / w;
+        T.events++;
+        if (time + dt_ > maxtime) dt_ = maxtime - time + 1.0e-8;
+        int guard = 0;
+        while (!almost_equal(dt_, 0.)) {
+            if (++guard > 1000000) throw limit_error("flight step cap");
+            evolparticle(S, p, v, dt_, rng, T, o);
+        }
+        if (p.q == 0 && p.alpha == 0) break;
+        time = p.t;
+    }
+}
+
+}  // namespace orc
+
+// ---------------------------------------------------------------- C API
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const char* what) {
+    g_err = what;
+    return code;
+}
+
+orc::Sim build_sim(const bte_mode_table* mt, const bte_geometry* gm) {
+    orc::Sim S;
+    S.m.nq = mt->nq;
+    S.m.nb = mt->nb;
+    const std::size_t n = std::size_t(mt->nq) * mt->nb;
+    S.m.omega.assign(mt->omega, mt->omega + n);
+    S.m.w.assign(mt->w, mt->w + n);
+    S.m.vx.resize(n);
+    S.m.vy.resize(n);
+    S.m.vz.resize(n);
+    for (std::size_t k = 0; k < n; ++k) {
+        S.m.vx[k] = mt->vg[3 * k];
+        S.m.vy[k] = mt->vg[3 * k + 1];
+        S.m.vz[k] = mt->vg[3 * k + 2];
+    }
+    std::memcpy(S.m.dq, mt->dq, sizeof(S.m.dq));
+    S.m.V = mt->V;
+    S.m.c = mt->c_lat;
+    for (int i = 0; i < 3; ++i) S.m.grid[i] = mt->grid[i];
+    S.thickness = gm->thickness;
+    std::size_t off = 0;
+    for (int i = 0; i < gm->nboxes; ++i) {
+        std::vector<orc::V2> verts;
+        for (int j = 0; j < gm->npoints[i]; ++j, ++off)
+            verts.push_back({gm->vertices[2 * off], gm->vertices[2 * off + 1]});
+        orc::Box b = orc::make_box(verts);
+        b.Teq = gm->Teq[i];
+        b.Treal = gm->Tinit ? gm->Tinit[i] : gm->Teq[i];
+        b.reservoir = gm->reservoir[i] != 0;
+        b.id = std::size_t(i);
+        S.sys.push_back(std::move(b));
+    }
+    orc::calculate_contacts(S.sys);
+    return S;
+}
+}  // namespace
+
+extern "C" {
+
+const char* oracle_last_error() { return g_err.c_str(); }
+
+// Borders and contacts of every box, for geometry known-answer tests.
+// Writes per box: nborders, then (p1x p1y p2x p2y npx npy) per border; then
+// ncontacts, then (id npx npy) per contact.  Returns doubles written.
+long long oracle_geometry_dump(const bte_mode_table* /*unused*/, const bte_geometry* gm,
+                               double* out, long long cap) {
+    try {
+        bte_mode_table dummy{};
+        (void)dummy;
+        orc::Sim S;
+        std::size_t off = 0;
+        for (int i = 0; i < gm->nboxes; ++i) {
+            std::vector<orc::V2> verts;
+            for (int j = 0; j < gm->npoints[i]; ++j, ++off)
+                verts.push_back({gm->vertices[2 * off], gm->vertices[2 * off + 1]});
+            orc::Box b = orc::make_box(verts);
+            b.id = std::size_t(i);
+            b.reservoir = gm->reservoir[i] != 0;
+            S.sys.push_back(std::move(b));
+        }
+        orc::calculate_contacts(S.sys);
+        long long k = 0;
+        auto put = [&](double x) {
+            if (k < cap) out[k] = x;
+            k++;
+        };
+        for (auto& b : S.sys) {
+            put(double(b.borders.size()));
+            for (auto& br : b.borders) {
+                put(br.p1.x); put(br.p1.y); put(br.p2.x); put(br.p2.y);
+                put(br.np.x); put(br.np.y);
+            }
+            put(double(b.contacts.size()));
+            for (auto& [id, cv] : b.contacts) {
+                put(double(id)); put(cv[0].np.x); put(cv[0].np.y);
+            }
+            put(b.center.x); put(b.center.y); put(b.area);
+        }
+        return k;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+// get_inter_side on box `ibox`: writes (time, rx, ry, nbids, bids...).
+int oracle_inter_side(const bte_geometry* gm, int ibox, double x, double y, double vx,
+                      double vy, double dt, double* out) {
+    try {
+        std::vector<orc::Box> sys;
+        std::size_t off = 0;
+        for (int i = 0; i < gm->nboxes; ++i) {
+            std::vector<orc::V2> verts;
+            for (int j = 0; j < gm->npoints[i]; ++j, ++off)
+                verts.push_back({gm->vertices[2 * off], gm->vertices[2 * off + 1]});
+            sys.push_back(orc::make_box(verts));
+        }
+        orc::Hit h = orc::get_inter_side(sys.at(std::size_t(ibox)), {x, y}, {vx, vy}, dt);
+        out[0] = h.time;
+        out[1] = h.rf.x;
+        out[2] = h.rf.y;
+        out[3] = double(h.bids.size());
+        for (std::size_t i = 0; i < h.bids.size() && i < 8; ++i) out[4 + i] = h.bids[i];
+        return 0;
+    } catch (const orc::geometry_error& e) {
+        g_err = e.what();
+        return BTE_ERR_GEOMETRY;
+    }
+}
+
+// pcg64 outputs and the libstdc++ mappings, for the golden-vector tests.
+void oracle_pcg64(uint64_t seed, uint64_t stream, int n, uint64_t* raw, double* canon,
+                  int* ints, int int_hi) {
+    orc::Pcg64 a(seed, stream), b(seed, stream), c(seed, stream);
+    for (int i = 0; i < n; ++i) {
+        raw[i] = a();
+        canon[i] = orc::canonical(b);
+        ints[i] = orc::uniform_int(c, 0, int_hi);
+    }
+}
+
+// The time grid of src/RTA_MC2D.cpp:2118-2124 (Eigen LinSpaced); returns ntime.
+int oracle_timegrid(double dt, double maxtime_in, double* out, int cap) {
+    std::size_t ntime = std::size_t(std::floor(maxtime_in / dt + 1.0e-6)) + 1;
+    double maxtime = double(ntime - 1) * dt;
+    double step = (maxtime - 0.0) / double(ntime - 1);
+    for (std::size_t i = 0; i < ntime && int(i) < cap; ++i)
+        out[i] = (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
+    return int(ntime);
+}
+
+void oracle_log(const double* x, double* y, long long n, int impl) {
+    for (long long i = 0; i < n; ++i) y[i] = impl == 0 ? orc::bte_log(x[i]) : std::log(x[i]);
+}
+
+void oracle_be(const double* omega, long long n, double T, double* be, double* kern) {
+    for (long long i = 0; i < n; ++i) {
+        be[i] = orc::bose_einstein(omega[i], T);
+        kern[i] = orc::bose_einstein_kernel(omega[i], T);
+    }
+}
+
+// Lambert table row sizes (for the table-equality tests): nnz per mode.
+int oracle_lambert_nnz(const bte_mode_table* mt, const bte_geometry* gm, long long* nnz) {
+    try {
+        orc::Sim S = build_sim(mt, gm);
+        orc::build_lambert(S);
+        for (std::size_t k = 0; k < S.lambert.size(); ++k) nnz[k] = (long long)S.lambert[k].size();
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_INPUT, e.what());
+    }
+}
+
+// One RTA run (walls source) over particles [begin, end) on `nthreads` host
+// threads (1 gives the reference's per-particle order of summation).
+// counters: events, wall_hits, crossings, absorbed, nudges, quirks.
+int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_rta_params* rp,
+                   int nthreads, int log_impl, bte_rta_result* out, int64_t* counters) {
+    try {
+        orc::Sim S = build_sim(mt, gm);
+        // time grid (src/RTA_MC2D.cpp:2118-2124), Eigen LinSpaced(low + i*step)
+        std::size_t ntime = std::size_t(std::floor(rp->maxtime / rp->dt + 1.0e-6)) + 1;
+        double maxtime = double(ntime - 1) * rp->dt;
+        S.timegrid.resize(ntime);
+        double step = (maxtime - 0.0) / double(ntime - 1);
+        for (std::size_t i = 0; i < ntime; ++i)
+            S.timegrid[i] = (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
+        // resampling distribution (BE_derivative_distribution)
+        std::vector<double> pmf(S.m.n());
+        for (std::size_t k = 0; k < S.m.n(); ++k)
+            pmf[k] = S.m.omega[k] <= 0. ? 0. : orc::bose_einstein_kernel(S.m.omega[k], rp->T0) * S.m.w[k];
+        S.resample_cdf = orc::fill_cumulative(pmf);
+        orc::build_lambert(S);
+        int64_t total_particles = rp->nparticles;
+        if (rp->source == BTE_SOURCE_WALLS) {
+            orc::build_generators(S, rp->T0);
+            S.Eeff = S.energy / double(rp->nparticles);
+        } else {
+            orc::build_initial(S, rp->nparticles, rp->seed);
+            total_particles = S.init_first.back();
+        }
+        orc::Opts o;
+        o.ballistic = rp->ballistic != 0;
+        o.log_impl = log_impl;
+        o.specularity = rp->specularity;
+        const std::size_t nbx = S.sys.size(), nbn = ntime - 1;
+        int64_t begin = rp->particle_begin,
+                end = rp->particle_end > 0 ? std::min<int64_t>(rp->particle_end, total_particles) : total_particles;
+        if (end < begin) end = begin;
+        if (nthreads < 1) nthreads = 1;
+        std::vector<orc::Tally> tl(static_cast<std::size_t>(nthreads));
+        std::vector<std::string> errs(static_cast<std::size_t>(nthreads));
+        std::vector<int> codes(static_cast<std::size_t>(nthreads), 0);
+        auto work = [&](int tid) {
+            orc::Tally& T = tl[std::size_t(tid)];
+            T.init(nbx, nbn);
+            int64_t n = end - begin;
+            int64_t lo = begin + n * tid / nthreads, hi = begin + n * (tid + 1) / nthreads;
+            try {
+                for (int64_t i = lo; i < hi; ++i)
+                    orc::run_particle(S, std::size_t(i), rp->seed, maxtime, T, o);
+            } catch (const orc::value_error& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_VALUE;
+            } catch (const orc::limit_error& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_LIMIT;
+            } catch (const orc::input_error& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_INPUT;
+            } catch (const std::exception& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_GEOMETRY;
+            }
+        };
+        if (nthreads == 1) {
+            work(0);
+        } else {
+            std::vector<std::thread> th;
+            for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+            for (auto& t : th) t.join();
+        }
+        for (std::size_t t = 0; t < errs.size(); ++t)
+            if (!errs[t].empty()) return fail(codes[t], errs[t].c_str());
+        orc::Tally T = std::move(tl[0]);
+        for (std::size_t t = 1; t < tl.size(); ++t) {
+            for (std::size_t k = 0; k < T.gz.size(); ++k) {
+                T.gz[k] += tl[t].gz[k];
+                T.jx[k] += tl[t].jx[k];
+                T.jy[k] += tl[t].jy[k];
+            }
+            for (std::size_t k = 0; k < T.ex.size(); ++k) T.ex[k] += tl[t].ex[k];
+            T.events += tl[t].events;
+            T.wall_hits += tl[t].wall_hits;
+            T.crossings += tl[t].crossings;
+            T.absorbed += tl[t].absorbed;
+            T.nudges += tl[t].nudges;
+            T.quirks += tl[t].quirks;
+            T.specular += tl[t].specular;
+        }
+        out->nboxes = int32_t(nbx);
+        out->nbins = int32_t(nbn);
+        out->Eeff = S.Eeff;
+        out->energy_rate = S.energy;
+        out->events = T.events;
+        out->wall_hits = T.wall_hits;
+        out->crossings = T.crossings;
+        out->absorbed = T.absorbed;
+        out->specular_hits = T.specular;
+        out->tally_updates = 0;
+        if (counters) {
+            counters[0] = T.events; counters[1] = T.wall_hits; counters[2] = T.crossings;
+            counters[3] = T.absorbed; counters[4] = T.nudges; counters[5] = T.quirks;
+        }
+        const std::size_t nk = nbx * nbn;
+        if (out->gz) std::copy(T.gz.begin(), T.gz.end(), out->gz);
+        if (out->gz_jx) std::copy(T.jx.begin(), T.jx.end(), out->gz_jx);
+        if (out->gz_jy) std::copy(T.jy.begin(), T.jy.end(), out->gz_jy);
+        if (out->exact)
+            for (std::size_t k = 0; k < nk * 3; ++k) {
+                unsigned __int128 u = (unsigned __int128)T.ex[k];
+                out->exact[2 * k] = int64_t(uint64_t(u >> 64));
+                out->exact[2 * k + 1] = int64_t(uint64_t(u));
+            }
+        // post-processing, src/RTA_MC2D.cpp:2336-2435
+        std::vector<double> gz = T.gz, jx = T.jx, jy = T.jy;
+        for (std::size_t ir = 0; ir < nbx; ++ir) {
+            double vbox = S.sys[ir].area * S.thickness;
+            for (std::size_t i = 0; i < nbn; ++i) {
+                gz[ir * nbn + i] /= vbox;
+                jx[ir * nbn + i] /= vbox;
+                jy[ir * nbn + i] /= vbox;
+            }
+        }
+        for (auto& x : gz) x *= S.Eeff;
+        for (auto& x : jx) x *= S.Eeff * 1e12 * 1e9 * 1e9;
+        for (auto& x : jy) x *= S.Eeff * 1e12 * 1e9 * 1e9;
+        if (rp->source == BTE_SOURCE_WALLS) {
+            for (std::size_t ir = 0; ir < nbx; ++ir)
+                for (std::size_t i = 1; i < nbn; ++i) {
+                    gz[ir * nbn + i] += gz[ir * nbn + i - 1];
+                    jx[ir * nbn + i] += jx[ir * nbn + i - 1];
+                    jy[ir * nbn + i] += jy[ir * nbn + i - 1];
+                }
+        } else {  // relaxation of an initial deviation: bin averages
+            for (std::size_t k = 0; k < nk; ++k) {
+                gz[k] /= step;
+                jx[k] /= step;
+                jy[k] /= step;
+            }
+        }
+        double cv = 0.;
+        for (std::size_t k = 0; k < S.m.n(); ++k) cv += orc::bose_einstein_kernel(S.m.omega[k], rp->T0);
+        cv *= orc::kB / double(S.m.nq) / S.m.V;
+        double vcorr = S.thickness / S.m.c;
+        if (out->temperature)
+            for (std::size_t k = 0; k < nk; ++k) out->temperature[k] = gz[k] / (cv / vcorr) + rp->T0;
+        if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
+        if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
+        return 0;
+    } catch (const orc::input_error& e) {
+        return fail(BTE_ERR_INPUT, e.what());
+    } catch (const orc::value_error& e) {
+        return fail(BTE_ERR_VALUE, e.what());
+    } catch (const orc::limit_error& e) {
+        return fail(BTE_ERR_LIMIT, e.what());
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
+}  // extern "C"
