@@ -20,6 +20,7 @@ constexpr int MAXB = 16;        // borders per box
 constexpr int MAXC = 32;        // candidate boxes at one crossing
 constexpr int FLIGHT_CAP = 1 << 20;  // evolparticle calls per free flight
 constexpr int NUDGE_CAP = 64;   // consecutive geometry nudges
+constexpr long long EVENT_CAP = 1ll << 26;  // free flights per particle
 
 // Error codes written to the device error word (bte_status values).
 constexpr int E_VALUE = 2, E_GEOM = 3, E_LIMIT = 4;
@@ -434,7 +435,9 @@ __device__ int run_particle(const DevTables& T, P& pol, long long pid, Counters&
     if (e) return e;
     double time = 0.;
     int nudges = 0;
+    long long nev = 0;
     while (time < T.maxtime) {
+        if (++nev > EVENT_CAP) return E_LIMIT;
         const int k = p.mode;
         const V2 v = v2(T.vxc[k], T.vyc[k]);
         const double w = T.w[k];

@@ -245,6 +245,7 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
     GridParticle p;
     Philox g;
     long long pid = -1;
+    long long nev = 0;
     bool active = false, done = false;
     double time = 0.;
     const long long total = T.pend - T.pbegin;
@@ -268,6 +269,7 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
                     } else {
                         active = true;
                         time = 0.;
+                        nev = 0;
                     }
                 } else {
                     done = true;
@@ -281,6 +283,13 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
         const ModeVel mv = A.mv[k];
         double dt = double(-__logf(g.uniformf())) * __ldg(T.tau + k);
         c.events++;
+        if (!(dt > 0.) || ++nev > EVENT_CAP) {  // zero rate or runaway particle
+            record_error(err, dt > 0. ? E_LIMIT : E_VALUE, pid);
+            active = false;
+            done = true;
+            pd.flush(tally);
+            continue;
+        }
         if (time + dt > T.maxtime) dt = T.maxtime - time;
         bool alive = true;
         for (int guard = 0;; ++guard) {

@@ -1006,7 +1006,9 @@ inline void run_particle(const Sim& S, std::size_t pid, uint64_t seed, double ma
     Particle p = S.init_first.empty() ? generate(S, rng) : generate_initial(S, pid, rng);
     const std::size_t nb = S.m.nb;
     double time = 0.;
+    long long nev = 0;
     while (time < maxtime) {
+        if (++nev > (1ll << 26)) throw limit_error("free flights per particle cap");
         std::size_t k = p.q * nb + p.alpha;
         V2 v = get_v(S.m, k);
         double w = S.m.w[k];
