@@ -48,7 +48,7 @@ struct ProdPolicy {
     __device__ double u() { return g.uniform(); }
     __device__ int choose(int n) { return uniform_below(g, uint32_t(n)); }
     __device__ double flight(const DevTables& T, int k) {
-        return double(-__logf(g.uniformf())) * __ldg(T.tau + k);
+        return double(-logf(g.uniformf())) * __ldg(T.tau + k);
     }
     __device__ int resample(const DevTables& T) {
         return alias_draw(g, T.resample_prob, T.resample_alt, T.n);
@@ -281,7 +281,8 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
         // one free flight
         const int k = p.mode;
         const ModeVel mv = A.mv[k];
-        double dt = double(-__logf(g.uniformf())) * __ldg(T.tau + k);
+        // u in (0, 1 - 2^-25]: logf keeps -log(u) > 0 down to u's last step
+        double dt = double(-logf(g.uniformf())) * __ldg(T.tau + k);
         c.events++;
         if (!(dt > 0.) || ++nev > EVENT_CAP) {  // zero rate or runaway particle
             record_error(err, dt > 0. ? E_LIMIT : E_VALUE, pid);

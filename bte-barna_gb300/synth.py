@@ -157,10 +157,10 @@ def write_geometry_xml(path: str, geom: dict, material: str = "synthetic") -> No
         lines.append(f'        <Vertices dim="2" npoints="{n}">')
         for k in range(n):
             x, y = geom["vertices"][2 * (off + k)], geom["vertices"][2 * (off + k) + 1]
-            lines.append(f"           {x!r} {y!r}")
+            lines.append(f"           {float(x)!r} {float(y)!r}")
         lines.append("        </Vertices>")
         off += n
-        teq, tin = geom["Teq"][i], geom["Tinit"][i]
+        teq, tin = float(geom["Teq"][i]), float(geom["Tinit"][i])
         if tin != teq:
             lines.append(f'        <initCnd Teq="{teq!r}" Tinit="{tin!r}"/>')
         else:
