@@ -172,8 +172,10 @@ struct Philox {
         uint64_t h = next32();
         return (h << 32) | next32();
     }
-    // Uniform in (0, 1) with 24 bits, for the single-precision -log(u).
-    BTE_HD float uniformf() { return (float(next32() >> 8) + 0.5f) * 0x1p-24f; }
+    // Uniform in [2^-24, 1 - 2^-24] on a 2^-23 lattice, for the
+    // single-precision -log(u): (k + 1/2) 2^-23 is exact in FP32 for every
+    // 23-bit k, so u never rounds to 0 or 1.
+    BTE_HD float uniformf() { return (float(next32() >> 9) + 0.5f) * 0x1p-23f; }
     // Uniform in [0, 1) with 53 bits.
     BTE_HD double uniform() { return u64_to_double(next() >> 11) * 0x1p-53; }
 };
