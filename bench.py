@@ -157,16 +157,14 @@ def profile_traffic():
 def cpu_sample(c, seconds, nthreads, seed=7, offset=0):
     """Time the restatement on a bounded slice of the workload's particles."""
     import pyoracle
-    # calibrate on a small slice, then size the sample to ~`seconds`
+    # calibrate on a small slice, then size the sample to ~`seconds` of the
+    # particle loop (the restatement times its loop without table set-up)
     probe = 64 * nthreads
-    t0 = time.perf_counter()
     r = pyoracle.rta_run(c, N=c["N"], seed=seed, nthreads=nthreads, begin=offset, end=offset + probe)
-    dt = time.perf_counter() - t0
+    dt = r["loop_seconds"]
     n = int(max(probe, min(probe * seconds / max(dt, 1e-3), 50_000_000)))
-    t0 = time.perf_counter()
     r = pyoracle.rta_run(c, N=c["N"], seed=seed, nthreads=nthreads, begin=offset, end=offset + n)
-    dt = time.perf_counter() - t0
-    return r["events"], dt, n
+    return r["events"], r["loop_seconds"], n
 
 
 def reference_arm(args, c, rank, world):
@@ -182,10 +180,8 @@ def reference_arm(args, c, rank, world):
     off = 0
     for i in range(args.warmup + args.steps):
         if per_step:
-            t0 = time.perf_counter()
             r = pyoracle.rta_run(c, N=c["N"], seed=11, nthreads=nthreads, begin=off, end=off + per_step)
-            dt = time.perf_counter() - t0
-            ev, n = r["events"], per_step
+            ev, dt, n = r["events"], r["loop_seconds"], per_step
         else:
             ev, dt, n = cpu_sample(c, secs, nthreads, seed=11, offset=off)
         off += n
@@ -233,8 +229,11 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     def step(k, seed):
-        # each rank carries its own slice of particles (weak scaling)
-        base = (k * world + rank) * per_step
+        # each rank carries its own slice of particles (weak scaling); when a
+        # step is the whole run (N == per_step) every step reruns it with a
+        # new seed
+        span = max(c["N"] - per_step + 1, 1)
+        base = ((k * world + rank) * per_step) % span
         return eng.rta_run(c["T0"], c["dt"], c["maxtime"], c["N"], seed=seed,
                            mode=btegpu.MODE_PRODUCTION, source=src,
                            specularity=c["specularity"], begin=base, end=base + per_step,

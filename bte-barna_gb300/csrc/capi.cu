@@ -114,8 +114,8 @@ void ensure_static(bte_ctx* c) {
             tau[k] = m.w[k] > 0. ? 1.0 / m.w[k] : 0.;
             mv[k].vx = m.vxc[k];
             mv[k].vy = m.vyc[k];
-            mv[k].ivx = m.vxc[k] != 0. ? 1.0 / m.vxc[k] : 0.;
-            mv[k].ivy = m.vyc[k] != 0. ? 1.0 / m.vyc[k] : 0.;
+            mv[k].ivx = m.vxc[k] != 0. ? 1.0 / m.vxc[k] : HUGE_VAL;
+            mv[k].ivy = m.vyc[k] != 0. ? 1.0 / m.vyc[k] : HUGE_VAL;
         }
         c->d_vxc.upload(m.vxc, c->stream);
         c->d_vyc.upload(m.vyc, c->stream);

@@ -32,7 +32,7 @@ void launch_prod_general(const DevTables& T, double* tally, unsigned long long* 
 // Per-mode velocity record of the grid path.
 struct __align__(32) ModeVel {
     double vx, vy;    // get_v velocities, nm/ps
-    double ivx, ivy;  // their inverses (0 where the component is 0)
+    double ivx, ivy;  // their inverses (+inf where the component is 0)
 };
 
 // Grid-path kernel parameters beyond the tables.

@@ -131,52 +131,35 @@ struct GridParticle {
     int box;
 };
 
-// Pending tally of one lane: contributions to one (box, bin) key summed in
-// registers and flushed to the tally with three FP64 atomics.
+// Pending tally of one lane: unsigned contributions to one (box, bin) key
+// summed in registers; the particle sign is applied to the sign bit when
+// the key changes and the sums go out as three FP64 atomics.
 struct Pending {
     int key;
     unsigned adds;
     double c0, c1, c2;
-    __device__ void flush(double* tally) {
+    __device__ __forceinline__ void flush(double* tally, unsigned long long signbit) {
         if (key >= 0) {
             double* b = tally + 3ll * key;
-            atomicAdd(b + 0, c0);
-            atomicAdd(b + 1, c1);
-            atomicAdd(b + 2, c2);
+            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(c0) ^ signbit));
+            atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(c1) ^ signbit));
+            atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(c2) ^ signbit));
         }
         key = -1;
         c0 = c1 = c2 = 0.;
     }
-    __device__ void add(double* tally, int k, double contr, double vx, double vy) {
+    __device__ __forceinline__ void add(double* tally, unsigned long long signbit, int k, double d,
+                                        double vx, double vy) {
         if (k != key) {
-            flush(tally);
+            flush(tally, signbit);
             key = k;
         }
-        c0 += contr;
-        c1 += vx * contr;
-        c2 += vy * contr;
+        c0 += d;
+        c1 = fma(vx, d, c1);
+        c2 = fma(vy, d, c2);
         adds++;
     }
 };
-
-__device__ __forceinline__ void grid_tally(const DevTables& T, double* tally, Pending& pd, int box,
-                                           double t0, double t1, int sign, double vx, double vy) {
-    int sb = int(t0 * T.inv_dt), eb = int(t1 * T.inv_dt);
-    const int last = T.nbins - 1;
-    sb = sb > last ? last : sb;
-    eb = eb > last ? last : eb;
-    const double sg = double(sign);
-    if (sb == eb) {
-        pd.add(tally, box * T.nbins + sb, sg * (t1 - t0), vx, vy);
-        return;
-    }
-    const double* g = T.timegrid;
-    for (int i = sb; i <= eb; ++i) {
-        const double lo = fmax(g[i], t0);
-        const double hi = fmin(g[i + 1], t1);
-        if (hi > lo) pd.add(tally, box * T.nbins + i, sg * (hi - lo), vx, vy);
-    }
-}
 
 __device__ __forceinline__ int grid_cell(const DevGrid& G, int i, int j) {
     if (i < 0 || j < 0 || i >= G.nx || j >= G.ny) return -1;
@@ -224,6 +207,11 @@ __device__ int grid_generate(const DevTables& T, const DevGrid& G, const int2* b
     return 0;
 }
 
+// One lane carries one particle; each pass of the loop advances every active
+// lane by exactly one segment -- to the end of its free flight or to the
+// next cell border -- so the FP64 work of a warp stays converged however
+// many cells a flight crosses.  Idle lanes take new particles from a global
+// counter, one atomic per warp.
 template <bool SMEM_TALLY>
 __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, double* gtally,
                                                      unsigned long long* counters, int* err,
@@ -238,17 +226,24 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
     }
     Counters c = {0, 0, 0, 0, 0, 0, 0, 0};
     const int lane = threadIdx.x & 31;
+    const long long total = T.pend - T.pbegin;
+    const int last_bin = T.nbins - 1;
     Pending pd;
     pd.key = -1;
     pd.adds = 0;
     pd.c0 = pd.c1 = pd.c2 = 0.;
     GridParticle p;
+    p.i = p.j = p.mode = p.box = 0;
+    p.sign = 1;
+    p.x = p.y = p.t = 0.;
     Philox g;
-    long long pid = -1;
-    long long nev = 0;
-    bool active = false, done = false;
-    double time = 0.;
-    const long long total = T.pend - T.pbegin;
+    g.init(0, 0);
+    ModeVel mv = {0., 0., 0., 0.};
+    double dt = 0., tnb = 0.;
+    long long pid = -1, nev = 0;
+    int bin = 0;
+    unsigned long long signbit = 0;
+    bool active = false, done = false, need_flight = false;
     for (;;) {
         // refill idle lanes of the warp with new particles
         const unsigned idle = __ballot_sync(0xffffffffu, !active && !done);
@@ -268,8 +263,11 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
                         done = true;
                     } else {
                         active = true;
-                        time = 0.;
+                        need_flight = true;
                         nev = 0;
+                        bin = 0;
+                        tnb = __ldg(T.timegrid + 1);
+                        signbit = p.sign < 0 ? 0x8000000000000000ull : 0ull;
                     }
                 } else {
                     done = true;
@@ -278,58 +276,59 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
         }
         if (__all_sync(0xffffffffu, done)) break;
         if (!active) continue;
-        // one free flight
-        const int k = p.mode;
-        const ModeVel mv = A.mv[k];
-        // u in (0, 1 - 2^-25]: logf keeps -log(u) > 0 down to u's last step
-        double dt = double(-logf(g.uniformf())) * __ldg(T.tau + k);
-        c.events++;
-        if (!(dt > 0.) || ++nev > EVENT_CAP) {  // zero rate or runaway particle
-            record_error(err, dt > 0. ? E_LIMIT : E_VALUE, pid);
-            active = false;
-            done = true;
-            pd.flush(tally);
-            continue;
+        if (need_flight) {
+            // a new free flight: u in (0, 1) -> dt = -tau ln u (FP32 log)
+            const int k = p.mode;
+            mv = A.mv[k];
+            dt = double(-logf(g.uniformf())) * __ldg(T.tau + k);
+            c.events++;
+            if (!(dt > 0.) || ++nev > EVENT_CAP) {  // zero rate or runaway particle
+                record_error(err, dt > 0. ? E_LIMIT : E_VALUE, pid);
+                active = false;
+                done = true;
+                pd.flush(tally, signbit);
+                continue;
+            }
+            if (p.t + dt > T.maxtime) dt = T.maxtime - p.t;
+            need_flight = false;
         }
-        if (time + dt > T.maxtime) dt = T.maxtime - time;
-        bool alive = true;
-        for (int guard = 0;; ++guard) {
-            if (guard > FLIGHT_CAP) {
-                record_error(err, E_LIMIT, pid);
-                alive = false;
-                break;
-            }
-            // exit times of the current cell
-            double tx = 1e300, ty = 1e300;
-            if (mv.vx > 0.) tx = (__ldg(A.G.gx + p.i + 1) - p.x) * mv.ivx;
-            else if (mv.vx < 0.) tx = (__ldg(A.G.gx + p.i) - p.x) * mv.ivx;
-            if (mv.vy > 0.) ty = (__ldg(A.G.gy + p.j + 1) - p.y) * mv.ivy;
-            else if (mv.vy < 0.) ty = (__ldg(A.G.gy + p.j) - p.y) * mv.ivy;
-            const double te = fmin(tx, ty);
-            if (dt <= te) {
-                // stays in the cell: move, tally and scatter
-                grid_tally(T, tally, pd, p.box, p.t, p.t + dt, p.sign, mv.vx, mv.vy);
-                p.x += dt * mv.vx;
-                p.y += dt * mv.vy;
-                p.t += dt;
-                if (!T.ballistic)
-                    p.mode = alias_draw(g, T.resample_prob, T.resample_alt, T.n);
-                break;
-            }
-            // reaches a cell border
-            const double tex = te > 0. ? te : 0.;
-            grid_tally(T, tally, pd, p.box, p.t, p.t + tex, p.sign, mv.vx, mv.vy);
-            p.t += tex;
-            dt -= tex;
+        // exit times of the current cell (zero velocity components give
+        // +inf or NaN, and fmin ignores a NaN operand)
+        const double xw = __ldg(A.G.gx + p.i + (mv.vx > 0. ? 1 : 0));
+        const double yw = __ldg(A.G.gy + p.j + (mv.vy > 0. ? 1 : 0));
+        const double tx = (xw - p.x) * mv.ivx;
+        const double ty = (yw - p.y) * mv.ivy;
+        const double te = fmin(tx, ty);
+        const bool ends = !(dt > te);              // stays in the cell (also for te = NaN)
+        const double seg = ends ? dt : fmax(te, 0.);
+        // tally [t, t + seg] in (box, bin), splitting at bin borders
+        const double t1 = p.t + seg;
+        double t0 = p.t;
+        while (t1 > tnb && bin < last_bin) {
+            pd.add(tally, signbit, p.box * T.nbins + bin, tnb - t0, mv.vx, mv.vy);
+            t0 = tnb;
+            ++bin;
+            tnb = __ldg(T.timegrid + bin + 1);
+        }
+        pd.add(tally, signbit, p.box * T.nbins + bin, t1 - t0, mv.vx, mv.vy);
+        p.t = t1;
+        dt -= seg;
+        if (ends) {
+            p.x = fma(seg, mv.vx, p.x);
+            p.y = fma(seg, mv.vy, p.y);
+            if (!T.ballistic) p.mode = alias_draw(g, T.resample_prob, T.resample_alt, T.n);
+            need_flight = true;
+        } else {
+            // reaches a cell border: snap the crossed coordinate to the grid line
             int ni = p.i, nj = p.j, wall;
             if (tx <= ty) {
-                if (mv.vx > 0.) { ni = p.i + 1; p.x = __ldg(A.G.gx + ni); wall = 0; }
-                else { ni = p.i - 1; p.x = __ldg(A.G.gx + p.i); wall = 1; }
-                p.y += tex * mv.vy;
+                p.x = xw;
+                p.y = fma(seg, mv.vy, p.y);
+                if (mv.vx > 0.) { ni = p.i + 1; wall = 0; } else { ni = p.i - 1; wall = 1; }
             } else {
-                if (mv.vy > 0.) { nj = p.j + 1; p.y = __ldg(A.G.gy + nj); wall = 2; }
-                else { nj = p.j - 1; p.y = __ldg(A.G.gy + p.j); wall = 3; }
-                p.x += tex * mv.vx;
+                p.y = yw;
+                p.x = fma(seg, mv.vx, p.x);
+                if (mv.vy > 0.) { nj = p.j + 1; wall = 2; } else { nj = p.j - 1; wall = 3; }
             }
             const int nb = grid_cell(A.G, ni, nj);
             if (nb >= 0) {
@@ -337,50 +336,54 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
                 p.j = nj;
                 p.box = nb;
                 c.crossings++;
-                continue;
-            }
-            if (nb <= -2) {
+            } else if (nb <= -2) {
                 c.absorbed++;
-                alive = false;
-                break;
-            }
-            // void: reflect at the wall, new flight afterwards
-            const int cls = A.cls[wall];
-            if (cls < 0) {
-                record_error(err, E_GEOM, pid);
-                alive = false;
-                break;
-            }
-            int nm = -1;
-            if (T.specularity > 0. && g.uniform() < T.specularity && T.mirror) {
-                nm = __ldg(T.mirror + (long long)cls * T.n + k);
-                if (nm >= 0) c.specular++;
-            }
-            if (nm < 0) {
-                const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
-                const long long b = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
-                const int len = int(b - a);
-                if (len <= 0) {
+                active = false;
+                pd.flush(tally, signbit);
+                continue;
+            } else {
+                // void: reflect at the wall; a new flight follows
+                const int cls = A.cls[wall];
+                if (cls < 0) {
                     record_error(err, E_GEOM, pid);
-                    alive = false;
-                    break;
+                    active = false;
+                    done = true;
+                    pd.flush(tally, signbit);
+                    continue;
                 }
-                const int jj = int(mulhi32(g.next32(), uint32_t(len)));
-                const int4 e = __ldg(T.lalias + a + jj);
-                const float acc = float(g.next32() >> 8) * 0x1p-24f;
-                nm = acc < __int_as_float(e.x) ? e.y : e.z;
+                const int k = p.mode;
+                int nm = -1;
+                if (T.specularity > 0. && g.uniform() < T.specularity && T.mirror) {
+                    nm = __ldg(T.mirror + (long long)cls * T.n + k);
+                    if (nm >= 0) c.specular++;
+                }
+                if (nm < 0) {
+                    const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
+                    const long long b = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
+                    const int len = int(b - a);
+                    if (len <= 0) {
+                        record_error(err, E_GEOM, pid);
+                        active = false;
+                        done = true;
+                        pd.flush(tally, signbit);
+                        continue;
+                    }
+                    const int jj = int(mulhi32(g.next32(), uint32_t(len)));
+                    const int4 e = __ldg(T.lalias + a + jj);
+                    const float acc = float(g.next32() >> 8) * 0x1p-24f;
+                    nm = acc < __int_as_float(e.x) ? e.y : e.z;
+                }
+                p.mode = nm;
+                c.wall_hits++;
+                need_flight = true;
             }
-            p.mode = nm;
-            c.wall_hits++;
-            break;
         }
-        time = p.t;
-        if (!alive || time >= T.maxtime) {
+        if (p.t >= T.maxtime) {
             active = false;
-            pd.flush(tally);
+            pd.flush(tally, signbit);
         }
     }
-    pd.flush(tally);
+    pd.flush(tally, signbit);
     c.tallies = pd.adds;
     flush_counters_p(c, counters);
     if (SMEM_TALLY) {

@@ -87,14 +87,14 @@ def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, 
     for k in ("gz", "gz_jx", "gz_jy", "temperature", "jx", "jy"):
         setattr(r, k, out[k].ctypes.data_as(C.POINTER(C.c_double)))
     r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
-    cnt = np.zeros(6, dtype=np.int64)
+    cnt = np.zeros(7, dtype=np.int64)
     st = lib.oracle_rta_run(C.byref(ms), C.byref(gs), C.byref(p), int(nthreads), int(log_impl),
                             C.byref(r), cnt.ctypes.data_as(C.POINTER(C.c_int64)))
     if st != 0:
         raise _bt.BteError(st, lib.oracle_last_error().decode())
     out.update(Eeff=r.Eeff, energy_rate=r.energy_rate, events=int(cnt[0]), wall_hits=int(cnt[1]),
                crossings=int(cnt[2]), absorbed=int(cnt[3]), nudges=int(cnt[4]), quirks=int(cnt[5]),
-               specular_hits=int(r.specular_hits))
+               specular_hits=int(r.specular_hits), loop_seconds=float(cnt[6]) * 1e-6)
     return out
 
 

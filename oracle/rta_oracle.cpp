@@ -41,6 +41,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1254,6 +1255,7 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
                 codes[std::size_t(tid)] = BTE_ERR_GEOMETRY;
             }
         };
+        const auto loop_start = std::chrono::steady_clock::now();
         if (nthreads == 1) {
             work(0);
         } else {
@@ -1261,6 +1263,8 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
             for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
             for (auto& t : th) t.join();
         }
+        const double loop_us = std::chrono::duration<double, std::micro>(
+                                   std::chrono::steady_clock::now() - loop_start).count();
         for (std::size_t t = 0; t < errs.size(); ++t)
             if (!errs[t].empty()) return fail(codes[t], errs[t].c_str());
         orc::Tally T = std::move(tl[0]);
@@ -1292,6 +1296,7 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
         if (counters) {
             counters[0] = T.events; counters[1] = T.wall_hits; counters[2] = T.crossings;
             counters[3] = T.absorbed; counters[4] = T.nudges; counters[5] = T.quirks;
+            counters[6] = int64_t(loop_us);  // the particle loop alone (no table set-up)
         }
         const std::size_t nk = nbx * nbn;
         if (out->gz) std::copy(T.gz.begin(), T.gz.end(), out->gz);
