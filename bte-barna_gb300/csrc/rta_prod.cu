@@ -292,10 +292,11 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
             if (p.t + dt > T.maxtime) dt = T.maxtime - p.t;
             need_flight = false;
         }
-        // exit times of the current cell (zero velocity components give
-        // +inf or NaN, and fmin ignores a NaN operand)
-        const double xw = __ldg(A.G.gx + p.i + (mv.vx > 0. ? 1 : 0));
-        const double yw = __ldg(A.G.gy + p.j + (mv.vy > 0. ? 1 : 0));
+        // exit times of the current cell.  A zero velocity component takes
+        // the upper cell line, so (line - position) >= 0 times its +inf
+        // inverse gives +inf (or NaN on the line), and fmin ignores a NaN.
+        const double xw = __ldg(A.G.gx + p.i + (mv.vx >= 0. ? 1 : 0));
+        const double yw = __ldg(A.G.gy + p.j + (mv.vy >= 0. ? 1 : 0));
         const double tx = (xw - p.x) * mv.ivx;
         const double ty = (yw - p.y) * mv.ivy;
         const double te = fmin(tx, ty);

@@ -190,6 +190,88 @@ def write_modes_file(path: str, m: dict) -> None:
         np.asarray(m["w"], dtype="<f8").tofile(f)
 
 
+def be_kernel(omega, T):
+    """(x / sinh x)^2 with x = hbar omega / 2 kB T (include/utilities.hpp:401-417)."""
+    x = 0.5 * 1e12 * HBAR / KB * np.asarray(omega) / T
+    out = np.ones_like(x)
+    big = x > 300.0
+    mid = (x >= 1e-320) & ~big
+    out[big] = 0.0
+    out[mid] = (x[mid] / np.sinh(x[mid])) ** 2
+    return out
+
+
+def propagator(modes: dict, dt: float = 1.0, T: float = 300.0, nnz_row: int = 64,
+               config: int = 2, flip: float = 0.25, use_torch: bool = False) -> np.ndarray:
+    """Dense propagator P = exp(B dt) over the non-Gamma modes (3..n-1), in the
+    column convention of PropagatorBuilder (src/collision_operator.cpp:1015-1064):
+    particle in mode j draws its next mode from column j; columns sum to 1.
+
+    Synthetic operator (symmetrised form, c = C^1/2 the square roots of the
+    mode heat capacities): A = A_RTA + L with
+      A_RTA = W - (W c)(W c)^T / (c^T W c), W = diag(1/tau): relaxation with
+              the energy-conserving resampling of the RTA;
+      L     = a seeded symmetric sparse coupling (~nnz_row entries per row)
+              with weights s_ij ~ LogNormal(0,1) min(1/tau_i, 1/tau_j) 0.1,
+              L_ij = -s_ij, L_ii = sum_j s_ij c_j / c_i; a seeded fraction
+              `flip` of the couplings changes sign, which gives P the
+              negative entries (and the branching) of real propagators.
+    Both parts are symmetric and annihilate c, so A C^1/2 = 0 (energy
+    conservation); negative eigenvalues are clipped to make A PSD (c stays
+    an eigenvector of eigenvalue 0).  B = -C^1/2 A C^-1/2, so
+    P = C^1/2 exp(-A dt) C^-1/2, evaluated through the eigenvectors of A."""
+    rng = _rng(config, 2)
+    w = np.asarray(modes["w"])[3:]
+    om = np.asarray(modes["omega"])[3:]
+    n = w.size
+    rate = np.where(w > 0, w, 0.0)
+    c = np.sqrt(be_kernel(om, T))
+    Wc = rate * c
+    A = np.diag(rate) - np.outer(Wc, Wc) / float(c @ Wc)
+    k = max(1, nnz_row // 2)
+    rows = np.repeat(np.arange(n), k)
+    cols = rng.integers(0, n, size=n * k)
+    keep = rows != cols
+    rows, cols = rows[keep], cols[keep]
+    wgt = rng.lognormal(0.0, 1.0, rows.size) * np.minimum(rate[rows], rate[cols]) * 0.1
+    wgt *= np.where(rng.random(rows.size) < flip, -1.0, 1.0)
+    S = np.zeros((n, n))
+    np.add.at(S, (rows, cols), wgt)
+    S = S + S.T
+    A -= S
+    A[np.diag_indices(n)] += (S @ c) / c
+    A = 0.5 * (A + A.T)
+    if use_torch:
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        lam, V = torch.linalg.eigh(torch.from_numpy(A).to(dev))
+        lam = torch.clamp(lam, min=0.0)
+        E = (V * torch.exp(-lam * dt)) @ V.T
+        E = E.cpu().numpy()
+    else:
+        lam, V = np.linalg.eigh(A)
+        lam = np.clip(lam, 0.0, None)
+        E = (V * np.exp(-lam * dt)) @ V.T
+    P = (c[:, None] * E) / c[None, :]
+    return np.asfortranarray(P)
+
+
+def write_propagator(path: str, P: np.ndarray) -> None:
+    """*.P.eigen.bin of save_P (src/collision_operator.cpp:931-970): int64
+    number of rows, then the matrix in column-major FP64."""
+    P = np.asfortranarray(P, dtype="<f8")
+    with open(path, "wb") as f:
+        np.array([P.shape[0]], dtype="<i8").tofile(f)
+        f.write(P.tobytes(order="F"))
+
+
+def read_propagator(path: str) -> np.ndarray:
+    with open(path, "rb") as f:
+        n = int(np.fromfile(f, dtype="<i8", count=1)[0])
+        data = np.fromfile(f, dtype="<f8", count=n * n)
+    return data.reshape((n, n), order="F")
+
+
 # ------------------------------------------------------------------ configs
 def config0(n_particles: int = 1_000_000) -> dict:
     """Plain RTA ribbon: 32x32x6 modes, 1 um x 100 nm, 50 cells, 301/299 K
