@@ -27,7 +27,7 @@ SOURCE_WALLS, SOURCE_INITIAL = 0, 1
 # Exported symbols declared in include/btegpu.h.
 PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
-                  "bte_version"]
+                  "bte_version", "bte_rta_run_noalloc"]
 
 
 class BteError(RuntimeError):
@@ -147,6 +147,8 @@ def load_library(path: str = LIB_PATH):
     lib.bte_query_sizes.argtypes = [vp, C.POINTER(RtaParams), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
     lib.bte_version.restype = C.c_int32
+    lib.bte_rta_run_noalloc.argtypes = [vp, C.POINTER(RtaParams), C.c_void_p, C.POINTER(RtaResult)]
+    lib.bte_rta_run_noalloc.restype = C.c_int
     for f in ("bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
               "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes"):
         getattr(lib, f).restype = C.c_int

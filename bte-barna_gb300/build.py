@@ -24,6 +24,7 @@ UNITS = [
     ("rta_replay.cu", ["-fmad=false"]),
     ("rta_prod.cu", []),
     ("capi.cu", []),
+    ("noalloc.cu", []),
 ]
 
 

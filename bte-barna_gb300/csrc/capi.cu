@@ -650,3 +650,138 @@ int btegpu_debug_log(const double* x, double* y, long long n) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ prepared runs
+// Read-only view of a context whose tables an earlier bte_rta_run built for
+// the same parameters: fills the kernel arguments without allocating or
+// uploading anything.  Used by the allocation-free entry point (noalloc.cu).
+namespace bte {
+
+bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r, std::string* why) {
+    if (!c || !p || !r) {
+        *why = "null argument";
+        return BTE_ERR_INPUT;
+    }
+    if (p->mode != BTE_MODE_PRODUCTION) {
+        *why = "the allocation-free run is the production grid kernel: mode must be BTE_MODE_PRODUCTION";
+        return BTE_ERR_INPUT;
+    }
+    if (!(p->dt > 0.) || !(p->maxtime > 0.) || p->nparticles < 1 ||
+        !(p->specularity >= 0. && p->specularity <= 1.) || !(p->T0 > 0.)) {
+        *why = "invalid run parameters";
+        return BTE_ERR_INPUT;
+    }
+    if (!c->have_modes || !c->have_geom || !c->modes_dev || !c->geom_dev || !c->lambert_dev) {
+        *why = "context not prepared: load the tables and run bte_rta_run once with these parameters";
+        return BTE_ERR_STATE;
+    }
+    const HostGeometry& g = c->geom;
+    const HostModes& m = c->modes;
+    if (!g.rect_grid) {
+        *why = "the allocation-free run needs boxes that tile an axis-aligned grid";
+        return BTE_ERR_INPUT;
+    }
+    if (c->resample_T0 != p->T0 || c->gen_key_source != p->source ||
+        (p->source == BTE_SOURCE_INITIAL &&
+         (c->gen_key_n != p->nparticles || c->gen_key_seed != p->seed))) {
+        *why = "context prepared for other parameters: run bte_rta_run once with this T0, source "
+               "(and, for the initial source, N and seed) first";
+        return BTE_ERR_STATE;
+    }
+    if (p->specularity > 0. && !c->have_mirror) {
+        *why = "specular walls need an axis-aligned q grid with mirror images";
+        return BTE_ERR_INPUT;
+    }
+    const std::size_t ntime = std::size_t(std::floor(p->maxtime / p->dt + 1.0e-6)) + 1;
+    if (ntime < 2) {
+        *why = "maxtime shorter than one time bin";
+        return BTE_ERR_INPUT;
+    }
+    r->ntime = int(ntime);
+    r->nbins = int(ntime - 1);
+    r->maxtime = double(ntime - 1) * p->dt;
+    r->step = (r->maxtime - 0.0) / double(ntime - 1);
+    r->nboxes = int(g.boxes.size());
+    long long total;
+    if (p->source == BTE_SOURCE_WALLS) {
+        r->Eeff = c->gens.total_energy / double(p->nparticles);
+        total = p->nparticles;
+    } else {
+        r->Eeff = c->gen_Eeff;
+        total = c->gens.init_first.back();
+    }
+    r->energy = c->gens.total_energy;
+    long long pbeg = std::max<long long>(0, p->particle_begin);
+    long long pend = p->particle_end > 0 ? std::min<long long>(p->particle_end, total) : total;
+    if (pend < pbeg) pend = pbeg;
+    DevTables& T = r->T;
+    T = DevTables{};
+    T.n = int(m.n());
+    T.nb = m.nb;
+    T.vxc = c->d_vxc.as<double>();
+    T.vyc = c->d_vyc.as<double>();
+    T.w = c->d_w.as<double>();
+    T.tau = c->d_tau.as<double>();
+    T.resample_cdf = c->d_rcdf.as<double>();
+    T.resample_prob = c->d_rprob.as<float>();
+    T.resample_alt = c->d_ralt.as<int>();
+    T.nboxes = r->nboxes;
+    T.boxes = c->d_boxes.as<GBox>();
+    T.hull = c->d_hull.as<V2>();
+    T.borders = c->d_borders.as<GBorder>();
+    T.contacts = c->d_contacts.as<GContact>();
+    T.nclass = c->nclass;
+    T.row_ptr = c->d_row_ptr.as<long long>();
+    T.lcol = c->d_lcol.as<int>();
+    T.lcdf = c->d_lcdf.as<double>();
+    T.lalias = c->d_lalias.as<int4>();
+    T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
+    T.ntime = r->ntime;
+    T.timegrid = nullptr;  // set by the caller
+    T.maxtime = r->maxtime;
+    T.inv_dt = 1.0 / r->step;
+    T.source = p->source;
+    T.ngen = p->source == BTE_SOURCE_WALLS ? int(c->gens.walls.size()) : int(c->gens.init_box.size());
+    T.gen_cdf = c->d_gcdf.as<double>();
+    T.gen_prob = c->d_gprob.as<float>();
+    T.gen_alt = c->d_galt.as<int>();
+    T.walls = c->d_walls.as<WallGenDev>();
+    T.wall_cum = c->d_wcum.as<double>();
+    T.init_first = c->d_ifirst.as<long long>();
+    T.init_box = c->d_ibox.as<int>();
+    T.init_sign = c->d_isign.as<int>();
+    T.seed = p->seed;
+    T.ballistic = p->ballistic;
+    T.specularity = p->specularity;
+    T.pbegin = pbeg;
+    T.pend = pend;
+    T.nbins = r->nbins;
+    GridArgs& A = r->A;
+    A = GridArgs{};
+    A.G.nx = g.gnx;
+    A.G.ny = g.gny;
+    A.G.gx = c->d_gx.as<double>();
+    A.G.gy = c->d_gy.as<double>();
+    A.G.cell = c->d_gcell.as<int>();
+    A.boxcell = c->d_boxcell.as<int2>();
+    A.mv = c->d_mv.as<ModeVel>();
+    const V2 want[4] = {v2(1, 0), v2(-1, 0), v2(0, 1), v2(0, -1)};
+    for (int w = 0; w < 4; ++w) {
+        A.cls[w] = -1;
+        for (std::size_t k = 0; k < g.normals.size(); ++k)
+            if (g.normals[k].x == want[w].x && g.normals[k].y == want[w].y) A.cls[w] = int(k);
+    }
+    r->stream = c->stream;
+    r->ev0 = c->ev0;
+    r->ev1 = c->ev1;
+    r->device = c->device;
+    r->nsm = c->nsm;
+    r->tune = c->tune;
+    return BTE_OK;
+}
+
+void set_ctx_error(bte_ctx* c, const std::string& m) {
+    if (c) c->err = m;
+}
+
+}  // namespace bte

@@ -49,4 +49,17 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
                       unsigned long long* counters, int* err, unsigned long long* work,
                       const ProdTuning& tune, int nsm, cudaStream_t s);
 
+// Kernel arguments of a context already prepared for one set of run
+// parameters (see prepared_grid_run in capi.cu).
+struct PreparedRun {
+    DevTables T;
+    GridArgs A;
+    double Eeff, energy, maxtime, step;
+    int nboxes, nbins, ntime;
+    cudaStream_t stream;
+    cudaEvent_t ev0, ev1;
+    int device, nsm;
+    ProdTuning tune;
+};
+
 }  // namespace bte
