@@ -239,7 +239,18 @@ def main():
                            specularity=c["specularity"], begin=base, end=base + per_step,
                            raw=False)
 
-    # first call builds the device tables (not timed)
+    # the first call builds the device tables; the autotuner then picks the
+    # kernel's block shape, residency and tally privatisation (not timed)
+    import autotune
+    trial = max(1000, min(per_step // 8, 250_000))
+
+    def trial_run(begin, end):
+        return eng.rta_run(c["T0"], c["dt"], c["maxtime"], c["N"], seed=999,
+                           mode=btegpu.MODE_PRODUCTION, source=src,
+                           specularity=c["specularity"], begin=begin, end=end, raw=False)
+    trial_run(0, trial)
+    nbins0 = int(math.floor(c["maxtime"] / c["dt"] + 1e-6))
+    choice, tuned = autotune.tune(eng, trial_run, trial, 3 * int(c["geom"]["nboxes"]) * nbins0 * 8)
     for w in range(args.warmup):
         step(w, 1000 + w)
     if dist:
@@ -304,6 +315,10 @@ def main():
                          "traffic": (bpe * ev / args.steps) if bpe else None,
                          "bytes_per_event": per_launch_bytes / max(ev / args.steps, 1)},
             "clocks": clk,
+            "tuning": {"block_threads": choice[0], "blocks_per_sm": choice[1],
+                       "smem_tally": choice[2],
+                       "ns_per_event": {f"{k[0]}x{k[1]}{'s' if k[2] else ''}": v
+                                        for k, v in tuned.items()}},
         }
         if world == 1 and not args.no_cpu_baseline:
             try:

@@ -74,6 +74,41 @@ class RtaResult(C.Structure):
                 ("kernel_ms", C.c_double)]
 
 
+class Propagator(C.Structure):
+    _fields_ = [("nmodes", C.c_int32), ("T", C.c_double), ("P", C.POINTER(C.c_double))]
+
+
+class BertaParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("maxtime", C.c_double), ("Eeff", C.c_double),
+                ("T0", C.c_double), ("seed", C.c_uint64), ("mode", C.c_int32),
+                ("rta", C.c_int32), ("cancel_every", C.c_int32), ("reserved0", C.c_int32),
+                ("capacity", C.c_int64)]
+
+
+class BertaResult(C.Structure):
+    _fields_ = [("nboxes", C.c_int32), ("nsteps", C.c_int32), ("ed", C.POINTER(C.c_double)),
+                ("flux", C.POINTER(C.c_double)), ("nparticles", C.POINTER(C.c_int64)),
+                ("histogram", C.POINTER(C.c_int32)), ("particle_steps", C.c_int64),
+                ("branchings", C.c_int64), ("kernel_ms", C.c_double)]
+
+
+def berta_steps(dt: float, maxtime: float) -> int:
+    """Iterations of `while (time <= maxtime) { ...; time += dt; }`."""
+    t, n = 0.0, 0
+    while t <= maxtime:
+        n += 1
+        t += dt
+    return n
+
+
+def berta_params(dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, mode=MODE_PRODUCTION,
+                 cancel_every=4, capacity=0):
+    p = BertaParams()
+    p.dt, p.maxtime, p.Eeff, p.T0, p.seed = float(dt), float(maxtime), float(Eeff), float(T0), int(seed)
+    p.mode, p.rta, p.cancel_every, p.capacity = int(mode), int(bool(rta)), int(cancel_every), int(capacity)
+    return p
+
+
 class Tuning(C.Structure):
     _fields_ = [("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
                 ("smem_tally", C.c_int32), ("smem_alias", C.c_int32)]

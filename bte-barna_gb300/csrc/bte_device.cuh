@@ -129,7 +129,7 @@ BTE_HD int uniform_below(G& g, uint32_t n) {
 struct Philox {
     uint32_t c0, c1, c2, c3;  // counter: draw index (c0,c1), particle (c2,c3)
     uint32_t k0, k1;          // key: master seed
-    uint32_t buf[4];
+    uint32_t b0, b1, b2, b3;  // unread words of the last block, b0 first
     int avail;
 
     BTE_HD void init(uint64_t seed, uint64_t particle) {
@@ -140,11 +140,14 @@ struct Philox {
         k0 = uint32_t(seed);
         k1 = uint32_t(seed >> 32);
         avail = 0;
+        b0 = b1 = b2 = b3 = 0;
     }
-    BTE_HD void block(uint32_t out[4]) const {
+    BTE_HD void block() {
         uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3;
         uint32_t a = k0, b = k1;
+#if defined(__CUDACC__)
 #pragma unroll
+#endif
         for (int r = 0; r < 10; ++r) {
             const uint32_t lo0 = 0xD2511F53u * x0, hi0 = mulhi32(0xD2511F53u, x0);
             const uint32_t lo1 = 0xCD9E8D57u * x2, hi1 = mulhi32(0xCD9E8D57u, x2);
@@ -155,18 +158,23 @@ struct Philox {
             a += 0x9E3779B9u;
             b += 0xBB67AE85u;
         }
-        out[0] = x0;
-        out[1] = x1;
-        out[2] = x2;
-        out[3] = x3;
+        b0 = x3;  // words leave in the order x3, x2, x1, x0
+        b1 = x2;
+        b2 = x1;
+        b3 = x0;
     }
     BTE_HD uint32_t next32() {
         if (avail == 0) {
-            block(buf);
+            block();
             if (++c0 == 0) ++c1;
             avail = 4;
         }
-        return buf[--avail];
+        const uint32_t r = b0;  // a register queue: no indexed (local-memory) access
+        b0 = b1;
+        b1 = b2;
+        b2 = b3;
+        --avail;
+        return r;
     }
     BTE_HD uint64_t next() {
         uint64_t h = next32();

@@ -70,7 +70,7 @@ struct bte_ctx {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
-    bte::ProdTuning tune{0, 0, 1, 0};
+    bte::ProdTuning tune{0, 0, 0, 0};
 
     bool have_modes = false, have_geom = false;
     bte::HostModes modes;
@@ -304,7 +304,7 @@ bte_status bte_last_error(const bte_ctx* c, char* buf, size_t size) {
 bte_status bte_set_tuning(bte_ctx* c, const bte_tuning* t) {
     if (!c) return BTE_ERR_INPUT;
     if (!t) {
-        c->tune = bte::ProdTuning{0, 0, 1, 0};
+        c->tune = bte::ProdTuning{0, 0, 0, 0};
         return BTE_OK;
     }
     if (t->block_threads < 0 || t->block_threads > 256 || (t->block_threads % 32) != 0) {

@@ -131,33 +131,46 @@ struct GridParticle {
     int box;
 };
 
-// Pending tally of one lane: unsigned contributions to one (box, bin) key
-// summed in registers; the particle sign is applied to the sign bit when
-// the key changes and the sums go out as three FP64 atomics.
+// Order of non-negative doubles (and +inf, and NaN above +inf) through their
+// bit patterns as signed 64-bit integers, on the integer pipe: a negative
+// operand keeps the sign bit and stays below every non-negative one.
+__device__ __forceinline__ long long ob(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ double obd(long long b) { return __longlong_as_double(b); }
+
+// float -> double for a positive normal float, by moving its exponent and
+// mantissa fields (integer pipe).
+__device__ __forceinline__ double widen_pos(float f) {
+    const unsigned fb = __float_as_uint(f);
+    const unsigned long long e = ((fb >> 23) & 0xffu) + (1023u - 127u);
+    return __longlong_as_double((long long)((e << 52) | ((unsigned long long)(fb & 0x7fffffu) << 29)));
+}
+
+// Pending tally of one lane.  Inside one (box, time bin) key the particle
+// moves continuously, so the key's contributions telescope: time spent =
+// t - t0 and the velocity-weighted sums are the displacement x - x0, y - y0
+// (sum of v * dt over the segments).  Nothing is accumulated per segment;
+// when the key changes the three differences go out as FP64 atomics, with
+// the particle sign applied to the sign bit.
 struct Pending {
     int key;
-    unsigned adds;
-    double c0, c1, c2;
-    __device__ __forceinline__ void flush(double* tally, unsigned long long signbit) {
+    unsigned flushes;
+    double t0, x0, y0;
+    __device__ __forceinline__ void start(int k, double t, double x, double y) {
+        key = k;
+        t0 = t;
+        x0 = x;
+        y0 = y;
+    }
+    __device__ __forceinline__ void flush(double* tally, unsigned long long signbit, double t, double x,
+                                          double y) {
         if (key >= 0) {
             double* b = tally + 3ll * key;
-            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(c0) ^ signbit));
-            atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(c1) ^ signbit));
-            atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(c2) ^ signbit));
+            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(t - t0) ^ signbit));
+            atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(x - x0) ^ signbit));
+            atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(y - y0) ^ signbit));
+            flushes++;
         }
         key = -1;
-        c0 = c1 = c2 = 0.;
-    }
-    __device__ __forceinline__ void add(double* tally, unsigned long long signbit, int k, double d,
-                                        double vx, double vy) {
-        if (k != key) {
-            flush(tally, signbit);
-            key = k;
-        }
-        c0 += d;
-        c1 = fma(vx, d, c1);
-        c2 = fma(vy, d, c2);
-        adds++;
     }
 };
 
@@ -211,9 +224,11 @@ __device__ int grid_generate(const DevTables& T, const DevGrid& G, const int2* b
 // lane by exactly one segment -- to the end of its free flight or to the
 // next cell border -- so the FP64 work of a warp stays converged however
 // many cells a flight crosses.  Idle lanes take new particles from a global
-// counter, one atomic per warp.
-template <bool SMEM_TALLY>
-__global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, double* gtally,
+// counter, one atomic per warp.  FP64 instructions are kept to the ones that
+// move the particle (exit times, position, clock); comparisons, min/max and
+// the float -> double widening run on the integer pipe.
+template <bool SMEM_TALLY, int MINB>
+__global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs A, double* gtally,
                                                      unsigned long long* counters, int* err,
                                                      unsigned long long* work) {
     extern __shared__ double stally[];
@@ -228,10 +243,11 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
     const int lane = threadIdx.x & 31;
     const long long total = T.pend - T.pbegin;
     const int last_bin = T.nbins - 1;
+    const long long maxtime_b = ob(T.maxtime);
     Pending pd;
     pd.key = -1;
-    pd.adds = 0;
-    pd.c0 = pd.c1 = pd.c2 = 0.;
+    pd.flushes = 0;
+    pd.t0 = pd.x0 = pd.y0 = 0.;
     GridParticle p;
     p.i = p.j = p.mode = p.box = 0;
     p.sign = 1;
@@ -268,6 +284,7 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
                         bin = 0;
                         tnb = __ldg(T.timegrid + 1);
                         signbit = p.sign < 0 ? 0x8000000000000000ull : 0ull;
+                        pd.start(p.box * T.nbins, 0., p.x, p.y);
                     }
                 } else {
                     done = true;
@@ -280,67 +297,77 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
             // a new free flight: u in (0, 1) -> dt = -tau ln u (FP32 log)
             const int k = p.mode;
             mv = A.mv[k];
-            dt = double(-logf(g.uniformf())) * __ldg(T.tau + k);
+            dt = widen_pos(-logf(g.uniformf())) * __ldg(T.tau + k);
             c.events++;
-            if (!(dt > 0.) || ++nev > EVENT_CAP) {  // zero rate or runaway particle
-                record_error(err, dt > 0. ? E_LIMIT : E_VALUE, pid);
+            if (ob(dt) <= 0 || ++nev > EVENT_CAP) {  // zero rate or runaway particle
+                record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
                 active = false;
                 done = true;
-                pd.flush(tally, signbit);
+                pd.flush(tally, signbit, p.t, p.x, p.y);
                 continue;
             }
-            if (p.t + dt > T.maxtime) dt = T.maxtime - p.t;
+            const double tend = p.t + dt;
+            if (ob(tend) > maxtime_b) dt = T.maxtime - p.t;
             need_flight = false;
         }
         // exit times of the current cell.  A zero velocity component takes
         // the upper cell line, so (line - position) >= 0 times its +inf
-        // inverse gives +inf (or NaN on the line), and fmin ignores a NaN.
-        const double xw = __ldg(A.G.gx + p.i + (mv.vx >= 0. ? 1 : 0));
-        const double yw = __ldg(A.G.gy + p.j + (mv.vy >= 0. ? 1 : 0));
+        // inverse gives +inf (or NaN on the line, ordered above +inf).
+        const int upx = ob(mv.vx) >= 0 ? 1 : 0;
+        const int upy = ob(mv.vy) >= 0 ? 1 : 0;
+        const double xw = __ldg(A.G.gx + p.i + upx);
+        const double yw = __ldg(A.G.gy + p.j + upy);
         const double tx = (xw - p.x) * mv.ivx;
         const double ty = (yw - p.y) * mv.ivy;
-        const double te = fmin(tx, ty);
-        const bool ends = !(dt > te);              // stays in the cell (also for te = NaN)
-        const double seg = ends ? dt : fmax(te, 0.);
-        // tally [t, t + seg] in (box, bin), splitting at bin borders
+        const bool xfirst = ob(tx) <= ob(ty);
+        const long long te_b = xfirst ? ob(tx) : ob(ty);
+        const bool ends = !(ob(dt) > te_b);          // stays in the cell (also for NaN)
+        const double seg = ends ? dt : obd(te_b > 0 ? te_b : 0);
         const double t1 = p.t + seg;
-        double t0 = p.t;
-        while (t1 > tnb && bin < last_bin) {
-            pd.add(tally, signbit, p.box * T.nbins + bin, tnb - t0, mv.vx, mv.vy);
-            t0 = tnb;
+        double nx = fma(seg, mv.vx, p.x);
+        double ny = fma(seg, mv.vy, p.y);
+        // time-bin borders crossed during the segment close the pending key
+        while (ob(t1) > ob(tnb) && bin < last_bin) {
+            const double d = tnb - p.t;
+            const double bx = fma(d, mv.vx, p.x), by = fma(d, mv.vy, p.y);
+            pd.flush(tally, signbit, tnb, bx, by);
             ++bin;
+            pd.start(p.box * T.nbins + bin, tnb, bx, by);
             tnb = __ldg(T.timegrid + bin + 1);
         }
-        pd.add(tally, signbit, p.box * T.nbins + bin, t1 - t0, mv.vx, mv.vy);
         p.t = t1;
         dt -= seg;
         if (ends) {
-            p.x = fma(seg, mv.vx, p.x);
-            p.y = fma(seg, mv.vy, p.y);
+            p.x = nx;
+            p.y = ny;
             if (!T.ballistic) p.mode = alias_draw(g, T.resample_prob, T.resample_alt, T.n);
             need_flight = true;
         } else {
-            // reaches a cell border: snap the crossed coordinate to the grid line
+            // reaches a cell border: the crossed coordinate is the grid line
             int ni = p.i, nj = p.j, wall;
-            if (tx <= ty) {
-                p.x = xw;
-                p.y = fma(seg, mv.vy, p.y);
-                if (mv.vx > 0.) { ni = p.i + 1; wall = 0; } else { ni = p.i - 1; wall = 1; }
+            if (xfirst) {
+                nx = xw;
+                ni = p.i + (upx ? 1 : -1);
+                wall = upx ? 0 : 1;
             } else {
-                p.y = yw;
-                p.x = fma(seg, mv.vx, p.x);
-                if (mv.vy > 0.) { nj = p.j + 1; wall = 2; } else { nj = p.j - 1; wall = 3; }
+                ny = yw;
+                nj = p.j + (upy ? 1 : -1);
+                wall = upy ? 2 : 3;
             }
+            p.x = nx;
+            p.y = ny;
             const int nb = grid_cell(A.G, ni, nj);
             if (nb >= 0) {
+                pd.flush(tally, signbit, p.t, p.x, p.y);
                 p.i = ni;
                 p.j = nj;
                 p.box = nb;
+                pd.start(nb * T.nbins + bin, p.t, p.x, p.y);
                 c.crossings++;
             } else if (nb <= -2) {
                 c.absorbed++;
                 active = false;
-                pd.flush(tally, signbit);
+                pd.flush(tally, signbit, p.t, p.x, p.y);
                 continue;
             } else {
                 // void: reflect at the wall; a new flight follows
@@ -349,7 +376,7 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
                     record_error(err, E_GEOM, pid);
                     active = false;
                     done = true;
-                    pd.flush(tally, signbit);
+                    pd.flush(tally, signbit, p.t, p.x, p.y);
                     continue;
                 }
                 const int k = p.mode;
@@ -366,7 +393,7 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
                         record_error(err, E_GEOM, pid);
                         active = false;
                         done = true;
-                        pd.flush(tally, signbit);
+                        pd.flush(tally, signbit, p.t, p.x, p.y);
                         continue;
                     }
                     const int jj = int(mulhi32(g.next32(), uint32_t(len)));
@@ -379,13 +406,12 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
                 need_flight = true;
             }
         }
-        if (p.t >= T.maxtime) {
+        if (ob(p.t) >= maxtime_b) {
             active = false;
-            pd.flush(tally, signbit);
+            pd.flush(tally, signbit, p.t, p.x, p.y);
         }
     }
-    pd.flush(tally, signbit);
-    c.tallies = pd.adds;
+    c.tallies = pd.flushes;
     flush_counters_p(c, counters);
     if (SMEM_TALLY) {
         __syncthreads();
@@ -397,32 +423,42 @@ __global__ void __launch_bounds__(256) rta_prod_grid(DevTables T, GridArgs A, do
 }
 
 bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
-                           unsigned long long* counters, int* err, unsigned long long* work,
-                           const ProdTuning& tune, int nsm, cudaStream_t s) {
+                      unsigned long long* counters, int* err, unsigned long long* work,
+                      const ProdTuning& tune, int nsm, cudaStream_t s) {
     const long long n = T.pend - T.pbegin;
     if (n <= 0) return true;
     const int threads = tune.block_threads > 0 ? tune.block_threads : 256;
     if (threads > 256 || threads % 32) return false;
     const size_t smem = size_t(3) * T.nboxes * T.nbins * sizeof(double);
-    bool use_smem = tune.smem_tally != 0 && smem <= 200 * 1024;
-    int bps = tune.blocks_per_sm > 0 ? tune.blocks_per_sm : (use_smem ? 1 : 8);
+    const bool use_smem = tune.smem_tally != 0 && smem <= 200 * 1024;
+    // residency variants: 3 blocks of 256 threads per SM (80 registers) or
+    // 2 (no register cap); the shared-memory tally allows one block per SM
+    int bps = tune.blocks_per_sm > 0 ? tune.blocks_per_sm : (use_smem ? 1 : 3);
+    const void* fn;
     if (use_smem) {
-        if (cudaFuncSetAttribute(rta_prod_grid<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        fn = reinterpret_cast<const void*>(rta_prod_grid<true, 1>);
+        if (cudaFuncSetAttribute(rta_prod_grid<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(smem)) != cudaSuccess)
             return false;
-        int maxb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, rta_prod_grid<true>, threads, smem);
-        if (maxb < 1) return false;
-        if (bps > maxb) bps = maxb;
+    } else if (bps >= 3) {
+        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 3>);
+    } else {
+        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2>);
     }
+    int maxb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, fn, threads, use_smem ? smem : 0);
+    if (maxb < 1) return false;
+    if (bps > maxb) bps = maxb;
     long long blocks = (long long)nsm * bps;
     const long long need = (n + threads - 1) / threads;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
     if (use_smem)
-        rta_prod_grid<true><<<unsigned(blocks), threads, smem, s>>>(T, A, tally, counters, err, work);
+        rta_prod_grid<true, 1><<<unsigned(blocks), threads, smem, s>>>(T, A, tally, counters, err, work);
+    else if (fn == reinterpret_cast<const void*>(rta_prod_grid<false, 3>))
+        rta_prod_grid<false, 3><<<unsigned(blocks), threads, 0, s>>>(T, A, tally, counters, err, work);
     else
-        rta_prod_grid<false><<<unsigned(blocks), threads, 0, s>>>(T, A, tally, counters, err, work);
+        rta_prod_grid<false, 2><<<unsigned(blocks), threads, 0, s>>>(T, A, tally, counters, err, work);
     return true;
 }
 

@@ -141,6 +141,44 @@ typedef struct bte_rta_result {
     double kernel_ms;        /* device time of the particle loop                 */
 } bte_rta_result;
 
+/* Propagator exp(B dt) of one material at one temperature over the modes
+ * 3..n-1 (the three Gamma acoustic modes have no column), as stored in
+ * *.P.eigen.bin by save_P (src/collision_operator.cpp:931-970). */
+typedef struct bte_propagator {
+    int32_t nmodes;      /* n - 3 */
+    double T;            /* temperature the propagator was built at, K */
+    const double* P;     /* [nmodes * nmodes] column-major: column j = mode j + 3 */
+} bte_propagator;
+
+/* Parameters of one beRTAMC2D run (<beRTAMC2D> XML,
+ * src/beyondRTA_MC2d.cpp:1299-1462). */
+typedef struct bte_berta_params {
+    double dt;               /* time step, ps                                    */
+    double maxtime;          /* the loop runs while time <= maxtime              */
+    double Eeff;             /* energy per particle, J (<Eeff Ed=...>)          */
+    double T0;               /* equilibrium temperature of the boxes, K          */
+    uint64_t seed;
+    int32_t mode;            /* BTE_MODE_PRODUCTION                              */
+    int32_t rta;             /* 1: RTA scattering (<RTA/>), 0: propagator        */
+    int32_t cancel_every;    /* cancellation period in steps (reference: 4)     */
+    int32_t reserved0;
+    int64_t capacity;        /* particle capacity on the device (0 = auto)       */
+} bte_berta_params;
+
+/* Results of one beRTAMC2D run; per step s = 0..nsteps (s = 0 is the
+ * initial state), the stdout table of src/beyondRTA_MC2d.cpp:2418-2423. */
+typedef struct bte_berta_result {
+    int32_t nboxes;          /* out */
+    int32_t nsteps;          /* out: loop iterations                             */
+    double* ed;              /* [nsteps+1][nboxes] deviational energy density, J m^-3 */
+    double* flux;            /* [nsteps+1][nboxes][2] heat flux, J m^-2 s^-1   */
+    int64_t* nparticles;     /* [nsteps+1] particles alive                       */
+    int32_t* histogram;      /* [nboxes][nmodes] final signed histogram (may be NULL) */
+    int64_t particle_steps;  /* particles advected, summed over steps           */
+    int64_t branchings;      /* sign flips that re-entered the scattering queue  */
+    double kernel_ms;        /* device time of the step loop                     */
+} bte_berta_result;
+
 /* Tuning knobs of the production kernels (project-written autotuner picks
  * them; 0 selects the built-in default). */
 typedef struct bte_tuning {

@@ -52,6 +52,11 @@ def load():
                               C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.oracle_lambert_nnz.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
                                        C.POINTER(C.c_longlong)]
+    lib.oracle_berta_run.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
+                                     C.POINTER(C.c_double), C.c_int, C.POINTER(_bt.BertaParams),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    lib.oracle_berta_run.restype = C.c_int
     lib.oracle_timegrid.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int]
     lib.oracle_timegrid.restype = C.c_int
     _lib = lib
@@ -151,3 +156,31 @@ def lambert_nnz(case: dict) -> np.ndarray:
     if st != 0:
         raise _bt.BteError(st, lib.oracle_last_error().decode())
     return out
+
+
+def berta_run(modes, geom, P, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False):
+    """beRTAMC2D restatement: per-step ed [s, box], flux [s, box, 2], N [s]."""
+    lib = load()
+    ms, k1 = _bt.mode_struct(modes)
+    gs, k2 = _bt.geom_struct(geom)
+    nsteps = _bt.berta_steps(dt, maxtime)
+    nbx = int(geom["nboxes"])
+    n = int(modes["nq"]) * int(modes["nb"])
+    ed = np.zeros((nsteps + 1, nbx))
+    flux = np.zeros((nsteps + 1, nbx, 2))
+    npart = np.zeros(nsteps + 1, dtype=np.int64)
+    H = np.zeros((nbx, n), dtype=np.int32)
+    cnt = np.zeros(3, dtype=np.int64)
+    Pa = np.ascontiguousarray(np.asfortranarray(P).ravel(order="F")) if P is not None else np.zeros(1)
+    nmP = int(P.shape[0]) if P is not None else 0
+    bp = _bt.berta_params(dt, maxtime, Eeff, T0, seed, rta)
+    st = lib.oracle_berta_run(C.byref(ms), C.byref(gs), Pa.ctypes.data_as(C.POINTER(C.c_double)), nmP,
+                              C.byref(bp), ed.ctypes.data_as(C.POINTER(C.c_double)),
+                              flux.ctypes.data_as(C.POINTER(C.c_double)),
+                              npart.ctypes.data_as(C.POINTER(C.c_int64)),
+                              H.ctypes.data_as(C.POINTER(C.c_int32)),
+                              cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    return {"ed": ed, "flux": flux, "nparticles": npart, "H": H, "particle_steps": int(cnt[0]),
+            "branchings": int(cnt[1]), "nsteps": int(cnt[2]) - 1}

@@ -481,6 +481,7 @@ struct WallGen {
     std::vector<double> cdf;  // Isothermal_wall_distribution
     int sign;
     double flux;              // J nm^-2 ps^-1 (get_flux)
+    double cumulsum;          // 1e12 hbar sum(pmf)
 };
 
 struct Sim {
@@ -601,7 +602,7 @@ inline std::size_t bounce(const Sim& S, V2 npout, std::size_t imode, Pcg64& rng)
 
 // Generators of Init_generator, src/RTA_MC2D.cpp:289-418, in the order
 // (reservoir id, injection box id).
-inline void build_generators(Sim& S, double /*T0*/) {
+inline void build_generators(Sim& S, double /*T0*/, bool required = true) {
     S.gens.clear();
     const Modes& m = S.m;
     const double vuc = m.V * S.thickness / m.c;
@@ -630,10 +631,15 @@ inline void build_generators(Sim& S, double /*T0*/) {
             g.sign = (Tw - Te) >= 0 ? 1 : -1;
             g.cdf = fill_cumulative(pmf);
             g.flux = g.sign * (cumulsum / (double(m.nq) * vuc));
+            g.cumulsum = cumulsum;
             S.gens.push_back(std::move(g));
         }
     }
-    if (S.gens.empty()) throw input_error("no isothermal wall generator (no reservoir with a different Teq)");
+    if (S.gens.empty()) {
+        if (required) throw input_error("no isothermal wall generator (no reservoir with a different Teq)");
+        S.energy = 0.;
+        return;
+    }
     std::vector<double> ws;
     double total = 0;
     for (auto& g : S.gens) {
@@ -1028,6 +1034,264 @@ inline void run_particle(const Sim& S, std::size_t pid, uint64_t seed, double ma
     }
 }
 
+
+// ================================================================ beRTAMC2D
+// Restatement of the beRTAMC2D step loop (src/beyondRTA_MC2d.cpp:2138-2425):
+// ballistic advection with absorbing walls (evolparticle :708-970),
+// isothermal-wall injection (Isothermal_walls :446-585), adiabatic diffuse
+// re-emission at the spline-interpolated wall temperature
+// (adiabatic_diffuse_walls :281-435, CubicSpline1D src/interpolation.cpp),
+// propagator scattering with sign branching (Scattering :1073-1210,
+// propagator_H src/collision_operator.cpp:857-903), the RTA alternative
+// (ScatteringRTA :983-1062), the per-box histogram, cancellation every 4th
+// step (:2295-2370) and calculate_prop (:1538-1602).
+//
+// Draws: the reference's `rng` (generators) is pcg64(seed, 0) and its
+// thread-local `rng_` (advection, scattering) is pcg64(seed, 1), consumed in
+// the serial order of a one-thread run.  The gradient source term is zero
+// here (all interior boxes share Teq), as in the benchmark configurations.
+
+// CubicSpline1D: natural cubic spline (src/interpolation.cpp:20-103).
+struct Spline {
+    std::vector<double> a, b, c, d, x0, xs;
+    void build(const std::vector<double>& X, const std::vector<double>& Y) {
+        const int n = int(Y.size()) - 1;
+        const std::size_t N = static_cast<std::size_t>(n);
+        std::vector<double> A(Y), B(N), D(N), h(N), alpha(N), C(N + 1), l(N + 1), mu(N + 1), z(N + 1);
+        for (int i = 0; i < n; i++) h[std::size_t(i)] = X[std::size_t(i) + 1] - X[std::size_t(i)];
+        for (int i = 1; i < n; i++)
+            alpha[std::size_t(i)] = 3. / h[std::size_t(i)] * (A[std::size_t(i) + 1] - A[std::size_t(i)]) -
+                                    3. / h[std::size_t(i) - 1] * (A[std::size_t(i)] - A[std::size_t(i) - 1]);
+        l[0] = 1;
+        mu[0] = 0;
+        z[0] = 0;
+        for (int i = 1; i < n; i++) {
+            const std::size_t k = std::size_t(i);
+            l[k] = 2 * (X[k + 1] - X[k - 1]) - h[k - 1] * mu[k - 1];
+            mu[k] = h[k] / l[k];
+            z[k] = (alpha[k] - h[k - 1] * z[k - 1]) / l[k];
+        }
+        l[std::size_t(n)] = 1;
+        z[std::size_t(n)] = 0;
+        C[std::size_t(n)] = 0;
+        for (int j = n - 1; j >= 0; j--) {
+            const std::size_t k = std::size_t(j);
+            C[k] = z[k] - mu[k] * C[k + 1];
+            B[k] = (A[k + 1] - A[k]) / h[k] - h[k] * (C[k + 1] + 2 * C[k]) / 3;
+            D[k] = (C[k + 1] - C[k]) / (3 * h[k]);
+        }
+        a.assign(A.begin(), A.begin() + n);
+        b = B;
+        c.assign(C.begin(), C.begin() + n);
+        d = D;
+        x0.assign(X.begin(), X.begin() + n);
+        xs.assign(X.begin() + 1, X.end());
+    }
+    double interp(double x) const {
+        std::size_t idx = std::size_t(std::lower_bound(xs.begin(), xs.end(), x) - xs.begin());
+        if (idx >= a.size()) idx--;
+        const double dx = x - x0[idx];
+        return a[idx] + dx * (b[idx] + dx * (c[idx] + d[idx] * dx));
+    }
+};
+
+struct BeParticle {
+    V2 pos;
+    std::size_t mode = 0;  // q * nb + alpha; 0 marks a particle to delete
+    int sign = 1;
+    std::size_t box = 0;
+};
+
+struct BeRun {
+    Sim S;
+    bool rta = false;
+    int nm = 0;                       // propagator size (modes minus the 3 Gamma acoustic)
+    std::vector<double> cumm;         // signed cumulative per column, column-major
+    std::vector<double> resample_cdf; // RTA resampling at T (BE_derivative_distribution)
+    double dt = 0, maxtime = 0, Eeff = 0;
+    std::vector<std::vector<int>> Eborder;   // per box, per border
+    std::vector<std::vector<Spline>> spl;    // J(T) -> T per box, per border
+    std::vector<std::vector<char>> spl_ok;
+};
+
+// propagator_H(b): |b| accumulated and signed by the entry, src/collision_operator.cpp:857-870
+inline void build_cumm(BeRun& R, const double* P) {
+    const std::size_t n = std::size_t(R.nm);
+    R.cumm.resize(n * n);
+    for (std::size_t j = 0; j < n; ++j) {
+        const double* col = P + j * n;
+        double abssum = 0.;
+        for (std::size_t i = 0; i < n; ++i) abssum += std::fabs(col[i]);
+        double acc = 0.;
+        for (std::size_t i = 0; i < n; ++i) {
+            acc += std::fabs(col[i]);
+            R.cumm[j * n + i] = (col[i] < 0.) ? -acc / abssum : acc / abssum;
+        }
+    }
+}
+
+// propagator_H::get: lower_bound on |cumm| (abs_less), sign of the entry,
+// index + 3.
+inline std::pair<int, std::size_t> prop_get(const BeRun& R, std::size_t col, double u) {
+    const double* c = &R.cumm[col * std::size_t(R.nm)];
+    const double* it = std::lower_bound(c, c + R.nm, u,
+                                        [](double a, double b) { return std::fabs(a) < std::fabs(b); });
+    std::size_t im = std::size_t(it - c);
+    if (im >= std::size_t(R.nm)) im = std::size_t(R.nm) - 1;
+    return {c[im] > 0. ? 1 : -1, im + 3};
+}
+
+inline void be_kill(BeParticle& p) { p.mode = 0; }
+
+// evolparticle (beyond RTA), src/beyondRTA_MC2d.cpp:708-970, with the
+// recursion written as a loop.
+inline void be_evolve(BeRun& R, BeParticle& p, V2 v, double dt, Pcg64& rng) {
+    const auto& sys = R.S.sys;
+    for (int guard = 0;; ++guard) {
+        if (guard > 1000000) throw limit_error("advection step cap");
+        const V2 opos = p.pos;
+        const Box& box = sys[p.box];
+        if (box.reservoir) {
+            be_kill(p);
+            return;
+        }
+        V2 rnew = {p.pos.x + dt * v.x, p.pos.y + dt * v.y};
+        if (box.inside(rnew)) {
+            p.pos = rnew;
+            return;
+        }
+        Hit mru;
+        try {
+            mru = get_inter_side(box, p.pos, v, dt);
+        } catch (const geometry_error&) {
+            V2 d = box.center - opos;
+            p.pos = p.pos + (1.0e-6 * d) / norm(d);
+            continue;
+        }
+        double left_time = dt - mru.time;
+        if (almost_equal(left_time, 0.)) left_time = 0.;
+        rnew = mru.rf;
+        V2 reps = rnew + (1.0e-6 * v) / norm(v);
+        std::vector<std::size_t> cboxes, pboxes;
+        for (auto& [ibc, bb] : box.contacts) cboxes.push_back(ibc);
+        for (auto test : cboxes) {
+            if (test == p.box) continue;
+            const double npv = dot(box.contacts.at(test)[0].np, v);
+            if ((sys[test].inside(rnew) || sys[test].inside(reps)) && !almost_equal(npv, 0.) && npv > 0.)
+                pboxes.push_back(test);
+        }
+        if (pboxes.empty()) {
+            std::vector<std::size_t> ids;
+            for (auto& g : sys)
+                if (g.inside(rnew)) ids.push_back(g.id);
+            if (ids.size() > 2) {
+                // correct_corner_problem: winner box and its first outgoing border at rnew
+                std::vector<std::pair<std::size_t, int>> fin;
+                for (auto cnd : ids) {
+                    std::vector<int> bids;
+                    int k = 0;
+                    for (auto& b : sys[cnd].borders) {
+                        if (on_segment(rnew, b.la, b.lb) && dot(b.np, v) > 0.) bids.push_back(k);
+                        k++;
+                    }
+                    if (bids.size() <= 1) fin.push_back({cnd, bids.empty() ? -1 : bids[0]});
+                }
+                if (fin.empty()) throw geometry_error("corner without a candidate box");
+                auto w = fin[std::size_t(uniform_int(rng, 0, int(fin.size()) - 1))];
+                if (w.second < 0) throw geometry_error("corner box without an outgoing border");
+                p.box = w.first;
+                p.pos = rnew;
+                R.Eborder[w.first][std::size_t(w.second)] += p.sign;
+                be_kill(p);
+                return;
+            }
+            std::size_t iborder;
+            if (mru.bids.size() > 1) {
+                std::vector<std::size_t> voidborders;
+                for (int tvb : mru.bids) {
+                    const Border& mb = box.borders[std::size_t(tvb)];
+                    V2 rc = rnew + 1.0e-4 * mb.np;
+                    bool isvoid = true;
+                    for (auto cb : cboxes)
+                        if (sys[cb].inside(rc)) {
+                            isvoid = false;
+                            break;
+                        }
+                    if (isvoid) voidborders.push_back(std::size_t(tvb));
+                }
+                if (voidborders.empty()) throw geometry_error("Error in void borders");
+                iborder = voidborders[std::size_t(uniform_int(rng, 0, int(voidborders.size()) - 1))];
+            } else {
+                iborder = std::size_t(mru.bids.at(0));
+            }
+            R.Eborder[p.box][iborder] += p.sign;
+            be_kill(p);
+            return;
+        } else if (pboxes.size() == 1) {
+            p.box = pboxes[0];
+            p.pos = rnew;
+            dt = left_time;
+            continue;
+        } else {
+            std::vector<std::size_t> pbox2;
+            double tau = 1.0e-6;
+            bool nudged = false;
+            while (true) {
+                V2 rcheck = rnew + tau * v;
+                for (auto PB : pboxes)
+                    if (sys[PB].inside(rcheck)) pbox2.push_back(PB);
+                if (pbox2.empty()) {
+                    tau /= 10.0;
+                    if (tau < 1.0e-15) {
+                        V2 d = box.center - rnew;
+                        p.pos = rnew + (1.0e-6 * d) / norm(d);
+                        dt = left_time;
+                        nudged = true;
+                        break;
+                    }
+                } else {
+                    break;
+                }
+            }
+            if (nudged) continue;
+            p.box = pbox2[std::size_t(uniform_int(rng, 0, int(pbox2.size()) - 1))];
+            p.pos = rnew;
+            dt = left_time;
+            continue;
+        }
+    }
+}
+
+// Random point on a border segment (geom2d_border::get_random_point).
+inline V2 border_point(const Border& b, Pcg64& rng) {
+    for (int tries = 0;; ++tries) {
+        if (tries > 1000) throw limit_error("border point rejection loop");
+        V2 rp = b.p1 + canonical(rng) * b.nd;
+        if (on_segment(rp, b.p1, b.p2)) return rp;
+    }
+}
+
+// Isothermal_wall_distribution pmf (src/sampling.cpp:189-269) for normal n.
+inline double wall_pmf(const Modes& m, V2 n, double Tw, double Te, std::vector<double>& pmf) {
+    pmf.assign(m.n(), 0.);
+    for (std::size_t k = 0; k < m.n(); ++k) {
+        const double vn = n.x * m.vx[k] + n.y * m.vy[k] + 0. * m.vz[k];
+        if (vn <= 0. || almost_equal(0., m.omega[k]))
+            pmf[k] = 0.;
+        else
+            pmf[k] = vn * m.omega[k] * std::fabs(bose_einstein(m.omega[k], Tw) - bose_einstein(m.omega[k], Te));
+    }
+    return 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+}
+
+// Ntogenerate stochastic rounding (src/sampling.cpp:243-260).
+inline std::size_t n_to_generate(double gen, Pcg64& rng) {
+    std::size_t np = std::size_t(gen);
+    const double rem = gen - std::floor(gen);
+    if (canonical(rng) <= rem) np++;
+    return np;
+}
+
 }  // namespace orc
 
 // ---------------------------------------------------------------- C API
@@ -1343,6 +1607,273 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
             for (std::size_t k = 0; k < nk; ++k) out->temperature[k] = gz[k] / (cv / vcorr) + rp->T0;
         if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
         if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
+        return 0;
+    } catch (const orc::input_error& e) {
+        return fail(BTE_ERR_INPUT, e.what());
+    } catch (const orc::value_error& e) {
+        return fail(BTE_ERR_VALUE, e.what());
+    } catch (const orc::limit_error& e) {
+        return fail(BTE_ERR_LIMIT, e.what());
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
+// One beRTAMC2D run (see the restatement above).  P: [nmP*nmP] column-major
+// propagator over modes 3..n-1 (ignored when params->rta).  Outputs per step
+// s = 0..nsteps: ed[s][box] (J m^-3), flux[s][box][2] (J m^-2 s^-1),
+// nparticles[s]; H_out: final histogram [box][mode] (optional).
+int oracle_berta_run(const bte_mode_table* mt, const bte_geometry* gm, const double* P, int nmP,
+                     const bte_berta_params* bp, double* ed_out, double* flux_out,
+                     int64_t* np_out, int32_t* H_out, int64_t* counters) {
+    try {
+        orc::BeRun R;
+        R.S = build_sim(mt, gm);
+        orc::Sim& S = R.S;
+        const orc::Modes& m = S.m;
+        const std::size_t n = m.n(), nbx = S.sys.size();
+        R.rta = bp->rta != 0;
+        R.dt = bp->dt;
+        R.maxtime = bp->maxtime;
+        R.Eeff = bp->Eeff;
+        if (!(R.Eeff > 0.)) return fail(BTE_ERR_INPUT, "Eeff must be positive");
+        if (!R.rta) {
+            if (nmP != int(n) - 3) return fail(BTE_ERR_INPUT, "propagator size must be nmodes - 3");
+            R.nm = nmP;
+            orc::build_cumm(R, P);
+        } else {
+            std::vector<double> pmf(n);
+            for (std::size_t k = 0; k < n; ++k)
+                pmf[k] = m.omega[k] <= 0. ? 0. : orc::bose_einstein_kernel(m.omega[k], bp->T0) * m.w[k];
+            R.resample_cdf = orc::fill_cumulative(pmf);
+        }
+        for (auto& b : S.sys) {
+            R.Eborder.push_back(std::vector<int>(b.borders.size(), 0));
+            R.spl.push_back(std::vector<orc::Spline>(b.borders.size()));
+            R.spl_ok.push_back(std::vector<char>(b.borders.size(), 0));
+        }
+        orc::build_generators(S, bp->T0, false);
+        orc::Pcg64 rng(bp->seed, 0), rng_(bp->seed, 1);
+        const double vuc = m.V * S.thickness / m.c;
+        std::vector<orc::BeParticle> parts;
+        // init_particles (Tinit != Teq), src/beyondRTA_MC2d.cpp:211-269
+        std::vector<double> pmf;
+        for (auto& s : S.sys) {
+            if (s.reservoir || orc::almost_equal(s.Teq, s.Treal)) continue;
+            pmf.assign(n, 0.);
+            for (std::size_t k = 0; k < n; ++k) {
+                const double om = m.omega[k];
+                if (orc::almost_equal(om, 0.)) continue;
+                pmf[k] = om * std::fabs(orc::bose_einstein(om, s.Treal) - orc::bose_einstein(om, s.Teq));
+            }
+            const double cumulsum = 1.0e+12 * orc::hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+            const int sgn = (s.Treal - s.Teq) >= 0 ? 1 : -1;
+            auto cdf = orc::fill_cumulative(pmf);
+            const double vol = s.area * S.thickness / vuc;
+            const std::size_t ngen = orc::n_to_generate(vol * cumulsum / (R.Eeff * double(m.nq)), rng);
+            double x0 = s.hull[0].x, x1 = x0, y0 = s.hull[0].y, y1 = y0;
+            for (auto& h : s.hull) {
+                x0 = std::min(x0, h.x); x1 = std::max(x1, h.x);
+                y0 = std::min(y0, h.y); y1 = std::max(y1, h.y);
+            }
+            for (std::size_t i = 0; i < ngen; ++i) {
+                orc::V2 r;
+                for (int tries = 0;; ++tries) {
+                    if (tries > 100000) throw orc::limit_error("random point rejection loop");
+                    r.x = x0 + orc::canonical(rng) * (x1 - x0);
+                    r.y = y0 + orc::canonical(rng) * (y1 - y0);
+                    if (s.inside(r)) break;
+                }
+                orc::BeParticle p;
+                p.pos = r;
+                p.mode = orc::lower_bound_idx(cdf, orc::canonical(rng));
+                p.sign = sgn;
+                p.box = s.id;
+                parts.push_back(p);
+            }
+        }
+        std::vector<double> vol(nbx);
+        for (std::size_t i = 0; i < nbx; ++i) vol[i] = S.sys[i].area * S.thickness;
+        int64_t step_out = 0, psteps = 0, branches = 0;
+        auto emit_props_particles = [&]() {
+            std::vector<double> ed(nbx, 0.), fx(nbx, 0.), fy(nbx, 0.);
+            for (auto& p : parts) {
+                ed[p.box] += p.sign;
+                fx[p.box] += p.sign * m.vx[p.mode];
+                fy[p.box] += p.sign * m.vy[p.mode];
+            }
+            for (std::size_t i = 0; i < nbx; ++i) {
+                ed_out[step_out * nbx + i] = ed[i] * (R.Eeff / vol[i] * 1.0e+27);
+                flux_out[(step_out * nbx + i) * 2] = fx[i] * (R.Eeff / vol[i] * 1e12 * 1e9 * 1e9);
+                flux_out[(step_out * nbx + i) * 2 + 1] = fy[i] * (R.Eeff / vol[i] * 1e12 * 1e9 * 1e9);
+            }
+            np_out[step_out] = int64_t(parts.size());
+            step_out++;
+        };
+        emit_props_particles();
+        std::vector<int> H(nbx * n);
+        double time = 0.;
+        std::size_t istep = 0;
+        auto advect_new = [&](std::vector<orc::BeParticle>& np) {
+            for (auto& p : np) {
+                const double rdt = R.dt * orc::canonical(rng_);
+                orc::be_evolve(R, p, orc::get_v(m, p.mode), rdt, rng_);
+            }
+            parts.insert(parts.end(), np.begin(), np.end());
+        };
+        while (time <= R.maxtime) {
+            // 1. advection
+            for (auto& p : parts) orc::be_evolve(R, p, orc::get_v(m, p.mode), R.dt, rng_);
+            psteps += int64_t(parts.size());
+            // 3. isothermal walls
+            {
+                std::vector<orc::BeParticle> np;
+                for (auto& g : S.gens) {
+                    const double Lb = orc::norm(g.b.p2 - g.b.p1);
+                    const double spf = Lb * S.thickness / (m.V * S.thickness / m.c);
+                    const std::size_t ngen =
+                        orc::n_to_generate(R.dt * spf * g.cumulsum / (R.Eeff * double(m.nq)), rng);
+                    const orc::Box& inj = S.sys[g.box];
+                    for (std::size_t i = 0; i < ngen; ++i) {
+                        orc::V2 pp = orc::border_point(g.b, rng);
+                        if (!inj.inside(pp)) {
+                            orc::V2 d = inj.center - pp;
+                            pp = pp + (1.0e-6 * d) / orc::norm(d);
+                            if (!inj.inside(pp)) throw orc::geometry_error("Generated particle out of insertion box");
+                        }
+                        orc::BeParticle p;
+                        p.pos = pp;
+                        p.mode = orc::lower_bound_idx(g.cdf, orc::canonical(rng));
+                        p.sign = g.sign;
+                        p.box = g.box;
+                        np.push_back(p);
+                    }
+                }
+                advect_new(np);
+            }
+            // 4. adiabatic diffuse walls
+            {
+                std::vector<orc::BeParticle> np;
+                for (auto& s : S.sys) {
+                    if (s.reservoir) continue;
+                    for (std::size_t k = 0; k < s.borders.size(); ++k) {
+                        const orc::Border& b = s.borders[k];
+                        const orc::V2 nwall = {-b.np.x, -b.np.y};
+                        if (!R.spl_ok[s.id][k]) {
+                            std::vector<double> J(100), Tv(100);
+                            for (int t = 0; t < 100; ++t) {
+                                const double T = 10.0 + 10.0 * t;
+                                Tv[std::size_t(t)] = T;
+                                const double cs = orc::wall_pmf(m, nwall, T, s.Teq, pmf);
+                                const int sg = (T - s.Teq) >= 0 ? 1 : -1;
+                                J[std::size_t(t)] = sg * (cs / (double(m.nq) * vuc));
+                            }
+                            R.spl[s.id][k].build(J, Tv);
+                            R.spl_ok[s.id][k] = 1;
+                        }
+                        int& E = R.Eborder[s.id][k];
+                        if (E != 0) {
+                            const double Jb = R.Eeff * E / R.dt / (orc::norm(b.p2 - b.p1) * S.thickness);
+                            const double Tb = R.spl[s.id][k].interp(Jb);
+                            orc::wall_pmf(m, nwall, Tb, s.Teq, pmf);
+                            auto cdf = orc::fill_cumulative(pmf);
+                            const int sg = (Tb - s.Teq) >= 0 ? 1 : -1;
+                            const std::size_t ng = std::size_t(std::abs(E) + 1.0e-6);
+                            for (std::size_t i = 0; i < ng; ++i) {
+                                orc::BeParticle p;
+                                p.pos = orc::border_point(b, rng);
+                                p.mode = orc::lower_bound_idx(cdf, orc::canonical(rng));
+                                p.sign = sg;
+                                p.box = s.id;
+                                np.push_back(p);
+                            }
+                            E = 0;
+                        }
+                    }
+                }
+                advect_new(np);
+            }
+            // 5. delete
+            parts.erase(std::remove_if(parts.begin(), parts.end(),
+                                       [](const orc::BeParticle& p) { return p.mode == 0; }),
+                        parts.end());
+            // 6. scattering
+            if (R.rta) {
+                for (auto& p : parts) {
+                    const double w = m.w[p.mode];
+                    const double u = orc::canonical(rng_);
+                    if (u < (1 - std::exp(-w * R.dt)))
+                        p.mode = orc::lower_bound_idx(R.resample_cdf, orc::canonical(rng_));
+                }
+            } else {
+                std::vector<orc::BeParticle> elements = parts, out;
+                int rounds = 0;
+                while (!elements.empty()) {
+                    if (++rounds > 4096) throw orc::limit_error("branching rounds cap");
+                    std::vector<orc::BeParticle> next;
+                    for (auto& p : elements) {
+                        if (p.mode < 3) throw orc::value_error("Gamma acoustic particle has no propagator column");
+                        const double u = orc::canonical(rng_);
+                        auto sol = orc::prop_get(R, p.mode - 3, u);
+                        const int newsign = (p.sign * sol.first) < 0 ? -1 : 1;
+                        orc::BeParticle s1 = p;
+                        s1.mode = sol.second;
+                        s1.sign = newsign;
+                        out.push_back(s1);
+                        if (newsign * p.sign < 0) {
+                            next.push_back(p);
+                            next.push_back(p);
+                            branches++;
+                        }
+                    }
+                    elements.swap(next);
+                }
+                parts.swap(out);
+            }
+            // 7. histogram
+            std::fill(H.begin(), H.end(), 0);
+            for (auto& p : parts) H[p.box * n + p.mode] += p.sign;
+            // 8. cancellation every 4th step
+            if (istep % 4 == 0) {
+                std::vector<int> Hc(H);
+                std::stable_sort(parts.begin(), parts.end(), [](const orc::BeParticle& a, const orc::BeParticle& b) {
+                    return std::make_tuple(a.box, a.mode, a.sign) < std::make_tuple(b.box, b.mode, b.sign);
+                });
+                std::vector<orc::BeParticle> kept;
+                for (auto& p : parts) {
+                    if (S.sys[p.box].reservoir) continue;
+                    int& h = Hc[p.box * n + p.mode];
+                    if (h == 0) continue;
+                    if ((p.sign < 0) != (h < 0)) continue;
+                    h -= p.sign;
+                    kept.push_back(p);
+                }
+                parts.swap(kept);
+            }
+            // 9. properties from the histogram
+            for (std::size_t i = 0; i < nbx; ++i) {
+                double e = 0., fx = 0., fy = 0.;
+                for (std::size_t k = 0; k < n; ++k) {
+                    const double hk = double(H[i * n + k]);
+                    e += hk;
+                    fx += hk * m.vx[k];
+                    fy += hk * m.vy[k];
+                }
+                ed_out[step_out * nbx + i] = (R.Eeff / vol[i] * 1.0e+27) * e;
+                flux_out[(step_out * nbx + i) * 2] = (R.Eeff / vol[i] * 1.0e+30) * fx;
+                flux_out[(step_out * nbx + i) * 2 + 1] = (R.Eeff / vol[i] * 1.0e+30) * fy;
+            }
+            np_out[step_out] = int64_t(parts.size());
+            step_out++;
+            istep++;
+            time += R.dt;
+        }
+        if (H_out) std::copy(H.begin(), H.end(), H_out);
+        if (counters) {
+            counters[0] = psteps;
+            counters[1] = branches;
+            counters[2] = step_out;
+        }
         return 0;
     } catch (const orc::input_error& e) {
         return fail(BTE_ERR_INPUT, e.what());
