@@ -27,7 +27,7 @@ SOURCE_WALLS, SOURCE_INITIAL = 0, 1
 # Exported symbols declared in include/btegpu.h.
 PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
-                  "bte_version", "bte_rta_run_noalloc"]
+                  "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run"]
 
 
 class BteError(RuntimeError):
@@ -182,6 +182,10 @@ def load_library(path: str = LIB_PATH):
     lib.bte_query_sizes.argtypes = [vp, C.POINTER(RtaParams), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
     lib.bte_version.restype = C.c_int32
+    lib.bte_load_propagator.argtypes = [vp, C.POINTER(Propagator)]
+    lib.bte_load_propagator.restype = C.c_int
+    lib.bte_berta_run.argtypes = [vp, C.POINTER(BertaParams), C.POINTER(BertaResult)]
+    lib.bte_berta_run.restype = C.c_int
     lib.bte_rta_run_noalloc.argtypes = [vp, C.POINTER(RtaParams), C.c_void_p, C.POINTER(RtaResult)]
     lib.bte_rta_run_noalloc.restype = C.c_int
     for f in ("bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
@@ -265,6 +269,40 @@ class Engine:
                   "specular_hits", "tally_updates", "kernel_ms"):
             out[k] = getattr(r, k)
         return out
+
+
+def _engine_load_propagator(self, P: np.ndarray, T: float = 300.0):
+    """Propagator over modes 3..n-1, column j = outgoing distribution of mode j + 3."""
+    Pf = np.asfortranarray(P, dtype=np.float64)
+    flat = np.ascontiguousarray(Pf.ravel(order="F"))
+    s = Propagator(int(P.shape[0]), float(T), _dptr(flat))
+    self._check(self.lib.bte_load_propagator(self.ctx, C.byref(s)))
+
+
+def _engine_berta_run(self, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, cancel_every=4,
+                      capacity=0, histogram=False):
+    """beRTAMC2D loop: per step ed [s, box] (J m^-3), flux [s, box, 2], N [s]."""
+    p = berta_params(dt, maxtime, Eeff, T0, seed, rta, MODE_PRODUCTION, cancel_every, capacity)
+    nsteps = berta_steps(dt, maxtime)
+    nbx = self.nboxes
+    ed = np.zeros((nsteps + 1, nbx))
+    flux = np.zeros((nsteps + 1, nbx, 2))
+    npart = np.zeros(nsteps + 1, dtype=np.int64)
+    r = BertaResult()
+    r.ed, r.flux = _dptr(ed), _dptr(flux)
+    r.nparticles = npart.ctypes.data_as(C.POINTER(C.c_int64))
+    H = None
+    if histogram:
+        n = int(self._keep["modes"]["omega"].size)
+        H = np.zeros((nbx, n), dtype=np.int32)
+        r.histogram = H.ctypes.data_as(C.POINTER(C.c_int32))
+    self._check(self.lib.bte_berta_run(self.ctx, C.byref(p), C.byref(r)))
+    return {"ed": ed, "flux": flux, "nparticles": npart, "H": H, "nsteps": r.nsteps,
+            "particle_steps": r.particle_steps, "branchings": r.branchings, "kernel_ms": r.kernel_ms}
+
+
+Engine.load_propagator = _engine_load_propagator
+Engine.berta_run = _engine_berta_run
 
 
 def debug_geometry(g: dict) -> np.ndarray:

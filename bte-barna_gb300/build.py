@@ -25,6 +25,7 @@ UNITS = [
     ("rta_prod.cu", []),
     ("capi.cu", []),
     ("noalloc.cu", []),
+    ("berta.cu", []),
 ]
 
 

@@ -1,0 +1,917 @@
+// berta.cu - beyond-RTA deviational MC (beRTAMC2D) on the device.
+//
+// The step loop of src/beyondRTA_MC2d.cpp:2138-2425, production mode:
+//   1 advection by dt; void walls absorb and count Eborder, reservoirs absorb
+//     (evolparticle :708-970)                                      be_advect
+//   3 isothermal-wall injection, random sub-step            be_generate
+//     (Isothermal_walls :446-585, Ntogenerate src/sampling.cpp:243-260)
+//   4 adiabatic diffuse re-emission of |Eborder| at the wall temperature from
+//     the J(T) cubic spline (adiabatic_diffuse_walls :281-435)    be_generate
+//   5 deletion                                                  be_compact
+//   6 propagator scattering with sign branching (Scattering :1073-1210,
+//     propagator_H::get src/collision_operator.cpp:892-903), or the RTA
+//     alternative (ScatteringRTA :983-1062)          be_scatter / be_scatter_rta
+//   7 histogram H[box][mode] += sign                            be_hist
+//   8 cancellation every 4th step: keep |H| particles of the majority sign
+//     per (box, mode) (:2295-2370), by per-key ranks, no sort   be_cancel
+//   9 calculate_prop: ed and flux per box from H (:1538-1602)   be_props
+// Particles live in HBM as structure-of-arrays (x, y FP64; mode, box, sign
+// int32).  Draws: Philox4x32-10 keyed by (seed, step, phase), counter =
+// particle index.  Geometry: boxes that tile an axis-aligned grid.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+
+namespace bte {
+
+struct PArr {
+    double* x;
+    double* y;
+    int* mode;
+    int* box;
+    int* sign;
+};
+
+// A particle source of one step: a border segment (walls) or a box
+// rectangle (initial deviation), a sign, a mode distribution (alias table at
+// `alias_off` of the step's alias buffer) and its particles [first, first+n).
+struct GenDesc {
+    double x0, y0, dx, dy;  // border: p1 + u (dx, dy); rectangle: x0 + u dx, y0 + v dy
+    int box, sign, rect, pad;
+    long long alias_off;
+    long long first;
+};
+
+// Propagator alias entry: slot j keeps outgoing mode j+3 with probability
+// prob, else takes alt; the two top bits carry the signs of P at the kept
+// and alternative slots.
+struct PAlias {
+    float prob;
+    unsigned alt;  // bits 0-29 slot, bit 30 alt negative, bit 31 keep negative
+};
+
+struct BertaState {
+    bool have_prop = false;
+    int nm = 0;
+    double T = 0;
+    DBuf d_palias;
+    long long cap = 0;
+    DBuf a_x, a_y, a_mode, a_box, a_sign;   // particles
+    DBuf b_x, b_y, b_mode, b_box, b_sign;   // compaction / scattering output
+    DBuf q_x, q_y, q_mode, q_box, q_sign;   // branching queues (two halves)
+    DBuf d_H, d_cnt, d_Eb, d_props, d_counts, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
+    std::vector<Spline1D> spl;
+    std::vector<char> spl_ok;
+};
+
+void destroy_berta(bte_ctx* c) {
+    delete c->berta;
+    c->berta = nullptr;
+}
+
+namespace {
+
+__device__ __forceinline__ long long obits(double x) { return __double_as_longlong(x); }
+
+__device__ __forceinline__ int grid_at(const DevGrid& G, int i, int j) {
+    if (i < 0 || j < 0 || i >= G.nx || j >= G.ny) return -1;
+    return __ldg(G.cell + i * G.ny + j);
+}
+
+// Ballistic advection of one particle for time `dt` on the grid.  Returns
+// false when it was absorbed (mode set to -1): at a void wall its signed
+// count goes to the wall's Eborder, at a reservoir it is dropped.
+__device__ bool advect_one(const DevGrid& G, const int2* boxcell, const ModeVel* mv, const int4* boxwall,
+                           int* Eb, double& x, double& y, int& box, int mode, int sign, double dt) {
+    const ModeVel v = mv[mode];
+    const int2 ij = __ldg(boxcell + box);
+    int i = ij.x, j = ij.y;
+    for (int guard = 0; guard < (1 << 20); ++guard) {
+        const int upx = obits(v.vx) >= 0 ? 1 : 0, upy = obits(v.vy) >= 0 ? 1 : 0;
+        const double xw = __ldg(G.gx + i + upx), yw = __ldg(G.gy + j + upy);
+        const double tx = (xw - x) * v.ivx, ty = (yw - y) * v.ivy;
+        const bool xfirst = obits(tx) <= obits(ty);
+        const long long te_b = xfirst ? obits(tx) : obits(ty);
+        if (!(obits(dt) > te_b)) {  // stays in the cell
+            x = fma(dt, v.vx, x);
+            y = fma(dt, v.vy, y);
+            return true;
+        }
+        const double seg = __longlong_as_double(te_b > 0 ? te_b : 0);
+        double nx = fma(seg, v.vx, x), ny = fma(seg, v.vy, y);
+        int ni = i, nj = j, wall;
+        if (xfirst) {
+            nx = xw;
+            ni = i + (upx ? 1 : -1);
+            wall = upx ? 0 : 1;
+        } else {
+            ny = yw;
+            nj = j + (upy ? 1 : -1);
+            wall = upy ? 2 : 3;
+        }
+        x = nx;
+        y = ny;
+        dt -= seg;
+        const int nb = grid_at(G, ni, nj);
+        if (nb >= 0) {
+            i = ni;
+            j = nj;
+            box = nb;
+            continue;
+        }
+        if (nb == -1) {  // void wall: absorbed, counted on the wall
+            const int4 bw = __ldg(boxwall + box);
+            const int gb = wall == 0 ? bw.x : wall == 1 ? bw.y : wall == 2 ? bw.z : bw.w;
+            if (gb >= 0) atomicAdd(Eb + gb, sign);
+        }
+        return false;
+    }
+    return false;
+}
+
+struct AdvectArgs {
+    DevGrid G;
+    const int2* boxcell;
+    const ModeVel* mv;
+    const int4* boxwall;
+    int* Eb;
+    double dt;
+    unsigned long long key;  // Philox key of the random sub-steps
+    int random_substep;
+};
+
+__global__ void be_advect(PArr P, long long begin, long long end, AdvectArgs a) {
+    for (long long i = begin + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < end;
+         i += (long long)gridDim.x * blockDim.x) {
+        int mode = P.mode[i];
+        if (mode < 0) continue;
+        double dt = a.dt;
+        if (a.random_substep) {
+            Philox g;
+            g.init(a.key, (uint64_t)i);
+            dt = a.dt * g.uniform();
+        }
+        double x = P.x[i], y = P.y[i];
+        int box = P.box[i];
+        if (!advect_one(a.G, a.boxcell, a.mv, a.boxwall, a.Eb, x, y, box, mode, P.sign[i], dt))
+            mode = -1;
+        P.x[i] = x;
+        P.y[i] = y;
+        P.box[i] = box;
+        P.mode[i] = mode;
+    }
+}
+
+// New particles [base, base + n) from the step's sources.
+__global__ void be_generate(PArr P, long long base, long long n, const GenDesc* gens, int ngen,
+                            const float* aprob, const int* aalt, int nmodes, unsigned long long key) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = ngen;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (gens[mid].first <= k) lo = mid; else hi = mid;
+        }
+        const GenDesc gd = gens[lo];
+        Philox g;
+        g.init(key, (uint64_t)k);
+        double x, y;
+        if (gd.rect) {
+            x = gd.x0 + g.uniform() * gd.dx;
+            y = gd.y0 + g.uniform() * gd.dy;
+        } else {
+            const double u = g.uniform();
+            x = gd.x0 + u * gd.dx;
+            y = gd.y0 + u * gd.dy;
+        }
+        const float* pr = aprob + gd.alias_off;
+        const int* al = aalt + gd.alias_off;
+        const int j = int(mulhi32(g.next32(), uint32_t(nmodes)));
+        const float acc = float(g.next32() >> 8) * 0x1p-24f;
+        const int mode = acc < __ldg(pr + j) ? j : __ldg(al + j);
+        const long long i = base + k;
+        P.x[i] = x;
+        P.y[i] = y;
+        P.box[i] = gd.box;
+        P.mode[i] = mode;
+        P.sign[i] = gd.sign;
+    }
+}
+
+// Append the live particles of [0, n) to `out` (warp-aggregated).
+__global__ void be_compact(PArr in, long long n, PArr out, unsigned long long* count) {
+    const int lane = threadIdx.x & 31;
+    for (long long base = blockIdx.x * (long long)blockDim.x; base < n;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long i = base + threadIdx.x;
+        const bool live = i < n && in.mode[i] >= 0;
+        const unsigned m = __ballot_sync(0xffffffffu, live);
+        unsigned long long w = 0;
+        if (lane == 0 && m) w = atomicAdd(count, (unsigned long long)__popc(m));
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (live) {
+            const long long o = (long long)w + __popc(m & ((1u << lane) - 1u));
+            out.x[o] = in.x[i];
+            out.y[o] = in.y[i];
+            out.mode[o] = in.mode[i];
+            out.box[o] = in.box[i];
+            out.sign[o] = in.sign[i];
+        }
+    }
+}
+
+// One branching round of the propagator scattering: every input particle
+// draws its next mode from its column; the outgoing particle is appended to
+// `out`; a sign flip sends two copies of the parent to `queue`.
+__global__ void be_scatter(PArr in, long long n, PArr out, unsigned long long* ocount, long long ocap,
+                           PArr queue, unsigned long long* qcount, long long qcap, const PAlias* pal,
+                           int nm, unsigned long long key, int* err) {
+    const int lane = threadIdx.x & 31;
+    for (long long base = blockIdx.x * (long long)blockDim.x; base < n;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long i = base + threadIdx.x;
+        const bool on = i < n;
+        int mode = 0, sign = 1, box = 0, nmode = 0, nsign = 1;
+        double x = 0., y = 0.;
+        if (on) {
+            mode = in.mode[i];
+            sign = in.sign[i];
+            box = in.box[i];
+            x = in.x[i];
+            y = in.y[i];
+            const int col = mode - 3;
+            if (col < 0 || col >= nm) {
+                atomicCAS(err, 0, E_VALUE);
+                nmode = mode;
+                nsign = sign;
+            } else {
+                Philox g;
+                g.init(key, (uint64_t)i);
+                const int j = int(mulhi32(g.next32(), uint32_t(nm)));
+                const float acc = float(g.next32() >> 8) * 0x1p-24f;
+                const PAlias e = pal[(long long)col * nm + j];
+                const bool keep = acc < e.prob;
+                const int slot = keep ? j : int(e.alt & 0x3fffffffu);
+                const bool neg = keep ? (e.alt >> 31) != 0u : ((e.alt >> 30) & 1u) != 0u;
+                nmode = slot + 3;
+                nsign = neg ? -sign : sign;
+            }
+        }
+        // append the outgoing particle
+        const unsigned m1 = __ballot_sync(0xffffffffu, on);
+        unsigned long long w = 0;
+        if (lane == 0 && m1) w = atomicAdd(ocount, (unsigned long long)__popc(m1));
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (on) {
+            const long long o = (long long)w + __popc(m1 & ((1u << lane) - 1u));
+            if (o < ocap) {
+                out.x[o] = x;
+                out.y[o] = y;
+                out.box[o] = box;
+                out.mode[o] = nmode;
+                out.sign[o] = nsign;
+            } else {
+                atomicCAS(err, 0, E_LIMIT);
+            }
+        }
+        // a sign flip re-enters two copies of the parent
+        const bool flip = on && nsign != sign;
+        const unsigned m2 = __ballot_sync(0xffffffffu, flip);
+        unsigned long long q = 0;
+        if (lane == 0 && m2) q = atomicAdd(qcount, 2ull * __popc(m2));
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (flip) {
+            const long long o = (long long)q + 2ll * __popc(m2 & ((1u << lane) - 1u));
+            if (o + 1 < qcap) {
+                for (int c2 = 0; c2 < 2; ++c2) {
+                    queue.x[o + c2] = x;
+                    queue.y[o + c2] = y;
+                    queue.box[o + c2] = box;
+                    queue.mode[o + c2] = mode;
+                    queue.sign[o + c2] = sign;
+                }
+            } else {
+                atomicCAS(err, 0, E_LIMIT);
+            }
+        }
+    }
+}
+
+// RTA scattering: with probability 1 - exp(-w dt) a particle is resampled
+// from the C w distribution.
+__global__ void be_scatter_rta(PArr P, long long n, const double* w, double dt, const float* rprob,
+                               const int* ralt, int nmodes, unsigned long long key) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int mode = P.mode[i];
+        Philox g;
+        g.init(key, (uint64_t)i);
+        const double u = g.uniform();
+        if (u < 1. - exp(-__ldg(w + mode) * dt)) {
+            const int j = int(mulhi32(g.next32(), uint32_t(nmodes)));
+            const float acc = float(g.next32() >> 8) * 0x1p-24f;
+            P.mode[i] = acc < __ldg(rprob + j) ? j : __ldg(ralt + j);
+        }
+    }
+}
+
+__global__ void be_hist(PArr P, long long n, int* H, int nmodes) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        atomicAdd(H + (long long)P.box[i] * nmodes + P.mode[i], P.sign[i]);
+}
+
+// Cancellation: a particle survives when its sign is the sign of H at its
+// (box, mode) and its rank among those particles is below |H|.
+__global__ void be_cancel(PArr P, long long n, const int* H, int* cnt, int nmodes, const int* reservoir) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long key = (long long)P.box[i] * nmodes + P.mode[i];
+        const int h = H[key];
+        const int s = P.sign[i];
+        bool keep = !reservoir[P.box[i]] && h != 0 && ((s < 0) == (h < 0));
+        if (keep) keep = atomicAdd(cnt + key, 1) < (h < 0 ? -h : h);
+        if (!keep) P.mode[i] = -1;
+    }
+}
+
+// ed, flux_x, flux_y sums of one box (raw velocities, as calculate_prop).
+__global__ void be_props(const int* H, int nmodes, const double* vx, const double* vy, double* out) {
+    const int box = blockIdx.x;
+    double e = 0., fx = 0., fy = 0.;
+    for (int k = threadIdx.x; k < nmodes; k += blockDim.x) {
+        const double h = double(H[(long long)box * nmodes + k]);
+        e += h;
+        fx += h * vx[k];
+        fy += h * vy[k];
+    }
+    __shared__ double red[3][256];
+    red[0][threadIdx.x] = e;
+    red[1][threadIdx.x] = fx;
+    red[2][threadIdx.x] = fy;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 3; ++q) out[3 * box + q] = red[q][0];
+}
+
+PArr arr(DBuf& x, DBuf& y, DBuf& m, DBuf& b, DBuf& s, long long off = 0) {
+    return PArr{x.as<double>() + off, y.as<double>() + off, m.as<int>() + off, b.as<int>() + off,
+                s.as<int>() + off};
+}
+
+void alloc_particles(BertaState& B, long long cap) {
+    if (B.cap >= cap) return;
+    for (DBuf* d : {&B.a_x, &B.a_y, &B.b_x, &B.b_y})
+        d->alloc(size_t(cap) * sizeof(double));
+    for (DBuf* d : {&B.a_mode, &B.a_box, &B.a_sign, &B.b_mode, &B.b_box, &B.b_sign})
+        d->alloc(size_t(cap) * sizeof(int));
+    for (DBuf* d : {&B.q_x, &B.q_y}) d->alloc(size_t(2 * cap) * sizeof(double));
+    for (DBuf* d : {&B.q_mode, &B.q_box, &B.q_sign}) d->alloc(size_t(2 * cap) * sizeof(int));
+    B.cap = cap;
+}
+
+unsigned long long mix_key(unsigned long long seed, long long step, int phase) {
+    unsigned long long k = seed ^ (0x9E3779B97F4A7C15ull * (unsigned long long)(step + 1));
+    k ^= (unsigned long long)phase << 56;
+    return k;
+}
+
+int launch_blocks(long long n, int nsm) {
+    long long b = (n + 255) / 256;
+    const long long cap = (long long)nsm * 8;
+    if (b > cap) b = cap;
+    return int(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+// Natural cubic spline (CubicSpline1D, src/interpolation.cpp:20-103).
+void Spline1D::build(const std::vector<double>& X, const std::vector<double>& Y) {
+    const int n = int(Y.size()) - 1;
+    const std::size_t N = static_cast<std::size_t>(n);
+    std::vector<double> A(Y), Bv(N), D(N), h(N), alpha(N), C(N + 1), l(N + 1), mu(N + 1), z(N + 1);
+    for (std::size_t i = 0; i < N; i++) h[i] = X[i + 1] - X[i];
+    for (std::size_t i = 1; i < N; i++)
+        alpha[i] = 3. / h[i] * (A[i + 1] - A[i]) - 3. / h[i - 1] * (A[i] - A[i - 1]);
+    l[0] = 1;
+    mu[0] = 0;
+    z[0] = 0;
+    for (std::size_t i = 1; i < N; i++) {
+        l[i] = 2 * (X[i + 1] - X[i - 1]) - h[i - 1] * mu[i - 1];
+        mu[i] = h[i] / l[i];
+        z[i] = (alpha[i] - h[i - 1] * z[i - 1]) / l[i];
+    }
+    l[N] = 1;
+    z[N] = 0;
+    C[N] = 0;
+    for (int jj = n - 1; jj >= 0; jj--) {
+        const std::size_t k = std::size_t(jj);
+        C[k] = z[k] - mu[k] * C[k + 1];
+        Bv[k] = (A[k + 1] - A[k]) / h[k] - h[k] * (C[k + 1] + 2 * C[k]) / 3;
+        D[k] = (C[k + 1] - C[k]) / (3 * h[k]);
+    }
+    a.assign(A.begin(), A.begin() + n);
+    b = Bv;
+    c.assign(C.begin(), C.begin() + n);
+    d = D;
+    x0.assign(X.begin(), X.begin() + n);
+    xs.assign(X.begin() + 1, X.end());
+}
+
+double Spline1D::interp(double x) const {
+    std::size_t idx = std::size_t(std::lower_bound(xs.begin(), xs.end(), x) - xs.begin());
+    if (idx >= a.size()) idx--;
+    const double dx = x - x0[idx];
+    return a[idx] + dx * (b[idx] + dx * (c[idx] + d[idx] * dx));
+}
+
+}  // namespace bte
+
+using bte::Error;
+
+extern "C" bte_status bte_load_propagator(bte_ctx* c, const bte_propagator* P) {
+    if (!c) return BTE_ERR_INPUT;
+    try {
+        if (!P || !P->P || P->nmodes < 1) throw Error(BTE_ERR_INPUT, "empty propagator");
+        if (!c->have_modes) throw Error(BTE_ERR_STATE, "load the mode table before the propagator");
+        if (std::size_t(P->nmodes) + 3 != c->modes.n())
+            throw Error(BTE_ERR_INPUT, "propagator size must be the number of modes minus 3");
+        bte::ck(cudaSetDevice(c->device), "cudaSetDevice");
+        if (!c->berta) c->berta = new bte::BertaState();
+        bte::BertaState& B = *c->berta;
+        const int nm = P->nmodes;
+        // propagator_H per column: |P| weights, sign of each entry
+        // (src/collision_operator.cpp:857-870); sampled by alias here
+        std::vector<bte::PAlias> tab(std::size_t(nm) * nm);
+        std::vector<double> w(static_cast<std::size_t>(nm));
+        std::vector<bte::Alias> al(static_cast<std::size_t>(nm));
+        for (int j = 0; j < nm; ++j) {
+            const double* col = P->P + std::size_t(j) * nm;
+            for (int i = 0; i < nm; ++i) {
+                if (!std::isfinite(col[i])) throw Error(BTE_ERR_VALUE, "non-finite propagator entry");
+                w[std::size_t(i)] = std::fabs(col[i]);
+            }
+            bte::alias_table(w.data(), nm, al.data());
+            for (int i = 0; i < nm; ++i) {
+                bte::PAlias e;
+                e.prob = al[std::size_t(i)].prob;
+                const int alt = al[std::size_t(i)].alt;
+                e.alt = unsigned(alt) | (col[alt] < 0. ? (1u << 30) : 0u) | (col[i] < 0. ? (1u << 31) : 0u);
+                tab[std::size_t(j) * nm + std::size_t(i)] = e;
+            }
+        }
+        B.d_palias.upload(tab, c->stream);
+        bte::sync(c);
+        B.nm = nm;
+        B.T = P->T;
+        B.have_prop = true;
+        return BTE_OK;
+    } catch (const Error& e) {
+        c->err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        c->err = e.what();
+        return BTE_ERR_CUDA;
+    }
+}
+
+namespace {
+
+std::size_t n_to_generate(double gen, bte::Pcg64& rng) {
+    std::size_t np = std::size_t(gen);
+    if (bte::canonical_from(rng.next()) <= gen - std::floor(gen)) np++;
+    return np;
+}
+
+// Isothermal_wall_distribution pmf for normal n (src/sampling.cpp:189-269);
+// returns cumulsum = 1e12 hbar sum(pmf).
+double wall_pmf(const bte::HostModes& m, bte::V2 n, double Tw, double Te, std::vector<double>& pmf) {
+    pmf.assign(m.n(), 0.);
+    for (std::size_t k = 0; k < m.n(); ++k) {
+        const double vn = n.x * m.vx[k] + n.y * m.vy[k] + 0. * m.vz[k];
+        if (vn <= 0. || bte::almost_equal(0., m.omega[k]))
+            pmf[k] = 0.;
+        else
+            pmf[k] = vn * m.omega[k] *
+                     std::fabs(bte::bose_einstein(m.omega[k], Tw) - bte::bose_einstein(m.omega[k], Te));
+    }
+    double s = 0.;
+    for (double x : pmf) s += x;
+    return 1.0e+12 * 1.054571726e-34 * s;
+}
+
+}  // namespace
+
+extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_berta_result* out) {
+    using namespace bte;
+    if (!c || !p || !out) return BTE_ERR_INPUT;
+    try {
+        if (!(p->dt > 0.) || !(p->maxtime >= 0.) || !(p->Eeff > 0.) || !(p->T0 > 0.))
+            throw Error(BTE_ERR_INPUT, "dt, Eeff and T0 must be positive and maxtime >= 0");
+        if (p->mode != BTE_MODE_PRODUCTION)
+            throw Error(BTE_ERR_INPUT, "beyond-RTA runs support the production mode only");
+        if (!c->have_modes || !c->have_geom) throw Error(BTE_ERR_STATE, "load modes and geometry first");
+        if (!p->rta && (!c->berta || !c->berta->have_prop))
+            throw Error(BTE_ERR_STATE, "load a propagator (or set rta) before a beyond-RTA run");
+        ck(cudaSetDevice(c->device), "cudaSetDevice");
+        ensure_static(c);
+        const HostModes& m = c->modes;
+        const HostGeometry& g = c->geom;
+        if (!g.rect_grid) throw Error(BTE_ERR_INPUT, "beyond-RTA runs need boxes that tile an axis-aligned grid");
+        for (std::size_t b = 0; b < g.boxes.size(); ++b)
+            if (!g.reservoir[b] && g.Teq[b] != p->T0)
+                throw Error(BTE_ERR_INPUT, "every box needs Teq = T0 (no gradient source term)");
+        if (p->rta) ensure_resample(c, p->T0);
+        if (!c->berta) c->berta = new BertaState();
+        BertaState& B = *c->berta;
+        const int n = int(m.n());
+        const int nbx = int(g.boxes.size());
+        const int nborders = int(g.borders.size());
+        const double vuc = m.V * g.thickness / m.c;
+        cudaStream_t s = c->stream;
+        // walls of each box: global border index of its +x, -x, +y, -y border
+        std::vector<int4> boxwall(std::size_t(nbx), make_int4(-1, -1, -1, -1));
+        for (int b = 0; b < nbx; ++b) {
+            const GBox& bx = g.boxes[std::size_t(b)];
+            for (int k = 0; k < bx.nborders; ++k) {
+                const V2 np = g.borders[std::size_t(bx.border_off + k)].np;
+                const int gb = bx.border_off + k;
+                if (np.x == 1. && np.y == 0.) boxwall[std::size_t(b)].x = gb;
+                if (np.x == -1. && np.y == 0.) boxwall[std::size_t(b)].y = gb;
+                if (np.x == 0. && np.y == 1.) boxwall[std::size_t(b)].z = gb;
+                if (np.x == 0. && np.y == -1.) boxwall[std::size_t(b)].w = gb;
+            }
+        }
+        std::vector<int> border_box(std::size_t(nborders), -1);
+        for (int b = 0; b < nbx; ++b)
+            for (int k = 0; k < g.boxes[std::size_t(b)].nborders; ++k)
+                border_box[std::size_t(g.boxes[std::size_t(b)].border_off + k)] = b;
+        B.d_boxwall.upload(boxwall, s);
+        B.d_Eb.alloc(std::size_t(nborders) * sizeof(int));
+        ck(cudaMemsetAsync(B.d_Eb.p, 0, std::size_t(nborders) * sizeof(int), s), "memset");
+        if (int(B.spl.size()) != nborders) {
+            B.spl.assign(std::size_t(nborders), Spline1D());
+            B.spl_ok.assign(std::size_t(nborders), 0);
+        }
+        B.d_rvx.upload(m.vx, s);
+        B.d_rvy.upload(m.vy, s);
+        B.d_H.alloc(std::size_t(nbx) * n * sizeof(int));
+        B.d_cnt.alloc(std::size_t(nbx) * n * sizeof(int));
+        B.d_props.alloc(std::size_t(nbx) * 3 * sizeof(double));
+        B.d_counts.alloc(4 * sizeof(unsigned long long));
+        c->d_err.alloc(4 * sizeof(int));
+        ck(cudaMemsetAsync(c->d_err.p, 0, 4 * sizeof(int), s), "memset");
+        std::vector<int> hres(g.reservoir.begin(), g.reservoir.end());
+        DBuf d_res;
+        d_res.upload(hres, s);
+        const long long cap = p->capacity > 0 ? p->capacity : (1ll << 24);
+        alloc_particles(B, cap);
+        // sources: isothermal walls (static tables) and the initial deviation
+        Generators iso;
+        try {
+            iso = build_wall_generators(m, g);
+        } catch (const Error&) {
+            iso = Generators();
+        }
+        Generators ini;
+        bool have_ini = false;
+        try {
+            ini = build_initial_generators(m, g);
+            have_ini = true;
+        } catch (const Error&) {
+            have_ini = false;
+        }
+        std::vector<std::pair<int, int>> cellof(std::size_t(nbx), {-1, -1});
+        for (int i = 0; i < g.gnx; ++i)
+            for (int j = 0; j < g.gny; ++j) {
+                const int v = g.gcell[std::size_t(i) * g.gny + j];
+                const int b = v >= 0 ? v : (v <= -2 ? -2 - v : -1);
+                if (b >= 0) cellof[std::size_t(b)] = {i, j};
+            }
+        Pcg64 rng;
+        rng.seed(p->seed, 0);
+        const GridArgs GA = [&] {
+            GridArgs A{};
+            A.G.nx = g.gnx;
+            A.G.ny = g.gny;
+            A.G.gx = c->d_gx.as<double>();
+            A.G.gy = c->d_gy.as<double>();
+            A.G.cell = c->d_gcell.as<int>();
+            A.boxcell = c->d_boxcell.as<int2>();
+            A.mv = c->d_mv.as<ModeVel>();
+            return A;
+        }();
+        auto* counts = B.d_counts.as<unsigned long long>();
+        int* err = c->d_err.as<int>();
+        std::vector<float> aprob;
+        std::vector<int> aalt;
+        std::vector<GenDesc> descs;
+        // generate the sources in `descs` (alias rows in aprob/aalt) at A[base..)
+        auto generate = [&](long long base, long long total, long long step, int phase, bool advect) {
+            if (total <= 0) return;
+            if (base + total > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded: raise capacity");
+            B.d_gens.upload(descs, s);
+            B.d_alias.alloc(aprob.size() * sizeof(float) + aalt.size() * sizeof(int));
+            ck(cudaMemcpyAsync(B.d_alias.p, aprob.data(), aprob.size() * sizeof(float), cudaMemcpyHostToDevice, s), "h2d");
+            int* dalt = reinterpret_cast<int*>(B.d_alias.as<char>() + aprob.size() * sizeof(float));
+            ck(cudaMemcpyAsync(dalt, aalt.data(), aalt.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
+            PArr A = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
+            be_generate<<<launch_blocks(total, c->nsm), 256, 0, s>>>(
+                A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), B.d_alias.as<float>(), dalt, n,
+                mix_key(p->seed, step, phase));
+            if (advect) {
+                AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt,
+                              mix_key(p->seed, step, phase + 1), 1};
+                be_advect<<<launch_blocks(total, c->nsm), 256, 0, s>>>(A, base, base + total, aa);
+            }
+        };
+        auto add_alias_row = [&](const std::vector<double>& w) {
+            const long long off = (long long)aprob.size();
+            std::vector<Alias> al(static_cast<std::size_t>(n));
+            alias_table(w.data(), n, al.data());
+            for (auto& e : al) {
+                aprob.push_back(e.prob);
+                aalt.push_back(e.alt);
+            }
+            return off;
+        };
+        auto read_count = [&](int k) {
+            unsigned long long v = 0;
+            ck(cudaMemcpyAsync(&v, counts + k, sizeof v, cudaMemcpyDeviceToHost, s), "d2h");
+            sync(c);
+            return (long long)v;
+        };
+        auto compact = [&](long long nn) {
+            ck(cudaMemsetAsync(counts, 0, sizeof(unsigned long long), s), "memset");
+            if (nn > 0)
+                be_compact<<<launch_blocks(nn, c->nsm), 256, 0, s>>>(
+                    arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), nn,
+                    arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), counts);
+            const long long m2 = read_count(0);
+            std::swap(B.a_x.p, B.b_x.p);
+            std::swap(B.a_y.p, B.b_y.p);
+            std::swap(B.a_mode.p, B.b_mode.p);
+            std::swap(B.a_box.p, B.b_box.p);
+            std::swap(B.a_sign.p, B.b_sign.p);
+            return m2;
+        };
+        std::vector<double> hprops(std::size_t(nbx) * 3);
+        std::vector<double> vol(static_cast<std::size_t>(nbx));
+        for (int b = 0; b < nbx; ++b) vol[std::size_t(b)] = g.boxes[std::size_t(b)].area * g.thickness;
+        auto props = [&](long long nn, int sidx) {
+            ck(cudaMemsetAsync(B.d_H.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
+            if (nn > 0)
+                be_hist<<<launch_blocks(nn, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
+                                                                  nn, B.d_H.as<int>(), n);
+            be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),
+                                          B.d_props.as<double>());
+            ck(cudaMemcpyAsync(hprops.data(), B.d_props.p, hprops.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "d2h");
+            sync(c);
+            for (int b = 0; b < nbx; ++b) {
+                const double f1 = p->Eeff / vol[std::size_t(b)] * 1.0e+27;
+                const double f2 = p->Eeff / vol[std::size_t(b)] * 1.0e+30;
+                if (out->ed) out->ed[std::size_t(sidx) * nbx + b] = f1 * hprops[3 * std::size_t(b)];
+                if (out->flux) {
+                    out->flux[(std::size_t(sidx) * nbx + b) * 2] = f2 * hprops[3 * std::size_t(b) + 1];
+                    out->flux[(std::size_t(sidx) * nbx + b) * 2 + 1] = f2 * hprops[3 * std::size_t(b) + 2];
+                }
+            }
+            if (out->nparticles) out->nparticles[sidx] = nn;
+        };
+        ck(cudaEventRecord(c->ev0, s), "event");
+        // initial deviation (init_particles, src/beyondRTA_MC2d.cpp:211-269)
+        long long np = 0;
+        descs.clear();
+        aprob.clear();
+        aalt.clear();
+        if (have_ini) {
+            long long first = 0;
+            for (std::size_t k = 0; k < ini.init_box.size(); ++k) {
+                const long long cnt = (long long)n_to_generate(ini.init_energy[k] / p->Eeff, rng);
+                if (cnt == 0) continue;
+                const int b = ini.init_box[k];
+                const auto ij = cellof[std::size_t(b)];
+                GenDesc d{};
+                d.x0 = g.gx[std::size_t(ij.first)];
+                d.dx = g.gx[std::size_t(ij.first) + 1] - d.x0;
+                d.y0 = g.gy[std::size_t(ij.second)];
+                d.dy = g.gy[std::size_t(ij.second) + 1] - d.y0;
+                d.box = b;
+                d.sign = ini.init_sign[k];
+                d.rect = 1;
+                const long long off = (long long)aprob.size();
+                for (std::size_t q = 0; q < std::size_t(n); ++q) {
+                    aprob.push_back(ini.alias[k * std::size_t(n) + q].prob);
+                    aalt.push_back(ini.alias[k * std::size_t(n) + q].alt);
+                }
+                d.alias_off = off;
+                d.first = first;
+                descs.push_back(d);
+                first += cnt;
+            }
+            generate(0, first, -1, 0, false);
+            np = first;
+        }
+        props(np, 0);
+        const PArr A0 = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
+        (void)A0;
+        long long psteps = 0, branchings = 0;
+        int istep = 0;
+        double time = 0.;
+        std::vector<int> hE(static_cast<std::size_t>(nborders));
+        std::vector<double> pmf;
+        const int cancel_every = p->cancel_every > 0 ? p->cancel_every : 4;
+        while (time <= p->maxtime) {
+            // 1. advection
+            if (np > 0) {
+                AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0};
+                be_advect<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
+                                                                    0, np, aa);
+            }
+            psteps += np;
+            // 3. isothermal walls
+            descs.clear();
+            aprob.clear();
+            aalt.clear();
+            long long nnew = 0;
+            for (std::size_t k = 0; k < iso.walls.size(); ++k) {
+                const WallGenerator& W = iso.walls[k];
+                const double Lb = norm(sub(W.sb, W.sa));
+                const double spf = Lb * g.thickness / (m.V * g.thickness / m.c);
+                const double cumulsum = std::fabs(W.flux) * double(m.nq) * vuc;
+                const long long cnt = (long long)n_to_generate(p->dt * spf * cumulsum / (p->Eeff * double(m.nq)), rng);
+                if (cnt == 0) continue;
+                GenDesc d{};
+                d.x0 = W.p1.x;
+                d.y0 = W.p1.y;
+                d.dx = W.nd.x;
+                d.dy = W.nd.y;
+                d.box = W.box;
+                d.sign = W.sign;
+                d.rect = 0;
+                const long long off = (long long)aprob.size();
+                for (std::size_t q = 0; q < std::size_t(n); ++q) {
+                    aprob.push_back(iso.alias[k * std::size_t(n) + q].prob);
+                    aalt.push_back(iso.alias[k * std::size_t(n) + q].alt);
+                }
+                d.alias_off = off;
+                d.first = nnew;
+                descs.push_back(d);
+                nnew += cnt;
+            }
+            generate(np, nnew, istep, 2, true);
+            np += nnew;
+            // 4. adiabatic diffuse walls: |Eborder| at the spline temperature
+            ck(cudaMemcpyAsync(hE.data(), B.d_Eb.p, hE.size() * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
+            sync(c);
+            ck(cudaMemsetAsync(B.d_Eb.p, 0, hE.size() * sizeof(int), s), "memset");
+            descs.clear();
+            aprob.clear();
+            aalt.clear();
+            nnew = 0;
+            for (int gb = 0; gb < nborders; ++gb) {
+                const int E = hE[std::size_t(gb)];
+                if (E == 0) continue;
+                const int b = border_box[std::size_t(gb)];
+                if (b < 0 || g.reservoir[std::size_t(b)]) continue;
+                const GBorder& br = g.borders[std::size_t(gb)];
+                const V2 nwall = v2(-br.np.x, -br.np.y);
+                const double Teq = g.Teq[std::size_t(b)];
+                if (!B.spl_ok[std::size_t(gb)]) {
+                    std::vector<double> J(100), Tv(100);
+                    for (int t = 0; t < 100; ++t) {
+                        const double T = 10.0 + 10.0 * t;
+                        Tv[std::size_t(t)] = T;
+                        const double cs = wall_pmf(m, nwall, T, Teq, pmf);
+                        J[std::size_t(t)] = ((T - Teq) >= 0 ? 1 : -1) * (cs / (double(m.nq) * vuc));
+                    }
+                    B.spl[std::size_t(gb)].build(J, Tv);
+                    B.spl_ok[std::size_t(gb)] = 1;
+                }
+                const double len = norm(sub(br.p2, br.p1));
+                const double Jb = p->Eeff * E / p->dt / (len * g.thickness);
+                const double Tb = B.spl[std::size_t(gb)].interp(Jb);
+                wall_pmf(m, nwall, Tb, Teq, pmf);
+                double tot = 0.;
+                for (double x : pmf) tot += x;
+                if (!(tot > 0.)) continue;
+                GenDesc d{};
+                d.x0 = br.p1.x;
+                d.y0 = br.p1.y;
+                d.dx = br.nd.x;
+                d.dy = br.nd.y;
+                d.box = b;
+                d.sign = (Tb - Teq) >= 0 ? 1 : -1;
+                d.rect = 0;
+                d.alias_off = add_alias_row(pmf);
+                d.first = nnew;
+                descs.push_back(d);
+                nnew += (long long)(std::abs(E) + 1.0e-6);
+            }
+            generate(np, nnew, istep, 4, true);
+            np += nnew;
+            // 5. delete absorbed particles
+            np = compact(np);
+            // 6. scattering
+            if (p->rta) {
+                if (np > 0)
+                    be_scatter_rta<<<launch_blocks(np, c->nsm), 256, 0, s>>>(
+                        arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np, c->d_w.as<double>(), p->dt,
+                        c->d_rprob.as<float>(), c->d_ralt.as<int>(), n, mix_key(p->seed, istep, 6));
+            } else if (np > 0) {
+                ck(cudaMemsetAsync(counts, 0, 4 * sizeof(unsigned long long), s), "memset");
+                PArr in = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
+                PArr outp = arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign);
+                long long nin = np;
+                int half = 0, round = 0;
+                for (;;) {
+                    PArr q = arr(B.q_x, B.q_y, B.q_mode, B.q_box, B.q_sign, half ? cap : 0);
+                    ck(cudaMemsetAsync(counts + 1 + half, 0, sizeof(unsigned long long), s), "memset");
+                    be_scatter<<<launch_blocks(nin, c->nsm), 256, 0, s>>>(
+                        in, nin, outp, counts, cap, q, counts + 1 + half, cap,
+                        B.d_palias.as<PAlias>(), B.nm, mix_key(p->seed, istep, 64 + round), err);
+                    const long long nq = read_count(1 + half);
+                    if (nq == 0) break;
+                    if (++round > 4096) throw Error(BTE_ERR_LIMIT, "branching rounds cap");
+                    branchings += nq / 2;
+                    in = q;
+                    nin = nq;
+                    half ^= 1;
+                }
+                np = read_count(0);
+                if (np > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded in scattering");
+                std::swap(B.a_x.p, B.b_x.p);
+                std::swap(B.a_y.p, B.b_y.p);
+                std::swap(B.a_mode.p, B.b_mode.p);
+                std::swap(B.a_box.p, B.b_box.p);
+                std::swap(B.a_sign.p, B.b_sign.p);
+            }
+            // 7.-9. histogram, cancellation, properties
+            ck(cudaMemsetAsync(B.d_H.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
+            if (np > 0)
+                be_hist<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
+                                                                  np, B.d_H.as<int>(), n);
+            if (istep % cancel_every == 0 && np > 0) {
+                ck(cudaMemsetAsync(B.d_cnt.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
+                be_cancel<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
+                                                                    np, B.d_H.as<int>(), B.d_cnt.as<int>(), n,
+                                                                    d_res.as<int>());
+                np = compact(np);
+            }
+            be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),
+                                          B.d_props.as<double>());
+            ck(cudaMemcpyAsync(hprops.data(), B.d_props.p, hprops.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "d2h");
+            sync(c);
+            for (int b = 0; b < nbx; ++b) {
+                const double f1 = p->Eeff / vol[std::size_t(b)] * 1.0e+27;
+                const double f2 = p->Eeff / vol[std::size_t(b)] * 1.0e+30;
+                const std::size_t sidx = std::size_t(istep) + 1;
+                if (out->ed) out->ed[sidx * nbx + b] = f1 * hprops[3 * std::size_t(b)];
+                if (out->flux) {
+                    out->flux[(sidx * nbx + b) * 2] = f2 * hprops[3 * std::size_t(b) + 1];
+                    out->flux[(sidx * nbx + b) * 2 + 1] = f2 * hprops[3 * std::size_t(b) + 2];
+                }
+            }
+            if (out->nparticles) out->nparticles[istep + 1] = np;
+            int herr[4];
+            ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
+            sync(c);
+            if (herr[0] != 0)
+                throw Error(bte_status(herr[0]), herr[0] == BTE_ERR_LIMIT ? "particle capacity exceeded"
+                                                                          : "particle without a propagator column");
+            istep++;
+            time += p->dt;
+        }
+        ck(cudaEventRecord(c->ev1, s), "event");
+        sync(c);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        if (out->histogram)
+            ck(cudaMemcpy(out->histogram, B.d_H.p, std::size_t(nbx) * n * sizeof(int), cudaMemcpyDeviceToHost), "d2h");
+        out->nboxes = nbx;
+        out->nsteps = istep;
+        out->particle_steps = psteps;
+        out->branchings = branchings;
+        out->kernel_ms = ms;
+        return BTE_OK;
+    } catch (const Error& e) {
+        c->err = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        c->err = e.what();
+        return BTE_ERR_CUDA;
+    }
+}

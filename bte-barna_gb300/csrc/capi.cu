@@ -15,6 +15,7 @@
 #include "btegpu_debug.h"
 #include "kernels.h"
 #include "tables.hpp"
+#include "ctx.hpp"
 
 using bte::Error;
 
@@ -22,84 +23,13 @@ namespace {
 
 thread_local std::string g_create_error;
 
-void ck(cudaError_t e, const char* what) {
-    if (e != cudaSuccess)
-        throw Error(BTE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-// Owned device allocation.
-struct DBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    DBuf() = default;
-    DBuf(const DBuf&) = delete;
-    DBuf& operator=(const DBuf&) = delete;
-    ~DBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-    void alloc(size_t n) {
-        if (n == 0) n = 16;
-        if (p && bytes >= n) return;
-        release();
-        ck(cudaMalloc(&p, n), "cudaMalloc");
-        bytes = n;
-    }
-    template <class T>
-    void upload(const std::vector<T>& v, cudaStream_t s) {
-        alloc(v.size() * sizeof(T));
-        if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
-    }
-    template <class T>
-    T* as() const { return static_cast<T*>(p); }
-};
-
-int hw_threads() {
-    unsigned n = std::thread::hardware_concurrency();
-    return n ? int(std::min(n, 64u)) : 4;
-}
-
 }  // namespace
 
-struct bte_ctx {
-    int device = 0;
-    int nsm = 0;
-    int verbose = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    std::string err;
-    bte::ProdTuning tune{0, 0, 0, 0};
+using bte::ck;
+using bte::DBuf;
+using bte::hw_threads;
 
-    bool have_modes = false, have_geom = false;
-    bte::HostModes modes;
-    bte::HostGeometry geom;
-
-    // static tables
-    bool modes_dev = false, geom_dev = false, lambert_dev = false;
-    DBuf d_vxc, d_vyc, d_w, d_tau, d_mv;
-    DBuf d_boxes, d_hull, d_borders, d_contacts;
-    DBuf d_gx, d_gy, d_gcell, d_boxcell;
-    DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;
-    int nclass = 0;
-    bool have_mirror = false;
-    // per-T0 resampling
-    double resample_T0 = -1;
-    DBuf d_rcdf, d_rprob, d_ralt;
-    // generators
-    int gen_key_source = -1;
-    long long gen_key_n = -1;
-    unsigned long long gen_key_seed = 0;
-    bte::Generators gens;
-    double gen_Eeff = 0;
-    DBuf d_gcdf, d_gprob, d_galt, d_walls, d_wcum, d_ifirst, d_ibox, d_isign;
-    // run buffers
-    DBuf d_time, d_tally, d_counters, d_err, d_work;
-    std::vector<double> h_time;
-};
-
-namespace {
+namespace bte {
 
 void sync(bte_ctx* c) { ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize"); }
 
@@ -180,6 +110,13 @@ void ensure_resample(bte_ctx* c, double T0) {
     sync(c);
     c->resample_T0 = T0;
 }
+
+}  // namespace bte
+
+namespace {
+using bte::ensure_resample;
+using bte::ensure_static;
+using bte::sync;
 
 void ensure_generators(bte_ctx* c, const bte_rta_params* p) {
     if (c->gen_key_source == p->source) {
@@ -289,6 +226,7 @@ bte_status bte_destroy(bte_ctx* c) {
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     cudaStream_t s = c->stream;
+    bte::destroy_berta(c);
     delete c;
     if (s) cudaStreamDestroy(s);
     return BTE_OK;

@@ -1,0 +1,103 @@
+// ctx.hpp - the engine context shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/btegpu.h"
+#include "kernels.h"
+#include "tables.hpp"
+
+namespace bte {
+
+inline void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess)
+        throw Error(BTE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Owned device allocation.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void alloc(size_t n) {
+        if (n == 0) n = 16;
+        if (p && bytes >= n) return;
+        release();
+        ck(cudaMalloc(&p, n), "cudaMalloc");
+        bytes = n;
+    }
+    template <class T>
+    void upload(const std::vector<T>& v, cudaStream_t s) {
+        alloc(v.size() * sizeof(T));
+        if (!v.empty()) ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+inline int hw_threads() {
+    unsigned n = std::thread::hardware_concurrency();
+    return n ? int(n < 64u ? n : 64u) : 4;
+}
+
+struct BertaState;  // berta.cu
+
+}  // namespace bte
+
+struct bte_ctx {
+    int device = 0;
+    int nsm = 0;
+    int verbose = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    bte::ProdTuning tune{0, 0, 0, 0};
+
+    bool have_modes = false, have_geom = false;
+    bte::HostModes modes;
+    bte::HostGeometry geom;
+
+    // static tables
+    bool modes_dev = false, geom_dev = false, lambert_dev = false;
+    bte::DBuf d_vxc, d_vyc, d_w, d_tau, d_mv;
+    bte::DBuf d_boxes, d_hull, d_borders, d_contacts;
+    bte::DBuf d_gx, d_gy, d_gcell, d_boxcell;
+    bte::DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;
+    int nclass = 0;
+    bool have_mirror = false;
+    // per-T0 resampling
+    double resample_T0 = -1;
+    bte::DBuf d_rcdf, d_rprob, d_ralt;
+    // generators
+    int gen_key_source = -1;
+    long long gen_key_n = -1;
+    unsigned long long gen_key_seed = 0;
+    bte::Generators gens;
+    double gen_Eeff = 0;
+    bte::DBuf d_gcdf, d_gprob, d_galt, d_walls, d_wcum, d_ifirst, d_ibox, d_isign;
+    // run buffers
+    bte::DBuf d_time, d_tally, d_counters, d_err, d_work;
+    std::vector<double> h_time;
+    // beyond-RTA (berta.cu)
+    bte::BertaState* berta = nullptr;
+};
+
+namespace bte {
+// Device tables shared by every run type (capi.cu).
+void ensure_static(bte_ctx* c);
+void ensure_resample(bte_ctx* c, double T0);
+void sync(bte_ctx* c);
+void destroy_berta(bte_ctx* c);
+}  // namespace bte

@@ -118,6 +118,14 @@ void alias_table(const double* w, int n, Alias* out);
 // axis-aligned or the grid has no mirror image).
 std::vector<int> build_mirror(const HostModes& m, const HostGeometry& g);
 
+// Natural cubic spline through (X, Y), X ascending (CubicSpline1D,
+// src/interpolation.cpp:20-103).
+struct Spline1D {
+    std::vector<double> a, b, c, d, x0, xs;
+    void build(const std::vector<double>& X, const std::vector<double>& Y);
+    double interp(double x) const;
+};
+
 double calc_cv(const HostModes& m, double T);
 double bose_einstein(double omega, double T);
 double bose_einstein_kernel(double omega, double T);

@@ -226,6 +226,17 @@ bte_status bte_query_sizes(const bte_ctx* ctx, const bte_rta_params* params,
 /* Library version (BTEGPU_VERSION). */
 int32_t bte_version(void);
 
+/* Load the propagator of the (single) material for beyond-RTA runs
+ * (replaces load_P and the propagator_H columns of process_input,
+ * src/collision_operator.cpp:972-1013, src/beyondRTA_MC2d.cpp:1363-1377). */
+bte_status bte_load_propagator(bte_ctx* ctx, const bte_propagator* P);
+
+/* Run the beRTAMC2D step loop (replaces the loop of
+ * src/beyondRTA_MC2d.cpp:2138-2425 and its stdout table).  Production mode;
+ * the boxes must tile an axis-aligned grid and share Teq = T0. */
+bte_status bte_berta_run(bte_ctx* ctx, const bte_berta_params* params,
+                         bte_berta_result* out);
+
 /* Largest number of time bins bte_rta_run_noalloc accepts. */
 #define BTE_NOALLOC_MAX_BINS 4096
 
