@@ -82,7 +82,7 @@ class BertaParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("maxtime", C.c_double), ("Eeff", C.c_double),
                 ("T0", C.c_double), ("seed", C.c_uint64), ("mode", C.c_int32),
                 ("rta", C.c_int32), ("cancel_every", C.c_int32), ("reserved0", C.c_int32),
-                ("capacity", C.c_int64)]
+                ("capacity", C.c_int64), ("on_step", C.c_void_p), ("user", C.c_void_p)]
 
 
 class BertaResult(C.Structure):
@@ -198,6 +198,9 @@ def load_library(path: str = LIB_PATH):
                                          C.POINTER(C.c_longlong), C.c_int]
     lib.btegpu_debug_lambert.restype = C.c_longlong
     lib.btegpu_debug_log.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong]
+    lib.btegpu_debug_frame.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                       C.c_int, C.c_int, C.c_char_p, C.c_longlong]
+    lib.btegpu_debug_frame.restype = C.c_longlong
     _lib = lib
     return lib
 
@@ -332,6 +335,31 @@ def debug_lambert(m: dict, g: dict, maxclass: int = 16):
     tot = lib.btegpu_debug_lambert(C.byref(ms), C.byref(gs),
                                    nnz.ctypes.data_as(C.POINTER(C.c_longlong)), maxclass)
     return tot, nnz
+
+
+def debug_frame(time: float, Eeff: float, temps, H: np.ndarray) -> bytes:
+    lib = load_library()
+    t = np.ascontiguousarray(temps, dtype=np.float64)
+    Hc = np.ascontiguousarray(H, dtype=np.int32)
+    n = lib.btegpu_debug_frame(time, Eeff, _dptr(t), Hc.ctypes.data_as(C.POINTER(C.c_int)),
+                               Hc.shape[0], Hc.shape[1], None, 0)
+    buf = C.create_string_buffer(int(n))
+    lib.btegpu_debug_frame(time, Eeff, _dptr(t), Hc.ctypes.data_as(C.POINTER(C.c_int)),
+                           Hc.shape[0], Hc.shape[1], buf, n)
+    return buf.raw[:n]
+
+
+def split_frames(data: bytes):
+    """Frames of a properties.msgpack.bin file ("<size>#<msgpack>" ..., "0#")."""
+    out, i = [], 0
+    while i < len(data):
+        j = data.index(b"#", i)
+        size = int(data[i:j])
+        if size == 0:
+            break
+        out.append(data[j + 1:j + 1 + size])
+        i = j + 1 + size
+    return out
 
 
 def debug_log(x: np.ndarray) -> np.ndarray:

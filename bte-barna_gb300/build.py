@@ -15,6 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libbtegpu.so")
 CLI = os.path.join(OUT, "rtamc2d_gpu")
+CLI_BE = os.path.join(OUT, "bertamc2d_gpu")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOSTFLAGS = "-fPIC,-ffp-contract=off,-O2"
@@ -52,7 +53,7 @@ def _run(cmd):
 
 def build(force: bool = False, verbose: bool = False) -> str:
     deps = _deps()
-    if not force and _newer(LIB, deps) and _newer(CLI, deps):
+    if not force and _newer(LIB, deps) and _newer(CLI, deps) and _newer(CLI_BE, deps):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     jobs = []
@@ -77,6 +78,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", os.path.join(CSRC, "cli_rtamc2d.cpp"),
           "-o", tmp, "-L", OUT, "-lbtegpu", "-Wl,-rpath,$ORIGIN", "-pthread"])
     os.replace(tmp, CLI)
+    tmp = CLI_BE + ".tmp%d" % os.getpid()
+    _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", os.path.join(CSRC, "cli_bertamc2d.cpp"),
+          "-o", tmp, "-L", OUT, "-lbtegpu", "-Wl,-rpath,$ORIGIN", "-pthread"])
+    os.replace(tmp, CLI_BE)
     return LIB
 
 

@@ -732,6 +732,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         int istep = 0;
         double time = 0.;
         std::vector<int> hE(static_cast<std::size_t>(nborders));
+        std::vector<int> hH;
         std::vector<double> pmf;
         const int cancel_every = p->cancel_every > 0 ? p->cancel_every : 4;
         while (time <= p->maxtime) {
@@ -886,6 +887,18 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 }
             }
             if (out->nparticles) out->nparticles[istep + 1] = np;
+            if (p->on_step) {
+                hH.resize(std::size_t(nbx) * n);
+                ck(cudaMemcpyAsync(hH.data(), B.d_H.p, hH.size() * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
+                sync(c);
+                std::vector<double> ed(static_cast<std::size_t>(nbx)), fl(std::size_t(nbx) * 2);
+                for (int b = 0; b < nbx; ++b) {
+                    ed[std::size_t(b)] = p->Eeff / vol[std::size_t(b)] * 1.0e+27 * hprops[3 * std::size_t(b)];
+                    fl[2 * std::size_t(b)] = p->Eeff / vol[std::size_t(b)] * 1.0e+30 * hprops[3 * std::size_t(b) + 1];
+                    fl[2 * std::size_t(b) + 1] = p->Eeff / vol[std::size_t(b)] * 1.0e+30 * hprops[3 * std::size_t(b) + 2];
+                }
+                p->on_step(p->user, istep + 1, time + p->dt, np, hH.data(), nbx, n, ed.data(), fl.data());
+            }
             int herr[4];
             ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
             sync(c);

@@ -21,6 +21,10 @@ int btegpu_debug_grid(const bte_geometry* g, int* nx, int* ny);
 long long btegpu_debug_lambert(const bte_mode_table* m, const bte_geometry* g,
                                long long* nnz_per_class, int maxclass);
 
+/* One properties.msgpack.bin frame; returns its byte count. */
+long long btegpu_debug_frame(double time, double Eeff, const double* temps, const int* H, int nboxes,
+                             int nmodes, char* out, long long cap);
+
 /* The host build of bte_log. */
 int btegpu_debug_log(const double* x, double* y, long long n);
 

@@ -16,6 +16,7 @@
 #include "kernels.h"
 #include "tables.hpp"
 #include "ctx.hpp"
+#include "frames.hpp"
 
 using bte::Error;
 
@@ -580,6 +581,14 @@ long long btegpu_debug_lambert(const bte_mode_table* mt, const bte_geometry* gm,
     } catch (const std::exception&) {
         return -1;
     }
+}
+
+long long btegpu_debug_frame(double time, double Eeff, const double* temps, const int* H, int nboxes,
+                             int nmodes, char* out, long long cap) {
+    std::vector<double> t(temps, temps + nboxes);
+    const std::string f = bte::berta_frame(time, Eeff, t, H, std::size_t(nboxes), std::size_t(nmodes));
+    if ((long long)f.size() <= cap) std::memcpy(out, f.data(), f.size());
+    return (long long)f.size();
 }
 
 int btegpu_debug_log(const double* x, double* y, long long n) {

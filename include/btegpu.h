@@ -150,6 +150,14 @@ typedef struct bte_propagator {
     const double* P;     /* [nmodes * nmodes] column-major: column j = mode j + 3 */
 } bte_propagator;
 
+/* Called after every step of a beyond-RTA run with that step's signed
+ * histogram H [nboxes][nmodes] (host memory, valid during the call) and
+ * its properties ed [nboxes], flux [nboxes][2]; the hook of the reference's
+ * stdout table and msgpack frames (src/beyondRTA_MC2d.cpp:2374-2423). */
+typedef void (*bte_berta_step_fn)(void* user, int32_t step, double time, int64_t nparticles,
+                                  const int32_t* H, int32_t nboxes, int32_t nmodes,
+                                  const double* ed, const double* flux);
+
 /* Parameters of one beRTAMC2D run (<beRTAMC2D> XML,
  * src/beyondRTA_MC2d.cpp:1299-1462). */
 typedef struct bte_berta_params {
@@ -163,6 +171,8 @@ typedef struct bte_berta_params {
     int32_t cancel_every;    /* cancellation period in steps (reference: 4)     */
     int32_t reserved0;
     int64_t capacity;        /* particle capacity on the device (0 = auto)       */
+    bte_berta_step_fn on_step; /* optional per-step hook (NULL: none)          */
+    void* user;              /* passed to on_step                                */
 } bte_berta_params;
 
 /* Results of one beRTAMC2D run; per step s = 0..nsteps (s = 0 is the

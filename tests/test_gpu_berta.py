@@ -55,3 +55,26 @@ def test_berta_counts_and_branching(engine):
     assert abs(r["nparticles"][-1] - o["nparticles"][-1]) < 0.1 * o["nparticles"][-1]
     # the histogram of the last step sums to the signed particle count
     assert r["H"].sum() != 0
+
+
+def test_bertamc2d_cli_writes_table_and_frames(built, tmp_path):
+    import os
+    import subprocess
+    m, g, P = _case()
+    synth.write_geometry_xml(str(tmp_path / "beam.xml"), g)
+    synth.write_modes_file(str(tmp_path / "modes.bin"), m)
+    synth.write_propagator(str(tmp_path / "p.P.eigen.bin"), P)
+    (tmp_path / "input.xml").write_text(
+        '<beRTAMC2D>\n  <geometry file="beam.xml"/>\n  <time dt="1.0" maxtime="10"/>\n'
+        '  <material name="synthetic" database="modes.bin" thickness="0.335">\n'
+        '    <propagator T="300" file="p.P.eigen.bin"/>\n  </material>\n'
+        '  <Eeff Ed="2e-23"/>\n</beRTAMC2D>\n')
+    exe = os.path.join(os.path.dirname(built), "bertamc2d_gpu")
+    r = subprocess.run([exe, "input.xml", "4"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    rows = [ln for ln in r.stdout.splitlines() if ln and ln[0].isdigit()]
+    assert len(rows) == 11                      # steps 1..11 for time <= 10
+    assert len(rows[0].split("\t")) >= 3 + 3 * g["nboxes"]
+    data = (tmp_path / "properties.msgpack.bin").read_bytes()
+    assert data.endswith(b"0#")
+    assert len(btegpu.split_frames(data)) == 11

@@ -174,3 +174,19 @@ def test_restatement_rejects_zero_rate_mode():
     with pytest.raises(btegpu.BteError) as e:
         pyoracle.rta_run({**case, "modes": m})
     assert e.value.code == btegpu.BTE_ERR_VALUE
+
+
+def test_berta_frame_layout(built):
+    """properties.msgpack.bin frames (src/beyondRTA_MC2d.cpp:1604-1769)."""
+    msgpack = pytest.importorskip("msgpack")
+    H = np.array([[0, 3, 0, -2, 0], [0, 0, 0, 0, 0], [200, 0, -70000, 0, 1]], dtype=np.int32)
+    raw = btegpu.debug_frame(12.5, 3e-24, [300.0, 301.0, 299.0], H)
+    head, _, body = raw.partition(b"#")
+    assert int(head) == len(body)
+    frame = msgpack.unpackb(body, strict_map_key=False)
+    assert frame[0] == 12.5 and frame[1] == 3e-24 and frame[2] == [300.0, 301.0, 299.0]
+    assert frame[3] == 4 and frame[4] == [1, 3, 3, -2]
+    assert frame[5] == 0 and frame[6] == [42.0]
+    assert frame[7] == 6 and frame[8] == [0, 200, 2, -70000, 4, 1]
+    assert len(frame) == 3 + 2 * 3
+    assert btegpu.split_frames(raw + b"0#") == [body]
