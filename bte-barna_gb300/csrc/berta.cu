@@ -330,10 +330,16 @@ __global__ void be_hist(PArr P, long long n, int* H, int nmodes) {
 }
 
 // Cancellation: a particle survives when its sign is the sign of H at its
-// (box, mode) and its rank among those particles is below |H|.
-__global__ void be_cancel(PArr P, long long n, const int* H, int* cnt, int nmodes, const int* reservoir) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
+// (box, mode) and its rank among those particles is below |H|.  Threads
+// visit the particles in the order of a random affine permutation
+// t -> (a t + b) mod n (a coprime to n), so the ranks, and with them the
+// survivors, do not follow the order of the particle list.
+__global__ void be_cancel(PArr P, long long n, const int* H, int* cnt, int nmodes, const int* reservoir,
+                          unsigned long long pa, unsigned long long pb) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long i = (long long)((unsigned __int128)(pa % (unsigned long long)n) * (unsigned long long)t %
+                                        (unsigned long long)n + pb % (unsigned long long)n) % n;
         const long long key = (long long)P.box[i] * nmodes + P.mode[i];
         const int h = H[key];
         const int s = P.sign[i];
@@ -867,9 +873,12 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                                                                   np, B.d_H.as<int>(), n);
             if (istep % cancel_every == 0 && np > 0) {
                 ck(cudaMemsetAsync(B.d_cnt.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
+                // random affine permutation of the visiting order (a coprime to np)
+                unsigned long long pa = rng.next() | 1ull, pb = rng.next();
+                while (std::gcd((unsigned long long)np, pa % (unsigned long long)np) != 1ull) pa += 2;
                 be_cancel<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
                                                                     np, B.d_H.as<int>(), B.d_cnt.as<int>(), n,
-                                                                    d_res.as<int>());
+                                                                    d_res.as<int>(), pa, pb);
                 np = compact(np);
             }
             be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),

@@ -1836,6 +1836,14 @@ int oracle_berta_run(const bte_mode_table* mt, const bte_geometry* gm, const dou
             // 8. cancellation every 4th step
             if (istep % 4 == 0) {
                 std::vector<int> Hc(H);
+                // the reference sorts with tbb::parallel_sort, which leaves the
+                // order of equal (box, mode, sign) particles unspecified; the
+                // survivors are taken uniformly at random here (a seeded
+                // Fisher-Yates shuffle before a stable sort)
+                for (std::size_t i = parts.size(); i > 1; --i) {
+                    const std::size_t j = std::size_t(orc::uniform_int(rng_, 0, int(i) - 1));
+                    std::swap(parts[i - 1], parts[j]);
+                }
                 std::stable_sort(parts.begin(), parts.end(), [](const orc::BeParticle& a, const orc::BeParticle& b) {
                     return std::make_tuple(a.box, a.mode, a.sign) < std::make_tuple(b.box, b.mode, b.sign);
                 });
