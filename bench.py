@@ -142,15 +142,22 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per event of the grid kernel from the committed ncu summary."""
+def nsm_of_device():
+    import torch
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
+def profile_figures():
+    """ncu figures of the grid kernel from the committed capture summary:
+    DRAM bytes per launch = fixed (tables, first touch) + per event, and the
+    FP64 thread operations per event."""
     p = os.path.join(REPO, "profiles", "rta_prod_grid_c1.json")
     if os.path.exists(p):
         try:
-            return json.load(open(p)).get("dram_bytes_per_event")
+            return json.load(open(p))
         except (ValueError, OSError):
-            return None
-    return None
+            return {}
+    return {}
 
 
 # ----------------------------------------------------------------- CPU leg
@@ -294,7 +301,19 @@ def main():
         peak, peak_kind = measured_peaks()
         per_launch_bytes = algorithmic_bytes(ev, tal, parts) / args.steps
         achieved = per_launch_bytes / (kern_ms * 1e-3 / args.steps) / 1e9
-        bpe = profile_traffic()
+        prof = profile_figures()
+        ev_launch = ev / args.steps
+        traffic = None
+        if "dram_bytes_per_event" in prof:
+            traffic = prof.get("dram_fixed_bytes", 0.0) + prof["dram_bytes_per_event"] * ev_launch
+        fp64 = None
+        if "fp64_thread_ops_per_event" in prof:
+            mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+            lane_peak = prof.get("fp64_lane_ops_per_sm_cycle", 2) * nsm_of_device() * mhz * 1e6
+            ops = prof["fp64_thread_ops_per_event"] * value
+            fp64 = {"pipe": "fp64", "ops_per_event": prof["fp64_thread_ops_per_event"],
+                    "achieved": ops / 1e9, "peak": lane_peak / 1e9, "unit": "Gop/s",
+                    "frac": ops / lane_peak, "pipe_busy_pct_ncu": prof.get("fp64_pipe_busy_pct")}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -312,8 +331,9 @@ def main():
             "tally_updates_per_event": tal / max(ev, 1),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": (bpe * ev / args.steps) if bpe else None,
-                         "bytes_per_event": per_launch_bytes / max(ev / args.steps, 1)},
+                         "traffic": traffic,
+                         "bytes_per_event": per_launch_bytes / max(ev_launch, 1)},
+            "co_bound": fp64,
             "clocks": clk,
             "tuning": {"block_threads": choice[0], "blocks_per_sm": choice[1],
                        "smem_tally": choice[2],
