@@ -51,7 +51,8 @@ class Geometry(C.Structure):
     _fields_ = [("nboxes", C.c_int32), ("npoints", C.POINTER(C.c_int32)),
                 ("vertices", C.POINTER(C.c_double)), ("Teq", C.POINTER(C.c_double)),
                 ("Tinit", C.POINTER(C.c_double)), ("reservoir", C.POINTER(C.c_int32)),
-                ("thickness", C.c_double)]
+                ("thickness", C.c_double), ("translate_to", C.POINTER(C.c_int32)),
+                ("translation", C.POINTER(C.c_double))]
 
 
 class RtaParams(C.Structure):
@@ -71,7 +72,7 @@ class RtaResult(C.Structure):
                 ("energy_rate", C.c_double), ("events", C.c_int64), ("wall_hits", C.c_int64),
                 ("crossings", C.c_int64), ("absorbed", C.c_int64),
                 ("specular_hits", C.c_int64), ("tally_updates", C.c_int64),
-                ("kernel_ms", C.c_double)]
+                ("kernel_ms", C.c_double), ("translations", C.c_int64)]
 
 
 class Propagator(C.Structure):
@@ -148,6 +149,11 @@ def geom_struct(g: dict):
     s.Tinit = _dptr(keep["Tinit"])
     s.reservoir = _iptr(keep["reservoir"])
     s.thickness = float(g["thickness"])
+    if g.get("translate_to") is not None:
+        keep["translate_to"] = np.ascontiguousarray(g["translate_to"], dtype=np.int32)
+        keep["translation"] = np.ascontiguousarray(g["translation"], dtype=np.float64).reshape(-1)
+        s.translate_to = _iptr(keep["translate_to"])
+        s.translation = _dptr(keep["translation"])
     return s, keep
 
 
@@ -269,7 +275,7 @@ class Engine:
             r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
         self._check(self.lib.bte_rta_run(self.ctx, C.byref(p), C.byref(r)))
         for k in ("Eeff", "energy_rate", "events", "wall_hits", "crossings", "absorbed",
-                  "specular_hits", "tally_updates", "kernel_ms"):
+                  "specular_hits", "tally_updates", "kernel_ms", "translations"):
             out[k] = getattr(r, k)
         return out
 

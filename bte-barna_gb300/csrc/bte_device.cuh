@@ -301,6 +301,46 @@ BTE_HD bool seg_intersect(V2 s0, V2 s1, V2 l0, V2 l1, V2& out) {
     return true;
 }
 
+// boost::geometry::intersects / intersection of two closed segments, as the
+// periodic translation uses them: true when s0-s1 and l0-l1 share a point;
+// `out` is the first shared point (a crossing is taken on l0-l1; for
+// collinear segments, the end of the overlap nearest s0; a degenerate l is
+// the point l0).
+BTE_HD bool seg_meet(V2 s0, V2 s1, V2 l0, V2 l1, V2& out) {
+    const V2 d1 = sub(s1, s0), d2 = sub(l1, l0);
+    if (d2.x == 0. && d2.y == 0.) {
+        if (!on_segment(l0, s0, s1)) return false;
+        out = l0;
+        return true;
+    }
+    const double den = cross(d1, d2);
+    const V2 w = sub(l0, s0);
+    if (den != 0.) {
+        const double t = cross(w, d2) / den;
+        const double u = cross(w, d1) / den;
+        if (!(t >= 0. && t <= 1. && u >= 0. && u <= 1.)) return false;
+        out = add(l0, scal(u, d2));
+        return true;
+    }
+    if (cross(w, d1) != 0.) return false;  // parallel, apart
+    const double dd = dot(d1, d1);
+    if (dd == 0.) {
+        if (!on_segment(s0, l0, l1)) return false;
+        out = s0;
+        return true;
+    }
+    // overlap of the parameter ranges along s
+    const double a = dot(sub(l0, s0), d1) / dd, b = dot(sub(l1, s0), d1) / dd;
+    const double lo = a < b ? a : b, hi = a < b ? b : a;
+    if (hi < 0. || lo > 1.) return false;
+    if (lo <= 0.) {
+        out = s0;
+    } else {
+        out = a < b ? l0 : l1;
+    }
+    return true;
+}
+
 // Device geometry records (built by the host from the boxes of the XML).
 struct GBorder {
     V2 p1, p2, nd, np, la, lb;  // ends, p2-p1, outward normal, lengthened ends
@@ -319,7 +359,7 @@ struct GBox {
     int border_off, nborders;
     int contact_off, ncontacts;
     int reservoir;
-    int pad;
+    int tto;  // periodic box: the box it translates to (<Translate_to id>); -1 otherwise
 };
 
 // Inside or on the border of a counter-clockwise convex hull.

@@ -61,6 +61,8 @@ void ensure_static(bte_ctx* c) {
         c->d_hull.upload(g.hull, c->stream);
         c->d_borders.upload(g.borders, c->stream);
         c->d_contacts.upload(g.contacts, c->stream);
+        c->d_cseg.upload(g.contact_seg, c->stream);
+        c->d_transl.upload(g.translation, c->stream);
         if (g.rect_grid) {
             c->d_gx.upload(g.gx, c->stream);
             c->d_gy.upload(g.gy, c->stream);
@@ -330,11 +332,11 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         const bool replay = p->mode == BTE_MODE_REPLAY;
         const std::size_t tally_bytes = replay ? nk * 6 * sizeof(unsigned long long) : nk * 3 * sizeof(double);
         c->d_tally.alloc(tally_bytes);
-        c->d_counters.alloc(8 * sizeof(unsigned long long));
+        c->d_counters.alloc(16 * sizeof(unsigned long long));
         c->d_err.alloc(4 * sizeof(int));
         c->d_work.alloc(sizeof(unsigned long long));
         ck(cudaMemsetAsync(c->d_tally.p, 0, tally_bytes, c->stream), "memset");
-        ck(cudaMemsetAsync(c->d_counters.p, 0, 8 * sizeof(unsigned long long), c->stream), "memset");
+        ck(cudaMemsetAsync(c->d_counters.p, 0, 16 * sizeof(unsigned long long), c->stream), "memset");
         ck(cudaMemsetAsync(c->d_err.p, 0, 4 * sizeof(int), c->stream), "memset");
         ck(cudaMemsetAsync(c->d_work.p, 0, sizeof(unsigned long long), c->stream), "memset");
 
@@ -367,6 +369,8 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         T.hull = c->d_hull.as<bte::V2>();
         T.borders = c->d_borders.as<bte::GBorder>();
         T.contacts = c->d_contacts.as<bte::GContact>();
+        T.cseg = c->d_cseg.as<bte::V2>();
+        T.translation = c->d_transl.as<bte::V2>();
         T.nclass = c->nclass;
         T.row_ptr = c->d_row_ptr.as<long long>();
         T.lcol = c->d_lcol.as<int>();
@@ -422,7 +426,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         }
         ck(cudaGetLastError(), "kernel launch");
         ck(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
-        std::vector<unsigned long long> hc(8);
+        std::vector<unsigned long long> hc(16);
         int herr[4];
         std::vector<unsigned long long> hex;
         std::vector<double> htal;
@@ -433,7 +437,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
             htal.resize(nk * 3);
             ck(cudaMemcpyAsync(htal.data(), c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
         }
-        ck(cudaMemcpyAsync(hc.data(), counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream), "d2h");
+        ck(cudaMemcpyAsync(hc.data(), counters, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream), "d2h");
         ck(cudaMemcpyAsync(herr, err, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream), "d2h");
         sync(c);
         float ms = 0;
@@ -477,6 +481,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         out->absorbed = (int64_t)hc[3];
         out->specular_hits = (int64_t)hc[4];
         out->tally_updates = (int64_t)hc[7];
+        out->translations = (int64_t)hc[8];
         if (out->gz) std::copy(gz.begin(), gz.end(), out->gz);
         if (out->gz_jx) std::copy(jx.begin(), jx.end(), out->gz_jx);
         if (out->gz_jy) std::copy(jy.begin(), jy.end(), out->gz_jy);
@@ -677,6 +682,8 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
     T.hull = c->d_hull.as<V2>();
     T.borders = c->d_borders.as<GBorder>();
     T.contacts = c->d_contacts.as<GContact>();
+    T.cseg = c->d_cseg.as<V2>();
+    T.translation = c->d_transl.as<V2>();
     T.nclass = c->nclass;
     T.row_ptr = c->d_row_ptr.as<long long>();
     T.lcol = c->d_lcol.as<int>();

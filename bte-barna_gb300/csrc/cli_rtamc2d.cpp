@@ -245,8 +245,9 @@ int main(int argc, char** argv) {
         }
         // geometry
         auto groot = read_xml(resolve(base, gfile));
-        std::vector<int32_t> npts, res;
-        std::vector<double> verts, teq, tinit;
+        std::vector<int32_t> npts, res, tto;
+        std::vector<double> verts, teq, tinit, transl;
+        bool any_periodic = false;
         for (auto& b : groot->kids) {
             if (b->name != "Box") continue;
             const Node* v = b->child("Vertices");
@@ -265,7 +266,17 @@ int main(int argc, char** argv) {
             teq.push_back(te);
             tinit.push_back(ic && ic->has("Tinit") ? std::stod(ic->get("Tinit")) : te);
             res.push_back(b->child("Reservoir") ? 1 : 0);
-            if (b->child("Translate_to")) throw std::runtime_error("periodic boxes are not supported yet");
+            // <Translate_to id="j"> tx ty [tz] </Translate_to>, src/geometry_2d.cpp:467-475
+            const Node* tr = b->child("Translate_to");
+            tto.push_back(tr ? std::stoi(tr->get("id")) : -1);
+            double tx = 0., ty = 0.;
+            if (tr) {
+                std::stringstream ts(tr->text);
+                ts >> tx >> ty;
+                any_periodic = true;
+            }
+            transl.push_back(tx);
+            transl.push_back(ty);
         }
         ModesFile mf = read_modes(resolve(base, dbfile));
         bte_ctx* ctx = nullptr;
@@ -295,6 +306,10 @@ int main(int argc, char** argv) {
         gm.Tinit = tinit.data();
         gm.reservoir = res.data();
         gm.thickness = thickness;
+        if (any_periodic) {
+            gm.translate_to = tto.data();
+            gm.translation = transl.data();
+        }
         check(ctx, bte_load_geometry(ctx, &gm), "load geometry");
         auto tB = std::chrono::high_resolution_clock::now();
         std::cout << "#Init variables -> Done (" << std::chrono::duration<double>(tB - tA).count() << " s )\n";

@@ -72,7 +72,7 @@ struct bte_ctx {
     // static tables
     bool modes_dev = false, geom_dev = false, lambert_dev = false;
     bte::DBuf d_vxc, d_vyc, d_w, d_tau, d_mv;
-    bte::DBuf d_boxes, d_hull, d_borders, d_contacts;
+    bte::DBuf d_boxes, d_hull, d_borders, d_contacts, d_cseg, d_transl;
     bte::DBuf d_gx, d_gy, d_gcell, d_boxcell;
     bte::DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;
     int nclass = 0;

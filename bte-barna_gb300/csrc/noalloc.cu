@@ -142,6 +142,7 @@ extern "C" bte_status bte_rta_run_noalloc(bte_ctx* ctx, const bte_rta_params* pa
     out->absorbed = (int64_t)hc[3];
     out->specular_hits = (int64_t)hc[4];
     out->tally_updates = (int64_t)hc[7];
+    out->translations = 0;
     out->kernel_ms = ms;
     return BTE_OK;
 }

@@ -6,6 +6,7 @@
 //   get_inter_side        src/geometry_2d.cpp:160-293
 //   in_corner3            src/geometry_2d.cpp:388-406
 //   correct_corner_problem include/geometry_2d.hpp:524-561
+//   translate             include/geometry_2d.hpp:366-493 (periodic boxes)
 //   Init_generator        src/RTA_MC2D.cpp:421-511 (walls)
 //   init_particles        src/beyondRTA_MC2d.cpp:211-269 (initial deviation)
 // The policy P supplies the random draws, the samplers and the tally, so the
@@ -46,6 +47,8 @@ struct DevTables {
     const V2* hull;
     const GBorder* borders;
     const GContact* contacts;
+    const V2* cseg;         // [contact][2]: lengthened contact segment (sbl)
+    const V2* translation;  // [box]: <Translate_to> vector of periodic boxes
     int nclass;
     // Lambert rows
     const long long* row_ptr;
@@ -77,7 +80,8 @@ struct DevTables {
 };
 
 struct Counters {
-    unsigned long long events, wall_hits, crossings, absorbed, specular, nudges, quirks, tallies;
+    unsigned long long events, wall_hits, crossings, absorbed, specular, nudges, quirks, tallies,
+        translations;
 };
 
 struct Particle {
@@ -199,12 +203,99 @@ __device__ int correct_corner_problem(const DevTables& T, P& pol, V2 rf, V2 v, c
     return 0;
 }
 
+// geometry_2d::translate, include/geometry_2d.hpp:366-493: a particle in
+// periodic box `box` jumps by 1.0005 x its translation vector into the box
+// it maps to and from there into the neighbour that the jump segment meets.
+// Two behaviours of the reference are kept: boost's intersection() appends
+// to one point list, so every contact met by the segment reports the first
+// contact's crossing point; with several candidates the point is taken from
+// the candidate list at the position drawn among the filtered candidates.
+// Returns 0 or an error code.
+template <class P>
+__device__ int translate(const DevTables& T, P& pol, int box, V2 r0, V2 v, int& nbox, V2& rf) {
+    const int tib = T.boxes[box].tto;
+    const V2 tv = T.translation[box];
+    const V2 tj = scal(1.0005, tv);
+    if (tib < 0 || tib >= T.nboxes || almost_equal(norm(tj), 0.)) return E_GEOM;
+    const V2 p1 = add(r0, tj);
+    const GBox& TB = T.boxes[tib];
+    V2 tp;
+    bool found = false;
+    for (int k = 0; k < TB.nborders && !found; ++k) {
+        const GBorder& b = T.borders[TB.border_off + k];
+        found = seg_meet(r0, p1, b.la, b.lb, tp);
+    }
+    if (!found) return E_GEOM;  // "Error in translation, no box found"
+    const V2 tp_T = sub(tp, divs(scal(1.0e-6, tv), norm(tv)));
+    const V2 tp_v = add(tp, divs(scal(1.0e-6, v), norm(v)));
+    int pb[MAXC];
+    V2 prf[MAXC];
+    int np = 0;
+    bool have_first = false;
+    V2 first = v2(0., 0.);
+    for (int i = 0; i < TB.ncontacts; ++i) {
+        const int ci = TB.contact_off + i;
+        const int ibc = T.contacts[ci].id;
+        V2 xin;
+        const bool here_i = seg_meet(r0, p1, T.cseg[2 * ci], T.cseg[2 * ci + 1], xin);
+        const bool here_T = box_inside(T, ibc, tp);
+        const bool here_Tv = box_inside(T, ibc, tp_v);
+        const bool here_TT = box_inside(T, ibc, tp_T);
+        const bool here = here_i || here_T || here_Tv || here_TT;
+        if (ibc == tib || !here || T.boxes[ibc].tto >= 0 || T.boxes[ibc].reservoir) continue;
+        V2 r;
+        if (here_i) {
+            if (!have_first) {
+                first = xin;
+                have_first = true;
+            }
+            r = first;
+        } else if (here_T) {
+            r = tp;
+        } else if (here_Tv) {
+            r = tp_v;
+        } else {
+            r = tp_T;
+        }
+        if (np == MAXC) return E_LIMIT;
+        pb[np] = ibc;
+        prf[np] = r;
+        np++;
+    }
+    if (np > 1) {
+        int p2[MAXC];
+        int n2 = 0;
+        for (int i = 0; i < np; ++i)
+            if (box_inside(T, pb[i], add(prf[i], scal(1.0e-6, v)))) p2[n2++] = i;
+        if (n2 == 0) return E_GEOM;  // the reference draws from an empty range here
+        const int pos = pol.choose(n2);
+        rf = prf[pos];
+        nbox = pb[p2[pos]];
+    } else if (np == 1) {
+        nbox = pb[0];
+        rf = prf[0];
+    } else {
+        return E_GEOM;  // "Error in Translation"
+    }
+    return 0;
+}
+
 // evolparticle (transient).  Returns 0 or an error code.
 template <class P>
 __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, double& dt,
                             Counters& c, int& nudges) {
     const V2 opos = p.pos;
     const GBox& box = T.boxes[p.box];
+    if (box.tto >= 0) {  // periodic box (src/RTA_MC2D.cpp:1034-1042)
+        int nb;
+        V2 rf;
+        const int e = translate(T, pol, p.box, opos, v, nb, rf);
+        if (e) return e;
+        p.box = nb;
+        p.pos = rf;
+        c.translations++;
+        return 0;
+    }
     if (box.reservoir) {
         p.mode = 0;
         dt = 0.;
@@ -354,7 +445,7 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
         if (n2 == 0) {
             newid = pboxes[pol.choose(np)];
             const V2 d = sub(T.boxes[newid].center, rnew);
-            p.pos = add(p.pos, divs(scal(1.0e-6, d), norm(d)));
+            if (T.boxes[newid].tto < 0) p.pos = add(p.pos, divs(scal(1.0e-6, d), norm(d)));
         } else {
             newid = pbox2[pol.choose(n2)];
         }

@@ -21,11 +21,14 @@ __device__ __forceinline__ void record_error(int* err, int e, long long pid) {
     }
 }
 
+// Warp-reduced counters: the first NC of (events, wall hits, crossings,
+// absorbed, specular, nudges, quirks, tally updates, translations).
+template <int NC = 9>
 __device__ __forceinline__ void flush_counters_p(const Counters& c, unsigned long long* out) {
-    unsigned long long v[8] = {c.events, c.wall_hits, c.crossings, c.absorbed,
-                               c.specular, c.nudges, c.quirks, c.tallies};
+    unsigned long long v[9] = {c.events, c.wall_hits, c.crossings, c.absorbed,
+                               c.specular, c.nudges, c.quirks, c.tallies, c.translations};
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < NC; ++i) {
         unsigned long long x = v[i];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + i, x);
@@ -92,7 +95,7 @@ struct ProdPolicy {
 
 __global__ void __launch_bounds__(128) rta_prod_general(DevTables T, double* tally,
                                                         unsigned long long* counters, int* err) {
-    Counters c = {0, 0, 0, 0, 0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long n = T.pend - T.pbegin;
     const long long trips = (n + stride - 1) / stride;
@@ -239,7 +242,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         __syncthreads();
         tally = stally;
     }
-    Counters c = {0, 0, 0, 0, 0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int lane = threadIdx.x & 31;
     const long long total = T.pend - T.pbegin;
     const int last_bin = T.nbins - 1;
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         }
     }
     c.tallies = pd.flushes;
-    flush_counters_p(c, counters);
+    flush_counters_p<8>(c, counters);  // no periodic boxes on the grid path
     if (SMEM_TALLY) {
         __syncthreads();
         for (int k = threadIdx.x; k < nk3; k += blockDim.x) {

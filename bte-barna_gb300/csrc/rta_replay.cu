@@ -75,10 +75,10 @@ struct ReplayPolicy {
 };
 
 __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long long* out) {
-    unsigned long long v[8] = {c.events, c.wall_hits, c.crossings, c.absorbed,
-                               c.specular, c.nudges, c.quirks, c.tallies};
+    unsigned long long v[9] = {c.events, c.wall_hits, c.crossings, c.absorbed,
+                               c.specular, c.nudges, c.quirks, c.tallies, c.translations};
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < 9; ++i) {
         unsigned long long x = v[i];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + i, x);
@@ -87,7 +87,7 @@ __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long 
 
 __global__ void __launch_bounds__(128) rta_replay_kernel(DevTables T, unsigned long long* ex,
                                                          unsigned long long* counters, int* err) {
-    Counters c = {0, 0, 0, 0, 0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     // every lane runs the same trip count so the closing shuffles see a full warp
     const long long n = T.pend - T.pbegin;

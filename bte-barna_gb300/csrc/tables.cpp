@@ -266,6 +266,18 @@ HostGeometry build_geometry(const bte_geometry* g) {
         G.Teq.push_back(g->Teq[i]);
         G.Tinit.push_back(g->Tinit ? g->Tinit[i] : g->Teq[i]);
         G.reservoir.push_back(g->reservoir[i] != 0);
+        const int to = g->translate_to ? g->translate_to[i] : -1;
+        G.tto.push_back(to);
+        G.translation.push_back(to >= 0 && g->translation
+                                    ? v2(g->translation[2 * i], g->translation[2 * i + 1])
+                                    : v2(0., 0.));
+        if (to >= 0) {
+            if (to >= g->nboxes || to == i)
+                throw Error(BTE_ERR_GEOMETRY, "Error: Bad id for mapping of periodic cells");
+            if (!g->translation) throw Error(BTE_ERR_INPUT, "periodic box without a translation vector");
+            if (g->reservoir[i]) throw Error(BTE_ERR_GEOMETRY, "a box cannot be periodic and a reservoir");
+            G.periodic = true;
+        }
     }
     const int nbx = g->nboxes;
     std::vector<std::array<double, 4>> bx(static_cast<std::size_t>(nbx));
@@ -338,11 +350,16 @@ HostGeometry build_geometry(const bte_geometry* g) {
             c.np = cb.np;
             G.contacts.push_back(c);
             G.contact_borders.push_back(cb);
+            const bool point = cb.p1.x == cb.p2.x && cb.p1.y == cb.p2.y;
+            G.contact_seg.push_back(point ? cb.p1 : cb.la);
+            G.contact_seg.push_back(point ? cb.p1 : cb.lb);
         }
         box.reservoir = G.reservoir[std::size_t(a)];
+        box.tto = G.tto[std::size_t(a)];
         G.boxes.push_back(box);
     }
-    detect_grid(G, bb);
+    // periodic jumps leave the cell walk of the grid path: general kernels
+    if (!G.periodic) detect_grid(G, bb);
     return G;
 }
 
@@ -565,7 +582,7 @@ Generators build_wall_generators(const HostModes& m, const HostGeometry& g) {
         const GBox& rb = g.boxes[std::size_t(s)];
         for (int ci = 0; ci < rb.ncontacts; ++ci) {
             const int c = g.contacts[std::size_t(rb.contact_off + ci)].id;
-            if (g.reservoir[std::size_t(c)]) continue;
+            if (g.reservoir[std::size_t(c)] || g.tto[std::size_t(c)] >= 0) continue;
             const GBorder& b = g.contact_borders[std::size_t(rb.contact_off + ci)];
             if (almost_equal(norm(sub(b.p2, b.p1)), 0.)) continue;
             const double Tw = g.Teq[std::size_t(s)], Te = g.Teq[std::size_t(c)];
@@ -622,7 +639,7 @@ Generators build_initial_generators(const HostModes& m, const HostGeometry& g) {
     const double vuc = m.V * g.thickness / m.c;
     std::vector<double> pmf(n);
     for (std::size_t s = 0; s < g.boxes.size(); ++s) {
-        if (g.reservoir[s]) continue;
+        if (g.reservoir[s] || g.tto[s] >= 0) continue;
         const double Tr = g.Tinit[s], Te = g.Teq[s];
         if (almost_equal(Te, Tr)) continue;
         if (Tr <= 0 || Te <= 0) throw Error(BTE_ERR_VALUE, "Invalid temperature value");

@@ -39,6 +39,10 @@ struct HostGeometry {
     std::vector<V2> normals;  // distinct border normals; GBorder::ncls indexes it
     std::vector<double> Teq, Tinit;
     std::vector<int> reservoir;
+    std::vector<int> tto;              // periodic: target box, -1 otherwise
+    std::vector<V2> translation;       // periodic: translation vector
+    std::vector<V2> contact_seg;       // [contact][2]: lengthened contact segment
+    bool periodic = false;             // any periodic box
     double thickness = 0;
     // axis-aligned grid description (production fast path); valid when
     // rect_grid is true: cell (i, j) -> box id or -1 (void / pore),

@@ -109,6 +109,39 @@ def ribbon_geometry(length: float = 1000.0, width: float = 100.0, ncells: int = 
     return _pack(boxes, Teq, list(Teq), res, thickness)
 
 
+def periodic_bar_geometry(width: float = 20.0, length: float = 40.0, nstrips: int = 10,
+                          T_hot: float = 302.0, T_cold: float = 300.0, T0: float = 300.0,
+                          thickness: float = C_LAT, side: float = 1.5, cap: float = 2.0) -> dict:
+    """A bar along y made of `nstrips` strips spanning the width, closed left
+    and right by periodic boxes that map onto each other (the layout of the
+    reference's example_bar: box nstrips at the right translates by -width
+    to box nstrips+1 at the left and back), with reservoirs below (T_hot) and
+    above (T_cold) that span the periodic boxes too."""
+    boxes, Teq, res = [], [], []
+    dy = length / nstrips
+    for j in range(nstrips):
+        boxes.append(_rect(0.0, j * dy, width, (j + 1) * dy))
+        Teq.append(T0)
+        res.append(0)
+    right, left = nstrips, nstrips + 1
+    boxes.append(_rect(width, 0.0, width + side, length))
+    boxes.append(_rect(-side, 0.0, 0.0, length))
+    Teq += [T0, T0]
+    res += [0, 0]
+    boxes.append(_rect(-side, -cap, width + side, 0.0))
+    boxes.append(_rect(-side, length, width + side, length + cap))
+    Teq += [T_hot, T_cold]
+    res += [1, 1]
+    g = _pack(boxes, Teq, list(Teq), res, thickness)
+    tto = np.full(len(boxes), -1, dtype=np.int32)
+    tr = np.zeros((len(boxes), 2))
+    tto[right], tr[right] = left, (-width, 0.0)
+    tto[left], tr[left] = right, (width, 0.0)
+    g["translate_to"] = tto
+    g["translation"] = tr
+    return g
+
+
 def grid_geometry(lx: float, ly: float, nx: int, ny: int, T0: float = 300.0,
                   pore_center=None, pore_diameter: float = 0.0,
                   hot_center=None, hot_sigma: float = 50.0, hot_dT: float = 0.0,
@@ -167,6 +200,12 @@ def write_geometry_xml(path: str, geom: dict, material: str = "synthetic") -> No
             lines.append(f'        <initCnd Teq="{teq!r}"/>')
         if geom["reservoir"][i]:
             lines.append("        <Reservoir/>")
+        tto = geom.get("translate_to")
+        if tto is not None and int(tto[i]) >= 0:
+            tx, ty = (float(v) for v in np.asarray(geom["translation"]).reshape(-1, 2)[i])
+            lines.append(f'        <Translate_to id="{int(tto[i])}">')
+            lines.append(f"            {tx!r} {ty!r} 0.0")
+            lines.append("        </Translate_to>")
         lines.append("    </Box>")
     lines.append("</Geometry>")
     with open(path, "w") as f:
@@ -292,6 +331,15 @@ def config1(n_particles: int = 100_000_000) -> dict:
                                   hot_center=(500.0, 250.0), hot_sigma=50.0, hot_dT=1.0),
             "T0": 300.0, "dt": 50.0, "maxtime": 10000.0, "N": n_particles,
             "specularity": 0.3, "source": "initial"}
+
+
+def periodic_case(n: int = 8, n_particles: int = 2000, maxtime: float = 200.0,
+                  dt: float = 10.0) -> dict:
+    """Parity-sized periodic bar (transient, walls source)."""
+    return {"modes": mode_table(n, 3, 3, 300.0, config=100),
+            "geom": periodic_bar_geometry(),
+            "T0": 300.0, "dt": dt, "maxtime": maxtime, "N": n_particles,
+            "specularity": 0.0, "source": "walls"}
 
 
 def small_case(n: int = 8, ncells: int = 5, n_particles: int = 2000, maxtime: float = 200.0,

@@ -98,6 +98,11 @@ typedef struct bte_geometry {
     const double* Tinit;      /* [nboxes] initCnd Tinit (= Teq when absent), K  */
     const int32_t* reservoir; /* [nboxes] 1 for <Reservoir/>                    */
     double thickness;         /* material thickness, nm (<material thickness>)  */
+    /* Periodic boxes, <Translate_to id="j"> tx ty </Translate_to>
+     * (src/geometry_2d.cpp:467-475, geometry_2d::translate
+     * include/geometry_2d.hpp:366-493).  Both NULL: no periodic box. */
+    const int32_t* translate_to; /* [nboxes] target box j, -1 = not periodic   */
+    const double* translation;   /* [nboxes][2] translation vector, nm         */
 } bte_geometry;
 
 /* Parameters of one RTA run (the <RTA_MC2d> XML of src/RTA_MC2D.cpp:1818-1947
@@ -139,6 +144,7 @@ typedef struct bte_rta_result {
     int64_t specular_hits;   /* specular reflections (p > 0)                     */
     int64_t tally_updates;   /* (box, time-bin) contributions made               */
     double kernel_ms;        /* device time of the particle loop                 */
+    int64_t translations;    /* jumps through periodic boxes                     */
 } bte_rta_result;
 
 /* Propagator exp(B dt) of one material at one temperature over the modes

@@ -45,6 +45,9 @@ def load():
     lib.oracle_inter_side.argtypes = [C.POINTER(_bt.Geometry), C.c_int] + [C.c_double] * 5 + [
         C.POINTER(C.c_double)]
     lib.oracle_inter_side.restype = C.c_int
+    lib.oracle_translate.argtypes = [C.POINTER(_bt.Geometry), C.c_int] + [C.c_double] * 4 + [
+        C.c_uint64, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.oracle_translate.restype = C.c_int
     lib.oracle_pcg64.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
     lib.oracle_log.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int]
@@ -69,6 +72,20 @@ def timegrid(dt, maxtime):
     out = np.zeros(n)
     lib.oracle_timegrid(dt, maxtime, out.ctypes.data_as(C.POINTER(C.c_double)), n)
     return out
+
+
+def translate(geom: dict, ibox: int, x: float, y: float, vx: float, vy: float, seed=1, stream=0):
+    """One periodic jump of the restatement: (new box, (x, y))."""
+    lib = load()
+    gs, keep = _bt.geom_struct(geom)
+    nb = C.c_int()
+    xy = np.zeros(2)
+    st = lib.oracle_translate(C.byref(gs), int(ibox), float(x), float(y), float(vx), float(vy),
+                              C.c_uint64(seed), C.c_uint64(stream), C.byref(nb),
+                              xy.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    return nb.value, (float(xy[0]), float(xy[1]))
 
 
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,
@@ -99,7 +116,8 @@ def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, 
         raise _bt.BteError(st, lib.oracle_last_error().decode())
     out.update(Eeff=r.Eeff, energy_rate=r.energy_rate, events=int(cnt[0]), wall_hits=int(cnt[1]),
                crossings=int(cnt[2]), absorbed=int(cnt[3]), nudges=int(cnt[4]), quirks=int(cnt[5]),
-               specular_hits=int(r.specular_hits), loop_seconds=float(cnt[6]) * 1e-6)
+               specular_hits=int(r.specular_hits), translations=int(r.translations),
+               loop_seconds=float(cnt[6]) * 1e-6)
     return out
 
 

@@ -219,6 +219,41 @@ inline bool seg_intersect(V2 s0, V2 s1, V2 l0, V2 l1, V2& out) {
     return true;
 }
 
+// boost::geometry::intersects + intersection of two closed segments: true
+// when s0-s1 and l0-l1 share a point, `out` = the first shared point (a
+// crossing is taken on l0-l1; collinear overlap: the overlap end nearest s0;
+// a degenerate l is its point).  Boost's own choice for collinear overlaps is
+// not available here; the restatement defines it.
+inline bool seg_meet(V2 s0, V2 s1, V2 l0, V2 l1, V2& out) {
+    V2 d1 = s1 - s0, d2 = l1 - l0;
+    if (d2.x == 0. && d2.y == 0.) {
+        if (!on_segment(l0, s0, s1)) return false;
+        out = l0;
+        return true;
+    }
+    double den = cross(d1, d2);
+    V2 w = l0 - s0;
+    if (den != 0.) {
+        double t = cross(w, d2) / den;
+        double u = cross(w, d1) / den;
+        if (!(t >= 0. && t <= 1. && u >= 0. && u <= 1.)) return false;
+        out = l0 + u * d2;
+        return true;
+    }
+    if (cross(w, d1) != 0.) return false;
+    double dd = dot(d1, d1);
+    if (dd == 0.) {
+        if (!on_segment(s0, l0, l1)) return false;
+        out = s0;
+        return true;
+    }
+    double a = dot(l0 - s0, d1) / dd, b = dot(l1 - s0, d1) / dd;
+    double lo = std::min(a, b), hi = std::max(a, b);
+    if (hi < 0. || lo > 1.) return false;
+    out = lo <= 0. ? s0 : (a < b ? l0 : l1);
+    return true;
+}
+
 struct Box {
     std::vector<V2> hull;  // counter-clockwise convex hull
     V2 center;
@@ -227,6 +262,9 @@ struct Box {
     std::map<std::size_t, std::vector<Border>> contacts;
     double Teq = -1, Treal = -1;
     bool reservoir = false;
+    bool periodic = false;       // <Translate_to>
+    std::size_t box2translate = 0;
+    V2 translation;
     std::size_t id = 0;
 
     bool inside(V2 p) const {
@@ -609,7 +647,7 @@ inline void build_generators(Sim& S, double /*T0*/, bool required = true) {
     for (auto& s : S.sys) {
         if (!s.reservoir) continue;
         for (auto& [c, bv] : s.contacts) {
-            if (S.sys[c].reservoir) continue;
+            if (S.sys[c].reservoir || S.sys[c].periodic) continue;
             const Border& b = bv[0];
             if (almost_equal(norm(b.p2 - b.p1), 0.)) continue;
             if (almost_equal(s.Teq, S.sys[c].Teq)) continue;
@@ -671,7 +709,7 @@ struct Tally {
     std::vector<double> gz, jx, jy;
     std::vector<__int128> ex;  // [box][bin][3]
     int64_t events = 0, wall_hits = 0, crossings = 0, absorbed = 0, nudges = 0,
-            quirks = 0, specular = 0;
+            quirks = 0, specular = 0, translations = 0;
     void init(std::size_t nbx, std::size_t nbn) {
         nboxes = nbx;
         nbins = nbn;
@@ -760,12 +798,83 @@ inline std::size_t correct_corner_problem(const Sim& S, V2 rf, V2 v,
     return finalist[std::size_t(uniform_int(rng, 0, int(finalist.size()) - 1))];
 }
 
+// geometry_2d::translate, include/geometry_2d.hpp:366-493.  The particle in
+// periodic box `ib` jumps by 1.0005 x the translation into box2translate and
+// from there into the first-level neighbour the jump segment meets.  As in
+// the reference, boost's intersection() appends to one point list, so every
+// contact met by the segment reports the first contact's point, and with
+// several candidates the point is read at the drawn position of the
+// filtered list.
+inline std::pair<std::size_t, V2> translate(const Sim& S, std::size_t ib, V2 r0, V2 v, Pcg64& rng) {
+    const Box& me = S.sys[ib];
+    if (!me.periodic) throw geometry_error("Error: this can only be used in periodic cells");
+    V2 T = 1.0005 * me.translation;
+    std::size_t tib = me.box2translate;
+    if (tib >= S.sys.size() || almost_equal(norm(T), 0.))
+        throw geometry_error("Error: Bad id for mapping of periodic cells");
+    V2 p1 = r0 + T;
+    const Box& TB = S.sys[tib];
+    V2 tp;
+    bool found = false;
+    for (auto& b : TB.borders)
+        if (seg_meet(r0, p1, b.la, b.lb, tp)) {
+            found = true;
+            break;
+        }
+    if (!found) throw geometry_error("Error in translation, no box found");
+    V2 tp_T = tp - (1.0e-6 * me.translation) / norm(me.translation);
+    V2 tp_v = tp + (1.0e-6 * v) / norm(v);
+    std::vector<V2> rf;
+    std::vector<std::size_t> pboxes;
+    std::vector<V2> rinter;  // boost's output list: appended, never cleared in the loop
+    for (auto& [ibc, bv] : TB.contacts) {
+        const Border& cb = bv[0];
+        bool point = cb.p1.x == cb.p2.x && cb.p1.y == cb.p2.y;
+        V2 la = point ? cb.p1 : cb.la, lb = point ? cb.p1 : cb.lb;
+        V2 xin;
+        bool here_i = seg_meet(r0, p1, la, lb, xin);
+        bool here_T = S.sys[ibc].inside(tp);
+        bool here_Tv = S.sys[ibc].inside(tp_v);
+        bool here_TT = S.sys[ibc].inside(tp_T);
+        bool here = here_i || here_T || here_Tv || here_TT;
+        if (ibc == tib || !here || S.sys[ibc].periodic || S.sys[ibc].reservoir) continue;
+        if (here_i) {
+            rinter.push_back(xin);
+            rf.push_back(rinter[0]);
+        } else if (here_T) {
+            rf.push_back(tp);
+        } else if (here_Tv) {
+            rf.push_back(tp_v);
+        } else {
+            rf.push_back(tp_T);
+        }
+        pboxes.push_back(ibc);
+    }
+    if (pboxes.size() > 1) {
+        std::vector<std::size_t> pboxes2;
+        for (std::size_t k = 0; k < pboxes.size(); ++k)
+            if (S.sys[pboxes[k]].inside(rf[k] + 1.0e-6 * v)) pboxes2.push_back(pboxes[k]);
+        if (pboxes2.empty()) throw geometry_error("translation: no candidate box ahead");
+        std::size_t pos = std::size_t(uniform_int(rng, 0, int(pboxes2.size()) - 1));
+        return {pboxes2[pos], rf[pos]};
+    }
+    if (pboxes.size() == 1) return {pboxes[0], rf[0]};
+    throw geometry_error("Error in Translation");
+}
+
 // evolparticle (transient, one material), src/RTA_MC2D.cpp:990-1386.
 inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng,
                          Tally& T, const Opts& o) {
     const std::size_t nb = S.m.nb;
     V2 opos = p.pos;
     const Box& box = S.sys[p.box];
+    if (box.periodic) {  // Apply PBC, :1034-1042
+        auto sol = translate(S, p.box, opos, v, rng);
+        p.box = sol.first;
+        p.pos = sol.second;
+        T.translations++;
+        return;
+    }
     if (box.reservoir) {
         p.q = 0;
         p.alpha = 0;
@@ -890,7 +999,7 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
         if (pbox2.empty()) {
             newid = pboxes[std::size_t(uniform_int(rng, 0, int(pboxes.size()) - 1))];
             V2 d = S.sys[newid].center - rnew;
-            p.pos = p.pos + (1.0e-6 * d) / norm(d);
+            if (!S.sys[newid].periodic) p.pos = p.pos + (1.0e-6 * d) / norm(d);
         } else {
             newid = pbox2[std::size_t(uniform_int(rng, 0, int(pbox2.size()) - 1))];
         }
@@ -973,7 +1082,7 @@ inline void build_initial(Sim& S, int64_t nparticles, uint64_t seed) {
     const double vuc = m.V * S.thickness / m.c;
     std::vector<double> pmf(m.n()), energy;
     for (auto& s : S.sys) {
-        if (s.reservoir) continue;
+        if (s.reservoir || s.periodic) continue;
         if (almost_equal(s.Teq, s.Treal)) continue;
         if (s.Treal <= 0 || s.Teq <= 0) throw value_error("Invalid temperature value");
         for (std::size_t k = 0; k < m.n(); ++k) {
@@ -1332,6 +1441,11 @@ orc::Sim build_sim(const bte_mode_table* mt, const bte_geometry* gm) {
         b.Teq = gm->Teq[i];
         b.Treal = gm->Tinit ? gm->Tinit[i] : gm->Teq[i];
         b.reservoir = gm->reservoir[i] != 0;
+        if (gm->translate_to && gm->translate_to[i] >= 0) {
+            b.periodic = true;
+            b.box2translate = std::size_t(gm->translate_to[i]);
+            b.translation = {gm->translation[2 * i], gm->translation[2 * i + 1]};
+        }
         b.id = std::size_t(i);
         S.sys.push_back(std::move(b));
     }
@@ -1445,6 +1559,42 @@ void oracle_be(const double* omega, long long n, double T, double* be, double* k
     }
 }
 
+// One periodic jump (geometry_2d::translate) of a particle at (x, y) with
+// velocity (vx, vy) in periodic box ibox; draws from pcg64(seed, stream).
+int oracle_translate(const bte_geometry* gm, int ibox, double x, double y, double vx, double vy,
+                     uint64_t seed, uint64_t stream, int* nbox, double* xy) {
+    try {
+        bte_mode_table mt{};
+        orc::Sim S;
+        S.thickness = gm->thickness;
+        std::size_t off = 0;
+        for (int i = 0; i < gm->nboxes; ++i) {
+            std::vector<orc::V2> verts;
+            for (int j = 0; j < gm->npoints[i]; ++j, ++off)
+                verts.push_back({gm->vertices[2 * off], gm->vertices[2 * off + 1]});
+            orc::Box b = orc::make_box(verts);
+            b.reservoir = gm->reservoir[i] != 0;
+            if (gm->translate_to && gm->translate_to[i] >= 0) {
+                b.periodic = true;
+                b.box2translate = std::size_t(gm->translate_to[i]);
+                b.translation = {gm->translation[2 * i], gm->translation[2 * i + 1]};
+            }
+            b.id = std::size_t(i);
+            S.sys.push_back(std::move(b));
+        }
+        orc::calculate_contacts(S.sys);
+        (void)mt;
+        orc::Pcg64 rng(seed, stream);
+        auto sol = orc::translate(S, std::size_t(ibox), {x, y}, {vx, vy}, rng);
+        *nbox = int(sol.first);
+        xy[0] = sol.second.x;
+        xy[1] = sol.second.y;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
 // Lambert table row sizes (for the table-equality tests): nnz per mode.
 int oracle_lambert_nnz(const bte_mode_table* mt, const bte_geometry* gm, long long* nnz) {
     try {
@@ -1546,6 +1696,7 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
             T.nudges += tl[t].nudges;
             T.quirks += tl[t].quirks;
             T.specular += tl[t].specular;
+            T.translations += tl[t].translations;
         }
         out->nboxes = int32_t(nbx);
         out->nbins = int32_t(nbn);
@@ -1557,6 +1708,7 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
         out->absorbed = T.absorbed;
         out->specular_hits = T.specular;
         out->tally_updates = 0;
+        out->translations = T.translations;
         if (counters) {
             counters[0] = T.events; counters[1] = T.wall_hits; counters[2] = T.crossings;
             counters[3] = T.absorbed; counters[4] = T.nudges; counters[5] = T.quirks;
