@@ -27,7 +27,8 @@ SOURCE_WALLS, SOURCE_INITIAL = 0, 1
 # Exported symbols declared in include/btegpu.h.
 PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
-                  "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run"]
+                  "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run",
+                  "bte_steady_run"]
 
 
 class BteError(RuntimeError):
@@ -91,6 +92,52 @@ class BertaResult(C.Structure):
                 ("flux", C.POINTER(C.c_double)), ("nparticles", C.POINTER(C.c_int64)),
                 ("histogram", C.POINTER(C.c_int32)), ("particle_steps", C.c_int64),
                 ("branchings", C.c_int64), ("kernel_ms", C.c_double)]
+
+
+class SteadyParams(C.Structure):
+    _fields_ = [("T0", C.c_double), ("gradient", C.c_double * 2), ("eps_energy", C.c_double),
+                ("eps_flux", C.c_double), ("nparticles", C.c_int64), ("seed", C.c_uint64),
+                ("mode", C.c_int32), ("max_generations", C.c_int32)]
+
+
+class SteadyResult(C.Structure):
+    _fields_ = [("nboxes", C.c_int32), ("generations", C.c_int32), ("converged", C.c_int32),
+                ("log_cap", C.c_int32), ("gz", C.POINTER(C.c_double)),
+                ("gz_jx", C.POINTER(C.c_double)), ("gz_jy", C.POINTER(C.c_double)),
+                ("temperature", C.POINTER(C.c_double)), ("jx", C.POINTER(C.c_double)),
+                ("jy", C.POINTER(C.c_double)), ("exact", C.POINTER(C.c_int64)),
+                ("log", C.POINTER(C.c_double)), ("Eeff", C.c_double), ("energy_rate", C.c_double),
+                ("events", C.c_int64), ("wall_hits", C.c_int64), ("crossings", C.c_int64),
+                ("absorbed", C.c_int64), ("translations", C.c_int64), ("scattered", C.c_int64),
+                ("births", C.c_int64), ("lost", C.c_int64), ("kernel_ms", C.c_double)]
+
+
+STEADY_KEYS = ("generations", "converged", "Eeff", "energy_rate", "events", "wall_hits", "crossings",
+               "absorbed", "translations", "scattered", "births", "lost", "kernel_ms")
+
+
+def steady_call(fn, nboxes, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_energy=-42.0,
+                eps_flux=-42.0, max_generations=0, log_cap=100000):
+    """Fill SteadyParams / SteadyResult, call fn(params, result), return a dict."""
+    p = SteadyParams()
+    p.T0 = float(T0)
+    p.gradient[0], p.gradient[1] = float(gradient[0]), float(gradient[1])
+    p.eps_energy, p.eps_flux = float(eps_energy), float(eps_flux)
+    p.nparticles, p.seed, p.mode = int(N), int(seed), int(mode)
+    p.max_generations = int(max_generations)
+    out = {k: np.zeros(nboxes) for k in ("gz", "gz_jx", "gz_jy", "temperature", "jx", "jy")}
+    out["exact"] = np.zeros((nboxes, 3, 2), dtype=np.int64)
+    out["log"] = np.zeros((log_cap, 4))
+    r = SteadyResult()
+    for k in ("gz", "gz_jx", "gz_jy", "temperature", "jx", "jy", "log"):
+        setattr(r, k, _dptr(out[k]))
+    r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
+    r.log_cap = log_cap
+    fn(p, r)
+    for k in STEADY_KEYS:
+        out[k] = getattr(r, k)
+    out["log"] = out["log"][:min(r.generations, log_cap)].copy()
+    return out
 
 
 def berta_steps(dt: float, maxtime: float) -> int:
@@ -192,6 +239,8 @@ def load_library(path: str = LIB_PATH):
     lib.bte_load_propagator.restype = C.c_int
     lib.bte_berta_run.argtypes = [vp, C.POINTER(BertaParams), C.POINTER(BertaResult)]
     lib.bte_berta_run.restype = C.c_int
+    lib.bte_steady_run.argtypes = [vp, C.POINTER(SteadyParams), C.POINTER(SteadyResult)]
+    lib.bte_steady_run.restype = C.c_int
     lib.bte_rta_run_noalloc.argtypes = [vp, C.POINTER(RtaParams), C.c_void_p, C.POINTER(RtaResult)]
     lib.bte_rta_run_noalloc.restype = C.c_int
     for f in ("bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
@@ -310,6 +359,16 @@ def _engine_berta_run(self, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, canc
             "particle_steps": r.particle_steps, "branchings": r.branchings, "kernel_ms": r.kernel_ms}
 
 
+def _engine_steady_run(self, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_energy=-42.0,
+                       eps_flux=-42.0, max_generations=0, log_cap=100000):
+    """Steady state of a periodic structure under `gradient` (K/nm)."""
+    def call(p, r):
+        self._check(self.lib.bte_steady_run(self.ctx, C.byref(p), C.byref(r)))
+    return steady_call(call, self.nboxes, T0, gradient, N, seed, mode, eps_energy, eps_flux,
+                       max_generations, log_cap)
+
+
+Engine.steady_run = _engine_steady_run
 Engine.load_propagator = _engine_load_propagator
 Engine.berta_run = _engine_berta_run
 

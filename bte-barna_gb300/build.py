@@ -27,6 +27,7 @@ UNITS = [
     ("capi.cu", []),
     ("noalloc.cu", []),
     ("berta.cu", []),
+    ("steady.cu", []),
 ]
 
 

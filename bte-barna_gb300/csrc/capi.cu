@@ -230,6 +230,7 @@ bte_status bte_destroy(bte_ctx* c) {
     if (c->ev1) cudaEventDestroy(c->ev1);
     cudaStream_t s = c->stream;
     bte::destroy_berta(c);
+    bte::destroy_steady(c);
     delete c;
     if (s) cudaStreamDestroy(s);
     return BTE_OK;
@@ -732,6 +733,31 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
     r->nsm = c->nsm;
     r->tune = c->tune;
     return BTE_OK;
+}
+
+void fill_static_tables(bte_ctx* c, DevTables& T) {
+    T.n = int(c->modes.n());
+    T.nb = c->modes.nb;
+    T.vxc = c->d_vxc.as<double>();
+    T.vyc = c->d_vyc.as<double>();
+    T.w = c->d_w.as<double>();
+    T.tau = c->d_tau.as<double>();
+    T.resample_cdf = c->d_rcdf.as<double>();
+    T.resample_prob = c->d_rprob.as<float>();
+    T.resample_alt = c->d_ralt.as<int>();
+    T.nboxes = int(c->geom.boxes.size());
+    T.boxes = c->d_boxes.as<GBox>();
+    T.hull = c->d_hull.as<V2>();
+    T.borders = c->d_borders.as<GBorder>();
+    T.contacts = c->d_contacts.as<GContact>();
+    T.cseg = c->d_cseg.as<V2>();
+    T.translation = c->d_transl.as<V2>();
+    T.nclass = c->nclass;
+    T.row_ptr = c->d_row_ptr.as<long long>();
+    T.lcol = c->d_lcol.as<int>();
+    T.lcdf = c->d_lcdf.as<double>();
+    T.lalias = c->d_lalias.as<int4>();
+    T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
 }
 
 void set_ctx_error(bte_ctx* c, const std::string& m) {

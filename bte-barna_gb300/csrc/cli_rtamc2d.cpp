@@ -218,6 +218,7 @@ int main(int argc, char** argv) {
         std::string gfile, dbfile;
         double dt = 0, maxtime = 0, thickness = 0, T0 = -1, p = 0;
         long long N = 0;
+        double grad[2] = {0., 0.}, eps_energy = -42.0, eps_flux = -42.0;
         unsigned long long seed = 20261203ULL;
         int mode = BTE_MODE_PRODUCTION, source = BTE_SOURCE_WALLS, ballistic = 0;
         for (auto& k : root->kids) {
@@ -233,7 +234,15 @@ int main(int argc, char** argv) {
             }
             if (k->name == "particles") N = std::stoll(k->get("N"));
             if (k->name == "ballistic") ballistic = 1;
-            if (k->name == "gradient") throw std::runtime_error("<gradient> (periodic steady state) is not supported yet");
+            // <gradient x= y=/> and <convergence energy= flux=/>, src/RTA_MC2D.cpp:1828-1840
+            if (k->name == "gradient") {
+                grad[0] = std::stod(k->get("x"));
+                grad[1] = std::stod(k->get("y"));
+            }
+            if (k->name == "convergence") {
+                eps_energy = std::stod(k->get("energy"));
+                eps_flux = std::stod(k->get("flux"));
+            }
             if (k->name == "layer" || k->name == "layers_connection")
                 throw std::runtime_error("multi-material layers are not supported");
             if (k->name == "engine") {
@@ -313,6 +322,59 @@ int main(int argc, char** argv) {
         check(ctx, bte_load_geometry(ctx, &gm), "load geometry");
         auto tB = std::chrono::high_resolution_clock::now();
         std::cout << "#Init variables -> Done (" << std::chrono::duration<double>(tB - tA).count() << " s )\n";
+        const double gnorm = std::sqrt(grad[0] * grad[0] + grad[1] * grad[1]);
+        if (!(std::fabs(gnorm) < 1e-8)) {
+            // periodic structure under a gradient: steady state only, :2544-2842
+            std::cout << "PERIODIC CASE: [only steady state is simulated]\n";
+            if (eps_energy > 0.) std::cout << "#energy convergence " << eps_energy << std::endl;
+            if (eps_flux > 0.) std::cout << "#flux convergence " << eps_flux << std::endl;
+            const int nbx = int(npts.size());
+            for (long irun = 0; irun < nruns; ++irun) {
+                bte_steady_params sp{};
+                sp.T0 = T0;
+                sp.gradient[0] = grad[0];
+                sp.gradient[1] = grad[1];
+                sp.eps_energy = eps_energy;
+                sp.eps_flux = eps_flux;
+                sp.nparticles = N;
+                sp.seed = seed + (unsigned long long)irun;
+                sp.mode = mode;
+                std::vector<double> T(static_cast<std::size_t>(nbx)), jx(T.size()), jy(T.size());
+                std::vector<double> log(static_cast<std::size_t>(4) * 100000);
+                bte_steady_result out{};
+                out.temperature = T.data();
+                out.jx = jx.data();
+                out.jy = jy.data();
+                out.log = log.data();
+                out.log_cap = 100000;
+                std::cout << "#Run: " << irun << std::endl;
+                auto t0 = std::chrono::high_resolution_clock::now();
+                check(ctx, bte_steady_run(ctx, &sp, &out), "steady run");
+                auto t1 = std::chrono::high_resolution_clock::now();
+                for (int gi = 0; gi < out.generations && gi < out.log_cap; ++gi) {
+                    const double* r = &log[std::size_t(gi) * 4];
+                    std::cout << gi + 1 << '\t' << (long long)r[0] << '\t' << r[1];
+                    if (std::fabs(grad[0]) < 1e-8 || std::fabs(grad[1]) < 1e-8)
+                        std::cout << '\t' << (std::fabs(grad[0]) < 1e-8 ? r[3] : r[2]) << '\n';
+                    else
+                        std::cout << '\t' << r[2] << '\t' << r[3] << '\n';
+                }
+                std::cout << "#|E| =" << out.energy_rate << " J/ps\n#Eeff = " << out.Eeff << "\n"
+                          << "#MC loop -> Done ( " << std::chrono::duration<double>(t1 - t0).count()
+                          << " s ), " << out.generations << " generations, " << out.events
+                          << " flight events" << std::endl;
+                std::cout << "# Writing steady state" << std::endl;
+                const std::string fn = "steady_" + fmt_g(T0) + "K_run_" + std::to_string(irun) + ".csv";
+                std::ofstream o(fn);
+                if (!o) throw std::runtime_error("cannot write " + fn);
+                const std::vector<double>* rows[3] = {&T, &jx, &jy};
+                for (auto* row : rows) {
+                    for (int b = 0; b < nbx; ++b) o << (b ? "," : "") << (*row)[std::size_t(b)];
+                    o << '\n';
+                }
+            }
+            return 0;
+        }
         for (long irun = 0; irun < nruns; ++irun) {
             bte_rta_params rp{};
             rp.T0 = T0;

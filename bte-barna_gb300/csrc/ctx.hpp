@@ -52,7 +52,8 @@ inline int hw_threads() {
     return n ? int(n < 64u ? n : 64u) : 4;
 }
 
-struct BertaState;  // berta.cu
+struct BertaState;   // berta.cu
+struct SteadyState;  // steady.cu
 
 }  // namespace bte
 
@@ -92,6 +93,8 @@ struct bte_ctx {
     std::vector<double> h_time;
     // beyond-RTA (berta.cu)
     bte::BertaState* berta = nullptr;
+    // periodic / gradient steady state (steady.cu)
+    bte::SteadyState* steady = nullptr;
 };
 
 namespace bte {
@@ -100,4 +103,7 @@ void ensure_static(bte_ctx* c);
 void ensure_resample(bte_ctx* c, double T0);
 void sync(bte_ctx* c);
 void destroy_berta(bte_ctx* c);
+void destroy_steady(bte_ctx* c);
+// Mode, geometry and Lambert tables of a context into the kernel tables.
+void fill_static_tables(bte_ctx* c, DevTables& T);
 }  // namespace bte

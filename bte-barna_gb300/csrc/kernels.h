@@ -29,6 +29,17 @@ void launch_replay(const DevTables& T, unsigned long long* ex, unsigned long lon
 void launch_prod_general(const DevTables& T, double* tally, unsigned long long* counters,
                          int* err, int nsm, cudaStream_t s);
 
+// One generation of the periodic / gradient steady state (rta_steady.cuh).
+// With `select_flags` set, only the generation-0 pre-pass runs: it writes 1
+// per slot whose first draw picks a gradient generator.
+struct SteadyArgs;
+void launch_steady_replay(const DevTables& T, const SteadyArgs& A, unsigned long long* ex,
+                          unsigned long long* counters, int* err, unsigned* select_flags, int nsm,
+                          cudaStream_t s);
+void launch_steady_prod(const DevTables& T, const SteadyArgs& A, double* tally,
+                        unsigned long long* counters, int* err, unsigned* select_flags, int nsm,
+                        cudaStream_t s);
+
 // Per-mode velocity record of the grid path.
 struct __align__(32) ModeVel {
     double vx, vy;    // get_v velocities, nm/ps

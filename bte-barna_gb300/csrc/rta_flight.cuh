@@ -81,8 +81,14 @@ struct DevTables {
 
 struct Counters {
     unsigned long long events, wall_hits, crossings, absorbed, specular, nudges, quirks, tallies,
-        translations;
+        translations, scattered, lost;
 };
+
+// How a steady-state flight ends (periodic / gradient branch).
+constexpr int FATE_LOST = 0;      // left_time rounded to 0 at a crossing: dropped
+constexpr int FATE_SCATTER = 1;   // scattered inside a box: counted in phi
+constexpr int FATE_BOUNCE = 2;    // reflected at a void wall: carried to the next generation
+constexpr int FATE_ABSORBED = 3;  // reached a reservoir
 
 struct Particle {
     V2 pos;
@@ -280,10 +286,22 @@ __device__ int translate(const DevTables& T, P& pol, int box, V2 r0, V2 v, int& 
     return 0;
 }
 
-// evolparticle (transient).  Returns 0 or an error code.
-template <class P>
+// process_segment of a segment of length d starting at the particle:
+// transient (time bins, src/RTA_MC2D.cpp:699-769) or steady (one value per
+// box, :784-834).
+template <bool STEADY, class P>
+__device__ __forceinline__ int seg_tally(const DevTables& T, P& pol, const Particle& p, double d, V2 v) {
+    if (STEADY) return pol.tally_dt(T, p.box, d, p.sign, v);
+    return pol.tally(T, p.box, p.t, p.t + d, p.sign, v);
+}
+
+// evolparticle: transient (src/RTA_MC2D.cpp:990-1386) or, with STEADY, the
+// periodic/gradient variant (:1406-1799): the flight ends inside a box with
+// phi += sign instead of a resample, and a reflected particle leaves the
+// generation (`fate`).  Returns 0 or an error code.
+template <class P, bool STEADY = false>
 __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, double& dt,
-                            Counters& c, int& nudges) {
+                            Counters& c, int& nudges, int& fate) {
     const V2 opos = p.pos;
     const GBox& box = T.boxes[p.box];
     if (box.tto >= 0) {  // periodic box (src/RTA_MC2D.cpp:1034-1042)
@@ -300,15 +318,21 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
         p.mode = 0;
         dt = 0.;
         c.absorbed++;
+        fate = FATE_ABSORBED;
         return 0;
     }
     V2 rnew = v2(p.pos.x + dt * v.x, p.pos.y + dt * v.y);
     if (inside_hull(T.hull + box.hull_off, box.nhull, rnew)) {
         p.pos = rnew;
-        int e = pol.tally(T, p.box, p.t, p.t + dt, p.sign, v);
+        int e = seg_tally<STEADY>(T, pol, p, dt, v);
         if (e) return e;
         p.t += dt;
-        if (!T.ballistic) p.mode = pol.resample(T);
+        if (STEADY) {
+            fate = FATE_SCATTER;
+            c.scattered++;
+        } else if (!T.ballistic) {
+            p.mode = pol.resample(T);
+        }
         dt = 0.;
         nudges = 0;
         return 0;
@@ -344,7 +368,7 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
         }
     }
     if (np == 0) {
-        int e = pol.tally(T, p.box, p.t, p.t + tf, p.sign, v);
+        int e = seg_tally<STEADY>(T, pol, p, tf, v);
         if (e) return e;
         p.t += tf;
         // in_corner3 over the boxes that can cover a border point: this box
@@ -422,17 +446,18 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
         p.mode = nm;
         dt = 0.;
         c.wall_hits++;
+        fate = FATE_BOUNCE;
         return 0;
     } else if (np == 1) {
         p.pos = rnew;
-        int e = pol.tally(T, p.box, p.t, p.t + tf, p.sign, v);
+        int e = seg_tally<STEADY>(T, pol, p, tf, v);
         if (e) return e;
         p.t += tf;
         p.box = pboxes[0];
         c.crossings++;
         return 0;
     } else {
-        int e = pol.tally(T, p.box, p.t, p.t + tf, p.sign, v);
+        int e = seg_tally<STEADY>(T, pol, p, tf, v);
         if (e) return e;
         p.t += tf;
         p.pos = rnew;
@@ -455,44 +480,38 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
     }
 }
 
-// Particle generation.  Returns 0 or an error code; `skip` is set when the
-// particle index has no particle (initial source beyond the generated count).
+// A wall particle of Init_generator (case 0, src/RTA_MC2D.cpp:453-497),
+// after the generator-type draw.
 template <class P>
-__device__ int generate(const DevTables& T, P& pol, long long pid, Particle& p) {
-    if (T.source == 0) {
-        const double selectGenR = pol.u();
-        (void)selectGenR;  // without a gradient source every particle comes from a wall
-        const double whereGenR = pol.u();
-        int g = lower_bound_d(T.wall_cum, T.ngen, whereGenR);
-        if (g >= T.ngen) g = T.ngen - 1;
-        const WallGenDev W = T.walls[g];
-        V2 ppos;
-        int tries = 0;
-        for (;;) {
-            if (++tries > 1000) return E_LIMIT;
-            ppos = add(W.p1, scal(pol.u(), W.nd));
-            if (on_segment(ppos, W.sa, W.sb)) break;
-        }
-        if (!box_inside(T, W.box, ppos)) {
-            const V2 d = sub(T.boxes[W.box].center, ppos);
-            ppos = add(ppos, divs(scal(1.0e-6, d), norm(d)));
-            if (!box_inside(T, W.box, ppos)) return E_GEOM;
-        }
-        p.mode = pol.gen_mode(T, g);
-        p.pos = ppos;
-        p.sign = W.sign;
-        p.t = 0.;
-        p.box = W.box;
-        return 0;
+__device__ int generate_wall(const DevTables& T, P& pol, Particle& p) {
+    const double whereGenR = pol.u();
+    int g = lower_bound_d(T.wall_cum, T.ngen, whereGenR);
+    if (g >= T.ngen) g = T.ngen - 1;
+    const WallGenDev W = T.walls[g];
+    V2 ppos;
+    int tries = 0;
+    for (;;) {
+        if (++tries > 1000) return E_LIMIT;
+        ppos = add(W.p1, scal(pol.u(), W.nd));
+        if (on_segment(ppos, W.sa, W.sb)) break;
     }
-    // initial deviation: particle -> box by the prefix of generated counts
-    int lo = 0, hi = T.ngen;  // find g with init_first[g] <= pid < init_first[g+1]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (T.init_first[mid] <= pid) lo = mid; else hi = mid;
+    if (!box_inside(T, W.box, ppos)) {
+        const V2 d = sub(T.boxes[W.box].center, ppos);
+        ppos = add(ppos, divs(scal(1.0e-6, d), norm(d)));
+        if (!box_inside(T, W.box, ppos)) return E_GEOM;
     }
-    const int g = lo;
-    const int b = T.init_box[g];
+    p.mode = pol.gen_mode(T, g);
+    p.pos = ppos;
+    p.sign = W.sign;
+    p.t = 0.;
+    p.box = W.box;
+    return 0;
+}
+
+// Uniform point of box b by bounding-box rejection
+// (geometry_2d::get_random_point, include/geometry_2d.hpp:338-356).
+template <class P>
+__device__ int random_point(const DevTables& T, P& pol, int b, V2& r) {
     const GBox& B = T.boxes[b];
     const V2* h = T.hull + B.hull_off;
     double x0 = h[0].x, x1 = h[0].x, y0 = h[0].y, y1 = h[0].y;
@@ -502,14 +521,33 @@ __device__ int generate(const DevTables& T, P& pol, long long pid, Particle& p) 
         y0 = fmin(y0, h[i].y);
         y1 = fmax(y1, h[i].y);
     }
-    V2 r;
     int tries = 0;
     for (;;) {
         if (++tries > 100000) return E_LIMIT;
         r.x = x0 + pol.u() * (x1 - x0);
         r.y = y0 + pol.u() * (y1 - y0);
-        if (inside_hull(h, B.nhull, r)) break;
+        if (inside_hull(h, B.nhull, r)) return 0;
     }
+}
+
+// Particle generation.  Returns 0 or an error code.
+template <class P>
+__device__ int generate(const DevTables& T, P& pol, long long pid, Particle& p) {
+    if (T.source == 0) {
+        (void)pol.u();  // generator type: without a gradient every particle comes from a wall
+        return generate_wall(T, pol, p);
+    }
+    // initial deviation: particle -> box by the prefix of generated counts
+    int lo = 0, hi = T.ngen;  // find g with init_first[g] <= pid < init_first[g+1]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (T.init_first[mid] <= pid) lo = mid; else hi = mid;
+    }
+    const int g = lo;
+    const int b = T.init_box[g];
+    V2 r;
+    const int e = random_point(T, pol, b, r);
+    if (e) return e;
     p.mode = pol.gen_mode(T, g);
     p.pos = r;
     p.sign = T.init_sign[g];
@@ -536,10 +574,10 @@ __device__ int run_particle(const DevTables& T, P& pol, long long pid, Counters&
         double dt = pol.flight(T, k);
         c.events++;
         if (time + dt > T.maxtime) dt = T.maxtime - time + 1.0e-8;
-        int guard = 0;
+        int guard = 0, fate = FATE_LOST;
         while (!almost_equal(dt, 0.)) {
             if (++guard > FLIGHT_CAP) return E_LIMIT;
-            e = evolparticle(T, pol, p, v, dt, c, nudges);
+            e = evolparticle(T, pol, p, v, dt, c, nudges, fate);
             if (e) return e;
         }
         if (p.mode == 0) break;

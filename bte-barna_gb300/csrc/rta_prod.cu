@@ -11,6 +11,7 @@
 //                     and that walks cells by exit times, with a per-lane
 //                     pending tally flushed when the (box, bin) key changes.
 #include "kernels.h"
+#include "rta_steady.cuh"
 
 namespace bte {
 
@@ -22,11 +23,13 @@ __device__ __forceinline__ void record_error(int* err, int e, long long pid) {
 }
 
 // Warp-reduced counters: the first NC of (events, wall hits, crossings,
-// absorbed, specular, nudges, quirks, tally updates, translations).
-template <int NC = 9>
+// absorbed, specular, nudges, quirks, tally updates, translations,
+// steady-state scatters, steady-state drops).
+template <int NC = 11>
 __device__ __forceinline__ void flush_counters_p(const Counters& c, unsigned long long* out) {
-    unsigned long long v[9] = {c.events, c.wall_hits, c.crossings, c.absorbed,
-                               c.specular, c.nudges, c.quirks, c.tallies, c.translations};
+    unsigned long long v[11] = {c.events, c.wall_hits, c.crossings, c.absorbed,
+                                c.specular, c.nudges, c.quirks, c.tallies, c.translations,
+                                c.scattered, c.lost};
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
         unsigned long long x = v[i];
@@ -71,6 +74,20 @@ struct ProdPolicy {
         const float acc = float(g.next32() >> 8) * 0x1p-24f;
         return acc < __int_as_float(e.x) ? e.y : e.z;
     }
+    __device__ int dist(const double*, const float* prob, const int* alt, int n) {
+        return alias_draw(g, prob, alt, n);
+    }
+    // process_segment (periodic), src/RTA_MC2D.cpp:784-834
+    __device__ int tally_dt(const DevTables& T, int box, double d, int sign, V2 v) {
+        (void)T;
+        const double contr = double(sign) * d;
+        double* base = out + 3ll * box;
+        atomicAdd(base + 0, contr);
+        atomicAdd(base + 1, v.x * contr);
+        atomicAdd(base + 2, v.y * contr);
+        ntally++;
+        return 0;
+    }
     __device__ int tally(const DevTables& T, int box, double t0, double t1, int sign, V2 v) {
         int sb = int(t0 * T.inv_dt), eb = int(t1 * T.inv_dt);
         const int last = T.nbins - 1;
@@ -95,7 +112,7 @@ struct ProdPolicy {
 
 __global__ void __launch_bounds__(128) rta_prod_general(DevTables T, double* tally,
                                                         unsigned long long* counters, int* err) {
-    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long n = T.pend - T.pbegin;
     const long long trips = (n + stride - 1) / stride;
@@ -112,6 +129,54 @@ __global__ void __launch_bounds__(128) rta_prod_general(DevTables T, double* tal
         if (e) record_error(err, e, pid);
     }
     flush_counters_p(c, counters);
+}
+
+// Generation 0: 1 per slot whose first draw picks a gradient generator.
+__global__ void steady_select_prod(SteadyArgs A, unsigned long long seed, unsigned* flags) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < A.n; s += stride) {
+        Philox g;
+        g.init(seed, steady_stream(0, s));
+        flags[s] = steady_gen_type(A, g.uniform()) == 1 ? 1u : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(128) rta_steady_prod(DevTables T, SteadyArgs A, double* tally,
+                                                       unsigned long long* counters, int* err) {
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long trips = (A.n + stride - 1) / stride;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long it = 0; it < trips; ++it) {
+        const long long slot = it * stride + tid;
+        if (slot >= A.n) continue;
+        ProdPolicy pol;
+        pol.g.init(T.seed, steady_stream(A.gen, slot));
+        pol.out = tally;
+        pol.ntally = 0;
+        Particle p;
+        int fate = FATE_LOST;
+        const int e = steady_slot(T, A, pol, slot, c, fate, p);
+        c.tallies += pol.ntally;
+        if (e) {
+            record_error(err, e, slot);
+            A.flag[slot] = 0;
+        } else {
+            steady_emit(A, slot, fate, p);
+        }
+    }
+    flush_counters_p(c, counters);
+}
+
+void launch_steady_prod(const DevTables& T, const SteadyArgs& A, double* tally,
+                        unsigned long long* counters, int* err, unsigned* select_flags, int nsm,
+                        cudaStream_t s) {
+    if (A.n <= 0) return;
+    long long blocks = (A.n + 127) / 128;
+    const long long cap = (long long)nsm * 16;
+    if (blocks > cap) blocks = cap;
+    if (select_flags) steady_select_prod<<<unsigned(blocks), 128, 0, s>>>(A, T.seed, select_flags);
+    else rta_steady_prod<<<unsigned(blocks), 128, 0, s>>>(T, A, tally, counters, err);
 }
 
 void launch_prod_general(const DevTables& T, double* tally, unsigned long long* counters,
@@ -242,7 +307,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         __syncthreads();
         tally = stally;
     }
-    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int lane = threadIdx.x & 31;
     const long long total = T.pend - T.pbegin;
     const int last_bin = T.nbins - 1;

@@ -7,6 +7,7 @@
 // lower_bound as Grid_distribution::sample does (include/sampling.hpp:92-114);
 // tallies are exact 128-bit fixed-point sums, independent of thread order.
 #include "rta_flight.cuh"
+#include "rta_steady.cuh"
 #include "kernels.h"
 
 namespace bte {
@@ -49,6 +50,24 @@ struct ReplayPolicy {
         if (j == len) j = len - 1;
         return T.lcol[a + j];
     }
+    // Grid_distribution::sample over a CDF (the alias arguments are unused)
+    __device__ int dist(const double* cdf, const float*, const int*, int n) {
+        return lower_bound_d(cdf, n, u());
+    }
+    // process_segment (periodic), src/RTA_MC2D.cpp:784-834: one value per box
+    __device__ int tally_dt(const DevTables& T, int box, double d, int sign, V2 v) {
+        (void)T;
+        const double contr = double(sign);
+        long long q0, q1, q2;
+        if (!quantise(contr * d, q0) || !quantise(v.x * contr * d, q1) || !quantise(v.y * contr * d, q2))
+            return E_LIMIT;
+        unsigned long long* base = ex + 6ll * box;
+        add128(base + 0, q0);
+        add128(base + 2, q1);
+        add128(base + 4, q2);
+        ntally++;
+        return 0;
+    }
     // process_segment (transient), src/RTA_MC2D.cpp:699-769
     __device__ int tally(const DevTables& T, int box, double t0, double t1, int sign, V2 v) {
         const double* g = T.timegrid;
@@ -75,10 +94,11 @@ struct ReplayPolicy {
 };
 
 __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long long* out) {
-    unsigned long long v[9] = {c.events, c.wall_hits, c.crossings, c.absorbed,
-                               c.specular, c.nudges, c.quirks, c.tallies, c.translations};
+    unsigned long long v[11] = {c.events, c.wall_hits, c.crossings, c.absorbed,
+                                c.specular, c.nudges, c.quirks, c.tallies, c.translations,
+                                c.scattered, c.lost};
 #pragma unroll
-    for (int i = 0; i < 9; ++i) {
+    for (int i = 0; i < 11; ++i) {
         unsigned long long x = v[i];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + i, x);
@@ -87,7 +107,7 @@ __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long 
 
 __global__ void __launch_bounds__(128) rta_replay_kernel(DevTables T, unsigned long long* ex,
                                                          unsigned long long* counters, int* err) {
-    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     // every lane runs the same trip count so the closing shuffles see a full warp
     const long long n = T.pend - T.pbegin;
@@ -110,6 +130,61 @@ __global__ void __launch_bounds__(128) rta_replay_kernel(DevTables T, unsigned l
         }
     }
     flush_counters(c, counters);
+}
+
+__device__ __forceinline__ void record_error_r(int* err, int e, long long pid) {
+    if (atomicCAS(err, 0, e) == 0) {
+        err[1] = int(pid & 0x7fffffff);
+        err[2] = int(pid >> 31);
+    }
+}
+
+// Generation 0: 1 per slot whose first draw picks a gradient generator.
+__global__ void steady_select_replay(SteadyArgs A, unsigned long long seed, unsigned* flags) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < A.n; s += stride) {
+        Pcg64 g;
+        g.seed(seed, steady_stream(0, s));
+        flags[s] = steady_gen_type(A, canonical_from(g.next())) == 1 ? 1u : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(128) rta_steady_replay(DevTables T, SteadyArgs A, unsigned long long* ex,
+                                                         unsigned long long* counters, int* err) {
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long trips = (A.n + stride - 1) / stride;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long it = 0; it < trips; ++it) {
+        const long long slot = it * stride + tid;
+        if (slot >= A.n) continue;
+        ReplayPolicy pol;
+        pol.g.seed(T.seed, steady_stream(A.gen, slot));
+        pol.ex = ex;
+        pol.ntally = 0;
+        Particle p;
+        int fate = FATE_LOST;
+        const int e = steady_slot(T, A, pol, slot, c, fate, p);
+        c.tallies += pol.ntally;
+        if (e) {
+            record_error_r(err, e, slot);
+            A.flag[slot] = 0;
+        } else {
+            steady_emit(A, slot, fate, p);
+        }
+    }
+    flush_counters(c, counters);
+}
+
+void launch_steady_replay(const DevTables& T, const SteadyArgs& A, unsigned long long* ex,
+                          unsigned long long* counters, int* err, unsigned* select_flags, int nsm,
+                          cudaStream_t s) {
+    if (A.n <= 0) return;
+    long long blocks = (A.n + 127) / 128;
+    const long long cap = (long long)nsm * 16;
+    if (blocks > cap) blocks = cap;
+    if (select_flags) steady_select_replay<<<unsigned(blocks), 128, 0, s>>>(A, T.seed, select_flags);
+    else rta_steady_replay<<<unsigned(blocks), 128, 0, s>>>(T, A, ex, counters, err);
 }
 
 void launch_replay(const DevTables& T, unsigned long long* ex, unsigned long long* counters,

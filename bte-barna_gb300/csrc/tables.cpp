@@ -571,7 +571,7 @@ LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthrea
     return L;
 }
 
-Generators build_wall_generators(const HostModes& m, const HostGeometry& g) {
+Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required) {
     Generators R;
     const std::size_t n = m.n();
     const double vuc = m.V * g.thickness / m.c;
@@ -613,8 +613,10 @@ Generators build_wall_generators(const HostModes& m, const HostGeometry& g) {
             R.walls.push_back(W);
         }
     }
-    if (R.walls.empty())
+    if (R.walls.empty()) {
+        if (!required) return R;
         throw Error(BTE_ERR_INPUT, "no isothermal wall generator (no reservoir with a different Teq)");
+    }
     std::vector<double> ws;
     double total = 0;
     for (auto& W : R.walls) {
@@ -630,6 +632,47 @@ Generators build_wall_generators(const HostModes& m, const HostGeometry& g) {
         R.wall_cum.push_back(cum);
     }
     R.total_energy = total;
+    return R;
+}
+
+GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry& g, double gx,
+                                         double gy) {
+    GradGenerators R;
+    const std::size_t n = m.n();
+    const double vuc = m.V * g.thickness / m.c;
+    std::vector<double> pmf(n);
+    std::vector<signed char> sg(n);
+    for (std::size_t s = 0; s < g.boxes.size(); ++s) {
+        if (g.reservoir[s] || g.tto[s] >= 0) continue;
+        const double T = g.Teq[s];
+        for (std::size_t k = 0; k < n; ++k) {
+            const double vgradT = -(gx * m.vx[k] + gy * m.vy[k] + 0. * m.vz[k]);
+            if (m.omega[k] == 0.) {
+                pmf[k] = 0.;
+                sg[k] = 1;
+            } else {
+                pmf[k] = std::fabs(vgradT * bose_einstein_kernel(m.omega[k], T));
+                sg[k] = vgradT >= 0 ? 1 : -1;
+            }
+        }
+        const double cumulsum = kB * std::accumulate(pmf.begin(), pmf.end(), 0.);
+        const double vol = g.boxes[s].area * g.thickness / vuc;
+        R.box.push_back(int(s));
+        R.energy.push_back(vol * cumulsum / double(m.nq));
+        auto cdf = fill_cumulative(pmf);
+        R.cdf.insert(R.cdf.end(), cdf.begin(), cdf.end());
+        std::vector<Alias> al(n);
+        alias_table(pmf.data(), int(n), al.data());
+        R.alias.insert(R.alias.end(), al.begin(), al.end());
+        R.sign.insert(R.sign.end(), sg.begin(), sg.end());
+    }
+    const double wnorm = std::accumulate(R.energy.begin(), R.energy.end(), 0.);
+    double cum = 0;
+    for (double w : R.energy) {
+        cum += w / wnorm;
+        R.cum.push_back(cum);
+    }
+    R.total_energy = wnorm;
     return R;
 }
 

@@ -107,7 +107,22 @@ void build_resample(const HostModes& m, double T0, std::vector<double>& cdf,
 // Lambert table rows per (wall-normal class, incoming mode).
 LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthreads);
 
-Generators build_wall_generators(const HostModes& m, const HostGeometry& g);
+Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required = true);
+
+// Temperature-gradient sources of the steady state: one Nabla_T_distribution
+// per box that is neither a reservoir nor periodic (src/sampling.cpp:118-187,
+// Init_generator src/RTA_MC2D.cpp:354-437), in ascending box order.
+struct GradGenerators {
+    std::vector<int> box;
+    std::vector<double> cum;            // cumulative box weights
+    std::vector<double> cdf;            // [nbox][n]
+    std::vector<Alias> alias;           // [nbox][n]
+    std::vector<signed char> sign;      // [nbox][n] sign of -gradT . v
+    std::vector<double> energy;         // get_energy(Vbox / Vucell) per box
+    double total_energy = 0;
+};
+GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry& g, double gx,
+                                         double gy);
 // Distributions of the initial deviation per box (no particle counts).
 Generators build_initial_generators(const HostModes& m, const HostGeometry& g);
 // Particle counts per box for N particles (Ntogenerate stochastic rounding):

@@ -142,6 +142,53 @@ def periodic_bar_geometry(width: float = 20.0, length: float = 40.0, nstrips: in
     return g
 
 
+def periodic_cell_geometry(lx: float = 40.0, ly: float = 40.0, nx: int = 2, ny: int = 2,
+                           T0: float = 300.0, thickness: float = C_LAT, side: float = 1.0) -> dict:
+    """An nx x ny block of cells closed on all four sides by periodic boxes
+    (right <-> left, top <-> bottom): an infinite medium for the steady
+    state under a gradient.  The corners outside the block are void."""
+    boxes, Teq, res = [], [], []
+    dx, dy = lx / nx, ly / ny
+    for i in range(nx):
+        for j in range(ny):
+            boxes.append(_rect(i * dx, j * dy, (i + 1) * dx, (j + 1) * dy))
+            Teq.append(T0)
+            res.append(0)
+    nc = len(boxes)
+    right, left, top, bottom = nc, nc + 1, nc + 2, nc + 3
+    boxes.append(_rect(lx, 0.0, lx + side, ly))
+    boxes.append(_rect(-side, 0.0, 0.0, ly))
+    boxes.append(_rect(0.0, ly, lx, ly + side))
+    boxes.append(_rect(0.0, -side, lx, 0.0))
+    Teq += [T0] * 4
+    res += [0] * 4
+    g = _pack(boxes, Teq, list(Teq), res, thickness)
+    tto = np.full(len(boxes), -1, dtype=np.int32)
+    tr = np.zeros((len(boxes), 2))
+    tto[right], tr[right] = left, (-lx, 0.0)
+    tto[left], tr[left] = right, (lx, 0.0)
+    tto[top], tr[top] = bottom, (0.0, -ly)
+    tto[bottom], tr[bottom] = top, (0.0, ly)
+    g["translate_to"] = tto
+    g["translation"] = tr
+    return g
+
+
+def kappa_rta(modes: dict, T: float, thickness: float = C_LAT) -> np.ndarray:
+    """Bulk RTA conductivity tensor (2x2, W m^-1 K^-1) of a mode table:
+    1e21 kB / (nq V_uc) sum C(omega, T) v v tau, with the 2D unit-cell volume
+    V thickness / c (the volume the engine's tallies use)."""
+    kB = 1.3806488e-23
+    om, w = modes["omega"], modes["w"]
+    v = modes["vg"].reshape(-1, 3)[:, :2]
+    ok = (om > 0) & (w > 0)
+    C = be_kernel(om[ok], T)
+    tau = 1.0 / w[ok]
+    vv = np.einsum("k,ki,kj->ij", C * tau, v[ok], v[ok])
+    vuc = modes["V"] * thickness / modes["c_lat"]
+    return 1e21 * kB / (modes["nq"] * vuc) * vv
+
+
 def grid_geometry(lx: float, ly: float, nx: int, ny: int, T0: float = 300.0,
                   pore_center=None, pore_diameter: float = 0.0,
                   hot_center=None, hot_sigma: float = 50.0, hot_dT: float = 0.0,

@@ -195,6 +195,49 @@ typedef struct bte_berta_result {
     double kernel_ms;        /* device time of the step loop                     */
 } bte_berta_result;
 
+/* Parameters of a steady-state run of a periodic structure under an applied
+ * temperature gradient (the gradient branch of RTAMC2D,
+ * src/RTA_MC2D.cpp:2544-2842; <gradient x= y=/> and <convergence energy=
+ * flux=/> of the <RTA_MC2d> XML, :1828-1840). */
+typedef struct bte_steady_params {
+    double T0;               /* reference temperature, K                       */
+    double gradient[2];      /* applied gradient, K/nm (must not be zero)      */
+    double eps_energy;       /* relative change of gz that ends the loop; <= 0: never */
+    double eps_flux;         /* relative change of the flux tallies; <= 0: never */
+    int64_t nparticles;      /* N: Eeff = |E|/N                                */
+    uint64_t seed;           /* master seed of all slot streams                 */
+    int32_t mode;            /* BTE_MODE_*                                      */
+    int32_t max_generations; /* safety cap of the generation loop (0: 100000)  */
+} bte_steady_params;
+
+/* Results of a steady-state run: one value per box (the rows of
+ * steady_<T0>K_run_<i>.csv) and the per-generation convergence table. */
+typedef struct bte_steady_result {
+    int32_t nboxes;          /* out */
+    int32_t generations;     /* out: iterations of the generation loop          */
+    int32_t converged;       /* out: 1 when the eps criteria ended the loop     */
+    int32_t log_cap;         /* in: rows available in `log`                     */
+    double* gz;              /* [nboxes] raw sign-weighted particle time        */
+    double* gz_jx;           /* [nboxes] raw vx-weighted tally                  */
+    double* gz_jy;           /* [nboxes] raw vy-weighted tally                  */
+    double* temperature;     /* [nboxes] K                                      */
+    double* jx;              /* [nboxes] J m^-2 s^-1                            */
+    double* jy;              /* [nboxes] J m^-2 s^-1                            */
+    int64_t* exact;          /* replay: [nboxes][3][2] 128-bit sums (hi, lo), 2^44 */
+    double* log;             /* [log_cap][4]: particles, rgz, rjx, rjy per generation */
+    double Eeff;             /* energy per particle, J/ps                       */
+    double energy_rate;      /* |E| of all generators, J/ps                     */
+    int64_t events;          /* free flights                                    */
+    int64_t wall_hits;       /* void-wall reflections (carried over)            */
+    int64_t crossings;
+    int64_t absorbed;
+    int64_t translations;
+    int64_t scattered;       /* flights ending inside a box (phi)               */
+    int64_t births;          /* particles created from phi                      */
+    int64_t lost;            /* flights dropped at a crossing with no time left */
+    double kernel_ms;        /* device time of the generation kernels           */
+} bte_steady_result;
+
 /* Tuning knobs of the production kernels (project-written autotuner picks
  * them; 0 selects the built-in default). */
 typedef struct bte_tuning {
@@ -252,6 +295,15 @@ bte_status bte_load_propagator(bte_ctx* ctx, const bte_propagator* P);
  * the boxes must tile an axis-aligned grid and share Teq = T0. */
 bte_status bte_berta_run(bte_ctx* ctx, const bte_berta_params* params,
                          bte_berta_result* out);
+
+/* Run the steady state of a periodic structure under a temperature
+ * gradient: generations of one free flight per particle, phi re-emission
+ * and the convergence test (replaces the gradient branch of the run loop,
+ * src/RTA_MC2D.cpp:2544-2842, with generation by Init_generator,
+ * :272-533, and the periodic evolparticle / process_segment, :784-834,
+ * :1406-1799). */
+bte_status bte_steady_run(bte_ctx* ctx, const bte_steady_params* params,
+                          bte_steady_result* out);
 
 /* Largest number of time bins bte_rta_run_noalloc accepts. */
 #define BTE_NOALLOC_MAX_BINS 4096

@@ -48,6 +48,9 @@ def load():
     lib.oracle_translate.argtypes = [C.POINTER(_bt.Geometry), C.c_int] + [C.c_double] * 4 + [
         C.c_uint64, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.oracle_translate.restype = C.c_int
+    lib.oracle_steady_run.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
+                                      C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult)]
+    lib.oracle_steady_run.restype = C.c_int
     lib.oracle_pcg64.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
     lib.oracle_log.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int]
@@ -86,6 +89,22 @@ def translate(geom: dict, ibox: int, x: float, y: float, vx: float, vy: float, s
     if st != 0:
         raise _bt.BteError(st, lib.oracle_last_error().decode())
     return nb.value, (float(xy[0]), float(xy[1]))
+
+
+def steady_run(case: dict, gradient, N=None, seed=1, nthreads=8, eps_energy=-42.0, eps_flux=-42.0,
+               max_generations=0):
+    """Steady state of the restatement (replay draws) on a synth case dict."""
+    lib = load()
+    ms, k1 = _bt.mode_struct(case["modes"])
+    gs, k2 = _bt.geom_struct(case["geom"])
+    N = case["N"] if N is None else N
+
+    def call(p, r):
+        st = lib.oracle_steady_run(C.byref(ms), C.byref(gs), C.byref(p), int(nthreads), C.byref(r))
+        if st != 0:
+            raise _bt.BteError(st, lib.oracle_last_error().decode())
+    return _bt.steady_call(call, int(case["geom"]["nboxes"]), case["T0"], gradient, N, seed,
+                           _bt.MODE_REPLAY, eps_energy, eps_flux, max_generations)
 
 
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,

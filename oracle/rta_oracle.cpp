@@ -1144,6 +1144,279 @@ inline void run_particle(const Sim& S, std::size_t pid, uint64_t seed, double ma
 }
 
 
+// ============================================================ steady state
+// The periodic / gradient branch of RTAMC2D (src/RTA_MC2D.cpp:2544-2842):
+// generations of one free flight per particle.
+//
+// Draws: slot s of generation g owns pcg64(seed, stream = g * 2^40 + s); the
+// reference's thread-local generators and its serial `rng` (used for the
+// births) are replaced by these per-slot streams.  Generation 0 is
+// Init_generator with a gradient (:443-529); later generations are the
+// particles reflected at void walls in the previous one, in slot order, then
+// |phi(box)| births per box in ascending box order (:2640-2658).
+
+inline uint64_t steady_stream(uint64_t gen, uint64_t slot) { return (gen << 40) | slot; }
+
+// Nabla_T_distribution, src/sampling.cpp:118-187, per interior box.
+struct GradGen {
+    std::size_t box;
+    std::vector<double> cdf;
+    std::vector<int> sign;
+    double energy;
+};
+
+inline std::vector<GradGen> build_gradient(const Sim& S, double gx, double gy) {
+    const Modes& m = S.m;
+    const double vuc = m.V * S.thickness / m.c;
+    std::vector<GradGen> out;
+    for (auto& s : S.sys) {
+        if (s.reservoir || s.periodic) continue;
+        GradGen G;
+        G.box = s.id;
+        std::vector<double> pmf(m.n());
+        G.sign.assign(m.n(), 1);
+        for (std::size_t k = 0; k < m.n(); ++k) {
+            double vgradT = -(gx * m.vx[k] + gy * m.vy[k] + 0. * m.vz[k]);
+            if (m.omega[k] == 0.) {
+                pmf[k] = 0.;
+            } else {
+                pmf[k] = std::fabs(vgradT * bose_einstein_kernel(m.omega[k], s.Teq));
+                G.sign[k] = vgradT >= 0 ? 1 : -1;
+            }
+        }
+        double cumulsum = kB * std::accumulate(pmf.begin(), pmf.end(), 0.);
+        double vol = s.area * S.thickness / vuc;
+        G.energy = vol * cumulsum / double(m.nq);
+        G.cdf = fill_cumulative(pmf);
+        out.push_back(std::move(G));
+    }
+    return out;
+}
+
+struct SteadyGen {
+    std::vector<GradGen> grad;
+    std::vector<double> grad_cum;
+    double exg0 = 0, exg1 = 0;
+};
+
+// process_segment (periodic), src/RTA_MC2D.cpp:784-834.
+inline void process_segment_steady(Tally& T, std::size_t ibox, int sign, double dt, V2 vg) {
+    double contr = double(sign);
+    T.ex[3 * ibox + 0] += quant(contr * dt);
+    T.ex[3 * ibox + 1] += quant(vg.x * contr * dt);
+    T.ex[3 * ibox + 2] += quant(vg.y * contr * dt);
+}
+
+enum Fate { F_LOST = 0, F_SCATTER = 1, F_BOUNCE = 2, F_ABSORBED = 3 };
+
+// evolparticle (periodic), src/RTA_MC2D.cpp:1406-1799, one material.
+inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng, Tally& T,
+                                Fate& fate) {
+    const std::size_t nb = S.m.nb;
+    V2 opos = p.pos;
+    const Box& box = S.sys[p.box];
+    if (box.periodic) {
+        auto sol = translate(S, p.box, opos, v, rng);
+        p.box = sol.first;
+        p.pos = sol.second;
+        T.translations++;
+        return;
+    }
+    if (box.reservoir) {
+        p.q = 0;
+        p.alpha = 0;
+        dt = 0.;
+        T.absorbed++;
+        fate = F_ABSORBED;
+        return;
+    }
+    V2 rnew = {p.pos.x + dt * v.x, p.pos.y + dt * v.y};
+    if (box.inside(rnew)) {
+        p.pos = rnew;
+        p.t += dt;
+        process_segment_steady(T, p.box, p.sign, dt, v);  // evalphi: phi += sign
+        dt = 0.;
+        fate = F_SCATTER;
+        return;
+    }
+    Hit mru;
+    try {
+        mru = get_inter_side(box, p.pos, v, dt);
+    } catch (const geometry_error&) {
+        V2 d = box.center - opos;
+        p.pos = p.pos + (1.0e-6 * d) / norm(d);
+        T.nudges++;
+        return;
+    }
+    double left_time = dt - mru.time;
+    double tf = mru.time;
+    if (almost_equal(left_time, 0.)) left_time = 0.;
+    rnew = mru.rf;
+    dt = left_time;
+    V2 reps = rnew + (1.0e-6 * v) / norm(v);
+    std::vector<std::size_t> cboxes;
+    for (auto& [ibc, bb] : box.contacts) cboxes.push_back(ibc);
+    std::vector<std::size_t> pboxes;
+    for (auto test : cboxes) {
+        if (test == p.box) continue;
+        const Border& bc = box.contacts.at(test)[0];
+        bool parallel = almost_equal(dot(bc.np, v), 0.);
+        bool oriented = dot(bc.np, v) > 0.;
+        if ((S.sys[test].inside(rnew) || S.sys[test].inside(reps)) && !parallel && oriented)
+            pboxes.push_back(test);
+    }
+    if (pboxes.empty()) {
+        process_segment_steady(T, p.box, p.sign, tf, v);
+        p.t += tf;
+        std::vector<std::size_t> ids;
+        for (auto& g : S.sys)
+            if (g.inside(rnew)) ids.push_back(g.id);
+        if (ids.size() > 2) {
+            p.box = correct_corner_problem(S, rnew, v, ids, rng);
+            V2 corr = S.sys[p.box].center - rnew;
+            V2 cpos = rnew + (1.0e-6 * corr) / norm(corr);
+            mru = get_inter_side(S.sys[p.box], cpos, v, 1.0e+18);
+            rnew = mru.rf;
+        }
+        const Box& cur = S.sys[p.box];
+        std::size_t iborder;
+        if (mru.bids.size() > 1) {
+            std::vector<std::size_t> voidborders;
+            for (int tvb : mru.bids) {
+                const Border& mb = cur.borders[std::size_t(tvb)];
+                V2 rc = rnew + 1.0e-4 * mb.np;
+                bool isvoid = true;
+                for (auto cb : cboxes)
+                    if (S.sys[cb].inside(rc)) {
+                        isvoid = false;
+                        break;
+                    }
+                if (isvoid) voidborders.push_back(std::size_t(tvb));
+            }
+            if (voidborders.empty()) throw geometry_error("Error in void borders");
+            int idx = uniform_int(rng, 0, int(voidborders.size()));
+            if (std::size_t(idx) == voidborders.size()) {
+                T.quirks++;
+                idx--;
+            }
+            iborder = voidborders[std::size_t(idx)];
+        } else {
+            iborder = std::size_t(mru.bids.at(0));
+        }
+        V2 u = cur.borders[iborder].np;
+        std::size_t nm = bounce(S, u, p.q * nb + p.alpha, rng);
+        p.pos = rnew;
+        p.q = nm / nb;
+        p.alpha = nm % nb;
+        dt = 0.;
+        T.wall_hits++;
+        fate = F_BOUNCE;  // pushed into the next generation
+        return;
+    } else if (pboxes.size() == 1) {
+        p.pos = rnew;
+        p.t += tf;
+        process_segment_steady(T, p.box, p.sign, tf, v);
+        p.box = pboxes[0];
+        T.crossings++;
+        return;
+    } else {
+        process_segment_steady(T, p.box, p.sign, tf, v);
+        p.t += tf;
+        p.pos = rnew;
+        std::vector<std::size_t> pbox2;
+        V2 rcheck = rnew + 1.0e-6 * v;
+        for (auto PB : pboxes)
+            if (S.sys[PB].inside(rcheck)) pbox2.push_back(PB);
+        std::size_t newid;
+        if (pbox2.empty()) {
+            newid = pboxes[std::size_t(uniform_int(rng, 0, int(pboxes.size()) - 1))];
+            V2 d = S.sys[newid].center - rnew;
+            if (!S.sys[newid].periodic) p.pos = p.pos + (1.0e-6 * d) / norm(d);
+        } else {
+            newid = pbox2[std::size_t(uniform_int(rng, 0, int(pbox2.size()) - 1))];
+        }
+        p.box = newid;
+        T.crossings++;
+        return;
+    }
+}
+
+inline int steady_gen_type(const Sim& S, const SteadyGen& SG, double u) {
+    int id = u <= SG.exg0 ? 0 : 1;  // lower_bound over ExGen
+    if (id == 0 && S.gens.empty()) id = 1;
+    if (id == 1 && SG.grad.empty()) id = 0;
+    return id;
+}
+
+inline V2 random_point(const Box& B, Pcg64& rng) {
+    double x0 = B.hull[0].x, x1 = B.hull[0].x, y0 = B.hull[0].y, y1 = B.hull[0].y;
+    for (auto& h : B.hull) {
+        x0 = std::min(x0, h.x);
+        x1 = std::max(x1, h.x);
+        y0 = std::min(y0, h.y);
+        y1 = std::max(y1, h.y);
+    }
+    V2 r;
+    for (int tries = 0;; ++tries) {
+        if (tries > 100000) throw limit_error("random point rejection loop");
+        r.x = x0 + canonical(rng) * (x1 - x0);
+        r.y = y0 + canonical(rng) * (y1 - y0);
+        if (B.inside(r)) return r;
+    }
+}
+
+// Generation-0 particle of slot s (Init_generator with a gradient); `rank`
+// counts the gradient-generated slots before s (gsign alternates from -).
+inline Particle steady_generate0(const Sim& S, const SteadyGen& SG, uint64_t rank, Pcg64& rng) {
+    double selectGenR = canonical(rng);
+    if (steady_gen_type(S, SG, selectGenR) == 0) {
+        // case 0 of Init_generator after the generator-type draw
+        double whereGenR = canonical(rng);
+        auto it = std::lower_bound(S.gen_cum.begin(), S.gen_cum.end(), whereGenR);
+        if (it == S.gen_cum.end()) --it;
+        const WallGen& G = S.gens[std::size_t(it - S.gen_cum.begin())];
+        V2 ppos;
+        for (int tries = 0;; ++tries) {
+            if (tries > 1000) throw limit_error("border point rejection loop");
+            ppos = G.b.p1 + canonical(rng) * G.b.nd;
+            if (on_segment(ppos, G.b.sa, G.b.sb)) break;
+        }
+        const Box& inj = S.sys[G.box];
+        if (!inj.inside(ppos)) {
+            V2 d = inj.center - ppos;
+            ppos = ppos + (1.0e-6 * d) / norm(d);
+            if (!inj.inside(ppos)) throw geometry_error("Generated particle out of insertion box");
+        }
+        std::size_t pos = lower_bound_idx(G.cdf, canonical(rng));
+        Particle p;
+        p.pos = ppos;
+        p.q = pos / S.m.nb;
+        p.alpha = pos % S.m.nb;
+        p.sign = G.sign;
+        p.box = G.box;
+        return p;
+    }
+    double whereGenR = canonical(rng);
+    auto it = std::lower_bound(SG.grad_cum.begin(), SG.grad_cum.end(), whereGenR);
+    if (it == SG.grad_cum.end()) --it;
+    const GradGen& G = SG.grad[std::size_t(it - SG.grad_cum.begin())];
+    V2 ppos = random_point(S.sys[G.box], rng);
+    const int want = (rank & 1u) ? 1 : -1;
+    std::size_t pos = 0;
+    for (int tries = 0;; ++tries) {
+        if (tries > 1000000) throw limit_error("gradient sign rejection loop");
+        pos = lower_bound_idx(G.cdf, canonical(rng));
+        if (G.sign[pos] == want) break;
+    }
+    Particle p;
+    p.pos = ppos;
+    p.q = pos / S.m.nb;
+    p.alpha = pos % S.m.nb;
+    p.sign = want;
+    p.box = G.box;
+    return p;
+}
+
 // ================================================================ beRTAMC2D
 // Restatement of the beRTAMC2D step loop (src/beyondRTA_MC2d.cpp:2138-2425):
 // ballistic advection with absorbing walls (evolparticle :708-970),
@@ -1759,6 +2032,241 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
             for (std::size_t k = 0; k < nk; ++k) out->temperature[k] = gz[k] / (cv / vcorr) + rp->T0;
         if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
         if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
+        return 0;
+    } catch (const orc::input_error& e) {
+        return fail(BTE_ERR_INPUT, e.what());
+    } catch (const orc::value_error& e) {
+        return fail(BTE_ERR_VALUE, e.what());
+    } catch (const orc::limit_error& e) {
+        return fail(BTE_ERR_LIMIT, e.what());
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
+// One steady-state run of a periodic structure under a gradient (the
+// restatement above) on `nthreads` host threads; fills `out` as
+// bte_steady_run does.  Tallies are exact 128-bit sums, turned into doubles
+// for the convergence test and the outputs.
+int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_steady_params* sp,
+                      int nthreads, bte_steady_result* out) {
+    try {
+        orc::Sim S = build_sim(mt, gm);
+        const double gx = sp->gradient[0], gy = sp->gradient[1];
+        if (orc::almost_equal(std::sqrt(gx * gx + gy * gy), 0.))
+            return fail(BTE_ERR_INPUT, "the steady state needs a non-zero temperature gradient");
+        const std::size_t n = S.m.n(), nbx = S.sys.size(), nb = std::size_t(S.m.nb);
+        std::vector<double> pmf(n);
+        for (std::size_t k = 0; k < n; ++k)
+            pmf[k] = S.m.omega[k] <= 0. ? 0. : orc::bose_einstein_kernel(S.m.omega[k], sp->T0) * S.m.w[k];
+        S.resample_cdf = orc::fill_cumulative(pmf);
+        orc::build_lambert(S);
+        orc::build_generators(S, sp->T0, false);
+        const double E0 = S.gens.empty() ? 0. : S.energy;
+        orc::SteadyGen SG;
+        SG.grad = orc::build_gradient(S, gx, gy);
+        std::vector<double> ge;
+        for (auto& G : SG.grad) ge.push_back(G.energy);
+        const double E1 = std::accumulate(ge.begin(), ge.end(), 0.);
+        double cum = 0.;
+        for (double w : ge) {
+            cum += w / E1;
+            SG.grad_cum.push_back(cum);
+        }
+        const double total = E0 + E1;
+        if (!(total > 0.)) return fail(BTE_ERR_INPUT, "the generators inject no energy");
+        SG.exg0 = E0 / total;
+        SG.exg1 = E1 / total + SG.exg0;
+        const int64_t N = sp->nparticles;
+        const double Eeff = total / double(N);
+        if (nthreads < 1) nthreads = 1;
+        const int max_gen = sp->max_generations > 0 ? sp->max_generations : 100000;
+
+        std::vector<__int128> ex(3 * nbx, 0);
+        std::vector<double> oldv(3 * nbx, 0.), cur(3 * nbx, 0.);
+        std::vector<orc::Particle> carry;
+        std::vector<std::size_t> bbox;
+        std::vector<int> bsign;
+        std::vector<int64_t> bfirst;
+        int64_t nbirth = 0, births_total = 0;
+        int64_t ev = 0, wh = 0, cr = 0, ab = 0, tr = 0, sc = 0, lost = 0;
+        int gen = 0, converged = 0;
+        for (;;) {
+            const int64_t nin = gen == 0 ? 0 : int64_t(carry.size());
+            const int64_t nslots = gen == 0 ? N : nin + nbirth;
+            std::vector<uint64_t> rank;
+            if (gen == 0) {
+                rank.resize(std::size_t(nslots));
+                uint64_t c = 0;
+                for (int64_t sl = 0; sl < nslots; ++sl) {
+                    orc::Pcg64 r(sp->seed, orc::steady_stream(0, uint64_t(sl)));
+                    rank[std::size_t(sl)] = c;
+                    if (orc::steady_gen_type(S, SG, orc::canonical(r)) == 1) c++;
+                }
+            }
+            std::vector<orc::Particle> outp(static_cast<std::size_t>(nslots));
+            std::vector<char> fate(static_cast<std::size_t>(nslots), 0);
+            std::vector<orc::Tally> tl(static_cast<std::size_t>(nthreads));
+            std::vector<std::vector<int64_t>> phis(static_cast<std::size_t>(nthreads));
+            std::vector<std::string> errs(static_cast<std::size_t>(nthreads));
+            std::vector<int> codes(static_cast<std::size_t>(nthreads), 0);
+            auto work = [&](int tid) {
+                orc::Tally& T = tl[std::size_t(tid)];
+                T.init(nbx, 1);
+                std::vector<int64_t>& phi = phis[std::size_t(tid)];
+                phi.assign(nbx, 0);
+                const int64_t lo = nslots * tid / nthreads, hi = nslots * (tid + 1) / nthreads;
+                try {
+                    for (int64_t sl = lo; sl < hi; ++sl) {
+                        orc::Pcg64 rng(sp->seed, orc::steady_stream(uint64_t(gen), uint64_t(sl)));
+                        orc::Particle p;
+                        if (gen == 0) {
+                            p = orc::steady_generate0(S, SG, rank[std::size_t(sl)], rng);
+                        } else if (sl < nin) {
+                            p = carry[std::size_t(sl)];
+                        } else {
+                            const int64_t k = sl - nin;
+                            auto it = std::upper_bound(bfirst.begin(), bfirst.end(), k);
+                            const std::size_t j = std::size_t(it - bfirst.begin()) - 1;
+                            p.pos = orc::random_point(S.sys[bbox[j]], rng);
+                            const std::size_t pos = orc::lower_bound_idx(S.resample_cdf, orc::canonical(rng));
+                            p.q = pos / nb;
+                            p.alpha = pos % nb;
+                            p.sign = bsign[j];
+                            p.box = bbox[j];
+                        }
+                        p.t = 0.;
+                        const std::size_t k = p.q * nb + p.alpha;
+                        const orc::V2 v = orc::get_v(S.m, k);
+                        const double w = S.m.w[k];
+                        if (w == 0.) throw orc::value_error("invalid scattering rate");
+                        double dt = -orc::bte_log(orc::canonical(rng)) / w;
+                        T.events++;
+                        orc::Fate f = orc::F_LOST;
+                        int guard = 0;
+                        while (!orc::almost_equal(dt, 0.)) {
+                            if (++guard > 1000000) throw orc::limit_error("flight step cap");
+                            orc::evolparticle_steady(S, p, v, dt, rng, T, f);
+                        }
+                        fate[std::size_t(sl)] = char(f);
+                        if (f == orc::F_SCATTER) phi[p.box] += p.sign;
+                        if (f == orc::F_BOUNCE) outp[std::size_t(sl)] = p;
+                    }
+                } catch (const orc::value_error& e) {
+                    errs[std::size_t(tid)] = e.what();
+                    codes[std::size_t(tid)] = BTE_ERR_VALUE;
+                } catch (const orc::limit_error& e) {
+                    errs[std::size_t(tid)] = e.what();
+                    codes[std::size_t(tid)] = BTE_ERR_LIMIT;
+                } catch (const std::exception& e) {
+                    errs[std::size_t(tid)] = e.what();
+                    codes[std::size_t(tid)] = BTE_ERR_GEOMETRY;
+                }
+            };
+            if (nthreads == 1) {
+                work(0);
+            } else {
+                std::vector<std::thread> th;
+                for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+                for (auto& t : th) t.join();
+            }
+            for (std::size_t t = 0; t < errs.size(); ++t)
+                if (!errs[t].empty()) return fail(codes[t], errs[t].c_str());
+            std::vector<int64_t> phi(nbx, 0);
+            for (auto& T : tl) {
+                for (std::size_t k = 0; k < 3 * nbx; ++k) ex[k] += T.ex[k];
+                ev += T.events;
+                wh += T.wall_hits;
+                cr += T.crossings;
+                ab += T.absorbed;
+                tr += T.translations;
+            }
+            for (auto& ph : phis)
+                for (std::size_t b = 0; b < nbx; ++b) phi[b] += ph[b];
+            carry.clear();
+            for (int64_t sl = 0; sl < nslots; ++sl) {
+                const char f = fate[std::size_t(sl)];
+                if (f == orc::F_BOUNCE) carry.push_back(outp[std::size_t(sl)]);
+                if (f == orc::F_SCATTER) sc++;
+                if (f == orc::F_LOST) lost++;
+            }
+            bbox.clear();
+            bsign.clear();
+            bfirst.clear();
+            nbirth = 0;
+            for (std::size_t b = 0; b < nbx; ++b) {
+                if (phi[b] == 0) continue;
+                bfirst.push_back(nbirth);
+                bbox.push_back(b);
+                bsign.push_back(phi[b] >= 0 ? 1 : -1);
+                nbirth += phi[b] >= 0 ? phi[b] : -phi[b];
+            }
+            births_total += nbirth;
+            for (std::size_t b = 0; b < nbx; ++b)
+                for (int q = 0; q < 3; ++q) cur[std::size_t(q) * nbx + b] = double(ex[3 * b + std::size_t(q)]) / 17592186044416.0;
+            auto rel = [&](int q) {
+                double a = 0., c = 0.;
+                for (std::size_t b = 0; b < nbx; ++b) {
+                    const double d = oldv[std::size_t(q) * nbx + b] - cur[std::size_t(q) * nbx + b];
+                    a += d * d;
+                }
+                for (std::size_t b = 0; b < nbx; ++b) c += cur[std::size_t(q) * nbx + b] * cur[std::size_t(q) * nbx + b];
+                return std::sqrt(a) / std::sqrt(c);
+            };
+            const double rgz = rel(0), rjx = rel(1), rjy = rel(2);
+            if (orc::almost_equal(gx, 0.))
+                converged = rgz < sp->eps_energy && rjy < sp->eps_flux;
+            else if (orc::almost_equal(gy, 0.))
+                converged = rgz < sp->eps_energy && rjx < sp->eps_flux;
+            else
+                converged = rgz < sp->eps_energy && rjx < sp->eps_flux && rjy < sp->eps_flux;
+            if (out->log && gen < out->log_cap) {
+                double* row = out->log + std::size_t(gen) * 4;
+                row[0] = double(int64_t(carry.size()) + nbirth);
+                row[1] = rgz;
+                row[2] = rjx;
+                row[3] = rjy;
+            }
+            oldv = cur;
+            gen++;
+            if (int64_t(carry.size()) + nbirth == 0 || converged || gen >= max_gen) break;
+        }
+        out->nboxes = int32_t(nbx);
+        out->generations = gen;
+        out->converged = converged;
+        out->Eeff = Eeff;
+        out->energy_rate = total;
+        out->events = ev;
+        out->wall_hits = wh;
+        out->crossings = cr;
+        out->absorbed = ab;
+        out->translations = tr;
+        out->scattered = sc;
+        out->births = births_total;
+        out->lost = lost;
+        out->kernel_ms = 0.;
+        if (out->exact)
+            for (std::size_t k = 0; k < 3 * nbx; ++k) {
+                unsigned __int128 u = (unsigned __int128)ex[k];
+                out->exact[2 * k] = int64_t(uint64_t(u >> 64));
+                out->exact[2 * k + 1] = int64_t(uint64_t(u));
+            }
+        // post-processing, src/RTA_MC2D.cpp:2698-2731
+        double cv = 0.;
+        for (std::size_t k = 0; k < n; ++k) cv += orc::bose_einstein_kernel(S.m.omega[k], sp->T0);
+        cv *= orc::kB / double(S.m.nq) / S.m.V;
+        const double vcorr = S.thickness / S.m.c;
+        for (std::size_t b = 0; b < nbx; ++b) {
+            const double vbox = S.sys[b].area * S.thickness;
+            const double z = cur[b], zx = cur[nbx + b], zy = cur[2 * nbx + b];
+            if (out->gz) out->gz[b] = z;
+            if (out->gz_jx) out->gz_jx[b] = zx;
+            if (out->gz_jy) out->gz_jy[b] = zy;
+            const double ed = z / vbox * Eeff;
+            if (out->temperature) out->temperature[b] = ed / (cv / vcorr) + sp->T0;
+            if (out->jx) out->jx[b] = zx / vbox * (Eeff * 1e12 * 1e9 * 1e9);
+            if (out->jy) out->jy[b] = zy / vbox * (Eeff * 1e12 * 1e9 * 1e9);
+        }
         return 0;
     } catch (const orc::input_error& e) {
         return fail(BTE_ERR_INPUT, e.what());
