@@ -34,8 +34,13 @@ def _rng(config: int, purpose: int) -> np.random.Generator:
 
 
 def mode_table(n: int = 32, n_acoustic: int = 3, n_optical: int = 3, T: float = 300.0,
-               config: int = 0) -> dict:
-    """Mode table as a dict of numpy arrays (keys mirror bte_mode_table)."""
+               config: int = 0, even: bool = False) -> dict:
+    """Mode table as a dict of numpy arrays (keys mirror bte_mode_table).
+
+    even=True (odd n) makes every mode quantity symmetric under the mirrors
+    q_x -> -q_x and q_y -> -q_y (the random lifetime amplitudes and optical
+    frequencies included), so that sources and wall re-emission carry no
+    net flux by symmetry: the analytic conductivities hold exactly."""
     rng = _rng(config, 1)
     nb = n_acoustic + n_optical
     idx = np.arange(n)
@@ -62,11 +67,18 @@ def mode_table(n: int = 32, n_acoustic: int = 3, n_optical: int = 3, T: float = 
     omega[0, :n_acoustic] = 0.0
     vg[0, :n_acoustic, :] = 0.0
     Om = 2 * math.pi * rng.uniform(15.0, 30.0, n_optical)
+    if even:
+        if n % 2 == 0:
+            raise ValueError("a mirror-symmetric grid needs an odd n")
+        ci = np.minimum(idx, (n - idx) % n)             # mirror representative
+        rep = (np.repeat(ci, n) * n + np.tile(ci, n))   # iq -> representative iq
+    else:
+        rep = np.arange(nq)
     for k in range(n_optical):
         b = n_acoustic + k
-        omega[:, b] = Om[k] * (1.0 + rng.uniform(-0.05, 0.05, nq))
+        omega[:, b] = (Om[k] * (1.0 + rng.uniform(-0.05, 0.05, nq)))[rep]
         wmax_b[b] = omega[:, b].max()
-    A = np.exp(rng.uniform(math.log(1.0), math.log(100.0), (nq, nb)))
+    A = np.exp(rng.uniform(math.log(1.0), math.log(100.0), (nq, nb)))[rep]
     theta = HBAR * 1e12 * omega.max() / KB
     ratio = np.where(omega > 0, omega / wmax_b[None, :], 1.0)
     tau = A * ratio ** -2 * math.exp(-theta / (3 * T)) / math.exp(-theta / 900.0)
@@ -187,6 +199,50 @@ def kappa_rta(modes: dict, T: float, thickness: float = C_LAT) -> np.ndarray:
     vv = np.einsum("k,ki,kj->ij", C * tau, v[ok], v[ok])
     vuc = modes["V"] * thickness / modes["c_lat"]
     return 1e21 * kB / (modes["nq"] * vuc) * vv
+
+
+def periodic_ribbon_geometry(length: float = 40.0, width: float = 100.0, nx: int = 2, ny: int = 2,
+                             T0: float = 300.0, thickness: float = C_LAT, side: float = 1.0) -> dict:
+    """A ribbon along x, periodic in x (left and right periodic boxes map
+    onto each other), with void above and below: the diffuse walls of an
+    infinite nanoribbon of the given width."""
+    boxes, Teq, res = [], [], []
+    dx, dy = length / nx, width / ny
+    for i in range(nx):
+        for j in range(ny):
+            boxes.append(_rect(i * dx, j * dy, (i + 1) * dx, (j + 1) * dy))
+            Teq.append(T0)
+            res.append(0)
+    nc = len(boxes)
+    boxes.append(_rect(length, 0.0, length + side, width))
+    boxes.append(_rect(-side, 0.0, 0.0, width))
+    Teq += [T0, T0]
+    res += [0, 0]
+    g = _pack(boxes, Teq, list(Teq), res, thickness)
+    tto = np.full(len(boxes), -1, dtype=np.int32)
+    tr = np.zeros((len(boxes), 2))
+    tto[nc], tr[nc] = nc + 1, (-length, 0.0)
+    tto[nc + 1], tr[nc + 1] = nc, (length, 0.0)
+    g["translate_to"] = tto
+    g["translation"] = tr
+    return g
+
+
+def kappa_ribbon(modes: dict, T: float, width: float, thickness: float = C_LAT) -> float:
+    """Conductivity along an infinite ribbon with fully diffuse walls:
+    kappa_xx with each lifetime scaled as scale_tau_nanoribbon does
+    (src/nanos.cpp:77-112), tau (1 + (l / w)(exp(-w / l) - 1)), l = tau |v_y|."""
+    kB = 1.3806488e-23
+    om, w = modes["omega"], modes["w"]
+    v = modes["vg"].reshape(-1, 3)
+    ok = (om > 0) & (w > 0)
+    C = be_kernel(om[ok], T)
+    tau = 1.0 / w[ok]
+    mfp = np.abs(tau * v[ok, 1])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        f = np.where(mfp > 1e-8, mfp / width * (np.exp(-width / np.maximum(mfp, 1e-300)) - 1.0) + 1.0, 1.0)
+    vuc = modes["V"] * thickness / modes["c_lat"]
+    return float(1e21 * kB / (modes["nq"] * vuc) * np.sum(C * tau * f * v[ok, 0] ** 2))
 
 
 def grid_geometry(lx: float, ly: float, nx: int, ny: int, T0: float = 300.0,

@@ -23,9 +23,10 @@ def _load(engine, case):
     engine.load_geometry(case["geom"])
 
 
-def _cell_case(N=20000):
-    return {"modes": synth.mode_table(8, 3, 3, 300.0, config=100),
-            "geom": synth.periodic_cell_geometry(40.0, 40.0, 2, 2), "T0": 300.0, "N": N}
+def _cell_case(N=20000, even=False):
+    m = synth.mode_table(9, 3, 3, 300.0, config=100, even=True) if even else \
+        synth.mode_table(8, 3, 3, 300.0, config=100)
+    return {"modes": m, "geom": synth.periodic_cell_geometry(40.0, 40.0, 2, 2), "T0": 300.0, "N": N}
 
 
 @pytest.mark.parametrize("which,grad", [("bar", (0.0, -0.01)), ("cell", (-0.01, 0.004))])
@@ -63,10 +64,23 @@ def test_steady_production_agrees_with_restatement(engine):
 
 
 def test_steady_production_bulk_kappa(engine):
-    case = _cell_case(200000)
+    case = _cell_case(200000, even=True)
     _load(engine, case)
     K = synth.kappa_rta(case["modes"], 300.0)[0, 0]
     ks = np.array([-engine.steady_run(300.0, (-0.01, 0.0), case["N"], seed=90 + i)["jx"][:4].mean()
+                   / (-0.01e9) for i in range(6)])
+    se = ks.std(ddof=1) / np.sqrt(len(ks))
+    assert abs(ks.mean() - K) < 4.5 * se, (ks.mean(), se, K)
+
+
+@pytest.mark.parametrize("width", [50.0, 500.0])
+def test_steady_production_ribbon_kappa(engine, width):
+    """Diffuse-wall nanoribbon (scale_tau_nanoribbon, src/nanos.cpp:77-112)."""
+    case = {"modes": synth.mode_table(9, 3, 3, 300.0, config=100, even=True),
+            "geom": synth.periodic_ribbon_geometry(40.0, width, 2, 2), "T0": 300.0, "N": 200000}
+    _load(engine, case)
+    K = synth.kappa_ribbon(case["modes"], 300.0, width)
+    ks = np.array([-engine.steady_run(300.0, (-0.01, 0.0), case["N"], seed=120 + i)["jx"][:4].mean()
                    / (-0.01e9) for i in range(6)])
     se = ks.std(ddof=1) / np.sqrt(len(ks))
     assert abs(ks.mean() - K) < 4.5 * se, (ks.mean(), se, K)

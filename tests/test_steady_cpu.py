@@ -3,7 +3,9 @@
 generations, and the physics check that pins it independently of the
 reference: in an infinite medium (a block closed by periodic boxes on all
 sides) the steady flux under a gradient is the bulk RTA conductivity,
-J = -kappa grad T with kappa = 1e21 kB / (nq V) sum C v v tau."""
+J = -kappa grad T with kappa = 1e21 kB / (nq V) sum C v v tau, and in a
+ribbon with diffuse walls it is the nanoribbon conductivity of the
+reference's analytic model."""
 import numpy as np
 import pytest
 
@@ -11,8 +13,14 @@ import pyoracle
 import synth
 
 
+def _even_modes():
+    # mirror-symmetric table: the gradient source's alternating signs then
+    # sample the + and - halves with equal weight, as the analytic forms assume
+    return synth.mode_table(9, 3, 3, 300.0, config=100, even=True)
+
+
 def _cell_case(N=20000):
-    return {"modes": synth.mode_table(8, 3, 3, 300.0, config=100),
+    return {"modes": _even_modes(),
             "geom": synth.periodic_cell_geometry(40.0, 40.0, 2, 2), "T0": 300.0, "N": N}
 
 
@@ -63,7 +71,33 @@ def test_steady_infinite_medium_gives_bulk_rta_kappa(axis, grad):
     assert se < 0.05 * K
 
 
+@pytest.mark.parametrize("width", [50.0, 200.0])
+def test_steady_ribbon_gives_diffuse_wall_kappa(width):
+    """A ribbon periodic along x with void walls: kappa_xx equals the
+    nanoribbon RTA conductivity of scale_tau_nanoribbon (src/nanos.cpp:77-112)."""
+    case = {"modes": _even_modes(), "geom": synth.periodic_ribbon_geometry(40.0, width, 2, 2),
+            "T0": 300.0, "N": 20000}
+    K = synth.kappa_ribbon(case["modes"], 300.0, width)
+    ks = np.array([-pyoracle.steady_run(case, (-0.01, 0.0), seed=10 + s)["jx"][:4].mean() / (-0.01e9)
+                   for s in range(8)])
+    se = ks.std(ddof=1) / np.sqrt(len(ks))
+    assert abs(ks.mean() - K) < 4.0 * se, (ks.mean(), se, K)
+    assert K < synth.kappa_rta(case["modes"], 300.0)[0, 0]
+
+
 def test_steady_needs_a_gradient():
     case = synth.periodic_case(n_particles=10)
     with pytest.raises(Exception):
         pyoracle.steady_run(case, (0.0, 0.0))
+
+
+def test_even_mode_table_is_mirror_symmetric():
+    m = _even_modes()
+    n, nb = 9, m["nb"]
+    om = m["omega"].reshape(n, n, nb)
+    w = m["w"].reshape(n, n, nb)
+    v = m["vg"].reshape(n, n, nb, 3)
+    flip = (n - np.arange(n)) % n
+    assert np.array_equal(om, om[flip]) and np.array_equal(om, om[:, flip])
+    assert np.array_equal(w, w[flip]) and np.array_equal(w, w[:, flip])
+    assert np.array_equal(v[..., 0], -v[flip][..., 0]) and np.array_equal(v[..., 1], v[flip][..., 1])
