@@ -289,12 +289,16 @@ __device__ int grid_generate(const DevTables& T, const DevGrid& G, const int2* b
 }
 
 // One lane carries one particle; each pass of the loop advances every active
-// lane by exactly one segment -- to the end of its free flight or to the
-// next cell border -- so the FP64 work of a warp stays converged however
-// many cells a flight crosses.  Idle lanes take new particles from a global
-// counter, one atomic per warp.  FP64 instructions are kept to the ones that
-// move the particle (exit times, position, clock); comparisons, min/max and
-// the float -> double widening run on the integer pipe.
+// lane by exactly one segment, which ends at the first of: the end of the
+// free flight, the next cell line, the next time-bin border (the last one is
+// maxtime).  Every pass therefore runs one fixed FP64 sequence on all lanes
+// -- the two exit times, the bin border, the advance and the three
+// differences of the pending tally -- and a lane flushes at most once per
+// pass, at the segment end; the FP64 pipe, the limit of this kernel on
+// GB300, never sees the same operation issued twice for different lanes.
+// Idle lanes take new particles from a global counter, one atomic per warp.
+// Comparisons, min/max and the float -> double widening run on the integer
+// pipe.
 template <bool SMEM_TALLY, int MINB>
 __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs A, double* gtally,
                                                      unsigned long long* counters, int* err,
@@ -311,7 +315,6 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     const int lane = threadIdx.x & 31;
     const long long total = T.pend - T.pbegin;
     const int last_bin = T.nbins - 1;
-    const long long maxtime_b = ob(T.maxtime);
     Pending pd;
     pd.key = -1;
     pd.flushes = 0;
@@ -374,109 +377,121 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                 pd.flush(tally, signbit, p.t, p.x, p.y);
                 continue;
             }
-            const double tend = p.t + dt;
-            if (ob(tend) > maxtime_b) dt = T.maxtime - p.t;
             need_flight = false;
         }
-        // exit times of the current cell.  A zero velocity component takes
-        // the upper cell line, so (line - position) >= 0 times its +inf
-        // inverse gives +inf (or NaN on the line, ordered above +inf).
+        // segment end.  A zero velocity component takes the upper cell line,
+        // so (line - position) >= 0 times its +inf inverse gives +inf (or NaN
+        // on the line, ordered above +inf); a negative value (a position that
+        // rounded past its line) orders below 0 and ends the segment at once.
         const int upx = ob(mv.vx) >= 0 ? 1 : 0;
         const int upy = ob(mv.vy) >= 0 ? 1 : 0;
         const double xw = __ldg(A.G.gx + p.i + upx);
         const double yw = __ldg(A.G.gy + p.j + upy);
         const double tx = (xw - p.x) * mv.ivx;
         const double ty = (yw - p.y) * mv.ivy;
+        const double tb = tnb - p.t;
         const bool xfirst = ob(tx) <= ob(ty);
-        const long long te_b = xfirst ? ob(tx) : ob(ty);
-        const bool ends = !(ob(dt) > te_b);          // stays in the cell (also for NaN)
-        const double seg = ends ? dt : obd(te_b > 0 ? te_b : 0);
-        const double t1 = p.t + seg;
+        long long te_b = xfirst ? ob(tx) : ob(ty);
+        long long tb_b = ob(tb);
+        te_b = te_b > 0 ? te_b : 0;
+        tb_b = tb_b > 0 ? tb_b : 0;
+        const long long dt_b = ob(dt);
+        const long long lim_b = te_b < tb_b ? te_b : tb_b;
+        const bool flight_end = !(dt_b > lim_b);             // the flight ends first (or ties)
+        const long long seg_b = flight_end ? dt_b : lim_b;
+        const bool wall = !flight_end && te_b <= tb_b;         // reaches a cell line
+        const bool bin_end = tb_b <= seg_b;                    // reaches the bin border
+        const double seg = obd(seg_b);
+        double t1 = p.t + seg;
         double nx = fma(seg, mv.vx, p.x);
         double ny = fma(seg, mv.vy, p.y);
-        // time-bin borders crossed during the segment close the pending key
-        while (ob(t1) > ob(tnb) && bin < last_bin) {
-            const double d = tnb - p.t;
-            const double bx = fma(d, mv.vx, p.x), by = fma(d, mv.vy, p.y);
-            pd.flush(tally, signbit, tnb, bx, by);
-            ++bin;
-            pd.start(p.box * T.nbins + bin, tnb, bx, by);
-            tnb = __ldg(T.timegrid + bin + 1);
-        }
-        p.t = t1;
         dt -= seg;
-        if (ends) {
-            p.x = nx;
-            p.y = ny;
-            if (!T.ballistic) p.mode = alias_draw(g, T.resample_prob, T.resample_alt, T.n);
-            need_flight = true;
-        } else {
-            // reaches a cell border: the crossed coordinate is the grid line
-            int ni = p.i, nj = p.j, wall;
+        if (bin_end) t1 = tnb;
+        int ni = p.i, nj = p.j, wside = 0;
+        if (wall) {  // the crossed coordinate is the grid line
             if (xfirst) {
                 nx = xw;
                 ni = p.i + (upx ? 1 : -1);
-                wall = upx ? 0 : 1;
+                wside = upx ? 0 : 1;
             } else {
                 ny = yw;
                 nj = p.j + (upy ? 1 : -1);
-                wall = upy ? 2 : 3;
+                wside = upy ? 2 : 3;
             }
-            p.x = nx;
-            p.y = ny;
-            const int nb = grid_cell(A.G, ni, nj);
-            if (nb >= 0) {
-                pd.flush(tally, signbit, p.t, p.x, p.y);
-                p.i = ni;
-                p.j = nj;
-                p.box = nb;
-                pd.start(nb * T.nbins + bin, p.t, p.x, p.y);
-                c.crossings++;
-            } else if (nb <= -2) {
-                c.absorbed++;
+        }
+        // differences of the pending tally at the segment end (telescoping)
+        const double d0 = t1 - pd.t0, d1 = nx - pd.x0, d2 = ny - pd.y0;
+        p.t = t1;
+        p.x = nx;
+        p.y = ny;
+        int nb = p.box;
+        if (wall) nb = grid_cell(A.G, ni, nj);
+        const bool move = wall && nb >= 0;        // into the next cell
+        const bool absorbed = wall && nb <= -2;   // into a reservoir
+        const bool reflect = wall && nb == -1;    // void: reflection, a new flight follows
+        const bool last = bin_end && bin == last_bin;
+        if (move || absorbed || bin_end) {
+            double* b = tally + 3ll * pd.key;
+            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(d0) ^ signbit));
+            atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(d1) ^ signbit));
+            atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(d2) ^ signbit));
+            pd.flushes++;
+            pd.key = -1;
+        }
+        if (absorbed || last) {
+            if (absorbed) c.absorbed++;
+            active = false;
+            continue;
+        }
+        if (bin_end) {
+            ++bin;
+            tnb = __ldg(T.timegrid + bin + 1);
+        }
+        if (move) {
+            p.i = ni;
+            p.j = nj;
+            p.box = nb;
+            c.crossings++;
+        }
+        if (move || bin_end) pd.start(p.box * T.nbins + bin, t1, nx, ny);
+        if (reflect) {
+            // (selects, not an indexed parameter array, which would live in local memory)
+            const int cls = wside == 0 ? A.cls[0] : wside == 1 ? A.cls[1] : wside == 2 ? A.cls[2] : A.cls[3];
+            if (cls < 0) {
+                record_error(err, E_GEOM, pid);
                 active = false;
+                done = true;
                 pd.flush(tally, signbit, p.t, p.x, p.y);
                 continue;
-            } else {
-                // void: reflect at the wall; a new flight follows
-                const int cls = A.cls[wall];
-                if (cls < 0) {
+            }
+            const int k = p.mode;
+            int nm = -1;
+            if (T.specularity > 0. && g.uniform() < T.specularity && T.mirror) {
+                nm = __ldg(T.mirror + (long long)cls * T.n + k);
+                if (nm >= 0) c.specular++;
+            }
+            if (nm < 0) {
+                const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
+                const long long bb = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
+                const int len = int(bb - a);
+                if (len <= 0) {
                     record_error(err, E_GEOM, pid);
                     active = false;
                     done = true;
                     pd.flush(tally, signbit, p.t, p.x, p.y);
                     continue;
                 }
-                const int k = p.mode;
-                int nm = -1;
-                if (T.specularity > 0. && g.uniform() < T.specularity && T.mirror) {
-                    nm = __ldg(T.mirror + (long long)cls * T.n + k);
-                    if (nm >= 0) c.specular++;
-                }
-                if (nm < 0) {
-                    const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
-                    const long long b = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
-                    const int len = int(b - a);
-                    if (len <= 0) {
-                        record_error(err, E_GEOM, pid);
-                        active = false;
-                        done = true;
-                        pd.flush(tally, signbit, p.t, p.x, p.y);
-                        continue;
-                    }
-                    const int jj = int(mulhi32(g.next32(), uint32_t(len)));
-                    const int4 e = __ldg(T.lalias + a + jj);
-                    const float acc = float(g.next32() >> 8) * 0x1p-24f;
-                    nm = acc < __int_as_float(e.x) ? e.y : e.z;
-                }
-                p.mode = nm;
-                c.wall_hits++;
-                need_flight = true;
+                const int jj = int(mulhi32(g.next32(), uint32_t(len)));
+                const int4 e = __ldg(T.lalias + a + jj);
+                const float acc = float(g.next32() >> 8) * 0x1p-24f;
+                nm = acc < __int_as_float(e.x) ? e.y : e.z;
             }
-        }
-        if (ob(p.t) >= maxtime_b) {
-            active = false;
-            pd.flush(tally, signbit, p.t, p.x, p.y);
+            p.mode = nm;
+            c.wall_hits++;
+            need_flight = true;
+        } else if (flight_end) {
+            if (!T.ballistic) p.mode = alias_draw(g, T.resample_prob, T.resample_alt, T.n);
+            need_flight = true;
         }
     }
     c.tallies = pd.flushes;
