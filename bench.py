@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c0"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2"])
     ap.add_argument("--per-step", type=int, default=0, help="particles per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -210,11 +210,92 @@ def reference_arm(args, c, rank, world):
 
 
 # ----------------------------------------------------------------- GPU leg
+def run_berta(args, rank, world, local):
+    """beRTAMC2D on the plain ribbon (6144 modes, 50 cells, 301/299 K
+    reservoirs) with a synthetic 6141 x 6141 propagator exp(B dt), dt = 1 ps,
+    100 steps; Eeff calibrated so that about 1e7 particles are alive at the
+    last step.  A step of this line is one whole 100-step run; the metric is
+    particle-steps (advect + scatter draw) per second."""
+    import torch
+    import btegpu
+    import synth
+    if world > 1 and rank != 0:
+        return 0  # one replica is enough for this extra workload line
+    torch.cuda.set_device(local)
+    c = synth.config0()
+    eng = btegpu.Engine(local)
+    eng.load_modes(c["modes"])
+    eng.load_geometry(c["geom"])
+    t0 = time.perf_counter()
+    P = synth.propagator(c["modes"], dt=1.0, T=300.0, use_torch=True)
+    eng.load_propagator(P, 300.0)
+    build_s = time.perf_counter() - t0
+    dt, maxtime, target = 1.0, 99.0, 10_000_000
+    E = 1e-21
+    for _ in range(4):  # the population scales as 1 / Eeff
+        r = eng.berta_run(dt, maxtime, E, seed=7)
+        n_end = int(r["nparticles"][-1])
+        if n_end >= 10_000:
+            E = E * n_end / target
+            break
+        E = E / 100.0
+    for w in range(args.warmup):
+        eng.berta_run(dt, maxtime, E, seed=100 + w)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ps = 0
+    kern_ms = 0.0
+    e2e_s = 0.0
+    alive = []
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r = eng.berta_run(dt, maxtime, E, seed=200 + k)
+        e2e_s += time.perf_counter() - t1
+        ps += int(r["particle_steps"])
+        kern_ms += float(r["kernel_ms"])
+        alive.append(int(r["nparticles"][-1]))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    nbx = int(c["geom"]["nboxes"])
+    nsteps = btegpu.berta_steps(dt, maxtime)
+    line = {
+        "metric": "beRTA particle-steps/s", "value": ps / (kern_ms * 1e-3), "unit": "particle-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * e2e_s / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded mode table and propagator, no database)",
+        "config": {"workload": "beRTAMC2D on the plain ribbon: 32x32 q x 6 branches (6144 modes), "
+                               "6141x6141 propagator exp(B dt), dt=1 ps, 100 steps, 1 um x 100 nm, "
+                               "50 cells, 301/299K reservoirs, ~1e7 particles alive",
+                   "Eeff_J": E, "alive_at_end": int(np.mean(alive)),
+                   "particle_steps_per_run": ps // args.steps, "propagator_build_s": build_s,
+                   "l2": "flushed between runs (256 MB write)", "parallelism": "replicas x1"},
+        "e2e": {"value": ps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": (nsteps + 1) * (nbx * 3 + 1) * 8},
+        "kernel_ms_per_step": kern_ms / args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    eng.close()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "c2":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the beRTA workload line has no "
+                              "CPU arm; the restatement's beRTA loop is a parity checker only"}))
+            return 0
+        return run_berta(args, rank, world, local)
     c = workload(args.workload)
     if args.impl == "reference":
         return reference_arm(args, c, rank, world)

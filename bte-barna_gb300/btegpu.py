@@ -28,7 +28,7 @@ SOURCE_WALLS, SOURCE_INITIAL = 0, 1
 PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
                   "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run",
-                  "bte_steady_run"]
+                  "bte_steady_run", "bte_load_materials"]
 
 
 class BteError(RuntimeError):
@@ -53,7 +53,7 @@ class Geometry(C.Structure):
                 ("vertices", C.POINTER(C.c_double)), ("Teq", C.POINTER(C.c_double)),
                 ("Tinit", C.POINTER(C.c_double)), ("reservoir", C.POINTER(C.c_int32)),
                 ("thickness", C.c_double), ("translate_to", C.POINTER(C.c_int32)),
-                ("translation", C.POINTER(C.c_double))]
+                ("translation", C.POINTER(C.c_double)), ("material", C.POINTER(C.c_int32))]
 
 
 class RtaParams(C.Structure):
@@ -201,6 +201,9 @@ def geom_struct(g: dict):
         keep["translation"] = np.ascontiguousarray(g["translation"], dtype=np.float64).reshape(-1)
         s.translate_to = _iptr(keep["translate_to"])
         s.translation = _dptr(keep["translation"])
+    if g.get("material") is not None:
+        keep["material"] = np.ascontiguousarray(g["material"], dtype=np.int32)
+        s.material = _iptr(keep["material"])
     return s, keep
 
 
@@ -239,6 +242,9 @@ def load_library(path: str = LIB_PATH):
     lib.bte_load_propagator.restype = C.c_int
     lib.bte_berta_run.argtypes = [vp, C.POINTER(BertaParams), C.POINTER(BertaResult)]
     lib.bte_berta_run.restype = C.c_int
+    lib.bte_load_materials.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]
+    lib.bte_load_materials.restype = C.c_int
     lib.bte_steady_run.argtypes = [vp, C.POINTER(SteadyParams), C.POINTER(SteadyResult)]
     lib.bte_steady_run.restype = C.c_int
     lib.bte_rta_run_noalloc.argtypes = [vp, C.POINTER(RtaParams), C.c_void_p, C.POINTER(RtaResult)]
@@ -368,6 +374,21 @@ def _engine_steady_run(self, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_
                        max_generations, log_cap)
 
 
+def _engine_load_materials(self, w_list, T0_list, share=None):
+    """Materials for batched runs: rates w_list[m] (per mode) at T0_list[m];
+    optional particle share per material (walls source)."""
+    if not w_list:
+        self._check(self.lib.bte_load_materials(self.ctx, 0, None, None, None))
+        return
+    W = np.ascontiguousarray(np.stack([np.asarray(w, dtype=np.float64) for w in w_list]))
+    T = np.ascontiguousarray(np.asarray(T0_list, dtype=np.float64))
+    S = None if share is None else np.ascontiguousarray(np.asarray(share, dtype=np.float64))
+    self._keep["materials"] = (W, T, S)
+    self._check(self.lib.bte_load_materials(self.ctx, len(w_list), _dptr(W), _dptr(T),
+                                            None if S is None else _dptr(S)))
+
+
+Engine.load_materials = _engine_load_materials
 Engine.steady_run = _engine_steady_run
 Engine.load_propagator = _engine_load_propagator
 Engine.berta_run = _engine_berta_run

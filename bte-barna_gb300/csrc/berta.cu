@@ -536,6 +536,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         ensure_static(c);
         const HostModes& m = c->modes;
         const HostGeometry& g = c->geom;
+        if (c->nmat > 0) throw Error(BTE_ERR_INPUT, "materials are for transient batched runs");
         if (!g.rect_grid) throw Error(BTE_ERR_INPUT, "beyond-RTA runs need boxes that tile an axis-aligned grid");
         for (std::size_t b = 0; b < g.boxes.size(); ++b)
             if (!g.reservoir[b] && g.Teq[b] != p->T0)

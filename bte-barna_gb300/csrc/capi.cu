@@ -39,10 +39,12 @@ void ensure_static(bte_ctx* c) {
     const bte::HostGeometry& g = c->geom;
     const std::size_t n = m.n();
     if (!c->modes_dev) {
-        std::vector<double> tau(n);
+        // rates of every material, [nmat][n] (one set without materials)
+        const std::vector<double>& wall = c->nmat > 0 ? c->mat_w : m.w;
+        std::vector<double> tau(wall.size());
+        for (std::size_t k = 0; k < wall.size(); ++k) tau[k] = wall[k] > 0. ? 1.0 / wall[k] : 0.;
         std::vector<bte::ModeVel> mv(n);
         for (std::size_t k = 0; k < n; ++k) {
-            tau[k] = m.w[k] > 0. ? 1.0 / m.w[k] : 0.;
             mv[k].vx = m.vxc[k];
             mv[k].vy = m.vyc[k];
             mv[k].ivx = m.vxc[k] != 0. ? 1.0 / m.vxc[k] : HUGE_VAL;
@@ -50,7 +52,7 @@ void ensure_static(bte_ctx* c) {
         }
         c->d_vxc.upload(m.vxc, c->stream);
         c->d_vyc.upload(m.vyc, c->stream);
-        c->d_w.upload(m.w, c->stream);
+        c->d_w.upload(wall, c->stream);
         c->d_tau.upload(tau, c->stream);
         c->d_mv.upload(mv, c->stream);
         sync(c);
@@ -63,6 +65,7 @@ void ensure_static(bte_ctx* c) {
         c->d_contacts.upload(g.contacts, c->stream);
         c->d_cseg.upload(g.contact_seg, c->stream);
         c->d_transl.upload(g.translation, c->stream);
+        c->d_boxmat.upload(g.mat, c->stream);
         if (g.rect_grid) {
             c->d_gx.upload(g.gx, c->stream);
             c->d_gy.upload(g.gy, c->stream);
@@ -97,10 +100,24 @@ void ensure_static(bte_ctx* c) {
 }
 
 void ensure_resample(bte_ctx* c, double T0) {
+    if (c->nmat > 0) T0 = -2.0;  // one table per material, at the material's T0
     if (c->resample_T0 == T0) return;
     std::vector<double> cdf;
     std::vector<bte::Alias> al;
-    bte::build_resample(c->modes, T0, cdf, al);
+    if (c->nmat > 0) {
+        bte::HostModes mm = c->modes;
+        const std::size_t n = mm.n();
+        for (int k = 0; k < c->nmat; ++k) {
+            std::vector<double> ck;
+            std::vector<bte::Alias> ak;
+            mm.w.assign(c->mat_w.begin() + std::ptrdiff_t(k * n), c->mat_w.begin() + std::ptrdiff_t((k + 1) * n));
+            bte::build_resample(mm, c->mat_T0[std::size_t(k)], ck, ak);
+            cdf.insert(cdf.end(), ck.begin(), ck.end());
+            al.insert(al.end(), ak.begin(), ak.end());
+        }
+    } else {
+        bte::build_resample(c->modes, T0, cdf, al);
+    }
     std::vector<float> prob(al.size());
     std::vector<int> alt(al.size());
     for (std::size_t i = 0; i < al.size(); ++i) {
@@ -121,8 +138,37 @@ using bte::ensure_resample;
 using bte::ensure_static;
 using bte::sync;
 
+// Per-material budgets of a walls-source run: wall w of material m is drawn
+// with probability share[m] E_w / E_m (energy-weighted when no shares).
+void apply_shares(bte_ctx* c, bool upload) {
+    c->shares_dirty = false;
+    if (c->mat_share.empty()) return;
+    const std::size_t nm = c->mat_share.size();
+    c->mat_energy.assign(nm, 0.);
+    for (auto& W : c->gens.walls) {
+        const std::size_t k = std::size_t(c->geom.mat[std::size_t(W.box)]);
+        if (k >= nm) throw Error(BTE_ERR_INPUT, "box material without loaded rates (bte_load_materials)");
+        c->mat_energy[k] += W.energy;
+    }
+    for (std::size_t k = 0; k < nm; ++k)
+        if (c->mat_share[k] > 0. && !(c->mat_energy[k] > 0.))
+            throw Error(BTE_ERR_INPUT, "a material with a particle share has no isothermal wall");
+    double cum = 0.;
+    for (std::size_t i = 0; i < c->gens.walls.size(); ++i) {
+        const auto& W = c->gens.walls[i];
+        const std::size_t k = std::size_t(c->geom.mat[std::size_t(W.box)]);
+        cum += c->mat_share[k] * W.energy / c->mat_energy[k];
+        c->gens.wall_cum[i] = cum;
+    }
+    if (upload) {
+        c->d_wcum.upload(c->gens.wall_cum, c->stream);
+        sync(c);
+    }
+}
+
 void ensure_generators(bte_ctx* c, const bte_rta_params* p) {
     if (c->gen_key_source == p->source) {
+        if (p->source == BTE_SOURCE_WALLS && c->shares_dirty) apply_shares(c, true);
         if (p->source == BTE_SOURCE_INITIAL &&
             (c->gen_key_n != p->nparticles || c->gen_key_seed != p->seed)) {
             c->gen_Eeff = bte::initial_counts(c->gens, p->nparticles, p->seed);
@@ -135,7 +181,9 @@ void ensure_generators(bte_ctx* c, const bte_rta_params* p) {
     }
     if (p->source == BTE_SOURCE_WALLS) {
         c->gens = bte::build_wall_generators(c->modes, c->geom);
+        apply_shares(c, false);
     } else {
+        if (!c->mat_share.empty()) throw Error(BTE_ERR_INPUT, "particle shares need the walls source");
         c->gens = bte::build_initial_generators(c->modes, c->geom);
         c->gen_Eeff = bte::initial_counts(c->gens, p->nparticles, p->seed);
     }
@@ -266,6 +314,9 @@ bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
         ck(cudaSetDevice(c->device), "cudaSetDevice");
         c->modes = bte::build_modes(mt);
         c->have_modes = true;
+        c->nmat = 0;  // materials are rate sets over one table
+        c->mat_w.clear();
+        c->mat_T0.clear();
         c->modes_dev = false;
         c->lambert_dev = false;
         c->resample_T0 = -1;
@@ -280,11 +331,63 @@ bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
     if (!c) return BTE_ERR_INPUT;
     try {
         ck(cudaSetDevice(c->device), "cudaSetDevice");
-        c->geom = bte::build_geometry(g);
+        bte::HostGeometry ng = bte::build_geometry(g);
+        // the Lambert wall table depends on the geometry only through its
+        // distinct wall normals: keep it when they are the same
+        const bool same_normals = c->have_geom && ng.normals.size() == c->geom.normals.size() &&
+                                  std::equal(ng.normals.begin(), ng.normals.end(), c->geom.normals.begin(),
+                                             [](const bte::V2& a, const bte::V2& b) {
+                                                 return a.x == b.x && a.y == b.y;
+                                             });
+        c->geom = std::move(ng);
         c->have_geom = true;
         c->geom_dev = false;
-        c->lambert_dev = false;
+        if (!same_normals) c->lambert_dev = false;
         c->gen_key_source = -1;
+        return BTE_OK;
+    } catch (const Error& e) {
+        return fail(c, e);
+    }
+}
+
+bte_status bte_load_materials(bte_ctx* c, int32_t nmat, const double* w, const double* T0,
+                              const double* share) {
+    if (!c) return BTE_ERR_INPUT;
+    try {
+        if (nmat < 0 || (nmat > 0 && (!w || !T0))) throw Error(BTE_ERR_INPUT, "bad material arrays");
+        if (share && nmat > 0) {
+            double sum = 0.;
+            for (int k = 0; k < nmat; ++k) {
+                if (!(share[k] >= 0.) || !std::isfinite(share[k])) throw Error(BTE_ERR_INPUT, "bad share");
+                sum += share[k];
+            }
+            if (std::fabs(sum - 1.0) > 1e-9) throw Error(BTE_ERR_INPUT, "material shares must sum to 1");
+        }
+        if (nmat > 0 && !c->have_modes) throw Error(BTE_ERR_STATE, "load the mode table first");
+        const std::size_t n = c->modes.n();
+        for (int k = 0; k < nmat; ++k) {
+            if (!(T0[k] > 0.) || !std::isfinite(T0[k])) throw Error(BTE_ERR_INPUT, "material T0 must be > 0");
+            for (std::size_t i = 0; i < n; ++i)
+                if (!std::isfinite(w[size_t(k) * n + i]) || w[size_t(k) * n + i] < 0.)
+                    throw Error(BTE_ERR_VALUE, "non-finite or negative material rate");
+        }
+        const bool same_rates = nmat > 0 && nmat == c->nmat &&
+                                std::equal(w, w + size_t(nmat) * n, c->mat_w.begin()) &&
+                                std::equal(T0, T0 + nmat, c->mat_T0.begin());
+        if (same_rates && share && !c->mat_share.empty()) {
+            // only the particle budgets change: reweight the walls
+            c->mat_share.assign(share, share + nmat);
+            c->shares_dirty = true;
+            return BTE_OK;
+        }
+        c->nmat = nmat;
+        c->mat_w.assign(w ? w : nullptr, w ? w + size_t(nmat) * n : nullptr);
+        c->mat_T0.assign(T0 ? T0 : nullptr, T0 ? T0 + nmat : nullptr);
+        c->mat_share.assign(share && nmat > 0 ? share : nullptr, share && nmat > 0 ? share + nmat : nullptr);
+        c->gen_key_source = -1;  // wall weights depend on the shares
+        c->modes_dev = false;    // rates and lifetimes
+        c->geom_dev = false;     // box materials
+        c->resample_T0 = -1;     // post-scattering tables
         return BTE_OK;
     } catch (const Error& e) {
         return fail(c, e);
@@ -307,10 +410,23 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         if (!c->have_modes || !c->have_geom)
             throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
         ck(cudaSetDevice(c->device), "cudaSetDevice");
-        for (std::size_t b = 0; b < c->geom.boxes.size(); ++b)
-            if (!c->geom.reservoir[b] && !bte::almost_equal(c->geom.Teq[b], p->T0) &&
-                c->geom.Teq[b] != p->T0)
+        for (std::size_t b = 0; b < c->geom.boxes.size(); ++b) {
+            if (c->geom.mat[b] >= std::max(c->nmat, 1))
+                throw Error(BTE_ERR_INPUT, "box material without loaded rates (bte_load_materials)");
+            const double T0b = bte::box_T0(c, int(b), p->T0);
+            if (c->nmat > 0) {  // a particle keeps its material: materials must not touch
+                const bte::GBox& B = c->geom.boxes[b];
+                for (int i = 0; i < B.ncontacts; ++i) {
+                    const int o = c->geom.contacts[std::size_t(B.contact_off + i)].id;
+                    if (c->geom.mat[std::size_t(o)] != c->geom.mat[b])
+                        throw Error(BTE_ERR_INPUT, "boxes of different materials touch");
+                }
+                if (c->geom.tto[b] >= 0 && c->geom.mat[std::size_t(c->geom.tto[b])] != c->geom.mat[b])
+                    throw Error(BTE_ERR_INPUT, "a periodic box maps to another material");
+            }
+            if (!c->geom.reservoir[b] && !bte::almost_equal(c->geom.Teq[b], T0b) && c->geom.Teq[b] != T0b)
                 throw Error(BTE_ERR_INPUT, "Tref in xml is different from provided T0");
+        }
         ensure_static(c);
         if (p->specularity > 0. && !c->have_mirror)
             throw Error(BTE_ERR_INPUT, "specular walls need an axis-aligned q grid with mirror images");
@@ -378,6 +494,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         T.lcdf = c->d_lcdf.as<double>();
         T.lalias = c->d_lalias.as<int4>();
         T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
+        T.box_mat = c->nmat > 0 ? c->d_boxmat.as<int>() : nullptr;
         T.ntime = int(ntime);
         T.timegrid = c->d_time.as<double>();
         T.maxtime = maxtime;
@@ -496,9 +613,23 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
                 jy[k] /= vbox;
             }
         }
-        for (auto& x : gz) x *= Eeff;
-        for (auto& x : jx) x *= Eeff * 1e12 * 1e9 * 1e9;
-        for (auto& x : jy) x *= Eeff * 1e12 * 1e9 * 1e9;
+        if (!c->mat_share.empty() && p->source == BTE_SOURCE_WALLS) {
+            // Eeff_m = E_m / (share_m N) per material
+            for (int ir = 0; ir < nbx; ++ir) {
+                const std::size_t k = std::size_t(g.mat[std::size_t(ir)]);
+                const double Em = c->mat_share[k] > 0. ? c->mat_energy[k] / (c->mat_share[k] * double(p->nparticles)) : 0.;
+                for (int i = 0; i < nbins; ++i) {
+                    const std::size_t q = std::size_t(ir) * nbins + i;
+                    gz[q] *= Em;
+                    jx[q] *= Em * 1e12 * 1e9 * 1e9;
+                    jy[q] *= Em * 1e12 * 1e9 * 1e9;
+                }
+            }
+        } else {
+            for (auto& x : gz) x *= Eeff;
+            for (auto& x : jx) x *= Eeff * 1e12 * 1e9 * 1e9;
+            for (auto& x : jy) x *= Eeff * 1e12 * 1e9 * 1e9;
+        }
         if (p->source == BTE_SOURCE_WALLS) {
             // step response: integrate in time
             for (int ir = 0; ir < nbx; ++ir)
@@ -516,10 +647,20 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
                 jy[k] /= step;
             }
         }
-        const double cv = bte::calc_cv(m, p->T0);
         const double vcorr = g.thickness / m.c;
-        if (out->temperature)
-            for (std::size_t k = 0; k < nk; ++k) out->temperature[k] = gz[k] / (cv / vcorr) + p->T0;
+        if (out->temperature) {
+            std::vector<double> cvm(std::size_t(std::max(c->nmat, 1)));
+            for (std::size_t k = 0; k < cvm.size(); ++k)
+                cvm[k] = bte::calc_cv(m, c->nmat > 0 ? c->mat_T0[k] : p->T0);
+            for (int ir = 0; ir < nbx; ++ir) {
+                const double cv = cvm[std::size_t(c->nmat > 0 ? g.mat[std::size_t(ir)] : 0)];
+                const double T0b = bte::box_T0(c, ir, p->T0);
+                for (int i = 0; i < nbins; ++i) {
+                    const std::size_t k = std::size_t(ir) * nbins + i;
+                    out->temperature[k] = gz[k] / (cv / vcorr) + T0b;
+                }
+            }
+        }
         if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
         if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
         return BTE_OK;
@@ -634,7 +775,7 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
         *why = "the allocation-free run needs boxes that tile an axis-aligned grid";
         return BTE_ERR_INPUT;
     }
-    if (c->resample_T0 != p->T0 || c->gen_key_source != p->source ||
+    if (c->resample_T0 != (c->nmat > 0 ? -2.0 : p->T0) || c->gen_key_source != p->source ||
         (p->source == BTE_SOURCE_INITIAL &&
          (c->gen_key_n != p->nparticles || c->gen_key_seed != p->seed))) {
         *why = "context prepared for other parameters: run bte_rta_run once with this T0, source "
@@ -691,6 +832,7 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
     T.lcdf = c->d_lcdf.as<double>();
     T.lalias = c->d_lalias.as<int4>();
     T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
+    T.box_mat = c->nmat > 0 ? c->d_boxmat.as<int>() : nullptr;
     T.ntime = r->ntime;
     T.timegrid = nullptr;  // set by the caller
     T.maxtime = r->maxtime;
@@ -758,6 +900,11 @@ void fill_static_tables(bte_ctx* c, DevTables& T) {
     T.lcdf = c->d_lcdf.as<double>();
     T.lalias = c->d_lalias.as<int4>();
     T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
+    T.box_mat = c->nmat > 0 ? c->d_boxmat.as<int>() : nullptr;
+}
+
+double box_T0(const bte_ctx* c, int b, double T0) {
+    return c->nmat > 0 ? c->mat_T0[std::size_t(c->geom.mat[std::size_t(b)])] : T0;
 }
 
 void set_ctx_error(bte_ctx* c, const std::string& m) {

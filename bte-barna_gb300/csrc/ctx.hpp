@@ -78,7 +78,13 @@ struct bte_ctx {
     bte::DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;
     int nclass = 0;
     bool have_mirror = false;
-    // per-T0 resampling
+    // materials of batched runs (0: the mode table's own rates at the run's T0)
+    int nmat = 0;
+    std::vector<double> mat_w, mat_T0, mat_share;
+    std::vector<double> mat_energy;   // walls-source energy rate per material (with shares)
+    bool shares_dirty = false;        // shares changed since the wall weights were set
+    bte::DBuf d_boxmat;
+    // per-T0 (or per-material) resampling
     double resample_T0 = -1;
     bte::DBuf d_rcdf, d_rprob, d_ralt;
     // generators
@@ -104,6 +110,8 @@ void ensure_resample(bte_ctx* c, double T0);
 void sync(bte_ctx* c);
 void destroy_berta(bte_ctx* c);
 void destroy_steady(bte_ctx* c);
+// T0 of box b's material (the run's T0 without materials).
+double box_T0(const bte_ctx* c, int b, double T0);
 // Mode, geometry and Lambert tables of a context into the kernel tables.
 void fill_static_tables(bte_ctx* c, DevTables& T);
 }  // namespace bte

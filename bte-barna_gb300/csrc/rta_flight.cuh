@@ -38,6 +38,7 @@ struct DevTables {
     const double* vyc;
     const double* w;
     const double* tau;
+    const int* box_mat;     // [box] material (null: one material)
     const double* resample_cdf;
     const float* resample_prob;
     const int* resample_alt;
@@ -96,7 +97,13 @@ struct Particle {
     int sign;
     double t;
     int box;
+    int mo;   // material offset into the per-material tables (material * n)
 };
+
+// Offset of box b's material in the [material][mode] tables.
+__device__ __forceinline__ int mat_off(const DevTables& T, int b) {
+    return T.box_mat ? __ldg(T.box_mat + b) * T.n : 0;
+}
 
 // std::lower_bound over a sorted double array: first index with a[i] >= u.
 __device__ __forceinline__ int lower_bound_d(const double* a, int n, double u) {
@@ -331,7 +338,7 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
             fate = FATE_SCATTER;
             c.scattered++;
         } else if (!T.ballistic) {
-            p.mode = pol.resample(T);
+            p.mode = pol.resample(T, p.mo);
         }
         dt = 0.;
         nudges = 0;
@@ -505,6 +512,7 @@ __device__ int generate_wall(const DevTables& T, P& pol, Particle& p) {
     p.sign = W.sign;
     p.t = 0.;
     p.box = W.box;
+    p.mo = mat_off(T, W.box);
     return 0;
 }
 
@@ -553,6 +561,7 @@ __device__ int generate(const DevTables& T, P& pol, long long pid, Particle& p) 
     p.sign = T.init_sign[g];
     p.t = 0.;
     p.box = b;
+    p.mo = mat_off(T, b);
     return 0;
 }
 
@@ -569,9 +578,9 @@ __device__ int run_particle(const DevTables& T, P& pol, long long pid, Counters&
         if (++nev > EVENT_CAP) return E_LIMIT;
         const int k = p.mode;
         const V2 v = v2(T.vxc[k], T.vyc[k]);
-        const double w = T.w[k];
+        const double w = T.w[p.mo + k];
         if (w == 0.) return E_VALUE;
-        double dt = pol.flight(T, k);
+        double dt = pol.flight(T, p.mo + k);
         c.events++;
         if (time + dt > T.maxtime) dt = T.maxtime - time + 1.0e-8;
         int guard = 0, fate = FATE_LOST;

@@ -54,10 +54,10 @@ struct ProdPolicy {
     __device__ double u() { return g.uniform(); }
     __device__ int choose(int n) { return uniform_below(g, uint32_t(n)); }
     __device__ double flight(const DevTables& T, int k) {
-        return double(-logf(g.uniformf())) * __ldg(T.tau + k);
+        return double(-logf(g.uniformf())) * __ldg(T.tau + k);  // k: material offset + mode
     }
-    __device__ int resample(const DevTables& T) {
-        return alias_draw(g, T.resample_prob, T.resample_alt, T.n);
+    __device__ int resample(const DevTables& T, int mo) {
+        return alias_draw(g, T.resample_prob + mo, T.resample_alt + mo, T.n);
     }
     __device__ int gen_mode(const DevTables& T, int gi) {
         const long long o = (long long)gi * T.n;
@@ -197,6 +197,7 @@ struct GridParticle {
     int mode;
     int sign;
     int box;
+    int mo;        // material offset (material * n)
 };
 
 // Order of non-negative doubles (and +inf, and NaN above +inf) through their
@@ -284,6 +285,7 @@ __device__ int grid_generate(const DevTables& T, const DevGrid& G, const int2* b
     p.i = ij.x;
     p.j = ij.y;
     p.box = box;
+    p.mo = mat_off(T, box);
     p.t = 0.;
     return 0;
 }
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     pd.flushes = 0;
     pd.t0 = pd.x0 = pd.y0 = 0.;
     GridParticle p;
-    p.i = p.j = p.mode = p.box = 0;
+    p.i = p.j = p.mode = p.box = p.mo = 0;
     p.sign = 1;
     p.x = p.y = p.t = 0.;
     Philox g;
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             // a new free flight: u in (0, 1) -> dt = -tau ln u (FP32 log)
             const int k = p.mode;
             mv = A.mv[k];
-            dt = widen_pos(-logf(g.uniformf())) * __ldg(T.tau + k);
+            dt = widen_pos(-logf(g.uniformf())) * __ldg(T.tau + p.mo + k);
             c.events++;
             if (ob(dt) <= 0 || ++nev > EVENT_CAP) {  // zero rate or runaway particle
                 record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
@@ -490,7 +492,8 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             c.wall_hits++;
             need_flight = true;
         } else if (flight_end) {
-            if (!T.ballistic) p.mode = alias_draw(g, T.resample_prob, T.resample_alt, T.n);
+            if (!T.ballistic)
+                p.mode = alias_draw(g, T.resample_prob + p.mo, T.resample_alt + p.mo, T.n);
             need_flight = true;
         }
     }

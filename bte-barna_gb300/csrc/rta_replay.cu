@@ -34,9 +34,11 @@ struct ReplayPolicy {
     __device__ int choose(int n) { return uniform_below(g, uint32_t(n)); }
     __device__ double flight(const DevTables& T, int k) {
         const double uu = u();
-        return -bte_log(uu) / T.w[k];
+        return -bte_log(uu) / T.w[k];  // k: material offset + mode
     }
-    __device__ int resample(const DevTables& T) { return lower_bound_d(T.resample_cdf, T.n, u()); }
+    __device__ int resample(const DevTables& T, int mo) {
+        return lower_bound_d(T.resample_cdf + mo, T.n, u());
+    }
     __device__ int gen_mode(const DevTables& T, int gi) {
         return lower_bound_d(T.gen_cdf + (long long)gi * T.n, T.n, u());
     }

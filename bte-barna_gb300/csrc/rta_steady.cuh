@@ -90,6 +90,7 @@ __device__ int steady_generate0(const DevTables& T, const SteadyArgs& A, P& pol,
     p.sign = want;
     p.t = 0.;
     p.box = b;
+    p.mo = mat_off(T, b);
     return 0;
 }
 
@@ -107,8 +108,9 @@ __device__ int steady_birth(const DevTables& T, const SteadyArgs& A, P& pol, lon
     V2 r;
     const int e = random_point(T, pol, b, r);
     if (e) return e;
+    p.mo = mat_off(T, b);
     p.pos = r;
-    p.mode = pol.resample(T);
+    p.mode = pol.resample(T, p.mo);
     p.sign = A.birth_sign[lo];
     p.t = 0.;
     p.box = b;
@@ -129,6 +131,7 @@ __device__ int steady_slot(const DevTables& T, const SteadyArgs& A, P& pol, long
         p.box = q.box;
         p.sign = q.sign;
         p.t = 0.;
+        p.mo = mat_off(T, q.box);
         e = 0;
     } else {
         e = steady_birth(T, A, pol, slot - A.nin, p);
@@ -136,8 +139,8 @@ __device__ int steady_slot(const DevTables& T, const SteadyArgs& A, P& pol, long
     if (e) return e;
     const int k = p.mode;
     const V2 v = v2(T.vxc[k], T.vyc[k]);
-    if (T.w[k] == 0.) return E_VALUE;
-    double dt = pol.flight(T, k);
+    if (T.w[p.mo + k] == 0.) return E_VALUE;
+    double dt = pol.flight(T, p.mo + k);
     c.events++;
     fate = FATE_LOST;
     int guard = 0, nudges = 0;

@@ -136,6 +136,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         using namespace bte;
         if (!c->have_modes || !c->have_geom)
             throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
+        if (c->nmat > 0) throw Error(BTE_ERR_INPUT, "materials are for transient batched runs");
         if (!(p->T0 > 0.) || !std::isfinite(p->T0)) throw Error(BTE_ERR_INPUT, "T0 must be > 0");
         if (p->nparticles < 1 || p->nparticles > 0x7fffffffll)
             throw Error(BTE_ERR_INPUT, "nparticles must be in [1, 2^31)");

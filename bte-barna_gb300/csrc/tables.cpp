@@ -266,6 +266,9 @@ HostGeometry build_geometry(const bte_geometry* g) {
         G.Teq.push_back(g->Teq[i]);
         G.Tinit.push_back(g->Tinit ? g->Tinit[i] : g->Teq[i]);
         G.reservoir.push_back(g->reservoir[i] != 0);
+        const int mt = g->material ? g->material[i] : 0;
+        if (mt < 0) throw Error(BTE_ERR_INPUT, "negative material index");
+        G.mat.push_back(mt);
         const int to = g->translate_to ? g->translate_to[i] : -1;
         G.tto.push_back(to);
         G.translation.push_back(to >= 0 && g->translation

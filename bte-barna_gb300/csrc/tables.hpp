@@ -42,6 +42,7 @@ struct HostGeometry {
     std::vector<int> tto;              // periodic: target box, -1 otherwise
     std::vector<V2> translation;       // periodic: translation vector
     std::vector<V2> contact_seg;       // [contact][2]: lengthened contact segment
+    std::vector<int> mat;              // material of each box (batched runs)
     bool periodic = false;             // any periodic box
     double thickness = 0;
     // axis-aligned grid description (production fast path); valid when

@@ -414,6 +414,62 @@ def read_propagator(path: str) -> np.ndarray:
     return data.reshape((n, n), order="F")
 
 
+# ------------------------------------------------------------------ sweep
+def sweep_cases(n_widths: int = 16, temps=(100.0, 200.0, 300.0, 500.0), w_min: float = 20.0,
+                w_max: float = 2000.0, n0: float = 1e5) -> list:
+    """The batched-sweep cases: n_widths ribbon widths log-spaced over
+    [w_min, w_max] at each temperature, budgets N_w = n0 * 100^(k/15)."""
+    widths = np.geomspace(w_min, w_max, n_widths)
+    budgets = [int(round(n0 * 100.0 ** (k / max(n_widths - 1, 1)))) for k in range(n_widths)]
+    return [{"T": float(T), "width": float(w), "budget": int(N)}
+            for T in temps for w, N in zip(widths, budgets)]
+
+
+def sweep_ribbon(width: float, T: float, length: float = 1000.0, ncells: int = 50, dT: float = 1.0,
+                 thickness: float = C_LAT) -> dict:
+    """One sweep case alone: the plain ribbon at temperature T with its
+    reservoirs at T + dT and T - dT."""
+    return ribbon_geometry(length, width, ncells, T_hot=T + dT, T_cold=T - dT, T0=T,
+                           thickness=thickness)
+
+
+def sweep_union_geometry(cases: list, length: float = 1000.0, ncells: int = 50, dT: float = 1.0,
+                         gap: float = 10.0, reservoir_depth: float = 20.0,
+                         thickness: float = C_LAT) -> dict:
+    """Every case's ribbon in one geometry: ribbons stacked along y with a
+    void gap between them (so no particle changes ribbon), each with its own
+    reservoirs at T +- dT; box material = case index.  The boxes tile one
+    axis-aligned grid (shared x lines), so the union runs on the grid path."""
+    boxes, Teq, res, mat = [], [], [], []
+    dx = length / ncells
+    y0 = 0.0
+    for ci, cs in enumerate(cases):
+        w, T = cs["width"], cs["T"]
+        for i in range(ncells):
+            boxes.append(_rect(i * dx, y0, (i + 1) * dx, y0 + w))
+            Teq.append(T)
+            res.append(0)
+            mat.append(ci)
+        boxes.append(_rect(-reservoir_depth, y0, 0.0, y0 + w))
+        boxes.append(_rect(length, y0, length + reservoir_depth, y0 + w))
+        Teq += [T + dT, T - dT]
+        res += [1, 1]
+        mat += [ci, ci]
+        y0 += w + gap
+    g = _pack(boxes, Teq, list(Teq), res, thickness)
+    g["material"] = np.array(mat, dtype=np.int32)
+    g["ncells"] = ncells
+    return g
+
+
+def sweep_kappa(jx: np.ndarray, cells, length: float = 1000.0, dT: float = 1.0, last: int = 10) -> float:
+    """kappa_eff = J_x L / Delta T (W m^-1 K^-1) from the flux of the given
+    cells averaged over the last time bins (the step response has reached
+    its steady state there)."""
+    J = float(np.mean(jx[cells, -last:]))
+    return J * length * 1e-9 / (2.0 * dT)
+
+
 # ------------------------------------------------------------------ configs
 def config0(n_particles: int = 1_000_000) -> dict:
     """Plain RTA ribbon: 32x32x6 modes, 1 um x 100 nm, 50 cells, 301/299 K

@@ -103,6 +103,9 @@ typedef struct bte_geometry {
      * include/geometry_2d.hpp:366-493).  Both NULL: no periodic box. */
     const int32_t* translate_to; /* [nboxes] target box j, -1 = not periodic   */
     const double* translation;   /* [nboxes][2] translation vector, nm         */
+    /* Material of each box for batched sweeps (NULL: every box is material
+     * 0); materials come from bte_load_materials. */
+    const int32_t* material;     /* [nboxes] */
 } bte_geometry;
 
 /* Parameters of one RTA run (the <RTA_MC2d> XML of src/RTA_MC2D.cpp:1818-1947
@@ -268,6 +271,27 @@ bte_status bte_load_modes(bte_ctx* ctx, const bte_mode_table* modes);
 /* Load the boxes and build borders and contacts (geometry_2d::get_sides and
  * calculate_contacts, src/geometry_2d.cpp:51-124, :295-381). */
 bte_status bte_load_geometry(bte_ctx* ctx, const bte_geometry* geom);
+
+/* Materials of batched sweeps: nmat relaxation-rate sets over the loaded
+ * mode table (the same crystal at several temperatures).  Material m has
+ * rates w[m][mode] and reference temperature T0[m], which set its
+ * lifetimes, its post-scattering distribution and its temperature
+ * conversion; a box of geometry.material = m uses material m, and a run
+ * checks each box's Teq against its material's T0 (bte_rta_params.T0 is
+ * then unused).  The reference keeps rates, sampler and C_v per material
+ * too (inpars.material_w0 / material_sampler / material_cv,
+ * src/RTA_MC2D.cpp:1893-1923); here the materials share the mode table and
+ * the Lambert wall table.  Boxes of different materials must not touch: a
+ * particle keeps its material.  nmat = 0 returns to the single table.
+ *
+ * share (optional, [nmat], summing to 1) gives each material its own
+ * particle budget in a walls-source run: a wall of material m is drawn with
+ * probability share[m] E_w / E_m instead of E_w / E (the reference's
+ * energy-weighted choice, src/RTA_MC2D.cpp:390-418), and the particles of
+ * material m carry Eeff_m = E_m / (share[m] N) (:2177) in the conversion of
+ * its boxes.  NULL keeps the energy-weighted choice and one Eeff. */
+bte_status bte_load_materials(bte_ctx* ctx, int32_t nmat, const double* w, const double* T0,
+                              const double* share);
 
 /* Run the RTA particle loop for one run and fill `out` (replaces one
  * iteration of the run loop of src/RTA_MC2D.cpp:2188-2543: generation,

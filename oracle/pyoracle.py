@@ -39,6 +39,12 @@ def load():
                                    C.POINTER(_bt.RtaParams), C.c_int, C.c_int,
                                    C.POINTER(_bt.RtaResult), C.POINTER(C.c_int64)]
     lib.oracle_rta_run.restype = C.c_int
+    lib.oracle_rta_run_mat.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry), C.c_int,
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double),
+                                       C.POINTER(_bt.RtaParams), C.c_int, C.c_int,
+                                       C.POINTER(_bt.RtaResult), C.POINTER(C.c_int64)]
+    lib.oracle_rta_run_mat.restype = C.c_int
     lib.oracle_geometry_dump.argtypes = [C.c_void_p, C.POINTER(_bt.Geometry),
                                          C.POINTER(C.c_double), C.c_longlong]
     lib.oracle_geometry_dump.restype = C.c_longlong
@@ -108,7 +114,9 @@ def steady_run(case: dict, gradient, N=None, seed=1, nthreads=8, eps_energy=-42.
 
 
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,
-            source=None, specularity=None):
+            source=None, specularity=None, materials=None):
+    """`materials`: optional (list of per-mode rate arrays, list of T0[,
+    shares]) for geometries whose boxes carry a `material` index."""
     """Run the restatement on a synth case dict; returns arrays and counters."""
     if source is None:
         source = _bt.SOURCE_INITIAL if case.get("source") == "initial" else _bt.SOURCE_WALLS
@@ -129,8 +137,21 @@ def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, 
         setattr(r, k, out[k].ctypes.data_as(C.POINTER(C.c_double)))
     r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
     cnt = np.zeros(7, dtype=np.int64)
-    st = lib.oracle_rta_run(C.byref(ms), C.byref(gs), C.byref(p), int(nthreads), int(log_impl),
-                            C.byref(r), cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+    if materials:
+        W = np.ascontiguousarray(np.stack([np.asarray(w, dtype=np.float64) for w in materials[0]]))
+        T = np.ascontiguousarray(np.asarray(materials[1], dtype=np.float64))
+        Sh = None
+        if len(materials) > 2 and materials[2] is not None:
+            Sh = np.ascontiguousarray(np.asarray(materials[2], dtype=np.float64))
+        st = lib.oracle_rta_run_mat(C.byref(ms), C.byref(gs), len(materials[0]),
+                                    W.ctypes.data_as(C.POINTER(C.c_double)),
+                                    T.ctypes.data_as(C.POINTER(C.c_double)),
+                                    None if Sh is None else Sh.ctypes.data_as(C.POINTER(C.c_double)),
+                                    C.byref(p), int(nthreads),
+                                    int(log_impl), C.byref(r), cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+    else:
+        st = lib.oracle_rta_run(C.byref(ms), C.byref(gs), C.byref(p), int(nthreads), int(log_impl),
+                                C.byref(r), cnt.ctypes.data_as(C.POINTER(C.c_int64)))
     if st != 0:
         raise _bt.BteError(st, lib.oracle_last_error().decode())
     out.update(Eeff=r.Eeff, energy_rate=r.energy_rate, events=int(cnt[0]), wall_hits=int(cnt[1]),

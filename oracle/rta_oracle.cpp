@@ -262,6 +262,7 @@ struct Box {
     std::map<std::size_t, std::vector<Border>> contacts;
     double Teq = -1, Treal = -1;
     bool reservoir = false;
+    int mat = 0;                 // material (batched sweeps)
     bool periodic = false;       // <Translate_to>
     std::size_t box2translate = 0;
     V2 translation;
@@ -529,6 +530,14 @@ struct Sim {
     // run state
     std::vector<double> timegrid;
     std::vector<double> resample_cdf;
+    // per-material rates and post-scattering CDFs (material 0 = w and
+    // resample_cdf when no materials are given)
+    std::vector<std::vector<double>> mat_w, mat_res;
+    std::vector<double> mat_T0;
+    const std::vector<double>& w_of(int mt) const { return mat_w.empty() ? m.w : mat_w[std::size_t(mt)]; }
+    const std::vector<double>& res_of(int mt) const {
+        return mat_res.empty() ? resample_cdf : mat_res[std::size_t(mt)];
+    }
     std::vector<std::vector<std::pair<std::size_t, double>>> lambert;  // rows by ascending mode
     std::vector<WallGen> gens;
     std::vector<double> gen_cum;  // cumulative generator weights
@@ -702,6 +711,7 @@ struct Particle {
     int sign = 1;
     double t = 0;
     std::size_t box = 0;
+    int mat = 0;  // material of the birth box, kept for the particle's life
 };
 
 struct Tally {
@@ -889,7 +899,7 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
         p.t += dt;
         if (!o.ballistic) {
             double u = canonical(rng);
-            std::size_t pos = lower_bound_idx(S.resample_cdf, u);
+            std::size_t pos = lower_bound_idx(S.res_of(p.mat), u);
             p.q = pos / nb;
             p.alpha = pos % nb;
         }
@@ -1039,6 +1049,7 @@ inline Particle generate(const Sim& S, Pcg64& rng) {
     p.sign = G.sign;
     p.t = 0.;
     p.box = G.box;
+    p.mat = S.sys[G.box].mat;
     return p;
 }
 
@@ -1074,6 +1085,7 @@ inline Particle generate_initial(const Sim& S, std::size_t pid, Pcg64& rng) {
     p.sign = S.init_sign[g];
     p.t = 0.;
     p.box = S.init_box[g];
+    p.mat = S.sys[p.box].mat;
     return p;
 }
 
@@ -1127,7 +1139,7 @@ inline void run_particle(const Sim& S, std::size_t pid, uint64_t seed, double ma
         if (++nev > (1ll << 26)) throw limit_error("free flights per particle cap");
         std::size_t k = p.q * nb + p.alpha;
         V2 v = get_v(S.m, k);
-        double w = S.m.w[k];
+        double w = S.w_of(p.mat)[k];
         if (w == 0.) throw value_error("invalid scattering rate");
         double u = canonical(rng);
         double dt_ = -(o.log_impl == 0 ? bte_log(u) : std::log(u)) / w;
@@ -1714,6 +1726,7 @@ orc::Sim build_sim(const bte_mode_table* mt, const bte_geometry* gm) {
         b.Teq = gm->Teq[i];
         b.Treal = gm->Tinit ? gm->Tinit[i] : gm->Teq[i];
         b.reservoir = gm->reservoir[i] != 0;
+        b.mat = gm->material ? gm->material[i] : 0;
         if (gm->translate_to && gm->translate_to[i] >= 0) {
             b.periodic = true;
             b.box2translate = std::size_t(gm->translate_to[i]);
@@ -1883,10 +1896,34 @@ int oracle_lambert_nnz(const bte_mode_table* mt, const bte_geometry* gm, long lo
 // One RTA run (walls source) over particles [begin, end) on `nthreads` host
 // threads (1 gives the reference's per-particle order of summation).
 // counters: events, wall_hits, crossings, absorbed, nudges, quirks.
+int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nmat, const double* mw,
+                       const double* mT0, const double* share, const bte_rta_params* rp, int nthreads,
+                       int log_impl, bte_rta_result* out, int64_t* counters);
+
 int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_rta_params* rp,
                    int nthreads, int log_impl, bte_rta_result* out, int64_t* counters) {
+    return oracle_rta_run_mat(mt, gm, 0, nullptr, nullptr, nullptr, rp, nthreads, log_impl, out, counters);
+}
+
+// The same with nmat materials: rates mw[m][mode] at reference temperature
+// mT0[m]; box b uses material gm->material[b] (rates, post-scattering
+// distribution, temperature conversion).  With share[m] (walls source) the
+// wall of material m is drawn with probability share[m] E_w / E_m and the
+// particles of material m carry Eeff_m = E_m / (share[m] N).
+int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nmat, const double* mw,
+                       const double* mT0, const double* share, const bte_rta_params* rp, int nthreads,
+                       int log_impl, bte_rta_result* out, int64_t* counters) {
     try {
         orc::Sim S = build_sim(mt, gm);
+        for (int k = 0; k < nmat; ++k) {
+            const std::size_t n = S.m.n();
+            S.mat_w.emplace_back(mw + std::size_t(k) * n, mw + std::size_t(k + 1) * n);
+            std::vector<double> pm(n);
+            for (std::size_t i = 0; i < n; ++i)
+                pm[i] = S.m.omega[i] <= 0. ? 0. : orc::bose_einstein_kernel(S.m.omega[i], mT0[k]) * S.mat_w.back()[i];
+            S.mat_res.push_back(orc::fill_cumulative(pm));
+            S.mat_T0.push_back(mT0[k]);
+        }
         // time grid (src/RTA_MC2D.cpp:2118-2124), Eigen LinSpaced(low + i*step)
         std::size_t ntime = std::size_t(std::floor(rp->maxtime / rp->dt + 1.0e-6)) + 1;
         double maxtime = double(ntime - 1) * rp->dt;
@@ -1901,9 +1938,25 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
         S.resample_cdf = orc::fill_cumulative(pmf);
         orc::build_lambert(S);
         int64_t total_particles = rp->nparticles;
+        std::vector<double> Em;  // energy rate per material (with shares)
         if (rp->source == BTE_SOURCE_WALLS) {
             orc::build_generators(S, rp->T0);
             S.Eeff = S.energy / double(rp->nparticles);
+            if (share && nmat > 0) {
+                Em.assign(std::size_t(nmat), 0.);
+                std::vector<double> e;
+                for (auto& g : S.gens) {
+                    double Lb = orc::norm(g.b.p2 - g.b.p1);
+                    e.push_back(std::fabs(g.flux) * Lb * S.thickness);
+                    Em[std::size_t(S.sys[g.box].mat)] += e.back();
+                }
+                double cum = 0.;
+                for (std::size_t i = 0; i < S.gens.size(); ++i) {
+                    const std::size_t k = std::size_t(S.sys[S.gens[i].box].mat);
+                    cum += share[k] * e[i] / Em[k];
+                    S.gen_cum[i] = cum;
+                }
+            }
         } else {
             orc::build_initial(S, rp->nparticles, rp->seed);
             total_particles = S.init_first.back();
@@ -2007,9 +2060,21 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
                 jy[ir * nbn + i] /= vbox;
             }
         }
-        for (auto& x : gz) x *= S.Eeff;
-        for (auto& x : jx) x *= S.Eeff * 1e12 * 1e9 * 1e9;
-        for (auto& x : jy) x *= S.Eeff * 1e12 * 1e9 * 1e9;
+        if (!Em.empty()) {
+            for (std::size_t ir = 0; ir < nbx; ++ir) {
+                const std::size_t k = std::size_t(S.sys[ir].mat);
+                const double E = share[k] > 0. ? Em[k] / (share[k] * double(rp->nparticles)) : 0.;
+                for (std::size_t i = 0; i < nbn; ++i) {
+                    gz[ir * nbn + i] *= E;
+                    jx[ir * nbn + i] *= E * 1e12 * 1e9 * 1e9;
+                    jy[ir * nbn + i] *= E * 1e12 * 1e9 * 1e9;
+                }
+            }
+        } else {
+            for (auto& x : gz) x *= S.Eeff;
+            for (auto& x : jx) x *= S.Eeff * 1e12 * 1e9 * 1e9;
+            for (auto& x : jy) x *= S.Eeff * 1e12 * 1e9 * 1e9;
+        }
         if (rp->source == BTE_SOURCE_WALLS) {
             for (std::size_t ir = 0; ir < nbx; ++ir)
                 for (std::size_t i = 1; i < nbn; ++i) {
@@ -2024,12 +2089,19 @@ int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_r
                 jy[k] /= step;
             }
         }
-        double cv = 0.;
-        for (std::size_t k = 0; k < S.m.n(); ++k) cv += orc::bose_einstein_kernel(S.m.omega[k], rp->T0);
-        cv *= orc::kB / double(S.m.nq) / S.m.V;
         double vcorr = S.thickness / S.m.c;
+        auto cv_at = [&](double T) {
+            double cv = 0.;
+            for (std::size_t k = 0; k < S.m.n(); ++k) cv += orc::bose_einstein_kernel(S.m.omega[k], T);
+            return cv * orc::kB / double(S.m.nq) / S.m.V;
+        };
         if (out->temperature)
-            for (std::size_t k = 0; k < nk; ++k) out->temperature[k] = gz[k] / (cv / vcorr) + rp->T0;
+            for (std::size_t ir = 0; ir < nbx; ++ir) {
+                const double T0b = nmat > 0 ? S.mat_T0[std::size_t(S.sys[ir].mat)] : rp->T0;
+                const double cv = cv_at(T0b);
+                for (std::size_t i = 0; i < nbn; ++i)
+                    out->temperature[ir * nbn + i] = gz[ir * nbn + i] / (cv / vcorr) + T0b;
+            }
         if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
         if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
         return 0;
