@@ -45,7 +45,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2"])
+    ap.add_argument("--workload", default="c1", choices=["c1", "c0", "c2", "c3", "c4"])
+    ap.add_argument("--sweep-tol", type=float, default=0.01, help="3 sigma / kappa target (c3)")
+    ap.add_argument("--sweep-seconds", type=float, default=240.0, help="time cap per arm (c3)")
     ap.add_argument("--per-step", type=int, default=0, help="particles per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -232,13 +234,15 @@ def run_berta(args, rank, world, local):
     build_s = time.perf_counter() - t0
     dt, maxtime, target = 1.0, 99.0, 10_000_000
     E = 1e-21
-    for _ in range(4):  # the population scales as 1 / Eeff
+    for _ in range(8):  # about 1 / Eeff, less where cancellation bites: iterate
         r = eng.berta_run(dt, maxtime, E, seed=7)
         n_end = int(r["nparticles"][-1])
-        if n_end >= 10_000:
-            E = E * n_end / target
+        if n_end < 10_000:
+            E = E / 100.0
+            continue
+        if abs(n_end / target - 1.0) < 0.15:
             break
-        E = E / 100.0
+        E = E * (n_end / target) ** 1.5
     for w in range(args.warmup):
         eng.berta_run(dt, maxtime, E, seed=100 + w)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -285,11 +289,320 @@ def run_berta(args, rank, world, local):
     return 0
 
 
+class SweepStats:
+    """Batch means of kappa_eff per case: replicas are independent runs."""
+
+    def __init__(self, n):
+        self.k = [[] for _ in range(n)]
+
+    def add(self, i, kappa):
+        self.k[i].append(kappa)
+
+    def rel3(self, i):
+        v = np.asarray(self.k[i])
+        if len(v) < 4:
+            return float("inf")
+        return 3.0 * v.std(ddof=1) / np.sqrt(len(v)) / abs(v.mean())
+
+    def mean(self, i):
+        return float(np.mean(self.k[i])) if self.k[i] else float("nan")
+
+
+def run_sweep(args, rank, world, local):
+    """The batched sweep: 64 ribbons (16 widths 20 nm - 2 um x 4 temperatures,
+    1 um long, p = 0, reservoirs at T +- 1 K) with budgets N_w = 1e5 100^(k/15).
+    Each arm repeats independent replicas until every case's kappa_eff has
+    3 sigma / kappa <= tol (batch means).  Plain: each case alone, one
+    context per temperature, replicas of N_w particles.  Batched: every
+    unconverged case in one grid-kernel launch (union geometry, one material
+    per case, particle shares = budgets), converged cases dropped by a share
+    update.  Table construction is outside both clocks."""
+    import torch
+    import btegpu
+    import synth
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    L, ncells, dt, maxtime = 1000.0, 50, 10.0, 1000.0
+    cases = synth.sweep_cases()
+    temps = sorted({c["T"] for c in cases})
+    tabs = {T: synth.mode_table(32, 3, 3, T, config=0) for T in temps}
+    nc = len(cases)
+    budgets = np.array([c["budget"] for c in cases], dtype=np.int64)
+    tol, cap = args.sweep_tol, args.sweep_seconds
+    clocks = ClockSampler(local)
+    clocks.start()
+
+    # ---- batched
+    g = synth.sweep_union_geometry(cases, length=L, ncells=ncells)
+    eng = btegpu.Engine(local)
+    eng.load_modes(tabs[300.0])
+    eng.load_geometry(g)
+    rates = [tabs[c["T"]]["w"] for c in cases]
+    Ts = [c["T"] for c in cases]
+    eng.load_materials(rates, Ts, budgets / budgets.sum())
+    eng.rta_run(300.0, dt, maxtime, 100000, seed=1)          # builds the tables
+    per = ncells + 2
+    sb = SweepStats(nc)
+    active = np.ones(nc, dtype=bool)
+    ev_b = 0
+    reps_b = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    while active.any() and time.perf_counter() - t0 < cap:
+        share = np.where(active, budgets, 0).astype(float)
+        eng.load_materials(rates, Ts, share / share.sum())
+        N = int(budgets[active].sum())
+        r = eng.rta_run(300.0, dt, maxtime, N, seed=1000 + reps_b, raw=False)
+        ev_b += int(r["events"])
+        reps_b += 1
+        for i in np.flatnonzero(active):
+            sb.add(i, synth.sweep_kappa(r["jx"], slice(per * i, per * i + ncells), length=L))
+            if sb.rel3(i) <= tol:
+                active[i] = False
+    t_b = time.perf_counter() - t0
+    conv_b = int((~active).sum())
+    eng.close()
+
+    # ---- plain
+    engs = {}
+    for T in temps:
+        e = btegpu.Engine(local)
+        e.load_modes(tabs[T])
+        engs[T] = e
+    sp = SweepStats(nc)
+    t_p = 0.0
+    ev_p = 0
+    reps_p = 0
+    conv_p = 0
+    for i, cs in enumerate(cases):
+        e = engs[cs["T"]]
+        e.load_geometry(synth.sweep_ribbon(cs["width"], cs["T"], length=L, ncells=ncells))
+        e.rta_run(cs["T"], dt, maxtime, 1000, seed=2)         # tables for this geometry
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        k = 0
+        while t_p + (time.perf_counter() - t1) < cap:
+            r = e.rta_run(cs["T"], dt, maxtime, int(cs["budget"]), seed=5000 + k, raw=False)
+            ev_p += int(r["events"])
+            k += 1
+            sp.add(i, synth.sweep_kappa(r["jx"], slice(0, ncells), length=L))
+            if sp.rel3(i) <= tol:
+                conv_p += 1
+                break
+        t_p += time.perf_counter() - t1
+        reps_p += k
+        if t_p >= cap:
+            break
+    for e in engs.values():
+        e.close()
+
+    # ---- plain, one fresh context per case (tables built per case, as one
+    # process per case would)
+    sf = SweepStats(nc)
+    t2 = time.perf_counter()
+    conv_f = 0
+    for i, cs in enumerate(cases):
+        if time.perf_counter() - t2 >= cap:
+            break
+        e = btegpu.Engine(local)
+        e.load_modes(tabs[cs["T"]])
+        e.load_geometry(synth.sweep_ribbon(cs["width"], cs["T"], length=L, ncells=ncells))
+        k = 0
+        while time.perf_counter() - t2 < cap:
+            r = e.rta_run(cs["T"], dt, maxtime, int(cs["budget"]), seed=5000 + k, raw=False)
+            k += 1
+            sf.add(i, synth.sweep_kappa(r["jx"], slice(0, ncells), length=L))
+            if sf.rel3(i) <= tol:
+                conv_f += 1
+                break
+        e.close()
+    t_f = time.perf_counter() - t2
+    # ---- batched with its table construction on the clock
+    t3 = time.perf_counter()
+    eng = btegpu.Engine(local)
+    eng.load_modes(tabs[300.0])
+    eng.load_geometry(g)
+    eng.load_materials(rates, Ts, budgets / budgets.sum())
+    eng.rta_run(300.0, dt, maxtime, 1000, seed=1)
+    t_setup_b = time.perf_counter() - t3
+    eng.close()
+    clk = clocks.stop()
+    worst_b = max(sb.rel3(i) for i in range(nc))
+    line = {
+        "metric": "seconds to 1% kappa_eff (3 sigma) over the 64-case sweep, batched",
+        "value": t_b, "unit": "s", "n_gpus": 1, "steps": reps_b, "warmup": 1,
+        "ms_per_step": 1e3 * t_b / max(reps_b, 1), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mode tables, no database)",
+        "config": {"workload": "64-case ribbon sweep: 16 widths 20nm-2um x T in {100,200,300,500} K, "
+                               "1 um long, p=0, 32x32x6 modes with tau at T, reservoirs T+-1 K, "
+                               "budgets 1e5*100^(k/15), 100 bins of 10 ps",
+                   "tol_3sigma": tol, "time_cap_s": cap, "parallelism": "replicas x1"},
+        "batched": {"seconds": t_b, "replicas": reps_b, "cases_converged": conv_b, "events": ev_b,
+                    "events_per_s": ev_b / max(t_b, 1e-9), "worst_3sigma_rel": worst_b},
+        "plain": {"seconds": t_p, "launches": reps_p, "cases_converged": conv_p, "events": ev_p,
+                  "events_per_s": ev_p / max(t_p, 1e-9)},
+        "speedup_plain_over_batched": (t_p / t_b) if (conv_b == nc and conv_p == nc) else None,
+        "with_table_setup": {"batched_seconds": t_b + t_setup_b, "batched_setup_s": t_setup_b,
+                             "plain_fresh_contexts_seconds": t_f, "plain_fresh_cases_converged": conv_f,
+                             "speedup": (t_f / (t_b + t_setup_b)) if (conv_b == nc and conv_f == nc)
+                             else None},
+        "kappa_eff_W_mK": {f"{c['T']:.0f}K_{c['width']:.0f}nm": round(sb.mean(i), 4)
+                           for i, c in enumerate(cases)},
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def kappa_weights(c, Eeff):
+    """Weights W[box][bin][q] of kappa_eff = J_x L / dT as a linear functional
+    of the raw tallies: the mean over the interior cells and the last 10
+    bins of the cumulative flux (/ V_box, x Eeff x 1e30)."""
+    nb = int(math.floor(c["maxtime"] / c["dt"] + 1e-6))
+    nbx = int(c["geom"]["nboxes"])
+    ncell = nbx - 2
+    last = 10
+    cnt = np.array([(nb - b) if b >= nb - last else last for b in range(nb)], float) / last
+    verts = np.asarray(c["geom"]["vertices"]).reshape(-1, 4, 2)
+    W = np.zeros((nbx, nb, 3))
+    L = float(verts[:ncell, :, 0].max() - verts[:ncell, :, 0].min())
+    for b in range(ncell):
+        xs, ys = verts[b, :, 0], verts[b, :, 1]
+        vbox = (xs.max() - xs.min()) * (ys.max() - ys.min()) * c["geom"]["thickness"]
+        W[b, :, 1] = cnt * Eeff * 1e30 / vbox / ncell * L * 1e-9 / 2.0
+    return W
+
+
+def run_adjoint(args, rank, world, local):
+    """Gradient of kappa_eff of the plain ribbon at p = 0.2 (6144 modes,
+    N = 1e7) with respect to 32 seeded mode lifetimes and p, to 1% (3 sigma,
+    L2 over the 33 components): the adjoint against central differences
+    with common random numbers (dtau/tau = 1e-3, dp = 1e-3).  Differences in
+    production mode follow the spec; alias tables decouple the two runs, so
+    differences in replay mode (CDF draws, coupled) are timed as well.  Each
+    arm is capped in time and reports the accuracy it reached."""
+    import torch
+    import btegpu
+    import synth
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    c = synth.config0(n_particles=10_000_000)
+    p0 = 0.2
+    m = c["modes"]
+    N = c["N"]
+    eng = btegpu.Engine(local)
+    eng.load_modes(m)
+    eng.load_geometry(c["geom"])
+    r = eng.rta_run(c["T0"], c["dt"], c["maxtime"], N, seed=1, specularity=p0, raw=False)
+    W = kappa_weights(c, r["Eeff"])
+    rng = np.random.default_rng(20261203)
+    movable = np.flatnonzero((m["w"] > 0) & (m["omega"] > 0))
+    modes = np.sort(rng.choice(movable, 32, replace=False))
+    tau = 1.0 / m["w"][modes]
+    cap = args.sweep_seconds
+    clocks = ClockSampler(local)
+    clocks.start()
+
+    def acc(rows):
+        a = np.asarray(rows)
+        if len(a) < 4:
+            return float("inf")
+        se = a.std(axis=0, ddof=1) / np.sqrt(len(a))
+        return 3.0 * float(np.linalg.norm(se) / np.linalg.norm(a.mean(axis=0)))
+
+    # adjoint arm
+    rows_a = []
+    t0 = time.perf_counter()
+    ev_a = 0
+    while acc(rows_a) > 0.01 and time.perf_counter() - t0 < cap:
+        g = eng.rta_adjoint(W, c["T0"], c["dt"], c["maxtime"], N, seed=100 + len(rows_a),
+                            specularity=p0)
+        rows_a.append(np.concatenate([g["dphi_dtau"][modes], [g["dphi_dp"]]]))
+        ev_a += 2 * int(g["events"])
+    t_a = time.perf_counter() - t0
+    ga = np.mean(rows_a, axis=0)
+
+    def fd_arm(mode, h):
+        rows = []
+        t1 = time.perf_counter()
+        runs = 0
+        while acc(rows) > 0.01 and time.perf_counter() - t1 < cap:
+            seed = 500 + len(rows)
+            row = []
+            for j, k in enumerate(modes):
+                v = []
+                for sgn in (1.0, -1.0):
+                    w = m["w"].copy()
+                    w[k] = 1.0 / (tau[j] * (1.0 + sgn * h))
+                    eng.load_materials([w], [c["T0"]])
+                    rr = eng.rta_run(c["T0"], c["dt"], c["maxtime"], N, seed=seed, mode=mode,
+                                     specularity=p0, raw=True)
+                    v.append(float(np.sum(W[..., 1] * rr["gz_jx"])))
+                    runs += 1
+                row.append((v[0] - v[1]) / (2.0 * h * tau[j]))
+            eng.load_materials([], [])
+            v = []
+            for sgn in (1.0, -1.0):
+                rr = eng.rta_run(c["T0"], c["dt"], c["maxtime"], N, seed=seed, mode=mode,
+                                 specularity=p0 + sgn * h, raw=True)
+                v.append(float(np.sum(W[..., 1] * rr["gz_jx"])))
+                runs += 1
+            row.append((v[0] - v[1]) / (2.0 * h))
+            rows.append(row)
+        return rows, time.perf_counter() - t1, runs
+
+    rows_fp, t_fp, runs_fp = fd_arm(btegpu.MODE_PRODUCTION, 1e-3)
+    rows_fr, t_fr, runs_fr = fd_arm(btegpu.MODE_REPLAY, 1e-3)
+    clk = clocks.stop()
+
+    def agree(rows):
+        if len(rows) < 2 or len(rows_a) < 2:
+            return None
+        f = np.asarray(rows)
+        se = np.sqrt(f.var(axis=0, ddof=1) / len(f) + np.var(rows_a, axis=0, ddof=1) / len(rows_a))
+        return float(np.max(np.abs(f.mean(axis=0) - ga) / np.maximum(se, 1e-300)))
+
+    line = {
+        "metric": "seconds to a 1% (3 sigma) gradient of kappa_eff, adjoint",
+        "value": t_a, "unit": "s", "n_gpus": 1, "steps": len(rows_a), "warmup": 1,
+        "ms_per_step": 1e3 * t_a / max(len(rows_a), 1), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mode table, no database)",
+        "config": {"workload": "plain ribbon at p=0.2: 32x32x6 modes, 1um x 100nm, 50 cells, 301/299K, "
+                               "100 bins of 10 ps, N=1e7; dkappa/dtau on 32 seeded modes + dkappa/dp",
+                   "accuracy": "3 * ||SE||_2 / ||g||_2 <= 1% over the 33 components",
+                   "time_cap_s": cap},
+        "adjoint": {"seconds": t_a, "replicas": len(rows_a), "accuracy": acc(rows_a),
+                    "events": ev_a, "dkappa_dp": float(ga[-1])},
+        "fd_production": {"seconds": t_fp, "replicas": len(rows_fp), "runs": runs_fp,
+                          "accuracy": acc(rows_fp), "max_z_vs_adjoint": agree(rows_fp)},
+        "fd_replay": {"seconds": t_fr, "replicas": len(rows_fr), "runs": runs_fr,
+                      "accuracy": acc(rows_fr), "max_z_vs_adjoint": agree(rows_fr)},
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    eng.close()
+    return 0
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "c4":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the gradient line compares the "
+                              "adjoint with differences of this engine"}))
+            return 0
+        return run_adjoint(args, rank, world, local)
+    if args.workload == "c3":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the sweep line compares two arms "
+                              "of this engine; the CPU restatement is a parity checker only"}))
+            return 0
+        return run_sweep(args, rank, world, local)
     if args.workload == "c2":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the beRTA workload line has no "

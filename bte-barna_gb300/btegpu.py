@@ -28,7 +28,7 @@ SOURCE_WALLS, SOURCE_INITIAL = 0, 1
 PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
                   "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run",
-                  "bte_steady_run", "bte_load_materials"]
+                  "bte_steady_run", "bte_load_materials", "bte_rta_adjoint"]
 
 
 class BteError(RuntimeError):
@@ -92,6 +92,11 @@ class BertaResult(C.Structure):
                 ("flux", C.POINTER(C.c_double)), ("nparticles", C.POINTER(C.c_int64)),
                 ("histogram", C.POINTER(C.c_int32)), ("particle_steps", C.c_int64),
                 ("branchings", C.c_int64), ("kernel_ms", C.c_double)]
+
+
+class AdjointResult(C.Structure):
+    _fields_ = [("phi", C.c_double), ("dphi_dtau", C.POINTER(C.c_double)), ("dphi_dp", C.c_double),
+                ("events", C.c_int64), ("kernel_ms", C.c_double)]
 
 
 class SteadyParams(C.Structure):
@@ -245,6 +250,9 @@ def load_library(path: str = LIB_PATH):
     lib.bte_load_materials.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]
     lib.bte_load_materials.restype = C.c_int
+    lib.bte_rta_adjoint.argtypes = [vp, C.POINTER(RtaParams), C.POINTER(C.c_double),
+                                    C.POINTER(AdjointResult)]
+    lib.bte_rta_adjoint.restype = C.c_int
     lib.bte_steady_run.argtypes = [vp, C.POINTER(SteadyParams), C.POINTER(SteadyResult)]
     lib.bte_steady_run.restype = C.c_int
     lib.bte_rta_run_noalloc.argtypes = [vp, C.POINTER(RtaParams), C.c_void_p, C.POINTER(RtaResult)]
@@ -388,6 +396,23 @@ def _engine_load_materials(self, w_list, T0_list, share=None):
                                             None if S is None else _dptr(S)))
 
 
+def _engine_rta_adjoint(self, weights, T0, dt, maxtime, N, seed=1, source=SOURCE_WALLS,
+                       specularity=0.0, ballistic=False, begin=0, end=0):
+    """dPhi/dtau per mode and dPhi/dp of Phi = sum(weights * raw tallies),
+    weights shaped [nboxes, nbins, 3] (gz, gz_jx, gz_jy)."""
+    p = params_struct(T0, dt, maxtime, N, seed, MODE_PRODUCTION, source, ballistic, specularity,
+                      begin, end)
+    W = np.ascontiguousarray(weights, dtype=np.float64)
+    n = int(self._keep["modes"]["omega"].size)
+    g = np.zeros(n)
+    r = AdjointResult()
+    r.dphi_dtau = _dptr(g)
+    self._check(self.lib.bte_rta_adjoint(self.ctx, C.byref(p), _dptr(W), C.byref(r)))
+    return {"phi": r.phi, "dphi_dtau": g, "dphi_dp": r.dphi_dp, "events": r.events,
+            "kernel_ms": r.kernel_ms}
+
+
+Engine.rta_adjoint = _engine_rta_adjoint
 Engine.load_materials = _engine_load_materials
 Engine.steady_run = _engine_steady_run
 Engine.load_propagator = _engine_load_propagator

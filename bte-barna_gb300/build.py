@@ -28,6 +28,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("berta.cu", []),
     ("steady.cu", []),
+    ("adjoint.cu", []),
 ]
 
 

@@ -240,6 +240,39 @@ void validate(const bte_rta_params* p) {
 
 }  // namespace
 
+namespace bte {
+// Validation and tables of one RTA run (shared by bte_rta_run and
+// bte_rta_adjoint).
+void prepare_run(bte_ctx* c, const bte_rta_params* p) {
+    validate(p);
+    if (!c->have_modes || !c->have_geom)
+        throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
+    ck(cudaSetDevice(c->device), "cudaSetDevice");
+    for (std::size_t b = 0; b < c->geom.boxes.size(); ++b) {
+        if (c->geom.mat[b] >= std::max(c->nmat, 1))
+            throw Error(BTE_ERR_INPUT, "box material without loaded rates (bte_load_materials)");
+        const double T0b = bte::box_T0(c, int(b), p->T0);
+        if (c->nmat > 0) {  // a particle keeps its material: materials must not touch
+            const bte::GBox& B = c->geom.boxes[b];
+            for (int i = 0; i < B.ncontacts; ++i) {
+                const int o = c->geom.contacts[std::size_t(B.contact_off + i)].id;
+                if (c->geom.mat[std::size_t(o)] != c->geom.mat[b])
+                    throw Error(BTE_ERR_INPUT, "boxes of different materials touch");
+            }
+            if (c->geom.tto[b] >= 0 && c->geom.mat[std::size_t(c->geom.tto[b])] != c->geom.mat[b])
+                throw Error(BTE_ERR_INPUT, "a periodic box maps to another material");
+        }
+        if (!c->geom.reservoir[b] && !bte::almost_equal(c->geom.Teq[b], T0b) && c->geom.Teq[b] != T0b)
+            throw Error(BTE_ERR_INPUT, "Tref in xml is different from provided T0");
+    }
+    ensure_static(c);
+    if (p->specularity > 0. && !c->have_mirror)
+        throw Error(BTE_ERR_INPUT, "specular walls need an axis-aligned q grid with mirror images");
+    ensure_resample(c, p->T0);
+    ensure_generators(c, p);
+}
+}  // namespace bte
+
 extern "C" {
 
 int32_t bte_version(void) { return BTEGPU_VERSION; }
@@ -406,32 +439,7 @@ bte_status bte_query_sizes(const bte_ctx* c, const bte_rta_params* p, int32_t* n
 bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out) {
     if (!c || !out) return BTE_ERR_INPUT;
     try {
-        validate(p);
-        if (!c->have_modes || !c->have_geom)
-            throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
-        ck(cudaSetDevice(c->device), "cudaSetDevice");
-        for (std::size_t b = 0; b < c->geom.boxes.size(); ++b) {
-            if (c->geom.mat[b] >= std::max(c->nmat, 1))
-                throw Error(BTE_ERR_INPUT, "box material without loaded rates (bte_load_materials)");
-            const double T0b = bte::box_T0(c, int(b), p->T0);
-            if (c->nmat > 0) {  // a particle keeps its material: materials must not touch
-                const bte::GBox& B = c->geom.boxes[b];
-                for (int i = 0; i < B.ncontacts; ++i) {
-                    const int o = c->geom.contacts[std::size_t(B.contact_off + i)].id;
-                    if (c->geom.mat[std::size_t(o)] != c->geom.mat[b])
-                        throw Error(BTE_ERR_INPUT, "boxes of different materials touch");
-                }
-                if (c->geom.tto[b] >= 0 && c->geom.mat[std::size_t(c->geom.tto[b])] != c->geom.mat[b])
-                    throw Error(BTE_ERR_INPUT, "a periodic box maps to another material");
-            }
-            if (!c->geom.reservoir[b] && !bte::almost_equal(c->geom.Teq[b], T0b) && c->geom.Teq[b] != T0b)
-                throw Error(BTE_ERR_INPUT, "Tref in xml is different from provided T0");
-        }
-        ensure_static(c);
-        if (p->specularity > 0. && !c->have_mirror)
-            throw Error(BTE_ERR_INPUT, "specular walls need an axis-aligned q grid with mirror images");
-        ensure_resample(c, p->T0);
-        ensure_generators(c, p);
+        bte::prepare_run(c, p);
         const bte::HostModes& m = c->modes;
         const bte::HostGeometry& g = c->geom;
         // time grid, src/RTA_MC2D.cpp:2118-2124

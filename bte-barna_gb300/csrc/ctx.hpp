@@ -112,6 +112,11 @@ void destroy_berta(bte_ctx* c);
 void destroy_steady(bte_ctx* c);
 // T0 of box b's material (the run's T0 without materials).
 double box_T0(const bte_ctx* c, int b, double T0);
+// Validation and tables of one RTA run (capi.cu).
+void prepare_run(bte_ctx* c, const bte_rta_params* p);
+// Kernel arguments of a prepared grid-path run (capi.cu); BTE_OK or a code
+// with the reason in *why.
+bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r, std::string* why);
 // Mode, geometry and Lambert tables of a context into the kernel tables.
 void fill_static_tables(bte_ctx* c, DevTables& T);
 }  // namespace bte

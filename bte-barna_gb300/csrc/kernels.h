@@ -54,11 +54,24 @@ struct GridArgs {
     int cls[4];              // normal classes of the +x, -x, +y, -y walls (-1: none)
 };
 
+// Adjoint passes of the grid kernel: the functional's weights per tally
+// value, each particle's total contribution (slot = particle - first),
+// per-mode gradient accumulators and {d/dp, sum of R over post-scattering
+// draws, sum of Phi}.
+struct AdjArgs {
+    const double* W;      // [nboxes * nbins][3]
+    double* phi_total;    // [particles]
+    double* g_tau;        // [nmodes]
+    double* g_scalar;     // [3]
+};
+
 // Axis-aligned grid production kernel (persistent, warp-refilled work).
+// adj_pass 1 / 2 runs the forward / adjoint pass of the adjoint with `adj`.
 // Returns false when the tuning cannot be honoured (e.g. smem too small).
 bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
                       unsigned long long* counters, int* err, unsigned long long* work,
-                      const ProdTuning& tune, int nsm, cudaStream_t s);
+                      const ProdTuning& tune, int nsm, cudaStream_t s, int adj_pass = 0,
+                      const AdjArgs* adj = nullptr);
 
 // Kernel arguments of a context already prepared for one set of run
 // parameters (see prepared_grid_run in capi.cu).

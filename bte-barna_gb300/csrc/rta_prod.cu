@@ -301,10 +301,21 @@ __device__ int grid_generate(const DevTables& T, const DevGrid& G, const int2* b
 // Idle lanes take new particles from a global counter, one atomic per warp.
 // Comparisons, min/max and the float -> double widening run on the integer
 // pipe.
-template <bool SMEM_TALLY, int MINB>
+//
+// ADJ selects the two passes of the adjoint (ADJ = 0 is the plain kernel):
+// 1 forward: also accumulates each particle's contribution to a linear
+//   functional Phi = sum W[box][bin][q] tally[box][bin][q] and stores it;
+// 2 adjoint: replays every particle from its Philox counter (the same draws
+//   as pass 1) and adds likelihood-ratio terms, each weighted by the
+//   particle's future contribution R = Phi_total - Phi so far:
+//   free flight of mode k, dt = tau_k e:  d log f / d tau_k = (e - 1) / tau_k
+//   post-scattering draw of mode k (p_k ~ C_k / tau_k): -1 / tau_k on tau_k,
+//     plus p_i / tau_i on every tau_i (summed once on the host from sum R)
+//   specularity draw at a void wall:       1 / p (specular) or -1 / (1 - p)
+template <bool SMEM_TALLY, int MINB, int ADJ>
 __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs A, double* gtally,
                                                      unsigned long long* counters, int* err,
-                                                     unsigned long long* work) {
+                                                     unsigned long long* work, AdjArgs adj) {
     extern __shared__ double stally[];
     const int nk3 = 3 * T.nboxes * T.nbins;
     double* tally = gtally;
@@ -333,6 +344,11 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     int bin = 0;
     unsigned long long signbit = 0;
     bool active = false, done = false, need_flight = false;
+    // adjoint state: Phi so far, the particle's total, pending score terms
+    double phi_run = 0., phi_tot = 0., spec_score = 0.;
+    double sum_r = 0., g_p = 0., phi_all = 0.;
+    long long slot = 0;
+    int pend_kind = 0;
     for (;;) {
         // refill idle lanes of the warp with new particles
         const unsigned idle = __ballot_sync(0xffffffffu, !active && !done);
@@ -354,6 +370,12 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                         active = true;
                         need_flight = true;
                         nev = 0;
+                        if (ADJ) {
+                            slot = mine;
+                            phi_run = 0.;
+                            pend_kind = 0;
+                            if (ADJ == 2) phi_tot = adj.phi_total[mine];
+                        }
                         bin = 0;
                         tnb = __ldg(T.timegrid + 1);
                         signbit = p.sign < 0 ? 0x8000000000000000ull : 0ull;
@@ -370,8 +392,25 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             // a new free flight: u in (0, 1) -> dt = -tau ln u (FP32 log)
             const int k = p.mode;
             mv = A.mv[k];
-            dt = widen_pos(-logf(g.uniformf())) * __ldg(T.tau + p.mo + k);
+            const float ef = -logf(g.uniformf());
+            const double tau_k = __ldg(T.tau + p.mo + k);
+            dt = widen_pos(ef) * tau_k;
             c.events++;
+            if (ADJ == 2) {
+                // future contribution from here: Phi_total - (flushed + pending part)
+                const double* Wk = adj.W + 3ll * pd.key;
+                const double part = __ldg(Wk) * (p.t - pd.t0) + __ldg(Wk + 1) * (p.x - pd.x0) +
+                                    __ldg(Wk + 2) * (p.y - pd.y0);
+                const double R = phi_tot - (phi_run + (p.sign < 0 ? -part : part));
+                double gk = (widen_pos(ef) - 1.0) / tau_k * R;
+                if (pend_kind & 1) {  // this mode came from a post-scattering draw
+                    gk -= R / tau_k;
+                    sum_r += R;
+                }
+                if (pend_kind & 2) g_p += spec_score * R;
+                pend_kind = 0;
+                atomicAdd(adj.g_tau + k, gk);
+            }
             if (ob(dt) <= 0 || ++nev > EVENT_CAP) {  // zero rate or runaway particle
                 record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
                 active = false;
@@ -432,6 +471,11 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         const bool absorbed = wall && nb <= -2;   // into a reservoir
         const bool reflect = wall && nb == -1;    // void: reflection, a new flight follows
         const bool last = bin_end && bin == last_bin;
+        if (ADJ && (move || absorbed || bin_end)) {
+            const double* Wk = adj.W + 3ll * pd.key;
+            const double cphi = __ldg(Wk) * d0 + __ldg(Wk + 1) * d1 + __ldg(Wk + 2) * d2;
+            phi_run += p.sign < 0 ? -cphi : cphi;
+        }
         if (move || absorbed || bin_end) {
             double* b = tally + 3ll * pd.key;
             atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(d0) ^ signbit));
@@ -443,6 +487,10 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         if (absorbed || last) {
             if (absorbed) c.absorbed++;
             active = false;
+            if (ADJ == 1) {
+                adj.phi_total[slot] = phi_run;
+                phi_all += phi_run;
+            }
             continue;
         }
         if (bin_end) {
@@ -468,7 +516,15 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             }
             const int k = p.mode;
             int nm = -1;
-            if (T.specularity > 0. && g.uniform() < T.specularity && T.mirror) {
+            bool spec = false;
+            if (T.specularity > 0.) {
+                spec = g.uniform() < T.specularity;
+                if (ADJ == 2) {
+                    spec_score = spec ? 1.0 / T.specularity : -1.0 / (1.0 - T.specularity);
+                    pend_kind |= 2;
+                }
+            }
+            if (spec && T.mirror) {
                 nm = __ldg(T.mirror + (long long)cls * T.n + k);
                 if (nm >= 0) c.specular++;
             }
@@ -492,9 +548,23 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             c.wall_hits++;
             need_flight = true;
         } else if (flight_end) {
-            if (!T.ballistic)
+            if (!T.ballistic) {
                 p.mode = alias_draw(g, T.resample_prob + p.mo, T.resample_alt + p.mo, T.n);
+                if (ADJ == 2) pend_kind |= 1;
+            }
             need_flight = true;
+        }
+    }
+    if (ADJ) {
+        for (int o = 16; o > 0; o >>= 1) {
+            sum_r += __shfl_down_sync(0xffffffffu, sum_r, o);
+            g_p += __shfl_down_sync(0xffffffffu, g_p, o);
+            phi_all += __shfl_down_sync(0xffffffffu, phi_all, o);
+        }
+        if (lane == 0) {
+            atomicAdd(adj.g_scalar + 0, g_p);
+            atomicAdd(adj.g_scalar + 1, sum_r);
+            atomicAdd(adj.g_scalar + 2, phi_all);
         }
     }
     c.tallies = pd.flushes;
@@ -510,26 +580,34 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
 
 bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
                       unsigned long long* counters, int* err, unsigned long long* work,
-                      const ProdTuning& tune, int nsm, cudaStream_t s) {
+                      const ProdTuning& tune, int nsm, cudaStream_t s, int adj_pass,
+                      const AdjArgs* adj) {
     const long long n = T.pend - T.pbegin;
     if (n <= 0) return true;
     const int threads = tune.block_threads > 0 ? tune.block_threads : 256;
     if (threads > 256 || threads % 32) return false;
     const size_t smem = size_t(3) * T.nboxes * T.nbins * sizeof(double);
-    const bool use_smem = tune.smem_tally != 0 && smem <= 200 * 1024;
+    // the adjoint passes run with the tally in global memory
+    const bool use_smem = tune.smem_tally != 0 && smem <= 200 * 1024 && adj_pass == 0;
     // residency variants: 3 blocks of 256 threads per SM (80 registers) or
     // 2 (no register cap); the shared-memory tally allows one block per SM
     int bps = tune.blocks_per_sm > 0 ? tune.blocks_per_sm : (use_smem ? 1 : 3);
+    const AdjArgs none{};
+    const AdjArgs& aa = adj ? *adj : none;
     const void* fn;
     if (use_smem) {
-        fn = reinterpret_cast<const void*>(rta_prod_grid<true, 1>);
-        if (cudaFuncSetAttribute(rta_prod_grid<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        fn = reinterpret_cast<const void*>(rta_prod_grid<true, 1, 0>);
+        if (cudaFuncSetAttribute(rta_prod_grid<true, 1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(smem)) != cudaSuccess)
             return false;
+    } else if (adj_pass == 1) {
+        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 1>);
+    } else if (adj_pass == 2) {
+        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 2>);
     } else if (bps >= 3) {
-        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 3>);
+        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 3, 0>);
     } else {
-        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2>);
+        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 0>);
     }
     int maxb = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, fn, threads, use_smem ? smem : 0);
@@ -539,12 +617,17 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
     const long long need = (n + threads - 1) / threads;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
+    const unsigned nb = unsigned(blocks);
     if (use_smem)
-        rta_prod_grid<true, 1><<<unsigned(blocks), threads, smem, s>>>(T, A, tally, counters, err, work);
-    else if (fn == reinterpret_cast<const void*>(rta_prod_grid<false, 3>))
-        rta_prod_grid<false, 3><<<unsigned(blocks), threads, 0, s>>>(T, A, tally, counters, err, work);
+        rta_prod_grid<true, 1, 0><<<nb, threads, smem, s>>>(T, A, tally, counters, err, work, aa);
+    else if (adj_pass == 1)
+        rta_prod_grid<false, 2, 1><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
+    else if (adj_pass == 2)
+        rta_prod_grid<false, 2, 2><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
+    else if (fn == reinterpret_cast<const void*>(rta_prod_grid<false, 3, 0>))
+        rta_prod_grid<false, 3, 0><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
     else
-        rta_prod_grid<false, 2><<<unsigned(blocks), threads, 0, s>>>(T, A, tally, counters, err, work);
+        rta_prod_grid<false, 2, 0><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
     return true;
 }
 

@@ -329,6 +329,27 @@ bte_status bte_berta_run(bte_ctx* ctx, const bte_berta_params* params,
 bte_status bte_steady_run(bte_ctx* ctx, const bte_steady_params* params,
                           bte_steady_result* out);
 
+/* Gradient of a linear functional of the tallies of a production run,
+ *   Phi = sum_{box, bin} W[box][bin][0] gz + W[..][1] gz_jx + W[..][2] gz_jy
+ * (raw tallies as in bte_rta_result; kappa_eff and any time- or
+ * box-averaged flux or temperature are such functionals), with respect to
+ * every mode's lifetime tau and the wall specularity p.  Likelihood-ratio
+ * weights of the free-flight, post-scattering and specularity draws; the
+ * adjoint pass recomputes each trajectory from its Philox counter after a
+ * forward pass has stored each particle's contribution.  Boxes that tile
+ * an axis-aligned grid, one material.  No reference counterpart: the
+ * reference has no derivatives (its finite differences are the check). */
+typedef struct bte_adjoint_result {
+    double phi;              /* the functional from the same particles        */
+    double* dphi_dtau;       /* [nmodes] dPhi/dtau_k, per ps                   */
+    double dphi_dp;          /* dPhi/dp (meaningful for 0 < p < 1)            */
+    int64_t events;          /* flight events of one pass                      */
+    double kernel_ms;        /* device time of both passes                     */
+} bte_adjoint_result;
+
+bte_status bte_rta_adjoint(bte_ctx* ctx, const bte_rta_params* params, const double* weights,
+                           bte_adjoint_result* out);
+
 /* Largest number of time bins bte_rta_run_noalloc accepts. */
 #define BTE_NOALLOC_MAX_BINS 4096
 

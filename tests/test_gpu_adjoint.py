@@ -1,0 +1,115 @@
+"""GPU tests of bte_rta_adjoint: gradients of kappa_eff (a linear functional
+of the tallies) with respect to per-mode lifetimes and the wall specularity,
+against central finite differences with common random numbers, and the
+functional itself against the plain run's tallies.
+
+The differences run in replay mode: its draws invert CDFs, so the same
+stream stays coupled when a rate changes.  (Production mode samples alias
+tables, whose layout reshuffles when one weight moves, which decouples the
+two runs of a difference.)"""
+import numpy as np
+import pytest
+
+import btegpu
+import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(p=0.2):
+    return {"modes": synth.mode_table(8, 3, 3, 300.0, config=100),
+            "geom": synth.ribbon_geometry(200.0, 50.0, 5), "T0": 300.0, "dt": 10.0,
+            "maxtime": 300.0, "N": 40000, "specularity": p}
+
+
+def _kappa_weights(case):
+    """Phi = kappa_eff = J_x L / dT from the mean flux of the interior cells
+    over the last 10 bins of the step response: a linear functional of the
+    raw gz_jx tallies (cumulative sum, / V_box, x Eeff x 1e30)."""
+    nb = int(round(case["maxtime"] / case["dt"]))
+    ncell = case["geom"]["nboxes"] - 2
+    W = np.zeros((case["geom"]["nboxes"], nb, 3))
+    last = 10
+    # mean over bins b >= nb - last of cumsum up to b: bin b' counts
+    # (number of those b with b >= b') / last times
+    cnt = np.array([min(last, nb - bp) if bp >= nb - last else last for bp in range(nb)], float) / last
+    return W, cnt, ncell, nb
+
+
+def _phi_weights(e, case):
+    W, cnt, ncell, nb = _kappa_weights(case)
+    r = e.rta_run(case["T0"], case["dt"], case["maxtime"], 1000, seed=1,
+                  specularity=case["specularity"])
+    Eeff = r["Eeff"] * 1000.0 / case["N"]        # Eeff = |E| / N
+    vbox = 200.0 / 5 * 50.0 * case["geom"]["thickness"]
+    L, dT = 200.0, 2.0
+    scale = Eeff * 1e30 / vbox / ncell * L * 1e-9 / dT
+    W[:ncell, :, 1] = cnt[None, :] * scale
+    return W
+
+
+def _kappa_from(r, case):
+    ncell = case["geom"]["nboxes"] - 2
+    return float(np.mean(r["jx"][:ncell, -10:])) * 200.0 * 1e-9 / 2.0
+
+
+def test_adjoint_functional_matches_plain_tallies(engine):
+    case = _case()
+    engine.load_modes(case["modes"])
+    engine.load_geometry(case["geom"])
+    W = _phi_weights(engine, case)
+    a = engine.rta_adjoint(W, case["T0"], case["dt"], case["maxtime"], case["N"], seed=7,
+                           specularity=case["specularity"])
+    r = engine.rta_run(case["T0"], case["dt"], case["maxtime"], case["N"], seed=7,
+                       specularity=case["specularity"])
+    k = _kappa_from(r, case)
+    assert abs(a["phi"] - k) <= 1e-9 * abs(k), (a["phi"], k)
+
+
+def test_adjoint_agrees_with_common_random_number_differences(engine):
+    case = _case()
+    m = case["modes"]
+    engine.load_modes(m)
+    engine.load_geometry(case["geom"])
+    W = _phi_weights(engine, case)
+    R = 6
+    ga = np.array([engine.rta_adjoint(W, 300.0, case["dt"], case["maxtime"], case["N"], seed=100 + i,
+                                      specularity=0.2)["dphi_dtau"] for i in range(R)])
+    gp = np.array([engine.rta_adjoint(W, 300.0, case["dt"], case["maxtime"], case["N"], seed=100 + i,
+                                      specularity=0.2)["dphi_dp"] for i in range(R)])
+    # the modes that carry the most of the gradient
+    tau = np.where(m["w"] > 0, 1.0 / np.where(m["w"] > 0, m["w"], 1.0), 0.0)
+    top = np.argsort(-np.abs(ga.mean(0) * tau))[:4]
+    h = 0.05
+    for k in top:
+        fd = []
+        for i in range(R):
+            vals = []
+            for sgn in (1.0, -1.0):
+                mm = dict(m)
+                w = m["w"].copy()
+                w[k] = 1.0 / (tau[k] * (1.0 + sgn * h))
+                mm["w"] = w
+                engine.load_modes(mm)
+                engine.load_geometry(case["geom"])
+                r = engine.rta_run(300.0, case["dt"], case["maxtime"], case["N"], seed=100 + i,
+                                   specularity=0.2, mode=btegpu.MODE_REPLAY)
+                vals.append(_kappa_from(r, case))
+            fd.append((vals[0] - vals[1]) / (2.0 * h * tau[k]))
+        fd = np.array(fd)
+        d = ga[:, k].mean() - fd.mean()
+        se = np.sqrt(ga[:, k].var(ddof=1) / R + fd.var(ddof=1) / R)
+        assert abs(d) < 4.5 * se + 0.02 * abs(fd.mean()), (k, ga[:, k].mean(), fd.mean(), se)
+    engine.load_modes(m)
+    engine.load_geometry(case["geom"])
+    fdp = []
+    hp = 0.05
+    for i in range(R):
+        v = [_kappa_from(engine.rta_run(300.0, case["dt"], case["maxtime"], case["N"], seed=100 + i,
+                                        specularity=0.2 + s * hp, mode=btegpu.MODE_REPLAY), case)
+             for s in (1.0, -1.0)]
+        fdp.append((v[0] - v[1]) / (2 * hp))
+    fdp = np.array(fdp)
+    d = gp.mean() - fdp.mean()
+    se = np.sqrt(gp.var(ddof=1) / R + fdp.var(ddof=1) / R)
+    assert abs(d) < 4.5 * se + 0.02 * abs(fdp.mean()), (gp.mean(), fdp.mean(), se)
