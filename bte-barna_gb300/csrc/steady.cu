@@ -151,7 +151,11 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         for (std::size_t b = 0; b < g.boxes.size(); ++b)
             if (!g.reservoir[b] && !almost_equal(g.Teq[b], p->T0) && g.Teq[b] != p->T0)
                 throw Error(BTE_ERR_INPUT, "Tref in xml is different from provided T0");
+        if (!(p->specularity >= 0. && p->specularity <= 1.))
+            throw Error(BTE_ERR_INPUT, "specularity must be in [0, 1]");
         ensure_static(c);
+        if (p->specularity > 0. && !c->have_mirror)
+            throw Error(BTE_ERR_INPUT, "specular walls need an axis-aligned q grid with mirror images");
         ensure_resample(c, p->T0);
         if (!c->steady) c->steady = new SteadyState();
         SteadyState& S = *c->steady;
@@ -236,6 +240,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         T.gen_alt = S.galt.as<int>();
         T.seed = p->seed;
         T.nbins = 1;
+        T.specularity = p->specularity;
 
         SteadyArgs A{};
         A.exg0 = exg0;

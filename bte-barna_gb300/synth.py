@@ -228,10 +228,13 @@ def periodic_ribbon_geometry(length: float = 40.0, width: float = 100.0, nx: int
     return g
 
 
-def kappa_ribbon(modes: dict, T: float, width: float, thickness: float = C_LAT) -> float:
-    """Conductivity along an infinite ribbon with fully diffuse walls:
-    kappa_xx with each lifetime scaled as scale_tau_nanoribbon does
-    (src/nanos.cpp:77-112), tau (1 + (l / w)(exp(-w / l) - 1)), l = tau |v_y|."""
+def kappa_ribbon(modes: dict, T: float, width: float, thickness: float = C_LAT, p: float = 0.0) -> float:
+    """Conductivity along an infinite ribbon whose walls reflect specularly
+    with probability p: kappa_xx with each lifetime scaled by the in-plane
+    Fuchs-Sondheimer factor of the reference's analytic1d
+    (src/analytic1d.cpp:244-273), with K = l / w, l = tau |v_y|:
+      (1 - p e^{-1/K} - (1 - p) K (1 - e^{-1/K})) / (1 - p e^{-1/K});
+    for p = 0 this is scale_tau_nanoribbon (src/nanos.cpp:77-112)."""
     kB = 1.3806488e-23
     om, w = modes["omega"], modes["w"]
     v = modes["vg"].reshape(-1, 3)
@@ -239,8 +242,10 @@ def kappa_ribbon(modes: dict, T: float, width: float, thickness: float = C_LAT) 
     C = be_kernel(om[ok], T)
     tau = 1.0 / w[ok]
     mfp = np.abs(tau * v[ok, 1])
-    with np.errstate(divide="ignore", invalid="ignore"):
-        f = np.where(mfp > 1e-8, mfp / width * (np.exp(-width / np.maximum(mfp, 1e-300)) - 1.0) + 1.0, 1.0)
+    K = mfp / width
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        e = np.exp(-1.0 / np.maximum(K, 1e-300))
+        f = np.where(K > 1e-12, (1.0 - p * e - (1.0 - p) * K * (1.0 - e)) / (1.0 - p * e), 1.0)
     vuc = modes["V"] * thickness / modes["c_lat"]
     return float(1e21 * kB / (modes["nq"] * vuc) * np.sum(C * tau * f * v[ok, 0] ** 2))
 

@@ -211,6 +211,7 @@ typedef struct bte_steady_params {
     uint64_t seed;           /* master seed of all slot streams                 */
     int32_t mode;            /* BTE_MODE_*                                      */
     int32_t max_generations; /* safety cap of the generation loop (0: 100000)  */
+    double specularity;      /* p of void walls; 0 = the reference's diffuse    */
 } bte_steady_params;
 
 /* Results of a steady-state run: one value per box (the rows of

@@ -98,7 +98,7 @@ def translate(geom: dict, ibox: int, x: float, y: float, vx: float, vy: float, s
 
 
 def steady_run(case: dict, gradient, N=None, seed=1, nthreads=8, eps_energy=-42.0, eps_flux=-42.0,
-               max_generations=0):
+               max_generations=0, specularity=0.0):
     """Steady state of the restatement (replay draws) on a synth case dict."""
     lib = load()
     ms, k1 = _bt.mode_struct(case["modes"])
@@ -110,7 +110,8 @@ def steady_run(case: dict, gradient, N=None, seed=1, nthreads=8, eps_energy=-42.
         if st != 0:
             raise _bt.BteError(st, lib.oracle_last_error().decode())
     return _bt.steady_call(call, int(case["geom"]["nboxes"]), case["T0"], gradient, N, seed,
-                           _bt.MODE_REPLAY, eps_energy, eps_flux, max_generations)
+                           _bt.MODE_REPLAY, eps_energy, eps_flux, max_generations,
+                           specularity=specularity)
 
 
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,

@@ -1223,7 +1223,7 @@ enum Fate { F_LOST = 0, F_SCATTER = 1, F_BOUNCE = 2, F_ABSORBED = 3 };
 
 // evolparticle (periodic), src/RTA_MC2D.cpp:1406-1799, one material.
 inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng, Tally& T,
-                                Fate& fate) {
+                                Fate& fate, double specularity = 0.) {
     const std::size_t nb = S.m.nb;
     V2 opos = p.pos;
     const Box& box = S.sys[p.box];
@@ -1316,7 +1316,15 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
             iborder = std::size_t(mru.bids.at(0));
         }
         V2 u = cur.borders[iborder].np;
-        std::size_t nm = bounce(S, u, p.q * nb + p.alpha, rng);
+        const std::size_t k0 = p.q * nb + p.alpha;
+        long long nmm = -1;
+        if (specularity > 0.) {  // this engine's extension, as in the transient flight
+            if (canonical(rng) < specularity) {
+                nmm = mirror_mode(S, u, k0);
+                if (nmm >= 0) T.specular++;
+            }
+        }
+        std::size_t nm = nmm >= 0 ? std::size_t(nmm) : bounce(S, u, k0, rng);
         p.pos = rnew;
         p.q = nm / nb;
         p.alpha = nm % nb;
@@ -2218,7 +2226,7 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
                         int guard = 0;
                         while (!orc::almost_equal(dt, 0.)) {
                             if (++guard > 1000000) throw orc::limit_error("flight step cap");
-                            orc::evolparticle_steady(S, p, v, dt, rng, T, f);
+                            orc::evolparticle_steady(S, p, v, dt, rng, T, f, sp->specularity);
                         }
                         fate[std::size_t(sl)] = char(f);
                         if (f == orc::F_SCATTER) phi[p.box] += p.sign;

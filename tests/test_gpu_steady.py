@@ -73,6 +73,22 @@ def test_steady_production_bulk_kappa(engine):
     assert abs(ks.mean() - K) < 4.5 * se, (ks.mean(), se, K)
 
 
+def test_steady_specular_replay_bit_exact_and_production_kappa(engine):
+    """Specular fraction p = 0.5: replay matches the restatement bit for bit;
+    production gives the analytic1d in-plane film conductivity."""
+    case = {"modes": synth.mode_table(9, 3, 3, 300.0, config=100, even=True),
+            "geom": synth.periodic_ribbon_geometry(40.0, 100.0, 2, 2), "T0": 300.0, "N": 3000}
+    _load(engine, case)
+    g = engine.steady_run(300.0, (-0.01, 0.0), 3000, seed=8, mode=btegpu.MODE_REPLAY, specularity=0.5)
+    o = pyoracle.steady_run(case, (-0.01, 0.0), N=3000, seed=8, specularity=0.5)
+    assert np.array_equal(g["exact"], o["exact"]) and np.array_equal(g["log"], o["log"])
+    K = synth.kappa_ribbon(case["modes"], 300.0, 100.0, p=0.5)
+    ks = np.array([-engine.steady_run(300.0, (-0.01, 0.0), 200000, seed=140 + i, specularity=0.5)["jx"][:4].mean()
+                   / (-0.01e9) for i in range(6)])
+    se = ks.std(ddof=1) / np.sqrt(len(ks))
+    assert abs(ks.mean() - K) < 4.5 * se, (ks.mean(), se, K)
+
+
 @pytest.mark.parametrize("width", [50.0, 500.0])
 def test_steady_production_ribbon_kappa(engine, width):
     """Diffuse-wall nanoribbon (scale_tau_nanoribbon, src/nanos.cpp:77-112)."""

@@ -85,6 +85,21 @@ def test_steady_ribbon_gives_diffuse_wall_kappa(width):
     assert K < synth.kappa_rta(case["modes"], 300.0)[0, 0]
 
 
+@pytest.mark.parametrize("p", [0.5, 0.9])
+def test_steady_specular_ribbon_gives_fuchs_sondheimer_kappa(p):
+    """Walls that reflect specularly with probability p: kappa_xx equals the
+    in-plane film conductivity of the reference's analytic1d
+    (src/analytic1d.cpp:244-273) on the same modes."""
+    case = {"modes": _even_modes(), "geom": synth.periodic_ribbon_geometry(40.0, 100.0, 2, 2),
+            "T0": 300.0, "N": 20000}
+    K = synth.kappa_ribbon(case["modes"], 300.0, 100.0, p=p)
+    ks = np.array([-pyoracle.steady_run(case, (-0.01, 0.0), seed=20 + s, specularity=p)["jx"][:4].mean()
+                   / (-0.01e9) for s in range(8)])
+    se = ks.std(ddof=1) / np.sqrt(len(ks))
+    assert abs(ks.mean() - K) < 4.0 * se, (ks.mean(), se, K)
+    assert K > synth.kappa_ribbon(case["modes"], 300.0, 100.0, p=0.0)
+
+
 def test_steady_needs_a_gradient():
     case = synth.periodic_case(n_particles=10)
     with pytest.raises(Exception):
