@@ -45,9 +45,16 @@ struct PArr {
 // `alias_off` of the step's alias buffer) and its particles [first, first+n).
 struct GenDesc {
     double x0, y0, dx, dy;  // border: p1 + u (dx, dy); rectangle: x0 + u dx, y0 + v dy
-    int box, sign, rect, pad;
+    int box, sign, rect;
+    int cdf;                // >= 0: mode from device CDF row `cdf`; -1: alias row at alias_off
     long long alias_off;
     long long first;
+};
+
+// One adiabatic re-emission distribution to build on the device: an
+// isothermal wall at Tw facing a box at Te, inward normal (nx, ny).
+struct WallReq {
+    double nx, ny, Tw, Te;
 };
 
 // Propagator alias entry: slot j keeps outgoing mode j+3 with probability
@@ -68,8 +75,10 @@ struct BertaState {
     DBuf b_x, b_y, b_mode, b_box, b_sign;   // compaction / scattering output
     DBuf q_x, q_y, q_mode, q_box, q_sign;   // branching queues (two halves)
     DBuf d_H, d_cnt, d_Eb, d_props, d_counts, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
+    DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     std::vector<Spline1D> spl;
     std::vector<char> spl_ok;
+    long long spl_version = -1;   // tables the splines were built for
 };
 
 void destroy_berta(bte_ctx* c) {
@@ -170,9 +179,50 @@ __global__ void be_advect(PArr P, long long begin, long long end, AdvectArgs a) 
     }
 }
 
+// Isothermal_wall_distribution (src/sampling.cpp:189-269) of each request,
+// one block per request: pmf_k = v_n omega_k |n(omega_k, Tw) - n(omega_k, Te)|
+// for v_n > 0, turned into a CDF row in place; tot[r] keeps the sum.
+__global__ void __launch_bounds__(256) be_wall_cdf(const double* om, const double* vx, const double* vy,
+                                                   int n, const WallReq* req, double* cdf, double* tot) {
+    __shared__ double part[256];
+    const WallReq R = req[blockIdx.x];
+    double* row = cdf + (long long)blockIdx.x * n;
+    const int seg = (n + blockDim.x - 1) / blockDim.x;
+    const int k0 = threadIdx.x * seg, k1 = min(n, k0 + seg);
+    constexpr double pre = 1e12 * 1.054571726e-34 / 1.3806488e-23;
+    double acc = 0.;
+    for (int k = k0; k < k1; ++k) {
+        const double w = om[k];
+        const double vn = R.nx * vx[k] + R.ny * vy[k];
+        double p = 0.;
+        if (vn > 0. && !almost_equal(0., w)) {
+            const double nw = 1. / (exp(pre * w / R.Tw) - 1.), ne = 1. / (exp(pre * w / R.Te) - 1.);
+            p = vn * w * fabs(nw - ne);
+        }
+        acc += p;
+        row[k] = acc;  // running sum within the thread's segment
+    }
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // exclusive offsets of the segments
+        double s = 0.;
+        for (int t = 0; t < blockDim.x; ++t) {
+            const double v = part[t];
+            part[t] = s;
+            s += v;
+        }
+        tot[blockIdx.x] = s;
+    }
+    __syncthreads();
+    const double off = part[threadIdx.x], total = tot[blockIdx.x];
+    if (total > 0.)
+        for (int k = k0; k < k1; ++k) row[k] = (row[k] + off) / total;
+}
+
 // New particles [base, base + n) from the step's sources.
 __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* gens, int ngen,
-                            const float* aprob, const int* aalt, int nmodes, unsigned long long key) {
+                            const float* aprob, const int* aalt, const double* cdfs, const double* cdftot,
+                            int nmodes, unsigned long long key) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = ngen;
@@ -192,11 +242,19 @@ __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* 
             x = gd.x0 + u * gd.dx;
             y = gd.y0 + u * gd.dy;
         }
-        const float* pr = aprob + gd.alias_off;
-        const int* al = aalt + gd.alias_off;
-        const int j = int(mulhi32(g.next32(), uint32_t(nmodes)));
-        const float acc = float(g.next32() >> 8) * 0x1p-24f;
-        const int mode = acc < __ldg(pr + j) ? j : __ldg(al + j);
+        int mode;
+        if (gd.cdf >= 0) {
+            // lower_bound over the border's CDF row (Grid_distribution::sample)
+            const double* row = cdfs + (long long)gd.cdf * nmodes;
+            mode = cdftot[gd.cdf] > 0. ? lower_bound_d(row, nmodes, g.uniform()) : -1;
+            if (mode >= nmodes) mode = nmodes - 1;
+        } else {
+            const float* pr = aprob + gd.alias_off;
+            const int* al = aalt + gd.alias_off;
+            const int j = int(mulhi32(g.next32(), uint32_t(nmodes)));
+            const float acc = float(g.next32() >> 8) * 0x1p-24f;
+            mode = acc < __ldg(pr + j) ? j : __ldg(al + j);
+        }
         const long long i = base + k;
         P.x[i] = x;
         P.y[i] = y;
@@ -569,9 +627,10 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         B.d_boxwall.upload(boxwall, s);
         B.d_Eb.alloc(std::size_t(nborders) * sizeof(int));
         ck(cudaMemsetAsync(B.d_Eb.p, 0, std::size_t(nborders) * sizeof(int), s), "memset");
-        if (int(B.spl.size()) != nborders) {
+        if (int(B.spl.size()) != nborders || B.spl_version != c->tables_version) {
             B.spl.assign(std::size_t(nborders), Spline1D());
             B.spl_ok.assign(std::size_t(nborders), 0);
+            B.spl_version = c->tables_version;
         }
         B.d_rvx.upload(m.vx, s);
         B.d_rvy.upload(m.vy, s);
@@ -626,34 +685,49 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         std::vector<float> aprob;
         std::vector<int> aalt;
         std::vector<GenDesc> descs;
+        std::vector<WallReq> reqs;
         // generate the sources in `descs` (alias rows in aprob/aalt) at A[base..)
-        auto generate = [&](long long base, long long total, long long step, int phase, bool advect) {
+        // the isothermal walls' alias rows do not change during a run
+        {
+            std::vector<float> ip(iso.alias.size());
+            std::vector<int> ia(iso.alias.size());
+            for (std::size_t i = 0; i < iso.alias.size(); ++i) {
+                ip[i] = iso.alias[i].prob;
+                ia[i] = iso.alias[i].alt;
+            }
+            B.d_isoprob.upload(ip, s);
+            B.d_isoalt.upload(ia, s);
+            B.d_om.upload(m.omega, s);
+            B.d_vx.upload(m.vx, s);
+            B.d_vy.upload(m.vy, s);
+        }
+        // generate the sources in `descs` at A[base..): alias rows from
+        // aprob/aalt (uploaded here) or from the isothermal walls' table
+        // (iso_rows), CDF rows from B.d_cdf
+        auto generate = [&](long long base, long long total, long long step, int phase, bool advect,
+                            bool iso_rows = false) {
             if (total <= 0) return;
             if (base + total > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded: raise capacity");
             B.d_gens.upload(descs, s);
-            B.d_alias.alloc(aprob.size() * sizeof(float) + aalt.size() * sizeof(int));
-            ck(cudaMemcpyAsync(B.d_alias.p, aprob.data(), aprob.size() * sizeof(float), cudaMemcpyHostToDevice, s), "h2d");
-            int* dalt = reinterpret_cast<int*>(B.d_alias.as<char>() + aprob.size() * sizeof(float));
-            ck(cudaMemcpyAsync(dalt, aalt.data(), aalt.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
+            const float* dprob = B.d_isoprob.as<float>();
+            const int* dalt = B.d_isoalt.as<int>();
+            if (!iso_rows && !aprob.empty()) {
+                B.d_alias.alloc(aprob.size() * sizeof(float) + aalt.size() * sizeof(int));
+                ck(cudaMemcpyAsync(B.d_alias.p, aprob.data(), aprob.size() * sizeof(float), cudaMemcpyHostToDevice, s), "h2d");
+                int* a2 = reinterpret_cast<int*>(B.d_alias.as<char>() + aprob.size() * sizeof(float));
+                ck(cudaMemcpyAsync(a2, aalt.data(), aalt.size() * sizeof(int), cudaMemcpyHostToDevice, s), "h2d");
+                dprob = B.d_alias.as<float>();
+                dalt = a2;
+            }
             PArr A = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
             be_generate<<<launch_blocks(total, c->nsm), 256, 0, s>>>(
-                A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), B.d_alias.as<float>(), dalt, n,
-                mix_key(p->seed, step, phase));
+                A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), dprob, dalt,
+                B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n, mix_key(p->seed, step, phase));
             if (advect) {
                 AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt,
                               mix_key(p->seed, step, phase + 1), 1};
                 be_advect<<<launch_blocks(total, c->nsm), 256, 0, s>>>(A, base, base + total, aa);
             }
-        };
-        auto add_alias_row = [&](const std::vector<double>& w) {
-            const long long off = (long long)aprob.size();
-            std::vector<Alias> al(static_cast<std::size_t>(n));
-            alias_table(w.data(), n, al.data());
-            for (auto& e : al) {
-                aprob.push_back(e.prob);
-                aalt.push_back(e.alt);
-            }
-            return off;
         };
         auto read_count = [&](int k) {
             unsigned long long v = 0;
@@ -719,6 +793,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 d.box = b;
                 d.sign = ini.init_sign[k];
                 d.rect = 1;
+                d.cdf = -1;
                 const long long off = (long long)aprob.size();
                 for (std::size_t q = 0; q < std::size_t(n); ++q) {
                     aprob.push_back(ini.alias[k * std::size_t(n) + q].prob);
@@ -770,17 +845,13 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 d.box = W.box;
                 d.sign = W.sign;
                 d.rect = 0;
-                const long long off = (long long)aprob.size();
-                for (std::size_t q = 0; q < std::size_t(n); ++q) {
-                    aprob.push_back(iso.alias[k * std::size_t(n) + q].prob);
-                    aalt.push_back(iso.alias[k * std::size_t(n) + q].alt);
-                }
-                d.alias_off = off;
+                d.cdf = -1;
+                d.alias_off = (long long)k * n;
                 d.first = nnew;
                 descs.push_back(d);
                 nnew += cnt;
             }
-            generate(np, nnew, istep, 2, true);
+            generate(np, nnew, istep, 2, true, true);
             np += nnew;
             // 4. adiabatic diffuse walls: |Eborder| at the spline temperature
             ck(cudaMemcpyAsync(hE.data(), B.d_Eb.p, hE.size() * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
@@ -789,6 +860,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             descs.clear();
             aprob.clear();
             aalt.clear();
+            reqs.clear();
             nnew = 0;
             for (int gb = 0; gb < nborders; ++gb) {
                 const int E = hE[std::size_t(gb)];
@@ -812,10 +884,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 const double len = norm(sub(br.p2, br.p1));
                 const double Jb = p->Eeff * E / p->dt / (len * g.thickness);
                 const double Tb = B.spl[std::size_t(gb)].interp(Jb);
-                wall_pmf(m, nwall, Tb, Teq, pmf);
-                double tot = 0.;
-                for (double x : pmf) tot += x;
-                if (!(tot > 0.)) continue;
                 GenDesc d{};
                 d.x0 = br.p1.x;
                 d.y0 = br.p1.y;
@@ -824,10 +892,22 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 d.box = b;
                 d.sign = (Tb - Teq) >= 0 ? 1 : -1;
                 d.rect = 0;
-                d.alias_off = add_alias_row(pmf);
+                d.cdf = int(reqs.size());
+                d.alias_off = 0;
                 d.first = nnew;
                 descs.push_back(d);
+                reqs.push_back(WallReq{nwall.x, nwall.y, Tb, Teq});
                 nnew += (long long)(std::abs(E) + 1.0e-6);
+            }
+            if (!reqs.empty()) {
+                // the re-emission distributions at the border temperatures,
+                // built on the device (one block per border)
+                B.d_req.upload(reqs, s);
+                B.d_cdf.alloc(reqs.size() * std::size_t(n) * sizeof(double));
+                B.d_cdftot.alloc(reqs.size() * sizeof(double));
+                be_wall_cdf<<<unsigned(reqs.size()), 256, 0, s>>>(B.d_om.as<double>(), B.d_vx.as<double>(),
+                                                                  B.d_vy.as<double>(), n, B.d_req.as<WallReq>(),
+                                                                  B.d_cdf.as<double>(), B.d_cdftot.as<double>());
             }
             generate(np, nnew, istep, 4, true);
             np += nnew;

@@ -347,6 +347,7 @@ bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
         ck(cudaSetDevice(c->device), "cudaSetDevice");
         c->modes = bte::build_modes(mt);
         c->have_modes = true;
+        c->tables_version++;
         c->nmat = 0;  // materials are rate sets over one table
         c->mat_w.clear();
         c->mat_T0.clear();
@@ -374,6 +375,7 @@ bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
                                              });
         c->geom = std::move(ng);
         c->have_geom = true;
+        c->tables_version++;
         c->geom_dev = false;
         if (!same_normals) c->lambert_dev = false;
         c->gen_key_source = -1;

@@ -67,6 +67,7 @@ struct bte_ctx {
     bte::ProdTuning tune{0, 0, 0, 0};
 
     bool have_modes = false, have_geom = false;
+    long long tables_version = 0;  // bumped by every load of modes or geometry
     bte::HostModes modes;
     bte::HostGeometry geom;
 
