@@ -250,6 +250,78 @@ def kappa_ribbon(modes: dict, T: float, width: float, thickness: float = C_LAT, 
     return float(1e21 * kB / (modes["nq"] * vuc) * np.sum(C * tau * f * v[ok, 0] ** 2))
 
 
+def pulse_geometry(lx: float = 400.0, nx: int = 40, ly: float = 20.0, T0: float = 300.0,
+                   dT: float = 1.0, thickness: float = C_LAT) -> dict:
+    """A row of nx cells closed on all sides by periodic boxes (an infinite
+    medium of period lx along x, uniform along y) whose first cell starts
+    dT above T0: the single-pulse experiment of transient_analytic1d."""
+    g = periodic_cell_geometry(lx, ly, nx, 1, T0=T0, thickness=thickness)
+    g["Tinit"] = g["Tinit"].copy()
+    g["Tinit"][0] = T0 + dT
+    return g
+
+
+def spr_fourier_laplace(modes: dict, T: float, xi, s) -> np.ndarray:
+    """Exact RTA single-pulse response of the infinite medium along x in
+    Fourier-Laplace space (SPR_calculator_FourierLaplace::getSPR,
+    src/analytic1d.cpp:1233-1283), in ps and nm:
+      P(xi, s) = sum C B / sum (C / tau)(1 - B),
+      B = (1 + s tau) / ((1 + s tau)^2 + xi^2 Lambda^2),  Lambda = |v_x tau|.
+    Every mode enters (the reference skips the Gamma point, whose optical
+    modes the engine does move)."""
+    om, w = modes["omega"], modes["w"]
+    vx = modes["vg"].reshape(-1, 3)[:, 0]
+    ok = (om > 0) & (w > 0)
+    C = be_kernel(om[ok], T)
+    tau = 1.0 / w[ok]
+    lam = np.abs(vx[ok] * tau)
+    xi = np.atleast_1d(np.asarray(xi, dtype=float))[:, None, None]
+    s = np.atleast_1d(np.asarray(s, dtype=complex))[None, :, None]
+    a = 1.0 + s * tau
+    B = a / (a * a + (xi * lam) ** 2)
+    return (C * B).sum(-1) / ((C / tau) * (1.0 - B)).sum(-1)
+
+
+def energy_fourier_laplace(modes: dict, T: float, xi, s) -> np.ndarray:
+    """Energy density of the same single pulse (thermal, deposited as C_k),
+    relative to the total: with g_k = C_k at t = 0 the linearised RTA
+    equation gives, per mode, tau (C + C_k P / tau) B, so
+      E(xi, s) = (sum tau C B + P sum C B) / sum C,
+    where P = spr_fourier_laplace is the scattering-weighted temperature
+    sum(g / tau) / sum(C / tau).  E(0, s) = 1 / s."""
+    om, w = modes["omega"], modes["w"]
+    vx = modes["vg"].reshape(-1, 3)[:, 0]
+    ok = (om > 0) & (w > 0)
+    C = be_kernel(om[ok], T)
+    tau = 1.0 / w[ok]
+    lam = np.abs(vx[ok] * tau)
+    xi = np.atleast_1d(np.asarray(xi, dtype=float))[:, None, None]
+    s = np.atleast_1d(np.asarray(s, dtype=complex))[None, :, None]
+    a = 1.0 + s * tau
+    B = a / (a * a + (xi * lam) ** 2)
+    P = (C * B).sum(-1) / ((C / tau) * (1.0 - B)).sum(-1)
+    return ((tau * C * B).sum(-1) + P * (C * B).sum(-1)) / C.sum()
+
+
+def talbot_inverse(F, t: float, M: int = 32) -> float:
+    """Inverse Laplace transform of F at t > 0 by the fixed Talbot contour
+    (Abate and Valko 2004): s(theta) = r theta (cot theta + i), r = 2M / (5t)."""
+    r = 2.0 * M / (5.0 * t)
+    th = np.arange(1, M) * math.pi / M
+    cot = 1.0 / np.tan(th)
+    sk = r * th * (cot + 1j)
+    sig = th + (th * cot - 1.0) * cot
+    Fk = F(np.concatenate([[r + 0j], sk]))
+    val = 0.5 * np.real(Fk[0] * np.exp(r * t)) + np.sum(np.real(np.exp(t * sk) * Fk[1:] * (1.0 + 1j * sig)))
+    return float(r / M * val)
+
+
+def pulse_response(modes: dict, T: float, xi: float, t: float) -> float:
+    """G(xi, t): the xi Fourier component of the energy density at time t
+    after a thermal pulse, relative to t = 0 (G(0, t) = 1)."""
+    return talbot_inverse(lambda s: energy_fourier_laplace(modes, T, [xi], s)[0], t)
+
+
 def grid_geometry(lx: float, ly: float, nx: int, ny: int, T0: float = 300.0,
                   pore_center=None, pore_diameter: float = 0.0,
                   hot_center=None, hot_sigma: float = 50.0, hot_dT: float = 0.0,

@@ -231,3 +231,20 @@ def test_cli_dropin_writes_reference_csvs(built, tmp_path):
     assert (tmp_path / "jx_300K_run_1.csv").exists() and (tmp_path / "jy_300K_run_1.csv").exists()
     o = pyoracle.rta_run(case, seed=5)
     assert np.allclose(T[:, 1:], o["temperature"].T, rtol=0, atol=6e-4)  # CSV keeps 6 digits
+
+
+def test_production_pulse_follows_the_analytic_response(engine):
+    """Production mode, single pulse in an infinite medium (periodic boxes on
+    all sides): Fourier components of the temperature against the exact RTA
+    response of transient_analytic1d (src/analytic1d.cpp:1233-1283)."""
+    import test_pulse_cpu as tp
+    m = synth.mode_table(9, 3, 3, 300.0, config=100, even=True)
+    case = {"modes": m, "geom": synth.pulse_geometry(tp.LX, tp.NX), "T0": 300.0, "dt": tp.DT,
+            "maxtime": tp.TMAX, "N": 400000, "source": "initial"}
+    runs = [_run(engine, case, seed=70 + k, source=btegpu.SOURCE_INITIAL) for k in range(8)]
+    comps = tp.pulse_components(runs)
+    for n, a in comps.items():
+        an = tp.analytic_components(m, n)
+        mu, se = a.mean(0), a.std(0, ddof=1) / np.sqrt(len(a))
+        z = np.abs(mu - an)[1:] / se[1:]
+        assert np.median(z) < 2.0 and z.max() < 6.0, (n, z)

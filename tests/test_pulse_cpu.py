@@ -1,0 +1,57 @@
+"""Transient physics pin: the single-pulse response of an infinite medium.
+
+A row of cells closed by periodic boxes on all sides, one cell 1 K hot at
+t = 0 (source: initial deviation).  The Fourier components of the MC
+temperature profile must follow the exact RTA response of the reference's
+transient_analytic1d (SPR_calculator_FourierLaplace, src/analytic1d.cpp:
+1233-1283, restated with the energy-density weighting in
+synth.energy_fourier_laplace and inverted by a fixed Talbot contour)."""
+import math
+
+import numpy as np
+import pytest
+
+import pyoracle
+import synth
+
+NX, LX, DT, TMAX = 40, 400.0, 10.0, 200.0
+
+
+def pulse_components(runs, ns=(1, 2)):
+    x = (np.arange(NX) + 0.5) * (LX / NX) - 0.5 * (LX / NX)
+    out = {n: [] for n in ns}
+    for r in runs:
+        T = r["temperature"][:NX] - 300.0
+        for n in ns:
+            xi = 2 * math.pi * n / LX
+            out[n].append((T * np.cos(xi * x)[:, None]).sum(0) / T.sum(0))
+    return {n: np.array(v) for n, v in out.items()}
+
+
+def analytic_components(modes, n):
+    xi = 2 * math.pi * n / LX
+    h = 0.5 * LX / NX
+    sinc2 = (math.sin(xi * h) / (xi * h)) ** 2   # slab source and cell averages
+    tc = (np.arange(int(TMAX / DT)) + 0.5) * DT
+    return sinc2 * np.array([np.mean([synth.pulse_response(modes, 300.0, xi, t)
+                                      for t in np.linspace(b - 0.45 * DT, b + 0.45 * DT, 10)])
+                             for b in tc])
+
+
+def test_talbot_inversion_of_known_transforms():
+    assert abs(synth.talbot_inverse(lambda s: 1.0 / (s + 0.3), 2.0) - math.exp(-0.6)) < 1e-10
+    assert abs(synth.talbot_inverse(lambda s: 1.0 / s ** 2, 3.0) - 3.0) < 1e-10
+
+
+def test_pulse_restatement_follows_the_analytic_response():
+    m = synth.mode_table(9, 3, 3, 300.0, config=100, even=True)
+    case = {"modes": m, "geom": synth.pulse_geometry(LX, NX), "T0": 300.0, "dt": DT,
+            "maxtime": TMAX, "N": 40000, "source": "initial"}
+    runs = [pyoracle.rta_run(case, seed=50 + k, nthreads=8) for k in range(10)]
+    comps = pulse_components(runs)
+    for n, a in comps.items():
+        an = analytic_components(m, n)
+        mu, se = a.mean(0), a.std(0, ddof=1) / np.sqrt(len(a))
+        z = np.abs(mu - an)[1:] / se[1:]   # bin 0: the 1 K pulse is not infinitesimal
+        assert np.median(z) < 2.0 and z.max() < 6.0, (n, z)
+        assert np.abs(mu - an).max() < 0.005
