@@ -28,7 +28,8 @@ SOURCE_WALLS, SOURCE_INITIAL = 0, 1
 PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
                   "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run",
-                  "bte_steady_run", "bte_load_materials", "bte_rta_adjoint"]
+                  "bte_steady_run", "bte_load_materials", "bte_rta_adjoint", "bte_set_spectral",
+                  "bte_get_spectral"]
 
 
 class BteError(RuntimeError):
@@ -92,6 +93,14 @@ class BertaResult(C.Structure):
                 ("flux", C.POINTER(C.c_double)), ("nparticles", C.POINTER(C.c_int64)),
                 ("histogram", C.POINTER(C.c_int32)), ("particle_steps", C.c_int64),
                 ("branchings", C.c_int64), ("kernel_ms", C.c_double)]
+
+
+class SpectralResult(C.Structure):
+    _fields_ = [("nloc", C.c_int32), ("nbins", C.c_int32), ("nomega", C.c_int32), ("nq", C.c_int32),
+                ("omega", C.POINTER(C.c_double)), ("dT_omega", C.POINTER(C.c_double)),
+                ("jx_omega", C.POINTER(C.c_double)), ("jy_omega", C.POINTER(C.c_double)),
+                ("fd_q", C.POINTER(C.c_double)), ("q1bz", C.POINTER(C.c_double)),
+                ("raw", C.POINTER(C.c_double))]
 
 
 class AdjointResult(C.Structure):
@@ -251,6 +260,10 @@ def load_library(path: str = LIB_PATH):
     lib.bte_load_materials.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]
     lib.bte_load_materials.restype = C.c_int
+    lib.bte_set_spectral.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32]
+    lib.bte_set_spectral.restype = C.c_int
+    lib.bte_get_spectral.argtypes = [vp, C.POINTER(SpectralResult)]
+    lib.bte_get_spectral.restype = C.c_int
     lib.bte_rta_adjoint.argtypes = [vp, C.POINTER(RtaParams), C.POINTER(C.c_double),
                                     C.POINTER(AdjointResult)]
     lib.bte_rta_adjoint.restype = C.c_int
@@ -413,6 +426,36 @@ def _engine_rta_adjoint(self, weights, T0, dt, maxtime, N, seed=1, source=SOURCE
             "kernel_ms": r.kernel_ms}
 
 
+def _engine_set_spectral(self, boxes, nomega=500):
+    """Spectral decomposition at the given boxes for the following runs."""
+    b = np.ascontiguousarray(np.asarray(boxes, dtype=np.int32))
+    self._keep["spectral"] = b
+    self._check(self.lib.bte_set_spectral(self.ctx, len(b), _iptr(b) if len(b) else None, int(nomega)))
+    self._spec_nomega = int(nomega)
+
+
+def _engine_get_spectral(self, nbins):
+    """The last run's spectral outputs (arrays [nloc, nbins, ...])."""
+    nloc = len(self._keep["spectral"])
+    nw = self._spec_nomega
+    n = int(self._keep["modes"]["omega"].size)
+    nq = int(self._keep["modes"].get("nq", 0)) or n
+    out = {"omega": np.zeros((nloc, nw)), "dT_omega": np.zeros((nloc, nbins, nw)),
+           "jx_omega": np.zeros((nloc, nbins, nw)), "jy_omega": np.zeros((nloc, nbins, nw)),
+           "raw": np.zeros((nloc, nbins, n))}
+    r = SpectralResult()
+    for k in ("omega", "dT_omega", "jx_omega", "jy_omega", "raw"):
+        setattr(r, k, _dptr(out[k]))
+    self._check(self.lib.bte_get_spectral(self.ctx, C.byref(r)))
+    out["fd_q"] = np.zeros((nloc, nbins, r.nq))
+    out["q1bz"] = np.zeros((r.nq, 2))
+    r.fd_q, r.q1bz = _dptr(out["fd_q"]), _dptr(out["q1bz"])
+    self._check(self.lib.bte_get_spectral(self.ctx, C.byref(r)))
+    return out
+
+
+Engine.set_spectral = _engine_set_spectral
+Engine.get_spectral = _engine_get_spectral
 Engine.rta_adjoint = _engine_rta_adjoint
 Engine.load_materials = _engine_load_materials
 Engine.steady_run = _engine_steady_run

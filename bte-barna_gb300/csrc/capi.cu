@@ -429,6 +429,128 @@ bte_status bte_load_materials(bte_ctx* c, int32_t nmat, const double* w, const d
     }
 }
 
+bte_status bte_set_spectral(bte_ctx* c, int32_t nloc, const int32_t* boxes, int32_t nomega) {
+    if (!c) return BTE_ERR_INPUT;
+    try {
+        if (nloc < 0 || (nloc > 0 && (!boxes || nomega < 1)))
+            throw Error(BTE_ERR_INPUT, "spectral locations need boxes and ticks >= 1");
+        if (nloc > 0 && !c->have_geom) throw Error(BTE_ERR_STATE, "load the geometry first");
+        for (int i = 0; i < nloc; ++i) {
+            if (boxes[i] < 0 || boxes[i] >= int(c->geom.boxes.size()))
+                throw Error(BTE_ERR_INPUT, "spectral location is not a box");
+            for (int j = 0; j < i; ++j)
+                if (boxes[j] == boxes[i]) throw Error(BTE_ERR_INPUT, "repeated spectral location");
+        }
+        c->spec_boxes.assign(boxes ? boxes : nullptr, boxes ? boxes + nloc : nullptr);
+        c->spec_nomega = nloc > 0 ? nomega : 0;
+        c->spec_valid = false;
+        return BTE_OK;
+    } catch (const Error& e) {
+        return fail(c, e);
+    }
+}
+
+bte_status bte_get_spectral(bte_ctx* c, bte_spectral_result* out) {
+    if (!c || !out) return BTE_ERR_INPUT;
+    try {
+        if (!c->spec_valid) throw Error(BTE_ERR_STATE, "no run with spectral locations yet");
+        const bte::HostModes& m = c->modes;
+        const bte::HostGeometry& g = c->geom;
+        const std::size_t n = m.n(), nb = std::size_t(m.nb), nq = std::size_t(m.nq);
+        const std::size_t nloc = c->spec_boxes.size(), nbins = std::size_t(c->spec_nbins);
+        const std::size_t nw = std::size_t(c->spec_nomega);
+        out->nloc = int32_t(nloc);
+        out->nbins = int32_t(nbins);
+        out->nomega = int32_t(nw);
+        out->nq = int32_t(nq);
+        // omega ticks: LinSpaced(nomega, 0, max omega) + delta/2 (:2041-2045)
+        double maxw = 0.;
+        for (double w : m.omega) maxw = std::max(maxw, w);
+        std::vector<double> grid(nw);
+        for (std::size_t i = 0; i < nw; ++i)
+            grid[i] = (nw > 1 ? maxw * double(i) / double(nw - 1) : 0.) + 0.5 * maxw / double(nw);
+        if (out->omega)
+            for (std::size_t l = 0; l < nloc; ++l) std::copy(grid.begin(), grid.end(), out->omega + l * nw);
+        // Gamma pdf of every mode over the ticks, shape k = w^2 / sigma,
+        // scale theta = sigma / w (gamma_pdf, :61-63), kept where it is not
+        // negligible
+        const std::vector<double> sig = bte::mode_sigmas(m);
+        std::vector<std::vector<std::pair<int, double>>> gw(n);
+        for (std::size_t k = 0; k < n; ++k) {
+            const double w = m.omega[k];
+            if (!(w > 0.)) continue;
+            const double kk = w * w / sig[k], th = sig[k] / w;
+            const double lg = std::lgamma(kk);
+            for (std::size_t i = 0; i < nw; ++i) {
+                const double x = grid[i] / th;
+                const double lp = (kk - 1.0) * std::log(x) - x - lg - std::log(th);
+                if (lp > -700.) {
+                    const double pdf = std::exp(lp);
+                    if (pdf > 0.) gw[k].emplace_back(int(i), pdf);
+                }
+            }
+        }
+        const double vcorr = g.thickness / m.c;
+        const double hbar = 1.054571726e-34;
+        for (std::size_t l = 0; l < nloc; ++l) {
+            const int box = c->spec_boxes[l];
+            const double vbox = g.boxes[std::size_t(box)].area * g.thickness;
+            const double T0b = bte::box_T0(c, box, c->spec_T0);
+            const double cv = bte::calc_cv(m, T0b);
+            const double Eeff = c->spec_Eeff;
+            std::vector<double> dT(nbins * nw, 0.), jx(nbins * nw, 0.), jy(nbins * nw, 0.), fq(nbins * nq, 0.);
+            for (std::size_t b = 0; b < nbins; ++b) {
+                const double* Tm = c->spec_raw.data() + (l * nbins + b) * n;
+                for (std::size_t k = 0; k < n; ++k) {
+                    const double t = Tm[k];
+                    if (t == 0.) continue;
+                    for (auto& [i, wgt] : gw[k]) {
+                        dT[b * nw + std::size_t(i)] += t * wgt;
+                        jx[b * nw + std::size_t(i)] += m.vxc[k] * t * wgt;
+                        jy[b * nw + std::size_t(i)] += m.vyc[k] * t * wgt;
+                    }
+                    if (m.omega[k] > 0.) fq[b * nq + k / nb] += t / m.omega[k];
+                }
+            }
+            // scaling (:2350-2376) and integration in time (:2386-2413)
+            const double sdT = Eeff / vbox, sj = Eeff * 1e12 * 1e9 * 1e9 / vbox;
+            const double sq = Eeff * vcorr * double(nq) / (vbox * 1.0e+12 * hbar);
+            for (auto& x : dT) x *= sdT;
+            for (auto& x : jx) x *= sj;
+            for (auto& x : jy) x *= sj;
+            for (auto& x : fq) x *= sq;
+            for (std::size_t b = 1; b < nbins; ++b) {
+                for (std::size_t i = 0; i < nw; ++i) {
+                    dT[b * nw + i] += dT[(b - 1) * nw + i];
+                    jx[b * nw + i] += jx[(b - 1) * nw + i];
+                    jy[b * nw + i] += jy[(b - 1) * nw + i];
+                }
+                for (std::size_t q = 0; q < nq; ++q) fq[b * nq + q] += fq[(b - 1) * nq + q];
+            }
+            for (auto& x : dT) x = x / (cv / vcorr);
+            if (out->dT_omega) std::copy(dT.begin(), dT.end(), out->dT_omega + l * nbins * nw);
+            if (out->jx_omega) std::copy(jx.begin(), jx.end(), out->jx_omega + l * nbins * nw);
+            if (out->jy_omega) std::copy(jy.begin(), jy.end(), out->jy_omega + l * nbins * nw);
+            if (out->fd_q) std::copy(fq.begin(), fq.end(), out->fd_q + l * nbins * nq);
+        }
+        if (out->raw) std::copy(c->spec_raw.begin(), c->spec_raw.end(), out->raw);
+        if (out->q1bz) {
+            // q points in Cartesian coordinates, reduced coordinates wrapped
+            // to [-1/2, 1/2) (a Gamma-centred n1 x n2 grid, iq = i n2 + j)
+            const int n1 = m.grid[0] > 0 ? m.grid[0] : 1, n2 = m.grid[1] > 0 ? m.grid[1] : 1;
+            for (std::size_t iq = 0; iq < nq; ++iq) {
+                const int i = int(iq) / n2, j = int(iq) % n2;
+                const int ii = (i + n1 / 2) % n1 - n1 / 2, jj = (j + n2 / 2) % n2 - n2 / 2;
+                out->q1bz[2 * iq + 0] = ii * m.dq[0] + jj * m.dq[3];
+                out->q1bz[2 * iq + 1] = ii * m.dq[1] + jj * m.dq[4];
+            }
+        }
+        return BTE_OK;
+    } catch (const Error& e) {
+        return fail(c, e);
+    }
+}
+
 bte_status bte_query_sizes(const bte_ctx* c, const bte_rta_params* p, int32_t* nboxes,
                            int32_t* nbins, int64_t* nmodes) {
     if (!c || !p) return BTE_ERR_INPUT;
@@ -525,6 +647,21 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         T.pbegin = pbeg;
         T.pend = pend;
         T.nbins = nbins;
+        // spectral decomposition: per-mode time at the selected boxes
+        const std::size_t nloc = c->spec_boxes.size();
+        const std::size_t spec_vals = nloc * std::size_t(nbins) * m.n();
+        if (nloc > 0) {
+            std::vector<int> loc(std::size_t(nbx), -1);
+            for (std::size_t i = 0; i < nloc; ++i) loc[std::size_t(c->spec_boxes[i])] = int(i);
+            c->d_specloc.upload(loc, c->stream);
+            const std::size_t bytes = spec_vals * (replay ? 2 * sizeof(unsigned long long) : sizeof(double));
+            c->d_spec.alloc(bytes);
+            ck(cudaMemsetAsync(c->d_spec.p, 0, bytes, c->stream), "memset");
+            T.spec_loc = c->d_specloc.as<int>();
+            T.spec = c->d_spec.as<double>();
+            T.spec_ex = c->d_spec.as<unsigned long long>();
+        }
+        c->spec_valid = false;
 
         auto* counters = c->d_counters.as<unsigned long long>();
         auto* err = c->d_err.as<int>();
@@ -567,7 +704,27 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         }
         ck(cudaMemcpyAsync(hc.data(), counters, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream), "d2h");
         ck(cudaMemcpyAsync(herr, err, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream), "d2h");
+        std::vector<unsigned long long> hspec;
+        if (nloc > 0) {
+            hspec.resize(replay ? 2 * spec_vals : spec_vals);
+            ck(cudaMemcpyAsync(hspec.data(), c->d_spec.p, hspec.size() * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, c->stream), "d2h");
+        }
         sync(c);
+        if (nloc > 0) {
+            c->spec_raw.resize(spec_vals);
+            for (std::size_t i = 0; i < spec_vals; ++i) {
+                if (replay) {
+                    const __int128 v = (__int128)(((unsigned __int128)hspec[2 * i] << 64) | hspec[2 * i + 1]);
+                    c->spec_raw[i] = double(v) / bte::FIX_SCALE;
+                } else {
+                    std::memcpy(&c->spec_raw[i], &hspec[i], sizeof(double));
+                }
+            }
+            c->spec_nbins = nbins;
+            c->spec_T0 = p->T0;
+            c->spec_valid = true;
+        }
         float ms = 0;
         ck(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "cudaEventElapsedTime");
         out->kernel_ms = ms;
@@ -602,6 +759,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         out->nboxes = nbx;
         out->nbins = nbins;
         out->Eeff = Eeff;
+        c->spec_Eeff = Eeff;
         out->energy_rate = c->gens.total_energy;
         out->events = (int64_t)hc[0];
         out->wall_hits = (int64_t)hc[1];

@@ -190,6 +190,59 @@ void write_csv(const std::string& fn, const std::vector<double>& data, int nboxe
     }
 }
 
+void check(bte_ctx* ctx, bte_status s, const char* what);
+
+// The spectral CSVs of one run (src/RTA_MC2D.cpp:2473-2541): per location,
+// deltaT_omega_, jx_omega_, jy_omega_ with a first row [-1, omega ticks] and
+// rows [(i + 0.5) dt, values of bin i-1] for i = 1..nbins (the reference's
+// time column), and fd_q_ with two header lines of q coordinates; the
+// reference's writer leaves the first data row on the third "# " line.
+void write_spectral(bte_ctx* ctx, const std::vector<int32_t>& boxes, int nw, int nbins, double dt,
+                    const std::string& T0s, long irun) {
+    bte_spectral_result r{};
+    check(ctx, bte_get_spectral(ctx, &r), "spectral outputs");
+    const std::size_t nloc = boxes.size(), nq = std::size_t(r.nq);
+    std::vector<double> om(nloc * nw), dT(nloc * nbins * nw), jx(dT.size()), jy(dT.size()),
+        fq(nloc * nbins * nq), q(2 * nq);
+    r.omega = om.data();
+    r.dT_omega = dT.data();
+    r.jx_omega = jx.data();
+    r.jy_omega = jy.data();
+    r.fd_q = fq.data();
+    r.q1bz = q.data();
+    check(ctx, bte_get_spectral(ctx, &r), "spectral outputs");
+    for (std::size_t l = 0; l < nloc; ++l) {
+        const std::string tail = std::to_string(boxes[l]) + "_" + T0s + "K_run_" + std::to_string(irun) + ".csv";
+        const std::pair<const char*, const std::vector<double>*> sets[3] = {
+            {"deltaT_omega_", &dT}, {"jx_omega_", &jx}, {"jy_omega_", &jy}};
+        for (auto& [name, data] : sets) {
+            std::ofstream o(std::string(name) + tail);
+            if (!o) throw std::runtime_error(std::string("cannot write ") + name + tail);
+            o << -1.0;
+            for (int i = 0; i < nw; ++i) o << ',' << om[l * nw + std::size_t(i)];
+            o << '\n';
+            for (int i = 1; i <= nbins; ++i) {
+                o << (i + 0.5) * dt;
+                for (int k = 0; k < nw; ++k) o << ',' << (*data)[(l * nbins + std::size_t(i - 1)) * nw + std::size_t(k)];
+                o << '\n';
+            }
+        }
+        std::ofstream o("fd_q_" + tail);
+        if (!o) throw std::runtime_error("cannot write fd_q_" + tail);
+        for (int a = 0; a < 2; ++a) {
+            o << "# ";
+            for (std::size_t iq = 0; iq < nq; ++iq) o << (iq ? "," : "") << std::to_string(q[2 * iq + std::size_t(a)]);
+            o << '\n';
+        }
+        o << "# ";
+        for (int i = 0; i < nbins; ++i) {
+            for (std::size_t iq = 0; iq < nq; ++iq)
+                o << (iq ? "," : "") << fq[(l * nbins + std::size_t(i)) * nq + iq];
+            o << '\n';
+        }
+    }
+}
+
 void check(bte_ctx* ctx, bte_status s, const char* what) {
     if (s != BTE_OK) {
         char buf[512];
@@ -219,6 +272,8 @@ int main(int argc, char** argv) {
         double dt = 0, maxtime = 0, thickness = 0, T0 = -1, p = 0;
         long long N = 0;
         double grad[2] = {0., 0.}, eps_energy = -42.0, eps_flux = -42.0;
+        std::vector<int32_t> spec_boxes;
+        int spec_ticks = 0;
         unsigned long long seed = 20261203ULL;
         int mode = BTE_MODE_PRODUCTION, source = BTE_SOURCE_WALLS, ballistic = 0;
         for (auto& k : root->kids) {
@@ -238,6 +293,13 @@ int main(int argc, char** argv) {
             if (k->name == "gradient") {
                 grad[0] = std::stod(k->get("x"));
                 grad[1] = std::stod(k->get("y"));
+            }
+            // <spectral><resolution ticks=/><location bin=/>...</spectral>
+            if (k->name == "spectral") {
+                for (auto& sk : k->kids) {
+                    if (sk->name == "resolution") spec_ticks = std::stoi(sk->get("ticks"));
+                    if (sk->name == "location") spec_boxes.push_back(std::stoi(sk->get("bin")));
+                }
             }
             if (k->name == "convergence") {
                 eps_energy = std::stod(k->get("energy"));
@@ -320,6 +382,11 @@ int main(int argc, char** argv) {
             gm.translation = transl.data();
         }
         check(ctx, bte_load_geometry(ctx, &gm), "load geometry");
+        if (!spec_boxes.empty()) {
+            if (spec_ticks < 1) throw std::runtime_error("<spectral> needs <resolution ticks>");
+            check(ctx, bte_set_spectral(ctx, int32_t(spec_boxes.size()), spec_boxes.data(), spec_ticks),
+                  "spectral locations");
+        }
         auto tB = std::chrono::high_resolution_clock::now();
         std::cout << "#Init variables -> Done (" << std::chrono::duration<double>(tB - tA).count() << " s )\n";
         const double gnorm = std::sqrt(grad[0] * grad[0] + grad[1] * grad[1]);
@@ -406,6 +473,7 @@ int main(int argc, char** argv) {
             write_csv("temperature_" + tag, T, nbx, nbn, dt);
             write_csv("jx_" + tag, jx, nbx, nbn, dt);
             write_csv("jy_" + tag, jy, nbx, nbn, dt);
+            if (!spec_boxes.empty()) write_spectral(ctx, spec_boxes, spec_ticks, nbn, dt, fmt_g(T0), irun);
         }
     } catch (const std::exception& e) {
         std::cerr << "error: " << e.what() << std::endl;

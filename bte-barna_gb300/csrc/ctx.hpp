@@ -95,6 +95,14 @@ struct bte_ctx {
     bte::Generators gens;
     double gen_Eeff = 0;
     bte::DBuf d_gcdf, d_gprob, d_galt, d_walls, d_wcum, d_ifirst, d_ibox, d_isign;
+    // spectral decomposition: selected boxes, ticks, the last run's tally
+    std::vector<int> spec_boxes;
+    int spec_nomega = 0;
+    bte::DBuf d_specloc, d_spec;
+    std::vector<double> spec_raw;      // [nloc][nbins][n] of the last run
+    int spec_nbins = 0;
+    double spec_Eeff = 0., spec_T0 = 0.;
+    bool spec_valid = false;
     // run buffers
     bte::DBuf d_time, d_tally, d_counters, d_err, d_work;
     std::vector<double> h_time;

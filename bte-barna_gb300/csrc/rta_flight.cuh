@@ -78,6 +78,11 @@ struct DevTables {
     double specularity;
     long long pbegin, pend;
     int nbins;
+    // spectral decomposition: box -> location (-1: none, null: off) and the
+    // per-mode time tally [location][bin][mode] (FP64; replay: 2 x u64)
+    const int* spec_loc;
+    double* spec;
+    unsigned long long* spec_ex;
 };
 
 struct Counters {
@@ -299,7 +304,7 @@ __device__ int translate(const DevTables& T, P& pol, int box, V2 r0, V2 v, int& 
 template <bool STEADY, class P>
 __device__ __forceinline__ int seg_tally(const DevTables& T, P& pol, const Particle& p, double d, V2 v) {
     if (STEADY) return pol.tally_dt(T, p.box, d, p.sign, v);
-    return pol.tally(T, p.box, p.t, p.t + d, p.sign, v);
+    return pol.tally(T, p.box, p.t, p.t + d, p.sign, v, p.mode);
 }
 
 // evolparticle: transient (src/RTA_MC2D.cpp:990-1386) or, with STEADY, the

@@ -88,7 +88,8 @@ struct ProdPolicy {
         ntally++;
         return 0;
     }
-    __device__ int tally(const DevTables& T, int box, double t0, double t1, int sign, V2 v) {
+    __device__ int tally(const DevTables& T, int box, double t0, double t1, int sign, V2 v, int mode) {
+        const int loc = T.spec_loc ? __ldg(T.spec_loc + box) : -1;
         int sb = int(t0 * T.inv_dt), eb = int(t1 * T.inv_dt);
         const int last = T.nbins - 1;
         sb = sb < 0 ? 0 : (sb > last ? last : sb);
@@ -103,6 +104,7 @@ struct ProdPolicy {
                 atomicAdd(base + 0, contr);
                 atomicAdd(base + 1, v.x * contr);
                 atomicAdd(base + 2, v.y * contr);
+                if (loc >= 0) atomicAdd(T.spec + (long long)(loc * T.nbins + i) * T.n + mode, contr);
                 ntally++;
             }
         }
@@ -458,6 +460,14 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                 ny = yw;
                 nj = p.j + (upy ? 1 : -1);
                 wside = upy ? 2 : 3;
+            }
+        }
+        // spectral decomposition: the segment's time per mode at selected boxes
+        if (ADJ == 0 && T.spec_loc) {
+            const int loc = __ldg(T.spec_loc + p.box);
+            if (loc >= 0) {
+                const double ds = t1 - p.t;
+                atomicAdd(T.spec + (long long)(loc * T.nbins + bin) * T.n + p.mode, p.sign < 0 ? -ds : ds);
             }
         }
         // differences of the pending tally at the segment end (telescoping)

@@ -71,7 +71,8 @@ struct ReplayPolicy {
         return 0;
     }
     // process_segment (transient), src/RTA_MC2D.cpp:699-769
-    __device__ int tally(const DevTables& T, int box, double t0, double t1, int sign, V2 v) {
+    __device__ int tally(const DevTables& T, int box, double t0, double t1, int sign, V2 v, int mode) {
+        const int loc = T.spec_loc ? T.spec_loc[box] : -1;
         const double* g = T.timegrid;
         int sb = lower_bound_d(g, T.ntime, t0) - 1;
         int eb = lower_bound_d(g, T.ntime, t1) - 1;
@@ -89,6 +90,7 @@ struct ReplayPolicy {
             add128(base + 0, q0);
             add128(base + 2, q1);
             add128(base + 4, q2);
+            if (loc >= 0) add128(T.spec_ex + 2ll * ((long long)(loc * T.nbins + i) * T.n + mode), q0);
             ntally++;
         }
         return 0;

@@ -423,8 +423,8 @@ void build_resample(const HostModes& m, double T0, std::vector<double>& cdf,
     alias_table(pmf.data(), int(m.n()), alias.data());
 }
 
-LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthreads) {
-    const std::size_t nq = std::size_t(m.nq), nb = std::size_t(m.nb), n = m.n();
+std::vector<double> mode_sigmas(const HostModes& m) {
+    const std::size_t n = m.n();
     // broadening per mode, Gamma_grid::base_sigma (include/qpoint_grid.hpp:179-181)
     std::vector<double> sig(n);
     for (std::size_t k = 0; k < n; ++k) {
@@ -434,16 +434,22 @@ LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthrea
             r[j] = v[0] * m.dq[0 + 3 * j] + v[1] * m.dq[1 + 3 * j] + v[2] * m.dq[2 + 3 * j];
         sig[k] = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) / std::sqrt(12.);
     }
-    {
-        std::vector<double> ls(n);
-        for (std::size_t k = 0; k < n; ++k)
-            ls[k] = sig[k] == 0. ? std::numeric_limits<double>::lowest() : std::log(sig[k]);
-        std::sort(ls.begin(), ls.end());
-        const double p25 = ls[25 * n / 100], p75 = ls[75 * n / 100];
-        const double lbound = std::exp(p25 - 1.5 * (p75 - p25));
-        for (auto& s : sig)
-            if (s < lbound) s = lbound;
-    }
+    // outliers clipped at exp(p25 - 1.5 (p75 - p25)) of the log-percentiles
+    // (calc_percentiles_log, src/RTA_MC2D.cpp:573-576, :2038-2040)
+    std::vector<double> ls(n);
+    for (std::size_t k = 0; k < n; ++k)
+        ls[k] = sig[k] == 0. ? std::numeric_limits<double>::lowest() : std::log(sig[k]);
+    std::sort(ls.begin(), ls.end());
+    const double p25 = ls[25 * n / 100], p75 = ls[75 * n / 100];
+    const double lbound = std::exp(p25 - 1.5 * (p75 - p25));
+    for (auto& s : sig)
+        if (s < lbound) s = lbound;
+    return sig;
+}
+
+LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthreads) {
+    const std::size_t nq = std::size_t(m.nq), nb = std::size_t(m.nb), n = m.n();
+    std::vector<double> sig = mode_sigmas(m);
     const double root_two_pi = std::sqrt(2. * PI);
     // candidate modes (not Gamma, omega not ~0), sorted by omega for windows
     std::vector<int> cand;

@@ -101,6 +101,9 @@ struct Generators {
 HostModes build_modes(const bte_mode_table* mt);
 HostGeometry build_geometry(const bte_geometry* g);
 
+// Broadening width of every mode (base_sigma with the outliers clipped).
+std::vector<double> mode_sigmas(const HostModes& m);
+
 // Resampling distribution after an RTA scattering: pmf ~ C(omega, T) w.
 void build_resample(const HostModes& m, double T0, std::vector<double>& cdf,
                     std::vector<Alias>& alias);

@@ -351,6 +351,34 @@ typedef struct bte_adjoint_result {
 bte_status bte_rta_adjoint(bte_ctx* ctx, const bte_rta_params* params, const double* weights,
                            bte_adjoint_result* out);
 
+/* Spectral decomposition at selected boxes (<spectral><resolution
+ * ticks=/><location bin=/>..., src/RTA_MC2D.cpp:150-175, :699-766,
+ * :1979-2052): the following bte_rta_run calls also tally, per location,
+ * time bin and mode, the time spent there; bte_get_spectral turns the last
+ * run's tally into the reference's four outputs (:2350-2420, :2473-2541).
+ * nloc = 0 switches it off. */
+bte_status bte_set_spectral(bte_ctx* ctx, int32_t nloc, const int32_t* boxes, int32_t nomega);
+
+/* Spectral outputs of the last run, each [nloc][nbins][...] and cumulated
+ * in time as the reference writes them:
+ *   dT_omega  Gamma-pdf weighted temperature per omega tick (deltaT_omega_*.csv)
+ *   jx_omega, jy_omega  the flux per omega tick (jx_omega_*, jy_omega_*.csv)
+ *   fd_q      the distribution per q point (fd_q_*.csv)
+ * with omega[nloc][nomega] the tick centres and q1bz[nq][2] the q points.
+ * Any pointer may be NULL. */
+typedef struct bte_spectral_result {
+    int32_t nloc, nbins, nomega, nq;   /* out */
+    double* omega;
+    double* dT_omega;
+    double* jx_omega;
+    double* jy_omega;
+    double* fd_q;
+    double* q1bz;
+    double* raw;     /* [nloc][nbins][nmodes] sign-weighted time per mode (unscaled) */
+} bte_spectral_result;
+
+bte_status bte_get_spectral(bte_ctx* ctx, bte_spectral_result* out);
+
 /* Largest number of time bins bte_rta_run_noalloc accepts. */
 #define BTE_NOALLOC_MAX_BINS 4096
 

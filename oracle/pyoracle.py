@@ -54,6 +54,9 @@ def load():
     lib.oracle_translate.argtypes = [C.POINTER(_bt.Geometry), C.c_int] + [C.c_double] * 4 + [
         C.c_uint64, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.oracle_translate.restype = C.c_int
+    lib.oracle_set_spectral.argtypes = [C.c_int, C.POINTER(C.c_int)]
+    lib.oracle_spectral_raw.argtypes = [C.POINTER(C.c_int64), C.c_longlong]
+    lib.oracle_spectral_raw.restype = C.c_longlong
     lib.oracle_steady_run.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
                                       C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult)]
     lib.oracle_steady_run.restype = C.c_int
@@ -112,6 +115,28 @@ def steady_run(case: dict, gradient, N=None, seed=1, nthreads=8, eps_energy=-42.
     return _bt.steady_call(call, int(case["geom"]["nboxes"]), case["T0"], gradient, N, seed,
                            _bt.MODE_REPLAY, eps_energy, eps_flux, max_generations,
                            specularity=specularity)
+
+
+def set_spectral(boxes):
+    """Spectral locations of the following rta_run calls ([] switches off)."""
+    lib = load()
+    b = np.ascontiguousarray(np.asarray(boxes, dtype=np.int32))
+    lib.oracle_set_spectral(len(b), b.ctypes.data_as(C.POINTER(C.c_int)) if len(b) else None)
+
+
+def spectral_raw(shape):
+    """The last run's per-mode time at the locations: (hi, lo) fixed-point
+    pairs [loc, bin, mode, 2] and their values in ps."""
+    lib = load()
+    n = int(np.prod(shape))
+    out = np.zeros(tuple(shape) + (2,), dtype=np.int64)
+    got = lib.oracle_spectral_raw(out.ctypes.data_as(C.POINTER(C.c_int64)), n)
+    if got != n:
+        raise ValueError(f"spectral tally has {got} values, expected {n}")
+    hi = out[..., 0].reshape(-1).tolist()
+    lo = out[..., 1].astype(np.uint64).reshape(-1).tolist()
+    val = np.array([float((h << 64) | l) for h, l in zip(hi, lo)]).reshape(shape) / 2.0 ** 44
+    return out, val
 
 
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,

@@ -718,6 +718,10 @@ struct Tally {
     std::size_t nboxes = 0, nbins = 0;
     std::vector<double> gz, jx, jy;
     std::vector<__int128> ex;  // [box][bin][3]
+    // spectral decomposition: box -> location, per-mode time [loc][bin][mode]
+    const std::vector<int>* loc = nullptr;
+    std::size_t nmodes = 0;
+    std::vector<__int128> spec;
     int64_t events = 0, wall_hits = 0, crossings = 0, absorbed = 0, nudges = 0,
             quirks = 0, specular = 0, translations = 0;
     void init(std::size_t nbx, std::size_t nbn) {
@@ -747,7 +751,8 @@ inline std::size_t bin_index(const std::vector<double>& g, double t) {
 // process_segment (transient), src/RTA_MC2D.cpp:699-769, without the
 // spectral decomposition.
 inline void process_segment(const Sim& S, Tally& T, std::size_t ibox, double t0,
-                            double t1, int sign, V2 v) {
+                            double t1, int sign, V2 v, std::size_t mode = 0) {
+    const int lc = T.loc ? (*T.loc)[ibox] : -1;
     const auto& g = S.timegrid;
     std::size_t sb = bin_index(g, t0), eb = bin_index(g, t1);
     double delta_t = t1 - t0;
@@ -762,6 +767,9 @@ inline void process_segment(const Sim& S, Tally& T, std::size_t ibox, double t0,
         T.ex[3 * k + 0] += quant(contr);
         T.ex[3 * k + 1] += quant(v.x * contr);
         T.ex[3 * k + 2] += quant(v.y * contr);
+        // per-mode time at a spectral location (the gamma weights, v and
+        // 1/omega of the reference's sd tallies are linear in it)
+        if (lc >= 0) T.spec[(std::size_t(lc) * T.nbins + i) * T.nmodes + mode] += quant(contr);
     }
 }
 
@@ -895,7 +903,7 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
     V2 rnew = {p.pos.x + dt * v.x, p.pos.y + dt * v.y};
     if (box.inside(rnew)) {
         p.pos = rnew;
-        process_segment(S, T, p.box, p.t, p.t + dt, p.sign, v);
+        process_segment(S, T, p.box, p.t, p.t + dt, p.sign, v, p.q * nb + p.alpha);
         p.t += dt;
         if (!o.ballistic) {
             double u = canonical(rng);
@@ -934,7 +942,7 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
             pboxes.push_back(test);
     }
     if (pboxes.empty()) {
-        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v);
+        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v, p.q * nb + p.alpha);
         p.t += tf;
         // in_corner3, src/geometry_2d.cpp:388-406
         std::vector<std::size_t> ids;
@@ -992,13 +1000,13 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
         return;
     } else if (pboxes.size() == 1) {
         p.pos = rnew;
-        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v);
+        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v, p.q * nb + p.alpha);
         p.t += tf;
         p.box = pboxes[0];
         T.crossings++;
         return;
     } else {
-        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v);
+        process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v, p.q * nb + p.alpha);
         p.t += tf;
         p.pos = rnew;
         std::vector<std::size_t> pbox2;
@@ -1908,6 +1916,29 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
                        const double* mT0, const double* share, const bte_rta_params* rp, int nthreads,
                        int log_impl, bte_rta_result* out, int64_t* counters);
 
+namespace {
+std::vector<int> g_spec_boxes;      // spectral locations of the following runs
+std::vector<__int128> g_spec_last;  // the last run's per-mode tally
+}  // namespace
+
+// Spectral locations for the following oracle_rta_run calls (nloc = 0: off).
+void oracle_set_spectral(int nloc, const int* boxes) {
+    g_spec_boxes.assign(boxes, boxes + (nloc > 0 ? nloc : 0));
+}
+
+// The last run's per-mode time at the locations, [loc][bin][mode] as
+// 128-bit fixed-point (hi, lo) pairs; returns the number of values.
+long long oracle_spectral_raw(int64_t* out, long long cap) {
+    const long long n = (long long)g_spec_last.size();
+    if (out && cap >= n)
+        for (long long i = 0; i < n; ++i) {
+            unsigned __int128 u = (unsigned __int128)g_spec_last[std::size_t(i)];
+            out[2 * i] = int64_t(uint64_t(u >> 64));
+            out[2 * i + 1] = int64_t(uint64_t(u));
+        }
+    return n;
+}
+
 int oracle_rta_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_rta_params* rp,
                    int nthreads, int log_impl, bte_rta_result* out, int64_t* counters) {
     return oracle_rta_run_mat(mt, gm, 0, nullptr, nullptr, nullptr, rp, nthreads, log_impl, out, counters);
@@ -1981,9 +2012,16 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
         std::vector<orc::Tally> tl(static_cast<std::size_t>(nthreads));
         std::vector<std::string> errs(static_cast<std::size_t>(nthreads));
         std::vector<int> codes(static_cast<std::size_t>(nthreads), 0);
+        std::vector<int> locs(nbx, -1);
+        for (std::size_t i = 0; i < g_spec_boxes.size(); ++i) locs[std::size_t(g_spec_boxes[i])] = int(i);
         auto work = [&](int tid) {
             orc::Tally& T = tl[std::size_t(tid)];
             T.init(nbx, nbn);
+            if (!g_spec_boxes.empty()) {
+                T.loc = &locs;
+                T.nmodes = S.m.n();
+                T.spec.assign(g_spec_boxes.size() * nbn * S.m.n(), 0);
+            }
             int64_t n = end - begin;
             int64_t lo = begin + n * tid / nthreads, hi = begin + n * (tid + 1) / nthreads;
             try {
@@ -2031,7 +2069,9 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
             T.quirks += tl[t].quirks;
             T.specular += tl[t].specular;
             T.translations += tl[t].translations;
+            for (std::size_t k = 0; k < T.spec.size(); ++k) T.spec[k] += tl[t].spec[k];
         }
+        g_spec_last = T.spec;
         out->nboxes = int32_t(nbx);
         out->nbins = int32_t(nbn);
         out->Eeff = S.Eeff;

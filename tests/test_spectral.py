@@ -1,0 +1,94 @@
+"""Spectral decomposition at selected boxes (<spectral>, src/RTA_MC2D.cpp:
+150-175, :699-766, :2350-2420): the per-mode time tally, exact in replay
+mode, and the four outputs built from it."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import btegpu
+import pyoracle
+import synth
+
+
+def _case():
+    return synth.small_case(n_particles=2000)
+
+
+def test_restatement_spectral_tally_sums_to_the_box_tally():
+    """Summed over modes, the per-mode time of a location is the box's gz
+    tally, to the last fixed-point unit."""
+    case = _case()
+    pyoracle.set_spectral([1, 3])
+    try:
+        r = pyoracle.rta_run(case, seed=4, nthreads=4)
+        nb = r["gz"].shape[1]
+        n = case["modes"]["omega"].size
+        ex, val = pyoracle.spectral_raw((2, nb, n))
+    finally:
+        pyoracle.set_spectral([])
+    exact = ex[..., 0].astype(object) * 2 ** 64 + ex[..., 1].astype(np.uint64).astype(object)
+    tot = exact.sum(axis=2)
+    gz = r["exact"][..., 0, 0].astype(object) * 2 ** 64 + r["exact"][..., 0, 1].astype(np.uint64).astype(object)
+    assert np.all(tot[0] == gz[1]) and np.all(tot[1] == gz[3])
+    assert np.abs(val).sum() > 0
+
+
+@pytest.mark.gpu
+def test_spectral_replay_bit_exact_and_outputs(engine):
+    case = _case()
+    engine.load_modes(case["modes"])
+    engine.load_geometry(case["geom"])
+    engine.set_spectral([1, 3], nomega=400)
+    g = engine.rta_run(case["T0"], case["dt"], case["maxtime"], case["N"], seed=4,
+                       mode=btegpu.MODE_REPLAY)
+    nb = g["gz"].shape[1]
+    sp = engine.get_spectral(nb)
+    pyoracle.set_spectral([1, 3])
+    try:
+        pyoracle.rta_run(case, seed=4, nthreads=4)
+        n = case["modes"]["omega"].size
+        _, val = pyoracle.spectral_raw((2, nb, n))
+    finally:
+        pyoracle.set_spectral([])
+    assert np.array_equal(sp["raw"], val)
+    # the Gamma weights integrate to ~1 over the ticks: sum over omega of the
+    # temperature per tick (x d omega) is the box's temperature rise
+    dw = sp["omega"][0, 1] - sp["omega"][0, 0]
+    dT_box = g["temperature"][[1, 3]] - case["T0"]
+    s = sp["dT_omega"].sum(axis=2) * dw
+    assert np.allclose(s[:, -1], dT_box[:, -1], rtol=0.1, atol=1e-4)
+    assert sp["fd_q"].shape == (2, nb, case["modes"]["nq"])
+    engine.set_spectral([])
+    # production: the same tallies, statistically; the grid kernel tallies them
+    engine.set_spectral([1, 3], nomega=400)
+    p = engine.rta_run(case["T0"], case["dt"], case["maxtime"], 20000, seed=5)
+    sp2 = engine.get_spectral(nb)
+    assert np.allclose(sp2["raw"].sum(axis=2), p["gz"][[1, 3]], rtol=1e-9, atol=1e-9)
+    engine.set_spectral([])
+
+
+@pytest.mark.gpu
+def test_cli_writes_spectral_csvs(built, tmp_path):
+    case = _case()
+    synth.write_geometry_xml(str(tmp_path / "beam.xml"), case["geom"])
+    synth.write_modes_file(str(tmp_path / "modes.bin"), case["modes"])
+    (tmp_path / "input.xml").write_text(
+        '<RTA_MC2d>\n  <geometry file="beam.xml"/>\n  <time dt="10" maxtime="200"/>\n'
+        '  <material name="synthetic" database="modes.bin" thickness="0.335" T0="300.0"/>\n'
+        '  <particles N="2000"/>\n  <engine mode="replay" seed="4"/>\n'
+        '  <spectral>\n    <resolution ticks="60"/>\n    <location bin="1"/>\n'
+        '    <location bin="3"/>\n  </spectral>\n</RTA_MC2d>\n')
+    exe = os.path.join(os.path.dirname(built), "rtamc2d_gpu")
+    r = subprocess.run([exe, "input.xml", "1"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    for loc in (1, 3):
+        d = np.loadtxt(tmp_path / f"deltaT_omega_{loc}_300K_run_0.csv", delimiter=",")
+        assert d.shape == (21, 61) and d[0, 0] == -1.0
+        assert np.allclose(d[1:, 0], (np.arange(1, 21) + 0.5) * 10.0)
+        for name in ("jx_omega", "jy_omega"):
+            assert np.loadtxt(tmp_path / f"{name}_{loc}_300K_run_0.csv", delimiter=",").shape == (21, 61)
+        lines = (tmp_path / f"fd_q_{loc}_300K_run_0.csv").read_text().splitlines()
+        assert lines[0].startswith("# ") and lines[1].startswith("# ") and lines[2].startswith("# ")
+        assert len(lines) == 2 + 20
