@@ -316,6 +316,47 @@ def talbot_inverse(F, t: float, M: int = 32) -> float:
     return float(r / M * val)
 
 
+def pulse_response_bins(modes: dict, T: float, xi_list, dt_bin: float, nbins: int,
+                        h: float = 0.01) -> np.ndarray:
+    """Bin averages of G(xi, t) over [i dt_bin, (i + 1) dt_bin) for each xi,
+    from the same linearised RTA equation integrated in time per mode
+    (RK4, step h ps): dg_k/dt = -(i xi v_k + 1/tau_k) g_k + C_k dT / tau_k,
+    dT = sum(g / tau) / sum(C / tau), g_k(0) = C_k, G = sum g / sum C.
+    Exact to the step error; the Talbot inversion of the transform agrees to
+    six digits except at late times and large xi."""
+    om, w = modes["omega"], modes["w"]
+    vx = modes["vg"].reshape(-1, 3)[:, 0]
+    ok = (om > 0) & (w > 0)
+    C = be_kernel(om[ok], T)
+    tau = 1.0 / w[ok]
+    xi = np.asarray(xi_list, dtype=float)[:, None]
+    rate = -(1j * xi * vx[ok][None, :] + 1.0 / tau[None, :])
+    Ct = C / tau
+    sCt = Ct.sum()
+
+    def f(g):
+        dT = (g / tau).sum(axis=1, keepdims=True) / sCt
+        return rate * g + Ct[None, :] * dT
+
+    g = np.tile(C.astype(complex), (xi.shape[0], 1))
+    steps = int(round(dt_bin / h))
+    out = np.zeros((xi.shape[0], nbins))
+    Gprev = (g.sum(axis=1) / C.sum()).real
+    for b in range(nbins):
+        acc = 0.0
+        for _ in range(steps):
+            k1 = f(g)
+            k2 = f(g + 0.5 * h * k1)
+            k3 = f(g + 0.5 * h * k2)
+            k4 = f(g + h * k3)
+            g = g + h / 6.0 * (k1 + 2 * k2 + 2 * k3 + k4)
+            Gnew = (g.sum(axis=1) / C.sum()).real
+            acc = acc + 0.5 * (Gprev + Gnew) * h   # trapezoid in time
+            Gprev = Gnew
+        out[:, b] = acc / dt_bin
+    return out
+
+
 def pulse_response(modes: dict, T: float, xi: float, t: float) -> float:
     """G(xi, t): the xi Fourier component of the energy density at time t
     after a thermal pulse, relative to t = 0 (G(0, t) = 1)."""
