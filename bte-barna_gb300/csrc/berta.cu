@@ -155,7 +155,176 @@ struct AdvectArgs {
     double dt;
     unsigned long long key;  // Philox key of the random sub-steps
     int random_substep;
+    // boxes that do not tile a grid (or periodic boxes): the convex-box
+    // tables and the key of the geometric choices
+    int general;
+    unsigned long long gkey;
+    int* err;
+    DevTables T;
 };
+
+// Draws of the geometric choices of one particle's advection.
+struct BePol {
+    Philox g;
+    __device__ double u() { return g.uniform(); }
+    __device__ int choose(int n) { return uniform_below(g, uint32_t(n)); }
+};
+
+// beRTA evolparticle on convex boxes (src/beyondRTA_MC2d.cpp:708-970):
+// ballistic advance by dt; a periodic box translates and the remaining time
+// goes on; a void wall absorbs the particle into its border's Eborder (at a
+// corner of three or more boxes, into the first border of the chosen box
+// that faces the velocity); reservoirs absorb.  Returns false when the
+// particle was absorbed; err is set on a geometry failure.
+__device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& x, double& y, int& box,
+                               int mode, int sign, double dt, int& err) {
+    const V2 v = v2(T.vxc[mode], T.vyc[mode]);
+    V2 pos = v2(x, y);
+    for (int guard = 0; guard < (1 << 16); ++guard) {
+        if (T.boxes[box].reservoir) return false;
+        if (T.boxes[box].tto >= 0) {
+            int nb;
+            V2 rf;
+            if (translate(T, pol, box, pos, v, nb, rf)) {
+                err = E_GEOM;
+                return false;
+            }
+            box = nb;
+            pos = rf;
+        }
+        const GBox& B = T.boxes[box];
+        V2 rnew = v2(pos.x + dt * v.x, pos.y + dt * v.y);
+        if (inside_hull(T.hull + B.hull_off, B.nhull, rnew)) {
+            x = rnew.x;
+            y = rnew.y;
+            return true;
+        }
+        HitD mru;
+        if (!get_inter_side(T, box, pos, v, dt, mru)) {
+            const V2 d = sub(B.center, pos);
+            pos = add(pos, divs(scal(1.0e-6, d), norm(d)));
+            continue;
+        }
+        double left = dt - mru.time;
+        if (almost_equal(left, 0.)) left = 0.;
+        rnew = mru.rf;
+        const V2 reps = add(rnew, divs(scal(1.0e-6, v), norm(v)));
+        int pb[MAXC];
+        int np = 0;
+        for (int i = 0; i < B.ncontacts; ++i) {
+            const GContact& gc = T.contacts[B.contact_off + i];
+            if (gc.id == box) continue;
+            const double npv = dot(gc.np, v);
+            if ((box_inside(T, gc.id, rnew) || box_inside(T, gc.id, reps)) && !almost_equal(npv, 0.) && npv > 0.) {
+                if (np == MAXC) {
+                    err = E_LIMIT;
+                    return false;
+                }
+                pb[np++] = gc.id;
+            }
+        }
+        if (np == 0) {
+            // in_corner3 over this box and its contacts
+            int ids[MAXC + 1];
+            int ni = 0;
+            if (box_inside(T, box, rnew)) ids[ni++] = box;
+            for (int i = 0; i < B.ncontacts && ni < MAXC; ++i) {
+                const int cnd = T.contacts[B.contact_off + i].id;
+                if (box_inside(T, cnd, rnew)) ids[ni++] = cnd;
+            }
+            if (ni > 2) {
+                // correct_corner_problem (include/geometry_2d.hpp:524-561):
+                // candidates with at most one border at rnew facing v; the
+                // particle goes to the first such border of the drawn one
+                int fin[MAXC + 1], fb[MAXC + 1];
+                int nf = 0;
+                for (int i = 0; i < ni; ++i) {
+                    const GBox& C = T.boxes[ids[i]];
+                    int cnt = 0, first = -1;
+                    for (int k = 0; k < C.nborders; ++k) {
+                        const GBorder& bb = T.borders[C.border_off + k];
+                        if (on_segment(rnew, bb.la, bb.lb) && dot(bb.np, v) > 0.) {
+                            if (cnt == 0) first = k;
+                            cnt++;
+                        }
+                    }
+                    if (cnt <= 1) {
+                        fin[nf] = ids[i];
+                        fb[nf] = first;
+                        nf++;
+                    }
+                }
+                if (nf == 0) {
+                    err = E_GEOM;
+                    return false;
+                }
+                const int w = pol.choose(nf);
+                if (fb[w] < 0) {  // the reference reads an empty border list here
+                    err = E_GEOM;
+                    return false;
+                }
+                box = fin[w];
+                atomicAdd(Eb + T.boxes[box].border_off + fb[w], sign);
+                x = rnew.x;
+                y = rnew.y;
+                return false;
+            }
+            int ib;
+            if (mru.nb > 1) {
+                int vb[MAXB];
+                int nv = 0;
+                for (int i = 0; i < mru.nb; ++i) {
+                    const GBorder& mb = T.borders[B.border_off + mru.bids[i]];
+                    const V2 rc = add(rnew, scal(1.0e-4, mb.np));
+                    bool isvoid = true;
+                    for (int j = 0; j < B.ncontacts; ++j)
+                        if (box_inside(T, T.contacts[B.contact_off + j].id, rc)) {
+                            isvoid = false;
+                            break;
+                        }
+                    if (isvoid) vb[nv++] = mru.bids[i];
+                }
+                if (nv == 0) {
+                    err = E_GEOM;
+                    return false;
+                }
+                ib = vb[pol.choose(nv)];  // alma::choose: uniform over the void borders
+            } else {
+                ib = mru.bids[0];
+            }
+            atomicAdd(Eb + B.border_off + ib, sign);
+            x = rnew.x;
+            y = rnew.y;
+            return false;
+        }
+        if (np == 1) {
+            box = pb[0];
+            pos = rnew;
+            dt = left;
+            continue;
+        }
+        // several candidates: the ones that contain rnew + tau v for the
+        // largest tau in 1e-6, 1e-7, ... 1e-15
+        int p2[MAXC];
+        int n2 = 0;
+        for (double tau = 1.0e-6; n2 == 0 && tau >= 1.0e-15; tau /= 10.0) {
+            const V2 rc = add(rnew, scal(tau, v));
+            for (int i = 0; i < np; ++i)
+                if (box_inside(T, pb[i], rc)) p2[n2++] = pb[i];
+        }
+        if (n2 == 0) {
+            const V2 d = sub(B.center, rnew);
+            pos = add(rnew, divs(scal(1.0e-6, d), norm(d)));
+            dt = left;
+            continue;
+        }
+        box = p2[pol.choose(n2)];
+        pos = rnew;
+        dt = left;
+    }
+    err = E_LIMIT;
+    return false;
+}
 
 __global__ void be_advect(PArr P, long long begin, long long end, AdvectArgs a) {
     for (long long i = begin + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < end;
@@ -170,8 +339,15 @@ __global__ void be_advect(PArr P, long long begin, long long end, AdvectArgs a) 
         }
         double x = P.x[i], y = P.y[i];
         int box = P.box[i];
-        if (!advect_one(a.G, a.boxcell, a.mv, a.boxwall, a.Eb, x, y, box, mode, P.sign[i], dt))
+        if (a.general) {
+            BePol pol;
+            pol.g.init(a.gkey, (uint64_t)i);
+            int err = 0;
+            if (!advect_general(a.T, pol, a.Eb, x, y, box, mode, P.sign[i], dt, err)) mode = -1;
+            if (err && a.err) atomicCAS(a.err, 0, err);
+        } else if (!advect_one(a.G, a.boxcell, a.mv, a.boxwall, a.Eb, x, y, box, mode, P.sign[i], dt)) {
             mode = -1;
+        }
         P.x[i] = x;
         P.y[i] = y;
         P.box[i] = box;
@@ -222,7 +398,7 @@ __global__ void __launch_bounds__(256) be_wall_cdf(const double* om, const doubl
 // New particles [base, base + n) from the step's sources.
 __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* gens, int ngen,
                             const float* aprob, const int* aalt, const double* cdfs, const double* cdftot,
-                            int nmodes, unsigned long long key) {
+                            int nmodes, unsigned long long key, const GBox* boxes, const V2* hull) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = ngen;
@@ -234,7 +410,18 @@ __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* 
         Philox g;
         g.init(key, (uint64_t)k);
         double x, y;
-        if (gd.rect) {
+        bool placed = true;
+        if (gd.rect == 2) {
+            // a box that is not a grid cell: bounding box and rejection
+            // (geometry_2d::get_random_point, include/geometry_2d.hpp:338-356)
+            const GBox& Bx = boxes[gd.box];
+            placed = false;
+            for (int tries = 0; tries < 100000 && !placed; ++tries) {
+                x = gd.x0 + g.uniform() * gd.dx;
+                y = gd.y0 + g.uniform() * gd.dy;
+                placed = inside_hull(hull + Bx.hull_off, Bx.nhull, v2(x, y));
+            }
+        } else if (gd.rect) {
             x = gd.x0 + g.uniform() * gd.dx;
             y = gd.y0 + g.uniform() * gd.dy;
         } else {
@@ -248,6 +435,7 @@ __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* 
             const double* row = cdfs + (long long)gd.cdf * nmodes;
             mode = cdftot[gd.cdf] > 0. ? lower_bound_d(row, nmodes, g.uniform()) : -1;
             if (mode >= nmodes) mode = nmodes - 1;
+            if (!placed) mode = -1;
         } else {
             const float* pr = aprob + gd.alias_off;
             const int* al = aalt + gd.alias_off;
@@ -595,7 +783,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         const HostModes& m = c->modes;
         const HostGeometry& g = c->geom;
         if (c->nmat > 0) throw Error(BTE_ERR_INPUT, "materials are for transient batched runs");
-        if (!g.rect_grid) throw Error(BTE_ERR_INPUT, "beyond-RTA runs need boxes that tile an axis-aligned grid");
         for (std::size_t b = 0; b < g.boxes.size(); ++b)
             if (!g.reservoir[b] && g.Teq[b] != p->T0)
                 throw Error(BTE_ERR_INPUT, "every box needs Teq = T0 (no gradient source term)");
@@ -682,6 +869,11 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         }();
         auto* counts = B.d_counts.as<unsigned long long>();
         int* err = c->d_err.as<int>();
+        // convex-box tables for geometries that are not a grid (or have
+        // periodic boxes)
+        const int general = g.rect_grid ? 0 : 1;
+        DevTables TT{};
+        fill_static_tables(c, TT);
         std::vector<float> aprob;
         std::vector<int> aalt;
         std::vector<GenDesc> descs;
@@ -722,10 +914,12 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             PArr A = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
             be_generate<<<launch_blocks(total, c->nsm), 256, 0, s>>>(
                 A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), dprob, dalt,
-                B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n, mix_key(p->seed, step, phase));
+                B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n, mix_key(p->seed, step, phase),
+                c->d_boxes.as<GBox>(), c->d_hull.as<V2>());
             if (advect) {
                 AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt,
-                              mix_key(p->seed, step, phase + 1), 1};
+                              mix_key(p->seed, step, phase + 1), 1,
+                              general, mix_key(p->seed, step, phase + 17), err, TT};
                 be_advect<<<launch_blocks(total, c->nsm), 256, 0, s>>>(A, base, base + total, aa);
             }
         };
@@ -784,15 +978,32 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 const long long cnt = (long long)n_to_generate(ini.init_energy[k] / p->Eeff, rng);
                 if (cnt == 0) continue;
                 const int b = ini.init_box[k];
-                const auto ij = cellof[std::size_t(b)];
                 GenDesc d{};
-                d.x0 = g.gx[std::size_t(ij.first)];
-                d.dx = g.gx[std::size_t(ij.first) + 1] - d.x0;
-                d.y0 = g.gy[std::size_t(ij.second)];
-                d.dy = g.gy[std::size_t(ij.second) + 1] - d.y0;
+                if (g.rect_grid) {
+                    const auto ij = cellof[std::size_t(b)];
+                    d.x0 = g.gx[std::size_t(ij.first)];
+                    d.dx = g.gx[std::size_t(ij.first) + 1] - d.x0;
+                    d.y0 = g.gy[std::size_t(ij.second)];
+                    d.dy = g.gy[std::size_t(ij.second) + 1] - d.y0;
+                    d.rect = 1;
+                } else {
+                    const GBox& bx = g.boxes[std::size_t(b)];
+                    double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+                    for (int h = 0; h < bx.nhull; ++h) {
+                        const V2 q = g.hull[std::size_t(bx.hull_off + h)];
+                        x0 = std::min(x0, q.x);
+                        x1 = std::max(x1, q.x);
+                        y0 = std::min(y0, q.y);
+                        y1 = std::max(y1, q.y);
+                    }
+                    d.x0 = x0;
+                    d.dx = x1 - x0;
+                    d.y0 = y0;
+                    d.dy = y1 - y0;
+                    d.rect = 2;
+                }
                 d.box = b;
                 d.sign = ini.init_sign[k];
-                d.rect = 1;
                 d.cdf = -1;
                 const long long off = (long long)aprob.size();
                 for (std::size_t q = 0; q < std::size_t(n); ++q) {
@@ -820,7 +1031,8 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         while (time <= p->maxtime) {
             // 1. advection
             if (np > 0) {
-                AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0};
+                AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0,
+                              general, mix_key(p->seed, istep, 31), err, TT};
                 be_advect<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
                                                                     0, np, aa);
             }
@@ -866,7 +1078,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 const int E = hE[std::size_t(gb)];
                 if (E == 0) continue;
                 const int b = border_box[std::size_t(gb)];
-                if (b < 0 || g.reservoir[std::size_t(b)]) continue;
+                if (b < 0 || g.reservoir[std::size_t(b)] || g.tto[std::size_t(b)] >= 0) continue;
                 const GBorder& br = g.borders[std::size_t(gb)];
                 const V2 nwall = v2(-br.np.x, -br.np.y);
                 const double Teq = g.Teq[std::size_t(b)];
@@ -993,8 +1205,9 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
             sync(c);
             if (herr[0] != 0)
-                throw Error(bte_status(herr[0]), herr[0] == BTE_ERR_LIMIT ? "particle capacity exceeded"
-                                                                          : "particle without a propagator column");
+                throw Error(bte_status(herr[0]), herr[0] == BTE_ERR_LIMIT      ? "particle capacity or step cap exceeded"
+                                                 : herr[0] == BTE_ERR_GEOMETRY ? "geometry error in the advection"
+                                                                               : "particle without a propagator column");
             istep++;
             time += p->dt;
         }

@@ -300,8 +300,9 @@ int main(int argc, char** argv) {
             }
         }
         auto groot = read_xml(resolve(base, gfile));
-        std::vector<int32_t> npts, res;
-        std::vector<double> verts, teq, tinit;
+        std::vector<int32_t> npts, res, tto;
+        std::vector<double> verts, teq, tinit, transl;
+        bool any_periodic = false;
         for (auto& b : groot->kids) {
             if (b->name != "Box") continue;
             const Node* v = b->child("Vertices");
@@ -320,27 +321,41 @@ int main(int argc, char** argv) {
             teq.push_back(te);
             tinit.push_back(ic && ic->has("Tinit") ? std::stod(ic->get("Tinit")) : te);
             res.push_back(b->child("Reservoir") ? 1 : 0);
-            if (b->child("Translate_to")) throw std::runtime_error("periodic boxes are not supported");
+            // <Translate_to id="j"> tx ty [tz] </Translate_to>, src/geometry_2d.cpp:467-475
+            const Node* tr = b->child("Translate_to");
+            tto.push_back(tr ? std::stoi(tr->get("id")) : -1);
+            double tx = 0., ty = 0.;
+            if (tr) {
+                std::stringstream ts(tr->text);
+                ts >> tx >> ty;
+                any_periodic = true;
+            }
+            transl.push_back(tx);
+            transl.push_back(ty);
         }
         ModesFile mf = read_modes(resolve(base, dbfile));
         // Eeff: <Eeff Ed> or the minimum of calc_Eeff over the boxes (:1995-2070)
         double T0 = -1.;
         for (std::size_t b = 0; b < teq.size(); ++b)
-            if (!res[b]) T0 = teq[b];
+            if (!res[b] && tto[b] < 0) T0 = teq[b];
         double Eeff = Ed;
         if (Eeff < 0.) {
             if (!(particles > 0.)) throw std::runtime_error("<Eeff> needs particles= or Ed=");
+            // periodic boxes take no part (src/beyondRTA_MC2d.cpp:2020-2066)
             double maxT = 0., minT = 1.416784e+32, meanT = 0.;
-            for (double t : teq) {
-                meanT += t;
-                maxT = std::max(maxT, t);
-                minT = std::min(minT, t);
+            std::size_t nT = 0;
+            for (std::size_t b = 0; b < teq.size(); ++b) {
+                if (tto[b] >= 0) continue;
+                meanT += teq[b];
+                maxT = std::max(maxT, teq[b]);
+                minT = std::min(minT, teq[b]);
+                ++nT;
             }
             if (Tmax != 0) {
                 maxT = Tmax;
                 minT = Tmin;
             }
-            meanT /= double(teq.size());
+            meanT /= double(nT);
             Eeff = 1e300;
             std::size_t off = 0;
             for (std::size_t b = 0; b < teq.size(); ++b) {
@@ -352,7 +367,7 @@ int main(int argc, char** argv) {
                     a2 += x1 * y2 - x2 * y1;
                 }
                 off += std::size_t(np);
-                if (res[b]) continue;
+                if (res[b] || tto[b] >= 0) continue;
                 const double area = std::fabs(0.5 * a2);
                 const double vuc = thickness * mf.V / mf.c;
                 Eeff = std::min(Eeff, calc_Eeff(mf, maxT, minT, meanT, area * thickness / vuc, particles));
@@ -381,6 +396,10 @@ int main(int argc, char** argv) {
         gm.Tinit = tinit.data();
         gm.reservoir = res.data();
         gm.thickness = thickness;
+        if (any_periodic) {
+            gm.translate_to = tto.data();
+            gm.translation = transl.data();
+        }
         check(ctx, bte_load_geometry(ctx, &gm), "load geometry");
         std::vector<double> P;
         if (!rta) {

@@ -323,22 +323,28 @@ def pulse_response_bins(modes: dict, T: float, xi_list, dt_bin: float, nbins: in
     (RK4, step h ps): dg_k/dt = -(i xi v_k + 1/tau_k) g_k + C_k dT / tau_k,
     dT = sum(g / tau) / sum(C / tau), g_k(0) = C_k, G = sum g / sum C.
     Exact to the step error; the Talbot inversion of the transform agrees to
-    six digits except at late times and large xi."""
+    six digits except at late times and large xi.
+
+    xi = inf gives the limit of large xi: every mode with vx != 0 has left
+    (its g stays 0), the modes with vx = 0 relax and exchange energy among
+    themselves through dT."""
     om, w = modes["omega"], modes["w"]
     vx = modes["vg"].reshape(-1, 3)[:, 0]
     ok = (om > 0) & (w > 0)
     C = be_kernel(om[ok], T)
     tau = 1.0 / w[ok]
     xi = np.asarray(xi_list, dtype=float)[:, None]
-    rate = -(1j * xi * vx[ok][None, :] + 1.0 / tau[None, :])
+    inf = np.isinf(xi)
+    keep = ~(inf & (vx[ok][None, :] != 0.0))
+    rate = np.where(keep, -(1j * np.where(inf, 0.0, xi) * vx[ok][None, :] + 1.0 / tau[None, :]), 0.0)
     Ct = C / tau
     sCt = Ct.sum()
 
     def f(g):
         dT = (g / tau).sum(axis=1, keepdims=True) / sCt
-        return rate * g + Ct[None, :] * dT
+        return keep * (rate * g + Ct[None, :] * dT)
 
-    g = np.tile(C.astype(complex), (xi.shape[0], 1))
+    g = keep * C.astype(complex)[None, :]
     steps = int(round(dt_bin / h))
     out = np.zeros((xi.shape[0], nbins))
     Gprev = (g.sum(axis=1) / C.sum()).real

@@ -139,6 +139,51 @@ def spectral_raw(shape):
     return out, val
 
 
+def mode_sigmas(modes):
+    """Broadening of every mode, Gamma_grid::base_sigma
+    (include/qpoint_grid.hpp:179-181), |v^T dq| / sqrt(12), with the low
+    outliers raised to exp(p25 - 1.5 (p75 - p25)) of the log-percentiles
+    (src/RTA_MC2D.cpp:573-576, :2038-2040)."""
+    v = np.asarray(modes["vg"], dtype=float).reshape(-1, 3)
+    dq = np.asarray(modes["dq"], dtype=float).reshape(3, 3, order="F")
+    sig = np.sqrt(((v @ dq) ** 2).sum(axis=1)) / np.sqrt(12.0)
+    n = sig.size
+    with np.errstate(divide="ignore", over="ignore"):
+        ls = np.sort(np.where(sig == 0.0, -np.finfo(float).max, np.log(np.where(sig == 0.0, 1.0, sig))))
+        p25, p75 = ls[25 * n // 100], ls[75 * n // 100]
+        lbound = np.exp(p25 - 1.5 * (p75 - p25))
+    return np.maximum(sig, lbound)
+
+
+def spectral_post(modes, raw, nomega):
+    """Post-processing of the per-mode time tally raw[loc, bin, mode]
+    (src/RTA_MC2D.cpp:2041-2045, :719-766, :2386-2413) before the constant
+    scalings: the omega ticks, and the time integrals of sum_k t_k g_k(w),
+    sum_k vx_k t_k g_k(w), sum_k vy_k t_k g_k(w) and of t_k / w_k per q
+    point, g_k the Gamma pdf of shape w_k^2 / sigma_k and scale
+    sigma_k / w_k."""
+    from math import lgamma
+    om = np.asarray(modes["omega"], dtype=float)
+    v = np.asarray(modes["vg"], dtype=float).reshape(-1, 3)
+    nb = int(modes["nb"])
+    maxw = om.max()
+    grid = maxw * np.arange(nomega) / max(nomega - 1, 1) + 0.5 * maxw / nomega
+    sig = mode_sigmas(modes)
+    W = np.zeros((om.size, nomega))
+    for k in np.nonzero(om > 0)[0]:
+        kk, th = om[k] ** 2 / sig[k], sig[k] / om[k]
+        x = grid / th
+        lp = (kk - 1.0) * np.log(x) - x - lgamma(kk) - np.log(th)
+        W[k] = np.where(lp > -700.0, np.exp(np.maximum(lp, -700.0)), 0.0)
+    dT = np.cumsum(raw @ W, axis=1)
+    jx = np.cumsum((raw * v[:, 0]) @ W, axis=1)
+    jy = np.cumsum((raw * v[:, 1]) @ W, axis=1)
+    fq = np.zeros(raw.shape[:2] + (om.size // nb,))
+    inv = np.where(om > 0, 1.0 / np.where(om > 0, om, 1.0), 0.0)
+    np.add.at(fq, (slice(None), slice(None), np.arange(om.size) // nb), raw * inv)
+    return grid, dT, jx, jy, np.cumsum(fq, axis=1)
+
+
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,
             source=None, specularity=None, materials=None):
     """`materials`: optional (list of per-mode rate arrays, list of T0[,

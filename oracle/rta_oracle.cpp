@@ -1559,12 +1559,17 @@ inline void be_evolve(BeRun& R, BeParticle& p, V2 v, double dt, Pcg64& rng) {
     const auto& sys = R.S.sys;
     for (int guard = 0;; ++guard) {
         if (guard > 1000000) throw limit_error("advection step cap");
-        const V2 opos = p.pos;
-        const Box& box = sys[p.box];
-        if (box.reservoir) {
+        if (sys[p.box].reservoir) {
             be_kill(p);
             return;
         }
+        if (sys[p.box].periodic) {  // Apply PBC and go on with the same time (:728-737)
+            auto sol = translate(R.S, p.box, p.pos, v, rng);
+            p.box = sol.first;
+            p.pos = sol.second;
+        }
+        const V2 opos = p.pos;
+        const Box& box = sys[p.box];
         V2 rnew = {p.pos.x + dt * v.x, p.pos.y + dt * v.y};
         if (box.inside(rnew)) {
             p.pos = rnew;
@@ -2439,7 +2444,7 @@ int oracle_berta_run(const bte_mode_table* mt, const bte_geometry* gm, const dou
         // init_particles (Tinit != Teq), src/beyondRTA_MC2d.cpp:211-269
         std::vector<double> pmf;
         for (auto& s : S.sys) {
-            if (s.reservoir || orc::almost_equal(s.Teq, s.Treal)) continue;
+            if (s.reservoir || s.periodic || orc::almost_equal(s.Teq, s.Treal)) continue;
             pmf.assign(n, 0.);
             for (std::size_t k = 0; k < n; ++k) {
                 const double om = m.omega[k];
@@ -2535,7 +2540,7 @@ int oracle_berta_run(const bte_mode_table* mt, const bte_geometry* gm, const dou
             {
                 std::vector<orc::BeParticle> np;
                 for (auto& s : S.sys) {
-                    if (s.reservoir) continue;
+                    if (s.reservoir || s.periodic) continue;
                     for (std::size_t k = 0; k < s.borders.size(); ++k) {
                         const orc::Border& b = s.borders[k];
                         const orc::V2 nwall = {-b.np.x, -b.np.y};

@@ -28,18 +28,23 @@ def pulse_components(runs, ns=(1, 2)):
     return {n: np.array(v) for n, v in out.items()}
 
 
-def analytic_components(modes, n, K=3):
+def analytic_components(modes, n, K=8):
     """What the cosine sum over cell averages of the analytic profile gives:
     the one-cell pulse has every wavenumber m with weight sinc(xi_m dx / 2),
     cell averaging multiplies by it again, and the sum at n collects the
     aliases m = n + k NX:  D_n(t) = sum_k sinc^2(xi_{n+kN} dx/2) G(xi_{n+kN}, t)
-    (D_n(0) = 1).  |k| <= K."""
+    (D_n(0) = 1).  |k| <= K exactly; the aliases beyond K carry the weights
+    sum_{|k|>K} sinc^2 (about 2 sin^2(pi n/N) / (pi^2 K)) times the large-xi
+    limit of G, which the modes with vx = 0 set."""
     h = 0.5 * LX / NX
     ms = [n + k * NX for k in range(-K, K + 1)]
-    xis = [2 * math.pi * m / LX for m in ms]
+    xis = [2 * math.pi * m / LX for m in ms] + [math.inf]
     G = synth.pulse_response_bins(modes, 300.0, xis, DT, int(TMAX / DT), h=0.005)
-    w = np.array([(math.sin(x * h) / (x * h)) ** 2 for x in xis])
-    return (w[:, None] * G).sum(axis=0)
+    w = np.array([(math.sin(x * h) / (x * h)) ** 2 for x in xis[:-1]])
+    k = np.arange(K + 1, 200000, dtype=float)
+    s2 = math.sin(math.pi * n / NX) ** 2
+    tail = s2 / math.pi ** 2 * ((1.0 / (k + n / NX) ** 2).sum() + (1.0 / (k - n / NX) ** 2).sum())
+    return (w[:, None] * G[:-1]).sum(axis=0) + tail * G[-1]
 
 
 def test_talbot_inversion_of_known_transforms():

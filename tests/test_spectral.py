@@ -35,6 +35,27 @@ def test_restatement_spectral_tally_sums_to_the_box_tally():
     assert np.abs(val).sum() > 0
 
 
+def _check_outputs(case, g, sp, nomega):
+    """The engine's four outputs against the restated post-processing: the
+    temperature per tick carries the box temperature's own scale (its time
+    integral summed over modes is the box's gz), the fluxes and the q-mesh
+    distribution one constant each."""
+    grid, dT, jx, jy, fq = pyoracle.spectral_post(case["modes"], sp["raw"], nomega)
+    assert np.allclose(sp["omega"], grid[None, :], rtol=1e-14)
+    dT_box = g["temperature"][[1, 3]] - case["T0"]
+    cum = np.cumsum(sp["raw"].sum(axis=2), axis=1)
+    for l in range(2):
+        b = np.nonzero(np.abs(cum[l]) > 1e-6 * np.abs(cum[l]).max())[0]
+        scale = dT_box[l, b] / cum[l, b]
+        assert np.allclose(scale, scale[0], rtol=1e-9)
+        assert np.allclose(sp["dT_omega"][l], scale[0] * dT[l], rtol=1e-9,
+                           atol=1e-12 * np.abs(sp["dT_omega"][l]).max())
+        for mine, ref in ((sp["jx_omega"][l], jx[l]), (sp["jy_omega"][l], jy[l]), (sp["fd_q"][l], fq[l])):
+            i = np.argmax(np.abs(ref))
+            c = mine.flat[i] / ref.flat[i]
+            assert np.allclose(mine, c * ref, rtol=1e-9, atol=1e-12 * np.abs(mine).max())
+
+
 @pytest.mark.gpu
 def test_spectral_replay_bit_exact_and_outputs(engine):
     case = _case()
@@ -53,12 +74,7 @@ def test_spectral_replay_bit_exact_and_outputs(engine):
     finally:
         pyoracle.set_spectral([])
     assert np.array_equal(sp["raw"], val)
-    # the Gamma weights integrate to ~1 over the ticks: sum over omega of the
-    # temperature per tick (x d omega) is the box's temperature rise
-    dw = sp["omega"][0, 1] - sp["omega"][0, 0]
-    dT_box = g["temperature"][[1, 3]] - case["T0"]
-    s = sp["dT_omega"].sum(axis=2) * dw
-    assert np.allclose(s[:, -1], dT_box[:, -1], rtol=0.1, atol=1e-4)
+    _check_outputs(case, g, sp, 400)
     assert sp["fd_q"].shape == (2, nb, case["modes"]["nq"])
     engine.set_spectral([])
     # production: the same tallies, statistically; the grid kernel tallies them
