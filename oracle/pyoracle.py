@@ -170,7 +170,7 @@ def spectral_post(modes, raw, nomega):
     grid = maxw * np.arange(nomega) / max(nomega - 1, 1) + 0.5 * maxw / nomega
     sig = mode_sigmas(modes)
     W = np.zeros((om.size, nomega))
-    for k in np.nonzero(om > 0)[0]:
+    for k in np.nonzero((om > 0) & (sig > 0))[0]:   # sigma = 0: no omega weight
         kk, th = om[k] ** 2 / sig[k], sig[k] / om[k]
         x = grid / th
         lp = (kk - 1.0) * np.log(x) - x - lgamma(kk) - np.log(th)
