@@ -84,8 +84,9 @@ class Propagator(C.Structure):
 class BertaParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("maxtime", C.c_double), ("Eeff", C.c_double),
                 ("T0", C.c_double), ("seed", C.c_uint64), ("mode", C.c_int32),
-                ("rta", C.c_int32), ("cancel_every", C.c_int32), ("reserved0", C.c_int32),
-                ("capacity", C.c_int64), ("on_step", C.c_void_p), ("user", C.c_void_p)]
+                ("rta", C.c_int32), ("cancel_every", C.c_int32), ("gradient_mode", C.c_int32),
+                ("capacity", C.c_int64), ("on_step", C.c_void_p), ("user", C.c_void_p),
+                ("gradient", C.c_double * 2)]
 
 
 class BertaResult(C.Structure):
@@ -165,10 +166,15 @@ def berta_steps(dt: float, maxtime: float) -> int:
 
 
 def berta_params(dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, mode=MODE_PRODUCTION,
-                 cancel_every=4, capacity=0):
+                 cancel_every=4, capacity=0, gradient=None):
+    """`gradient`: None for the gradients of the boxes' Teq (the reference's
+    default), or (gx, gy) in K/nm, the homogeneous <gradient x y>."""
     p = BertaParams()
     p.dt, p.maxtime, p.Eeff, p.T0, p.seed = float(dt), float(maxtime), float(Eeff), float(T0), int(seed)
     p.mode, p.rta, p.cancel_every, p.capacity = int(mode), int(bool(rta)), int(cancel_every), int(capacity)
+    if gradient is not None:
+        p.gradient_mode = 1
+        p.gradient[0], p.gradient[1] = float(gradient[0]), float(gradient[1])
     return p
 
 
@@ -366,9 +372,11 @@ def _engine_load_propagator(self, P: np.ndarray, T: float = 300.0):
 
 
 def _engine_berta_run(self, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, cancel_every=4,
-                      capacity=0, histogram=False):
-    """beRTAMC2D loop: per step ed [s, box] (J m^-3), flux [s, box, 2], N [s]."""
-    p = berta_params(dt, maxtime, Eeff, T0, seed, rta, MODE_PRODUCTION, cancel_every, capacity)
+                      capacity=0, histogram=False, gradient=None):
+    """beRTAMC2D loop: per step ed [s, box] (J m^-3), flux [s, box, 2], N [s].
+    `gradient` (K/nm): the homogeneous <gradient x y> source term."""
+    p = berta_params(dt, maxtime, Eeff, T0, seed, rta, MODE_PRODUCTION, cancel_every, capacity,
+                     gradient)
     nsteps = berta_steps(dt, maxtime)
     nbx = self.nboxes
     ed = np.zeros((nsteps + 1, nbx))

@@ -3,6 +3,9 @@
 // The step loop of src/beyondRTA_MC2d.cpp:2138-2425, production mode:
 //   1 advection by dt; void walls absorb and count Eborder, reservoirs absorb
 //     (evolparticle :708-970)                                      be_advect
+//   2 gradient source term: Nabla_T particles at random points of every box
+//     with a gradient, random sub-step (source_term_gradient :597-676,
+//     Nabla_T_distribution src/sampling.cpp:118-187)            be_generate
 //   3 isothermal-wall injection, random sub-step            be_generate
 //     (Isothermal_walls :446-585, Ntogenerate src/sampling.cpp:243-260)
 //   4 adiabatic diffuse re-emission of |Eborder| at the wall temperature from
@@ -49,6 +52,8 @@ struct GenDesc {
     int cdf;                // >= 0: mode from device CDF row `cdf`; -1: alias row at alias_off
     long long alias_off;
     long long first;
+    int msign;              // 1: sign of each mode from the sign row at alias_off
+    int pad;
 };
 
 // One adiabatic re-emission distribution to build on the device: an
@@ -76,6 +81,8 @@ struct BertaState {
     DBuf q_x, q_y, q_mode, q_box, q_sign;   // branching queues (two halves)
     DBuf d_H, d_cnt, d_Eb, d_props, d_counts, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
+    DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
+
     std::vector<Spline1D> spl;
     std::vector<char> spl_ok;
     long long spl_version = -1;   // tables the splines were built for
@@ -397,8 +404,9 @@ __global__ void __launch_bounds__(256) be_wall_cdf(const double* om, const doubl
 
 // New particles [base, base + n) from the step's sources.
 __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* gens, int ngen,
-                            const float* aprob, const int* aalt, const double* cdfs, const double* cdftot,
-                            int nmodes, unsigned long long key, const GBox* boxes, const V2* hull) {
+                            const float* aprob, const int* aalt, const signed char* asign,
+                            const double* cdfs, const double* cdftot, int nmodes, unsigned long long key,
+                            const GBox* boxes, const V2* hull) {
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = ngen;
@@ -448,7 +456,7 @@ __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* 
         P.y[i] = y;
         P.box[i] = gd.box;
         P.mode[i] = mode;
-        P.sign[i] = gd.sign;
+        P.sign[i] = (gd.msign && mode >= 0) ? int(__ldg(asign + gd.alias_off + mode)) : gd.sign;
     }
 }
 
@@ -783,9 +791,16 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         const HostModes& m = c->modes;
         const HostGeometry& g = c->geom;
         if (c->nmat > 0) throw Error(BTE_ERR_INPUT, "materials are for transient batched runs");
+        // one temperature for the scattering tables: every box that is
+        // neither a reservoir nor periodic at T0, so the gradients of the
+        // boxes' Teq (calculate_gradientT, src/geometry_2d.cpp:524-575) are
+        // zero and only a homogeneous <gradient> adds a source term
         for (std::size_t b = 0; b < g.boxes.size(); ++b)
-            if (!g.reservoir[b] && g.Teq[b] != p->T0)
-                throw Error(BTE_ERR_INPUT, "every box needs Teq = T0 (no gradient source term)");
+            if (!g.reservoir[b] && g.tto[b] < 0 && g.Teq[b] != p->T0)
+                throw Error(BTE_ERR_INPUT, "every box needs Teq = T0 (one scattering temperature per run)");
+        if (p->gradient_mode != 0 && p->gradient_mode != 1) throw Error(BTE_ERR_INPUT, "bad gradient_mode");
+        if (p->gradient_mode == 1 && !(std::isfinite(p->gradient[0]) && std::isfinite(p->gradient[1])))
+            throw Error(BTE_ERR_INPUT, "gradient must be finite");
         if (p->rta) ensure_resample(c, p->T0);
         if (!c->berta) c->berta = new BertaState();
         BertaState& B = *c->berta;
@@ -878,6 +893,54 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         std::vector<int> aalt;
         std::vector<GenDesc> descs;
         std::vector<WallReq> reqs;
+        // a source spread over box b: its grid cell, or its bounding box with
+        // rejection (geometry_2d::get_random_point)
+        auto box_desc = [&](int b) {
+            GenDesc d{};
+            if (g.rect_grid) {
+                const auto ij = cellof[std::size_t(b)];
+                d.x0 = g.gx[std::size_t(ij.first)];
+                d.dx = g.gx[std::size_t(ij.first) + 1] - d.x0;
+                d.y0 = g.gy[std::size_t(ij.second)];
+                d.dy = g.gy[std::size_t(ij.second) + 1] - d.y0;
+                d.rect = 1;
+            } else {
+                const GBox& bx = g.boxes[std::size_t(b)];
+                double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
+                for (int h = 0; h < bx.nhull; ++h) {
+                    const V2 q = g.hull[std::size_t(bx.hull_off + h)];
+                    x0 = std::min(x0, q.x);
+                    x1 = std::max(x1, q.x);
+                    y0 = std::min(y0, q.y);
+                    y1 = std::max(y1, q.y);
+                }
+                d.x0 = x0;
+                d.dx = x1 - x0;
+                d.y0 = y0;
+                d.dy = y1 - y0;
+                d.rect = 2;
+            }
+            d.box = b;
+            d.cdf = -1;
+            return d;
+        };
+        // the gradient source term: a homogeneous <gradient> on every box
+        // that is neither a reservoir nor periodic (the gradients of the
+        // boxes' Teq are zero here); Nabla_T rows at each box's Teq, built
+        // once as the reference's static generators are
+        GradGenerators grad;
+        if (p->gradient_mode == 1 && !almost_equal(std::hypot(p->gradient[0], p->gradient[1]), 0.)) {
+            grad = build_gradient_generators(m, g, p->gradient[0], p->gradient[1]);
+            std::vector<float> gp(grad.alias.size());
+            std::vector<int> ga(grad.alias.size());
+            for (std::size_t i = 0; i < grad.alias.size(); ++i) {
+                gp[i] = grad.alias[i].prob;
+                ga[i] = grad.alias[i].alt;
+            }
+            B.d_gprob.upload(gp, s);
+            B.d_galt.upload(ga, s);
+            B.d_gsign.upload(grad.sign, s);
+        }
         // generate the sources in `descs` (alias rows in aprob/aalt) at A[base..)
         // the isothermal walls' alias rows do not change during a run
         {
@@ -894,16 +957,17 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             B.d_vy.upload(m.vy, s);
         }
         // generate the sources in `descs` at A[base..): alias rows from
-        // aprob/aalt (uploaded here) or from the isothermal walls' table
-        // (iso_rows), CDF rows from B.d_cdf
+        // aprob/aalt (uploaded here) or from a table already on the device
+        // (rprob/ralt, with per-mode signs rsign), CDF rows from B.d_cdf
         auto generate = [&](long long base, long long total, long long step, int phase, bool advect,
-                            bool iso_rows = false) {
+                            const float* rprob = nullptr, const int* ralt = nullptr,
+                            const signed char* rsign = nullptr) {
             if (total <= 0) return;
             if (base + total > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded: raise capacity");
             B.d_gens.upload(descs, s);
-            const float* dprob = B.d_isoprob.as<float>();
-            const int* dalt = B.d_isoalt.as<int>();
-            if (!iso_rows && !aprob.empty()) {
+            const float* dprob = rprob;
+            const int* dalt = ralt;
+            if (!rprob && !aprob.empty()) {
                 B.d_alias.alloc(aprob.size() * sizeof(float) + aalt.size() * sizeof(int));
                 ck(cudaMemcpyAsync(B.d_alias.p, aprob.data(), aprob.size() * sizeof(float), cudaMemcpyHostToDevice, s), "h2d");
                 int* a2 = reinterpret_cast<int*>(B.d_alias.as<char>() + aprob.size() * sizeof(float));
@@ -913,7 +977,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             PArr A = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
             be_generate<<<launch_blocks(total, c->nsm), 256, 0, s>>>(
-                A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), dprob, dalt,
+                A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), dprob, dalt, rsign,
                 B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n, mix_key(p->seed, step, phase),
                 c->d_boxes.as<GBox>(), c->d_hull.as<V2>());
             if (advect) {
@@ -978,31 +1042,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 const long long cnt = (long long)n_to_generate(ini.init_energy[k] / p->Eeff, rng);
                 if (cnt == 0) continue;
                 const int b = ini.init_box[k];
-                GenDesc d{};
-                if (g.rect_grid) {
-                    const auto ij = cellof[std::size_t(b)];
-                    d.x0 = g.gx[std::size_t(ij.first)];
-                    d.dx = g.gx[std::size_t(ij.first) + 1] - d.x0;
-                    d.y0 = g.gy[std::size_t(ij.second)];
-                    d.dy = g.gy[std::size_t(ij.second) + 1] - d.y0;
-                    d.rect = 1;
-                } else {
-                    const GBox& bx = g.boxes[std::size_t(b)];
-                    double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300;
-                    for (int h = 0; h < bx.nhull; ++h) {
-                        const V2 q = g.hull[std::size_t(bx.hull_off + h)];
-                        x0 = std::min(x0, q.x);
-                        x1 = std::max(x1, q.x);
-                        y0 = std::min(y0, q.y);
-                        y1 = std::max(y1, q.y);
-                    }
-                    d.x0 = x0;
-                    d.dx = x1 - x0;
-                    d.y0 = y0;
-                    d.dy = y1 - y0;
-                    d.rect = 2;
-                }
-                d.box = b;
+                GenDesc d = box_desc(b);
                 d.sign = ini.init_sign[k];
                 d.cdf = -1;
                 const long long off = (long long)aprob.size();
@@ -1037,6 +1077,24 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                                                                     0, np, aa);
             }
             psteps += np;
+            // 2. gradient source term: Ntogenerate(dt, vol, Eeff) per box
+            if (!grad.box.empty()) {
+                descs.clear();
+                long long nnew = 0;
+                for (std::size_t k = 0; k < grad.box.size(); ++k) {
+                    const long long cnt = (long long)n_to_generate(p->dt * grad.energy[k] / p->Eeff, rng);
+                    if (cnt == 0) continue;
+                    GenDesc d = box_desc(grad.box[k]);
+                    d.alias_off = (long long)k * n;
+                    d.msign = 1;
+                    d.first = nnew;
+                    descs.push_back(d);
+                    nnew += cnt;
+                }
+                generate(np, nnew, istep, 8, true, B.d_gprob.as<float>(), B.d_galt.as<int>(),
+                         B.d_gsign.as<signed char>());
+                np += nnew;
+            }
             // 3. isothermal walls
             descs.clear();
             aprob.clear();
@@ -1063,7 +1121,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 descs.push_back(d);
                 nnew += cnt;
             }
-            generate(np, nnew, istep, 2, true, true);
+            generate(np, nnew, istep, 2, true, B.d_isoprob.as<float>(), B.d_isoalt.as<int>());
             np += nnew;
             // 4. adiabatic diffuse walls: |Eborder| at the spline temperature
             ck(cudaMemcpyAsync(hE.data(), B.d_Eb.p, hE.size() * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");

@@ -264,7 +264,8 @@ int main(int argc, char** argv) {
         const std::string base = dir_of(input);
         std::string gfile, dbfile, pfile;
         double dt = 0, maxtime = 0, thickness = 0, Ed = -1, Tmax = 0, Tmin = 0, particles = 0;
-        bool rta = false;
+        bool rta = false, have_grad = false;
+        double grad[2] = {0., 0.};
         unsigned long long seed = 20261203ULL;
         long long capacity = 0;
         for (auto& k : root->kids) {
@@ -291,7 +292,12 @@ int main(int argc, char** argv) {
                 }
             }
             if (k->name == "RTA") rta = true;
-            if (k->name == "gradient") throw std::runtime_error("<gradient> source terms are not supported");
+            // <gradient x y/>: homogeneous gradient in K/nm (:1328-1333)
+            if (k->name == "gradient") {
+                have_grad = true;
+                grad[0] = std::stod(k->get("x"));
+                grad[1] = std::stod(k->get("y"));
+            }
             if (k->name == "transmission") throw std::runtime_error("This is currently not supported");
             if (k->name == "init_distribution") throw std::runtime_error("<init_distribution> is not supported");
             if (k->name == "engine") {
@@ -423,6 +429,11 @@ int main(int argc, char** argv) {
         bp.mode = BTE_MODE_PRODUCTION;
         bp.rta = rta ? 1 : 0;
         bp.cancel_every = 4;
+        if (have_grad) {
+            bp.gradient_mode = 1;
+            bp.gradient[0] = grad[0];
+            bp.gradient[1] = grad[1];
+        }
         bp.capacity = capacity;
         bp.on_step = on_step;
         bp.user = &so;

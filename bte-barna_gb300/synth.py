@@ -201,6 +201,29 @@ def kappa_rta(modes: dict, T: float, thickness: float = C_LAT) -> np.ndarray:
     return 1e21 * kB / (modes["nq"] * vuc) * vv
 
 
+def kappa_berta_steps(modes: dict, T: float, dt: float, steps, thickness: float = C_LAT) -> np.ndarray:
+    """Expected kappa_xx of the beRTAMC2D loop with RTA scattering and a
+    homogeneous gradient source in an infinite medium, at output rows
+    `steps` (row s follows s loop iterations).  A source particle is born
+    in an iteration and meets the scattering test 1 - exp(-w dt) at the end
+    of that iteration and of every later one; the flux counts it while it
+    has not scattered (after scattering the resampled modes carry no net
+    flux), so tau_k becomes dt q (1 - q^s) / (1 - q), q = exp(-w_k dt), in
+    the bulk formula."""
+    om, w = modes["omega"], modes["w"]
+    v = modes["vg"].reshape(-1, 3)[:, 0]
+    ok = (om > 0) & (w > 0)
+    C = be_kernel(om[ok], T)
+    q = np.exp(-w[ok] * dt)
+    kB = 1.3806488e-23
+    vuc = modes["V"] * thickness / modes["c_lat"]
+    out = []
+    for s_ in np.atleast_1d(steps):
+        teff = dt * q * (1 - q ** float(s_)) / (1 - q)
+        out.append(1e21 * kB / (modes["nq"] * vuc) * (C * teff * v[ok] * v[ok]).sum())
+    return np.array(out)
+
+
 def periodic_ribbon_geometry(length: float = 40.0, width: float = 100.0, nx: int = 2, ny: int = 2,
                              T0: float = 300.0, thickness: float = C_LAT, side: float = 1.0) -> dict:
     """A ribbon along x, periodic in x (left and right periodic boxes map

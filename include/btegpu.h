@@ -178,10 +178,18 @@ typedef struct bte_berta_params {
     int32_t mode;            /* BTE_MODE_PRODUCTION                              */
     int32_t rta;             /* 1: RTA scattering (<RTA/>), 0: propagator        */
     int32_t cancel_every;    /* cancellation period in steps (reference: 4)     */
-    int32_t reserved0;
+    int32_t gradient_mode;   /* source term of step 2 (source_term_gradient,
+                                src/beyondRTA_MC2d.cpp:597-676):
+                                0: gradients from the boxes' Teq
+                                   (calculate_gradientT, the reference's
+                                   default; zero while every box has Teq = T0)
+                                1: the homogeneous <gradient x y> below on
+                                   every box that is neither a reservoir nor
+                                   periodic                                 */
     int64_t capacity;        /* particle capacity on the device (0 = auto)       */
     bte_berta_step_fn on_step; /* optional per-step hook (NULL: none)          */
     void* user;              /* passed to on_step                                */
+    double gradient[2];      /* K/nm, gradient_mode 1                            */
 } bte_berta_params;
 
 /* Results of one beRTAMC2D run; per step s = 0..nsteps (s = 0 is the

@@ -287,8 +287,9 @@ def lambert_nnz(case: dict) -> np.ndarray:
     return out
 
 
-def berta_run(modes, geom, P, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False):
-    """beRTAMC2D restatement: per-step ed [s, box], flux [s, box, 2], N [s]."""
+def berta_run(modes, geom, P, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, gradient=None):
+    """beRTAMC2D restatement: per-step ed [s, box], flux [s, box, 2], N [s].
+    `gradient` (K/nm): the homogeneous <gradient x y> source term."""
     lib = load()
     ms, k1 = _bt.mode_struct(modes)
     gs, k2 = _bt.geom_struct(geom)
@@ -302,7 +303,7 @@ def berta_run(modes, geom, P, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False):
     cnt = np.zeros(3, dtype=np.int64)
     Pa = np.ascontiguousarray(np.asfortranarray(P).ravel(order="F")) if P is not None else np.zeros(1)
     nmP = int(P.shape[0]) if P is not None else 0
-    bp = _bt.berta_params(dt, maxtime, Eeff, T0, seed, rta)
+    bp = _bt.berta_params(dt, maxtime, Eeff, T0, seed, rta, gradient=gradient)
     st = lib.oracle_berta_run(C.byref(ms), C.byref(gs), Pa.ctypes.data_as(C.POINTER(C.c_double)), nmP,
                               C.byref(bp), ed.ctypes.data_as(C.POINTER(C.c_double)),
                               flux.ctypes.data_as(C.POINTER(C.c_double)),

@@ -2506,10 +2506,34 @@ int oracle_berta_run(const bte_mode_table* mt, const bte_geometry* gm, const dou
             }
             parts.insert(parts.end(), np.begin(), np.end());
         };
+        // gradient source term (source_term_gradient, src/beyondRTA_MC2d.cpp:
+        // 597-676): the homogeneous <gradient> on every box that is neither a
+        // reservoir nor periodic; the generators are built once
+        std::vector<orc::GradGen> grad;
+        if (bp->gradient_mode == 1 &&
+            !orc::almost_equal(std::hypot(bp->gradient[0], bp->gradient[1]), 0.))
+            grad = orc::build_gradient(S, bp->gradient[0], bp->gradient[1]);
         while (time <= R.maxtime) {
             // 1. advection
             for (auto& p : parts) orc::be_evolve(R, p, orc::get_v(m, p.mode), R.dt, rng_);
             psteps += int64_t(parts.size());
+            // 2. gradient source: Ntogenerate(dt, vol, Eeff) particles per box at
+            // random points, mode and sign from the Nabla_T distribution
+            if (!grad.empty()) {
+                std::vector<orc::BeParticle> np;
+                for (auto& G : grad) {
+                    const std::size_t ngen = orc::n_to_generate(R.dt * G.energy / R.Eeff, rng);
+                    for (std::size_t i = 0; i < ngen; ++i) {
+                        orc::BeParticle p;
+                        p.pos = orc::random_point(S.sys[G.box], rng);
+                        p.mode = orc::lower_bound_idx(G.cdf, orc::canonical(rng));
+                        p.sign = G.sign[std::size_t(p.mode)];
+                        p.box = int(G.box);
+                        np.push_back(p);
+                    }
+                }
+                advect_new(np);
+            }
             // 3. isothermal walls
             {
                 std::vector<orc::BeParticle> np;

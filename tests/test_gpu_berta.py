@@ -105,3 +105,62 @@ def test_berta_periodic_bar_agrees_with_restatement(engine, rta):
     se = np.sqrt(gpu.var(0, ddof=1) / R + cpu.var(0, ddof=1) / R)
     z = np.abs(d) / np.maximum(se, 1e-300)
     assert z.max() < 4.5, (z, gpu.mean(0), cpu.mean(0))
+
+
+def test_berta_gradient_source_gives_bulk_kappa(engine):
+    """Homogeneous <gradient> source term in an infinite medium (periodic
+    boxes on all sides), RTA scattering: the flux follows the bulk
+    conductivity with the loop's discrete lifetime at every step."""
+    from test_berta_gradient_cpu import DT, GX, berta_kappa
+    m = synth.mode_table(9, 3, 3, 300.0, config=100, even=True)
+    g = synth.periodic_cell_geometry(40.0, 40.0, 2, 2)
+    engine.load_modes(m)
+    engine.load_geometry(g)
+    runs = [engine.berta_run(DT, 800.0, 1e-23, seed=40 + k, rta=True, gradient=(GX, 0.0)) for k in range(8)]
+    nrow = runs[0]["flux"].shape[0]
+    per = berta_kappa(runs, 200)
+    expect = synth.kappa_berta_steps(m, 300.0, DT, np.arange(200, nrow)).mean()
+    z = abs(per.mean() - expect) / (per.std(ddof=1) / np.sqrt(len(per)))
+    assert z < 4.5, (per, expect)
+
+
+def test_berta_gradient_with_propagator_agrees_with_restatement(engine):
+    """The gradient source with propagator scattering (sign branching) on
+    the periodic block: energy density and flux against the restatement."""
+    m = synth.mode_table(8, 3, 3, 300.0, config=100)
+    g = synth.periodic_cell_geometry(40.0, 40.0, 2, 2)
+    P = synth.propagator(m)
+    engine.load_modes(m)
+    engine.load_geometry(g)
+    engine.load_propagator(P)
+    R = 5
+    kw = dict(dt=1.0, maxtime=30.0, Eeff=1e-23, gradient=(0.01, 0.005))
+
+    def obs(r):
+        f = r["flux"][-10:, :4].mean(axis=(0, 1)) * 1e-8
+        return np.concatenate([f, [r["nparticles"][-1] * 1e-3]])
+    gpu = np.array([obs(engine.berta_run(seed=10 + i, **kw)) for i in range(R)])
+    cpu = np.array([obs(pyoracle.berta_run(m, g, P, seed=20 + i, **kw)) for i in range(R)])
+    d = gpu.mean(0) - cpu.mean(0)
+    se = np.sqrt(gpu.var(0, ddof=1) / R + cpu.var(0, ddof=1) / R)
+    z = np.abs(d) / np.maximum(se, 1e-300)
+    assert z.max() < 4.5, (z, gpu.mean(0), cpu.mean(0))
+
+
+def test_bertamc2d_cli_gradient_on_periodic_block(built, tmp_path):
+    import os
+    import subprocess
+    m = synth.mode_table(9, 3, 3, 300.0, config=100, even=True)
+    g = synth.periodic_cell_geometry(40.0, 40.0, 2, 2)
+    synth.write_geometry_xml(str(tmp_path / "block.xml"), g)
+    synth.write_modes_file(str(tmp_path / "modes.bin"), m)
+    (tmp_path / "input.xml").write_text(
+        '<beRTAMC2D>\n  <geometry file="block.xml"/>\n  <time dt="1.0" maxtime="20"/>\n'
+        '  <material name="synthetic" database="modes.bin" thickness="0.335"/>\n'
+        '  <RTA/>\n  <gradient x="0.01" y="0"/>\n  <Eeff Ed="1e-23"/>\n</beRTAMC2D>\n')
+    exe = os.path.join(os.path.dirname(built), "bertamc2d_gpu")
+    r = subprocess.run([exe, "input.xml", "4"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    rows = [ln.split("\t") for ln in r.stdout.splitlines() if ln and ln[0].isdigit()]
+    assert len(rows) == 21
+    assert int(rows[-1][2]) > 0                 # particles from the source term
