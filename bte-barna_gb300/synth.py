@@ -202,7 +202,8 @@ def kappa_rta(modes: dict, T: float, thickness: float = C_LAT) -> np.ndarray:
 
 
 def kappa_berta_steps(modes: dict, T: float, dt: float, steps, thickness: float = C_LAT) -> np.ndarray:
-    """Expected kappa_xx of the beRTAMC2D loop with RTA scattering and a
+    """Expected conductivity tensor [len(steps), 2, 2] of the beRTAMC2D loop
+    with RTA scattering and a
     homogeneous gradient source in an infinite medium, at output rows
     `steps` (row s follows s loop iterations).  A source particle is born
     in an iteration and meets the scattering test 1 - exp(-w dt) at the end
@@ -211,7 +212,7 @@ def kappa_berta_steps(modes: dict, T: float, dt: float, steps, thickness: float 
     flux), so tau_k becomes dt q (1 - q^s) / (1 - q), q = exp(-w_k dt), in
     the bulk formula."""
     om, w = modes["omega"], modes["w"]
-    v = modes["vg"].reshape(-1, 3)[:, 0]
+    v = modes["vg"].reshape(-1, 3)[:, :2]
     ok = (om > 0) & (w > 0)
     C = be_kernel(om[ok], T)
     q = np.exp(-w[ok] * dt)
@@ -220,7 +221,7 @@ def kappa_berta_steps(modes: dict, T: float, dt: float, steps, thickness: float 
     out = []
     for s_ in np.atleast_1d(steps):
         teff = dt * q * (1 - q ** float(s_)) / (1 - q)
-        out.append(1e21 * kB / (modes["nq"] * vuc) * (C * teff * v[ok] * v[ok]).sum())
+        out.append(1e21 * kB / (modes["nq"] * vuc) * np.einsum("k,ki,kj->ij", C * teff, v[ok], v[ok]))
     return np.array(out)
 
 

@@ -111,17 +111,13 @@ def test_berta_gradient_source_gives_bulk_kappa(engine):
     """Homogeneous <gradient> source term in an infinite medium (periodic
     boxes on all sides), RTA scattering: the flux follows the bulk
     conductivity with the loop's discrete lifetime at every step."""
-    from test_berta_gradient_cpu import DT, GX, berta_kappa
+    from test_berta_gradient_cpu import DT, GRAD, check_bulk
     m = synth.mode_table(9, 3, 3, 300.0, config=100, even=True)
     g = synth.periodic_cell_geometry(40.0, 40.0, 2, 2)
     engine.load_modes(m)
     engine.load_geometry(g)
-    runs = [engine.berta_run(DT, 800.0, 1e-23, seed=40 + k, rta=True, gradient=(GX, 0.0)) for k in range(8)]
-    nrow = runs[0]["flux"].shape[0]
-    per = berta_kappa(runs, 200)
-    expect = synth.kappa_berta_steps(m, 300.0, DT, np.arange(200, nrow)).mean()
-    z = abs(per.mean() - expect) / (per.std(ddof=1) / np.sqrt(len(per)))
-    assert z < 4.5, (per, expect)
+    runs = [engine.berta_run(DT, 800.0, 1e-23, seed=40 + k, rta=True, gradient=GRAD) for k in range(10)]
+    check_bulk(runs, m, 200, 4.5)
 
 
 def test_berta_gradient_with_propagator_agrees_with_restatement(engine):
@@ -133,7 +129,7 @@ def test_berta_gradient_with_propagator_agrees_with_restatement(engine):
     engine.load_modes(m)
     engine.load_geometry(g)
     engine.load_propagator(P)
-    R = 5
+    R = 12
     kw = dict(dt=1.0, maxtime=30.0, Eeff=1e-23, gradient=(0.01, 0.005))
 
     def obs(r):
