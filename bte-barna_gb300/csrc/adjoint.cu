@@ -33,9 +33,7 @@ bte_status bte_rta_adjoint(bte_ctx* c, const bte_rta_params* p, const double* we
         const bte_status st = prepared_grid_run(c, p, &r, &why);
         if (st != BTE_OK) throw Error(st, why);
         // time grid, src/RTA_MC2D.cpp:2118-2124
-        std::vector<double> grid(std::size_t(r.ntime));
-        for (int i = 0; i < r.ntime; ++i) grid[std::size_t(i)] = (i == r.ntime - 1) ? r.maxtime : double(i) * r.step;
-        c->d_time.upload(grid, c->stream);
+        c->d_time.upload(time_grid_with_widths(r.ntime, r.maxtime, r.step), c->stream);
         r.T.timegrid = c->d_time.as<double>();
         const std::size_t nk = std::size_t(r.nboxes) * std::size_t(r.nbins);
         const std::size_t n = c->modes.n();

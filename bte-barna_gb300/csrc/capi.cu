@@ -570,11 +570,12 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         const std::size_t ntime = std::size_t(std::floor(p->maxtime / p->dt + 1.0e-6)) + 1;
         if (ntime < 2) throw Error(BTE_ERR_INPUT, "maxtime shorter than one time bin");
         const double maxtime = double(ntime - 1) * p->dt;
-        c->h_time.resize(ntime);
         const double step = (maxtime - 0.0) / double(ntime - 1);
-        for (std::size_t i = 0; i < ntime; ++i)
-            c->h_time[i] = (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
-        c->d_time.upload(c->h_time, c->stream);
+        {
+            const std::vector<double> tg = bte::time_grid_with_widths(int(ntime), maxtime, step);
+            c->h_time.assign(tg.begin(), tg.begin() + std::ptrdiff_t(ntime));
+            c->d_time.upload(tg, c->stream);
+        }
         const int nbins = int(ntime - 1);
         const int nbx = int(g.boxes.size());
         const std::size_t nk = std::size_t(nbx) * std::size_t(nbins);
@@ -1043,6 +1044,13 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
     r->nsm = c->nsm;
     r->tune = c->tune;
     return BTE_OK;
+}
+
+std::vector<double> time_grid_with_widths(int ntime, double maxtime, double step) {
+    std::vector<double> g(std::size_t(2 * ntime - 1));
+    for (int i = 0; i < ntime; ++i) g[std::size_t(i)] = (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
+    for (int i = 0; i + 1 < ntime; ++i) g[std::size_t(ntime + i)] = g[std::size_t(i + 1)] - g[std::size_t(i)];
+    return g;
 }
 
 void fill_static_tables(bte_ctx* c, DevTables& T) {

@@ -128,4 +128,8 @@ void prepare_run(bte_ctx* c, const bte_rta_params* p);
 bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r, std::string* why);
 // Mode, geometry and Lambert tables of a context into the kernel tables.
 void fill_static_tables(bte_ctx* c, DevTables& T);
+// The ntime points of the time grid (src/RTA_MC2D.cpp:2118-2124: i * step,
+// the last exactly maxtime) followed by the ntime - 1 bin widths, the
+// layout DevTables::timegrid points to.
+std::vector<double> time_grid_with_widths(int ntime, double maxtime, double step);
 }  // namespace bte

@@ -40,7 +40,7 @@ void set_ctx_error(bte_ctx* c, const std::string& m);
 namespace {
 
 constexpr int kHeaderBytes = 256;  // counters (8 x u64), error word (4 x int), work counter
-constexpr size_t kScratchBytes = kHeaderBytes + sizeof(double) * (BTE_NOALLOC_MAX_BINS + 1);
+constexpr size_t kScratchBytes = kHeaderBytes + sizeof(double) * (2 * BTE_NOALLOC_MAX_BINS + 1);
 
 // The scratch of every allocation-free call.  Host code must not use the
 // symbol as an address; it asks the runtime for the device address below.
@@ -72,10 +72,16 @@ bool scratch_address(int device, unsigned char** out, std::string* why) {
 }
 
 // The time grid of src/RTA_MC2D.cpp:2118-2124 (LinSpaced: i * step, the
-// last point exactly maxtime), written into the scratch.
+// last point exactly maxtime) and its ntime - 1 bin widths after it, written
+// into the scratch.
+__device__ __forceinline__ double noalloc_point(int i, int ntime, double maxtime, double step) {
+    return (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
+}
 __global__ void noalloc_time_grid(double* grid, int ntime, double maxtime, double step) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ntime) grid[i] = (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
+    if (i < ntime) grid[i] = noalloc_point(i, ntime, maxtime, step);
+    if (i + 1 < ntime)
+        grid[ntime + i] = noalloc_point(i + 1, ntime, maxtime, step) - noalloc_point(i, ntime, maxtime, step);
 }
 
 bte_status fail(bte_ctx* c, bte_status s, const std::string& m) {

@@ -59,7 +59,7 @@ struct DevTables {
     const int* mirror;    // [nclass][n] or null
     // time grid
     int ntime;
-    const double* timegrid;
+    const double* timegrid;   // ntime points, then the ntime - 1 bin widths
     double maxtime;
     double inv_dt;        // 1 / bin width (production)
     // generators

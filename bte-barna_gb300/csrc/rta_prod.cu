@@ -218,25 +218,26 @@ __device__ __forceinline__ double widen_pos(float f) {
 
 // Pending tally of one lane.  Inside one (box, time bin) key the particle
 // moves continuously, so the key's contributions telescope: time spent =
-// t - t0 and the velocity-weighted sums are the displacement x - x0, y - y0
-// (sum of v * dt over the segments).  Nothing is accumulated per segment;
-// when the key changes the three differences go out as FP64 atomics, with
-// the particle sign applied to the sign bit.
+// r0 - r, r the time left to the bin's end, and the velocity-weighted sums
+// are the displacement x - x0, y - y0 (sum of v * dt over the segments).
+// Nothing is accumulated per segment; when the key changes the three
+// differences go out as FP64 atomics, with the particle sign applied to the
+// sign bit.
 struct Pending {
     int key;
     unsigned flushes;
-    double t0, x0, y0;
-    __device__ __forceinline__ void start(int k, double t, double x, double y) {
+    double r0, x0, y0;
+    __device__ __forceinline__ void start(int k, double r, double x, double y) {
         key = k;
-        t0 = t;
+        r0 = r;
         x0 = x;
         y0 = y;
     }
-    __device__ __forceinline__ void flush(double* tally, unsigned long long signbit, double t, double x,
+    __device__ __forceinline__ void flush(double* tally, unsigned long long signbit, double r, double x,
                                           double y) {
         if (key >= 0) {
             double* b = tally + 3ll * key;
-            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(t - t0) ^ signbit));
+            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(r0 - r) ^ signbit));
             atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(x - x0) ^ signbit));
             atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(y - y0) ^ signbit));
             flushes++;
@@ -330,10 +331,15 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     const int lane = threadIdx.x & 31;
     const long long total = T.pend - T.pbegin;
     const int last_bin = T.nbins - 1;
+    // specular draw on the integer pipe: u32 < p 2^32 (p >= 1: always);
+    // 0 when the walls are diffuse
+    const unsigned long long spec_thr =
+        T.specularity >= 1.0 ? (1ull << 32)
+                             : (T.specularity > 0. ? (unsigned long long)(T.specularity * 4294967296.0) : 0ull);
     Pending pd;
     pd.key = -1;
     pd.flushes = 0;
-    pd.t0 = pd.x0 = pd.y0 = 0.;
+    pd.r0 = pd.x0 = pd.y0 = 0.;
     GridParticle p;
     p.i = p.j = p.mode = p.box = p.mo = 0;
     p.sign = 1;
@@ -341,7 +347,10 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     Philox g;
     g.init(0, 0);
     ModeVel mv = {0., 0., 0., 0.};
-    double dt = 0., tnb = 0.;
+    // dt: time left in the free flight; rb: time left to the end of the
+    // current time bin (bin widths follow the ntime grid points)
+    const double* binw = T.timegrid + T.ntime;
+    double dt = 0., rb = 0.;
     long long pid = -1, nev = 0;
     int bin = 0;
     unsigned long long signbit = 0;
@@ -379,9 +388,9 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                             if (ADJ == 2) phi_tot = adj.phi_total[mine];
                         }
                         bin = 0;
-                        tnb = __ldg(T.timegrid + 1);
+                        rb = __ldg(binw);
                         signbit = p.sign < 0 ? 0x8000000000000000ull : 0ull;
-                        pd.start(p.box * T.nbins, 0., p.x, p.y);
+                        pd.start(p.box * T.nbins, rb, p.x, p.y);
                     }
                 } else {
                     done = true;
@@ -401,7 +410,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             if (ADJ == 2) {
                 // future contribution from here: Phi_total - (flushed + pending part)
                 const double* Wk = adj.W + 3ll * pd.key;
-                const double part = __ldg(Wk) * (p.t - pd.t0) + __ldg(Wk + 1) * (p.x - pd.x0) +
+                const double part = __ldg(Wk) * (pd.r0 - rb) + __ldg(Wk + 1) * (p.x - pd.x0) +
                                     __ldg(Wk + 2) * (p.y - pd.y0);
                 const double R = phi_tot - (phi_run + (p.sign < 0 ? -part : part));
                 double gk = (widen_pos(ef) - 1.0) / tau_k * R;
@@ -417,7 +426,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                 record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
                 active = false;
                 done = true;
-                pd.flush(tally, signbit, p.t, p.x, p.y);
+                pd.flush(tally, signbit, rb, p.x, p.y);
                 continue;
             }
             need_flight = false;
@@ -432,7 +441,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         const double yw = __ldg(A.G.gy + p.j + upy);
         const double tx = (xw - p.x) * mv.ivx;
         const double ty = (yw - p.y) * mv.ivy;
-        const double tb = tnb - p.t;
+        const double tb = rb;
         const bool xfirst = ob(tx) <= ob(ty);
         long long te_b = xfirst ? ob(tx) : ob(ty);
         long long tb_b = ob(tb);
@@ -445,11 +454,11 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         const bool wall = !flight_end && te_b <= tb_b;         // reaches a cell line
         const bool bin_end = tb_b <= seg_b;                    // reaches the bin border
         const double seg = obd(seg_b);
-        double t1 = p.t + seg;
+        double r1 = rb - seg;
         double nx = fma(seg, mv.vx, p.x);
         double ny = fma(seg, mv.vy, p.y);
         dt -= seg;
-        if (bin_end) t1 = tnb;
+        if (bin_end) r1 = 0.;
         int ni = p.i, nj = p.j, wside = 0;
         if (wall) {  // the crossed coordinate is the grid line
             if (xfirst) {
@@ -466,13 +475,13 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         if (ADJ == 0 && T.spec_loc) {
             const int loc = __ldg(T.spec_loc + p.box);
             if (loc >= 0) {
-                const double ds = t1 - p.t;
+                const double ds = rb - r1;
                 atomicAdd(T.spec + (long long)(loc * T.nbins + bin) * T.n + p.mode, p.sign < 0 ? -ds : ds);
             }
         }
         // differences of the pending tally at the segment end (telescoping)
-        const double d0 = t1 - pd.t0, d1 = nx - pd.x0, d2 = ny - pd.y0;
-        p.t = t1;
+        const double d0 = pd.r0 - r1, d1 = nx - pd.x0, d2 = ny - pd.y0;
+        rb = r1;
         p.x = nx;
         p.y = ny;
         int nb = p.box;
@@ -505,7 +514,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         }
         if (bin_end) {
             ++bin;
-            tnb = __ldg(T.timegrid + bin + 1);
+            rb = __ldg(binw + bin);
         }
         if (move) {
             p.i = ni;
@@ -513,7 +522,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             p.box = nb;
             c.crossings++;
         }
-        if (move || bin_end) pd.start(p.box * T.nbins + bin, t1, nx, ny);
+        if (move || bin_end) pd.start(p.box * T.nbins + bin, rb, nx, ny);
         if (reflect) {
             // (selects, not an indexed parameter array, which would live in local memory)
             const int cls = wside == 0 ? A.cls[0] : wside == 1 ? A.cls[1] : wside == 2 ? A.cls[2] : A.cls[3];
@@ -521,14 +530,14 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                 record_error(err, E_GEOM, pid);
                 active = false;
                 done = true;
-                pd.flush(tally, signbit, p.t, p.x, p.y);
+                pd.flush(tally, signbit, rb, p.x, p.y);
                 continue;
             }
             const int k = p.mode;
             int nm = -1;
             bool spec = false;
-            if (T.specularity > 0.) {
-                spec = g.uniform() < T.specularity;
+            if (spec_thr) {
+                spec = (unsigned long long)g.next32() < spec_thr;
                 if (ADJ == 2) {
                     spec_score = spec ? 1.0 / T.specularity : -1.0 / (1.0 - T.specularity);
                     pend_kind |= 2;
@@ -546,7 +555,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                     record_error(err, E_GEOM, pid);
                     active = false;
                     done = true;
-                    pd.flush(tally, signbit, p.t, p.x, p.y);
+                    pd.flush(tally, signbit, rb, p.x, p.y);
                     continue;
                 }
                 const int jj = int(mulhi32(g.next32(), uint32_t(len)));
