@@ -293,6 +293,22 @@ __device__ int grid_generate(const DevTables& T, const DevGrid& G, const int2* b
     return 0;
 }
 
+// The draws of one loop pass: Philox4x32-10 block (pass, 2^30, particle)
+// under the run's seed, a counter range the particle's generation draws
+// (counter words from 0) never reach.  Every active lane computes one block
+// per pass at the same point of the loop, so the generator runs with the
+// whole warp instead of once per call site that finds its queue empty.
+// x: the free flight, y and z: the alias draw (slot, acceptance), w: the
+// specular test.
+__device__ __forceinline__ uint4 pass_block(uint32_t pass, uint64_t pid, uint64_t seed) {
+    Philox q;
+    q.init(seed, pid);
+    q.c0 = pass;
+    q.c1 = 0x40000000u;
+    q.block();
+    return make_uint4(q.b0, q.b1, q.b2, q.b3);
+}
+
 // One lane carries one particle; each pass of the loop advances every active
 // lane by exactly one segment, which ends at the first of: the end of the
 // free flight, the next cell line, the next time-bin border (the last one is
@@ -303,7 +319,10 @@ __device__ int grid_generate(const DevTables& T, const DevGrid& G, const int2* b
 // GB300, never sees the same operation issued twice for different lanes.
 // Idle lanes take new particles from a global counter, one atomic per warp.
 // Comparisons, min/max and the float -> double widening run on the integer
-// pipe.
+// pipe.  The random words of a pass come from one Philox block per lane
+// (pass_block); a flight that ends at a void wall or by scattering draws
+// its next mode in one block for both cases (Lambert row or post-scattering
+// alias table), and the next pass draws the flight length.
 //
 // ADJ selects the two passes of the adjoint (ADJ = 0 is the plain kernel):
 // 1 forward: also accumulates each particle's contribution to a linear
@@ -352,6 +371,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     const double* binw = T.timegrid + T.ntime;
     double dt = 0., rb = 0.;
     long long pid = -1, nev = 0;
+    uint32_t npass = 0;
     int bin = 0;
     unsigned long long signbit = 0;
     bool active = false, done = false, need_flight = false;
@@ -381,6 +401,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                         active = true;
                         need_flight = true;
                         nev = 0;
+                        npass = 0;
                         if (ADJ) {
                             slot = mine;
                             phi_run = 0.;
@@ -399,11 +420,13 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         }
         if (__all_sync(0xffffffffu, done)) break;
         if (!active) continue;
+        const uint4 rr = pass_block(npass++, (uint64_t)pid, T.seed);
         if (need_flight) {
-            // a new free flight: u in (0, 1) -> dt = -tau ln u (FP32 log)
+            // a new free flight: u in (0, 1) -> dt = -tau ln u (FP32 log);
+            // u = (k + 1/2) 2^-23 from 23 bits, never 0 or 1
             const int k = p.mode;
             mv = A.mv[k];
-            const float ef = -logf(g.uniformf());
+            const float ef = -logf((float(rr.x >> 9) + 0.5f) * 0x1p-23f);
             const double tau_k = __ldg(T.tau + p.mo + k);
             dt = widen_pos(ef) * tau_k;
             c.events++;
@@ -523,54 +546,67 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             c.crossings++;
         }
         if (move || bin_end) pd.start(p.box * T.nbins + bin, rb, nx, ny);
-        if (reflect) {
-            // (selects, not an indexed parameter array, which would live in local memory)
-            const int cls = wside == 0 ? A.cls[0] : wside == 1 ? A.cls[1] : wside == 2 ? A.cls[2] : A.cls[3];
-            if (cls < 0) {
-                record_error(err, E_GEOM, pid);
-                active = false;
-                done = true;
-                pd.flush(tally, signbit, rb, p.x, p.y);
-                continue;
-            }
+        if (reflect || flight_end) {
+            // the next mode: a Lambert row at a void wall (or the mirror
+            // mode on a specular draw), the post-scattering table after a
+            // scattering (none for ballistic runs)
             const int k = p.mode;
-            int nm = -1;
-            bool spec = false;
-            if (spec_thr) {
-                spec = (unsigned long long)g.next32() < spec_thr;
-                if (ADJ == 2) {
-                    spec_score = spec ? 1.0 / T.specularity : -1.0 / (1.0 - T.specularity);
-                    pend_kind |= 2;
+            int nm = k;
+            if (reflect || !T.ballistic) {
+                float pr = 0.f;
+                int keep = k, alt = k;
+                if (reflect) {
+                    // (selects, not an indexed parameter array, which would live in local memory)
+                    const int cls =
+                        wside == 0 ? A.cls[0] : wside == 1 ? A.cls[1] : wside == 2 ? A.cls[2] : A.cls[3];
+                    if (cls < 0) {
+                        record_error(err, E_GEOM, pid);
+                        active = false;
+                        done = true;
+                        pd.flush(tally, signbit, rb, p.x, p.y);
+                        continue;
+                    }
+                    int mirror_mode = -1;
+                    if (spec_thr) {
+                        const bool spec = (unsigned long long)rr.w < spec_thr;
+                        if (ADJ == 2) {
+                            spec_score = spec ? 1.0 / T.specularity : -1.0 / (1.0 - T.specularity);
+                            pend_kind |= 2;
+                        }
+                        if (spec && T.mirror) mirror_mode = __ldg(T.mirror + (long long)cls * T.n + k);
+                    }
+                    if (mirror_mode >= 0) {
+                        c.specular++;
+                        pr = 2.f;  // keep = the mirror mode whatever the acceptance word
+                        keep = mirror_mode;
+                    } else {
+                        const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
+                        const long long bb = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
+                        const int len = int(bb - a);
+                        if (len <= 0) {
+                            record_error(err, E_GEOM, pid);
+                            active = false;
+                            done = true;
+                            pd.flush(tally, signbit, rb, p.x, p.y);
+                            continue;
+                        }
+                        const int4 e = __ldg(T.lalias + a + int(mulhi32(rr.y, uint32_t(len))));
+                        pr = __int_as_float(e.x);
+                        keep = e.y;
+                        alt = e.z;
+                    }
+                    c.wall_hits++;
+                } else {
+                    const int j = int(mulhi32(rr.y, uint32_t(T.n)));
+                    pr = __ldg(T.resample_prob + p.mo + j);
+                    keep = j;
+                    alt = __ldg(T.resample_alt + p.mo + j);
+                    if (ADJ == 2) pend_kind |= 1;
                 }
-            }
-            if (spec && T.mirror) {
-                nm = __ldg(T.mirror + (long long)cls * T.n + k);
-                if (nm >= 0) c.specular++;
-            }
-            if (nm < 0) {
-                const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
-                const long long bb = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
-                const int len = int(bb - a);
-                if (len <= 0) {
-                    record_error(err, E_GEOM, pid);
-                    active = false;
-                    done = true;
-                    pd.flush(tally, signbit, rb, p.x, p.y);
-                    continue;
-                }
-                const int jj = int(mulhi32(g.next32(), uint32_t(len)));
-                const int4 e = __ldg(T.lalias + a + jj);
-                const float acc = float(g.next32() >> 8) * 0x1p-24f;
-                nm = acc < __int_as_float(e.x) ? e.y : e.z;
+                const float acc = float(rr.z >> 8) * 0x1p-24f;
+                nm = acc < pr ? keep : alt;
             }
             p.mode = nm;
-            c.wall_hits++;
-            need_flight = true;
-        } else if (flight_end) {
-            if (!T.ballistic) {
-                p.mode = alias_draw(g, T.resample_prob + p.mo, T.resample_alt + p.mo, T.n);
-                if (ADJ == 2) pend_kind |= 1;
-            }
             need_flight = true;
         }
     }
