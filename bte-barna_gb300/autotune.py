@@ -8,7 +8,7 @@ leaves the fastest setting on the engine.  Runs before any timed region.
 import btegpu
 
 # (threads per block, blocks per SM, shared-memory tally)
-CANDIDATES = [(256, 3, 0), (256, 2, 0), (128, 6, 0), (128, 4, 0), (256, 1, 1)]
+CANDIDATES = [(256, 4, 0), (128, 8, 0), (256, 3, 0), (256, 2, 0), (128, 6, 0), (128, 4, 0), (256, 1, 1)]
 
 
 def tune(engine, run, trial_particles: int, smem_bytes: int, repeats: int = 2):

@@ -644,8 +644,9 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
     const size_t smem = size_t(3) * T.nboxes * T.nbins * sizeof(double);
     // the adjoint passes run with the tally in global memory
     const bool use_smem = tune.smem_tally != 0 && smem <= 200 * 1024 && adj_pass == 0;
-    // residency variants: 3 blocks of 256 threads per SM (80 registers) or
-    // 2 (no register cap); the shared-memory tally allows one block per SM
+    // residency variants: 4 blocks of 256 threads per SM (64 registers, a
+    // few spills), 3 (80 registers) or 2 (no register cap); the
+    // shared-memory tally allows one block per SM
     int bps = tune.blocks_per_sm > 0 ? tune.blocks_per_sm : (use_smem ? 1 : 3);
     const AdjArgs none{};
     const AdjArgs& aa = adj ? *adj : none;
@@ -659,6 +660,8 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 1>);
     } else if (adj_pass == 2) {
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 2>);
+    } else if (bps >= 4) {
+        fn = reinterpret_cast<const void*>(rta_prod_grid<false, 4, 0>);
     } else if (bps >= 3) {
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 3, 0>);
     } else {
@@ -679,6 +682,8 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
         rta_prod_grid<false, 2, 1><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
     else if (adj_pass == 2)
         rta_prod_grid<false, 2, 2><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
+    else if (fn == reinterpret_cast<const void*>(rta_prod_grid<false, 4, 0>))
+        rta_prod_grid<false, 4, 0><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
     else if (fn == reinterpret_cast<const void*>(rta_prod_grid<false, 3, 0>))
         rta_prod_grid<false, 3, 0><<<nb, threads, 0, s>>>(T, A, tally, counters, err, work, aa);
     else
