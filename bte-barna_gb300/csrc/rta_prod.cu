@@ -660,9 +660,9 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 1>);
     } else if (adj_pass == 2) {
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 2>);
-    } else if (bps >= 4) {
+    } else if (threads * bps > 768) {  // the register cap follows the resident threads
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 4, 0>);
-    } else if (bps >= 3) {
+    } else if (threads * bps > 512) {
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 3, 0>);
     } else {
         fn = reinterpret_cast<const void*>(rta_prod_grid<false, 2, 0>);
