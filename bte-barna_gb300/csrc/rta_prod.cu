@@ -322,7 +322,7 @@ __device__ __forceinline__ uint4 pass_block(uint32_t pass, uint64_t pid, uint64_
 // pipe.  The random words of a pass come from one Philox block per lane
 // (pass_block); a flight that ends at a void wall or by scattering draws
 // its next mode in one block for both cases (Lambert row or post-scattering
-// alias table), and the next pass draws the flight length.
+// alias table) and draws the next flight length there.
 //
 // ADJ selects the two passes of the adjoint (ADJ = 0 is the plain kernel):
 // 1 forward: also accumulates each particle's contribution to a linear
@@ -374,12 +374,47 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     uint32_t npass = 0;
     int bin = 0;
     unsigned long long signbit = 0;
-    bool active = false, done = false, need_flight = false;
+    bool active = false, done = false;
     // adjoint state: Phi so far, the particle's total, pending score terms
     double phi_run = 0., phi_tot = 0., spec_score = 0.;
     double sum_r = 0., g_p = 0., phi_all = 0.;
     long long slot = 0;
     int pend_kind = 0;
+    // A new free flight of the current mode from one random word:
+    // dt = -tau ln u (FP32 log), u = (k + 1/2) 2^-23 from 23 bits, never 0
+    // or 1; its velocities stay in registers for the segments that follow.
+    // Returns false when the particle stops with an error.
+    auto new_flight = [&](uint32_t word) -> bool {
+        const int k = p.mode;
+        mv = A.mv[k];
+        const float ef = -logf((float(word >> 9) + 0.5f) * 0x1p-23f);
+        const double tau_k = __ldg(T.tau + p.mo + k);
+        dt = widen_pos(ef) * tau_k;
+        c.events++;
+        if (ADJ == 2) {
+            // future contribution from here: Phi_total - (flushed + pending part)
+            const double* Wk = adj.W + 3ll * pd.key;
+            const double part = __ldg(Wk) * (pd.r0 - rb) + __ldg(Wk + 1) * (p.x - pd.x0) +
+                                __ldg(Wk + 2) * (p.y - pd.y0);
+            const double R = phi_tot - (phi_run + (p.sign < 0 ? -part : part));
+            double gk = (widen_pos(ef) - 1.0) / tau_k * R;
+            if (pend_kind & 1) {  // this mode came from a post-scattering draw
+                gk -= R / tau_k;
+                sum_r += R;
+            }
+            if (pend_kind & 2) g_p += spec_score * R;
+            pend_kind = 0;
+            atomicAdd(adj.g_tau + k, gk);
+        }
+        if (ob(dt) <= 0 || ++nev > EVENT_CAP) {  // zero rate or runaway particle
+            record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
+            active = false;
+            done = true;
+            pd.flush(tally, signbit, rb, p.x, p.y);
+            return false;
+        }
+        return true;
+    };
     for (;;) {
         // refill idle lanes of the warp with new particles
         const unsigned idle = __ballot_sync(0xffffffffu, !active && !done);
@@ -399,7 +434,6 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                         done = true;
                     } else {
                         active = true;
-                        need_flight = true;
                         nev = 0;
                         npass = 0;
                         if (ADJ) {
@@ -412,6 +446,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                         rb = __ldg(binw);
                         signbit = p.sign < 0 ? 0x8000000000000000ull : 0ull;
                         pd.start(p.box * T.nbins, rb, p.x, p.y);
+                        new_flight(g.next32());  // the first flight, from the generation stream
                     }
                 } else {
                     done = true;
@@ -420,40 +455,9 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         }
         if (__all_sync(0xffffffffu, done)) break;
         if (!active) continue;
+        // this pass's random words (used at its end); computed ahead of the
+        // segment, with which it shares no data
         const uint4 rr = pass_block(npass++, (uint64_t)pid, T.seed);
-        if (need_flight) {
-            // a new free flight: u in (0, 1) -> dt = -tau ln u (FP32 log);
-            // u = (k + 1/2) 2^-23 from 23 bits, never 0 or 1
-            const int k = p.mode;
-            mv = A.mv[k];
-            const float ef = -logf((float(rr.x >> 9) + 0.5f) * 0x1p-23f);
-            const double tau_k = __ldg(T.tau + p.mo + k);
-            dt = widen_pos(ef) * tau_k;
-            c.events++;
-            if (ADJ == 2) {
-                // future contribution from here: Phi_total - (flushed + pending part)
-                const double* Wk = adj.W + 3ll * pd.key;
-                const double part = __ldg(Wk) * (pd.r0 - rb) + __ldg(Wk + 1) * (p.x - pd.x0) +
-                                    __ldg(Wk + 2) * (p.y - pd.y0);
-                const double R = phi_tot - (phi_run + (p.sign < 0 ? -part : part));
-                double gk = (widen_pos(ef) - 1.0) / tau_k * R;
-                if (pend_kind & 1) {  // this mode came from a post-scattering draw
-                    gk -= R / tau_k;
-                    sum_r += R;
-                }
-                if (pend_kind & 2) g_p += spec_score * R;
-                pend_kind = 0;
-                atomicAdd(adj.g_tau + k, gk);
-            }
-            if (ob(dt) <= 0 || ++nev > EVENT_CAP) {  // zero rate or runaway particle
-                record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
-                active = false;
-                done = true;
-                pd.flush(tally, signbit, rb, p.x, p.y);
-                continue;
-            }
-            need_flight = false;
-        }
         // segment end.  A zero velocity component takes the upper cell line,
         // so (line - position) >= 0 times its +inf inverse gives +inf (or NaN
         // on the line, ordered above +inf); a negative value (a position that
@@ -607,7 +611,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                 nm = acc < pr ? keep : alt;
             }
             p.mode = nm;
-            need_flight = true;
+            if (!new_flight(rr.x)) continue;
         }
     }
     if (ADJ) {
