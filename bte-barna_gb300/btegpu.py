@@ -101,7 +101,8 @@ class SpectralResult(C.Structure):
                 ("omega", C.POINTER(C.c_double)), ("dT_omega", C.POINTER(C.c_double)),
                 ("jx_omega", C.POINTER(C.c_double)), ("jy_omega", C.POINTER(C.c_double)),
                 ("fd_q", C.POINTER(C.c_double)), ("q1bz", C.POINTER(C.c_double)),
-                ("raw", C.POINTER(C.c_double))]
+                ("raw", C.POINTER(C.c_double)), ("steady", C.c_int32), ("reserved0", C.c_int32),
+                ("counts", C.POINTER(C.c_double))]
 
 
 class AdjointResult(C.Structure):
@@ -442,23 +443,27 @@ def _engine_set_spectral(self, boxes, nomega=500):
     self._spec_nomega = int(nomega)
 
 
-def _engine_get_spectral(self, nbins):
-    """The last run's spectral outputs (arrays [nloc, nbins, ...])."""
+def _engine_get_spectral(self, nbins=1):
+    """The last run's spectral outputs (arrays [nloc, nbins, ...]; a steady
+    run has one bin and also returns `counts` [nloc, nmodes], the signed
+    segments per mode)."""
     nloc = len(self._keep["spectral"])
     nw = self._spec_nomega
     n = int(self._keep["modes"]["omega"].size)
-    nq = int(self._keep["modes"].get("nq", 0)) or n
     out = {"omega": np.zeros((nloc, nw)), "dT_omega": np.zeros((nloc, nbins, nw)),
            "jx_omega": np.zeros((nloc, nbins, nw)), "jy_omega": np.zeros((nloc, nbins, nw)),
-           "raw": np.zeros((nloc, nbins, n))}
+           "raw": np.zeros((nloc, nbins, n)), "counts": np.zeros((nloc, n))}
     r = SpectralResult()
-    for k in ("omega", "dT_omega", "jx_omega", "jy_omega", "raw"):
-        setattr(r, k, _dptr(out[k]))
     self._check(self.lib.bte_get_spectral(self.ctx, C.byref(r)))
+    if r.nbins != nbins:
+        raise ValueError(f"the last run has {r.nbins} spectral bins, not {nbins}")
+    for k in ("omega", "dT_omega", "jx_omega", "jy_omega", "raw", "counts"):
+        setattr(r, k, _dptr(out[k]))
     out["fd_q"] = np.zeros((nloc, nbins, r.nq))
     out["q1bz"] = np.zeros((r.nq, 2))
     r.fd_q, r.q1bz = _dptr(out["fd_q"]), _dptr(out["q1bz"])
     self._check(self.lib.bte_get_spectral(self.ctx, C.byref(r)))
+    out["steady"] = bool(r.steady)
     return out
 
 

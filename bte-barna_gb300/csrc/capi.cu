@@ -499,17 +499,21 @@ bte_status bte_get_spectral(bte_ctx* c, bte_spectral_result* out) {
             const double cv = bte::calc_cv(m, T0b);
             const double Eeff = c->spec_Eeff;
             std::vector<double> dT(nbins * nw, 0.), jx(nbins * nw, 0.), jy(nbins * nw, 0.), fq(nbins * nq, 0.);
+            const bool steady = c->spec_steady;
             for (std::size_t b = 0; b < nbins; ++b) {
                 const double* Tm = c->spec_raw.data() + (l * nbins + b) * n;
                 for (std::size_t k = 0; k < n; ++k) {
                     const double t = Tm[k];
+                    // fd_qmesh: time / omega (transient, :757), sign / omega
+                    // per segment (steady, :829)
+                    const double f = steady ? double(c->spec_cnt[l * n + k]) : t;
+                    if (f != 0. && m.omega[k] > 0.) fq[b * nq + k / nb] += f / m.omega[k];
                     if (t == 0.) continue;
                     for (auto& [i, wgt] : gw[k]) {
                         dT[b * nw + std::size_t(i)] += t * wgt;
                         jx[b * nw + std::size_t(i)] += m.vxc[k] * t * wgt;
                         jy[b * nw + std::size_t(i)] += m.vyc[k] * t * wgt;
                     }
-                    if (m.omega[k] > 0.) fq[b * nq + k / nb] += t / m.omega[k];
                 }
             }
             // scaling (:2350-2376) and integration in time (:2386-2413)
@@ -519,7 +523,7 @@ bte_status bte_get_spectral(bte_ctx* c, bte_spectral_result* out) {
             for (auto& x : jx) x *= sj;
             for (auto& x : jy) x *= sj;
             for (auto& x : fq) x *= sq;
-            for (std::size_t b = 1; b < nbins; ++b) {
+            for (std::size_t b = 1; b < nbins && !steady; ++b) {
                 for (std::size_t i = 0; i < nw; ++i) {
                     dT[b * nw + i] += dT[(b - 1) * nw + i];
                     jx[b * nw + i] += jx[(b - 1) * nw + i];
@@ -534,6 +538,9 @@ bte_status bte_get_spectral(bte_ctx* c, bte_spectral_result* out) {
             if (out->fd_q) std::copy(fq.begin(), fq.end(), out->fd_q + l * nbins * nq);
         }
         if (out->raw) std::copy(c->spec_raw.begin(), c->spec_raw.end(), out->raw);
+        out->steady = c->spec_steady ? 1 : 0;
+        if (out->counts && c->spec_steady)
+            for (std::size_t i = 0; i < c->spec_cnt.size(); ++i) out->counts[i] = double(c->spec_cnt[i]);
         if (out->q1bz) {
             // q points in Cartesian coordinates, reduced coordinates wrapped
             // to [-1/2, 1/2) (a Gamma-centred n1 x n2 grid, iq = i n2 + j)
@@ -724,6 +731,8 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
             }
             c->spec_nbins = nbins;
             c->spec_T0 = p->T0;
+            c->spec_steady = false;
+            c->spec_cnt.clear();
             c->spec_valid = true;
         }
         float ms = 0;

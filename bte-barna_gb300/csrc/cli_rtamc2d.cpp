@@ -243,6 +243,54 @@ void write_spectral(bte_ctx* ctx, const std::vector<int32_t>& boxes, int nw, int
     }
 }
 
+// The spectral CSVs of one steady run (src/RTA_MC2D.cpp:2775-2830): per
+// location steady_deltaT_omega_, steady_jx_omega_, steady_jy_omega_ with
+// the omega ticks on the first row and the values on the second, and
+// steady_fd_q_ with the two q-coordinate header lines, the one data row
+// left on the third "# " line as in the transient writer.
+void write_spectral_steady(bte_ctx* ctx, const std::vector<int32_t>& boxes, int nw, const std::string& T0s,
+                           long irun) {
+    bte_spectral_result r{};
+    check(ctx, bte_get_spectral(ctx, &r), "spectral outputs");
+    const std::size_t nloc = boxes.size(), nq = std::size_t(r.nq);
+    std::vector<double> om(nloc * nw), dT(nloc * nw), jx(dT.size()), jy(dT.size()), fq(nloc * nq), q(2 * nq);
+    r.omega = om.data();
+    r.dT_omega = dT.data();
+    r.jx_omega = jx.data();
+    r.jy_omega = jy.data();
+    r.fd_q = fq.data();
+    r.q1bz = q.data();
+    check(ctx, bte_get_spectral(ctx, &r), "spectral outputs");
+    std::cout << "# Writing spectral decompositions" << std::endl;
+    for (std::size_t l = 0; l < nloc; ++l) {
+        const std::string tail = std::to_string(boxes[l]) + "_" + T0s + "K_run_" + std::to_string(irun) + ".csv";
+        auto two_rows = [&](const std::string& name, const std::vector<double>& data) {
+            std::ofstream o(name + tail);
+            if (!o) throw std::runtime_error("cannot write " + name + tail);
+            for (int i = 0; i < nw; ++i) o << (i ? "," : "") << om[l * nw + std::size_t(i)];
+            o << '\n';
+            for (int i = 0; i < nw; ++i) o << (i ? "," : "") << data[l * nw + std::size_t(i)];
+            o << '\n';
+        };
+        two_rows("steady_deltaT_omega_", dT);
+        {
+            std::ofstream o("steady_fd_q_" + tail);
+            if (!o) throw std::runtime_error("cannot write steady_fd_q_" + tail);
+            for (int a = 0; a < 2; ++a) {
+                o << "# ";
+                for (std::size_t iq = 0; iq < nq; ++iq)
+                    o << (iq ? "," : "") << std::to_string(q[2 * iq + std::size_t(a)]);
+                o << '\n';
+            }
+            o << "# ";
+            for (std::size_t iq = 0; iq < nq; ++iq) o << (iq ? "," : "") << fq[l * nq + iq];
+            o << '\n';
+        }
+        two_rows("steady_jx_omega_", jx);
+        two_rows("steady_jy_omega_", jy);
+    }
+}
+
 void check(bte_ctx* ctx, bte_status s, const char* what) {
     if (s != BTE_OK) {
         char buf[512];
@@ -439,6 +487,7 @@ int main(int argc, char** argv) {
                     for (int b = 0; b < nbx; ++b) o << (b ? "," : "") << (*row)[std::size_t(b)];
                     o << '\n';
                 }
+                if (!spec_boxes.empty()) write_spectral_steady(ctx, spec_boxes, spec_ticks, fmt_g(T0), irun);
             }
             return 0;
         }

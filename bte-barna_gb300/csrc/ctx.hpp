@@ -100,6 +100,9 @@ struct bte_ctx {
     int spec_nomega = 0;
     bte::DBuf d_specloc, d_spec;
     std::vector<double> spec_raw;      // [nloc][nbins][n] of the last run
+    bte::DBuf d_speccnt;
+    std::vector<long long> spec_cnt;   // steady runs: signed segments [nloc][n]
+    bool spec_steady = false;
     int spec_nbins = 0;
     double spec_Eeff = 0., spec_T0 = 0.;
     bool spec_valid = false;

@@ -83,6 +83,7 @@ struct DevTables {
     const int* spec_loc;
     double* spec;
     unsigned long long* spec_ex;
+    unsigned long long* spec_cnt;  // steady state: signed segments per [loc][mode]
 };
 
 struct Counters {
@@ -303,7 +304,7 @@ __device__ int translate(const DevTables& T, P& pol, int box, V2 r0, V2 v, int& 
 // box, :784-834).
 template <bool STEADY, class P>
 __device__ __forceinline__ int seg_tally(const DevTables& T, P& pol, const Particle& p, double d, V2 v) {
-    if (STEADY) return pol.tally_dt(T, p.box, d, p.sign, v);
+    if (STEADY) return pol.tally_dt(T, p.box, d, p.sign, v, p.mode);
     return pol.tally(T, p.box, p.t, p.t + d, p.sign, v, p.mode);
 }
 

@@ -78,13 +78,18 @@ struct ProdPolicy {
         return alias_draw(g, prob, alt, n);
     }
     // process_segment (periodic), src/RTA_MC2D.cpp:784-834
-    __device__ int tally_dt(const DevTables& T, int box, double d, int sign, V2 v) {
-        (void)T;
+    __device__ int tally_dt(const DevTables& T, int box, double d, int sign, V2 v, int mode) {
         const double contr = double(sign) * d;
         double* base = out + 3ll * box;
         atomicAdd(base + 0, contr);
         atomicAdd(base + 1, v.x * contr);
         atomicAdd(base + 2, v.y * contr);
+        const int loc = T.spec_loc ? __ldg(T.spec_loc + box) : -1;
+        if (loc >= 0) {
+            const long long o = (long long)loc * T.n + mode;
+            atomicAdd(T.spec + o, contr);
+            atomicAdd(T.spec_cnt + o, (unsigned long long)(long long)sign);
+        }
         ntally++;
         return 0;
     }

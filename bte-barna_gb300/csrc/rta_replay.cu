@@ -56,9 +56,10 @@ struct ReplayPolicy {
     __device__ int dist(const double* cdf, const float*, const int*, int n) {
         return lower_bound_d(cdf, n, u());
     }
-    // process_segment (periodic), src/RTA_MC2D.cpp:784-834: one value per box
-    __device__ int tally_dt(const DevTables& T, int box, double d, int sign, V2 v) {
-        (void)T;
+    // process_segment (periodic), src/RTA_MC2D.cpp:784-834: one value per box;
+    // at a spectral location also the mode's time and its signed segment
+    // count (fd_qmesh adds contr / omega per segment there, not per time)
+    __device__ int tally_dt(const DevTables& T, int box, double d, int sign, V2 v, int mode) {
         const double contr = double(sign);
         long long q0, q1, q2;
         if (!quantise(contr * d, q0) || !quantise(v.x * contr * d, q1) || !quantise(v.y * contr * d, q2))
@@ -67,6 +68,12 @@ struct ReplayPolicy {
         add128(base + 0, q0);
         add128(base + 2, q1);
         add128(base + 4, q2);
+        const int loc = T.spec_loc ? T.spec_loc[box] : -1;
+        if (loc >= 0) {
+            const long long o = (long long)loc * T.n + mode;
+            add128(T.spec_ex + 2 * o, q0);
+            atomicAdd(T.spec_cnt + o, (unsigned long long)(long long)sign);
+        }
         ntally++;
         return 0;
     }

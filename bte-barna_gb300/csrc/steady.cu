@@ -241,6 +241,25 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         T.seed = p->seed;
         T.nbins = 1;
         T.specularity = p->specularity;
+        // spectral decomposition at the selected boxes: per-mode time and
+        // signed segment counts, summed over every generation
+        const size_t nloc = c->spec_boxes.size();
+        const size_t spec_vals = nloc * size_t(n);
+        c->spec_valid = false;
+        if (nloc > 0) {
+            std::vector<int> loc(size_t(nbx), -1);
+            for (size_t i = 0; i < nloc; ++i) loc[size_t(c->spec_boxes[i])] = int(i);
+            c->d_specloc.upload(loc, st);
+            const size_t bytes = spec_vals * (replay ? 2 * sizeof(unsigned long long) : sizeof(double));
+            c->d_spec.alloc(bytes);
+            c->d_speccnt.alloc(spec_vals * sizeof(unsigned long long));
+            ck(cudaMemsetAsync(c->d_spec.p, 0, bytes, st), "memset");
+            ck(cudaMemsetAsync(c->d_speccnt.p, 0, spec_vals * sizeof(unsigned long long), st), "memset");
+            T.spec_loc = c->d_specloc.as<int>();
+            T.spec = c->d_spec.as<double>();
+            T.spec_ex = c->d_spec.as<unsigned long long>();
+            T.spec_cnt = c->d_speccnt.as<unsigned long long>();
+        }
 
         SteadyArgs A{};
         A.exg0 = exg0;
@@ -383,7 +402,34 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         std::vector<unsigned long long> hc(16);
         ck(cudaMemcpyAsync(hc.data(), S.counters.p, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            st), "d2h");
+        std::vector<unsigned long long> hspec, hcnt;
+        if (nloc > 0) {
+            hspec.resize(replay ? 2 * spec_vals : spec_vals);
+            hcnt.resize(spec_vals);
+            ck(cudaMemcpyAsync(hspec.data(), c->d_spec.p, hspec.size() * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st), "d2h");
+            ck(cudaMemcpyAsync(hcnt.data(), c->d_speccnt.p, spec_vals * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st), "d2h");
+        }
         ck(cudaStreamSynchronize(st), "counters");
+        if (nloc > 0) {
+            c->spec_raw.resize(spec_vals);
+            c->spec_cnt.resize(spec_vals);
+            for (size_t i = 0; i < spec_vals; ++i) {
+                if (replay) {
+                    const __int128 v = (__int128)(((unsigned __int128)hspec[2 * i] << 64) | hspec[2 * i + 1]);
+                    c->spec_raw[i] = double(v) / FIX_SCALE;
+                } else {
+                    std::memcpy(&c->spec_raw[i], &hspec[i], sizeof(double));
+                }
+                c->spec_cnt[i] = (long long)hcnt[i];
+            }
+            c->spec_nbins = 1;
+            c->spec_T0 = p->T0;
+            c->spec_Eeff = Eeff;
+            c->spec_steady = true;
+            c->spec_valid = true;
+        }
         out->nboxes = nbx;
         out->generations = gen;
         out->converged = converged;

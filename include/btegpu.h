@@ -361,17 +361,21 @@ bte_status bte_rta_adjoint(bte_ctx* ctx, const bte_rta_params* params, const dou
 
 /* Spectral decomposition at selected boxes (<spectral><resolution
  * ticks=/><location bin=/>..., src/RTA_MC2D.cpp:150-175, :699-766,
- * :1979-2052): the following bte_rta_run calls also tally, per location,
- * time bin and mode, the time spent there; bte_get_spectral turns the last
- * run's tally into the reference's four outputs (:2350-2420, :2473-2541).
- * nloc = 0 switches it off. */
+ * :1979-2052): the following bte_rta_run and bte_steady_run calls also
+ * tally, per location, time bin and mode, the time spent there (a steady
+ * run has one bin and also counts the signed segments per mode,
+ * process_segment :784-834); bte_get_spectral turns the last run's tally
+ * into the reference's four outputs (transient :2350-2420, :2473-2541;
+ * steady :2729-2830).  nloc = 0 switches it off. */
 bte_status bte_set_spectral(bte_ctx* ctx, int32_t nloc, const int32_t* boxes, int32_t nomega);
 
-/* Spectral outputs of the last run, each [nloc][nbins][...] and cumulated
- * in time as the reference writes them:
+/* Spectral outputs of the last run, each [nloc][nbins][...], cumulated in
+ * time after a transient run as the reference writes them (a steady run has
+ * nbins = 1 and no cumulation):
  *   dT_omega  Gamma-pdf weighted temperature per omega tick (deltaT_omega_*.csv)
  *   jx_omega, jy_omega  the flux per omega tick (jx_omega_*, jy_omega_*.csv)
- *   fd_q      the distribution per q point (fd_q_*.csv)
+ *   fd_q      the distribution per q point (fd_q_*.csv); after a steady run
+ *             the reference adds sign / omega per segment, not per time
  * with omega[nloc][nomega] the tick centres and q1bz[nq][2] the q points.
  * Any pointer may be NULL. */
 typedef struct bte_spectral_result {
@@ -383,6 +387,9 @@ typedef struct bte_spectral_result {
     double* fd_q;
     double* q1bz;
     double* raw;     /* [nloc][nbins][nmodes] sign-weighted time per mode (unscaled) */
+    int32_t steady;  /* out: 1 when the last run was a steady-state run      */
+    int32_t reserved0;
+    double* counts;  /* [nloc][nmodes] signed segments per mode (steady runs) */
 } bte_spectral_result;
 
 bte_status bte_get_spectral(bte_ctx* ctx, bte_spectral_result* out);

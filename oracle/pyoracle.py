@@ -57,6 +57,8 @@ def load():
     lib.oracle_set_spectral.argtypes = [C.c_int, C.POINTER(C.c_int)]
     lib.oracle_spectral_raw.argtypes = [C.POINTER(C.c_int64), C.c_longlong]
     lib.oracle_spectral_raw.restype = C.c_longlong
+    lib.oracle_spectral_counts.argtypes = [C.POINTER(C.c_int64), C.c_longlong]
+    lib.oracle_spectral_counts.restype = C.c_longlong
     lib.oracle_steady_run.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
                                       C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult)]
     lib.oracle_steady_run.restype = C.c_int
@@ -155,7 +157,7 @@ def mode_sigmas(modes):
     return np.maximum(sig, lbound)
 
 
-def spectral_post(modes, raw, nomega):
+def spectral_post(modes, raw, nomega, counts=None):
     """Post-processing of the per-mode time tally raw[loc, bin, mode]
     (src/RTA_MC2D.cpp:2041-2045, :719-766, :2386-2413) before the constant
     scalings: the omega ticks, and the time integrals of sum_k t_k g_k(w),
@@ -175,13 +177,29 @@ def spectral_post(modes, raw, nomega):
         x = grid / th
         lp = (kk - 1.0) * np.log(x) - x - lgamma(kk) - np.log(th)
         W[k] = np.where(lp > -700.0, np.exp(np.maximum(lp, -700.0)), 0.0)
+    inv = np.where(om > 0, 1.0 / np.where(om > 0, om, 1.0), 0.0)
+    fq = np.zeros(raw.shape[:2] + (om.size // nb,))
+    if counts is not None:
+        # steady state (:2729-2830): one bin, no time integration, and
+        # fd_qmesh from the signed segment counts (sign / omega per segment)
+        np.add.at(fq, (slice(None), slice(None), np.arange(om.size) // nb), counts[:, None, :] * inv)
+        return grid, raw @ W, (raw * v[:, 0]) @ W, (raw * v[:, 1]) @ W, fq
     dT = np.cumsum(raw @ W, axis=1)
     jx = np.cumsum((raw * v[:, 0]) @ W, axis=1)
     jy = np.cumsum((raw * v[:, 1]) @ W, axis=1)
-    fq = np.zeros(raw.shape[:2] + (om.size // nb,))
-    inv = np.where(om > 0, 1.0 / np.where(om > 0, om, 1.0), 0.0)
     np.add.at(fq, (slice(None), slice(None), np.arange(om.size) // nb), raw * inv)
     return grid, dT, jx, jy, np.cumsum(fq, axis=1)
+
+
+def spectral_counts(shape):
+    """The last steady run's signed segment counts per mode [loc, mode]."""
+    lib = load()
+    n = int(np.prod(shape))
+    out = np.zeros(tuple(shape), dtype=np.int64)
+    got = lib.oracle_spectral_counts(out.ctypes.data_as(C.POINTER(C.c_int64)), n)
+    if got != n:
+        raise ValueError(f"spectral counts have {got} values, expected {n}")
+    return out
 
 
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,

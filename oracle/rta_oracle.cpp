@@ -722,6 +722,7 @@ struct Tally {
     const std::vector<int>* loc = nullptr;
     std::size_t nmodes = 0;
     std::vector<__int128> spec;
+    std::vector<int64_t> scnt;  // steady: signed segments per [loc][mode]
     int64_t events = 0, wall_hits = 0, crossings = 0, absorbed = 0, nudges = 0,
             quirks = 0, specular = 0, translations = 0;
     void init(std::size_t nbx, std::size_t nbn) {
@@ -1220,11 +1221,19 @@ struct SteadyGen {
 };
 
 // process_segment (periodic), src/RTA_MC2D.cpp:784-834.
-inline void process_segment_steady(Tally& T, std::size_t ibox, int sign, double dt, V2 vg) {
+inline void process_segment_steady(Tally& T, std::size_t ibox, int sign, double dt, V2 vg,
+                                   std::size_t mode) {
     double contr = double(sign);
     T.ex[3 * ibox + 0] += quant(contr * dt);
     T.ex[3 * ibox + 1] += quant(vg.x * contr * dt);
     T.ex[3 * ibox + 2] += quant(vg.y * contr * dt);
+    // spectral location: the mode's time and, for fd_qmesh (contr / omega
+    // once per segment, :829), its signed segment count
+    const int lc = T.loc ? (*T.loc)[ibox] : -1;
+    if (lc >= 0) {
+        T.spec[std::size_t(lc) * T.nmodes + mode] += quant(contr * dt);
+        T.scnt[std::size_t(lc) * T.nmodes + mode] += sign;
+    }
 }
 
 enum Fate { F_LOST = 0, F_SCATTER = 1, F_BOUNCE = 2, F_ABSORBED = 3 };
@@ -1254,7 +1263,7 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
     if (box.inside(rnew)) {
         p.pos = rnew;
         p.t += dt;
-        process_segment_steady(T, p.box, p.sign, dt, v);  // evalphi: phi += sign
+        process_segment_steady(T, p.box, p.sign, dt, v, p.q * nb + p.alpha);  // evalphi: phi += sign
         dt = 0.;
         fate = F_SCATTER;
         return;
@@ -1286,7 +1295,7 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
             pboxes.push_back(test);
     }
     if (pboxes.empty()) {
-        process_segment_steady(T, p.box, p.sign, tf, v);
+        process_segment_steady(T, p.box, p.sign, tf, v, p.q * nb + p.alpha);
         p.t += tf;
         std::vector<std::size_t> ids;
         for (auto& g : S.sys)
@@ -1343,12 +1352,12 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
     } else if (pboxes.size() == 1) {
         p.pos = rnew;
         p.t += tf;
-        process_segment_steady(T, p.box, p.sign, tf, v);
+        process_segment_steady(T, p.box, p.sign, tf, v, p.q * nb + p.alpha);
         p.box = pboxes[0];
         T.crossings++;
         return;
     } else {
-        process_segment_steady(T, p.box, p.sign, tf, v);
+        process_segment_steady(T, p.box, p.sign, tf, v, p.q * nb + p.alpha);
         p.t += tf;
         p.pos = rnew;
         std::vector<std::size_t> pbox2;
@@ -1924,6 +1933,7 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
 namespace {
 std::vector<int> g_spec_boxes;      // spectral locations of the following runs
 std::vector<__int128> g_spec_last;  // the last run's per-mode tally
+std::vector<int64_t> g_spec_cnt;     // the last steady run's signed segment counts
 }  // namespace
 
 // Spectral locations for the following oracle_rta_run calls (nloc = 0: off).
@@ -1941,6 +1951,14 @@ long long oracle_spectral_raw(int64_t* out, long long cap) {
             out[2 * i] = int64_t(uint64_t(u >> 64));
             out[2 * i + 1] = int64_t(uint64_t(u));
         }
+    return n;
+}
+
+// The last steady run's signed segment counts per [loc][mode].
+long long oracle_spectral_counts(int64_t* out, long long cap) {
+    const long long n = (long long)g_spec_cnt.size();
+    if (out && cap >= n)
+        for (long long i = 0; i < n; ++i) out[i] = g_spec_cnt[std::size_t(i)];
     return n;
 }
 
@@ -2209,6 +2227,12 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
 
         std::vector<__int128> ex(3 * nbx, 0);
         std::vector<double> oldv(3 * nbx, 0.), cur(3 * nbx, 0.);
+        // spectral locations: per-mode time and segment counts over all generations
+        std::vector<int> locs(nbx, -1);
+        for (std::size_t i = 0; i < g_spec_boxes.size(); ++i) locs[std::size_t(g_spec_boxes[i])] = int(i);
+        const std::size_t nspec = g_spec_boxes.size() * S.m.n();
+        std::vector<__int128> spec_tot(nspec, 0);
+        std::vector<int64_t> cnt_tot(nspec, 0);
         std::vector<orc::Particle> carry;
         std::vector<std::size_t> bbox;
         std::vector<int> bsign;
@@ -2238,6 +2262,12 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
             auto work = [&](int tid) {
                 orc::Tally& T = tl[std::size_t(tid)];
                 T.init(nbx, 1);
+                if (nspec > 0) {
+                    T.loc = &locs;
+                    T.nmodes = S.m.n();
+                    T.spec.assign(nspec, 0);
+                    T.scnt.assign(nspec, 0);
+                }
                 std::vector<int64_t>& phi = phis[std::size_t(tid)];
                 phi.assign(nbx, 0);
                 const int64_t lo = nslots * tid / nthreads, hi = nslots * (tid + 1) / nthreads;
@@ -2300,6 +2330,10 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
             std::vector<int64_t> phi(nbx, 0);
             for (auto& T : tl) {
                 for (std::size_t k = 0; k < 3 * nbx; ++k) ex[k] += T.ex[k];
+                for (std::size_t k = 0; k < nspec; ++k) {
+                    spec_tot[k] += T.spec[k];
+                    cnt_tot[k] += T.scnt[k];
+                }
                 ev += T.events;
                 wh += T.wall_hits;
                 cr += T.crossings;
@@ -2370,6 +2404,8 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
         out->births = births_total;
         out->lost = lost;
         out->kernel_ms = 0.;
+        g_spec_last = spec_tot;
+        g_spec_cnt = cnt_tot;
         if (out->exact)
             for (std::size_t k = 0; k < 3 * nbx; ++k) {
                 unsigned __int128 u = (unsigned __int128)ex[k];
