@@ -12,7 +12,8 @@
 //     the J(T) cubic spline (adiabatic_diffuse_walls :281-435)    be_generate
 //   5 deletion                                                  be_compact
 //   6 propagator scattering with sign branching (Scattering :1073-1210,
-//     propagator_H::get src/collision_operator.cpp:892-903), or the RTA
+//     propagator_H::get src/collision_operator.cpp:892-903), each parent's
+//     branching attempts made in place by its thread, or the RTA
 //     alternative (ScatteringRTA :983-1062)          be_scatter / be_scatter_rta
 //   7 histogram H[box][mode] += sign                            be_hist
 //   8 cancellation every 4th step: keep |H| particles of the majority sign
@@ -78,7 +79,6 @@ struct BertaState {
     long long cap = 0;
     DBuf a_x, a_y, a_mode, a_box, a_sign;   // particles
     DBuf b_x, b_y, b_mode, b_box, b_sign;   // compaction / scattering output
-    DBuf q_x, q_y, q_mode, q_box, q_sign;   // branching queues (two halves)
     DBuf d_H, d_cnt, d_Eb, d_props, d_counts, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
@@ -482,33 +482,47 @@ __global__ void be_compact(PArr in, long long n, PArr out, unsigned long long* c
     }
 }
 
-// One branching round of the propagator scattering: every input particle
-// draws its next mode from its column; the outgoing particle is appended to
-// `out`; a sign flip sends two copies of the parent to `queue`.
+// Propagator scattering with sign branching (Scattering, src/beyondRTA_MC2d.cpp:
+// 1073-1210).  Every scattering attempt of a parent draws its next mode from
+// the parent's column and emits one outgoing particle; when the drawn sign
+// differs from the parent's, the reference puts two copies of the parent
+// back into the queue, and each copy makes an attempt of its own.  The copies
+// are identical to the parent, so here a thread keeps only the number of
+// attempts its parent still owes and makes them in place, with fresh draws,
+// until none is left: one launch per step instead of one per round.  The
+// outgoing particles are appended warp by warp.  BRANCH_CAP bounds the
+// attempts of one parent (a supercritical propagator never stops).
+constexpr unsigned BRANCH_CAP = 1u << 20;
+
 __global__ void be_scatter(PArr in, long long n, PArr out, unsigned long long* ocount, long long ocap,
-                           PArr queue, unsigned long long* qcount, long long qcap, const PAlias* pal,
-                           int nm, unsigned long long key, int* err) {
+                           unsigned long long* nflips, const PAlias* pal, int nm, unsigned long long key,
+                           int* err) {
     const int lane = threadIdx.x & 31;
+    unsigned long long flips = 0;
     for (long long base = blockIdx.x * (long long)blockDim.x; base < n;
          base += (long long)gridDim.x * blockDim.x) {
         const long long i = base + threadIdx.x;
         const bool on = i < n;
-        int mode = 0, sign = 1, box = 0, nmode = 0, nsign = 1;
+        int mode = 0, sign = 1, box = 0;
         double x = 0., y = 0.;
+        unsigned todo = 0, made = 0;
         if (on) {
             mode = in.mode[i];
             sign = in.sign[i];
             box = in.box[i];
             x = in.x[i];
             y = in.y[i];
-            const int col = mode - 3;
-            if (col < 0 || col >= nm) {
-                atomicCAS(err, 0, E_VALUE);
-                nmode = mode;
-                nsign = sign;
-            } else {
-                Philox g;
-                g.init(key, (uint64_t)i);
+            todo = 1;
+        }
+        const int col = mode - 3;
+        const bool valid = col >= 0 && col < nm;
+        if (on && !valid) atomicCAS(err, 0, E_VALUE);
+        Philox g;
+        g.init(key, (uint64_t)(on ? i : 0));
+        while (__any_sync(0xffffffffu, todo > 0)) {
+            const bool act = todo > 0;
+            int nmode = mode, nsign = sign;
+            if (act && valid) {
                 const int j = int(mulhi32(g.next32(), uint32_t(nm)));
                 const float acc = float(g.next32() >> 8) * 0x1p-24f;
                 const PAlias e = pal[(long long)col * nm + j];
@@ -518,45 +532,36 @@ __global__ void be_scatter(PArr in, long long n, PArr out, unsigned long long* o
                 nmode = slot + 3;
                 nsign = neg ? -sign : sign;
             }
-        }
-        // append the outgoing particle
-        const unsigned m1 = __ballot_sync(0xffffffffu, on);
-        unsigned long long w = 0;
-        if (lane == 0 && m1) w = atomicAdd(ocount, (unsigned long long)__popc(m1));
-        w = __shfl_sync(0xffffffffu, w, 0);
-        if (on) {
-            const long long o = (long long)w + __popc(m1 & ((1u << lane) - 1u));
-            if (o < ocap) {
-                out.x[o] = x;
-                out.y[o] = y;
-                out.box[o] = box;
-                out.mode[o] = nmode;
-                out.sign[o] = nsign;
-            } else {
-                atomicCAS(err, 0, E_LIMIT);
-            }
-        }
-        // a sign flip re-enters two copies of the parent
-        const bool flip = on && nsign != sign;
-        const unsigned m2 = __ballot_sync(0xffffffffu, flip);
-        unsigned long long q = 0;
-        if (lane == 0 && m2) q = atomicAdd(qcount, 2ull * __popc(m2));
-        q = __shfl_sync(0xffffffffu, q, 0);
-        if (flip) {
-            const long long o = (long long)q + 2ll * __popc(m2 & ((1u << lane) - 1u));
-            if (o + 1 < qcap) {
-                for (int c2 = 0; c2 < 2; ++c2) {
-                    queue.x[o + c2] = x;
-                    queue.y[o + c2] = y;
-                    queue.box[o + c2] = box;
-                    queue.mode[o + c2] = mode;
-                    queue.sign[o + c2] = sign;
+            // append the outgoing particle of this attempt
+            const unsigned m1 = __ballot_sync(0xffffffffu, act);
+            unsigned long long w = 0;
+            if (lane == 0) w = atomicAdd(ocount, (unsigned long long)__popc(m1));
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (act) {
+                const long long o = (long long)w + __popc(m1 & ((1u << lane) - 1u));
+                if (o < ocap) {
+                    out.x[o] = x;
+                    out.y[o] = y;
+                    out.box[o] = box;
+                    out.mode[o] = nmode;
+                    out.sign[o] = nsign;
+                } else {
+                    atomicCAS(err, 0, E_LIMIT);
                 }
-            } else {
-                atomicCAS(err, 0, E_LIMIT);
+                --todo;
+                if (nsign != sign) {  // two more attempts of the parent
+                    todo += 2;
+                    ++flips;
+                }
+                if (++made >= BRANCH_CAP) {
+                    atomicCAS(err, 0, E_LIMIT);
+                    todo = 0;
+                }
             }
         }
     }
+    for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(0xffffffffu, flips, o);
+    if (lane == 0 && flips) atomicAdd(nflips, flips);
 }
 
 // RTA scattering: with probability 1 - exp(-w dt) a particle is resampled
@@ -638,8 +643,6 @@ void alloc_particles(BertaState& B, long long cap) {
         d->alloc(size_t(cap) * sizeof(double));
     for (DBuf* d : {&B.a_mode, &B.a_box, &B.a_sign, &B.b_mode, &B.b_box, &B.b_sign})
         d->alloc(size_t(cap) * sizeof(int));
-    for (DBuf* d : {&B.q_x, &B.q_y}) d->alloc(size_t(2 * cap) * sizeof(double));
-    for (DBuf* d : {&B.q_mode, &B.q_box, &B.q_sign}) d->alloc(size_t(2 * cap) * sizeof(int));
     B.cap = cap;
 }
 
@@ -1190,26 +1193,17 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                         arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np, c->d_w.as<double>(), p->dt,
                         c->d_rprob.as<float>(), c->d_ralt.as<int>(), n, mix_key(p->seed, istep, 6));
             } else if (np > 0) {
-                ck(cudaMemsetAsync(counts, 0, 4 * sizeof(unsigned long long), s), "memset");
-                PArr in = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
-                PArr outp = arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign);
-                long long nin = np;
-                int half = 0, round = 0;
-                for (;;) {
-                    PArr q = arr(B.q_x, B.q_y, B.q_mode, B.q_box, B.q_sign, half ? cap : 0);
-                    ck(cudaMemsetAsync(counts + 1 + half, 0, sizeof(unsigned long long), s), "memset");
-                    be_scatter<<<launch_blocks(nin, c->nsm), 256, 0, s>>>(
-                        in, nin, outp, counts, cap, q, counts + 1 + half, cap,
-                        B.d_palias.as<PAlias>(), B.nm, mix_key(p->seed, istep, 64 + round), err);
-                    const long long nq = read_count(1 + half);
-                    if (nq == 0) break;
-                    if (++round > 4096) throw Error(BTE_ERR_LIMIT, "branching rounds cap");
-                    branchings += nq / 2;
-                    in = q;
-                    nin = nq;
-                    half ^= 1;
-                }
-                np = read_count(0);
+                // counts: [0] outgoing particles, [1] sign flips
+                ck(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s), "memset");
+                be_scatter<<<launch_blocks(np, c->nsm), 256, 0, s>>>(
+                    arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np,
+                    arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), counts, cap, counts + 1,
+                    B.d_palias.as<PAlias>(), B.nm, mix_key(p->seed, istep, 64), err);
+                unsigned long long hcnt[2] = {0, 0};
+                ck(cudaMemcpyAsync(hcnt, counts, sizeof hcnt, cudaMemcpyDeviceToHost, s), "d2h");
+                sync(c);
+                branchings += (long long)hcnt[1];
+                np = (long long)hcnt[0];
                 if (np > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded in scattering");
                 std::swap(B.a_x.p, B.b_x.p);
                 std::swap(B.a_y.p, B.b_y.p);
@@ -1234,7 +1228,9 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),
                                           B.d_props.as<double>());
+            int herr[4];
             ck(cudaMemcpyAsync(hprops.data(), B.d_props.p, hprops.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
             sync(c);
             for (int b = 0; b < nbx; ++b) {
                 const double f1 = p->Eeff / vol[std::size_t(b)] * 1.0e+27;
@@ -1259,9 +1255,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 }
                 p->on_step(p->user, istep + 1, time + p->dt, np, hH.data(), nbx, n, ed.data(), fl.data());
             }
-            int herr[4];
-            ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
-            sync(c);
             if (herr[0] != 0)
                 throw Error(bte_status(herr[0]), herr[0] == BTE_ERR_LIMIT      ? "particle capacity or step cap exceeded"
                                                  : herr[0] == BTE_ERR_GEOMETRY ? "geometry error in the advection"
