@@ -82,6 +82,7 @@ struct BertaState {
     DBuf d_H, d_cnt, d_Eb, d_props, d_counts, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
+    DBuf d_ne, d_ctot;                      // n(omega, T0) per mode; wall-CDF chunk sums
 
     std::vector<Spline1D> spl;
     std::vector<char> spl_ok;
@@ -362,25 +363,37 @@ __global__ void be_advect(PArr P, long long begin, long long end, AdvectArgs a) 
     }
 }
 
-// Isothermal_wall_distribution (src/sampling.cpp:189-269) of each request,
-// one block per request: pmf_k = v_n omega_k |n(omega_k, Tw) - n(omega_k, Te)|
-// for v_n > 0, turned into a CDF row in place; tot[r] keeps the sum.
-__global__ void __launch_bounds__(256) be_wall_cdf(const double* om, const double* vx, const double* vy,
-                                                   int n, const WallReq* req, double* cdf, double* tot) {
+// Isothermal_wall_distribution (src/sampling.cpp:189-269) of each request:
+// pmf_k = v_n omega_k |n(omega_k, Tw) - n(omega_k, Te)| for v_n > 0, turned
+// into a CDF row; tot[r] keeps the sum.  Each request's row is split into
+// chunks of WCDF_CHUNK modes, one block each, so that every SM's FP64 units
+// take part.  ne[k] = n(omega_k, Te_ref) is precomputed: a request at that
+// Te needs one exponential per mode instead of two.
+constexpr int WCDF_CHUNK = 1024;
+
+// pass 1: the chunk's running sums in place and its total
+__global__ void __launch_bounds__(256) be_wall_cdf1(const double* om, const double* vx, const double* vy,
+                                                    const double* ne, double Te_ref, int n,
+                                                    const WallReq* req, double* cdf, double* chunk_tot) {
     __shared__ double part[256];
-    const WallReq R = req[blockIdx.x];
-    double* row = cdf + (long long)blockIdx.x * n;
-    const int seg = (n + blockDim.x - 1) / blockDim.x;
-    const int k0 = threadIdx.x * seg, k1 = min(n, k0 + seg);
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
+    const WallReq R = req[r];
+    double* row = cdf + (long long)r * n;
+    const int c0 = ch * WCDF_CHUNK, c1 = min(n, c0 + WCDF_CHUNK);
+    const int seg = (c1 - c0 + blockDim.x - 1) / blockDim.x;
+    const int k0 = c0 + threadIdx.x * seg, k1 = min(c1, k0 + seg);
     constexpr double pre = 1e12 * 1.054571726e-34 / 1.3806488e-23;
+    const bool pre_e = R.Te == Te_ref;
     double acc = 0.;
     for (int k = k0; k < k1; ++k) {
         const double w = om[k];
         const double vn = R.nx * vx[k] + R.ny * vy[k];
         double p = 0.;
         if (vn > 0. && !almost_equal(0., w)) {
-            const double nw = 1. / (exp(pre * w / R.Tw) - 1.), ne = 1. / (exp(pre * w / R.Te) - 1.);
-            p = vn * w * fabs(nw - ne);
+            const double nw = 1. / (exp(pre * w / R.Tw) - 1.);
+            const double nE = pre_e ? ne[k] : 1. / (exp(pre * w / R.Te) - 1.);
+            p = vn * w * fabs(nw - nE);
         }
         acc += p;
         row[k] = acc;  // running sum within the thread's segment
@@ -388,18 +401,34 @@ __global__ void __launch_bounds__(256) be_wall_cdf(const double* om, const doubl
     part[threadIdx.x] = acc;
     __syncthreads();
     if (threadIdx.x == 0) {  // exclusive offsets of the segments
-        double s = 0.;
+        double sum = 0.;
         for (int t = 0; t < blockDim.x; ++t) {
             const double v = part[t];
-            part[t] = s;
-            s += v;
+            part[t] = sum;
+            sum += v;
         }
-        tot[blockIdx.x] = s;
+        chunk_tot[blockIdx.x] = sum;
     }
     __syncthreads();
-    const double off = part[threadIdx.x], total = tot[blockIdx.x];
-    if (total > 0.)
-        for (int k = k0; k < k1; ++k) row[k] = (row[k] + off) / total;
+    const double off = part[threadIdx.x];
+    for (int k = k0; k < k1; ++k) row[k] += off;
+}
+
+// pass 2: offsets of the chunks, normalisation, the request's total
+__global__ void __launch_bounds__(256) be_wall_cdf2(int n, const double* chunk_tot, double* cdf, double* tot) {
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
+    double off = 0., total = 0.;
+    for (int c = 0; c < nch; ++c) {
+        const double v = chunk_tot[(long long)r * nch + c];
+        if (c < ch) off += v;
+        total += v;
+    }
+    if (ch == 0 && threadIdx.x == 0) tot[r] = total;
+    if (!(total > 0.)) return;
+    double* row = cdf + (long long)r * n;
+    const int c0 = ch * WCDF_CHUNK, c1 = min(n, c0 + WCDF_CHUNK);
+    for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) row[k] = (row[k] + off) / total;
 }
 
 // New particles [base, base + n) from the step's sources.
@@ -494,69 +523,84 @@ __global__ void be_compact(PArr in, long long n, PArr out, unsigned long long* c
 // attempts of one parent (a supercritical propagator never stops).
 constexpr unsigned BRANCH_CAP = 1u << 20;
 
+// Persistent warps: a lane whose parent owes no attempt takes the next
+// parent from a global counter (one atomic per warp), so the warp keeps its
+// lanes busy while chains of different lengths run out.
 __global__ void be_scatter(PArr in, long long n, PArr out, unsigned long long* ocount, long long ocap,
-                           unsigned long long* nflips, const PAlias* pal, int nm, unsigned long long key,
-                           int* err) {
+                           unsigned long long* nflips, unsigned long long* work, const PAlias* pal, int nm,
+                           unsigned long long key, int* err) {
     const int lane = threadIdx.x & 31;
     unsigned long long flips = 0;
-    for (long long base = blockIdx.x * (long long)blockDim.x; base < n;
-         base += (long long)gridDim.x * blockDim.x) {
-        const long long i = base + threadIdx.x;
-        const bool on = i < n;
-        int mode = 0, sign = 1, box = 0;
-        double x = 0., y = 0.;
-        unsigned todo = 0, made = 0;
-        if (on) {
-            mode = in.mode[i];
-            sign = in.sign[i];
-            box = in.box[i];
-            x = in.x[i];
-            y = in.y[i];
-            todo = 1;
-        }
-        const int col = mode - 3;
-        const bool valid = col >= 0 && col < nm;
-        if (on && !valid) atomicCAS(err, 0, E_VALUE);
-        Philox g;
-        g.init(key, (uint64_t)(on ? i : 0));
-        while (__any_sync(0xffffffffu, todo > 0)) {
-            const bool act = todo > 0;
-            int nmode = mode, nsign = sign;
-            if (act && valid) {
-                const int j = int(mulhi32(g.next32(), uint32_t(nm)));
-                const float acc = float(g.next32() >> 8) * 0x1p-24f;
-                const PAlias e = pal[(long long)col * nm + j];
-                const bool keep = acc < e.prob;
-                const int slot = keep ? j : int(e.alt & 0x3fffffffu);
-                const bool neg = keep ? (e.alt >> 31) != 0u : ((e.alt >> 30) & 1u) != 0u;
-                nmode = slot + 3;
-                nsign = neg ? -sign : sign;
-            }
-            // append the outgoing particle of this attempt
-            const unsigned m1 = __ballot_sync(0xffffffffu, act);
-            unsigned long long w = 0;
-            if (lane == 0) w = atomicAdd(ocount, (unsigned long long)__popc(m1));
-            w = __shfl_sync(0xffffffffu, w, 0);
-            if (act) {
-                const long long o = (long long)w + __popc(m1 & ((1u << lane) - 1u));
-                if (o < ocap) {
-                    out.x[o] = x;
-                    out.y[o] = y;
-                    out.box[o] = box;
-                    out.mode[o] = nmode;
-                    out.sign[o] = nsign;
+    int mode = 0, sign = 1, box = 0, col = 0;
+    double x = 0., y = 0.;
+    unsigned todo = 0, made = 0;
+    bool done = false, valid = false;
+    Philox g;
+    g.init(key, 0);
+    for (;;) {
+        // refill the lanes whose parent is finished
+        const unsigned idle = __ballot_sync(0xffffffffu, todo == 0 && !done);
+        if (idle) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (todo == 0 && !done) {
+                const long long i = (long long)base + __popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    mode = in.mode[i];
+                    sign = in.sign[i];
+                    box = in.box[i];
+                    x = in.x[i];
+                    y = in.y[i];
+                    col = mode - 3;
+                    valid = col >= 0 && col < nm;
+                    if (!valid) atomicCAS(err, 0, E_VALUE);
+                    g.init(key, (uint64_t)i);
+                    todo = 1;
+                    made = 0;
                 } else {
-                    atomicCAS(err, 0, E_LIMIT);
+                    done = true;
                 }
-                --todo;
-                if (nsign != sign) {  // two more attempts of the parent
-                    todo += 2;
-                    ++flips;
-                }
-                if (++made >= BRANCH_CAP) {
-                    atomicCAS(err, 0, E_LIMIT);
-                    todo = 0;
-                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        const bool act = todo > 0;
+        int nmode = mode, nsign = sign;
+        if (act && valid) {
+            const int j = int(mulhi32(g.next32(), uint32_t(nm)));
+            const float acc = float(g.next32() >> 8) * 0x1p-24f;
+            const PAlias e = pal[(long long)col * nm + j];
+            const bool keep = acc < e.prob;
+            const int slot = keep ? j : int(e.alt & 0x3fffffffu);
+            const bool neg = keep ? (e.alt >> 31) != 0u : ((e.alt >> 30) & 1u) != 0u;
+            nmode = slot + 3;
+            nsign = neg ? -sign : sign;
+        }
+        // append the outgoing particle of this attempt
+        const unsigned m1 = __ballot_sync(0xffffffffu, act);
+        unsigned long long w = 0;
+        if (lane == 0 && m1) w = atomicAdd(ocount, (unsigned long long)__popc(m1));
+        w = __shfl_sync(0xffffffffu, w, 0);
+        if (act) {
+            const long long o = (long long)w + __popc(m1 & ((1u << lane) - 1u));
+            if (o < ocap) {
+                out.x[o] = x;
+                out.y[o] = y;
+                out.box[o] = box;
+                out.mode[o] = nmode;
+                out.sign[o] = nsign;
+            } else {
+                atomicCAS(err, 0, E_LIMIT);
+            }
+            --todo;
+            if (nsign != sign) {  // two more attempts of the parent
+                todo += 2;
+                ++flips;
+            }
+            if (++made >= BRANCH_CAP) {
+                atomicCAS(err, 0, E_LIMIT);
+                todo = 0;
             }
         }
     }
@@ -958,6 +1002,12 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             B.d_om.upload(m.omega, s);
             B.d_vx.upload(m.vx, s);
             B.d_vy.upload(m.vy, s);
+            // n(omega, T0) of every mode for the adiabatic re-emission rows
+            std::vector<double> ne(m.omega.size(), 0.);
+            const double pre = 1e12 * 1.054571726e-34 / 1.3806488e-23;
+            for (std::size_t k = 0; k < ne.size(); ++k)
+                if (m.omega[k] > 0.) ne[k] = 1. / (std::exp(pre * m.omega[k] / p->T0) - 1.);
+            B.d_ne.upload(ne, s);
         }
         // generate the sources in `descs` at A[base..): alias rows from
         // aprob/aalt (uploaded here) or from a table already on the device
@@ -1178,9 +1228,13 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 B.d_req.upload(reqs, s);
                 B.d_cdf.alloc(reqs.size() * std::size_t(n) * sizeof(double));
                 B.d_cdftot.alloc(reqs.size() * sizeof(double));
-                be_wall_cdf<<<unsigned(reqs.size()), 256, 0, s>>>(B.d_om.as<double>(), B.d_vx.as<double>(),
-                                                                  B.d_vy.as<double>(), n, B.d_req.as<WallReq>(),
-                                                                  B.d_cdf.as<double>(), B.d_cdftot.as<double>());
+                const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+                B.d_ctot.alloc(reqs.size() * std::size_t(nch) * sizeof(double));
+                be_wall_cdf1<<<unsigned(reqs.size()) * unsigned(nch), 256, 0, s>>>(
+                    B.d_om.as<double>(), B.d_vx.as<double>(), B.d_vy.as<double>(), B.d_ne.as<double>(), p->T0, n,
+                    B.d_req.as<WallReq>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
+                be_wall_cdf2<<<unsigned(reqs.size()) * unsigned(nch), 256, 0, s>>>(
+                    n, B.d_ctot.as<double>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
             }
             generate(np, nnew, istep, 4, true);
             np += nnew;
@@ -1193,11 +1247,13 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                         arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np, c->d_w.as<double>(), p->dt,
                         c->d_rprob.as<float>(), c->d_ralt.as<int>(), n, mix_key(p->seed, istep, 6));
             } else if (np > 0) {
-                // counts: [0] outgoing particles, [1] sign flips
-                ck(cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s), "memset");
-                be_scatter<<<launch_blocks(np, c->nsm), 256, 0, s>>>(
+                // counts: [0] outgoing particles, [1] sign flips, [2] parents taken
+                ck(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), s), "memset");
+                long long sblocks = (np + 255) / 256;
+                if (sblocks > 8ll * c->nsm) sblocks = 8ll * c->nsm;
+                be_scatter<<<unsigned(sblocks), 256, 0, s>>>(
                     arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np,
-                    arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), counts, cap, counts + 1,
+                    arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), counts, cap, counts + 1, counts + 2,
                     B.d_palias.as<PAlias>(), B.nm, mix_key(p->seed, istep, 64), err);
                 unsigned long long hcnt[2] = {0, 0};
                 ck(cudaMemcpyAsync(hcnt, counts, sizeof hcnt, cudaMemcpyDeviceToHost, s), "d2h");
