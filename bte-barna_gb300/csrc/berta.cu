@@ -71,6 +71,38 @@ struct PAlias {
     unsigned alt;  // bits 0-29 slot, bit 30 alt negative, bit 31 keep negative
 };
 
+// Page-locked staging for the per-step uploads: a copy from pageable memory
+// may wait for the stream's earlier work, a copy from here does not.  Each
+// upload site has its own buffer, written again only after a later sync.
+struct Pinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    Pinned() = default;
+    Pinned(const Pinned&) = delete;
+    Pinned& operator=(const Pinned&) = delete;
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+    void reserve(size_t n) {
+        if (bytes >= n) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        ck(cudaMallocHost(&p, n), "cudaMallocHost");
+        bytes = n;
+    }
+};
+
+template <class T>
+void upload_pinned(DBuf& d, Pinned& h, const std::vector<T>& v, cudaStream_t s) {
+    const size_t bytes = v.size() * sizeof(T);
+    if (bytes == 0) return;
+    d.alloc(bytes);
+    h.reserve(bytes);
+    std::memcpy(h.p, v.data(), bytes);
+    ck(cudaMemcpyAsync(d.p, h.p, bytes, cudaMemcpyHostToDevice, s), "h2d");
+}
+
 struct BertaState {
     bool have_prop = false;
     int nm = 0;
@@ -83,6 +115,7 @@ struct BertaState {
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
     DBuf d_ne, d_ctot;                      // n(omega, T0) per mode; wall-CDF chunk sums
+    Pinned h_gens[4], h_req;                // staging: descriptors per phase, wall requests
 
     std::vector<Spline1D> spl;
     std::vector<char> spl_ok;
@@ -875,6 +908,12 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 border_box[std::size_t(g.boxes[std::size_t(b)].border_off + k)] = b;
         B.d_boxwall.upload(boxwall, s);
         B.d_Eb.alloc(std::size_t(nborders) * sizeof(int));
+        // per-step buffers at their largest size (one request per border),
+        // so that no step reallocates
+        B.d_req.alloc(std::size_t(nborders) * sizeof(WallReq));
+        B.d_cdf.alloc(std::size_t(nborders) * std::size_t(m.n()) * sizeof(double));
+        B.d_cdftot.alloc(std::size_t(nborders) * sizeof(double));
+        B.d_ctot.alloc(std::size_t(nborders) * ((m.n() + WCDF_CHUNK - 1) / WCDF_CHUNK) * sizeof(double));
         ck(cudaMemsetAsync(B.d_Eb.p, 0, std::size_t(nborders) * sizeof(int), s), "memset");
         if (int(B.spl.size()) != nborders || B.spl_version != c->tables_version) {
             B.spl.assign(std::size_t(nborders), Spline1D());
@@ -939,6 +978,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         std::vector<float> aprob;
         std::vector<int> aalt;
         std::vector<GenDesc> descs;
+        B.d_gens.alloc(std::size_t(std::max({nborders, nbx, int(iso.walls.size())}) + 1) * sizeof(GenDesc));
         std::vector<WallReq> reqs;
         // a source spread over box b: its grid cell, or its bounding box with
         // rejection (geometry_2d::get_random_point)
@@ -1017,7 +1057,9 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                             const signed char* rsign = nullptr) {
             if (total <= 0) return;
             if (base + total > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded: raise capacity");
-            B.d_gens.upload(descs, s);
+            // one staging buffer per phase (initial, gradient, isothermal, adiabatic)
+            const int slot = phase == 0 ? 0 : phase == 8 ? 1 : phase == 2 ? 2 : 3;
+            upload_pinned(B.d_gens, B.h_gens[slot], descs, s);
             const float* dprob = rprob;
             const int* dalt = ralt;
             if (!rprob && !aprob.empty()) {
@@ -1225,11 +1267,8 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             if (!reqs.empty()) {
                 // the re-emission distributions at the border temperatures,
                 // built on the device (one block per border)
-                B.d_req.upload(reqs, s);
-                B.d_cdf.alloc(reqs.size() * std::size_t(n) * sizeof(double));
-                B.d_cdftot.alloc(reqs.size() * sizeof(double));
+                upload_pinned(B.d_req, B.h_req, reqs, s);
                 const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
-                B.d_ctot.alloc(reqs.size() * std::size_t(nch) * sizeof(double));
                 be_wall_cdf1<<<unsigned(reqs.size()) * unsigned(nch), 256, 0, s>>>(
                     B.d_om.as<double>(), B.d_vx.as<double>(), B.d_vy.as<double>(), B.d_ne.as<double>(), p->T0, n,
                     B.d_req.as<WallReq>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
