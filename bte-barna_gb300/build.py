@@ -16,6 +16,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libbtegpu.so")
 CLI = os.path.join(OUT, "rtamc2d_gpu")
 CLI_BE = os.path.join(OUT, "bertamc2d_gpu")
+CLI_DR = os.path.join(OUT, "dist_reader_gpu")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOSTFLAGS = "-fPIC,-ffp-contract=off,-O2"
@@ -55,7 +56,8 @@ def _run(cmd):
 
 def build(force: bool = False, verbose: bool = False) -> str:
     deps = _deps()
-    if not force and _newer(LIB, deps) and _newer(CLI, deps) and _newer(CLI_BE, deps):
+    if (not force and _newer(LIB, deps) and _newer(CLI, deps) and _newer(CLI_BE, deps)
+            and _newer(CLI_DR, deps)):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     jobs = []
@@ -84,6 +86,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", os.path.join(CSRC, "cli_bertamc2d.cpp"),
           "-o", tmp, "-L", OUT, "-lbtegpu", "-Wl,-rpath,$ORIGIN", "-pthread"])
     os.replace(tmp, CLI_BE)
+    tmp = CLI_DR + ".tmp%d" % os.getpid()
+    _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", os.path.join(CSRC, "cli_dist_reader.cpp"), "-o", tmp])
+    os.replace(tmp, CLI_DR)
     return LIB
 
 

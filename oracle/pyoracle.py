@@ -202,6 +202,104 @@ def spectral_counts(shape):
     return out
 
 
+def decode_berta_frame(body: bytes):
+    """One properties.msgpack.bin frame body (src/beyondRTA_MC2d.cpp:
+    1604-1769): (time, Eeff, temperatures, [{mode: count} per box]).  Reads
+    the msgpack subset the frames use (arrays, float64/32, integers)."""
+    import struct
+    pos = [0]
+
+    def byte():
+        c = body[pos[0]]
+        pos[0] += 1
+        return c
+
+    def be(n):
+        v = int.from_bytes(body[pos[0]:pos[0] + n], "big")
+        pos[0] += n
+        return v
+
+    def array():
+        c = byte()
+        if c & 0xF0 == 0x90:
+            return c & 0x0F
+        return be(2) if c == 0xDC else be(4)
+
+    def number():
+        c = byte()
+        if c <= 0x7F:
+            return c
+        if c >= 0xE0:
+            return c - 256
+        if c == 0xCB:
+            v = struct.unpack(">d", body[pos[0]:pos[0] + 8])[0]
+            pos[0] += 8
+            return v
+        if c == 0xCA:
+            v = struct.unpack(">f", body[pos[0]:pos[0] + 4])[0]
+            pos[0] += 4
+            return v
+        if 0xCC <= c <= 0xCF:
+            return be(1 << (c - 0xCC))
+        n = 1 << (c - 0xD0)
+        v = be(n)
+        return v - (1 << (8 * n)) if v >> (8 * n - 1) else v
+
+    top = array()
+    time, Eeff = number(), number()
+    temps = [number() for _ in range(array())]
+    hists = []
+    for _ in range((top - 3) // 2):
+        nel = int(number())
+        vals = [number() for _ in range(array())]
+        hists.append({int(vals[2 * j]): vals[2 * j + 1] for j in range(nel // 2)})
+    return time, Eeff, temps, hists
+
+
+def dist_reader_restated(modes, area, thickness, boxes, nbins, hists, temps, Eeff):
+    """print_distribution of dist_reader (src/dist_reader.cpp:270-508) for one
+    frame: per listed box (d, dvx, dvy) on the omega mesh and dfd per q
+    point, plus the mesh.  `hists` is [{mode: count} per box]."""
+    from math import lgamma
+    om = np.asarray(modes["omega"], dtype=float)
+    v = np.asarray(modes["vg"], dtype=float).reshape(-1, 3)
+    dq = np.asarray(modes["dq"], dtype=float).reshape(3, 3, order="F")
+    nb, nq = int(modes["nb"]), int(modes["nq"])
+    zero = np.abs(om) < 1e-8 + 1e-5 * np.abs(om)       # almost_equal(omega, 0)
+    sig = np.where(zero, 0.0, np.sqrt(((v @ dq) ** 2).sum(axis=1)) / np.sqrt(12.0))
+    n = sig.size
+    with np.errstate(divide="ignore", over="ignore"):
+        ls = np.sort(np.where(sig == 0.0, -np.finfo(float).max, np.log(np.where(sig == 0.0, 1.0, sig))))
+        p25, p75 = ls[25 * n // 100], ls[75 * n // 100]
+        sig = np.maximum(sig, np.exp(p25 - 1.5 * (p75 - p25)))
+    mesh = np.linspace(0.0, om.max(), nbins)
+    mesh = mesh + mesh[1] / 2.0
+    kB, hbar = 1.3806488e-23, 1.054571726e-34
+    T = temps[boxes[0]]
+    vuc = modes["V"] * thickness / modes["c_lat"]
+    import synth
+    Cv = kB / vuc / nq * synth.be_kernel(om[~zero], T).sum()
+    out = {}
+    for b in boxes:
+        d, dx, dy, fd = np.zeros(nbins), np.zeros(nbins), np.zeros(nbins), np.zeros(nq)
+        vol = area[b] * thickness
+        for k, val in hists[b].items():
+            if val == 0:
+                continue
+            fd[k // nb] += val / om[k]
+            if zero[k] or abs(sig[k]) < 1e-8:
+                continue
+            kk, th = om[k] ** 2 / sig[k], sig[k] / om[k]
+            z = mesh / th
+            g = np.exp((kk - 1.0) * np.log(z) - z - lgamma(kk) - np.log(th))
+            d += val * g
+            dx += val * g * 1e3 * v[k, 0]
+            dy += val * g * 1e3 * v[k, 1]
+        out[b] = (d * Eeff / (vol * Cv), dx * Eeff * 1e27 / vol, dy * Eeff * 1e27 / vol,
+                  fd * Eeff * vuc * nq / (1e12 * vol * hbar))
+    return mesh, out
+
+
 def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, ballistic=False,
             source=None, specularity=None, materials=None):
     """`materials`: optional (list of per-mode rate arrays, list of T0[,

@@ -160,3 +160,41 @@ def test_bertamc2d_cli_gradient_on_periodic_block(built, tmp_path):
     rows = [ln.split("\t") for ln in r.stdout.splitlines() if ln and ln[0].isdigit()]
     assert len(rows) == 21
     assert int(rows[-1][2]) > 0                 # particles from the source term
+
+
+def test_dist_reader_on_bertamc2d_frames(built, tmp_path):
+    """bertamc2d_gpu writes the frames, dist_reader_gpu reads them back: the
+    distribution at the dump times against the restatement of dist_reader."""
+    import os
+    import subprocess
+    m, g, P = _case()
+    synth.write_geometry_xml(str(tmp_path / "beam.xml"), g)
+    synth.write_modes_file(str(tmp_path / "modes.bin"), m)
+    synth.write_propagator(str(tmp_path / "p.P.eigen.bin"), P)
+    (tmp_path / "input.xml").write_text(
+        '<beRTAMC2D>\n  <geometry file="beam.xml"/>\n  <time dt="1.0" maxtime="10"/>\n'
+        '  <material name="synthetic" database="modes.bin" thickness="0.335">\n'
+        '    <propagator T="300" file="p.P.eigen.bin"/>\n  </material>\n'
+        '  <Eeff Ed="2e-23"/>\n'
+        '  <spectral>\n    <resolution ticks="30"/>\n    <location bin="0"/>\n'
+        '    <location bin="2"/>\n    <time t="5"/>\n    <time t="9"/>\n  </spectral>\n</beRTAMC2D>\n')
+    d = os.path.dirname(built)
+    r = subprocess.run([os.path.join(d, "bertamc2d_gpu"), "input.xml", "4"], cwd=tmp_path,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([os.path.join(d, "dist_reader_gpu"), "input.xml", "properties.msgpack.bin"],
+                       cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    frames = [pyoracle.decode_berta_frame(f)
+              for f in btegpu.split_frames((tmp_path / "properties.msgpack.bin").read_bytes())]
+    dumps = [f for f in frames if f[0] in (5.0, 9.0)]
+    assert len(dumps) == 2
+    area = [200.0 / 5 * 50.0] * 5
+    for b in (0, 2):
+        dT = np.loadtxt(tmp_path / f"deltaT_omega_{b}.csv", delimiter=",")
+        assert dT.shape == (3, 31)
+        for row, (t, E, T, hists) in enumerate(dumps, start=1):
+            assert dT[row, 0] == t and len(hists[b]) > 0
+            _, out = pyoracle.dist_reader_restated(m, area, 0.335, [0, 2], 30, hists, T, E)
+            ref = out[b][0]
+            assert np.allclose(dT[row, 1:], ref, rtol=2e-5, atol=1e-5 * np.abs(ref).max())
