@@ -55,6 +55,13 @@ def load():
         C.c_uint64, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.oracle_translate.restype = C.c_int
     lib.oracle_set_spectral.argtypes = [C.c_int, C.POINTER(C.c_int)]
+    lib.oracle_kat_segment.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double, C.c_double, C.c_int,
+                                       C.POINTER(C.c_double)]
+    lib.oracle_kat_cdf_sample.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double]
+    lib.oracle_kat_cdf_sample.restype = C.c_longlong
+    lib.oracle_kat_propagator.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.c_double,
+                                          C.POINTER(C.c_int)]
+    lib.oracle_kat_propagator.restype = C.c_int
     lib.oracle_spectral_raw.argtypes = [C.POINTER(C.c_int64), C.c_longlong]
     lib.oracle_spectral_raw.restype = C.c_longlong
     lib.oracle_spectral_counts.argtypes = [C.POINTER(C.c_int64), C.c_longlong]
@@ -200,6 +207,28 @@ def spectral_counts(shape):
     if got != n:
         raise ValueError(f"spectral counts have {got} values, expected {n}")
     return out
+
+
+def kat_segment(grid, t0, t1, sign):
+    g = np.ascontiguousarray(grid, dtype=float)
+    out = np.zeros(g.size - 1)
+    load().oracle_kat_segment(g.ctypes.data_as(C.POINTER(C.c_double)), g.size, t0, t1, sign,
+                              out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+def kat_cdf_sample(pmf, u):
+    p = np.ascontiguousarray(pmf, dtype=float)
+    return int(load().oracle_kat_cdf_sample(p.ctypes.data_as(C.POINTER(C.c_double)), p.size, u))
+
+
+def kat_propagator(P, col, u):
+    """(outgoing mode, sign) of propagator_H::get on column `col` of P."""
+    a = np.ascontiguousarray(np.asarray(P, dtype=float).ravel(order="F"))
+    s = C.c_int(0)
+    m = load().oracle_kat_propagator(a.ctypes.data_as(C.POINTER(C.c_double)), int(np.asarray(P).shape[0]),
+                                     col, u, C.byref(s))
+    return m, s.value
 
 
 def decode_berta_frame(body: bytes):

@@ -1936,6 +1936,41 @@ std::vector<__int128> g_spec_last;  // the last run's per-mode tally
 std::vector<int64_t> g_spec_cnt;     // the last steady run's signed segment counts
 }  // namespace
 
+// Known-answer hooks into single pieces of the restatement.
+// process_segment's split of [t0, t1] over the time grid: the signed time
+// each bin receives, added to bins[ntime - 1].
+void oracle_kat_segment(const double* grid, int ntime, double t0, double t1, int sign, double* bins) {
+    orc::Sim S;
+    S.timegrid.assign(grid, grid + ntime);
+    orc::Tally T;
+    T.init(1, std::size_t(ntime - 1));
+    orc::process_segment(S, T, 0, t0, t1, sign, orc::V2{0., 0.});
+    for (int i = 0; i + 1 < ntime; ++i) bins[i] += T.gz[std::size_t(i)];
+}
+
+// Grid_distribution::sample: index drawn by u from the pmf's CDF; -1 when
+// fill_cumulative rejects the pmf (a negative weight).
+long long oracle_kat_cdf_sample(const double* pmf, int n, double u) {
+    try {
+        const std::vector<double> p(pmf, pmf + n);
+        return (long long)orc::lower_bound_idx(orc::fill_cumulative(p), u);
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+// propagator_H::get on column `col` of the column-major n x n P: the
+// outgoing mode (row + 3) and its sign.
+int oracle_kat_propagator(const double* P, int n, int col, double u, int* sign) {
+    orc::BeRun R;
+    R.nm = n;
+    orc::build_cumm(R, P);
+    const auto r = orc::prop_get(R, std::size_t(col), u);
+    *sign = r.first;
+    return int(r.second);
+}
+
 // Spectral locations for the following oracle_rta_run calls (nloc = 0: off).
 void oracle_set_spectral(int nloc, const int* boxes) {
     g_spec_boxes.assign(boxes, boxes + (nloc > 0 ? nloc : 0));
