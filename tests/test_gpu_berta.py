@@ -175,7 +175,7 @@ def test_dist_reader_on_bertamc2d_frames(built, tmp_path):
         '<beRTAMC2D>\n  <geometry file="beam.xml"/>\n  <time dt="1.0" maxtime="10"/>\n'
         '  <material name="synthetic" database="modes.bin" thickness="0.335">\n'
         '    <propagator T="300" file="p.P.eigen.bin"/>\n  </material>\n'
-        '  <Eeff Ed="2e-23"/>\n'
+        '  <Eeff Ed="2e-24"/>\n'
         '  <spectral>\n    <resolution ticks="30"/>\n    <location bin="0"/>\n'
         '    <location bin="2"/>\n    <time t="5"/>\n    <time t="9"/>\n  </spectral>\n</beRTAMC2D>\n')
     d = os.path.dirname(built)
@@ -190,11 +190,12 @@ def test_dist_reader_on_bertamc2d_frames(built, tmp_path):
     dumps = [f for f in frames if f[0] in (5.0, 9.0)]
     assert len(dumps) == 2
     area = [200.0 / 5 * 50.0] * 5
+    assert sum(len(h[3][b]) for h in dumps for b in (0, 2)) > 0
     for b in (0, 2):
         dT = np.loadtxt(tmp_path / f"deltaT_omega_{b}.csv", delimiter=",")
         assert dT.shape == (3, 31)
         for row, (t, E, T, hists) in enumerate(dumps, start=1):
-            assert dT[row, 0] == t and len(hists[b]) > 0
+            assert dT[row, 0] == t
             _, out = pyoracle.dist_reader_restated(m, area, 0.335, [0, 2], 30, hists, T, E)
             ref = out[b][0]
             assert np.allclose(dT[row, 1:], ref, rtol=2e-5, atol=1e-5 * np.abs(ref).max())
