@@ -256,7 +256,9 @@ typedef struct bte_tuning {
     int32_t block_threads;   /* threads per block                              */
     int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid  */
     int32_t smem_tally;      /* 1: privatise tallies in shared memory           */
-    int32_t smem_alias;      /* 1: stage the resampling alias table in smem     */
+    int32_t smem_alias;      /* reserved, ignored: the alias tables are read
+                                through the read-only path and stay in L2 (the
+                                C1 table, 36864 modes, exceeds shared memory)  */
 } bte_tuning;
 
 /* ------------------------------------------------------------------------ */
