@@ -715,6 +715,12 @@ def main():
             fp64 = {"pipe": "fp64", "ops_per_event": prof["fp64_thread_ops_per_event"],
                     "achieved": ops / 1e9, "peak": lane_peak / 1e9, "unit": "Gop/s",
                     "frac": ops / lane_peak, "pipe_busy_pct_ncu": prof.get("fp64_pipe_busy_pct")}
+        l2red = None
+        if "l2_red_sectors_per_event" in prof and "l2_red_peak_sectors_per_s" in prof:
+            red = prof["l2_red_sectors_per_event"] * value
+            l2red = {"per_event": prof["l2_red_sectors_per_event"], "achieved": red,
+                     "peak": prof["l2_red_peak_sectors_per_s"], "unit": "sectors/s",
+                     "frac": red / prof["l2_red_peak_sectors_per_s"]}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -735,6 +741,7 @@ def main():
                          "traffic": traffic,
                          "bytes_per_event": per_launch_bytes / max(ev_launch, 1)},
             "co_bound": fp64,
+            "l2_reductions": l2red,
             "clocks": clk,
             "tuning": {"block_threads": choice[0], "blocks_per_sm": choice[1],
                        "smem_tally": choice[2],
