@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -107,7 +108,16 @@ struct BertaState {
     bool have_prop = false;
     int nm = 0;
     double T = 0;
-    DBuf d_palias;
+    // propagators tabulated in temperature (one bte_load_propagator call
+    // each), host copies kept for the interpolation of lirp
+    std::map<double, std::vector<double>> props;
+    long long props_version = 0;
+    // what the device holds: the alias table of the propagator at sel_T, or
+    // (sel_lirp) the interpolated signed CDF at sel_T
+    double sel_T = 0;
+    bool sel_lirp = false;
+    long long sel_version = -1;
+    DBuf d_palias, d_pcdf;
     long long cap = 0;
     DBuf a_x, a_y, a_mode, a_box, a_sign;   // particles
     DBuf b_x, b_y, b_mode, b_box, b_sign;   // compaction / scattering output
@@ -121,6 +131,13 @@ struct BertaState {
     std::vector<char> spl_ok;
     long long spl_version = -1;   // tables the splines were built for
 };
+
+void reset_propagators(bte_ctx* c) {
+    if (!c->berta) return;
+    c->berta->props.clear();
+    c->berta->have_prop = false;
+    c->berta->props_version++;
+}
 
 void destroy_berta(bte_ctx* c) {
     delete c->berta;
@@ -559,9 +576,30 @@ constexpr unsigned BRANCH_CAP = 1u << 20;
 // Persistent warps: a lane whose parent owes no attempt takes the next
 // parent from a global counter (one atomic per warp), so the warp keeps its
 // lanes busy while chains of different lengths run out.
+// propagator_H::lower_bound (include/collision_operator.hpp:263-269): the
+// first entry whose |value| is not below u, by std::lower_bound's own
+// probing, so that an interpolated column whose |values| are not monotone
+// gives the same index as in the reference; clamped to the last entry.
+__device__ __forceinline__ int lower_bound_abs(const double* a, int n, double u) {
+    int lo = 0, cnt = n;
+    while (cnt > 0) {
+        const int step = cnt >> 1;
+        const int it = lo + step;
+        if (fabs(__ldg(a + it)) < fabs(u)) {
+            lo = it + 1;
+            cnt -= step + 1;
+        } else {
+            cnt = step;
+        }
+    }
+    return lo < n ? lo : n - 1;
+}
+
+// pcdf set: draw from the signed CDF columns instead of the alias table (an
+// interpolated propagator, which has no alias form in general).
 __global__ void be_scatter(PArr in, long long n, PArr out, unsigned long long* ocount, long long ocap,
-                           unsigned long long* nflips, unsigned long long* work, const PAlias* pal, int nm,
-                           unsigned long long key, int* err) {
+                           unsigned long long* nflips, unsigned long long* work, const PAlias* pal,
+                           const double* pcdf, int nm, unsigned long long key, int* err) {
     const int lane = threadIdx.x & 31;
     unsigned long long flips = 0;
     int mode = 0, sign = 1, box = 0, col = 0;
@@ -600,7 +638,12 @@ __global__ void be_scatter(PArr in, long long n, PArr out, unsigned long long* o
         if (__all_sync(0xffffffffu, done)) break;
         const bool act = todo > 0;
         int nmode = mode, nsign = sign;
-        if (act && valid) {
+        if (act && valid && pcdf) {
+            const double* c = pcdf + (long long)col * nm;
+            const int im = lower_bound_abs(c, nm, g.uniform());
+            nmode = im + 3;
+            nsign = __ldg(c + im) > 0. ? sign : -sign;
+        } else if (act && valid) {
             const int j = int(mulhi32(g.next32(), uint32_t(nm)));
             const float acc = float(g.next32() >> 8) * 0x1p-24f;
             const PAlias e = pal[(long long)col * nm + j];
@@ -789,32 +832,16 @@ extern "C" bte_status bte_load_propagator(bte_ctx* c, const bte_propagator* P) {
         if (!c->have_modes) throw Error(BTE_ERR_STATE, "load the mode table before the propagator");
         if (std::size_t(P->nmodes) + 3 != c->modes.n())
             throw Error(BTE_ERR_INPUT, "propagator size must be the number of modes minus 3");
-        bte::ck(cudaSetDevice(c->device), "cudaSetDevice");
+        if (!std::isfinite(P->T) || !(P->T > 0.)) throw Error(BTE_ERR_INPUT, "propagator temperature must be positive");
         if (!c->berta) c->berta = new bte::BertaState();
         bte::BertaState& B = *c->berta;
         const int nm = P->nmodes;
-        // propagator_H per column: |P| weights, sign of each entry
-        // (src/collision_operator.cpp:857-870); sampled by alias here
-        std::vector<bte::PAlias> tab(std::size_t(nm) * nm);
-        std::vector<double> w(static_cast<std::size_t>(nm));
-        std::vector<bte::Alias> al(static_cast<std::size_t>(nm));
-        for (int j = 0; j < nm; ++j) {
-            const double* col = P->P + std::size_t(j) * nm;
-            for (int i = 0; i < nm; ++i) {
-                if (!std::isfinite(col[i])) throw Error(BTE_ERR_VALUE, "non-finite propagator entry");
-                w[std::size_t(i)] = std::fabs(col[i]);
-            }
-            bte::alias_table(w.data(), nm, al.data());
-            for (int i = 0; i < nm; ++i) {
-                bte::PAlias e;
-                e.prob = al[std::size_t(i)].prob;
-                const int alt = al[std::size_t(i)].alt;
-                e.alt = unsigned(alt) | (col[alt] < 0. ? (1u << 30) : 0u) | (col[i] < 0. ? (1u << 31) : 0u);
-                tab[std::size_t(j) * nm + std::size_t(i)] = e;
-            }
-        }
-        B.d_palias.upload(tab, c->stream);
-        bte::sync(c);
+        if (B.have_prop && nm != B.nm) B.props.clear();  // another mode table
+        const std::size_t nn = std::size_t(nm) * std::size_t(nm);
+        for (std::size_t i = 0; i < nn; ++i)
+            if (!std::isfinite(P->P[i])) throw Error(BTE_ERR_VALUE, "non-finite propagator entry");
+        B.props[P->T].assign(P->P, P->P + nn);
+        B.props_version++;
         B.nm = nm;
         B.T = P->T;
         B.have_prop = true;
@@ -829,6 +856,75 @@ extern "C" bte_status bte_load_propagator(bte_ctx* c, const bte_propagator* P) {
 }
 
 namespace {
+
+// signed_cumm of propagator_H (src/collision_operator.cpp:857-870) for every
+// column of the column-major nm x nm P: running sums of |P| over the column
+// sum, each with the sign of its entry.
+std::vector<double> signed_cumm(const std::vector<double>& P, int nm) {
+    std::vector<double> c(P.size());
+    for (int j = 0; j < nm; ++j) {
+        const double* col = P.data() + std::size_t(j) * nm;
+        double abssum = 0.;
+        for (int i = 0; i < nm; ++i) abssum += std::fabs(col[i]);
+        double acc = 0.;
+        for (int i = 0; i < nm; ++i) {
+            acc += std::fabs(col[i]);
+            c[std::size_t(j) * nm + i] = col[i] < 0. ? -acc / abssum : acc / abssum;
+        }
+    }
+    return c;
+}
+
+// The device tables of the propagator at Teq = T0 (Scattering,
+// src/beyondRTA_MC2d.cpp:1130-1165): the tabulated one when T0 is in the
+// table, sampled through per-column alias tables; otherwise lirp
+// (src/collision_operator.cpp:918-929) between the first tabulated
+// temperature above T0 and the next one -- both above T0, as the reference
+// picks them -- sampled through the interpolated signed CDF.
+void select_propagator(bte_ctx* c, bte::BertaState& B, double T0) {
+    using namespace bte;
+    if (B.sel_version == B.props_version && B.sel_T == T0) return;
+    const int nm = B.nm;
+    const std::size_t nn = std::size_t(nm) * std::size_t(nm);
+    auto it = B.props.find(T0);
+    if (it != B.props.end()) {
+        const std::vector<double>& P = it->second;
+        std::vector<PAlias> tab(nn);
+        std::vector<double> w(static_cast<std::size_t>(nm));
+        std::vector<Alias> al(static_cast<std::size_t>(nm));
+        for (int j = 0; j < nm; ++j) {
+            const double* col = P.data() + std::size_t(j) * nm;
+            for (int i = 0; i < nm; ++i) w[std::size_t(i)] = std::fabs(col[i]);
+            alias_table(w.data(), nm, al.data());
+            for (int i = 0; i < nm; ++i) {
+                PAlias e;
+                e.prob = al[std::size_t(i)].prob;
+                const int alt = al[std::size_t(i)].alt;
+                e.alt = unsigned(alt) | (col[alt] < 0. ? (1u << 30) : 0u) | (col[i] < 0. ? (1u << 31) : 0u);
+                tab[std::size_t(j) * nm + std::size_t(i)] = e;
+            }
+        }
+        B.d_palias.upload(tab, c->stream);
+        B.sel_lirp = false;
+    } else {
+        auto m1 = B.props.lower_bound(T0);
+        const double Tlow = B.props.begin()->first;
+        if (m1 == B.props.end() || std::next(m1) == B.props.end() || T0 < Tlow)
+            throw Error(BTE_ERR_INPUT,
+                        "Extrapolation is not allowed: limit Tref between the min and max temperatures "
+                        "used in the propagator calculation");
+        const auto m2 = std::next(m1);
+        const double T1 = m1->first, T2 = m2->first;
+        const std::vector<double> c1 = signed_cumm(m1->second, nm), c2 = signed_cumm(m2->second, nm);
+        std::vector<double> pint(nn);
+        for (std::size_t i = 0; i < nn; ++i) pint[i] = c1[i] + (T0 - T1) * (c2[i] - c1[i]) / (T2 - T1);
+        B.d_pcdf.upload(pint, c->stream);
+        B.sel_lirp = true;
+    }
+    sync(c);
+    B.sel_T = T0;
+    B.sel_version = B.props_version;
+}
 
 std::size_t n_to_generate(double gen, bte::Pcg64& rng) {
     std::size_t np = std::size_t(gen);
@@ -882,6 +978,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         if (p->gradient_mode == 1 && !(std::isfinite(p->gradient[0]) && std::isfinite(p->gradient[1])))
             throw Error(BTE_ERR_INPUT, "gradient must be finite");
         if (p->rta) ensure_resample(c, p->T0);
+        else select_propagator(c, *c->berta, p->T0);
         if (!c->berta) c->berta = new BertaState();
         BertaState& B = *c->berta;
         const int n = int(m.n());
@@ -1293,7 +1390,8 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 be_scatter<<<unsigned(sblocks), 256, 0, s>>>(
                     arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np,
                     arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), counts, cap, counts + 1, counts + 2,
-                    B.d_palias.as<PAlias>(), B.nm, mix_key(p->seed, istep, 64), err);
+                    B.d_palias.as<PAlias>(), B.sel_lirp ? B.d_pcdf.as<double>() : nullptr, B.nm,
+                    mix_key(p->seed, istep, 64), err);
                 unsigned long long hcnt[2] = {0, 0};
                 ck(cudaMemcpyAsync(hcnt, counts, sizeof hcnt, cudaMemcpyDeviceToHost, s), "d2h");
                 sync(c);

@@ -348,6 +348,7 @@ bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
         c->modes = bte::build_modes(mt);
         c->have_modes = true;
         c->tables_version++;
+        bte::reset_propagators(c);
         c->nmat = 0;  // materials are rate sets over one table
         c->mat_w.clear();
         c->mat_T0.clear();

@@ -3,7 +3,7 @@
 //   bertamc2d_gpu <inputfile.xml> nthreads          (src/beyondRTA_MC2d.cpp:1928-1942)
 //
 // Reads the <beRTAMC2D> XML (src/beyondRTA_MC2d.cpp:1299-1462): geometry,
-// time, material with one <propagator T file> (*.P.eigen.bin, save_P
+// time, material with <propagator T file> entries (*.P.eigen.bin, save_P
 // format), <Eeff particles=|Ed=|Tmax Tmin>, <RTA/>; runs the step loop on the
 // GPU through the C ABI; prints the per-step table "step time N (ed jx jy)
 // per box" (:2418-2423) and writes properties.msgpack.bin frames
@@ -113,7 +113,8 @@ int main(int argc, char** argv) {
         auto root = read_xml(input);
         if (root->name != "beRTAMC2D") throw std::runtime_error("root element must be <beRTAMC2D>");
         const std::string base = dir_of(input);
-        std::string gfile, dbfile, pfile;
+        std::string gfile, dbfile;
+        std::vector<std::pair<double, std::string>> pfiles;  // <propagator T file>, one per temperature
         double dt = 0, maxtime = 0, thickness = 0, Ed = -1, Tmax = 0, Tmin = 0, particles = 0;
         bool rta = false, have_grad = false;
         double grad[2] = {0., 0.};
@@ -130,8 +131,7 @@ int main(int argc, char** argv) {
                 thickness = std::stod(k->get("thickness"));
                 for (auto& q : k->kids)
                     if (q->name == "propagator") {
-                        if (!pfile.empty()) throw std::runtime_error("one propagator temperature is supported");
-                        pfile = q->get("file");
+                        pfiles.emplace_back(std::stod(q->get("T")), q->get("file"));
                     }
             }
             if (k->name == "Eeff") {
@@ -258,13 +258,16 @@ int main(int argc, char** argv) {
             gm.translation = transl.data();
         }
         check(ctx, bte_load_geometry(ctx, &gm), "load geometry");
-        std::vector<double> P;
         if (!rta) {
-            if (pfile.empty()) throw std::runtime_error("no <propagator> given and no <RTA/>");
-            int64_t nP = 0;
-            P = read_P(resolve(base, pfile), nP);
-            bte_propagator pr{int32_t(nP), T0, P.data()};
-            check(ctx, bte_load_propagator(ctx, &pr), "load propagator");
+            if (pfiles.empty()) throw std::runtime_error("no <propagator> given and no <RTA/>");
+            // every tabulated temperature; a run at a Teq in between
+            // interpolates (lirp, src/collision_operator.cpp:918-929)
+            for (auto& [Tp, file] : pfiles) {
+                int64_t nP = 0;
+                const std::vector<double> P = read_P(resolve(base, file), nP);
+                bte_propagator pr{int32_t(nP), Tp, P.data()};
+                check(ctx, bte_load_propagator(ctx, &pr), "load propagator");
+            }
         }
         std::cout << "#Eeff is: " << Eeff << " J" << std::endl;
         StepOut so;

@@ -121,6 +121,8 @@ void ensure_static(bte_ctx* c);
 void ensure_resample(bte_ctx* c, double T0);
 void sync(bte_ctx* c);
 void destroy_berta(bte_ctx* c);
+// Forget the loaded propagators (they refer to the previous mode table).
+void reset_propagators(bte_ctx* c);
 void destroy_steady(bte_ctx* c);
 // T0 of box b's material (the run's T0 without materials).
 double box_T0(const bte_ctx* c, int b, double T0);

@@ -320,9 +320,17 @@ bte_status bte_query_sizes(const bte_ctx* ctx, const bte_rta_params* params,
 /* Library version (BTEGPU_VERSION). */
 int32_t bte_version(void);
 
-/* Load the propagator of the (single) material for beyond-RTA runs
- * (replaces load_P and the propagator_H columns of process_input,
- * src/collision_operator.cpp:972-1013, src/beyondRTA_MC2d.cpp:1363-1377). */
+/* Load the propagator of the (single) material at temperature P->T for
+ * beyond-RTA runs (replaces load_P and the propagator_H columns of
+ * process_input, src/collision_operator.cpp:972-1013,
+ * src/beyondRTA_MC2d.cpp:1363-1377).  Calls with different T tabulate the
+ * propagator in temperature (a call at a T already loaded replaces it).  A
+ * run at T0 uses the propagator at T0 when it is tabulated; otherwise it
+ * interpolates as the reference does (Scattering :1130-1165, lirp
+ * src/collision_operator.cpp:918-929): linearly in the signed CDFs between
+ * the first tabulated temperature above T0 and the next one, and fails with
+ * BTE_ERR_INPUT when those two do not exist or T0 is below the lowest.
+ * bte_load_modes forgets every loaded propagator. */
 bte_status bte_load_propagator(bte_ctx* ctx, const bte_propagator* P);
 
 /* Run the beRTAMC2D step loop (replaces the loop of

@@ -55,6 +55,7 @@ def load():
         C.c_uint64, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.oracle_translate.restype = C.c_int
     lib.oracle_set_spectral.argtypes = [C.c_int, C.POINTER(C.c_int)]
+    lib.oracle_berta_run_tab.restype = C.c_int
     lib.oracle_kat_segment.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double, C.c_double, C.c_int,
                                        C.POINTER(C.c_double)]
     lib.oracle_kat_cdf_sample.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double]
@@ -446,15 +447,21 @@ def berta_run(modes, geom, P, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, gr
     npart = np.zeros(nsteps + 1, dtype=np.int64)
     H = np.zeros((nbx, n), dtype=np.int32)
     cnt = np.zeros(3, dtype=np.int64)
-    Pa = np.ascontiguousarray(np.asfortranarray(P).ravel(order="F")) if P is not None else np.zeros(1)
-    nmP = int(P.shape[0]) if P is not None else 0
+    # P: one matrix (taken at T0) or {T: matrix}, the propagator tabulated in temperature
+    tab = P if isinstance(P, dict) else ({T0: P} if P is not None else {})
+    Ts = np.array(sorted(tab), dtype=float)
+    Pa = (np.concatenate([np.asfortranarray(tab[t]).ravel(order="F") for t in Ts]) if len(tab)
+          else np.zeros(1))
+    Pa = np.ascontiguousarray(Pa, dtype=float)
+    nmP = int(next(iter(tab.values())).shape[0]) if tab else 0
     bp = _bt.berta_params(dt, maxtime, Eeff, T0, seed, rta, gradient=gradient)
-    st = lib.oracle_berta_run(C.byref(ms), C.byref(gs), Pa.ctypes.data_as(C.POINTER(C.c_double)), nmP,
-                              C.byref(bp), ed.ctypes.data_as(C.POINTER(C.c_double)),
-                              flux.ctypes.data_as(C.POINTER(C.c_double)),
-                              npart.ctypes.data_as(C.POINTER(C.c_int64)),
-                              H.ctypes.data_as(C.POINTER(C.c_int32)),
-                              cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+    dp = C.POINTER(C.c_double)
+    st = lib.oracle_berta_run_tab(C.byref(ms), C.byref(gs), Pa.ctypes.data_as(dp),
+                                  Ts.ctypes.data_as(dp) if len(Ts) else None, len(Ts), nmP,
+                                  C.byref(bp), ed.ctypes.data_as(dp), flux.ctypes.data_as(dp),
+                                  npart.ctypes.data_as(C.POINTER(C.c_int64)),
+                                  H.ctypes.data_as(C.POINTER(C.c_int32)),
+                                  cnt.ctypes.data_as(C.POINTER(C.c_int64)))
     if st != 0:
         raise _bt.BteError(st, lib.oracle_last_error().decode())
     return {"ed": ed, "flux": flux, "nparticles": npart, "H": H, "particle_steps": int(cnt[0]),

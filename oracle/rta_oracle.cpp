@@ -2479,9 +2479,25 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
 // propagator over modes 3..n-1 (ignored when params->rta).  Outputs per step
 // s = 0..nsteps: ed[s][box] (J m^-3), flux[s][box][2] (J m^-2 s^-1),
 // nparticles[s]; H_out: final histogram [box][mode] (optional).
+// beRTA with the propagator tabulated at nprop temperatures Ts (P: the
+// nprop column-major nmP x nmP matrices one after the other).  The run at
+// Teq = T0 takes the tabulated propagator at T0, or lirp between the first
+// tabulated temperature above T0 and the next one (Scattering,
+// src/beyondRTA_MC2d.cpp:1130-1165; lirp src/collision_operator.cpp:918-929).
+int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const double* P,
+                         const double* Ts, int nprop, int nmP, const bte_berta_params* bp, double* ed_out,
+                         double* flux_out, int64_t* np_out, int32_t* H_out, int64_t* counters);
+
 int oracle_berta_run(const bte_mode_table* mt, const bte_geometry* gm, const double* P, int nmP,
                      const bte_berta_params* bp, double* ed_out, double* flux_out,
                      int64_t* np_out, int32_t* H_out, int64_t* counters) {
+    const double T0 = bp->T0;
+    return oracle_berta_run_tab(mt, gm, P, &T0, 1, nmP, bp, ed_out, flux_out, np_out, H_out, counters);
+}
+
+int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const double* P,
+                         const double* Ts, int nprop, int nmP, const bte_berta_params* bp, double* ed_out,
+                         double* flux_out, int64_t* np_out, int32_t* H_out, int64_t* counters) {
     try {
         orc::BeRun R;
         R.S = build_sim(mt, gm);
@@ -2495,8 +2511,27 @@ int oracle_berta_run(const bte_mode_table* mt, const bte_geometry* gm, const dou
         if (!(R.Eeff > 0.)) return fail(BTE_ERR_INPUT, "Eeff must be positive");
         if (!R.rta) {
             if (nmP != int(n) - 3) return fail(BTE_ERR_INPUT, "propagator size must be nmodes - 3");
+            if (nprop < 1) return fail(BTE_ERR_INPUT, "no propagator");
             R.nm = nmP;
-            orc::build_cumm(R, P);
+            const std::size_t nn = std::size_t(nmP) * std::size_t(nmP);
+            std::map<double, const double*> tab;
+            for (int i = 0; i < nprop; ++i) tab[Ts[i]] = P + std::size_t(i) * nn;
+            const auto hit = tab.find(bp->T0);
+            if (hit != tab.end()) {
+                orc::build_cumm(R, hit->second);
+            } else {
+                const auto m1 = tab.lower_bound(bp->T0);
+                if (m1 == tab.end() || std::next(m1) == tab.end() || bp->T0 < tab.begin()->first)
+                    return fail(BTE_ERR_INPUT, "Extrapolation is not allowed");
+                const auto m2 = std::next(m1);
+                orc::BeRun R2;
+                R2.nm = nmP;
+                orc::build_cumm(R, m1->second);
+                orc::build_cumm(R2, m2->second);
+                const double T1 = m1->first, T2 = m2->first;
+                for (std::size_t i = 0; i < nn; ++i)
+                    R.cumm[i] = R.cumm[i] + (bp->T0 - T1) * (R2.cumm[i] - R.cumm[i]) / (T2 - T1);
+            }
         } else {
             std::vector<double> pmf(n);
             for (std::size_t k = 0; k < n; ++k)

@@ -199,3 +199,36 @@ def test_dist_reader_on_bertamc2d_frames(built, tmp_path):
             _, out = pyoracle.dist_reader_restated(m, area, 0.335, [0, 2], 30, hists, T, E)
             ref = out[b][0]
             assert np.allclose(dT[row, 1:], ref, rtol=2e-5, atol=1e-5 * np.abs(ref).max())
+
+
+def test_berta_interpolated_propagator_agrees_with_restatement(engine):
+    """Propagators tabulated at 290, 305 and 320 K, a run at 300 K: the
+    engine interpolates the signed CDFs (lirp, between 305 and 320 as the
+    reference picks them, so extrapolating) and draws from them by the
+    reference's lower_bound, whose |values| are not monotone in most
+    columns; energy density and flux against the restatement."""
+    m, g, _ = _case()
+    tab = {T: synth.propagator(m, T=T) for T in (290.0, 305.0, 320.0)}
+    engine.load_modes(m)
+    engine.load_geometry(g)
+    for T, P in tab.items():
+        engine.load_propagator(P, T)
+    R = 6
+    kw = dict(dt=1.0, maxtime=30.0, Eeff=2e-23, T0=300.0)
+    gpu = np.array([_obs(engine.berta_run(seed=10 + i, **kw)) for i in range(R)])
+    cpu = np.array([_obs(pyoracle.berta_run(m, g, tab, seed=20 + i, **kw)) for i in range(R)])
+    d = gpu.mean(0) - cpu.mean(0)
+    se = np.sqrt(gpu.var(0, ddof=1) / R + cpu.var(0, ddof=1) / R)
+    z = np.abs(d) / np.maximum(se, 1e-300)
+    assert z.max() < 4.5, (z, gpu.mean(0), cpu.mean(0))
+    # with 290 and 305 only, 300 K has one tabulated temperature above it
+    e2 = btegpu.Engine(0)
+    try:
+        e2.load_modes(m)
+        e2.load_geometry(g)
+        e2.load_propagator(tab[290.0], 290.0)
+        e2.load_propagator(tab[305.0], 305.0)
+        with pytest.raises(btegpu.BteError, match="Extrapolation"):
+            e2.berta_run(1.0, 5.0, 2e-23, T0=300.0)
+    finally:
+        e2.close()
