@@ -696,7 +696,8 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
                                        c->d_work.as<unsigned long long>(), c->tune, c->nsm, c->stream))
                 throw Error(BTE_ERR_INPUT, "tuning not supported by the grid kernel");
         } else {
-            bte::launch_prod_general(T, c->d_tally.as<double>(), counters, err, c->nsm, c->stream);
+            bte::launch_prod_general(T, c->d_tally.as<double>(), counters, err,
+                                     c->d_work.as<unsigned long long>(), c->nsm, c->stream);
         }
         ck(cudaGetLastError(), "kernel launch");
         ck(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");

@@ -25,9 +25,10 @@ struct ProdTuning {
 void launch_replay(const DevTables& T, unsigned long long* ex, unsigned long long* counters,
                    int* err, int nsm, cudaStream_t s);
 
-// General convex-box production kernel (any geometry).
+// General convex-box production kernel (any geometry); `work` is a zeroed
+// particle counter.
 void launch_prod_general(const DevTables& T, double* tally, unsigned long long* counters,
-                         int* err, int nsm, cudaStream_t s);
+                         int* err, unsigned long long* work, int nsm, cudaStream_t s);
 
 // One generation of the periodic / gradient steady state (rta_steady.cuh).
 // With `select_flags` set, only the generation-0 pre-pass runs: it writes 1

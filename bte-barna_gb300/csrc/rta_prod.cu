@@ -117,24 +117,101 @@ struct ProdPolicy {
     }
 };
 
+// Any convex-box geometry, the flight logic of rta_flight.cuh (run_particle
+// unrolled into one evolparticle step per loop pass).  Warps are persistent
+// and a lane whose particle has finished takes the next one from a global
+// counter (one atomic per warp), so lanes stay busy while particles of very
+// different lifetimes run out; each particle keeps its own Philox stream,
+// so its trajectory is the one run_particle would draw.
 __global__ void __launch_bounds__(128) rta_prod_general(DevTables T, double* tally,
-                                                        unsigned long long* counters, int* err) {
+                                                        unsigned long long* counters, int* err,
+                                                        unsigned long long* work) {
     Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const long long n = T.pend - T.pbegin;
-    const long long trips = (n + stride - 1) / stride;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    for (long long it = 0; it < trips; ++it) {
-        const long long pid = T.pbegin + it * stride + tid;
-        if (pid >= T.pend) continue;
-        ProdPolicy pol;
-        pol.g.init(T.seed, (uint64_t)pid);
-        pol.out = tally;
-        pol.ntally = 0;
-        const int e = run_particle(T, pol, pid, c);
-        c.tallies += pol.ntally;
-        if (e) record_error(err, e, pid);
+    const int lane = threadIdx.x & 31;
+    const long long total = T.pend - T.pbegin;
+    ProdPolicy pol;
+    pol.g.init(0, 0);
+    pol.out = tally;
+    pol.ntally = 0;
+    Particle p;
+    p.pos = v2(0., 0.);
+    p.mode = 0;
+    p.sign = 1;
+    p.t = 0.;
+    p.box = 0;
+    p.mo = 0;
+    V2 v = v2(0., 0.);
+    double dt = 0., time = 0.;
+    int nudges = 0, guard = 0, fate = FATE_LOST;
+    long long nev = 0, pid = -1;
+    bool active = false, done = false, need_flight = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active && !done);
+        if (idle) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active && !done) {
+                const long long mine = (long long)base + __popc(idle & ((1u << lane) - 1u));
+                if (mine < total) {
+                    pid = T.pbegin + mine;
+                    pol.g.init(T.seed, (uint64_t)pid);
+                    const int e = generate(T, pol, pid, p);
+                    if (e) {
+                        record_error(err, e, pid);
+                    } else {
+                        active = true;
+                        need_flight = true;
+                        time = 0.;
+                        nudges = 0;
+                        nev = 0;
+                    }
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!active) continue;
+        if (need_flight) {  // the body of run_particle's outer loop
+            if (!(time < T.maxtime)) {
+                active = false;
+                continue;
+            }
+            const int k = p.mode;
+            if (++nev > EVENT_CAP || T.w[p.mo + k] == 0.) {
+                record_error(err, nev > EVENT_CAP ? E_LIMIT : E_VALUE, pid);
+                active = false;
+                continue;
+            }
+            v = v2(T.vxc[k], T.vyc[k]);
+            dt = pol.flight(T, p.mo + k);
+            c.events++;
+            if (time + dt > T.maxtime) dt = T.maxtime - time + 1.0e-8;
+            guard = 0;
+            fate = FATE_LOST;
+            need_flight = false;
+        }
+        if (!almost_equal(dt, 0.)) {
+            int e = ++guard > FLIGHT_CAP ? E_LIMIT : 0;
+            if (!e) e = evolparticle(T, pol, p, v, dt, c, nudges, fate);
+            if (e) {
+                record_error(err, e, pid);
+                active = false;
+                continue;
+            }
+        }
+        if (almost_equal(dt, 0.)) {  // the flight is over
+            if (p.mode == 0) {       // absorbed
+                active = false;
+                continue;
+            }
+            time = p.t;
+            need_flight = true;
+        }
     }
+    c.tallies += pol.ntally;
     flush_counters_p(c, counters);
 }
 
@@ -187,13 +264,13 @@ void launch_steady_prod(const DevTables& T, const SteadyArgs& A, double* tally,
 }
 
 void launch_prod_general(const DevTables& T, double* tally, unsigned long long* counters,
-                         int* err, int nsm, cudaStream_t s) {
+                         int* err, unsigned long long* work, int nsm, cudaStream_t s) {
     const long long n = T.pend - T.pbegin;
     if (n <= 0) return;
     long long blocks = (n + 127) / 128;
-    const long long cap = (long long)nsm * 16;
+    const long long cap = (long long)nsm * 3;  // resident blocks (145 registers x 128 threads)
     if (blocks > cap) blocks = cap;
-    rta_prod_general<<<unsigned(blocks), 128, 0, s>>>(T, tally, counters, err);
+    rta_prod_general<<<unsigned(blocks), 128, 0, s>>>(T, tally, counters, err, work);
 }
 
 // ------------------------------------------------------------------ grid path
