@@ -225,30 +225,73 @@ __global__ void steady_select_prod(SteadyArgs A, unsigned long long seed, unsign
     }
 }
 
+// One generation: each slot's one flight, one evolparticle step per loop
+// pass, with persistent warps whose finished lanes take the next slot.
 __global__ void __launch_bounds__(128) rta_steady_prod(DevTables T, SteadyArgs A, double* tally,
                                                        unsigned long long* counters, int* err) {
     Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const long long trips = (A.n + stride - 1) / stride;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    for (long long it = 0; it < trips; ++it) {
-        const long long slot = it * stride + tid;
-        if (slot >= A.n) continue;
-        ProdPolicy pol;
-        pol.g.init(T.seed, steady_stream(A.gen, slot));
-        pol.out = tally;
-        pol.ntally = 0;
-        Particle p;
-        int fate = FATE_LOST;
-        const int e = steady_slot(T, A, pol, slot, c, fate, p);
-        c.tallies += pol.ntally;
-        if (e) {
-            record_error(err, e, slot);
-            A.flag[slot] = 0;
-        } else {
+    const int lane = threadIdx.x & 31;
+    ProdPolicy pol;
+    pol.g.init(0, 0);
+    pol.out = tally;
+    pol.ntally = 0;
+    Particle p;
+    p.pos = v2(0., 0.);
+    p.mode = 0;
+    p.sign = 1;
+    p.t = 0.;
+    p.box = 0;
+    p.mo = 0;
+    V2 v = v2(0., 0.);
+    double dt = 0.;
+    int nudges = 0, guard = 0, fate = FATE_LOST;
+    long long slot = -1;
+    bool active = false, done = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active && !done);
+        if (idle) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader) base = atomicAdd(A.work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active && !done) {
+                slot = (long long)base + __popc(idle & ((1u << lane) - 1u));
+                if (slot < A.n) {
+                    pol.g.init(T.seed, steady_stream(A.gen, slot));
+                    const int e = steady_begin(T, A, pol, slot, c, p, v, dt);
+                    if (e) {
+                        record_error(err, e, slot);
+                        A.flag[slot] = 0;
+                    } else {
+                        active = true;
+                        fate = FATE_LOST;
+                        guard = 0;
+                        nudges = 0;
+                    }
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!active) continue;
+        if (!almost_equal(dt, 0.)) {
+            int e = ++guard > FLIGHT_CAP ? E_LIMIT : 0;
+            if (!e) e = evolparticle<ProdPolicy, true>(T, pol, p, v, dt, c, nudges, fate);
+            if (e) {
+                record_error(err, e, slot);
+                A.flag[slot] = 0;
+                active = false;
+                continue;
+            }
+        }
+        if (almost_equal(dt, 0.)) {  // the flight is over
+            if (fate == FATE_LOST) c.lost++;
             steady_emit(A, slot, fate, p);
+            active = false;
         }
     }
+    c.tallies += pol.ntally;
     flush_counters_p(c, counters);
 }
 
@@ -257,10 +300,16 @@ void launch_steady_prod(const DevTables& T, const SteadyArgs& A, double* tally,
                         cudaStream_t s) {
     if (A.n <= 0) return;
     long long blocks = (A.n + 127) / 128;
-    const long long cap = (long long)nsm * 16;
+    if (select_flags) {
+        const long long cap = (long long)nsm * 16;
+        if (blocks > cap) blocks = cap;
+        steady_select_prod<<<unsigned(blocks), 128, 0, s>>>(A, T.seed, select_flags);
+        return;
+    }
+    const long long cap = (long long)nsm * 4;  // resident blocks of the persistent kernel (128 registers)
     if (blocks > cap) blocks = cap;
-    if (select_flags) steady_select_prod<<<unsigned(blocks), 128, 0, s>>>(A, T.seed, select_flags);
-    else rta_steady_prod<<<unsigned(blocks), 128, 0, s>>>(T, A, tally, counters, err);
+    cudaMemsetAsync(A.work, 0, sizeof(unsigned long long), s);
+    rta_steady_prod<<<unsigned(blocks), 128, 0, s>>>(T, A, tally, counters, err);
 }
 
 void launch_prod_general(const DevTables& T, double* tally, unsigned long long* counters,

@@ -48,6 +48,7 @@ struct SteadyArgs {
     SteadyP* out;              // [slots] the reflected particle of each slot
     unsigned* flag;            // [slots] 1 when the slot's particle was reflected
     unsigned long long* phi;   // [nboxes] signed counts, two's complement
+    unsigned long long* work;  // slots taken (production kernel), zeroed per launch
 };
 
 __device__ __forceinline__ uint64_t steady_stream(int gen, long long slot) {
@@ -117,10 +118,11 @@ __device__ int steady_birth(const DevTables& T, const SteadyArgs& A, P& pol, lon
     return 0;
 }
 
-// The slot's particle and its one flight.  Returns 0 or an error code.
+// The slot's particle and the draw of its one flight (v, dt).  Returns 0 or
+// an error code.
 template <class P>
-__device__ int steady_slot(const DevTables& T, const SteadyArgs& A, P& pol, long long slot,
-                           Counters& c, int& fate, Particle& p) {
+__device__ int steady_begin(const DevTables& T, const SteadyArgs& A, P& pol, long long slot,
+                            Counters& c, Particle& p, V2& v, double& dt) {
     int e;
     if (A.gen == 0) {
         e = steady_generate0(T, A, pol, slot, p);
@@ -138,10 +140,21 @@ __device__ int steady_slot(const DevTables& T, const SteadyArgs& A, P& pol, long
     }
     if (e) return e;
     const int k = p.mode;
-    const V2 v = v2(T.vxc[k], T.vyc[k]);
+    v = v2(T.vxc[k], T.vyc[k]);
     if (T.w[p.mo + k] == 0.) return E_VALUE;
-    double dt = pol.flight(T, p.mo + k);
+    dt = pol.flight(T, p.mo + k);
     c.events++;
+    return 0;
+}
+
+// The slot's particle and its one flight.  Returns 0 or an error code.
+template <class P>
+__device__ int steady_slot(const DevTables& T, const SteadyArgs& A, P& pol, long long slot,
+                           Counters& c, int& fate, Particle& p) {
+    V2 v;
+    double dt = 0.;
+    int e = steady_begin(T, A, pol, slot, c, p, v, dt);
+    if (e) return e;
     fate = FATE_LOST;
     int guard = 0, nudges = 0;
     while (!almost_equal(dt, 0.)) {

@@ -26,7 +26,7 @@ struct SteadyState {
     DBuf sbox, scum, scdf, sprob, salt, ssign;    // gradient generators
     DBuf pin, ptmp, flag, pos, sums, rank, phi;   // particles and scan scratch
     DBuf bfirst, bbox, bsign;                     // births
-    DBuf tally, counters, err;
+    DBuf tally, counters, err, work;
 };
 
 namespace {
@@ -277,6 +277,8 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         A.out = S.ptmp.as<SteadyP>();
         A.flag = S.flag.as<unsigned>();
         A.phi = S.phi.as<unsigned long long>();
+        S.work.alloc(sizeof(unsigned long long));
+        A.work = S.work.as<unsigned long long>();
 
         const int max_gen = p->max_generations > 0 ? p->max_generations : 100000;
         std::vector<double> oldv(size_t(3) * nbx, 0.), cur(size_t(3) * nbx, 0.);
