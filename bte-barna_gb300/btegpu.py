@@ -18,7 +18,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbtegpu.so")
 
-BTE_OK, BTE_ERR_INPUT, BTE_ERR_VALUE, BTE_ERR_GEOMETRY, BTE_ERR_LIMIT, BTE_ERR_CUDA, BTE_ERR_STATE = range(7)
+(BTE_OK, BTE_ERR_INPUT, BTE_ERR_VALUE, BTE_ERR_GEOMETRY, BTE_ERR_LIMIT, BTE_ERR_CUDA, BTE_ERR_STATE,
+ BTE_ERR_CHECK) = range(8)
+FLAG_CHECKS = 1
 STATUS_NAMES = {0: "ok", 1: "input_error", 2: "value_error", 3: "geometry_error",
                 4: "limit", 5: "cuda_error", 6: "state_error"}
 MODE_REPLAY, MODE_PRODUCTION = 0, 1
@@ -60,9 +62,9 @@ class Geometry(C.Structure):
 class RtaParams(C.Structure):
     _fields_ = [("T0", C.c_double), ("dt", C.c_double), ("maxtime", C.c_double),
                 ("nparticles", C.c_int64), ("seed", C.c_uint64), ("mode", C.c_int32),
-                ("source", C.c_int32), ("ballistic", C.c_int32), ("reserved0", C.c_int32),
+                ("source", C.c_int32), ("ballistic", C.c_int32), ("flags", C.c_int32),
                 ("specularity", C.c_double), ("particle_begin", C.c_int64),
-                ("particle_end", C.c_int64)]
+                ("particle_end", C.c_int64), ("flight_cap", C.c_int64)]
 
 
 class RtaResult(C.Structure):
@@ -230,11 +232,14 @@ def geom_struct(g: dict):
 
 
 def params_struct(T0, dt, maxtime, N, seed=1, mode=MODE_PRODUCTION, source=SOURCE_WALLS,
-                  ballistic=False, specularity=0.0, begin=0, end=0):
+                  ballistic=False, specularity=0.0, begin=0, end=0, flags=0, flight_cap=0):
+    """`flags`: FLAG_CHECKS for the checked grid kernel; `flight_cap`: free
+    flights per particle before BTE_ERR_LIMIT (0: the default)."""
     p = RtaParams()
     p.T0, p.dt, p.maxtime, p.nparticles, p.seed = float(T0), float(dt), float(maxtime), int(N), int(seed)
     p.mode, p.source, p.ballistic = int(mode), int(source), int(bool(ballistic))
     p.specularity, p.particle_begin, p.particle_end = float(specularity), int(begin), int(end)
+    p.flags, p.flight_cap = int(flags), int(flight_cap)
     return p
 
 
@@ -342,8 +347,10 @@ class Engine:
         self._check(self.lib.bte_set_tuning(self.ctx, C.byref(t)))
 
     def rta_run(self, T0, dt, maxtime, N, seed=1, mode=MODE_PRODUCTION, source=SOURCE_WALLS,
-                ballistic=False, specularity=0.0, begin=0, end=0, raw=True, exact=False):
-        p = params_struct(T0, dt, maxtime, N, seed, mode, source, ballistic, specularity, begin, end)
+                ballistic=False, specularity=0.0, begin=0, end=0, raw=True, exact=False, flags=0,
+                flight_cap=0):
+        p = params_struct(T0, dt, maxtime, N, seed, mode, source, ballistic, specularity, begin, end,
+                          flags, flight_cap)
         nbx, nbn, nm = C.c_int32(), C.c_int32(), C.c_int64()
         self._check(self.lib.bte_query_sizes(self.ctx, C.byref(p), C.byref(nbx), C.byref(nbn), C.byref(nm)))
         shape = (nbx.value, nbn.value)

@@ -651,6 +651,8 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         T.init_box = c->d_ibox.as<int>();
         T.init_sign = c->d_isign.as<int>();
         T.seed = p->seed;
+        T.flight_cap = p->flight_cap > 0 ? p->flight_cap : bte::EVENT_CAP;
+        T.checks = (p->flags & BTE_FLAG_CHECKS) ? 1 : 0;
         T.ballistic = p->ballistic;
         T.specularity = p->specularity;
         T.pbegin = pbeg;
@@ -746,6 +748,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
             std::snprintf(msg, sizeof msg, "particle %lld: %s", pid,
                           herr[0] == BTE_ERR_VALUE ? "invalid scattering rate"
                           : herr[0] == BTE_ERR_LIMIT ? "iteration cap reached"
+                          : herr[0] == BTE_ERR_CHECK ? "index check failed"
                                                       : "geometry error");
             throw Error(bte_status(herr[0]), msg);
         }
@@ -1028,6 +1031,8 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
     T.init_box = c->d_ibox.as<int>();
     T.init_sign = c->d_isign.as<int>();
     T.seed = p->seed;
+    T.flight_cap = p->flight_cap > 0 ? p->flight_cap : EVENT_CAP;
+    T.checks = (p->flags & BTE_FLAG_CHECKS) ? 1 : 0;
     T.ballistic = p->ballistic;
     T.specularity = p->specularity;
     T.pbegin = pbeg;

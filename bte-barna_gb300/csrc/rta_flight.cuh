@@ -24,7 +24,7 @@ constexpr int NUDGE_CAP = 64;   // consecutive geometry nudges
 constexpr long long EVENT_CAP = 1ll << 26;  // free flights per particle
 
 // Error codes written to the device error word (bte_status values).
-constexpr int E_VALUE = 2, E_GEOM = 3, E_LIMIT = 4;
+constexpr int E_VALUE = 2, E_GEOM = 3, E_LIMIT = 4, E_CHECK = 7;
 
 struct WallGenDev {
     V2 p1, nd, sa, sb;
@@ -76,6 +76,8 @@ struct DevTables {
     unsigned long long seed;
     int ballistic;
     double specularity;
+    long long flight_cap;  // free flights per particle (EVENT_CAP unless the run sets one)
+    int checks;            // BTE_FLAG_CHECKS: the checked grid-kernel variant
     long long pbegin, pend;
     int nbins;
     // spectral decomposition: box -> location (-1: none, null: off) and the
@@ -581,7 +583,7 @@ __device__ int run_particle(const DevTables& T, P& pol, long long pid, Counters&
     int nudges = 0;
     long long nev = 0;
     while (time < T.maxtime) {
-        if (++nev > EVENT_CAP) return E_LIMIT;
+        if (++nev > T.flight_cap) return E_LIMIT;
         const int k = p.mode;
         const V2 v = v2(T.vxc[k], T.vyc[k]);
         const double w = T.w[p.mo + k];

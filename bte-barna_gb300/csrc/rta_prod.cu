@@ -180,8 +180,8 @@ __global__ void __launch_bounds__(128) rta_prod_general(DevTables T, double* tal
                 continue;
             }
             const int k = p.mode;
-            if (++nev > EVENT_CAP || T.w[p.mo + k] == 0.) {
-                record_error(err, nev > EVENT_CAP ? E_LIMIT : E_VALUE, pid);
+            if (++nev > T.flight_cap || T.w[p.mo + k] == 0.) {
+                record_error(err, nev > T.flight_cap ? E_LIMIT : E_VALUE, pid);
                 active = false;
                 continue;
             }
@@ -465,7 +465,10 @@ __device__ __forceinline__ uint4 pass_block(uint32_t pass, uint64_t pid, uint64_
 //   post-scattering draw of mode k (p_k ~ C_k / tau_k): -1 / tau_k on tau_k,
 //     plus p_i / tau_i on every tau_i (summed once on the host from sum R)
 //   specularity draw at a void wall:       1 / p (specular) or -1 / (1 - p)
-template <bool SMEM_TALLY, int MINB, int ADJ>
+// CHECK: the checked variant (BTE_FLAG_CHECKS): every table, tally and grid
+// index is tested before use; a violation stops the particle with E_CHECK.
+// The checks draw nothing, so the trajectories are the plain variant's.
+template <bool SMEM_TALLY, int MINB, int ADJ, bool CHECK = false>
 __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs A, double* gtally,
                                                      unsigned long long* counters, int* err,
                                                      unsigned long long* work, AdjArgs adj) {
@@ -515,8 +518,18 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     // dt = -tau ln u (FP32 log), u = (k + 1/2) 2^-23 from 23 bits, never 0
     // or 1; its velocities stay in registers for the segments that follow.
     // Returns false when the particle stops with an error.
+    // a failed index check stops the particle (checked variant only)
+    auto check_fail = [&]() {
+        record_error(err, E_CHECK, pid);
+        active = false;
+        done = true;
+    };
     auto new_flight = [&](uint32_t word) -> bool {
         const int k = p.mode;
+        if (CHECK && (k < 0 || k >= T.n || p.mo < 0)) {
+            check_fail();
+            return false;
+        }
         mv = A.mv[k];
         const float ef = -logf((float(word >> 9) + 0.5f) * 0x1p-23f);
         const double tau_k = __ldg(T.tau + p.mo + k);
@@ -537,7 +550,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             pend_kind = 0;
             atomicAdd(adj.g_tau + k, gk);
         }
-        if (ob(dt) <= 0 || ++nev > EVENT_CAP) {  // zero rate or runaway particle
+        if (ob(dt) <= 0 || ++nev > T.flight_cap) {  // zero rate or runaway particle
             record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
             active = false;
             done = true;
@@ -559,7 +572,10 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                 if (mine < total) {
                     pid = T.pbegin + mine;
                     g.init(T.seed, (uint64_t)pid);
-                    const int e = grid_generate(T, A.G, A.boxcell, g, pid, p);
+                    int e = grid_generate(T, A.G, A.boxcell, g, pid, p);
+                    if (CHECK && !e &&
+                        (p.box < 0 || p.box >= T.nboxes || p.i < 0 || p.i >= A.G.nx || p.j < 0 || p.j >= A.G.ny))
+                        e = E_CHECK;
                     if (e) {
                         record_error(err, e, pid);
                         done = true;
@@ -593,6 +609,11 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
         // so (line - position) >= 0 times its +inf inverse gives +inf (or NaN
         // on the line, ordered above +inf); a negative value (a position that
         // rounded past its line) orders below 0 and ends the segment at once.
+        if (CHECK && (p.i < 0 || p.i >= A.G.nx || p.j < 0 || p.j >= A.G.ny || p.box < 0 || p.box >= T.nboxes ||
+                      bin < 0 || bin > last_bin)) {
+            check_fail();
+            continue;
+        }
         const int upx = ob(mv.vx) >= 0 ? 1 : 0;
         const int upy = ob(mv.vy) >= 0 ? 1 : 0;
         const double xw = __ldg(A.G.gx + p.i + upx);
@@ -653,6 +674,14 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             const double cphi = __ldg(Wk) * d0 + __ldg(Wk + 1) * d1 + __ldg(Wk + 2) * d2;
             phi_run += p.sign < 0 ? -cphi : cphi;
         }
+        if (CHECK && (move || absorbed || bin_end) && (pd.key < 0 || pd.key >= T.nboxes * T.nbins)) {
+            check_fail();
+            continue;
+        }
+        if (CHECK && move && nb >= T.nboxes) {
+            check_fail();
+            continue;
+        }
         if (move || absorbed || bin_end) {
             double* b = tally + 3ll * pd.key;
             atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(d0) ^ signbit));
@@ -699,6 +728,10 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                         active = false;
                         done = true;
                         pd.flush(tally, signbit, rb, p.x, p.y);
+                        continue;
+                    }
+                    if (CHECK && cls >= T.nclass) {
+                        check_fail();
                         continue;
                     }
                     int mirror_mode = -1;
@@ -785,6 +818,16 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
     int bps = tune.blocks_per_sm > 0 ? tune.blocks_per_sm : (use_smem ? 1 : 3);
     const AdjArgs none{};
     const AdjArgs& aa = adj ? *adj : none;
+    if (T.checks && adj_pass == 0) {  // the checked variant, at its own residency
+        int maxb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, rta_prod_grid<false, 2, 0, true>, 256, 0);
+        if (maxb < 1) return false;
+        long long blocks = (long long)nsm * (maxb < 2 ? maxb : 2);
+        const long long need = (n + 255) / 256;
+        if (blocks > need) blocks = need;
+        rta_prod_grid<false, 2, 0, true><<<unsigned(blocks), 256, 0, s>>>(T, A, tally, counters, err, work, aa);
+        return true;
+    }
     const void* fn;
     if (use_smem) {
         fn = reinterpret_cast<const void*>(rta_prod_grid<true, 1, 0>);

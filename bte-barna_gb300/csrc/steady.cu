@@ -239,6 +239,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         T.gen_prob = S.gprob.as<float>();
         T.gen_alt = S.galt.as<int>();
         T.seed = p->seed;
+        T.flight_cap = EVENT_CAP;
         T.nbins = 1;
         T.specularity = p->specularity;
         // spectral decomposition at the selected boxes: per-mode time and

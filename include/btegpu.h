@@ -40,7 +40,8 @@ typedef enum bte_status {
     BTE_ERR_GEOMETRY = 3, /* alma::geometry_error: inconsistent geometry      */
     BTE_ERR_LIMIT = 4,    /* a device loop reached its iteration cap          */
     BTE_ERR_CUDA = 5,     /* CUDA runtime failure                             */
-    BTE_ERR_STATE = 6     /* wrong call order (e.g. run before load)          */
+    BTE_ERR_STATE = 6,    /* wrong call order (e.g. run before load)          */
+    BTE_ERR_CHECK = 7     /* an index check of BTE_FLAG_CHECKS failed          */
 } bte_status;
 
 /* Run modes. */
@@ -119,11 +120,19 @@ typedef struct bte_rta_params {
     int32_t mode;            /* BTE_MODE_*                                      */
     int32_t source;          /* BTE_SOURCE_*                                    */
     int32_t ballistic;       /* 1: no intrinsic scattering (<ballistic/>)       */
-    int32_t reserved0;
+    int32_t flags;           /* BTE_FLAG_* (0: none)                            */
     double specularity;      /* p of void walls; 0 = the reference's diffuse    */
     int64_t particle_begin;  /* simulate particles [begin, end) of the N;      */
     int64_t particle_end;    /*   end <= 0 means N                              */
+    int64_t flight_cap;      /* free flights per particle before BTE_ERR_LIMIT
+                                (0: 2^26); a small cap injects the limit path   */
 } bte_rta_params;
+
+/* Run flags.  BTE_FLAG_CHECKS runs the production grid kernel in its checked
+ * variant: every table, tally and grid index is tested before use and a
+ * violation stops the particle with BTE_ERR_CHECK instead of an out-of-range
+ * access (the same draws as the plain variant, so the same trajectories). */
+#define BTE_FLAG_CHECKS 1
 
 /* Results of one RTA run.  Every array pointer may be NULL (not written).
  * Arrays are row-major [nboxes][nbins]. */
