@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -954,6 +955,7 @@ double wall_pmf(const bte::HostModes& m, bte::V2 n, double Tw, double Te, std::v
 extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_berta_result* out) {
     using namespace bte;
     if (!c || !p || !out) return BTE_ERR_INPUT;
+    const auto t_start = std::chrono::steady_clock::now();
     try {
         if (!(p->dt > 0.) || !(p->maxtime >= 0.) || !(p->Eeff > 0.) || !(p->T0 > 0.))
             throw Error(BTE_ERR_INPUT, "dt, Eeff and T0 must be positive and maxtime >= 0");
@@ -1256,11 +1258,25 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         long long psteps = 0, branchings = 0;
         int istep = 0;
         double time = 0.;
+        // phase timing (the reference's timer buckets): events at the phase
+        // borders of every step, read after the step's last sync
+        enum { PH_ADV, PH_CANCEL, PH_GEN, PH_HIST, PH_PROPS, PH_READ, PH_SAVE, PH_SCAT };
+        double phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        cudaEvent_t pe[7];
+        for (auto& e : pe) ck(cudaEventCreate(&e), "cudaEventCreate");
+        struct EvGuard {
+            cudaEvent_t* e;
+            ~EvGuard() {
+                for (int i = 0; i < 7; ++i) cudaEventDestroy(e[i]);
+            }
+        } pe_guard{pe};
+        phase[PH_READ] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         std::vector<int> hE(static_cast<std::size_t>(nborders));
         std::vector<int> hH;
         std::vector<double> pmf;
         const int cancel_every = p->cancel_every > 0 ? p->cancel_every : 4;
         while (time <= p->maxtime) {
+            ck(cudaEventRecord(pe[0], s), "event");
             // 1. advection
             if (np > 0) {
                 AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0,
@@ -1269,6 +1285,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                                                                     0, np, aa);
             }
             psteps += np;
+            ck(cudaEventRecord(pe[1], s), "event");
             // 2. gradient source term: Ntogenerate(dt, vol, Eeff) per box
             if (!grad.box.empty()) {
                 descs.clear();
@@ -1374,6 +1391,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             generate(np, nnew, istep, 4, true);
             np += nnew;
+            ck(cudaEventRecord(pe[2], s), "event");
             // 5. delete absorbed particles
             np = compact(np);
             // 6. scattering
@@ -1404,11 +1422,13 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 std::swap(B.a_box.p, B.b_box.p);
                 std::swap(B.a_sign.p, B.b_sign.p);
             }
+            ck(cudaEventRecord(pe[3], s), "event");
             // 7.-9. histogram, cancellation, properties
             ck(cudaMemsetAsync(B.d_H.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
             if (np > 0)
                 be_hist<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
                                                                   np, B.d_H.as<int>(), n);
+            ck(cudaEventRecord(pe[4], s), "event");
             if (istep % cancel_every == 0 && np > 0) {
                 ck(cudaMemsetAsync(B.d_cnt.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
                 // random affine permutation of the visiting order (a coprime to np)
@@ -1419,12 +1439,21 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                                                                     d_res.as<int>(), pa, pb);
                 np = compact(np);
             }
+            ck(cudaEventRecord(pe[5], s), "event");
             be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),
                                           B.d_props.as<double>());
             int herr[4];
             ck(cudaMemcpyAsync(hprops.data(), B.d_props.p, hprops.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "d2h");
             ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaEventRecord(pe[6], s), "event");
             sync(c);
+            {
+                const int bucket[6] = {PH_ADV, PH_GEN, PH_SCAT, PH_HIST, PH_CANCEL, PH_PROPS};
+                for (int k = 0; k < 6; ++k) {
+                    float ms = 0.f;
+                    if (cudaEventElapsedTime(&ms, pe[k], pe[k + 1]) == cudaSuccess) phase[bucket[k]] += ms;
+                }
+            }
             for (int b = 0; b < nbx; ++b) {
                 const double f1 = p->Eeff / vol[std::size_t(b)] * 1.0e+27;
                 const double f2 = p->Eeff / vol[std::size_t(b)] * 1.0e+30;
@@ -1446,7 +1475,9 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                     fl[2 * std::size_t(b)] = p->Eeff / vol[std::size_t(b)] * 1.0e+30 * hprops[3 * std::size_t(b) + 1];
                     fl[2 * std::size_t(b) + 1] = p->Eeff / vol[std::size_t(b)] * 1.0e+30 * hprops[3 * std::size_t(b) + 2];
                 }
+                const auto t_save = std::chrono::steady_clock::now();
                 p->on_step(p->user, istep + 1, time + p->dt, np, hH.data(), nbx, n, ed.data(), fl.data());
+                phase[PH_SAVE] += 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t_save).count();
             }
             if (herr[0] != 0)
                 throw Error(bte_status(herr[0]), herr[0] == BTE_ERR_LIMIT      ? "particle capacity or step cap exceeded"
@@ -1466,6 +1497,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         out->particle_steps = psteps;
         out->branchings = branchings;
         out->kernel_ms = ms;
+        for (int k = 0; k < 8; ++k) out->phase_ms[k] = phase[k];
         return BTE_OK;
     } catch (const Error& e) {
         c->err = e.what();

@@ -299,6 +299,14 @@ int main(int argc, char** argv) {
         std::cout << "#steps " << out.nsteps << ", particle-steps " << out.particle_steps << " in "
                   << std::chrono::duration<double>(t1 - t0).count() << " s (device " << out.kernel_ms << " ms)"
                   << std::endl;
+        // the reference's time report (timer::print_report, src/beyondRTA_MC2d.cpp:1883-1896)
+        static const char* names[8] = {"advection", "cancelling", "generators", "histogram",
+                                       "properties", "read_data", "saving", "scattering"};
+        std::cout << "###################\n#TIME report:" << std::endl;
+        for (int k = 0; k < 8; ++k) std::cout << " *" << names[k] << " : " << out.phase_ms[k] * 1e-3 << " s " << std::endl;
+        std::cout << "###################\n";
+        std::cout << "TOTAL TIME : " << std::chrono::duration<double>(t1 - t0).count() << " s " << std::endl;
+        std::cout << "###################\n";
     } catch (const std::exception& e) {
         std::cerr << "error: " << e.what() << std::endl;
         return 2;

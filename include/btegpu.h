@@ -213,6 +213,11 @@ typedef struct bte_berta_result {
     int64_t particle_steps;  /* particles advected, summed over steps           */
     int64_t branchings;      /* sign flips that re-entered the scattering queue  */
     double kernel_ms;        /* device time of the step loop                     */
+    double phase_ms[8];      /* out: the reference's timer buckets (src/beyondRTA_MC2d.cpp:
+                                1838-1897), sorted by name: advection, cancelling,
+                                generators, histogram, properties, read_data, saving,
+                                scattering; device time per step phase, host time
+                                for read_data (set-up) and saving (on_step)     */
 } bte_berta_result;
 
 /* Parameters of a steady-state run of a periodic structure under an applied

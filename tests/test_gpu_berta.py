@@ -78,6 +78,7 @@ def test_bertamc2d_cli_writes_table_and_frames(built, tmp_path):
     data = (tmp_path / "properties.msgpack.bin").read_bytes()
     assert data.endswith(b"0#")
     assert len(btegpu.split_frames(data)) == 11
+    assert "#TIME report:" in r.stdout and " *scattering : " in r.stdout
 
 
 def _bar_obs(r):
@@ -232,3 +233,20 @@ def test_berta_interpolated_propagator_agrees_with_restatement(engine):
             e2.berta_run(1.0, 5.0, 2e-23, T0=300.0)
     finally:
         e2.close()
+
+
+def test_berta_phase_times(engine, built, tmp_path):
+    """The reference's timer buckets: device time per step phase, which add
+    up to no more than the device time of the loop; the CLI prints the
+    reference's time report."""
+    m, g, P = _case()
+    engine.load_modes(m)
+    engine.load_geometry(g)
+    engine.load_propagator(P)
+    r = engine.berta_run(1.0, 20.0, 2e-23, seed=3)
+    ph = r["phase_ms"]
+    for k in ("advection", "generators", "scattering", "histogram", "properties", "read_data"):
+        assert ph[k] > 0.0, k
+    device = sum(ph[k] for k in ("advection", "cancelling", "generators", "histogram", "properties", "scattering"))
+    assert device <= r["kernel_ms"] * 1.01 + 0.1
+    assert ph["saving"] == 0.0  # no on_step hook here
