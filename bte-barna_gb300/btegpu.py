@@ -21,6 +21,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libbtegpu.so")
 (BTE_OK, BTE_ERR_INPUT, BTE_ERR_VALUE, BTE_ERR_GEOMETRY, BTE_ERR_LIMIT, BTE_ERR_CUDA, BTE_ERR_STATE,
  BTE_ERR_CHECK) = range(8)
 FLAG_CHECKS = 1
+FLAG_GENERAL = 2
 STATUS_NAMES = {0: "ok", 1: "input_error", 2: "value_error", 3: "geometry_error",
                 4: "limit", 5: "cuda_error", 6: "state_error"}
 MODE_REPLAY, MODE_PRODUCTION = 0, 1
@@ -237,7 +238,8 @@ def geom_struct(g: dict):
 
 def params_struct(T0, dt, maxtime, N, seed=1, mode=MODE_PRODUCTION, source=SOURCE_WALLS,
                   ballistic=False, specularity=0.0, begin=0, end=0, flags=0, flight_cap=0):
-    """`flags`: FLAG_CHECKS for the checked grid kernel; `flight_cap`: free
+    """`flags`: FLAG_CHECKS for the checked grid kernel, FLAG_GENERAL for the
+    evolparticle-faithful kernel on boxes off a grid; `flight_cap`: free
     flights per particle before BTE_ERR_LIMIT (0: the default)."""
     p = RtaParams()
     p.T0, p.dt, p.maxtime, p.nparticles, p.seed = float(T0), float(dt), float(maxtime), int(N), int(seed)

@@ -78,6 +78,49 @@ void ensure_static(bte_ctx* c) {
                     if (b >= 0) bc[std::size_t(b)] = make_int2(i, j);
                 }
             c->d_boxcell.upload(bc, c->stream);
+        } else {
+            // border lines and neighbour pieces of the convex-polygon path:
+            // a segment contact of box a lies on the border of a whose
+            // outward normal is the contact's normal; its ends give the
+            // interval of arc length that leads into the neighbour
+            std::vector<bte::PolyBorder> pb(g.borders.size());
+            std::vector<bte::PolyPiece> pieces;
+            for (std::size_t a = 0; a < g.boxes.size(); ++a) {
+                const bte::GBox& bx = g.boxes[a];
+                for (int k = 0; k < bx.nborders; ++k) {
+                    const std::size_t gb = std::size_t(bx.border_off + k);
+                    const bte::GBorder& br = g.borders[gb];
+                    bte::PolyBorder& P = pb[gb];
+                    const double len = std::hypot(br.p2.x - br.p1.x, br.p2.y - br.p1.y);
+                    P.nx = br.np.x;
+                    P.ny = br.np.y;
+                    P.c = br.np.x * br.p1.x + br.np.y * br.p1.y;
+                    P.px = br.p1.x;
+                    P.py = br.p1.y;
+                    P.ux = len > 0. ? (br.p2.x - br.p1.x) / len : 0.;
+                    P.uy = len > 0. ? (br.p2.y - br.p1.y) / len : 0.;
+                    P.cls = br.ncls;
+                    P.piece_off = int(pieces.size());
+                    for (int i = 0; i < bx.ncontacts; ++i) {
+                        const std::size_t ci = std::size_t(bx.contact_off + i);
+                        const bte::GBorder& cb = g.contact_borders[ci];
+                        if (cb.p1.x == cb.p2.x && cb.p1.y == cb.p2.y) continue;  // point contact
+                        const bte::GContact& gc = g.contacts[ci];
+                        if (std::fabs(gc.np.x - br.np.x) > 1e-9 || std::fabs(gc.np.y - br.np.y) > 1e-9) continue;
+                        const double d1 = br.np.x * cb.p1.x + br.np.y * cb.p1.y - P.c;
+                        const double d2 = br.np.x * cb.p2.x + br.np.y * cb.p2.y - P.c;
+                        if (std::fabs(d1) > 1e-6 || std::fabs(d2) > 1e-6) continue;  // on another line
+                        double s0 = (cb.p1.x - P.px) * P.ux + (cb.p1.y - P.py) * P.uy;
+                        double s1 = (cb.p2.x - P.px) * P.ux + (cb.p2.y - P.py) * P.uy;
+                        if (s0 > s1) std::swap(s0, s1);
+                        pieces.push_back(bte::PolyPiece{s0, s1, gc.id, 0});
+                    }
+                    P.npieces = int(pieces.size()) - P.piece_off;
+                }
+            }
+            if (pieces.empty()) pieces.push_back(bte::PolyPiece{0., 0., -1, 0});
+            c->d_pborders.upload(pb, c->stream);
+            c->d_ppieces.upload(pieces, c->stream);
         }
         sync(c);
         c->geom_dev = true;
@@ -697,9 +740,15 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
             if (!bte::launch_prod_grid(T, A, c->d_tally.as<double>(), counters, err,
                                        c->d_work.as<unsigned long long>(), c->tune, c->nsm, c->stream))
                 throw Error(BTE_ERR_INPUT, "tuning not supported by the grid kernel");
-        } else {
+        } else if (p->flags & BTE_FLAG_GENERAL) {
             bte::launch_prod_general(T, c->d_tally.as<double>(), counters, err,
                                      c->d_work.as<unsigned long long>(), c->nsm, c->stream);
+        } else {
+            const bte::PolyArgs A{c->d_pborders.as<bte::PolyBorder>(), c->d_ppieces.as<bte::PolyPiece>(),
+                                  c->d_mv.as<bte::ModeVel>()};
+            if (!bte::launch_prod_poly(T, A, c->d_tally.as<double>(), counters, err,
+                                       c->d_work.as<unsigned long long>(), c->nsm, c->stream))
+                throw Error(BTE_ERR_CUDA, "polygon kernel does not fit on the device");
         }
         ck(cudaGetLastError(), "kernel launch");
         ck(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");

@@ -55,6 +55,25 @@ struct GridArgs {
     int cls[4];              // normal classes of the +x, -x, +y, -y walls (-1: none)
 };
 
+// Convex-polygon production path: every border as the line n.x = c (n its
+// outward unit normal) with its start p, unit direction u, its wall class,
+// and the pieces of it that touch a neighbour box, as intervals of the
+// arc length s = (x - p).u.
+struct PolyBorder {
+    double nx, ny, c;
+    double px, py, ux, uy;
+    int piece_off, npieces, cls, pad;
+};
+struct PolyPiece {
+    double s0, s1;
+    int box, pad;
+};
+struct PolyArgs {
+    const PolyBorder* pb;     // [global border index]
+    const PolyPiece* pieces;
+    const ModeVel* mv;
+};
+
 // Adjoint passes of the grid kernel: the functional's weights per tally
 // value, each particle's total contribution (slot = particle - first),
 // per-mode gradient accumulators and {d/dp, sum of R over post-scattering
@@ -69,6 +88,11 @@ struct AdjArgs {
 // Axis-aligned grid production kernel (persistent, warp-refilled work).
 // adj_pass 1 / 2 runs the forward / adjoint pass of the adjoint with `adj`.
 // Returns false when the tuning cannot be honoured (e.g. smem too small).
+// Production kernel of geometries that are not a grid: exit times from the
+// convex box's border lines, neighbours from the border pieces.
+bool launch_prod_poly(const DevTables& T, const PolyArgs& A, double* tally, unsigned long long* counters,
+                      int* err, unsigned long long* work, int nsm, cudaStream_t s);
+
 bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
                       unsigned long long* counters, int* err, unsigned long long* work,
                       const ProdTuning& tune, int nsm, cudaStream_t s, int adj_pass = 0,

@@ -3,13 +3,15 @@
 // Draws come from counter-based Philox4x32-10 streams keyed by (seed,
 // particle); mode distributions and Lambert rows are sampled through alias
 // tables; positions, times and tallies stay FP64, with tallies reduced by FP64
-// atomics.  Two kernels:
+// atomics.  Three kernels:
 //   rta_prod_general  any convex-box geometry, the flight logic of
-//                     rta_flight.cuh (one particle per thread);
+//                     rta_flight.cuh (one evolparticle step per pass);
 //   rta_prod_grid     boxes that tile an axis-aligned grid: a persistent
 //                     kernel whose warps refill idle lanes with new particles
 //                     and that walks cells by exit times, with a per-lane
-//                     pending tally flushed when the (box, bin) key changes.
+//                     pending tally flushed when the (box, bin) key changes;
+//   rta_prod_poly     the grid kernel's loop over any convex boxes, exit
+//                     times taken against each box's border lines.
 #include "kernels.h"
 #include "rta_steady.cuh"
 
@@ -799,6 +801,273 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             if (x != 0.) atomicAdd(gtally + k, x);
         }
     }
+}
+
+// ------------------------------------------------------------ polygon path
+
+// Production loop of geometries that are not a grid: the grid kernel's
+// organisation (persistent warps refilling idle lanes, one segment per lane
+// per pass, time left in the bin, telescoping pending tally, one Philox block
+// per pass, one mode-redraw block) with the convex box's border lines in
+// place of cell lines.  A segment ends at the flight end, the bin border or
+// the first border line the flight leaves through (n.v > 0, exit time
+// (c - n.x) / n.v, compared without divisions); across that border the
+// piece holding the exit point names the neighbour: a box (the flight goes
+// on there), a reservoir (absorbed), a periodic box (translated as
+// geometry_2d::translate does, the flight goes on) or none (a void wall:
+// Lambert or specular redraw).  The reference's handling of corners and ties
+// between borders, which has measure zero, is not repeated here.
+constexpr uint32_t POLY_SEG_CAP = 1u << 20;  // segments of one free flight
+
+__global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, double* tally,
+                                                      unsigned long long* counters, int* err,
+                                                      unsigned long long* work) {
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int lane = threadIdx.x & 31;
+    const long long total = T.pend - T.pbegin;
+    const int last_bin = T.nbins - 1;
+    const unsigned long long spec_thr =
+        T.specularity >= 1.0 ? (1ull << 32)
+                             : (T.specularity > 0. ? (unsigned long long)(T.specularity * 4294967296.0) : 0ull);
+    Pending pd;
+    pd.key = -1;
+    pd.flushes = 0;
+    pd.r0 = pd.x0 = pd.y0 = 0.;
+    ProdPolicy pol;  // generation and translation draws
+    pol.g.init(0, 0);
+    pol.out = tally;
+    pol.ntally = 0;
+    Particle p;
+    p.pos = v2(0., 0.);
+    p.mode = p.box = p.mo = 0;
+    p.sign = 1;
+    p.t = 0.;
+    ModeVel mv = {0., 0., 0., 0.};
+    const double* binw = T.timegrid + T.ntime;
+    double dt = 0., rb = 0.;
+    long long pid = -1, nev = 0;
+    uint32_t npass = 0, nseg = 0;
+    int bin = 0;
+    unsigned long long signbit = 0;
+    bool active = false, done = false;
+    auto new_flight = [&](uint32_t word) -> bool {
+        const int k = p.mode;
+        mv = A.mv[k];
+        const float ef = -logf((float(word >> 9) + 0.5f) * 0x1p-23f);
+        dt = widen_pos(ef) * __ldg(T.tau + p.mo + k);
+        c.events++;
+        nseg = 0;
+        if (ob(dt) <= 0 || ++nev > T.flight_cap) {  // zero rate or runaway particle
+            record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
+            active = false;
+            done = true;
+            pd.flush(tally, signbit, rb, p.pos.x, p.pos.y);
+            return false;
+        }
+        return true;
+    };
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active && !done);
+        if (idle) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active && !done) {
+                const long long mine = (long long)base + __popc(idle & ((1u << lane) - 1u));
+                if (mine < total) {
+                    pid = T.pbegin + mine;
+                    pol.g.init(T.seed, (uint64_t)pid);
+                    const int e = generate(T, pol, pid, p);
+                    if (e) {
+                        record_error(err, e, pid);
+                        done = true;
+                    } else {
+                        active = true;
+                        nev = 0;
+                        npass = 0;
+                        bin = 0;
+                        rb = __ldg(binw);
+                        signbit = p.sign < 0 ? 0x8000000000000000ull : 0ull;
+                        pd.start(p.box * T.nbins, rb, p.pos.x, p.pos.y);
+                        new_flight(pol.g.next32());  // the first flight, from the generation stream
+                    }
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!active) continue;
+        const uint4 rr = pass_block(npass++, (uint64_t)pid, T.seed);
+        if (++nseg > POLY_SEG_CAP) {  // a flight that keeps meeting borders without advancing
+            record_error(err, E_LIMIT, pid);
+            active = false;
+            done = true;
+            continue;
+        }
+        // the first border line the flight leaves through: smallest
+        // num / den over the borders with den = n.v > 0, num = c - n.x >= 0
+        const GBox& B = T.boxes[p.box];
+        int best = -1;
+        double bnum = 0., bden = 1.;
+        for (int k = 0; k < B.nborders; ++k) {
+            const PolyBorder& L = A.pb[B.border_off + k];
+            const double den = L.nx * mv.vx + L.ny * mv.vy;
+            if (!(den > 0.)) continue;
+            double num = L.c - (L.nx * p.pos.x + L.ny * p.pos.y);
+            num = num > 0. ? num : 0.;
+            if (best < 0 || num * bden < bnum * den) {
+                best = k;
+                bnum = num;
+                bden = den;
+            }
+        }
+        const double te = best >= 0 ? bnum / bden : HUGE_VAL;
+        long long te_b = ob(te);
+        long long tb_b = ob(rb);
+        tb_b = tb_b > 0 ? tb_b : 0;
+        const long long dt_b = ob(dt);
+        const long long lim_b = te_b < tb_b ? te_b : tb_b;
+        const bool flight_end = !(dt_b > lim_b);
+        const long long seg_b = flight_end ? dt_b : lim_b;
+        const bool wall = !flight_end && te_b <= tb_b;
+        const bool bin_end = tb_b <= seg_b;
+        const double seg = obd(seg_b);
+        double r1 = rb - seg;
+        double nx = fma(seg, mv.vx, p.pos.x);
+        double ny = fma(seg, mv.vy, p.pos.y);
+        dt -= seg;
+        if (bin_end) r1 = 0.;
+        // what lies across the exit border
+        int target = -1, cls = 0;
+        if (wall) {
+            const PolyBorder& L = A.pb[B.border_off + best];
+            cls = L.cls;
+            // onto the border line
+            const double off = L.nx * nx + L.ny * ny - L.c;
+            nx -= off * L.nx;
+            ny -= off * L.ny;
+            const double sx = (nx - L.px) * L.ux + (ny - L.py) * L.uy;
+            for (int j = 0; j < L.npieces; ++j) {
+                const PolyPiece pc = A.pieces[L.piece_off + j];
+                if (sx >= pc.s0 - 1.0e-9 && sx <= pc.s1 + 1.0e-9) {
+                    target = pc.box;
+                    break;
+                }
+            }
+        }
+        if (T.spec_loc) {
+            const int loc = __ldg(T.spec_loc + p.box);
+            if (loc >= 0) {
+                const double ds = rb - r1;
+                atomicAdd(T.spec + (long long)(loc * T.nbins + bin) * T.n + p.mode, p.sign < 0 ? -ds : ds);
+            }
+        }
+        const double d0 = pd.r0 - r1, d1 = nx - pd.x0, d2 = ny - pd.y0;
+        rb = r1;
+        p.pos = v2(nx, ny);
+        const bool cross = wall && target >= 0;
+        const bool absorbed = cross && T.boxes[target].reservoir;
+        const bool periodic = cross && !absorbed && T.boxes[target].tto >= 0;
+        const bool move = cross && !absorbed;
+        const bool reflect = wall && target < 0;
+        const bool last = bin_end && bin == last_bin;
+        if (move || absorbed || bin_end) {
+            double* b = tally + 3ll * pd.key;
+            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(d0) ^ signbit));
+            atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(d1) ^ signbit));
+            atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(d2) ^ signbit));
+            pd.flushes++;
+            pd.key = -1;
+        }
+        if (absorbed || last) {
+            if (absorbed) c.absorbed++;
+            active = false;
+            continue;
+        }
+        if (bin_end) {
+            ++bin;
+            rb = __ldg(binw + bin);
+        }
+        if (move) {
+            int nb = target;
+            if (periodic) {  // translated into the target of the periodic box
+                V2 rf;
+                const int e = translate(T, pol, target, p.pos, v2(mv.vx, mv.vy), nb, rf);
+                if (e) {
+                    record_error(err, e, pid);
+                    active = false;
+                    done = true;
+                    continue;
+                }
+                p.pos = rf;
+                c.translations++;
+            }
+            p.box = nb;
+            p.mo = mat_off(T, nb);
+            c.crossings++;
+        }
+        if (move || bin_end) pd.start(p.box * T.nbins + bin, rb, p.pos.x, p.pos.y);
+        if (reflect || flight_end) {
+            const int k = p.mode;
+            int nm = k;
+            if (reflect || !T.ballistic) {
+                float pr = 0.f;
+                int keep = k, alt = k;
+                if (reflect) {
+                    int mirror_mode = -1;
+                    if (spec_thr && (unsigned long long)rr.w < spec_thr && T.mirror)
+                        mirror_mode = __ldg(T.mirror + (long long)cls * T.n + k);
+                    if (mirror_mode >= 0) {
+                        c.specular++;
+                        pr = 2.f;
+                        keep = mirror_mode;
+                    } else {
+                        const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
+                        const long long bb = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
+                        const int len = int(bb - a);
+                        if (len <= 0) {
+                            record_error(err, E_GEOM, pid);
+                            active = false;
+                            done = true;
+                            continue;
+                        }
+                        const int4 e = __ldg(T.lalias + a + int(mulhi32(rr.y, uint32_t(len))));
+                        pr = __int_as_float(e.x);
+                        keep = e.y;
+                        alt = e.z;
+                    }
+                    c.wall_hits++;
+                } else {
+                    const int j = int(mulhi32(rr.y, uint32_t(T.n)));
+                    pr = __ldg(T.resample_prob + p.mo + j);
+                    keep = j;
+                    alt = __ldg(T.resample_alt + p.mo + j);
+                }
+                const float acc = float(rr.z >> 8) * 0x1p-24f;
+                nm = acc < pr ? keep : alt;
+            }
+            p.mode = nm;
+            if (!new_flight(rr.x)) continue;
+        }
+    }
+    c.tallies = pd.flushes;
+    flush_counters_p(c, counters);
+}
+
+bool launch_prod_poly(const DevTables& T, const PolyArgs& A, double* tally, unsigned long long* counters,
+                      int* err, unsigned long long* work, int nsm, cudaStream_t s) {
+    const long long n = T.pend - T.pbegin;
+    if (n <= 0) return true;
+    int maxb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, rta_prod_poly, 256, 0);
+    if (maxb < 1) return false;
+    long long blocks = (long long)nsm * maxb;
+    const long long need = (n + 255) / 256;
+    if (blocks > need) blocks = need;
+    rta_prod_poly<<<unsigned(blocks), 256, 0, s>>>(T, A, tally, counters, err, work);
+    return true;
 }
 
 bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,

@@ -133,6 +133,11 @@ typedef struct bte_rta_params {
  * violation stops the particle with BTE_ERR_CHECK instead of an out-of-range
  * access (the same draws as the plain variant, so the same trajectories). */
 #define BTE_FLAG_CHECKS 1
+/* BTE_FLAG_GENERAL runs production boxes that do not tile a grid through the
+ * evolparticle-faithful kernel (the reference's corner and nudge handling,
+ * one evolparticle step per pass) instead of the convex-polygon kernel
+ * (exit times against the box's border lines, one segment per pass). */
+#define BTE_FLAG_GENERAL 2
 
 /* Results of one RTA run.  Every array pointer may be NULL (not written).
  * Arrays are row-major [nboxes][nbins]. */

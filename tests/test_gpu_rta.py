@@ -29,9 +29,10 @@ def _run(engine, case, **kw):
     return engine.rta_run(**args)
 
 
-def _triangle_ribbon(length=200.0, width=50.0, ncells=4, T_hot=301.0, T_cold=299.0):
+def _triangle_ribbon(length=200.0, width=50.0, ncells=4, T_hot=301.0, T_cold=299.0, closed=False):
     """Ribbon whose cells are split into two triangles (not an axis-aligned
-    grid: exercises the general convex-box kernels)."""
+    grid: exercises the general convex-box kernels).  `closed`: the end boxes
+    are ordinary boxes at T_hot and T_cold instead of reservoirs."""
     boxes, Teq, res = [], [], []
     dx = length / ncells
     for i in range(ncells):
@@ -43,8 +44,9 @@ def _triangle_ribbon(length=200.0, width=50.0, ncells=4, T_hot=301.0, T_cold=299
     boxes.append([(-20.0, 0.0), (-20.0, width), (0.0, width), (0.0, 0.0)])
     boxes.append([(length, 0.0), (length, width), (length + 20.0, width), (length + 20.0, 0.0)])
     Teq += [T_hot, T_cold]
-    res += [1, 1]
-    return synth._pack(boxes, Teq, list(Teq), res, synth.C_LAT)
+    if closed:  # initial deviation of the end boxes; Teq = T0 everywhere
+        return synth._pack(boxes, [300.0] * len(Teq), Teq, res + [0, 0], synth.C_LAT)
+    return synth._pack(boxes, Teq, list(Teq), res + [1, 1], synth.C_LAT)
 
 
 @pytest.mark.parametrize("seed", [1, 7])
@@ -144,11 +146,14 @@ def test_production_agrees_with_restatement(engine):
     assert z.max() < 4.5, (z, prod.mean(0), orc.mean(0))
 
 
-def test_production_general_kernel_agrees(engine):
+@pytest.mark.parametrize("flags", [0, btegpu.FLAG_GENERAL], ids=["polygon", "general"])
+def test_production_general_kernel_agrees(engine, flags):
+    """Boxes off a grid: the convex-polygon kernel (default) and the
+    evolparticle-faithful kernel both agree with the restatement."""
     case = synth.small_case(n_particles=4000, maxtime=300.0)
     case["geom"] = _triangle_ribbon()
     R = 6
-    prod = np.array([_observables(_run(engine, case, seed=300 + i)) for i in range(R)])
+    prod = np.array([_observables(_run(engine, case, seed=300 + i, flags=flags)) for i in range(R)])
     orc = np.array([_observables(pyoracle.rta_run(case, seed=400 + i, nthreads=8)) for i in range(R)])
     d = prod.mean(0) - orc.mean(0)
     se = np.sqrt(prod.var(0, ddof=1) / R + orc.var(0, ddof=1) / R)
@@ -172,6 +177,24 @@ def test_production_conserves_particle_time(engine):
         assert r["absorbed"] == 0
         if p > 0:
             assert r["specular_hits"] > 0
+
+
+@pytest.mark.parametrize("spec", [0.0, 0.6])
+def test_polygon_kernel_conserves_particle_time(engine, spec):
+    """Closed triangle ribbon (no reservoirs), initial deviation: every
+    particle of the polygon kernel spends each whole bin in some box, so the
+    tally of every bin is N * dt to FP64 rounding."""
+    g = _triangle_ribbon(ncells=6, T_hot=300.5, T_cold=299.5, closed=True)
+    case = {"modes": synth.mode_table(8, 3, 3, 300.0, config=100), "geom": g, "T0": 300.0,
+            "dt": 10.0, "maxtime": 200.0, "N": 20000}
+    r = _run(engine, case, seed=11, source=btegpu.SOURCE_INITIAL, specularity=spec)
+    per_bin = r["gz"].sum(axis=0)
+    n = per_bin[0] / case["dt"]
+    assert n > 0 and abs(n - round(n)) < 1e-6
+    assert np.allclose(per_bin, per_bin[0], rtol=1e-9, atol=0)
+    assert r["absorbed"] == 0 and r["crossings"] > 0 and r["wall_hits"] > 0
+    if spec > 0:
+        assert r["specular_hits"] > 0
 
 
 def test_walls_source_time_budget(engine):
