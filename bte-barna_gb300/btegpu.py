@@ -120,7 +120,8 @@ class AdjointResult(C.Structure):
 class SteadyParams(C.Structure):
     _fields_ = [("T0", C.c_double), ("gradient", C.c_double * 2), ("eps_energy", C.c_double),
                 ("eps_flux", C.c_double), ("nparticles", C.c_int64), ("seed", C.c_uint64),
-                ("mode", C.c_int32), ("max_generations", C.c_int32), ("specularity", C.c_double)]
+                ("mode", C.c_int32), ("max_generations", C.c_int32), ("specularity", C.c_double),
+                ("flags", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class SteadyResult(C.Structure):
@@ -140,8 +141,9 @@ STEADY_KEYS = ("generations", "converged", "Eeff", "energy_rate", "events", "wal
 
 
 def steady_call(fn, nboxes, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_energy=-42.0,
-                eps_flux=-42.0, max_generations=0, log_cap=100000, specularity=0.0):
-    """Fill SteadyParams / SteadyResult, call fn(params, result), return a dict."""
+                eps_flux=-42.0, max_generations=0, log_cap=100000, specularity=0.0, flags=0):
+    """Fill SteadyParams / SteadyResult, call fn(params, result), return a dict.
+    `flags`: FLAG_GENERAL for the evolparticle-faithful kernel."""
     p = SteadyParams()
     p.T0 = float(T0)
     p.gradient[0], p.gradient[1] = float(gradient[0]), float(gradient[1])
@@ -149,6 +151,7 @@ def steady_call(fn, nboxes, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_e
     p.nparticles, p.seed, p.mode = int(N), int(seed), int(mode)
     p.max_generations = int(max_generations)
     p.specularity = float(specularity)
+    p.flags = int(flags)
     out = {k: np.zeros(nboxes) for k in ("gz", "gz_jx", "gz_jy", "temperature", "jx", "jy")}
     out["exact"] = np.zeros((nboxes, 3, 2), dtype=np.int64)
     out["log"] = np.zeros((log_cap, 4))
@@ -411,12 +414,12 @@ def _engine_berta_run(self, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, canc
 
 
 def _engine_steady_run(self, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_energy=-42.0,
-                       eps_flux=-42.0, max_generations=0, log_cap=100000, specularity=0.0):
+                       eps_flux=-42.0, max_generations=0, log_cap=100000, specularity=0.0, flags=0):
     """Steady state of a periodic structure under `gradient` (K/nm)."""
     def call(p, r):
         self._check(self.lib.bte_steady_run(self.ctx, C.byref(p), C.byref(r)))
     return steady_call(call, self.nboxes, T0, gradient, N, seed, mode, eps_energy, eps_flux,
-                       max_generations, log_cap, specularity)
+                       max_generations, log_cap, specularity, flags)
 
 
 def _engine_load_materials(self, w_list, T0_list, share=None):

@@ -78,8 +78,10 @@ void ensure_static(bte_ctx* c) {
                     if (b >= 0) bc[std::size_t(b)] = make_int2(i, j);
                 }
             c->d_boxcell.upload(bc, c->stream);
-        } else {
-            // border lines and neighbour pieces of the convex-polygon path:
+        }
+        {
+            // border lines and neighbour pieces of the convex-polygon path
+            // (transient boxes off a grid, every steady-state geometry):
             // a segment contact of box a lies on the border of a whose
             // outward normal is the contact's normal; its ends give the
             // interval of arc length that leads into the neighbour

@@ -92,6 +92,8 @@ struct AdjArgs {
 // convex box's border lines, neighbours from the border pieces.
 bool launch_prod_poly(const DevTables& T, const PolyArgs& A, double* tally, unsigned long long* counters,
                       int* err, unsigned long long* work, int nsm, cudaStream_t s);
+bool launch_steady_poly(const DevTables& T, const SteadyArgs& A, const PolyArgs& PA, double* tally,
+                        unsigned long long* counters, int* err, int nsm, cudaStream_t s);
 
 bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
                       unsigned long long* counters, int* err, unsigned long long* work,

@@ -1070,6 +1070,168 @@ bool launch_prod_poly(const DevTables& T, const PolyArgs& A, double* tally, unsi
     return true;
 }
 
+// One steady-state generation on convex boxes, the polygon kernel's segment
+// walk: each slot's one flight runs box to box by exit times against the
+// border lines (one box visit per pass, tallied at its end as the reference's
+// periodic process_segment does) until it scatters inside a box (phi +=
+// sign), reaches a void wall (redrawn and carried over), enters a reservoir
+// (absorbed) or a periodic box (translated, the flight goes on).
+__global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A, PolyArgs PA, double* tally,
+                                                       unsigned long long* counters, int* err) {
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int lane = threadIdx.x & 31;
+    ProdPolicy pol;
+    pol.g.init(0, 0);
+    pol.out = tally;
+    pol.ntally = 0;
+    Particle p;
+    p.pos = v2(0., 0.);
+    p.mode = p.box = p.mo = 0;
+    p.sign = 1;
+    p.t = 0.;
+    V2 v = v2(0., 0.);
+    double dt = 0.;
+    long long slot = -1;
+    uint32_t nseg = 0;
+    bool active = false, done = false;
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, !active && !done);
+        if (idle) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader) base = atomicAdd(A.work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active && !done) {
+                slot = (long long)base + __popc(idle & ((1u << lane) - 1u));
+                if (slot < A.n) {
+                    pol.g.init(T.seed, steady_stream(A.gen, slot));
+                    const int e = steady_begin(T, A, pol, slot, c, p, v, dt);
+                    if (e) {
+                        record_error(err, e, slot);
+                        A.flag[slot] = 0;
+                    } else {
+                        active = true;
+                        nseg = 0;
+                    }
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        if (!active) continue;
+        if (++nseg > POLY_SEG_CAP) {
+            record_error(err, E_LIMIT, slot);
+            A.flag[slot] = 0;
+            active = false;
+            continue;
+        }
+        const GBox& B = T.boxes[p.box];
+        int best = -1;
+        double bnum = 0., bden = 1.;
+        for (int k = 0; k < B.nborders; ++k) {
+            const PolyBorder& L = PA.pb[B.border_off + k];
+            const double den = L.nx * v.x + L.ny * v.y;
+            if (!(den > 0.)) continue;
+            double num = L.c - (L.nx * p.pos.x + L.ny * p.pos.y);
+            num = num > 0. ? num : 0.;
+            if (best < 0 || num * bden < bnum * den) {
+                best = k;
+                bnum = num;
+                bden = den;
+            }
+        }
+        const double te = best >= 0 ? bnum / bden : HUGE_VAL;
+        const bool wall = dt > te;
+        const double seg = wall ? te : dt;
+        double nx = fma(seg, v.x, p.pos.x);
+        double ny = fma(seg, v.y, p.pos.y);
+        dt -= seg;
+        int target = -1, cls = 0;
+        if (wall) {
+            const PolyBorder& L = PA.pb[B.border_off + best];
+            cls = L.cls;
+            const double off = L.nx * nx + L.ny * ny - L.c;
+            nx -= off * L.nx;
+            ny -= off * L.ny;
+            const double sx = (nx - L.px) * L.ux + (ny - L.py) * L.uy;
+            for (int j = 0; j < L.npieces; ++j) {
+                const PolyPiece pc = PA.pieces[L.piece_off + j];
+                if (sx >= pc.s0 - 1.0e-9 && sx <= pc.s1 + 1.0e-9) {
+                    target = pc.box;
+                    break;
+                }
+            }
+        }
+        pol.tally_dt(T, p.box, seg, p.sign, v, p.mode);
+        p.pos = v2(nx, ny);
+        int fate = -1;
+        if (!wall) {  // scattering inside the box
+            fate = FATE_SCATTER;
+            c.scattered++;
+        } else if (target < 0) {  // void wall: the new mode, carried to the next generation
+            int nm = -1;
+            if (T.specularity > 0. && pol.u() < T.specularity) {
+                const int mm = T.mirror ? T.mirror[cls * T.n + p.mode] : -1;
+                if (mm >= 0) {
+                    nm = mm;
+                    c.specular++;
+                }
+            }
+            if (nm < 0) nm = pol.bounce(T, cls, p.mode);
+            if (nm < 0) {
+                record_error(err, E_GEOM, slot);
+                A.flag[slot] = 0;
+                active = false;
+                continue;
+            }
+            p.mode = nm;
+            c.wall_hits++;
+            fate = FATE_BOUNCE;
+        } else if (T.boxes[target].reservoir) {
+            c.absorbed++;
+            fate = FATE_ABSORBED;
+        } else {
+            int nb = target;
+            if (T.boxes[target].tto >= 0) {
+                V2 rf;
+                const int e = translate(T, pol, target, p.pos, v, nb, rf);
+                if (e) {
+                    record_error(err, e, slot);
+                    A.flag[slot] = 0;
+                    active = false;
+                    continue;
+                }
+                p.pos = rf;
+                c.translations++;
+            }
+            p.box = nb;
+            p.mo = mat_off(T, nb);
+            c.crossings++;
+        }
+        if (fate >= 0) {
+            steady_emit(A, slot, fate, p);
+            active = false;
+        }
+    }
+    c.tallies += pol.ntally;
+    flush_counters_p(c, counters);
+}
+
+bool launch_steady_poly(const DevTables& T, const SteadyArgs& A, const PolyArgs& PA, double* tally,
+                        unsigned long long* counters, int* err, int nsm, cudaStream_t s) {
+    if (A.n <= 0) return true;
+    int maxb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, rta_steady_poly, 128, 0);
+    if (maxb < 1) return false;
+    long long blocks = (long long)nsm * maxb;
+    const long long need = (A.n + 127) / 128;
+    if (blocks > need) blocks = need;
+    cudaMemsetAsync(A.work, 0, sizeof(unsigned long long), s);
+    rta_steady_poly<<<unsigned(blocks), 128, 0, s>>>(T, A, PA, tally, counters, err);
+    return true;
+}
+
 bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
                       unsigned long long* counters, int* err, unsigned long long* work,
                       const ProdTuning& tune, int nsm, cudaStream_t s, int adj_pass,

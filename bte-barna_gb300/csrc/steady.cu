@@ -281,6 +281,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         S.work.alloc(sizeof(unsigned long long));
         A.work = S.work.as<unsigned long long>();
 
+        const PolyArgs PA{c->d_pborders.as<PolyBorder>(), c->d_ppieces.as<PolyPiece>(), c->d_mv.as<ModeVel>()};
         const int max_gen = p->max_generations > 0 ? p->max_generations : 100000;
         std::vector<double> oldv(size_t(3) * nbx, 0.), cur(size_t(3) * nbx, 0.);
         std::vector<unsigned long long> hex, hphi(static_cast<size_t>(nbx));
@@ -307,9 +308,12 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
             if (replay)
                 launch_steady_replay(T, A, S.tally.as<unsigned long long>(), S.counters.as<unsigned long long>(),
                                      S.err.as<int>(), nullptr, c->nsm, st);
-            else
+            else if (p->flags & BTE_FLAG_GENERAL)
                 launch_steady_prod(T, A, S.tally.as<double>(), S.counters.as<unsigned long long>(),
                                    S.err.as<int>(), nullptr, c->nsm, st);
+            else if (!launch_steady_poly(T, A, PA, S.tally.as<double>(), S.counters.as<unsigned long long>(),
+                                         S.err.as<int>(), c->nsm, st))
+                throw Error(BTE_ERR_CUDA, "steady polygon kernel does not fit on the device");
             ck(cudaGetLastError(), "steady launch");
             ck(cudaEventRecord(c->ev1, st), "cudaEventRecord");
             int herr[4];

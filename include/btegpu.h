@@ -239,6 +239,9 @@ typedef struct bte_steady_params {
     int32_t mode;            /* BTE_MODE_*                                      */
     int32_t max_generations; /* safety cap of the generation loop (0: 100000)  */
     double specularity;      /* p of void walls; 0 = the reference's diffuse    */
+    int32_t flags;           /* BTE_FLAG_GENERAL: the evolparticle-faithful
+                                kernel instead of the convex-polygon one       */
+    int32_t reserved0;
 } bte_steady_params;
 
 /* Results of a steady-state run: one value per box (the rows of

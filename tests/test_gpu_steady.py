@@ -46,7 +46,10 @@ def test_steady_replay_bit_exact(engine, which, grad):
     assert np.array_equal(g["jx"], o["jx"]) and np.array_equal(g["jy"], o["jy"])
 
 
-def test_steady_production_agrees_with_restatement(engine):
+@pytest.mark.parametrize("flags", [0, btegpu.FLAG_GENERAL], ids=["polygon", "general"])
+def test_steady_production_agrees_with_restatement(engine, flags):
+    """The convex-polygon kernel (default) and the evolparticle-faithful
+    kernel both agree with the restatement."""
     case = synth.periodic_case(n_particles=4000)
     _load(engine, case)
     R = 6
@@ -54,7 +57,7 @@ def test_steady_production_agrees_with_restatement(engine):
     def obs(r):
         return np.concatenate([r["temperature"][:10], [r["jy"][:10].mean() * 1e-8]])
 
-    prod = np.array([obs(engine.steady_run(300.0, (0.0, -0.01), case["N"], seed=40 + i))
+    prod = np.array([obs(engine.steady_run(300.0, (0.0, -0.01), case["N"], seed=40 + i, flags=flags))
                      for i in range(R)])
     orc = np.array([obs(pyoracle.steady_run(case, (0.0, -0.01), seed=60 + i)) for i in range(R)])
     d = prod.mean(0) - orc.mean(0)
@@ -63,11 +66,12 @@ def test_steady_production_agrees_with_restatement(engine):
     assert z.max() < 4.5, (z, prod.mean(0), orc.mean(0))
 
 
-def test_steady_production_bulk_kappa(engine):
+@pytest.mark.parametrize("flags", [0, btegpu.FLAG_GENERAL], ids=["polygon", "general"])
+def test_steady_production_bulk_kappa(engine, flags):
     case = _cell_case(200000, even=True)
     _load(engine, case)
     K = synth.kappa_rta(case["modes"], 300.0)[0, 0]
-    ks = np.array([-engine.steady_run(300.0, (-0.01, 0.0), case["N"], seed=90 + i)["jx"][:4].mean()
+    ks = np.array([-engine.steady_run(300.0, (-0.01, 0.0), case["N"], seed=90 + i, flags=flags)["jx"][:4].mean()
                    / (-0.01e9) for i in range(6)])
     se = ks.std(ddof=1) / np.sqrt(len(ks))
     assert abs(ks.mean() - K) < 4.5 * se, (ks.mean(), se, K)
