@@ -232,7 +232,15 @@ __device__ int correct_corner_problem(const DevTables& T, P& pol, V2 rf, V2 v, c
 // contact's crossing point; with several candidates the point is taken from
 // the candidate list at the position drawn among the filtered candidates.
 // Returns 0 or an error code.
-template <class P>
+// FAST (production kernels): contacts that cannot take part are skipped
+// before the segment and hull tests -- the excluded kinds first, then those
+// whose contact segment's bounding box is apart from both the jump segment
+// (no meet is possible) and the entry point tp (tp, tp + 1e-6 v and
+// tp - 1e-6 T lie on this machine's border, so they can be inside the
+// neighbour only next to the contact between the two).  A skipped contact
+// is one the full tests reject too, so the candidates, their order and the
+// draws are unchanged.
+template <class P, bool FAST = false>
 __device__ int translate(const DevTables& T, P& pol, int box, V2 r0, V2 v, int& nbox, V2& rf) {
     const int tib = T.boxes[box].tto;
     const V2 tv = T.translation[box];
@@ -257,6 +265,17 @@ __device__ int translate(const DevTables& T, P& pol, int box, V2 r0, V2 v, int& 
     for (int i = 0; i < TB.ncontacts; ++i) {
         const int ci = TB.contact_off + i;
         const int ibc = T.contacts[ci].id;
+        if (FAST) {
+            if (ibc == tib || T.boxes[ibc].tto >= 0 || T.boxes[ibc].reservoir) continue;
+            const V2 a = T.cseg[2 * ci], b = T.cseg[2 * ci + 1];
+            const double lox = fmin(a.x, b.x), hix = fmax(a.x, b.x);
+            const double loy = fmin(a.y, b.y), hiy = fmax(a.y, b.y);
+            const double mp = 1.0e-3, ms = 1.0e-9;  // nm
+            const bool near_tp = tp.x >= lox - mp && tp.x <= hix + mp && tp.y >= loy - mp && tp.y <= hiy + mp;
+            const bool near_seg = fmax(r0.x, p1.x) >= lox - ms && fmin(r0.x, p1.x) <= hix + ms &&
+                                  fmax(r0.y, p1.y) >= loy - ms && fmin(r0.y, p1.y) <= hiy + ms;
+            if (!near_tp && !near_seg) continue;
+        }
         V2 xin;
         const bool here_i = seg_meet(r0, p1, T.cseg[2 * ci], T.cseg[2 * ci + 1], xin);
         const bool here_T = box_inside(T, ibc, tp);

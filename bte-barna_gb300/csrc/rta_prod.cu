@@ -923,7 +923,36 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
                 bden = den;
             }
         }
-        const double te = best >= 0 ? bnum / bden : HUGE_VAL;
+        double te = best >= 0 ? bnum / bden : HUGE_VAL;
+        // time bins that end before the flight end and the exit border are
+        // closed here, without a pass each: advance to the bin end, flush
+        // the pending tally, open the next bin (two FMAs per bin instead of
+        // a new exit-time search).  The last bin is left to the pass below.
+        {
+            long long lim0 = ob(te) < ob(dt) ? ob(te) : ob(dt);
+            while (ob(rb) < lim0 && bin < last_bin) {
+                const double adv = ob(rb) > 0 ? rb : 0.;
+                const double xb = fma(adv, mv.vx, p.pos.x);
+                const double yb = fma(adv, mv.vy, p.pos.y);
+                if (T.spec_loc) {
+                    const int loc = __ldg(T.spec_loc + p.box);
+                    if (loc >= 0)
+                        atomicAdd(T.spec + (long long)(loc * T.nbins + bin) * T.n + p.mode, p.sign < 0 ? -adv : adv);
+                }
+                double* b = tally + 3ll * pd.key;
+                atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(pd.r0) ^ signbit));
+                atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(xb - pd.x0) ^ signbit));
+                atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(yb - pd.y0) ^ signbit));
+                pd.flushes++;
+                dt -= adv;
+                te -= adv;
+                p.pos = v2(xb, yb);
+                ++bin;
+                rb = __ldg(binw + bin);
+                pd.start(p.box * T.nbins + bin, rb, xb, yb);
+                lim0 = ob(te) < ob(dt) ? ob(te) : ob(dt);
+            }
+        }
         long long te_b = ob(te);
         long long tb_b = ob(rb);
         tb_b = tb_b > 0 ? tb_b : 0;
@@ -994,7 +1023,7 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
             int nb = target;
             if (periodic) {  // translated into the target of the periodic box
                 V2 rf;
-                const int e = translate(T, pol, target, p.pos, v2(mv.vx, mv.vy), nb, rf);
+                const int e = translate<ProdPolicy, true>(T, pol, target, p.pos, v2(mv.vx, mv.vy), nb, rf);
                 if (e) {
                     record_error(err, e, pid);
                     active = false;
@@ -1195,7 +1224,7 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
             int nb = target;
             if (T.boxes[target].tto >= 0) {
                 V2 rf;
-                const int e = translate(T, pol, target, p.pos, v, nb, rf);
+                const int e = translate<ProdPolicy, true>(T, pol, target, p.pos, v, nb, rf);
                 if (e) {
                     record_error(err, e, slot);
                     A.flag[slot] = 0;
