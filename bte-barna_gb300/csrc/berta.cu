@@ -244,7 +244,7 @@ __device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& 
         if (T.boxes[box].tto >= 0) {
             int nb;
             V2 rf;
-            if (translate(T, pol, box, pos, v, nb, rf)) {
+            if (translate<BePol, true>(T, pol, box, pos, v, nb, rf)) {
                 err = E_GEOM;
                 return false;
             }
