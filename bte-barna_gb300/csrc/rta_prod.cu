@@ -816,9 +816,9 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
 // on there), a reservoir (absorbed), a periodic box (translated as
 // geometry_2d::translate does, the flight goes on) or none (a void wall:
 // Lambert or specular redraw).  The reference's handling of corners and ties
-// between borders, which has measure zero, is not repeated here.
-constexpr uint32_t POLY_SEG_CAP = 1u << 20;  // segments of one free flight
-
+// between borders, which has measure zero, is not repeated here.  A flight
+// that runs more than POLY_SEG_CAP segments stops the run with E_LIMIT.
+constexpr uint32_t POLY_SEG_CAP = 1u << 20;
 __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, double* tally,
                                                       unsigned long long* counters, int* err,
                                                       unsigned long long* work) {
