@@ -764,6 +764,11 @@ def main():
                                         "kind": "port",
                                         "sample": f"{cn} particles of the same workload "
                                                   f"({cev} events, {cdt:.1f} s)"}
+                # the same restatement on one host core, on its own bounded sample
+                oev, odt, on = cpu_sample(c, max(2.0, args.cpu_seconds / 3), 1, offset=cn)
+                line["cpu_baseline"]["one_core"] = {
+                    "value": oev / odt, "unit": UNIT, "cores": 1,
+                    "sample": f"{on} particles of the same workload ({oev} events, {odt:.1f} s)"}
             except Exception as e:  # the baseline must not hide the GPU line
                 line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(),
                                         "kind": "port", "sample": f"failed: {e}"}

@@ -2,10 +2,11 @@
 // no device allocation during the call.
 //
 // Who needs it: callers that cannot call cudaMalloc when they run the loop --
-// code inside a stream capture, a host framework that owns every device
-// allocation through its own pool, or a real-time loop that must not hit
-// the driver's allocator.  They hand in a device buffer for the tallies and
-// get the counters back in host memory.
+// a host framework that owns every device allocation through its own pool
+// and forbids others, or a loop that must not reach the driver's allocator
+// (whose calls can synchronise the device and take unbounded time).  They
+// hand in a device buffer for the tallies and get the counters back in host
+// memory.  The call synchronises the context's stream before it returns.
 //
 // The kernel's scratch (work counter, event counters, error word and the
 // time grid) lives in one file-scope device array of fixed size instead of
@@ -20,7 +21,10 @@
 //     depend on an earlier call, but calls that overlap on the GPU (on
 //     several streams or threads at once) race and must be serialised;
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress; make that first call before any stream capture.
+//     cudaGetSymbolAddress (set-up, once per device); make that first call
+//     before any stream capture.  The address is kept for the life of the
+//     process and never looked up again, so a process that calls
+//     cudaDeviceReset must not use this entry point on that device after it.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -51,7 +55,7 @@ std::mutex g_setup_mutex;
 unsigned char* g_scratch_addr[kMaxDevices] = {nullptr};
 
 // Device address of the scratch on `device` (which must be current); looked
-// up once per device.
+// up once per device, on the first call there, and kept.
 bool scratch_address(int device, unsigned char** out, std::string* why) {
     if (device < 0 || device >= kMaxDevices) {
         *why = "device ordinal beyond the allocation-free path's table";
@@ -118,20 +122,25 @@ extern "C" bte_status bte_rta_run_noalloc(bte_ctx* ctx, const bte_rta_params* pa
         cudaMemsetAsync(d_tally, 0, tally_bytes, s) != cudaSuccess)
         return fail(ctx, BTE_ERR_CUDA, "cudaMemsetAsync failed (is d_tally a device pointer?)");
     noalloc_time_grid<<<(r.ntime + 255) / 256, 256, 0, s>>>(grid, r.ntime, r.maxtime, r.step);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, BTE_ERR_CUDA, std::string("time grid launch: ") + cudaGetErrorString(e));
     r.T.timegrid = grid;
-    cudaEventRecord(r.ev0, s);
+    if (cudaEventRecord(r.ev0, s) != cudaSuccess) return fail(ctx, BTE_ERR_CUDA, "cudaEventRecord failed");
     if (!bte::launch_prod_grid(r.T, r.A, d_tally, counters, err, work, r.tune, r.nsm, s))
         return fail(ctx, BTE_ERR_INPUT, "tuning not supported by the grid kernel");
-    cudaEventRecord(r.ev1, s);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, BTE_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    if (cudaEventRecord(r.ev1, s) != cudaSuccess) return fail(ctx, BTE_ERR_CUDA, "cudaEventRecord failed");
     unsigned long long hc[8];
     int herr[4];
     if (cudaMemcpyAsync(hc, counters, sizeof hc, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return fail(ctx, BTE_ERR_CUDA, "cudaMemcpyAsync failed");
-    const cudaError_t e = cudaStreamSynchronize(s);
+    e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(ctx, BTE_ERR_CUDA, std::string("kernel: ") + cudaGetErrorString(e));
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, r.ev0, r.ev1);
+    e = cudaEventElapsedTime(&ms, r.ev0, r.ev1);
+    if (e != cudaSuccess) return fail(ctx, BTE_ERR_CUDA, std::string("cudaEventElapsedTime: ") + cudaGetErrorString(e));
     if (herr[0] != 0) {
         const long long pid = (long long)herr[1] | ((long long)herr[2] << 31);
         char m[160];

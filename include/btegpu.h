@@ -431,20 +431,24 @@ bte_status bte_get_spectral(bte_ctx* ctx, bte_spectral_result* out);
 
 /* The production RTA particle loop with no device allocation during the
  * call.  No counterpart in the reference: it serves callers that cannot call
- * cudaMalloc at run time (inside a stream capture, under a framework that
- * owns all device memory through its own pool, in a loop that must not
- * reach the driver's allocator).  The caller passes the run parameters and a
- * device buffer d_tally of nboxes * nbins * 3 doubles, written as
- * [box][bin][gz, gz_jx, gz_jy] (the raw tallies of bte_rta_run); counters,
- * Eeff and kernel_ms come back in `out` (its array pointers are ignored).
- * The kernel's scratch is one fixed device array of the library (at most
- * BTE_NOALLOC_MAX_BINS time bins), shared by every call: calls that overlap
- * on the GPU race and must be serialised.  The context must already hold
- * the tables for these parameters (one bte_rta_run with the same T0 and
- * source, and for the initial source the same N and seed); the boxes must
- * tile an axis-aligned grid and mode must be BTE_MODE_PRODUCTION.  The first
- * call on a device looks up the scratch address; make it before any stream
- * capture. */
+ * cudaMalloc at run time -- a framework that owns all device memory through
+ * its own pool and forbids other allocations, or a loop that must not reach
+ * the driver's allocator, whose calls can synchronise the device and take
+ * unbounded time.  The caller passes the run parameters and a device buffer
+ * d_tally of nboxes * nbins * 3 doubles, written as [box][bin][gz, gz_jx,
+ * gz_jy] (the raw tallies of bte_rta_run); counters, Eeff and kernel_ms come
+ * back in `out` (its array pointers are ignored).  The call synchronises the
+ * context's stream before it returns.  The kernel's scratch is one fixed
+ * device array of the library (at most BTE_NOALLOC_MAX_BINS time bins),
+ * shared by every call and held by every GPU that loads the library until
+ * the process exits: calls that overlap on the GPU race and must be
+ * serialised.  The context must already hold the tables for these
+ * parameters (one bte_rta_run with the same T0 and source, and for the
+ * initial source the same N and seed); the boxes must tile an axis-aligned
+ * grid and mode must be BTE_MODE_PRODUCTION.  The first call on a device
+ * does the set-up: it looks up the scratch address once (kept until the
+ * process exits, so not after a cudaDeviceReset); make that first call
+ * before any stream capture. */
 bte_status bte_rta_run_noalloc(bte_ctx* ctx, const bte_rta_params* params,
                                double* d_tally, bte_rta_result* out);
 

@@ -6,7 +6,10 @@ it, and writes tests/golden/ref_kat.json.  Only this script reads the
 reference tree, and only where it exists (the build container); the fixture
 it writes is committed so that tests elsewhere need no reference.
 
-Usage: python oracle/build_ref.py [--reference /root/reference] [--no-write]
+The reference tree is taken from --reference, else from the environment
+variable BTE_REFERENCE_TREE, else from the build container's mount point.
+
+Usage: python oracle/build_ref.py [--reference DIR] [--no-write]
 """
 import argparse
 import json
@@ -16,6 +19,15 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
+
+
+_MOUNT = "/root/reference"  # where the build container mounts the reference
+
+
+def reference_tree():
+    """The reference tree to build from, or None where it does not exist."""
+    path = os.environ.get("BTE_REFERENCE_TREE", _MOUNT)
+    return path if os.path.isdir(path) else None
 
 
 def build(reference: str) -> str:
@@ -34,10 +46,12 @@ def build(reference: str) -> str:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None)
     ap.add_argument("--no-write", action="store_true")
     args = ap.parse_args()
-    if not os.path.isdir(args.reference):
+    if args.reference is None:
+        args.reference = reference_tree()
+    if not args.reference or not os.path.isdir(args.reference):
         print(f"reference tree {args.reference} absent; nothing to build")
         return 0
     exe = build(args.reference)

@@ -1,13 +1,16 @@
 """bte_rta_run_noalloc, the allocation-free entry point, against bte_rta_run.
 
-Callers that cannot allocate device memory at run time (inside a stream
-capture, or under a framework that owns every allocation) pass their own
-device buffer for the tallies; the entry point keeps its scratch in a fixed
-device array of the library.  Both entry points carry the same particles
-with the same counter-based streams, so their tallies agree to FP64 atomic
-ordering (1e-12 of the largest tally, the tolerance of the other GPU tests)
-and their event counters agree exactly.  Two calls in a row check that the
-shared scratch starts clean on every call.
+Callers that cannot allocate device memory at run time (a framework that
+owns every device allocation through its own pool, or a loop that must not
+reach the driver's allocator) pass their own device buffer for the tallies;
+the entry point keeps its scratch in a fixed device array of the library.
+Both entry points carry the same particles with the same counter-based
+streams, so their tallies agree to FP64 atomic ordering (1e-12 of the
+largest tally, the tolerance of the other GPU tests) and their event
+counters agree exactly.  Two calls in a row check that the
+shared scratch starts clean on every call; the device's free memory must not
+change across the second call, and the context's own entry point must give
+its result unchanged after the allocation-free calls.
 """
 import ctypes as C
 
@@ -54,17 +57,29 @@ def test_noalloc_matches_bte_rta_run(built, which):
         params = btegpu.params_struct(case["T0"], case["dt"], case["maxtime"], case["N"], 21,
                                       btegpu.MODE_PRODUCTION, src, False, p)
         dev = torch.empty((nboxes, nbins, 3), dtype=torch.float64, device="cuda:0")
-        for _ in range(2):
+        for call in range(2):
             dev.fill_(123.0)  # stale contents must not leak into the result
+            torch.cuda.synchronize()
+            free_before = torch.cuda.mem_get_info(0)[0]
             r = btegpu.RtaResult()
             st = eng.lib.bte_rta_run_noalloc(eng.ctx, C.byref(params), C.c_void_p(dev.data_ptr()),
                                              C.byref(r))
             assert st == btegpu.BTE_OK, st
             torch.cuda.synchronize()
+            free_after = torch.cuda.mem_get_info(0)[0]
+            if call == 1:  # the first call may load the module; the second allocates nothing
+                assert free_after == free_before, (free_before, free_after)
             got = dev.cpu().numpy()
             _check_against(ref, got, r.events)
             assert (r.nboxes, r.nbins) == (nboxes, nbins)
             assert r.Eeff == ref["Eeff"]
+        # the context's own tables and buffers are untouched by the calls above
+        again = eng.rta_run(case["T0"], case["dt"], case["maxtime"], case["N"], seed=21,
+                            mode=btegpu.MODE_PRODUCTION, source=src, specularity=p)
+        assert again["events"] == ref["events"]
+        for key in ("gz", "gz_jx", "gz_jy"):
+            scale = np.abs(ref[key]).max()
+            assert np.abs(again[key] - ref[key]).max() <= REL_TOL * scale, key
     finally:
         eng.close()
 
