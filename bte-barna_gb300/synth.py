@@ -531,19 +531,27 @@ def propagator(modes: dict, dt: float = 1.0, T: float = 300.0, nnz_row: int = 64
     A -= S
     A[np.diag_indices(n)] += (S @ c) / c
     A = 0.5 * (A + A.T)
+    E = exp_neg_psd(A, dt, use_torch)
+    P = (c[:, None] * E) / c[None, :]
+    return np.asfortranarray(P)
+
+
+def exp_neg_psd(A: np.ndarray, dt: float, use_torch: bool = False) -> np.ndarray:
+    """exp(-A dt) of a symmetric A through its eigenvectors, with negative
+    eigenvalues clipped to 0 (A made positive semi-definite): V e^{-lambda dt}
+    V^T.  The propagator builder of the reference (build_P,
+    src/collision_operator.cpp:1015-1064) computes the same exponential by
+    Arnoldi iterations and a dense exponential of the Krylov matrix."""
     if use_torch:
         import torch
         dev = "cuda" if torch.cuda.is_available() else "cpu"
         lam, V = torch.linalg.eigh(torch.from_numpy(A).to(dev))
         lam = torch.clamp(lam, min=0.0)
         E = (V * torch.exp(-lam * dt)) @ V.T
-        E = E.cpu().numpy()
-    else:
-        lam, V = np.linalg.eigh(A)
-        lam = np.clip(lam, 0.0, None)
-        E = (V * np.exp(-lam * dt)) @ V.T
-    P = (c[:, None] * E) / c[None, :]
-    return np.asfortranarray(P)
+        return E.cpu().numpy()
+    lam, V = np.linalg.eigh(A)
+    lam = np.clip(lam, 0.0, None)
+    return (V * np.exp(-lam * dt)) @ V.T
 
 
 def write_propagator(path: str, P: np.ndarray) -> None:

@@ -84,6 +84,30 @@ def load():
     lib.oracle_berta_run.restype = C.c_int
     lib.oracle_timegrid.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int]
     lib.oracle_timegrid.restype = C.c_int
+    # hooks compared with the reference's own code (tests/golden/ref_pins.json)
+    dp, lp, ip = C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_int)
+    mtp = C.POINTER(_bt.ModeTable)
+    lib.oracle_uniform_int_seq.argtypes = [C.c_uint64, C.c_uint64, ip, C.c_int, ip]
+    lib.oracle_kat_almost_equal.argtypes = [C.c_double, C.c_double]
+    lib.oracle_kat_almost_equal.restype = C.c_int
+    lib.oracle_kat_bin_index.argtypes = [dp, C.c_int, C.c_double]
+    lib.oracle_kat_bin_index.restype = C.c_longlong
+    lib.oracle_kat_segment3.argtypes = [dp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
+                                        dp, dp, dp]
+    lib.oracle_kat_steady_terms.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, dp]
+    lib.oracle_kat_get_v.argtypes = [mtp, dp, dp]
+    lib.oracle_kat_random_dt.argtypes = [C.c_uint64, C.c_uint64, dp, C.c_int, C.c_int, C.c_int, dp]
+    lib.oracle_kat_random_dt.restype = C.c_int
+    lib.oracle_kat_distribution.argtypes = [mtp, C.c_int, dp, dp, ip, dp]
+    lib.oracle_kat_distribution.restype = C.c_int
+    lib.oracle_kat_ntogen.argtypes = [C.c_int, dp, C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_uint64, lp]
+    lib.oracle_kat_be_samples.argtypes = [mtp, C.c_double, C.c_uint64, C.c_uint64, C.c_int, lp]
+    lib.oracle_kat_lambert.argtypes = [mtp, lp, lp, dp, C.c_longlong]
+    lib.oracle_kat_lambert.restype = C.c_longlong
+    lib.oracle_kat_bounce.argtypes = [mtp, C.c_double, C.c_double, C.c_int, C.c_uint64, C.c_uint64, C.c_int, lp]
+    lib.oracle_kat_bounce.restype = C.c_int
+    lib.oracle_kat_prop_cumm.argtypes = [dp, C.c_int, C.c_int, dp]
+    lib.oracle_kat_lirp.argtypes = [dp, dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp]
     _lib = lib
     return lib
 

@@ -506,6 +506,14 @@ inline std::size_t lower_bound_idx(const std::vector<double>& c, double u) {
     return std::size_t(std::lower_bound(c.begin(), c.end(), u) - c.begin());
 }
 
+// random_dt, include/sampling.hpp:40-46: -log(u) / w from one uniform, with
+// bte_log (log_impl 0) or glibc's log (log_impl 1).
+inline double random_dt(double w, Pcg64& rng, int log_impl) {
+    if (w == 0.) throw value_error("invalid scattering rate");
+    double u = canonical(rng);
+    return -(log_impl == 0 ? bte_log(u) : std::log(u)) / w;
+}
+
 struct Modes {
     int nq = 0, nb = 0, grid[3] = {0, 0, 0};
     std::vector<double> omega, vx, vy, vz, w;
@@ -513,6 +521,74 @@ struct Modes {
     double V = 0, c = 0;
     std::size_t n() const { return std::size_t(nq) * nb; }
 };
+
+// BE_derivative_distribution, src/sampling.cpp:47-68: pmf C(omega, T) w,
+// zero for omega <= 0.
+inline std::vector<double> be_derivative_pmf(const Modes& m, const std::vector<double>& w, double T) {
+    std::vector<double> pmf(m.n());
+    for (std::size_t k = 0; k < m.n(); ++k)
+        pmf[k] = m.omega[k] <= 0. ? 0. : bose_einstein_kernel(m.omega[k], T) * w[k];
+    return pmf;
+}
+
+// outTref_distribution, src/sampling.cpp:271-330: pmf omega |n(Tinit) -
+// n(Tref)|, zero where omega is almost 0; returns cumulsum.
+inline double out_tref_pmf(const Modes& m, double Tinit, double Tref, std::vector<double>& pmf) {
+    pmf.assign(m.n(), 0.);
+    for (std::size_t k = 0; k < m.n(); ++k) {
+        const double om = m.omega[k];
+        if (almost_equal(om, 0.)) continue;
+        pmf[k] = om * std::fabs(bose_einstein(om, Tinit) - bose_einstein(om, Tref));
+    }
+    return 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+}
+
+// Nabla_T_distribution, src/sampling.cpp:118-164 (theta = 0): pmf
+// |v.gradT C(omega, T)| with the sign of -v.gradT; returns cumulsum.
+inline double nabla_t_pmf(const Modes& m, double gx, double gy, double T, std::vector<double>& pmf,
+                          std::vector<int>& sign) {
+    pmf.assign(m.n(), 0.);
+    sign.assign(m.n(), 1);
+    for (std::size_t k = 0; k < m.n(); ++k) {
+        double vgradT = -(gx * m.vx[k] + gy * m.vy[k] + 0. * m.vz[k]);
+        if (m.omega[k] == 0.) {
+            pmf[k] = 0.;
+        } else {
+            pmf[k] = std::fabs(vgradT * bose_einstein_kernel(m.omega[k], T));
+            sign[k] = vgradT >= 0 ? 1 : -1;
+        }
+    }
+    return kB * std::accumulate(pmf.begin(), pmf.end(), 0.);
+}
+
+// The particle numbers of the distributions' Ntogenerate before stochastic
+// rounding: time spf cumulsum / (Eff nq) for walls (src/sampling.cpp:243),
+// time vol cumulsum / (Eff nq) for Nabla_T (:166), vol cumulsum / (Eff nq)
+// for outTref (:310); get_energy is vol cumulsum / nq (:185, :328) and
+// get_flux sign cumulsum / (nq vuc) (:263-269).
+inline double gen_scaled(double time, double f, double cumulsum, double Eff, double nq) {
+    return time * f * cumulsum / (Eff * nq);
+}
+inline double gen_plain(double vol, double cumulsum, double Eff, double nq) {
+    return vol * cumulsum / (Eff * nq);
+}
+inline double dist_energy(double vol, double cumulsum, double nq) { return vol * cumulsum / nq; }
+inline double wall_flux(int sign, double cumulsum, double nq, double vuc) { return sign * (cumulsum / (nq * vuc)); }
+
+// Isothermal_wall_distribution, src/sampling.cpp:189-269 (theta = 0), for
+// the outward normal n of the wall seen from the emitting side; returns
+// cumulsum.
+inline double wall_pmf(const Modes& m, V2 n, double Tw, double Te, std::vector<double>& pmf) {
+    pmf.assign(m.n(), 0.);
+    for (std::size_t k = 0; k < m.n(); ++k) {
+        const double vn = n.x * m.vx[k] + n.y * m.vy[k] + 0. * m.vz[k];
+        if (vn <= 0. || almost_equal(0., m.omega[k]))
+            pmf[k] = 0.;
+        else
+            pmf[k] = vn * m.omega[k] * std::fabs(bose_einstein(m.omega[k], Tw) - bose_einstein(m.omega[k], Te));
+    }
+    return 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+}
 
 struct WallGen {
     std::size_t res, box;     // reservoir id, injection box id
@@ -665,19 +741,11 @@ inline void build_generators(Sim& S, double /*T0*/, bool required = true) {
             g.box = c;
             g.b = b;
             const double Tw = s.Teq, Te = S.sys[c].Teq;
-            std::vector<double> pmf(m.n());
-            for (std::size_t k = 0; k < m.n(); ++k) {
-                double vn = b.np.x * m.vx[k] + b.np.y * m.vy[k] + 0. * m.vz[k];
-                if (vn <= 0. || almost_equal(0., m.omega[k]))
-                    pmf[k] = 0.;
-                else
-                    pmf[k] = vn * m.omega[k] *
-                             std::fabs(bose_einstein(m.omega[k], Tw) - bose_einstein(m.omega[k], Te));
-            }
-            double cumulsum = 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+            std::vector<double> pmf;
+            double cumulsum = wall_pmf(m, b.np, Tw, Te, pmf);
             g.sign = (Tw - Te) >= 0 ? 1 : -1;
             g.cdf = fill_cumulative(pmf);
-            g.flux = g.sign * (cumulsum / (double(m.nq) * vuc));
+            g.flux = wall_flux(g.sign, cumulsum, double(m.nq), vuc);
             g.cumulsum = cumulsum;
             S.gens.push_back(std::move(g));
         }
@@ -1101,23 +1169,17 @@ inline Particle generate_initial(const Sim& S, std::size_t pid, Pcg64& rng) {
 inline void build_initial(Sim& S, int64_t nparticles, uint64_t seed) {
     const Modes& m = S.m;
     const double vuc = m.V * S.thickness / m.c;
-    std::vector<double> pmf(m.n()), energy;
+    std::vector<double> pmf, energy;
     for (auto& s : S.sys) {
         if (s.reservoir || s.periodic) continue;
         if (almost_equal(s.Teq, s.Treal)) continue;
         if (s.Treal <= 0 || s.Teq <= 0) throw value_error("Invalid temperature value");
-        for (std::size_t k = 0; k < m.n(); ++k) {
-            const double om = m.omega[k];
-            pmf[k] = almost_equal(om, 0.)
-                         ? 0.
-                         : om * std::fabs(bose_einstein(om, s.Treal) - bose_einstein(om, s.Teq));
-        }
-        const double cumulsum = 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+        const double cumulsum = out_tref_pmf(m, s.Treal, s.Teq, pmf);
         const double vol = s.area * S.thickness / vuc;
         S.init_box.push_back(s.id);
         S.init_sign.push_back((s.Treal - s.Teq) >= 0 ? 1 : -1);
         S.init_cdf.push_back(fill_cumulative(pmf));
-        energy.push_back(vol * cumulsum / double(m.nq));
+        energy.push_back(dist_energy(vol, cumulsum, double(m.nq)));
     }
     if (S.init_box.empty()) throw input_error("no box with Tinit different from Teq");
     double total = 0;
@@ -1148,10 +1210,7 @@ inline void run_particle(const Sim& S, std::size_t pid, uint64_t seed, double ma
         if (++nev > (1ll << 26)) throw limit_error("free flights per particle cap");
         std::size_t k = p.q * nb + p.alpha;
         V2 v = get_v(S.m, k);
-        double w = S.w_of(p.mat)[k];
-        if (w == 0.) throw value_error("invalid scattering rate");
-        double u = canonical(rng);
-        double dt_ = -(o.log_impl == 0 ? bte_log(u) : std::log(u)) / w;
+        double dt_ = random_dt(S.w_of(p.mat)[k], rng, o.log_impl);
         T.events++;
         if (time + dt_ > maxtime) dt_ = maxtime - time + 1.0e-8;
         int guard = 0;
@@ -1183,7 +1242,9 @@ struct GradGen {
     std::size_t box;
     std::vector<double> cdf;
     std::vector<int> sign;
-    double energy;
+    double energy;    // get_energy(vol) = vol cumulsum / nq
+    double vol;       // box volume in unit cells
+    double cumulsum;
 };
 
 inline std::vector<GradGen> build_gradient(const Sim& S, double gx, double gy) {
@@ -1194,20 +1255,12 @@ inline std::vector<GradGen> build_gradient(const Sim& S, double gx, double gy) {
         if (s.reservoir || s.periodic) continue;
         GradGen G;
         G.box = s.id;
-        std::vector<double> pmf(m.n());
-        G.sign.assign(m.n(), 1);
-        for (std::size_t k = 0; k < m.n(); ++k) {
-            double vgradT = -(gx * m.vx[k] + gy * m.vy[k] + 0. * m.vz[k]);
-            if (m.omega[k] == 0.) {
-                pmf[k] = 0.;
-            } else {
-                pmf[k] = std::fabs(vgradT * bose_einstein_kernel(m.omega[k], s.Teq));
-                G.sign[k] = vgradT >= 0 ? 1 : -1;
-            }
-        }
-        double cumulsum = kB * std::accumulate(pmf.begin(), pmf.end(), 0.);
+        std::vector<double> pmf;
+        double cumulsum = nabla_t_pmf(m, gx, gy, s.Teq, pmf, G.sign);
         double vol = s.area * S.thickness / vuc;
-        G.energy = vol * cumulsum / double(m.nq);
+        G.energy = dist_energy(vol, cumulsum, double(m.nq));
+        G.vol = vol;
+        G.cumulsum = cumulsum;
         G.cdf = fill_cumulative(pmf);
         out.push_back(std::move(G));
     }
@@ -1221,12 +1274,23 @@ struct SteadyGen {
 };
 
 // process_segment (periodic), src/RTA_MC2D.cpp:784-834.
+// The three contributions of one periodic segment (gz, gz_jx, gz_jy),
+// src/RTA_MC2D.cpp:798-801.
+inline void steady_terms(int sign, double dt, V2 vg, double out[3]) {
+    double contr = double(sign);
+    out[0] = contr * dt;
+    out[1] = vg.x * contr * dt;
+    out[2] = vg.y * contr * dt;
+}
+
 inline void process_segment_steady(Tally& T, std::size_t ibox, int sign, double dt, V2 vg,
                                    std::size_t mode) {
     double contr = double(sign);
-    T.ex[3 * ibox + 0] += quant(contr * dt);
-    T.ex[3 * ibox + 1] += quant(vg.x * contr * dt);
-    T.ex[3 * ibox + 2] += quant(vg.y * contr * dt);
+    double c[3];
+    steady_terms(sign, dt, vg, c);
+    T.ex[3 * ibox + 0] += quant(c[0]);
+    T.ex[3 * ibox + 1] += quant(c[1]);
+    T.ex[3 * ibox + 2] += quant(c[2]);
     // spectral location: the mode's time and, for fd_qmesh (contr / omega
     // once per segment, :829), its signed segment count
     const int lc = T.loc ? (*T.loc)[ibox] : -1;
@@ -1534,13 +1598,47 @@ struct BeRun {
 };
 
 // propagator_H(b): |b| accumulated and signed by the entry, src/collision_operator.cpp:857-870
+// Sum of |x| in the order of the reference's b.array().abs().sum()
+// (propagator_H, src/collision_operator.cpp:857-870): Eigen's vectorised
+// reduction of a 16-byte aligned vector over packets of two doubles, as in
+// its redux_impl for LinearVectorizedTraversal: two packet accumulators over
+// blocks of four, their lane-wise sum, the last whole packet, then the two
+// lanes, then the tail element.
+inline double eigen_abs_sum(const double* x, std::size_t n) {
+    if (n < 2) return n ? std::fabs(x[0]) : 0.;
+    const std::size_t end2 = n / 4 * 4, end = n / 2 * 2;
+    double a0 = std::fabs(x[0]), a1 = std::fabs(x[1]);
+    if (end > 2) {
+        double b0 = std::fabs(x[2]), b1 = std::fabs(x[3]);
+        for (std::size_t i = 4; i < end2; i += 4) {
+            a0 += std::fabs(x[i]);
+            a1 += std::fabs(x[i + 1]);
+            b0 += std::fabs(x[i + 2]);
+            b1 += std::fabs(x[i + 3]);
+        }
+        a0 += b0;
+        a1 += b1;
+        if (end > end2) {
+            a0 += std::fabs(x[end2]);
+            a1 += std::fabs(x[end2 + 1]);
+        }
+    }
+    double r = a0 + a1;
+    for (std::size_t i = end; i < n; ++i) r += std::fabs(x[i]);
+    return r;
+}
+
+// lirp of two signed CDFs, src/collision_operator.cpp:918-929.
+inline double lirp_value(double a, double b, double T1, double T2, double Tx) {
+    return a + (Tx - T1) * (b - a) / (T2 - T1);
+}
+
 inline void build_cumm(BeRun& R, const double* P) {
     const std::size_t n = std::size_t(R.nm);
     R.cumm.resize(n * n);
     for (std::size_t j = 0; j < n; ++j) {
         const double* col = P + j * n;
-        double abssum = 0.;
-        for (std::size_t i = 0; i < n; ++i) abssum += std::fabs(col[i]);
+        const double abssum = eigen_abs_sum(col, n);
         double acc = 0.;
         for (std::size_t i = 0; i < n; ++i) {
             acc += std::fabs(col[i]);
@@ -1695,19 +1793,6 @@ inline V2 border_point(const Border& b, Pcg64& rng) {
     }
 }
 
-// Isothermal_wall_distribution pmf (src/sampling.cpp:189-269) for normal n.
-inline double wall_pmf(const Modes& m, V2 n, double Tw, double Te, std::vector<double>& pmf) {
-    pmf.assign(m.n(), 0.);
-    for (std::size_t k = 0; k < m.n(); ++k) {
-        const double vn = n.x * m.vx[k] + n.y * m.vy[k] + 0. * m.vz[k];
-        if (vn <= 0. || almost_equal(0., m.omega[k]))
-            pmf[k] = 0.;
-        else
-            pmf[k] = vn * m.omega[k] * std::fabs(bose_einstein(m.omega[k], Tw) - bose_einstein(m.omega[k], Te));
-    }
-    return 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
-}
-
 // Ntogenerate stochastic rounding (src/sampling.cpp:243-260).
 inline std::size_t n_to_generate(double gen, Pcg64& rng) {
     std::size_t np = std::size_t(gen);
@@ -1727,25 +1812,31 @@ int fail(int code, const char* what) {
     return code;
 }
 
+orc::Modes modes_from(const bte_mode_table* mt) {
+    orc::Modes m;
+    m.nq = mt->nq;
+    m.nb = mt->nb;
+    const std::size_t n = std::size_t(mt->nq) * mt->nb;
+    m.omega.assign(mt->omega, mt->omega + n);
+    m.w.assign(mt->w, mt->w + n);
+    m.vx.resize(n);
+    m.vy.resize(n);
+    m.vz.resize(n);
+    for (std::size_t k = 0; k < n; ++k) {
+        m.vx[k] = mt->vg[3 * k];
+        m.vy[k] = mt->vg[3 * k + 1];
+        m.vz[k] = mt->vg[3 * k + 2];
+    }
+    std::memcpy(m.dq, mt->dq, sizeof(m.dq));
+    m.V = mt->V;
+    m.c = mt->c_lat;
+    for (int i = 0; i < 3; ++i) m.grid[i] = mt->grid[i];
+    return m;
+}
+
 orc::Sim build_sim(const bte_mode_table* mt, const bte_geometry* gm) {
     orc::Sim S;
-    S.m.nq = mt->nq;
-    S.m.nb = mt->nb;
-    const std::size_t n = std::size_t(mt->nq) * mt->nb;
-    S.m.omega.assign(mt->omega, mt->omega + n);
-    S.m.w.assign(mt->w, mt->w + n);
-    S.m.vx.resize(n);
-    S.m.vy.resize(n);
-    S.m.vz.resize(n);
-    for (std::size_t k = 0; k < n; ++k) {
-        S.m.vx[k] = mt->vg[3 * k];
-        S.m.vy[k] = mt->vg[3 * k + 1];
-        S.m.vz[k] = mt->vg[3 * k + 2];
-    }
-    std::memcpy(S.m.dq, mt->dq, sizeof(S.m.dq));
-    S.m.V = mt->V;
-    S.m.c = mt->c_lat;
-    for (int i = 0; i < 3; ++i) S.m.grid[i] = mt->grid[i];
+    S.m = modes_from(mt);
     S.thickness = gm->thickness;
     std::size_t off = 0;
     for (int i = 0; i < gm->nboxes; ++i) {
@@ -1852,6 +1943,13 @@ void oracle_pcg64(uint64_t seed, uint64_t stream, int n, uint64_t* raw, double* 
         canon[i] = orc::canonical(b);
         ints[i] = orc::uniform_int(c, 0, int_hi);
     }
+}
+
+// uniform_int_distribution<int>(0, his[i]) for i = 0..n-1, drawn in sequence
+// from one pcg64(seed, stream), as one engine shared by successive calls.
+void oracle_uniform_int_seq(uint64_t seed, uint64_t stream, const int* his, int n, int* out) {
+    orc::Pcg64 g(seed, stream);
+    for (int i = 0; i < n; ++i) out[i] = orc::uniform_int(g, 0, his[i]);
 }
 
 // The time grid of src/RTA_MC2D.cpp:2118-2124 (Eigen LinSpaced); returns ntime.
@@ -1971,6 +2069,189 @@ int oracle_kat_propagator(const double* P, int n, int col, double u, int* sign) 
     return int(r.second);
 }
 
+// ---- Hooks compared with the reference's own code (tests/golden/
+// ref_pins.json, built by oracle/build_ref.py from the cited functions).
+// Each calls the helper the runs above use.
+int oracle_kat_almost_equal(double a, double b) { return orc::almost_equal(a, b) ? 1 : 0; }
+
+// get_bin_index, src/RTA_MC2D.cpp:140-148.
+long long oracle_kat_bin_index(const double* grid, int n, double t) {
+    const std::vector<double> g(grid, grid + n);
+    return (long long)orc::bin_index(g, t);
+}
+
+// process_segment (transient), src/RTA_MC2D.cpp:699-769: the three tallies
+// of one segment with velocity (vx, vy), per bin.
+void oracle_kat_segment3(const double* grid, int ntime, double t0, double t1, int sign, double vx, double vy,
+                         double* gz, double* jx, double* jy) {
+    orc::Sim S;
+    S.timegrid.assign(grid, grid + ntime);
+    orc::Tally T;
+    T.init(1, std::size_t(ntime - 1));
+    orc::process_segment(S, T, 0, t0, t1, sign, orc::V2{vx, vy});
+    for (int i = 0; i + 1 < ntime; ++i) {
+        gz[i] = T.gz[std::size_t(i)];
+        jx[i] = T.jx[std::size_t(i)];
+        jy[i] = T.jy[std::size_t(i)];
+    }
+}
+
+// process_segment (periodic), src/RTA_MC2D.cpp:784-834: the contributions.
+void oracle_kat_steady_terms(int sign, double dt, double vx, double vy, double* out) {
+    orc::steady_terms(sign, dt, orc::V2{vx, vy}, out);
+}
+
+// get_v, src/RTA_MC2D.cpp:843-856, for every mode.
+void oracle_kat_get_v(const bte_mode_table* mt, double* vx, double* vy) {
+    const orc::Modes m = modes_from(mt);
+    for (std::size_t k = 0; k < m.n(); ++k) {
+        const orc::V2 v = orc::get_v(m, k);
+        vx[k] = v.x;
+        vy[k] = v.y;
+    }
+}
+
+// random_dt, include/sampling.hpp:40-46: K draws from pcg64(seed, stream)
+// with rates w[i % nw].
+int oracle_kat_random_dt(uint64_t seed, uint64_t stream, const double* w, int nw, int K, int log_impl,
+                         double* out) {
+    try {
+        orc::Pcg64 rng(seed, stream);
+        for (int i = 0; i < K; ++i) out[i] = orc::random_dt(w[i % nw], rng, log_impl);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_VALUE, e.what());
+    }
+}
+
+// The distributions of src/sampling.cpp over the mode table: kind 0
+// BE_derivative (a = {T}), 1 Isothermal_wall (a = {Tw, Teq, nx, ny, vuc}),
+// 2 outTref (a = {Tinit, Tref, vol}), 3 Nabla_T (a = {gx, gy, T, vol}).
+// Writes the cumulative distribution, the signs and scal = {cumulsum,
+// flux (1) or energy (2, 3)}.
+int oracle_kat_distribution(const bte_mode_table* mt, int kind, const double* a, double* cum, int* sign,
+                            double* scal) {
+    try {
+        const orc::Modes m = modes_from(mt);
+        const double nq = double(m.nq);
+        std::vector<double> pmf;
+        std::vector<int> sg(m.n(), 1);
+        double cs = 0., extra = 0.;
+        if (kind == 0) {
+            pmf = orc::be_derivative_pmf(m, m.w, a[0]);
+        } else if (kind == 1) {
+            cs = orc::wall_pmf(m, orc::V2{a[2], a[3]}, a[0], a[1], pmf);
+            const int s = (a[0] - a[1]) >= 0 ? 1 : -1;
+            sg.assign(m.n(), s);
+            extra = orc::wall_flux(s, cs, nq, a[4]);
+        } else if (kind == 2) {
+            cs = orc::out_tref_pmf(m, a[0], a[1], pmf);
+            sg.assign(m.n(), (a[0] - a[1]) >= 0 ? 1 : -1);
+            extra = orc::dist_energy(a[2], cs, nq);
+        } else if (kind == 3) {
+            cs = orc::nabla_t_pmf(m, a[0], a[1], a[2], pmf, sg);
+            extra = orc::dist_energy(a[3], cs, nq);
+        } else {
+            return fail(BTE_ERR_INPUT, "unknown distribution");
+        }
+        const std::vector<double> c = orc::fill_cumulative(pmf);
+        for (std::size_t k = 0; k < m.n(); ++k) {
+            cum[k] = c[k];
+            sign[k] = sg[k];
+        }
+        scal[0] = cs;
+        scal[1] = extra;
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_VALUE, e.what());
+    }
+}
+
+// Ntogenerate with stochastic rounding from one pcg64(seed, stream):
+// K calls, kind 1 (wall) and 3 (Nabla_T) with args[i] = {time, spf or vol,
+// Eff}, kind 2 (outTref) with args[i] = {vol, Eff, unused}.
+void oracle_kat_ntogen(int kind, const double* args, int K, double cumulsum, double nq, uint64_t seed,
+                       uint64_t stream, long long* out) {
+    orc::Pcg64 rng(seed, stream);
+    for (int i = 0; i < K; ++i) {
+        const double* q = args + 3 * i;
+        const double gen = kind == 2 ? orc::gen_plain(q[0], cumulsum, q[1], nq)
+                                     : orc::gen_scaled(q[0], q[1], cumulsum, q[2], nq);
+        out[i] = (long long)orc::n_to_generate(gen, rng);
+    }
+}
+
+// K draws of the BE_derivative distribution at T (Grid_distribution::sample).
+void oracle_kat_be_samples(const bte_mode_table* mt, double T, uint64_t seed, uint64_t stream, int K,
+                           long long* out) {
+    const orc::Modes m = modes_from(mt);
+    const std::vector<double> c = orc::fill_cumulative(orc::be_derivative_pmf(m, m.w, T));
+    orc::Pcg64 rng(seed, stream);
+    for (int i = 0; i < K; ++i) out[i] = (long long)orc::lower_bound_idx(c, orc::canonical(rng));
+}
+
+// The Lambert table of diffusive_bouncing (src/RTA_MC2D.cpp:556-626) in
+// CSR form: row k holds idx[rowptr[k] .. rowptr[k+1]) with their values.
+// Returns the number of entries (written only when it fits `cap`).
+long long oracle_kat_lambert(const bte_mode_table* mt, long long* rowptr, long long* idx, double* val,
+                             long long cap) {
+    orc::Sim S;
+    S.m = modes_from(mt);
+    orc::build_lambert(S);
+    long long nnz = 0;
+    for (auto& r : S.lambert) nnz += (long long)r.size();
+    if (nnz > cap) return nnz;
+    long long o = 0;
+    for (std::size_t k = 0; k < S.lambert.size(); ++k) {
+        rowptr[k] = o;
+        for (auto& [f, v] : S.lambert[k]) {
+            idx[o] = (long long)f;
+            val[o] = v;
+            ++o;
+        }
+    }
+    rowptr[S.lambert.size()] = o;
+    return nnz;
+}
+
+// K bounces (diffusive_bouncing::bounce, :635-678) of mode imode at a wall
+// of outward normal (npx, npy), one pcg64(seed, stream) for all of them.
+int oracle_kat_bounce(const bte_mode_table* mt, double npx, double npy, int imode, uint64_t seed,
+                      uint64_t stream, int K, long long* out) {
+    try {
+        orc::Sim S;
+        S.m = modes_from(mt);
+        orc::build_lambert(S);
+        orc::Pcg64 rng(seed, stream);
+        for (int i = 0; i < K; ++i) out[i] = (long long)orc::bounce(S, orc::V2{npx, npy}, std::size_t(imode), rng);
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
+// propagator_H(b) (src/collision_operator.cpp:857-870): the signed
+// cumulative distribution of column `col` of the column-major n x n P.
+void oracle_kat_prop_cumm(const double* P, int n, int col, double* out) {
+    orc::BeRun R;
+    R.nm = n;
+    orc::build_cumm(R, P);
+    for (int i = 0; i < n; ++i) out[i] = R.cumm[std::size_t(col) * std::size_t(n) + std::size_t(i)];
+}
+
+// lirp (src/collision_operator.cpp:918-929) of column `col` of P1 (at T1)
+// and P2 (at T2), at Tx.
+void oracle_kat_lirp(const double* P1, const double* P2, int n, int col, double T1, double T2, double Tx,
+                     double* out) {
+    orc::BeRun A, B;
+    A.nm = B.nm = n;
+    orc::build_cumm(A, P1);
+    orc::build_cumm(B, P2);
+    const std::size_t o = std::size_t(col) * std::size_t(n);
+    for (int i = 0; i < n; ++i)
+        out[i] = orc::lirp_value(A.cumm[o + std::size_t(i)], B.cumm[o + std::size_t(i)], T1, T2, Tx);
+}
+
 // Spectral locations for the following oracle_rta_run calls (nloc = 0: off).
 void oracle_set_spectral(int nloc, const int* boxes) {
     g_spec_boxes.assign(boxes, boxes + (nloc > 0 ? nloc : 0));
@@ -2015,10 +2296,7 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
         for (int k = 0; k < nmat; ++k) {
             const std::size_t n = S.m.n();
             S.mat_w.emplace_back(mw + std::size_t(k) * n, mw + std::size_t(k + 1) * n);
-            std::vector<double> pm(n);
-            for (std::size_t i = 0; i < n; ++i)
-                pm[i] = S.m.omega[i] <= 0. ? 0. : orc::bose_einstein_kernel(S.m.omega[i], mT0[k]) * S.mat_w.back()[i];
-            S.mat_res.push_back(orc::fill_cumulative(pm));
+            S.mat_res.push_back(orc::fill_cumulative(orc::be_derivative_pmf(S.m, S.mat_w.back(), mT0[k])));
             S.mat_T0.push_back(mT0[k]);
         }
         // time grid (src/RTA_MC2D.cpp:2118-2124), Eigen LinSpaced(low + i*step)
@@ -2029,10 +2307,7 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
         for (std::size_t i = 0; i < ntime; ++i)
             S.timegrid[i] = (i == ntime - 1) ? maxtime : 0.0 + double(i) * step;
         // resampling distribution (BE_derivative_distribution)
-        std::vector<double> pmf(S.m.n());
-        for (std::size_t k = 0; k < S.m.n(); ++k)
-            pmf[k] = S.m.omega[k] <= 0. ? 0. : orc::bose_einstein_kernel(S.m.omega[k], rp->T0) * S.m.w[k];
-        S.resample_cdf = orc::fill_cumulative(pmf);
+        S.resample_cdf = orc::fill_cumulative(orc::be_derivative_pmf(S.m, S.m.w, rp->T0));
         orc::build_lambert(S);
         int64_t total_particles = rp->nparticles;
         std::vector<double> Em;  // energy rate per material (with shares)
@@ -2234,10 +2509,7 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
         if (orc::almost_equal(std::sqrt(gx * gx + gy * gy), 0.))
             return fail(BTE_ERR_INPUT, "the steady state needs a non-zero temperature gradient");
         const std::size_t n = S.m.n(), nbx = S.sys.size(), nb = std::size_t(S.m.nb);
-        std::vector<double> pmf(n);
-        for (std::size_t k = 0; k < n; ++k)
-            pmf[k] = S.m.omega[k] <= 0. ? 0. : orc::bose_einstein_kernel(S.m.omega[k], sp->T0) * S.m.w[k];
-        S.resample_cdf = orc::fill_cumulative(pmf);
+        S.resample_cdf = orc::fill_cumulative(orc::be_derivative_pmf(S.m, S.m.w, sp->T0));
         orc::build_lambert(S);
         orc::build_generators(S, sp->T0, false);
         const double E0 = S.gens.empty() ? 0. : S.energy;
@@ -2530,13 +2802,10 @@ int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const
                 orc::build_cumm(R2, m2->second);
                 const double T1 = m1->first, T2 = m2->first;
                 for (std::size_t i = 0; i < nn; ++i)
-                    R.cumm[i] = R.cumm[i] + (bp->T0 - T1) * (R2.cumm[i] - R.cumm[i]) / (T2 - T1);
+                    R.cumm[i] = orc::lirp_value(R.cumm[i], R2.cumm[i], T1, T2, bp->T0);
             }
         } else {
-            std::vector<double> pmf(n);
-            for (std::size_t k = 0; k < n; ++k)
-                pmf[k] = m.omega[k] <= 0. ? 0. : orc::bose_einstein_kernel(m.omega[k], bp->T0) * m.w[k];
-            R.resample_cdf = orc::fill_cumulative(pmf);
+            R.resample_cdf = orc::fill_cumulative(orc::be_derivative_pmf(m, m.w, bp->T0));
         }
         for (auto& b : S.sys) {
             R.Eborder.push_back(std::vector<int>(b.borders.size(), 0));
@@ -2551,17 +2820,11 @@ int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const
         std::vector<double> pmf;
         for (auto& s : S.sys) {
             if (s.reservoir || s.periodic || orc::almost_equal(s.Teq, s.Treal)) continue;
-            pmf.assign(n, 0.);
-            for (std::size_t k = 0; k < n; ++k) {
-                const double om = m.omega[k];
-                if (orc::almost_equal(om, 0.)) continue;
-                pmf[k] = om * std::fabs(orc::bose_einstein(om, s.Treal) - orc::bose_einstein(om, s.Teq));
-            }
-            const double cumulsum = 1.0e+12 * orc::hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
+            const double cumulsum = orc::out_tref_pmf(m, s.Treal, s.Teq, pmf);
             const int sgn = (s.Treal - s.Teq) >= 0 ? 1 : -1;
             auto cdf = orc::fill_cumulative(pmf);
             const double vol = s.area * S.thickness / vuc;
-            const std::size_t ngen = orc::n_to_generate(vol * cumulsum / (R.Eeff * double(m.nq)), rng);
+            const std::size_t ngen = orc::n_to_generate(orc::gen_plain(vol, cumulsum, R.Eeff, double(m.nq)), rng);
             double x0 = s.hull[0].x, x1 = x0, y0 = s.hull[0].y, y1 = y0;
             for (auto& h : s.hull) {
                 x0 = std::min(x0, h.x); x1 = std::max(x1, h.x);
@@ -2628,7 +2891,8 @@ int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const
             if (!grad.empty()) {
                 std::vector<orc::BeParticle> np;
                 for (auto& G : grad) {
-                    const std::size_t ngen = orc::n_to_generate(R.dt * G.energy / R.Eeff, rng);
+                    const std::size_t ngen = orc::n_to_generate(
+                        orc::gen_scaled(R.dt, G.vol, G.cumulsum, R.Eeff, double(m.nq)), rng);
                     for (std::size_t i = 0; i < ngen; ++i) {
                         orc::BeParticle p;
                         p.pos = orc::random_point(S.sys[G.box], rng);
@@ -2647,7 +2911,7 @@ int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const
                     const double Lb = orc::norm(g.b.p2 - g.b.p1);
                     const double spf = Lb * S.thickness / (m.V * S.thickness / m.c);
                     const std::size_t ngen =
-                        orc::n_to_generate(R.dt * spf * g.cumulsum / (R.Eeff * double(m.nq)), rng);
+                        orc::n_to_generate(orc::gen_scaled(R.dt, spf, g.cumulsum, R.Eeff, double(m.nq)), rng);
                     const orc::Box& inj = S.sys[g.box];
                     for (std::size_t i = 0; i < ngen; ++i) {
                         orc::V2 pp = orc::border_point(g.b, rng);

@@ -26,45 +26,18 @@ def test_canonical_matches_uniform_real_distribution():
 
 
 def test_uniform_int_matches_libstdcxx():
-    g = GOLD["uniform_int"]
-    # the golden run drew all cases from one stream in sequence; replay it
-    # with a mixed-range generator built from the same raw stream
+    """The compiled restatement of uniform_int_distribution draws the golden
+    sequence: every range (0 .. 2^31 - 2) from one shared stream, as the
+    golden run did."""
     import ctypes as C
-    lib = pyoracle.load()
-    his = [c[0] for c in g["cases"]]
-    # draw sequentially: each uniform_int consumes >= 1 raw output; emulate by
-    # re-seeding and drawing with the oracle's own routine one value at a time
-    raw, _, _ = pyoracle.pcg64(g["seed"], g["stream"], 4 * len(his))
-    # Lemire without rejection for these ranges (rejection probability < 2^-30)
-    vals = []
-    k = 0
-    for hi in his:
-        rng = hi + 1
-        x = int(raw[k])
-        k += 1
-        prod = x * rng
-        lo = prod & ((1 << 64) - 1)
-        if lo < rng:
-            thr = ((1 << 64) - rng) % rng
-            while lo < thr:
-                x = int(raw[k]); k += 1
-                prod = x * rng
-                lo = prod & ((1 << 64) - 1)
-        vals.append(prod >> 64)
-    assert vals == [c[1] for c in g["cases"]]
-    # and the oracle's compiled routine agrees on a single range
-    _, _, ints = pyoracle.pcg64(g["seed"], g["stream"], 8, int_hi=0)
-    assert all(v == 0 for v in ints)
-
-
-def test_oracle_uniform_int_routine_matches_golden_range():
     g = GOLD["uniform_int"]
-    # first 8 cases have hi = 0, then 1, ...: check the compiled routine on hi=0
-    # and the pure-Python restatement above on all; here the compiled routine
-    # on a fresh stream against the Python restatement for hi = 6
-    raw, _, ints = pyoracle.pcg64(7, 11, 64, int_hi=6)
-    py = [(int(x) * 7) >> 64 for x in raw]
-    assert list(ints) == py
+    lib = pyoracle.load()
+    his = np.array([c[0] for c in g["cases"]], dtype=np.int32)
+    out = np.zeros(his.size, dtype=np.int32)
+    ip = C.POINTER(C.c_int)
+    lib.oracle_uniform_int_seq(g["seed"], g["stream"], his.ctypes.data_as(ip), his.size, out.ctypes.data_as(ip))
+    assert list(out) == [c[1] for c in g["cases"]]
+    assert len(set(c[0] for c in g["cases"])) == 7
 
 
 @pytest.mark.parametrize("idx", range(5))
