@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--sweep-seconds", type=float, default=240.0, help="time cap per arm (c3)")
     ap.add_argument("--per-step", type=int, default=0, help="particles per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the time-to-1%% summaries of the sweep and the gradient")
+    ap.add_argument("--extra-seconds", type=float, default=30.0,
+                    help="time cap of each arm of those summaries")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     return ap.parse_args()
 
@@ -318,31 +322,58 @@ class SweepStats:
 
 
 def run_sweep(args, rank, world, local):
-    """The batched sweep: 64 ribbons (16 widths 20 nm - 2 um x 4 temperatures,
-    1 um long, p = 0, reservoirs at T +- 1 K) with budgets N_w = 1e5 100^(k/15).
-    Each arm repeats independent replicas until every case's kappa_eff has
-    3 sigma / kappa <= tol (batch means).  Plain: each case alone, one
-    context per temperature, replicas of N_w particles.  Batched: every
-    unconverged case in one grid-kernel launch (union geometry, one material
-    per case, particle shares = budgets), converged cases dropped by a share
-    update.  Table construction is outside both clocks."""
+    """The C3 workload line (see sweep_arms)."""
     import torch
-    import btegpu
-    import synth
     if world > 1 and rank != 0:
         return 0
     torch.cuda.set_device(local)
+    print(json.dumps(sweep_arms(local, args.sweep_tol, args.sweep_seconds)))
+    return 0
+
+
+def kappa_agreement(kap_b, rel_b, sp):
+    """Largest |z| between the batched and the per-case kappa_eff over the
+    cases both arms converged (sigma of each from its own batch means)."""
+    zs = []
+    for i in range(len(kap_b)):
+        v = np.asarray(sp.k[i])
+        if len(v) < 4 or not np.isfinite(rel_b[i]):
+            continue
+        sb = rel_b[i] * abs(kap_b[i]) / 3.0
+        spl = v.std(ddof=1) / np.sqrt(len(v))
+        zs.append(abs(kap_b[i] - v.mean()) / np.sqrt(sb ** 2 + spl ** 2))
+    return float(max(zs)) if zs else None
+
+
+def sweep_arms(local, tol, cap):
+    """The batched sweep: 64 ribbons (16 widths 20 nm - 2 um x 4 temperatures,
+    1 um long, p = 0, reservoirs at T +- 1 K) with budgets N_w = 1e5 100^(k/15).
+    Each arm runs until every case's kappa_eff has 3 sigma / kappa <= tol.
+    Plain: each case alone, one context per temperature, independent
+    replicas of N_w particles (batch means over at least four).  Batched:
+    every unconverged case in one grid-kernel launch per round (union
+    geometry, one material per case); each launch deals its particles to 8
+    replica groups, so batch means exist after one launch, and each round
+    gives each case, through its particle share, what its measured variance
+    still asks for (a quarter budget in the first round); converged cases
+    drop out.  Table construction is outside both clocks.  Returns the line."""
+    import torch
+    import btegpu
+    import synth
     L, ncells, dt, maxtime = 1000.0, 50, 10.0, 1000.0
     cases = synth.sweep_cases()
     temps = sorted({c["T"] for c in cases})
     tabs = {T: synth.mode_table(32, 3, 3, T, config=0) for T in temps}
     nc = len(cases)
     budgets = np.array([c["budget"] for c in cases], dtype=np.int64)
-    tol, cap = args.sweep_tol, args.sweep_seconds
     clocks = ClockSampler(local)
     clocks.start()
 
-    # ---- batched
+    # ---- batched: every unconverged case in one launch per round; the
+    # launch deals its particles to G replica groups (batch means inside
+    # the launch) and each round gives each case the particles its measured
+    # variance still asks for
+    G = 8
     g = synth.sweep_union_geometry(cases, length=L, ncells=ncells)
     eng = btegpu.Engine(local)
     eng.load_modes(tabs[300.0])
@@ -351,26 +382,51 @@ def run_sweep(args, rank, world, local):
     Ts = [c["T"] for c in cases]
     eng.load_materials(rates, Ts, budgets / budgets.sum())
     eng.rta_run(300.0, dt, maxtime, 100000, seed=1)          # builds the tables
+    eng.set_groups(G)
     per = ncells + 2
-    sb = SweepStats(nc)
     active = np.ones(nc, dtype=bool)
+    nmin = 2000.0 * G
+    need = np.maximum(budgets / 4.0, nmin)                     # first round: a quarter budget
+    w_sum = np.zeros(nc)                                       # particles so far per case
+    wk_sum = np.zeros(nc)                                      # particle-weighted kappa sum
+    rounds_i = [[] for _ in range(nc)]                         # (particles, variance of the round mean)
+    kap_b = np.full(nc, np.nan)
+    rel_b = np.full(nc, np.inf)
     ev_b = 0
     reps_b = 0
+    parts_b = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     while active.any() and time.perf_counter() - t0 < cap:
-        share = np.where(active, budgets, 0).astype(float)
-        eng.load_materials(rates, Ts, share / share.sum())
-        N = int(budgets[active].sum())
+        alloc = np.where(active, np.maximum(need, nmin), 0.0)
+        N = int(alloc.sum())
+        eng.load_materials(rates, Ts, alloc / alloc.sum())
         r = eng.rta_run(300.0, dt, maxtime, N, seed=1000 + reps_b, raw=False)
+        grs = [eng.group_result(k, r["jx"].shape) for k in range(G)]
         ev_b += int(r["events"])
         reps_b += 1
+        parts_b += N
         for i in np.flatnonzero(active):
-            sb.add(i, synth.sweep_kappa(r["jx"], slice(per * i, per * i + ncells), length=L))
-            if sb.rel3(i) <= tol:
+            sl = slice(per * i, per * i + ncells)
+            kg = np.array([synth.sweep_kappa(x["jx"], sl, length=L) for x in grs])
+            n_i = alloc[i]
+            rounds_i[i].append((n_i, kg.var(ddof=1) / G))
+            w_sum[i] += n_i
+            wk_sum[i] += n_i * kg.mean()
+            kap_b[i] = wk_sum[i] / w_sum[i]
+            var = sum((n / w_sum[i]) ** 2 * v for n, v in rounds_i[i])
+            rel_b[i] = 3.0 * np.sqrt(var) / abs(kap_b[i])
+            if rel_b[i] <= tol:
                 active[i] = False
+                continue
+            # per-particle variance pooled over the rounds, and the
+            # particles still needed for 3 sigma / kappa <= tol
+            s2 = np.mean([v * n for n, v in rounds_i[i]])
+            total = 9.0 * s2 / (tol * kap_b[i]) ** 2
+            need[i] = max(1.1 * (total - w_sum[i]), nmin)
     t_b = time.perf_counter() - t0
     conv_b = int((~active).sum())
+    eng.set_groups(0)
     eng.close()
 
     # ---- plain
@@ -383,6 +439,7 @@ def run_sweep(args, rank, world, local):
     t_p = 0.0
     ev_p = 0
     reps_p = 0
+    parts_p = 0
     conv_p = 0
     for i, cs in enumerate(cases):
         e = engs[cs["T"]]
@@ -394,6 +451,7 @@ def run_sweep(args, rank, world, local):
         while t_p + (time.perf_counter() - t1) < cap:
             r = e.rta_run(cs["T"], dt, maxtime, int(cs["budget"]), seed=5000 + k, raw=False)
             ev_p += int(r["events"])
+            parts_p += int(cs["budget"])
             k += 1
             sp.add(i, synth.sweep_kappa(r["jx"], slice(0, ncells), length=L))
             if sp.rel3(i) <= tol:
@@ -437,7 +495,7 @@ def run_sweep(args, rank, world, local):
     t_setup_b = time.perf_counter() - t3
     eng.close()
     clk = clocks.stop()
-    worst_b = max(sb.rel3(i) for i in range(nc))
+    worst_b = float(np.max(rel_b))
     line = {
         "metric": "seconds to 1% kappa_eff (3 sigma) over the 64-case sweep, batched",
         "value": t_b, "unit": "s", "n_gpus": 1, "steps": reps_b, "warmup": 1,
@@ -447,21 +505,23 @@ def run_sweep(args, rank, world, local):
                                "1 um long, p=0, 32x32x6 modes with tau at T, reservoirs T+-1 K, "
                                "budgets 1e5*100^(k/15), 100 bins of 10 ps",
                    "tol_3sigma": tol, "time_cap_s": cap, "parallelism": "replicas x1"},
-        "batched": {"seconds": t_b, "replicas": reps_b, "cases_converged": conv_b, "events": ev_b,
+        "batched": {"seconds": t_b, "launches": reps_b, "replica_groups": G, "particles": parts_b,
+                    "cases_converged": conv_b, "events": ev_b,
                     "events_per_s": ev_b / max(t_b, 1e-9), "worst_3sigma_rel": worst_b},
-        "plain": {"seconds": t_p, "launches": reps_p, "cases_converged": conv_p, "events": ev_p,
+        "plain": {"seconds": t_p, "launches": reps_p, "particles": parts_p, "cases_converged": conv_p,
+                  "events": ev_p,
                   "events_per_s": ev_p / max(t_p, 1e-9)},
         "speedup_plain_over_batched": (t_p / t_b) if (conv_b == nc and conv_p == nc) else None,
         "with_table_setup": {"batched_seconds": t_b + t_setup_b, "batched_setup_s": t_setup_b,
                              "plain_fresh_contexts_seconds": t_f, "plain_fresh_cases_converged": conv_f,
                              "speedup": (t_f / (t_b + t_setup_b)) if (conv_b == nc and conv_f == nc)
                              else None},
-        "kappa_eff_W_mK": {f"{c['T']:.0f}K_{c['width']:.0f}nm": round(sb.mean(i), 4)
+        "kappa_eff_W_mK": {f"{c['T']:.0f}K_{c['width']:.0f}nm": round(float(kap_b[i]), 4)
                            for i, c in enumerate(cases)},
+        "kappa_batched_vs_plain_max_z": kappa_agreement(kap_b, rel_b, sp),
         "clocks": clk,
     }
-    print(json.dumps(line))
-    return 0
+    return line
 
 
 def kappa_weights(c, Eeff):
@@ -484,19 +544,27 @@ def kappa_weights(c, Eeff):
 
 
 def run_adjoint(args, rank, world, local):
+    """The C4 workload line (see adjoint_arms)."""
+    import torch
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    print(json.dumps(adjoint_arms(local, args.sweep_seconds)))
+    return 0
+
+
+def adjoint_arms(local, cap):
     """Gradient of kappa_eff of the plain ribbon at p = 0.2 (6144 modes,
     N = 1e7) with respect to 32 seeded mode lifetimes and p, to 1% (3 sigma,
     L2 over the 33 components): the adjoint against central differences
     with common random numbers (dtau/tau = 1e-3, dp = 1e-3).  Differences in
     production mode follow the spec; alias tables decouple the two runs, so
     differences in replay mode (CDF draws, coupled) are timed as well.  Each
-    arm is capped in time and reports the accuracy it reached."""
-    import torch
+    arm is capped in time and reports the accuracy it reached, and the time
+    to 1 % extrapolated from it (the error falls as the inverse square root
+    of the time spent).  Returns the line."""
     import btegpu
     import synth
-    if world > 1 and rank != 0:
-        return 0
-    torch.cuda.set_device(local)
     c = synth.config0(n_particles=10_000_000)
     p0 = 0.2
     m = c["modes"]
@@ -510,7 +578,6 @@ def run_adjoint(args, rank, world, local):
     movable = np.flatnonzero((m["w"] > 0) & (m["omega"] > 0))
     modes = np.sort(rng.choice(movable, 32, replace=False))
     tau = 1.0 / m["w"][modes]
-    cap = args.sweep_seconds
     clocks = ClockSampler(local)
     clocks.start()
 
@@ -580,6 +647,14 @@ def run_adjoint(args, rank, world, local):
         se = np.sqrt(f.var(axis=0, ddof=1) / len(f) + np.var(rows_a, axis=0, ddof=1) / len(rows_a))
         return float(np.max(np.abs(f.mean(axis=0) - ga) / np.maximum(se, 1e-300)))
 
+    def to_1pct(t, a):
+        """Seconds to 1 % at the rate observed: accuracy ~ t^-1/2."""
+        if not np.isfinite(a) or t <= 0:
+            return None
+        return t if a <= 0.01 else t * (a / 0.01) ** 2
+
+    acc_a, acc_fp, acc_fr = acc(rows_a), acc(rows_fp), acc(rows_fr)
+    t1_a, t1_fp, t1_fr = to_1pct(t_a, acc_a), to_1pct(t_fp, acc_fp), to_1pct(t_fr, acc_fr)
     line = {
         "metric": "seconds to a 1% (3 sigma) gradient of kappa_eff, adjoint",
         "value": t_a, "unit": "s", "n_gpus": 1, "steps": len(rows_a), "warmup": 1,
@@ -589,17 +664,54 @@ def run_adjoint(args, rank, world, local):
                                "100 bins of 10 ps, N=1e7; dkappa/dtau on 32 seeded modes + dkappa/dp",
                    "accuracy": "3 * ||SE||_2 / ||g||_2 <= 1% over the 33 components",
                    "time_cap_s": cap},
-        "adjoint": {"seconds": t_a, "replicas": len(rows_a), "accuracy": acc(rows_a),
-                    "events": ev_a, "dkappa_dp": float(ga[-1])},
+        "adjoint": {"seconds": t_a, "replicas": len(rows_a), "accuracy": acc_a,
+                    "events": ev_a, "dkappa_dp": float(ga[-1]), "seconds_to_1pct": t1_a},
         "fd_production": {"seconds": t_fp, "replicas": len(rows_fp), "runs": runs_fp,
-                          "accuracy": acc(rows_fp), "max_z_vs_adjoint": agree(rows_fp)},
+                          "accuracy": acc_fp, "max_z_vs_adjoint": agree(rows_fp),
+                          "seconds_to_1pct_extrapolated": t1_fp},
         "fd_replay": {"seconds": t_fr, "replicas": len(rows_fr), "runs": runs_fr, "particles_per_run": N // 10,
-                      "accuracy": acc(rows_fr), "max_z_vs_adjoint": agree(rows_fr)},
+                      "accuracy": acc_fr, "max_z_vs_adjoint": agree(rows_fr),
+                      "seconds_to_1pct_extrapolated": t1_fr},
+        "speedup_over_fd": ({"production": (t1_fp / t1_a) if t1_fp else None,
+                             "replay": (t1_fr / t1_a) if t1_fr else None}
+                            if t1_a and acc_a <= 0.01 else None),
         "clocks": clk,
     }
-    print(json.dumps(line))
     eng.close()
-    return 0
+    return line
+
+
+def time_to_1pct(local, cap):
+    """The metric's second half, bounded for the default run: seconds to a
+    1 % (3 sigma) kappa_eff over the 64-case sweep, batched against per-case
+    launches, and seconds to a 1 % gradient of kappa_eff, the adjoint
+    against central differences (each arm capped at `cap` seconds; the
+    differences' time to 1 % is extrapolated from the accuracy they reach)."""
+    out = {}
+    try:
+        sw = sweep_arms(local, 0.01, cap)
+        out["sweep"] = {
+            "workload": sw["config"]["workload"], "tol_3sigma": 0.01, "time_cap_s": cap,
+            "batched_s": sw["batched"]["seconds"], "batched_cases_converged": sw["batched"]["cases_converged"],
+            "plain_s": sw["plain"]["seconds"], "plain_cases_converged": sw["plain"]["cases_converged"],
+            "speedup_plain_over_batched": sw["speedup_plain_over_batched"],
+            "with_table_setup": sw["with_table_setup"], "clocks": sw["clocks"]}
+    except Exception as e:  # the summaries must not hide the headline line
+        out["sweep"] = {"failed": str(e)}
+    try:
+        ad = adjoint_arms(local, cap)
+        out["gradient"] = {
+            "workload": ad["config"]["workload"], "accuracy": ad["config"]["accuracy"], "time_cap_s": cap,
+            "adjoint_s": ad["adjoint"]["seconds_to_1pct"], "adjoint_accuracy": ad["adjoint"]["accuracy"],
+            "fd_production_s_extrapolated": ad["fd_production"]["seconds_to_1pct_extrapolated"],
+            "fd_production_accuracy": ad["fd_production"]["accuracy"],
+            "fd_production_max_z_vs_adjoint": ad["fd_production"]["max_z_vs_adjoint"],
+            "fd_replay_s_extrapolated": ad["fd_replay"]["seconds_to_1pct_extrapolated"],
+            "fd_replay_accuracy": ad["fd_replay"]["accuracy"],
+            "speedup_over_fd": ad["speedup_over_fd"], "clocks": ad["clocks"]}
+    except Exception as e:
+        out["gradient"] = {"failed": str(e)}
+    return out
 
 
 def main():
@@ -753,8 +865,8 @@ def main():
             "l2_reductions": l2red,
             "clocks": clk,
             "tuning": {"block_threads": choice[0], "blocks_per_sm": choice[1],
-                       "smem_tally": choice[2],
-                       "ns_per_event": {f"{k[0]}x{k[1]}{'s' if k[2] else ''}": v
+                       "smem_tally": choice[2], "particles_per_thread": choice[3],
+                       "ns_per_event": {f"{k[0]}x{k[1]}{'s' if k[2] else ''}{'p2' if k[3] == 2 else ''}": v
                                         for k, v in tuned.items()}},
         }
         if world == 1 and not args.no_cpu_baseline:
@@ -772,8 +884,11 @@ def main():
             except Exception as e:  # the baseline must not hide the GPU line
                 line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": os.cpu_count(),
                                         "kind": "port", "sample": f"failed: {e}"}
-        print(json.dumps(line))
     eng.close()
+    if rank == 0:
+        if world == 1 and args.workload == "c1" and not args.no_extras:
+            line["time_to_1pct"] = time_to_1pct(local, args.extra_seconds)
+        print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
     return 0

@@ -32,7 +32,7 @@ PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
                   "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run",
                   "bte_steady_run", "bte_load_materials", "bte_rta_adjoint", "bte_set_spectral",
-                  "bte_get_spectral"]
+                  "bte_get_spectral", "bte_set_groups", "bte_get_group_result"]
 
 
 class BteError(RuntimeError):
@@ -191,7 +191,7 @@ def berta_params(dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, mode=MODE_PRODU
 
 class Tuning(C.Structure):
     _fields_ = [("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
-                ("smem_tally", C.c_int32), ("smem_alias", C.c_int32)]
+                ("smem_tally", C.c_int32), ("particles_per_thread", C.c_int32)]
 
 
 def _dptr(a):
@@ -292,6 +292,10 @@ def load_library(path: str = LIB_PATH):
     lib.bte_steady_run.restype = C.c_int
     lib.bte_rta_run_noalloc.argtypes = [vp, C.POINTER(RtaParams), C.c_void_p, C.POINTER(RtaResult)]
     lib.bte_rta_run_noalloc.restype = C.c_int
+    lib.bte_set_groups.argtypes = [vp, C.c_int32]
+    lib.bte_set_groups.restype = C.c_int
+    lib.bte_get_group_result.argtypes = [vp, C.c_int32, C.POINTER(RtaResult)]
+    lib.bte_get_group_result.restype = C.c_int
     for f in ("bte_create", "bte_destroy", "bte_last_error", "bte_load_modes",
               "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes"):
         getattr(lib, f).restype = C.c_int
@@ -351,8 +355,8 @@ class Engine:
         self._keep["geom"] = keep
         self.nboxes = int(g["nboxes"])
 
-    def set_tuning(self, block_threads=0, blocks_per_sm=0, smem_tally=1, smem_alias=0):
-        t = Tuning(block_threads, blocks_per_sm, smem_tally, smem_alias)
+    def set_tuning(self, block_threads=0, blocks_per_sm=0, smem_tally=1, particles_per_thread=0):
+        t = Tuning(block_threads, blocks_per_sm, smem_tally, particles_per_thread)
         self._check(self.lib.bte_set_tuning(self.ctx, C.byref(t)))
 
     def rta_run(self, T0, dt, maxtime, N, seed=1, mode=MODE_PRODUCTION, source=SOURCE_WALLS,
@@ -484,6 +488,27 @@ def _engine_get_spectral(self, nbins=1):
     return out
 
 
+def _engine_set_groups(self, ngroups: int):
+    """Replica groups of the following production grid runs (0 or 1: off)."""
+    self._check(self.lib.bte_set_groups(self.ctx, int(ngroups)))
+
+
+def _engine_group_result(self, group: int, shape, raw: bool = False):
+    """Outputs of one replica group of the last run, scaled to the whole run."""
+    out = {k: np.zeros(shape) for k in ("temperature", "jx", "jy")}
+    r = RtaResult()
+    r.temperature, r.jx, r.jy = (_dptr(out[k]) for k in ("temperature", "jx", "jy"))
+    if raw:
+        for k in ("gz", "gz_jx", "gz_jy"):
+            out[k] = np.zeros(shape)
+        r.gz, r.gz_jx, r.gz_jy = (_dptr(out[k]) for k in ("gz", "gz_jx", "gz_jy"))
+    self._check(self.lib.bte_get_group_result(self.ctx, int(group), C.byref(r)))
+    out["Eeff"] = r.Eeff
+    return out
+
+
+Engine.set_groups = _engine_set_groups
+Engine.group_result = _engine_group_result
 Engine.set_spectral = _engine_set_spectral
 Engine.get_spectral = _engine_get_spectral
 Engine.rta_adjoint = _engine_rta_adjoint

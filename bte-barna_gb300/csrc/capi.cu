@@ -318,6 +318,79 @@ void prepare_run(bte_ctx* c, const bte_rta_params* p) {
 }
 }  // namespace bte
 
+namespace bte {
+// The post-processing of one run's raw tallies into its outputs
+// (src/RTA_MC2D.cpp:2336-2435): / V_box, x Eeff (per material with shares),
+// the flux factor, the time integration of a walls source (or bin averages
+// of an initial deviation) and T = gz / (C_v / vcorr) + T0.
+void rta_post(const bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, double Eeff, double step,
+              std::vector<double> gz, std::vector<double> jx, std::vector<double> jy, bte_rta_result* out) {
+    const bte::HostModes& m = c->modes;
+    const bte::HostGeometry& g = c->geom;
+    const std::size_t nk = std::size_t(nbx) * std::size_t(nbins);
+    // post-processing, src/RTA_MC2D.cpp:2336-2435
+    for (int ir = 0; ir < nbx; ++ir) {
+        const double vbox = g.boxes[std::size_t(ir)].area * g.thickness;
+        for (int i = 0; i < nbins; ++i) {
+            const std::size_t k = std::size_t(ir) * nbins + i;
+            gz[k] /= vbox;
+            jx[k] /= vbox;
+            jy[k] /= vbox;
+        }
+    }
+    if (!c->mat_share.empty() && p->source == BTE_SOURCE_WALLS) {
+        // Eeff_m = E_m / (share_m N) per material
+        for (int ir = 0; ir < nbx; ++ir) {
+            const std::size_t k = std::size_t(g.mat[std::size_t(ir)]);
+            const double Em = c->mat_share[k] > 0. ? c->mat_energy[k] / (c->mat_share[k] * double(p->nparticles)) : 0.;
+            for (int i = 0; i < nbins; ++i) {
+                const std::size_t q = std::size_t(ir) * nbins + i;
+                gz[q] *= Em;
+                jx[q] *= Em * 1e12 * 1e9 * 1e9;
+                jy[q] *= Em * 1e12 * 1e9 * 1e9;
+            }
+        }
+    } else {
+        for (auto& x : gz) x *= Eeff;
+        for (auto& x : jx) x *= Eeff * 1e12 * 1e9 * 1e9;
+        for (auto& x : jy) x *= Eeff * 1e12 * 1e9 * 1e9;
+    }
+    if (p->source == BTE_SOURCE_WALLS) {
+        // step response: integrate in time
+        for (int ir = 0; ir < nbx; ++ir)
+            for (int i = 1; i < nbins; ++i) {
+                const std::size_t k = std::size_t(ir) * nbins + i;
+                gz[k] += gz[k - 1];
+                jx[k] += jx[k - 1];
+                jy[k] += jy[k - 1];
+            }
+    } else {
+        // relaxation of an initial deviation: bin averages
+        for (std::size_t k = 0; k < nk; ++k) {
+            gz[k] /= step;
+            jx[k] /= step;
+            jy[k] /= step;
+        }
+    }
+    const double vcorr = g.thickness / m.c;
+    if (out->temperature) {
+        std::vector<double> cvm(std::size_t(std::max(c->nmat, 1)));
+        for (std::size_t k = 0; k < cvm.size(); ++k)
+            cvm[k] = bte::calc_cv(m, c->nmat > 0 ? c->mat_T0[k] : p->T0);
+        for (int ir = 0; ir < nbx; ++ir) {
+            const double cv = cvm[std::size_t(c->nmat > 0 ? g.mat[std::size_t(ir)] : 0)];
+            const double T0b = bte::box_T0(c, ir, p->T0);
+            for (int i = 0; i < nbins; ++i) {
+                const std::size_t k = std::size_t(ir) * nbins + i;
+                out->temperature[k] = gz[k] / (cv / vcorr) + T0b;
+            }
+        }
+    }
+    if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
+    if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
+}
+}  // namespace bte
+
 extern "C" {
 
 int32_t bte_version(void) { return BTEGPU_VERSION; }
@@ -382,12 +455,17 @@ bte_status bte_set_tuning(bte_ctx* c, const bte_tuning* t) {
     c->tune.block_threads = t->block_threads;
     c->tune.blocks_per_sm = t->blocks_per_sm;
     c->tune.smem_tally = t->smem_tally;
-    c->tune.smem_alias = t->smem_alias;
+    if (t->particles_per_thread < 0 || t->particles_per_thread > 2) {
+        c->err = "particles_per_thread must be 1 or 2 (0 = default)";
+        return BTE_ERR_INPUT;
+    }
+    c->tune.particles_per_thread = t->particles_per_thread;
     return BTE_OK;
 }
 
 bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
     if (!c) return BTE_ERR_INPUT;
+    c->group_valid = false;
     try {
         ck(cudaSetDevice(c->device), "cudaSetDevice");
         c->modes = bte::build_modes(mt);
@@ -409,6 +487,7 @@ bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
 
 bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
     if (!c) return BTE_ERR_INPUT;
+    c->group_valid = false;
     try {
         ck(cudaSetDevice(c->device), "cudaSetDevice");
         bte::HostGeometry ng = bte::build_geometry(g);
@@ -434,6 +513,7 @@ bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
 bte_status bte_load_materials(bte_ctx* c, int32_t nmat, const double* w, const double* T0,
                               const double* share) {
     if (!c) return BTE_ERR_INPUT;
+    c->group_valid = false;
     try {
         if (nmat < 0 || (nmat > 0 && (!w || !T0))) throw Error(BTE_ERR_INPUT, "bad material arrays");
         if (share && nmat > 0) {
@@ -604,6 +684,57 @@ bte_status bte_get_spectral(bte_ctx* c, bte_spectral_result* out) {
     }
 }
 
+bte_status bte_set_groups(bte_ctx* c, int32_t ngroups) {
+    if (!c) return BTE_ERR_INPUT;
+    if (ngroups < 0 || ngroups > 4096) {
+        c->err = "ngroups must be in [0, 4096]";
+        return BTE_ERR_INPUT;
+    }
+    c->ngroups = ngroups;
+    c->group_valid = false;
+    return BTE_OK;
+}
+
+bte_status bte_get_group_result(bte_ctx* c, int32_t group, bte_rta_result* out) {
+    if (!c || !out) return BTE_ERR_INPUT;
+    if (!c->group_valid) {
+        c->err = "no run with replica groups since the last bte_set_groups";
+        return BTE_ERR_STATE;
+    }
+    if (group < 0 || group >= c->group_n) {
+        c->err = "group index out of range";
+        return BTE_ERR_INPUT;
+    }
+    try {
+        const std::size_t nk = std::size_t(c->group_nbx) * std::size_t(c->group_nbins);
+        const double* raw = c->group_raw.data() + std::size_t(group) * nk * 3;
+        const double G = double(c->group_n);
+        // the group holds 1/G of the run's particles: x G estimates the whole run
+        std::vector<double> gz(nk), jx(nk), jy(nk);
+        for (std::size_t k = 0; k < nk; ++k) {
+            gz[k] = raw[3 * k] * G;
+            jx[k] = raw[3 * k + 1] * G;
+            jy[k] = raw[3 * k + 2] * G;
+        }
+        out->nboxes = c->group_nbx;
+        out->nbins = c->group_nbins;
+        out->Eeff = c->group_Eeff;
+        out->energy_rate = c->gens.total_energy;
+        out->events = out->wall_hits = out->crossings = out->absorbed = 0;
+        out->specular_hits = out->tally_updates = out->translations = 0;
+        out->kernel_ms = 0.;
+        if (out->gz) std::copy(gz.begin(), gz.end(), out->gz);
+        if (out->gz_jx) std::copy(jx.begin(), jx.end(), out->gz_jx);
+        if (out->gz_jy) std::copy(jy.begin(), jy.end(), out->gz_jy);
+        bte::rta_post(c, &c->group_params, c->group_nbx, c->group_nbins, c->group_Eeff, c->group_step,
+                      std::move(gz), std::move(jx), std::move(jy), out);
+        return BTE_OK;
+    } catch (const std::exception& e) {
+        c->err = e.what();
+        return BTE_ERR_INPUT;
+    }
+}
+
 bte_status bte_query_sizes(const bte_ctx* c, const bte_rta_params* p, int32_t* nboxes,
                            int32_t* nbins, int64_t* nmodes) {
     if (!c || !p) return BTE_ERR_INPUT;
@@ -633,7 +764,12 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         const int nbx = int(g.boxes.size());
         const std::size_t nk = std::size_t(nbx) * std::size_t(nbins);
         const bool replay = p->mode == BTE_MODE_REPLAY;
-        const std::size_t tally_bytes = replay ? nk * 6 * sizeof(unsigned long long) : nk * 3 * sizeof(double);
+        c->group_valid = false;
+        if (c->ngroups > 1 && (replay || !g.rect_grid))
+            throw Error(BTE_ERR_INPUT, "replica groups need production mode on boxes that tile a grid");
+        const int ngroups = c->ngroups > 1 ? c->ngroups : 1;
+        const std::size_t tally_bytes =
+            replay ? nk * 6 * sizeof(unsigned long long) : nk * 3 * sizeof(double) * std::size_t(ngroups);
         c->d_tally.alloc(tally_bytes);
         c->d_counters.alloc(16 * sizeof(unsigned long long));
         c->d_err.alloc(4 * sizeof(int));
@@ -703,6 +839,8 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         T.pbegin = pbeg;
         T.pend = pend;
         T.nbins = nbins;
+        T.ngroups = ngroups;
+        T.group_stride = (long long)(nk * 3);
         // spectral decomposition: per-mode time at the selected boxes
         const std::size_t nloc = c->spec_boxes.size();
         const std::size_t spec_vals = nloc * std::size_t(nbins) * m.n();
@@ -762,7 +900,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
             hex.resize(nk * 6);
             ck(cudaMemcpyAsync(hex.data(), c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
         } else {
-            htal.resize(nk * 3);
+            htal.resize(nk * 3 * std::size_t(ngroups));
             ck(cudaMemcpyAsync(htal.data(), c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
         }
         ck(cudaMemcpyAsync(hc.data(), counters, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream), "d2h");
@@ -803,6 +941,21 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
                                                       : "geometry error");
             throw Error(bte_status(herr[0]), msg);
         }
+        if (ngroups > 1) {
+            // keep the groups; the run's outputs are their sum, in group order
+            c->group_raw = htal;
+            std::vector<double> sum(nk * 3, 0.);
+            for (int gi = 0; gi < ngroups; ++gi)
+                for (std::size_t k = 0; k < nk * 3; ++k) sum[k] += htal[std::size_t(gi) * nk * 3 + k];
+            htal.swap(sum);
+            c->group_n = ngroups;
+            c->group_nbx = nbx;
+            c->group_nbins = nbins;
+            c->group_Eeff = Eeff;
+            c->group_step = step;
+            c->group_params = *p;
+            c->group_valid = true;
+        }
         // raw tallies
         std::vector<double> gz(nk), jx(nk), jy(nk);
         if (replay) {
@@ -837,66 +990,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         if (out->gz) std::copy(gz.begin(), gz.end(), out->gz);
         if (out->gz_jx) std::copy(jx.begin(), jx.end(), out->gz_jx);
         if (out->gz_jy) std::copy(jy.begin(), jy.end(), out->gz_jy);
-        // post-processing, src/RTA_MC2D.cpp:2336-2435
-        for (int ir = 0; ir < nbx; ++ir) {
-            const double vbox = g.boxes[std::size_t(ir)].area * g.thickness;
-            for (int i = 0; i < nbins; ++i) {
-                const std::size_t k = std::size_t(ir) * nbins + i;
-                gz[k] /= vbox;
-                jx[k] /= vbox;
-                jy[k] /= vbox;
-            }
-        }
-        if (!c->mat_share.empty() && p->source == BTE_SOURCE_WALLS) {
-            // Eeff_m = E_m / (share_m N) per material
-            for (int ir = 0; ir < nbx; ++ir) {
-                const std::size_t k = std::size_t(g.mat[std::size_t(ir)]);
-                const double Em = c->mat_share[k] > 0. ? c->mat_energy[k] / (c->mat_share[k] * double(p->nparticles)) : 0.;
-                for (int i = 0; i < nbins; ++i) {
-                    const std::size_t q = std::size_t(ir) * nbins + i;
-                    gz[q] *= Em;
-                    jx[q] *= Em * 1e12 * 1e9 * 1e9;
-                    jy[q] *= Em * 1e12 * 1e9 * 1e9;
-                }
-            }
-        } else {
-            for (auto& x : gz) x *= Eeff;
-            for (auto& x : jx) x *= Eeff * 1e12 * 1e9 * 1e9;
-            for (auto& x : jy) x *= Eeff * 1e12 * 1e9 * 1e9;
-        }
-        if (p->source == BTE_SOURCE_WALLS) {
-            // step response: integrate in time
-            for (int ir = 0; ir < nbx; ++ir)
-                for (int i = 1; i < nbins; ++i) {
-                    const std::size_t k = std::size_t(ir) * nbins + i;
-                    gz[k] += gz[k - 1];
-                    jx[k] += jx[k - 1];
-                    jy[k] += jy[k - 1];
-                }
-        } else {
-            // relaxation of an initial deviation: bin averages
-            for (std::size_t k = 0; k < nk; ++k) {
-                gz[k] /= step;
-                jx[k] /= step;
-                jy[k] /= step;
-            }
-        }
-        const double vcorr = g.thickness / m.c;
-        if (out->temperature) {
-            std::vector<double> cvm(std::size_t(std::max(c->nmat, 1)));
-            for (std::size_t k = 0; k < cvm.size(); ++k)
-                cvm[k] = bte::calc_cv(m, c->nmat > 0 ? c->mat_T0[k] : p->T0);
-            for (int ir = 0; ir < nbx; ++ir) {
-                const double cv = cvm[std::size_t(c->nmat > 0 ? g.mat[std::size_t(ir)] : 0)];
-                const double T0b = bte::box_T0(c, ir, p->T0);
-                for (int i = 0; i < nbins; ++i) {
-                    const std::size_t k = std::size_t(ir) * nbins + i;
-                    out->temperature[k] = gz[k] / (cv / vcorr) + T0b;
-                }
-            }
-        }
-        if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
-        if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
+        bte::rta_post(c, p, nbx, nbins, Eeff, step, std::move(gz), std::move(jx), std::move(jy), out);
         return BTE_OK;
     } catch (const Error& e) {
         return fail(c, e);

@@ -107,6 +107,14 @@ struct bte_ctx {
     int spec_nbins = 0;
     double spec_Eeff = 0., spec_T0 = 0.;
     bool spec_valid = false;
+    // replica groups (bte_set_groups): the last grid-kernel run's raw
+    // tallies per group, [group][box][bin][3], with what their outputs need
+    int ngroups = 0;
+    bool group_valid = false;
+    int group_n = 0, group_nbx = 0, group_nbins = 0;
+    double group_Eeff = 0., group_step = 0.;
+    bte_rta_params group_params{};
+    std::vector<double> group_raw;
     // run buffers
     bte::DBuf d_time, d_tally, d_counters, d_err, d_work;
     std::vector<double> h_time;

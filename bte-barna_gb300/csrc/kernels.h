@@ -19,7 +19,7 @@ struct ProdTuning {
     int block_threads;
     int blocks_per_sm;
     int smem_tally;
-    int smem_alias;
+    int particles_per_thread;  // 1 or 2 (the interleaved grid kernel)
 };
 
 void launch_replay(const DevTables& T, unsigned long long* ex, unsigned long long* counters,

@@ -86,6 +86,11 @@ struct DevTables {
     double* spec;
     unsigned long long* spec_ex;
     unsigned long long* spec_cnt;  // steady state: signed segments per [loc][mode]
+    // replica groups of the grid kernel: particle p tallies into group
+    // p mod ngroups, group_stride doubles after the previous group (ngroups
+    // <= 1: one tally)
+    int ngroups;
+    long long group_stride;
 };
 
 struct Counters {

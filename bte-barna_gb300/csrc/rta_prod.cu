@@ -507,6 +507,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
     const double* binw = T.timegrid + T.ntime;
     double dt = 0., rb = 0.;
     long long pid = -1, nev = 0;
+    double* tgrp = tally;  // the tally of the particle's replica group
     uint32_t npass = 0;
     int bin = 0;
     unsigned long long signbit = 0;
@@ -556,7 +557,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             record_error(err, ob(dt) > 0 ? E_LIMIT : E_VALUE, pid);
             active = false;
             done = true;
-            pd.flush(tally, signbit, rb, p.x, p.y);
+            pd.flush(tgrp, signbit, rb, p.x, p.y);
             return false;
         }
         return true;
@@ -573,6 +574,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                 const long long mine = (long long)base + __popc(idle & ((1u << lane) - 1u));
                 if (mine < total) {
                     pid = T.pbegin + mine;
+                    tgrp = T.ngroups > 1 ? tally + (long long)(pid % T.ngroups) * T.group_stride : tally;
                     g.init(T.seed, (uint64_t)pid);
                     int e = grid_generate(T, A.G, A.boxcell, g, pid, p);
                     if (CHECK && !e &&
@@ -685,7 +687,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             continue;
         }
         if (move || absorbed || bin_end) {
-            double* b = tally + 3ll * pd.key;
+            double* b = tgrp + 3ll * pd.key;
             atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(d0) ^ signbit));
             atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(d1) ^ signbit));
             atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(d2) ^ signbit));
@@ -729,7 +731,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                         record_error(err, E_GEOM, pid);
                         active = false;
                         done = true;
-                        pd.flush(tally, signbit, rb, p.x, p.y);
+                        pd.flush(tgrp, signbit, rb, p.x, p.y);
                         continue;
                     }
                     if (CHECK && cls >= T.nclass) {
@@ -757,7 +759,7 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
                             record_error(err, E_GEOM, pid);
                             active = false;
                             done = true;
-                            pd.flush(tally, signbit, rb, p.x, p.y);
+                            pd.flush(tgrp, signbit, rb, p.x, p.y);
                             continue;
                         }
                         const int4 e = __ldg(T.lalias + a + int(mulhi32(rr.y, uint32_t(len))));
@@ -801,6 +803,282 @@ __global__ void __launch_bounds__(256, MINB) rta_prod_grid(DevTables T, GridArgs
             if (x != 0.) atomicAdd(gtally + k, x);
         }
     }
+}
+
+// ------------------------------------------------ grid path, PPT per thread
+
+// One particle slot of the interleaved grid kernel.
+struct GridSlot {
+    GridParticle p;
+    Pending pd;
+    Philox g;
+    ModeVel mv;
+    double* tb;  // the tally of the particle's replica group
+    double dt, rb;
+    long long pid, nev;
+    uint32_t npass;
+    int bin;
+    unsigned long long signbit;
+    bool active, done;
+};
+
+// The segment one slot takes in one pass.
+struct GridSeg {
+    uint4 rr;
+    double r1, nx, ny, dt, d0, d1, d2;
+    int ni, nj, wside;
+    bool xfirst, flight_end, wall, bin_end;
+};
+
+// The plain production grid kernel (global tally, no spectral locations)
+// with PPT particles per thread.  It follows rta_prod_grid's loop (same
+// draws, same segments, same tallies) but splits every pass in two phases:
+// first the segment of each slot, a straight-line FP64 sequence computed for
+// every slot (a slot without a particle computes on its last state, whose
+// indices stay in range, and drops the result), so that the FP64 chains of
+// the PPT particles interleave and hide each other's latency; then, slot
+// by slot, the branchy end of the segment (tally flush, crossing, wall or
+// scattering redraw).  Each slot refills from the global particle counter
+// on its own ballot.
+template <int PPT, int MINB>
+__global__ void __launch_bounds__(256, MINB) rta_prod_grid_ilp(DevTables T, GridArgs A, double* tally,
+                                                         unsigned long long* counters, int* err,
+                                                         unsigned long long* work) {
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int lane = threadIdx.x & 31;
+    const long long total = T.pend - T.pbegin;
+    const int last_bin = T.nbins - 1;
+    const unsigned long long spec_thr =
+        T.specularity >= 1.0 ? (1ull << 32)
+                             : (T.specularity > 0. ? (unsigned long long)(T.specularity * 4294967296.0) : 0ull);
+    const double* binw = T.timegrid + T.ntime;
+    GridSlot S[PPT];
+#pragma unroll
+    for (int s = 0; s < PPT; ++s) {
+        GridSlot& L = S[s];
+        L.pd.key = -1;
+        L.pd.flushes = 0;
+        L.pd.r0 = L.pd.x0 = L.pd.y0 = 0.;
+        L.p.i = L.p.j = L.p.mode = L.p.box = L.p.mo = 0;
+        L.p.sign = 1;
+        L.p.x = L.p.y = L.p.t = 0.;
+        L.g.init(0, 0);
+        L.mv = ModeVel{0., 0., 0., 0.};
+        L.dt = L.rb = 0.;
+        L.pid = -1;
+        L.tb = tally;
+        L.nev = 0;
+        L.npass = 0;
+        L.bin = 0;
+        L.signbit = 0;
+        L.active = L.done = false;
+    }
+    // a new free flight of the slot's current mode from one random word (as
+    // rta_prod_grid's new_flight); false when the particle stops with an error
+    auto new_flight = [&](GridSlot& L, uint32_t word) -> bool {
+        const int k = L.p.mode;
+        L.mv = A.mv[k];
+        const float ef = -logf((float(word >> 9) + 0.5f) * 0x1p-23f);
+        L.dt = widen_pos(ef) * __ldg(T.tau + L.p.mo + k);
+        c.events++;
+        if (ob(L.dt) <= 0 || ++L.nev > T.flight_cap) {
+            record_error(err, ob(L.dt) > 0 ? E_LIMIT : E_VALUE, L.pid);
+            L.active = false;
+            L.done = true;
+            L.pd.flush(L.tb, L.signbit, L.rb, L.p.x, L.p.y);
+            return false;
+        }
+        return true;
+    };
+    // the branchy end of one slot's segment
+    auto finish = [&](GridSlot& L, const GridSeg& G) {
+        L.dt = G.dt;
+        L.rb = G.r1;
+        L.p.x = G.nx;
+        L.p.y = G.ny;
+        int nb = L.p.box;
+        if (G.wall) nb = grid_cell(A.G, G.ni, G.nj);
+        const bool move = G.wall && nb >= 0;
+        const bool absorbed = G.wall && nb <= -2;
+        const bool reflect = G.wall && nb == -1;
+        const bool last = G.bin_end && L.bin == last_bin;
+        if (move || absorbed || G.bin_end) {
+            double* b = L.tb + 3ll * L.pd.key;
+            atomicAdd(b + 0, __longlong_as_double(__double_as_longlong(G.d0) ^ L.signbit));
+            atomicAdd(b + 1, __longlong_as_double(__double_as_longlong(G.d1) ^ L.signbit));
+            atomicAdd(b + 2, __longlong_as_double(__double_as_longlong(G.d2) ^ L.signbit));
+            L.pd.flushes++;
+            L.pd.key = -1;
+        }
+        if (absorbed || last) {
+            if (absorbed) c.absorbed++;
+            L.active = false;
+            return;
+        }
+        if (G.bin_end) {
+            ++L.bin;
+            L.rb = __ldg(binw + L.bin);
+        }
+        if (move) {
+            L.p.i = G.ni;
+            L.p.j = G.nj;
+            L.p.box = nb;
+            c.crossings++;
+        }
+        if (move || G.bin_end) L.pd.start(L.p.box * T.nbins + L.bin, L.rb, G.nx, G.ny);
+        if (reflect || G.flight_end) {
+            const int k = L.p.mode;
+            int nm = k;
+            if (reflect || !T.ballistic) {
+                float pr = 0.f;
+                int keep = k, alt = k;
+                if (reflect) {
+                    const int cls = G.wside == 0   ? A.cls[0]
+                                    : G.wside == 1 ? A.cls[1]
+                                    : G.wside == 2 ? A.cls[2]
+                                                   : A.cls[3];
+                    if (cls < 0) {
+                        record_error(err, E_GEOM, L.pid);
+                        L.active = false;
+                        L.done = true;
+                        L.pd.flush(L.tb, L.signbit, L.rb, L.p.x, L.p.y);
+                        return;
+                    }
+                    int mirror_mode = -1;
+                    if (spec_thr && (unsigned long long)G.rr.w < spec_thr && T.mirror)
+                        mirror_mode = __ldg(T.mirror + (long long)cls * T.n + k);
+                    if (mirror_mode >= 0) {
+                        c.specular++;
+                        pr = 2.f;
+                        keep = mirror_mode;
+                    } else {
+                        const long long a = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k);
+                        const long long bb = __ldg(T.row_ptr + (long long)cls * (T.n + 1) + k + 1);
+                        const int len = int(bb - a);
+                        if (len <= 0) {
+                            record_error(err, E_GEOM, L.pid);
+                            L.active = false;
+                            L.done = true;
+                            L.pd.flush(L.tb, L.signbit, L.rb, L.p.x, L.p.y);
+                            return;
+                        }
+                        const int4 e = __ldg(T.lalias + a + int(mulhi32(G.rr.y, uint32_t(len))));
+                        pr = __int_as_float(e.x);
+                        keep = e.y;
+                        alt = e.z;
+                    }
+                    c.wall_hits++;
+                } else {
+                    const int j = int(mulhi32(G.rr.y, uint32_t(T.n)));
+                    pr = __ldg(T.resample_prob + L.p.mo + j);
+                    keep = j;
+                    alt = __ldg(T.resample_alt + L.p.mo + j);
+                }
+                const float acc = float(G.rr.z >> 8) * 0x1p-24f;
+                nm = acc < pr ? keep : alt;
+            }
+            L.p.mode = nm;
+            new_flight(L, G.rr.x);
+        }
+    };
+    for (;;) {
+#pragma unroll
+        for (int s = 0; s < PPT; ++s) {
+            GridSlot& L = S[s];
+            const unsigned idle = __ballot_sync(0xffffffffu, !L.active && !L.done);
+            if (idle) {
+                unsigned long long base = 0;
+                const int leader = __ffs(idle) - 1;
+                if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (!L.active && !L.done) {
+                    const long long mine = (long long)base + __popc(idle & ((1u << lane) - 1u));
+                    if (mine < total) {
+                        L.pid = T.pbegin + mine;
+                        L.tb = T.ngroups > 1 ? tally + (long long)(L.pid % T.ngroups) * T.group_stride : tally;
+                        L.g.init(T.seed, (uint64_t)L.pid);
+                        const int e = grid_generate(T, A.G, A.boxcell, L.g, L.pid, L.p);
+                        if (e) {
+                            record_error(err, e, L.pid);
+                            L.done = true;
+                        } else {
+                            L.active = true;
+                            L.nev = 0;
+                            L.npass = 0;
+                            L.bin = 0;
+                            L.rb = __ldg(binw);
+                            L.signbit = L.p.sign < 0 ? 0x8000000000000000ull : 0ull;
+                            L.pd.start(L.p.box * T.nbins, L.rb, L.p.x, L.p.y);
+                            new_flight(L, L.g.next32());
+                        }
+                    } else {
+                        L.done = true;
+                    }
+                }
+            }
+        }
+        bool finished = true;
+#pragma unroll
+        for (int s = 0; s < PPT; ++s) finished = finished && S[s].done;
+        if (__all_sync(0xffffffffu, finished)) break;
+        // phase 1: every slot's segment, straight-line
+        GridSeg G[PPT];
+#pragma unroll
+        for (int s = 0; s < PPT; ++s) {
+            GridSlot& L = S[s];
+            GridSeg& q = G[s];
+            q.rr = pass_block(L.npass, (uint64_t)L.pid, T.seed);
+            L.npass += L.active ? 1u : 0u;
+            const int upx = ob(L.mv.vx) >= 0 ? 1 : 0;
+            const int upy = ob(L.mv.vy) >= 0 ? 1 : 0;
+            const double xw = __ldg(A.G.gx + L.p.i + upx);
+            const double yw = __ldg(A.G.gy + L.p.j + upy);
+            const double tx = (xw - L.p.x) * L.mv.ivx;
+            const double ty = (yw - L.p.y) * L.mv.ivy;
+            q.xfirst = ob(tx) <= ob(ty);
+            long long te_b = q.xfirst ? ob(tx) : ob(ty);
+            long long tb_b = ob(L.rb);
+            te_b = te_b > 0 ? te_b : 0;
+            tb_b = tb_b > 0 ? tb_b : 0;
+            const long long dt_b = ob(L.dt);
+            const long long lim_b = te_b < tb_b ? te_b : tb_b;
+            q.flight_end = !(dt_b > lim_b);
+            const long long seg_b = q.flight_end ? dt_b : lim_b;
+            q.wall = !q.flight_end && te_b <= tb_b;
+            q.bin_end = tb_b <= seg_b;
+            const double seg = obd(seg_b);
+            q.r1 = q.bin_end ? 0. : L.rb - seg;
+            q.nx = fma(seg, L.mv.vx, L.p.x);
+            q.ny = fma(seg, L.mv.vy, L.p.y);
+            q.dt = L.dt - seg;
+            q.ni = L.p.i;
+            q.nj = L.p.j;
+            q.wside = 0;
+            if (q.wall) {
+                if (q.xfirst) {
+                    q.nx = xw;
+                    q.ni = L.p.i + (upx ? 1 : -1);
+                    q.wside = upx ? 0 : 1;
+                } else {
+                    q.ny = yw;
+                    q.nj = L.p.j + (upy ? 1 : -1);
+                    q.wside = upy ? 2 : 3;
+                }
+            }
+            q.d0 = L.pd.r0 - q.r1;
+            q.d1 = q.nx - L.pd.x0;
+            q.d2 = q.ny - L.pd.y0;
+        }
+        // phase 2: the ends of the segments, slot by slot
+#pragma unroll
+        for (int s = 0; s < PPT; ++s)
+            if (S[s].active) finish(S[s], G[s]);
+    }
+    unsigned flushes = 0;
+#pragma unroll
+    for (int s = 0; s < PPT; ++s) flushes += S[s].pd.flushes;
+    c.tallies = flushes;
+    flush_counters_p<8>(c, counters);
 }
 
 // ------------------------------------------------------------ polygon path
@@ -1271,7 +1549,7 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
     if (threads > 256 || threads % 32) return false;
     const size_t smem = size_t(3) * T.nboxes * T.nbins * sizeof(double);
     // the adjoint passes run with the tally in global memory
-    const bool use_smem = tune.smem_tally != 0 && smem <= 200 * 1024 && adj_pass == 0;
+    const bool use_smem = tune.smem_tally != 0 && smem <= 200 * 1024 && adj_pass == 0 && T.ngroups <= 1;
     // residency variants: 4 blocks of 256 threads per SM (64 registers, a
     // few spills), 3 (80 registers) or 2 (no register cap); the
     // shared-memory tally allows one block per SM
@@ -1286,6 +1564,26 @@ bool launch_prod_grid(const DevTables& T, const GridArgs& A, double* tally,
         const long long need = (n + 255) / 256;
         if (blocks > need) blocks = need;
         rta_prod_grid<false, 2, 0, true><<<unsigned(blocks), 256, 0, s>>>(T, A, tally, counters, err, work, aa);
+        return true;
+    }
+    if (tune.particles_per_thread == 2 && adj_pass == 0 && !use_smem && !T.spec_loc) {
+        // two particles per thread: the register cap follows the resident
+        // threads (152 registers up to 384 threads per SM, 128 above)
+        const bool capped = threads * bps > 384;
+        const void* f2 = capped ? reinterpret_cast<const void*>(rta_prod_grid_ilp<2, 2>)
+                                : reinterpret_cast<const void*>(rta_prod_grid_ilp<2, 1>);
+        int maxb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, f2, threads, 0);
+        if (maxb < 1) return false;
+        const int b2 = bps > maxb ? maxb : bps;
+        long long blocks = (long long)nsm * b2;
+        const long long need = (n + 2ll * threads - 1) / (2ll * threads);
+        if (blocks > need) blocks = need;
+        if (blocks < 1) blocks = 1;
+        if (capped)
+            rta_prod_grid_ilp<2, 2><<<unsigned(blocks), threads, 0, s>>>(T, A, tally, counters, err, work);
+        else
+            rta_prod_grid_ilp<2, 1><<<unsigned(blocks), threads, 0, s>>>(T, A, tally, counters, err, work);
         return true;
     }
     const void* fn;

@@ -278,9 +278,10 @@ typedef struct bte_tuning {
     int32_t block_threads;   /* threads per block                              */
     int32_t blocks_per_sm;   /* resident blocks per SM of the persistent grid  */
     int32_t smem_tally;      /* 1: privatise tallies in shared memory           */
-    int32_t smem_alias;      /* reserved, ignored: the alias tables are read
-                                through the read-only path and stay in L2 (the
-                                C1 table, 36864 modes, exceeds shared memory)  */
+    int32_t particles_per_thread; /* particles each thread carries at once in
+                                the grid kernel: 1, or 2 for the interleaved
+                                variant (plain production runs with a global
+                                tally and no spectral locations; others use 1) */
 } bte_tuning;
 
 /* ------------------------------------------------------------------------ */
@@ -425,6 +426,23 @@ typedef struct bte_spectral_result {
 } bte_spectral_result;
 
 bte_status bte_get_spectral(bte_ctx* ctx, bte_spectral_result* out);
+
+/* Replica groups of the following production runs on boxes that tile a
+ * grid: particle p tallies into group p mod ngroups, so one run gives
+ * ngroups independent estimates of every output (batch means inside one
+ * launch); the run's own outputs are the sums over the groups.  The
+ * reference estimates errors from independent runs (nruns,
+ * src/RTA_MC2D.cpp:2099-2101, :2188); a group is one such run made with
+ * 1/ngroups of the particles.  ngroups = 0 or 1 switches it off; a replay
+ * run or a geometry off a grid fails with BTE_ERR_INPUT while it is on. */
+bte_status bte_set_groups(bte_ctx* ctx, int32_t ngroups);
+
+/* Outputs of group `group` of the last run with replica groups, scaled to
+ * estimate the whole run (the group's tallies x ngroups, then the run's
+ * post-processing): gz, gz_jx, gz_jy, temperature, jx, jy as in
+ * bte_rta_result (exact, counters and kernel_ms are not kept per group and
+ * come back as 0).  Valid until the next run, load or bte_set_groups. */
+bte_status bte_get_group_result(bte_ctx* ctx, int32_t group, bte_rta_result* out);
 
 /* Largest number of time bins bte_rta_run_noalloc accepts. */
 #define BTE_NOALLOC_MAX_BINS 4096

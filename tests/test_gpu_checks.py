@@ -7,7 +7,11 @@
   no check may fire on the benchmark-shaped cases;
 - a small flight cap per particle (a host-side parameter) sends every
   kernel down its limit path: the run returns BTE_ERR_LIMIT and the context
-  stays usable."""
+  stays usable;
+- the grid kernel with two particles per thread draws the same streams and
+  runs the same FP64 sequence per particle as the one-per-thread kernel, so
+  it repeats its integer counters exactly and its tallies to FP64
+  atomic-order rounding."""
 import numpy as np
 import pytest
 
@@ -62,3 +66,29 @@ def test_flight_cap_injects_the_limit_path(engine):
         engine.rta_run(300.0, 10.0, 200.0, 2000, seed=3, flight_cap=2)
     assert ex.value.code == btegpu.BTE_ERR_LIMIT
     assert engine.rta_run(300.0, 10.0, 200.0, 2000, seed=3)["events"] > 0
+
+
+@pytest.mark.parametrize("which", ["benchmark_slice", "ribbon"])
+@pytest.mark.parametrize("shape", [(256, 1), (128, 4)])
+def test_two_particles_per_thread_repeat_one_per_thread(engine, which, shape):
+    if which == "benchmark_slice":
+        c = synth.config1()
+        kw = dict(source=btegpu.SOURCE_INITIAL, specularity=0.3, begin=3_000_000, end=3_200_000)
+    else:
+        c, kw = synth.config0(n_particles=200000), dict(source=btegpu.SOURCE_WALLS)
+    engine.load_modes(c["modes"])
+    engine.load_geometry(c["geom"])
+    args = dict(T0=c["T0"], dt=c["dt"], maxtime=c["maxtime"], N=c["N"], seed=23, **kw)
+    try:
+        engine.set_tuning(block_threads=256, blocks_per_sm=3, smem_tally=0, particles_per_thread=1)
+        one = engine.rta_run(**args)
+        engine.set_tuning(block_threads=shape[0], blocks_per_sm=shape[1], smem_tally=0, particles_per_thread=2)
+        two = engine.rta_run(**args)
+    finally:  # back to the context's defaults
+        engine.set_tuning(block_threads=0, blocks_per_sm=0, smem_tally=0, particles_per_thread=0)
+    assert one["events"] > 0
+    for k in KEYS:
+        assert one[k] == two[k], k
+    for k in ("gz", "gz_jx", "gz_jy"):
+        scale = np.abs(one[k]).max()
+        assert np.abs(two[k] - one[k]).max() <= 1e-9 * scale, k

@@ -93,3 +93,42 @@ def test_share_update_and_geometry_reload(engine):
     b = e.rta_run(300.0, 10.0, 100.0, 1500, seed=4, mode=btegpu.MODE_REPLAY, exact=True)
     e.close()
     assert np.array_equal(a["exact"], b["exact"])
+
+
+def test_replica_groups_sum_to_the_run_and_estimate_it(engine):
+    """bte_set_groups: particle p tallies into group p mod G.  The run's
+    outputs are the groups' sum, so a grouped run repeats the plain run
+    (same particles, same counters, tallies to atomic-order rounding), the
+    mean of the group results (each scaled to the whole run) is the run's
+    result, and the spread of the groups is the batch-means error: it
+    agrees with the spread of independent plain runs."""
+    c = synth.config0(n_particles=400000)
+    engine.load_modes(c["modes"])
+    engine.load_geometry(c["geom"])
+    args = dict(T0=c["T0"], dt=c["dt"], maxtime=c["maxtime"], N=c["N"])
+    plain = engine.rta_run(seed=41, **args)
+    G = 8
+    engine.set_groups(G)
+    try:
+        grouped = engine.rta_run(seed=41, **args)
+        shape = grouped["jx"].shape
+        groups = [engine.group_result(g, shape, raw=True) for g in range(G)]
+    finally:
+        engine.set_groups(0)
+    for k in ("events", "wall_hits", "crossings", "absorbed", "tally_updates"):
+        assert grouped[k] == plain[k], k
+    for k in ("gz", "gz_jx", "gz_jy", "jx"):
+        scale = np.abs(plain[k]).max()
+        assert np.abs(grouped[k] - plain[k]).max() <= 1e-9 * scale, k
+        mean = np.mean([g[k] for g in groups], axis=0)
+        assert np.abs(mean - grouped[k]).max() <= 1e-9 * scale, k
+    ncell = int(c["geom"]["nboxes"]) - 2
+    kap = lambda r: synth.sweep_kappa(r["jx"], slice(0, ncell), length=1000.0)
+    kg = np.array([kap(g) for g in groups])
+    assert abs(kg.mean() - kap(grouped)) <= 1e-9 * abs(kap(grouped))
+    # the groups' spread estimates the error of one run of N/G particles;
+    # independent runs of N/G particles give the same spread
+    runs = np.array([kap(engine.rta_run(seed=500 + i, **{**args, "N": c["N"] // G})) for i in range(G)])
+    ratio = kg.var(ddof=1) / runs.var(ddof=1)
+    assert 1 / 9.0 < ratio < 9.0, (kg.std(ddof=1), runs.std(ddof=1))  # F(7, 7): about 1 % two-sided
+    assert abs(kg.mean() - runs.mean()) < 4.5 * np.sqrt(kg.var(ddof=1) / G + runs.var(ddof=1) / G)
