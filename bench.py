@@ -345,7 +345,7 @@ def kappa_agreement(kap_b, rel_b, sp):
     return float(max(zs)) if zs else None
 
 
-def sweep_arms(local, tol, cap):
+def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
     """The batched sweep: 64 ribbons (16 widths 20 nm - 2 um x 4 temperatures,
     1 um long, p = 0, reservoirs at T +- 1 K) with budgets N_w = 1e5 100^(k/15).
     Each arm runs until every case's kappa_eff has 3 sigma / kappa <= tol.
@@ -355,7 +355,7 @@ def sweep_arms(local, tol, cap):
     geometry, one material per case); each launch deals its particles to 8
     replica groups, so batch means exist after one launch, and each round
     gives each case, through its particle share, what its measured variance
-    still asks for (a quarter budget in the first round); converged cases
+    still asks for (a fraction of a budget in the first round); converged cases
     drop out.  Table construction is outside both clocks.  Returns the line."""
     import torch
     import btegpu
@@ -373,7 +373,7 @@ def sweep_arms(local, tol, cap):
     # launch deals its particles to G replica groups (batch means inside
     # the launch) and each round gives each case the particles its measured
     # variance still asks for
-    G = 8
+    G = groups
     g = synth.sweep_union_geometry(cases, length=L, ncells=ncells)
     eng = btegpu.Engine(local)
     eng.load_modes(tabs[300.0])
@@ -386,7 +386,7 @@ def sweep_arms(local, tol, cap):
     per = ncells + 2
     active = np.ones(nc, dtype=bool)
     nmin = 2000.0 * G
-    need = np.maximum(budgets / 4.0, nmin)                     # first round: a quarter budget
+    need = np.maximum(budgets * first_frac, nmin)              # first round: a fraction of a budget
     w_sum = np.zeros(nc)                                       # particles so far per case
     wk_sum = np.zeros(nc)                                      # particle-weighted kappa sum
     rounds_i = [[] for _ in range(nc)]                         # (particles, variance of the round mean)
@@ -395,17 +395,26 @@ def sweep_arms(local, tol, cap):
     ev_b = 0
     reps_b = 0
     parts_b = 0
+    round_log = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     while active.any() and time.perf_counter() - t0 < cap:
         alloc = np.where(active, np.maximum(need, nmin), 0.0)
         N = int(alloc.sum())
+        ta = time.perf_counter()
         eng.load_materials(rates, Ts, alloc / alloc.sum())
+        tb = time.perf_counter()
         r = eng.rta_run(300.0, dt, maxtime, N, seed=1000 + reps_b, raw=False)
-        grs = [eng.group_result(k, r["jx"].shape) for k in range(G)]
+        tc = time.perf_counter()
+        grs = [eng.group_result(k, r["jx"].shape, keys=("jx",)) for k in range(G)]
+        td = time.perf_counter()
         ev_b += int(r["events"])
         reps_b += 1
         parts_b += N
+        # active cases, particles, kernel ms, and host ms of the share
+        # update, the run call and the group results
+        round_log.append([int(active.sum()), N, round(float(r["kernel_ms"]), 2), round(1e3 * (tb - ta), 1),
+                          round(1e3 * (tc - tb), 1), round(1e3 * (td - tc), 1)])
         for i in np.flatnonzero(active):
             sl = slice(per * i, per * i + ncells)
             kg = np.array([synth.sweep_kappa(x["jx"], sl, length=L) for x in grs])
@@ -423,25 +432,31 @@ def sweep_arms(local, tol, cap):
             # particles still needed for 3 sigma / kappa <= tol
             s2 = np.mean([v * n for n, v in rounds_i[i]])
             total = 9.0 * s2 / (tol * kap_b[i]) ** 2
-            need[i] = max(1.1 * (total - w_sum[i]), nmin)
+            # a round costs host work whatever its size, so a case is topped
+            # up with margin, and by at least a quarter of what it has used
+            # (its estimate may say it is nearly there while it is not)
+            need[i] = max(1.3 * (total - w_sum[i]), 0.25 * w_sum[i], nmin)
     t_b = time.perf_counter() - t0
     conv_b = int((~active).sum())
     eng.set_groups(0)
     eng.close()
 
-    # ---- plain
-    engs = {}
-    for T in temps:
-        e = btegpu.Engine(local)
-        e.load_modes(tabs[T])
-        engs[T] = e
     sp = SweepStats(nc)
     t_p = 0.0
     ev_p = 0
     reps_p = 0
     parts_p = 0
     conv_p = 0
-    for i, cs in enumerate(cases):
+    t_f = 0.0
+    conv_f = 0
+    cases_iter = list(enumerate(cases)) if plain else []
+    # ---- plain
+    engs = {}
+    for T in (temps if plain else []):
+        e = btegpu.Engine(local)
+        e.load_modes(tabs[T])
+        engs[T] = e
+    for i, cs in cases_iter:
         e = engs[cs["T"]]
         e.load_geometry(synth.sweep_ribbon(cs["width"], cs["T"], length=L, ncells=ncells))
         e.rta_run(cs["T"], dt, maxtime, 1000, seed=2)         # tables for this geometry
@@ -468,8 +483,7 @@ def sweep_arms(local, tol, cap):
     # process per case would)
     sf = SweepStats(nc)
     t2 = time.perf_counter()
-    conv_f = 0
-    for i, cs in enumerate(cases):
+    for i, cs in cases_iter:
         if time.perf_counter() - t2 >= cap:
             break
         e = btegpu.Engine(local)
@@ -484,7 +498,7 @@ def sweep_arms(local, tol, cap):
                 conv_f += 1
                 break
         e.close()
-    t_f = time.perf_counter() - t2
+    t_f = time.perf_counter() - t2 if plain else 0.0
     # ---- batched with its table construction on the clock
     t3 = time.perf_counter()
     eng = btegpu.Engine(local)
@@ -506,6 +520,7 @@ def sweep_arms(local, tol, cap):
                                "budgets 1e5*100^(k/15), 100 bins of 10 ps",
                    "tol_3sigma": tol, "time_cap_s": cap, "parallelism": "replicas x1"},
         "batched": {"seconds": t_b, "launches": reps_b, "replica_groups": G, "particles": parts_b,
+                    "first_round_fraction": first_frac, "rounds": round_log,
                     "cases_converged": conv_b, "events": ev_b,
                     "events_per_s": ev_b / max(t_b, 1e-9), "worst_3sigma_rel": worst_b},
         "plain": {"seconds": t_p, "launches": reps_p, "particles": parts_p, "cases_converged": conv_p,
@@ -553,7 +568,7 @@ def run_adjoint(args, rank, world, local):
     return 0
 
 
-def adjoint_arms(local, cap):
+def adjoint_arms(local, cap, replay_particles=1_000_000):
     """Gradient of kappa_eff of the plain ribbon at p = 0.2 (6144 modes,
     N = 1e7) with respect to 32 seeded mode lifetimes and p, to 1% (3 sigma,
     L2 over the 33 components): the adjoint against central differences
@@ -636,8 +651,8 @@ def adjoint_arms(local, cap):
     rows_fp, t_fp, runs_fp = fd_arm(btegpu.MODE_PRODUCTION, 1e-3, N)
     # replay-mode differences: CDF draws keep the two runs coupled; the
     # replay kernel is the bit-exact checker (pcg64, 128-bit tallies), slow,
-    # so it runs 1e6 particles per evaluation
-    rows_fr, t_fr, runs_fr = fd_arm(btegpu.MODE_REPLAY, 1e-3, N // 10)
+    # so it runs `replay_particles` per evaluation
+    rows_fr, t_fr, runs_fr = fd_arm(btegpu.MODE_REPLAY, 1e-3, replay_particles)
     clk = clocks.stop()
 
     def agree(rows):
@@ -669,7 +684,7 @@ def adjoint_arms(local, cap):
         "fd_production": {"seconds": t_fp, "replicas": len(rows_fp), "runs": runs_fp,
                           "accuracy": acc_fp, "max_z_vs_adjoint": agree(rows_fp),
                           "seconds_to_1pct_extrapolated": t1_fp},
-        "fd_replay": {"seconds": t_fr, "replicas": len(rows_fr), "runs": runs_fr, "particles_per_run": N // 10,
+        "fd_replay": {"seconds": t_fr, "replicas": len(rows_fr), "runs": runs_fr, "particles_per_run": replay_particles,
                       "accuracy": acc_fr, "max_z_vs_adjoint": agree(rows_fr),
                       "seconds_to_1pct_extrapolated": t1_fr},
         "speedup_over_fd": ({"production": (t1_fp / t1_a) if t1_fp else None,
@@ -693,13 +708,17 @@ def time_to_1pct(local, cap):
         out["sweep"] = {
             "workload": sw["config"]["workload"], "tol_3sigma": 0.01, "time_cap_s": cap,
             "batched_s": sw["batched"]["seconds"], "batched_cases_converged": sw["batched"]["cases_converged"],
+            "batched_launches": sw["batched"]["launches"], "batched_particles": sw["batched"]["particles"],
+            "replica_groups": sw["batched"]["replica_groups"],
             "plain_s": sw["plain"]["seconds"], "plain_cases_converged": sw["plain"]["cases_converged"],
+            "plain_launches": sw["plain"]["launches"], "plain_particles": sw["plain"]["particles"],
+            "kappa_batched_vs_plain_max_z": sw["kappa_batched_vs_plain_max_z"],
             "speedup_plain_over_batched": sw["speedup_plain_over_batched"],
             "with_table_setup": sw["with_table_setup"], "clocks": sw["clocks"]}
     except Exception as e:  # the summaries must not hide the headline line
         out["sweep"] = {"failed": str(e)}
     try:
-        ad = adjoint_arms(local, cap)
+        ad = adjoint_arms(local, cap, replay_particles=100_000)
         out["gradient"] = {
             "workload": ad["config"]["workload"], "accuracy": ad["config"]["accuracy"], "time_cap_s": cap,
             "adjoint_s": ad["adjoint"]["seconds_to_1pct"], "adjoint_accuracy": ad["adjoint"]["accuracy"],

@@ -493,11 +493,13 @@ def _engine_set_groups(self, ngroups: int):
     self._check(self.lib.bte_set_groups(self.ctx, int(ngroups)))
 
 
-def _engine_group_result(self, group: int, shape, raw: bool = False):
-    """Outputs of one replica group of the last run, scaled to the whole run."""
-    out = {k: np.zeros(shape) for k in ("temperature", "jx", "jy")}
+def _engine_group_result(self, group: int, shape, raw: bool = False, keys=("temperature", "jx", "jy")):
+    """Outputs of one replica group of the last run, scaled to the whole run
+    (`keys`: which of temperature, jx, jy to form)."""
+    out = {k: np.zeros(shape) for k in keys}
     r = RtaResult()
-    r.temperature, r.jx, r.jy = (_dptr(out[k]) for k in ("temperature", "jx", "jy"))
+    for k in keys:
+        setattr(r, k, _dptr(out[k]))
     if raw:
         for k in ("gz", "gz_jx", "gz_jy"):
             out[k] = np.zeros(shape)

@@ -323,21 +323,25 @@ namespace bte {
 // (src/RTA_MC2D.cpp:2336-2435): / V_box, x Eeff (per material with shares),
 // the flux factor, the time integration of a walls source (or bin averages
 // of an initial deviation) and T = gz / (C_v / vcorr) + T0.
-void rta_post(const bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, double Eeff, double step,
+void rta_post(bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, double Eeff, double step,
               std::vector<double> gz, std::vector<double> jx, std::vector<double> jy, bte_rta_result* out) {
     const bte::HostModes& m = c->modes;
     const bte::HostGeometry& g = c->geom;
     const std::size_t nk = std::size_t(nbx) * std::size_t(nbins);
+    // only the tallies an output needs: gz for the temperature, jx, jy
+    const bool need_gz = out->temperature != nullptr, need_jx = out->jx != nullptr, need_jy = out->jy != nullptr;
+    auto each = [&](auto&& f) {
+        if (need_gz) f(gz);
+        if (need_jx) f(jx);
+        if (need_jy) f(jy);
+    };
     // post-processing, src/RTA_MC2D.cpp:2336-2435
-    for (int ir = 0; ir < nbx; ++ir) {
-        const double vbox = g.boxes[std::size_t(ir)].area * g.thickness;
-        for (int i = 0; i < nbins; ++i) {
-            const std::size_t k = std::size_t(ir) * nbins + i;
-            gz[k] /= vbox;
-            jx[k] /= vbox;
-            jy[k] /= vbox;
+    each([&](std::vector<double>& v) {
+        for (int ir = 0; ir < nbx; ++ir) {
+            const double vbox = g.boxes[std::size_t(ir)].area * g.thickness;
+            for (int i = 0; i < nbins; ++i) v[std::size_t(ir) * nbins + i] /= vbox;
         }
-    }
+    });
     if (!c->mat_share.empty() && p->source == BTE_SOURCE_WALLS) {
         // Eeff_m = E_m / (share_m N) per material
         for (int ir = 0; ir < nbx; ++ir) {
@@ -345,38 +349,46 @@ void rta_post(const bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, dou
             const double Em = c->mat_share[k] > 0. ? c->mat_energy[k] / (c->mat_share[k] * double(p->nparticles)) : 0.;
             for (int i = 0; i < nbins; ++i) {
                 const std::size_t q = std::size_t(ir) * nbins + i;
-                gz[q] *= Em;
-                jx[q] *= Em * 1e12 * 1e9 * 1e9;
-                jy[q] *= Em * 1e12 * 1e9 * 1e9;
+                if (need_gz) gz[q] *= Em;
+                if (need_jx) jx[q] *= Em * 1e12 * 1e9 * 1e9;
+                if (need_jy) jy[q] *= Em * 1e12 * 1e9 * 1e9;
             }
         }
     } else {
-        for (auto& x : gz) x *= Eeff;
-        for (auto& x : jx) x *= Eeff * 1e12 * 1e9 * 1e9;
-        for (auto& x : jy) x *= Eeff * 1e12 * 1e9 * 1e9;
+        if (need_gz)
+            for (auto& x : gz) x *= Eeff;
+        if (need_jx)
+            for (auto& x : jx) x *= Eeff * 1e12 * 1e9 * 1e9;
+        if (need_jy)
+            for (auto& x : jy) x *= Eeff * 1e12 * 1e9 * 1e9;
     }
     if (p->source == BTE_SOURCE_WALLS) {
         // step response: integrate in time
-        for (int ir = 0; ir < nbx; ++ir)
-            for (int i = 1; i < nbins; ++i) {
-                const std::size_t k = std::size_t(ir) * nbins + i;
-                gz[k] += gz[k - 1];
-                jx[k] += jx[k - 1];
-                jy[k] += jy[k - 1];
-            }
+        each([&](std::vector<double>& v) {
+            for (int ir = 0; ir < nbx; ++ir)
+                for (int i = 1; i < nbins; ++i) {
+                    const std::size_t k = std::size_t(ir) * nbins + i;
+                    v[k] += v[k - 1];
+                }
+        });
     } else {
         // relaxation of an initial deviation: bin averages
-        for (std::size_t k = 0; k < nk; ++k) {
-            gz[k] /= step;
-            jx[k] /= step;
-            jy[k] /= step;
-        }
+        each([&](std::vector<double>& v) {
+            for (std::size_t k = 0; k < nk; ++k) v[k] /= step;
+        });
     }
     const double vcorr = g.thickness / m.c;
     if (out->temperature) {
-        std::vector<double> cvm(std::size_t(std::max(c->nmat, 1)));
-        for (std::size_t k = 0; k < cvm.size(); ++k)
-            cvm[k] = bte::calc_cv(m, c->nmat > 0 ? c->mat_T0[k] : p->T0);
+        // C_v per material, cached while the tables and temperatures stay
+        std::vector<double> T0s(std::size_t(std::max(c->nmat, 1)));
+        for (std::size_t k = 0; k < T0s.size(); ++k) T0s[k] = c->nmat > 0 ? c->mat_T0[k] : p->T0;
+        if (c->cv_version != c->tables_version || c->cv_T0s != T0s) {
+            c->cv_cache.resize(T0s.size());
+            for (std::size_t k = 0; k < T0s.size(); ++k) c->cv_cache[k] = bte::calc_cv(m, T0s[k]);
+            c->cv_T0s = T0s;
+            c->cv_version = c->tables_version;
+        }
+        const std::vector<double>& cvm = c->cv_cache;
         for (int ir = 0; ir < nbx; ++ir) {
             const double cv = cvm[std::size_t(c->nmat > 0 ? g.mat[std::size_t(ir)] : 0)];
             const double T0b = bte::box_T0(c, ir, p->T0);
@@ -710,12 +722,16 @@ bte_status bte_get_group_result(bte_ctx* c, int32_t group, bte_rta_result* out) 
         const double* raw = c->group_raw.data() + std::size_t(group) * nk * 3;
         const double G = double(c->group_n);
         // the group holds 1/G of the run's particles: x G estimates the whole run
-        std::vector<double> gz(nk), jx(nk), jy(nk);
-        for (std::size_t k = 0; k < nk; ++k) {
-            gz[k] = raw[3 * k] * G;
-            jx[k] = raw[3 * k + 1] * G;
-            jy[k] = raw[3 * k + 2] * G;
+        const bool want[3] = {out->gz || out->temperature, out->gz_jx || out->jx, out->gz_jy || out->jy};
+        std::vector<double> v[3];
+        for (int q = 0; q < 3; ++q) {
+            if (!want[q]) continue;
+            v[q].resize(nk);
+            for (std::size_t k = 0; k < nk; ++k) v[q][k] = raw[3 * k + std::size_t(q)] * G;
         }
+        std::vector<double>& gz = v[0];
+        std::vector<double>& jx = v[1];
+        std::vector<double>& jy = v[2];
         out->nboxes = c->group_nbx;
         out->nbins = c->group_nbins;
         out->Eeff = c->group_Eeff;

@@ -84,6 +84,12 @@ struct bte_ctx {
     int nmat = 0;
     std::vector<double> mat_w, mat_T0, mat_share;
     std::vector<double> mat_energy;   // walls-source energy rate per material (with shares)
+    // C_v per material (or at the run's T0 without materials), kept for the
+    // temperature conversion of successive runs: valid for these tables,
+    // these material temperatures and that T0
+    std::vector<double> cv_cache;
+    std::vector<double> cv_T0s;
+    long long cv_version = -1;
     bool shares_dirty = false;        // shares changed since the wall weights were set
     bte::DBuf d_boxmat;
     // per-T0 (or per-material) resampling
