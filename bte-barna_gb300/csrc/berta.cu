@@ -1,27 +1,35 @@
 // berta.cu - beyond-RTA deviational MC (beRTAMC2D) on the device.
 //
-// The step loop of src/beyondRTA_MC2d.cpp:2138-2425, production mode:
+// The step loop of src/beyondRTA_MC2d.cpp:2138-2425, production mode, with
+// the particle numbers kept on the device (no host wait inside the loop):
 //   1 advection by dt; void walls absorb and count Eborder, reservoirs absorb
-//     (evolparticle :708-970)                                      be_advect
+//     (evolparticle :708-970), fused with 5-7 for the particles of the last
+//     step                                                        be_advance
 //   2 gradient source term: Nabla_T particles at random points of every box
 //     with a gradient, random sub-step (source_term_gradient :597-676,
-//     Nabla_T_distribution src/sampling.cpp:118-187)            be_generate
-//   3 isothermal-wall injection, random sub-step            be_generate
-//     (Isothermal_walls :446-585, Ntogenerate src/sampling.cpp:243-260)
+//     Nabla_T_distribution src/sampling.cpp:118-187)
+//                                           be_plan_sources, be_generate_dev
+//   3 isothermal-wall injection, random sub-step (Isothermal_walls :446-585,
+//     Ntogenerate src/sampling.cpp:243-260)
+//                                           be_plan_sources, be_generate_dev
 //   4 adiabatic diffuse re-emission of |Eborder| at the wall temperature from
-//     the J(T) cubic spline (adiabatic_diffuse_walls :281-435)    be_generate
-//   5 deletion                                                  be_compact
-//   6 propagator scattering with sign branching (Scattering :1073-1210,
-//     propagator_H::get src/collision_operator.cpp:892-903), each parent's
-//     branching attempts made in place by its thread, or the RTA
-//     alternative (ScatteringRTA :983-1062)          be_scatter / be_scatter_rta
-//   7 histogram H[box][mode] += sign                            be_hist
+//     the J(T) cubic spline (adiabatic_diffuse_walls :281-435)
+//                  be_plan_adiabatic, be_wall_cdf1/2_dev, be_generate_dev
+//   5 deletion of the absorbed particles, 6 propagator scattering with sign
+//     branching (Scattering :1073-1210, propagator_H::get
+//     src/collision_operator.cpp:892-903), each parent's branching attempts
+//     made in place by its thread, or the RTA alternative (ScatteringRTA
+//     :983-1062), 7 histogram H[box][mode] += sign: one pass that reads each
+//     particle once and writes each outgoing particle once     be_advance
 //   8 cancellation every 4th step: keep |H| particles of the majority sign
-//     per (box, mode) (:2295-2370), by per-key ranks, no sort   be_cancel
-//   9 calculate_prop: ed and flux per box from H (:1538-1602)   be_props
+//     per (box, mode) (:2295-2370), by per-key ranks, no sort
+//                                            be_cancel_dev, be_compact_dev
+//   9 calculate_prop: ed and flux per box from H (:1538-1602), recorded per
+//     step on the device                                          be_props
 // Particles live in HBM as structure-of-arrays (x, y FP64; mode, box, sign
 // int32).  Draws: Philox4x32-10 keyed by (seed, step, phase), counter =
-// particle index.  Geometry: boxes that tile an axis-aligned grid.
+// particle index.  Geometry: boxes that tile an axis-aligned grid, or any
+// convex boxes with periodic boxes (the general advection).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -122,11 +130,14 @@ struct BertaState {
     long long cap = 0;
     DBuf a_x, a_y, a_mode, a_box, a_sign;   // particles
     DBuf b_x, b_y, b_mode, b_box, b_sign;   // compaction / scattering output
-    DBuf d_H, d_cnt, d_Eb, d_props, d_counts, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
+    DBuf d_H, d_cnt, d_Eb, d_props, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
     DBuf d_ne, d_ctot;                      // n(omega, T0) per mode; wall-CDF chunk sums
-    Pinned h_gens[4], h_req;                // staging: descriptors per phase, wall requests
+    Pinned h_gens[1];                       // staging: descriptors of the initial particles
+    // device-resident step loop: counters, planned sources, per-step records
+    DBuf d_dc, d_span, d_gdesc, d_ggenf, d_gcnt, d_idesc, d_igenf, d_icnt, d_adi, d_adesc, d_acnt;
+    DBuf d_phist, d_nhist, d_sa, d_sb, d_sc, d_sd, d_sx0, d_sxs;
 
     std::vector<Spline1D> spl;
     std::vector<char> spl_ok;
@@ -385,35 +396,6 @@ __device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& 
     return false;
 }
 
-__global__ void be_advect(PArr P, long long begin, long long end, AdvectArgs a) {
-    for (long long i = begin + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < end;
-         i += (long long)gridDim.x * blockDim.x) {
-        int mode = P.mode[i];
-        if (mode < 0) continue;
-        double dt = a.dt;
-        if (a.random_substep) {
-            Philox g;
-            g.init(a.key, (uint64_t)i);
-            dt = a.dt * g.uniform();
-        }
-        double x = P.x[i], y = P.y[i];
-        int box = P.box[i];
-        if (a.general) {
-            BePol pol;
-            pol.g.init(a.gkey, (uint64_t)i);
-            int err = 0;
-            if (!advect_general(a.T, pol, a.Eb, x, y, box, mode, P.sign[i], dt, err)) mode = -1;
-            if (err && a.err) atomicCAS(a.err, 0, err);
-        } else if (!advect_one(a.G, a.boxcell, a.mv, a.boxwall, a.Eb, x, y, box, mode, P.sign[i], dt)) {
-            mode = -1;
-        }
-        P.x[i] = x;
-        P.y[i] = y;
-        P.box[i] = box;
-        P.mode[i] = mode;
-    }
-}
-
 // Isothermal_wall_distribution (src/sampling.cpp:189-269) of each request:
 // pmf_k = v_n omega_k |n(omega_k, Tw) - n(omega_k, Te)| for v_n > 0, turned
 // into a CDF row; tot[r] keeps the sum.  Each request's row is split into
@@ -423,9 +405,9 @@ __global__ void be_advect(PArr P, long long begin, long long end, AdvectArgs a) 
 constexpr int WCDF_CHUNK = 1024;
 
 // pass 1: the chunk's running sums in place and its total
-__global__ void __launch_bounds__(256) be_wall_cdf1(const double* om, const double* vx, const double* vy,
-                                                    const double* ne, double Te_ref, int n,
-                                                    const WallReq* req, double* cdf, double* chunk_tot) {
+__device__ __forceinline__ void wall_cdf1_body(const double* om, const double* vx, const double* vy,
+                                               const double* ne, double Te_ref, int n, const WallReq* req,
+                                               double* cdf, double* chunk_tot) {
     __shared__ double part[256];
     const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
     const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
@@ -466,7 +448,7 @@ __global__ void __launch_bounds__(256) be_wall_cdf1(const double* om, const doub
 }
 
 // pass 2: offsets of the chunks, normalisation, the request's total
-__global__ void __launch_bounds__(256) be_wall_cdf2(int n, const double* chunk_tot, double* cdf, double* tot) {
+__device__ __forceinline__ void wall_cdf2_body(int n, const double* chunk_tot, double* cdf, double* tot) {
     const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
     const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
     double off = 0., total = 0.;
@@ -541,7 +523,7 @@ __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* 
 }
 
 // Append the live particles of [0, n) to `out` (warp-aggregated).
-__global__ void be_compact(PArr in, long long n, PArr out, unsigned long long* count) {
+__device__ __forceinline__ void compact_body(PArr in, long long n, PArr out, unsigned long long* count) {
     const int lane = threadIdx.x & 31;
     for (long long base = blockIdx.x * (long long)blockDim.x; base < n;
          base += (long long)gridDim.x * blockDim.x) {
@@ -562,21 +544,6 @@ __global__ void be_compact(PArr in, long long n, PArr out, unsigned long long* c
     }
 }
 
-// Propagator scattering with sign branching (Scattering, src/beyondRTA_MC2d.cpp:
-// 1073-1210).  Every scattering attempt of a parent draws its next mode from
-// the parent's column and emits one outgoing particle; when the drawn sign
-// differs from the parent's, the reference puts two copies of the parent
-// back into the queue, and each copy makes an attempt of its own.  The copies
-// are identical to the parent, so here a thread keeps only the number of
-// attempts its parent still owes and makes them in place, with fresh draws,
-// until none is left: one launch per step instead of one per round.  The
-// outgoing particles are appended warp by warp.  BRANCH_CAP bounds the
-// attempts of one parent (a supercritical propagator never stops).
-constexpr unsigned BRANCH_CAP = 1u << 20;
-
-// Persistent warps: a lane whose parent owes no attempt takes the next
-// parent from a global counter (one atomic per warp), so the warp keeps its
-// lanes busy while chains of different lengths run out.
 // propagator_H::lower_bound (include/collision_operator.hpp:263-269): the
 // first entry whose |value| is not below u, by std::lower_bound's own
 // probing, so that an interpolated column whose |values| are not monotone
@@ -596,113 +563,6 @@ __device__ __forceinline__ int lower_bound_abs(const double* a, int n, double u)
     return lo < n ? lo : n - 1;
 }
 
-// pcdf set: draw from the signed CDF columns instead of the alias table (an
-// interpolated propagator, which has no alias form in general).
-__global__ void be_scatter(PArr in, long long n, PArr out, unsigned long long* ocount, long long ocap,
-                           unsigned long long* nflips, unsigned long long* work, const PAlias* pal,
-                           const double* pcdf, int nm, unsigned long long key, int* err) {
-    const int lane = threadIdx.x & 31;
-    unsigned long long flips = 0;
-    int mode = 0, sign = 1, box = 0, col = 0;
-    double x = 0., y = 0.;
-    unsigned todo = 0, made = 0;
-    bool done = false, valid = false;
-    Philox g;
-    g.init(key, 0);
-    for (;;) {
-        // refill the lanes whose parent is finished
-        const unsigned idle = __ballot_sync(0xffffffffu, todo == 0 && !done);
-        if (idle) {
-            unsigned long long base = 0;
-            const int leader = __ffs(idle) - 1;
-            if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (todo == 0 && !done) {
-                const long long i = (long long)base + __popc(idle & ((1u << lane) - 1u));
-                if (i < n) {
-                    mode = in.mode[i];
-                    sign = in.sign[i];
-                    box = in.box[i];
-                    x = in.x[i];
-                    y = in.y[i];
-                    col = mode - 3;
-                    valid = col >= 0 && col < nm;
-                    if (!valid) atomicCAS(err, 0, E_VALUE);
-                    g.init(key, (uint64_t)i);
-                    todo = 1;
-                    made = 0;
-                } else {
-                    done = true;
-                }
-            }
-        }
-        if (__all_sync(0xffffffffu, done)) break;
-        const bool act = todo > 0;
-        int nmode = mode, nsign = sign;
-        if (act && valid && pcdf) {
-            const double* c = pcdf + (long long)col * nm;
-            const int im = lower_bound_abs(c, nm, g.uniform());
-            nmode = im + 3;
-            nsign = __ldg(c + im) > 0. ? sign : -sign;
-        } else if (act && valid) {
-            const int j = int(mulhi32(g.next32(), uint32_t(nm)));
-            const float acc = float(g.next32() >> 8) * 0x1p-24f;
-            const PAlias e = pal[(long long)col * nm + j];
-            const bool keep = acc < e.prob;
-            const int slot = keep ? j : int(e.alt & 0x3fffffffu);
-            const bool neg = keep ? (e.alt >> 31) != 0u : ((e.alt >> 30) & 1u) != 0u;
-            nmode = slot + 3;
-            nsign = neg ? -sign : sign;
-        }
-        // append the outgoing particle of this attempt
-        const unsigned m1 = __ballot_sync(0xffffffffu, act);
-        unsigned long long w = 0;
-        if (lane == 0 && m1) w = atomicAdd(ocount, (unsigned long long)__popc(m1));
-        w = __shfl_sync(0xffffffffu, w, 0);
-        if (act) {
-            const long long o = (long long)w + __popc(m1 & ((1u << lane) - 1u));
-            if (o < ocap) {
-                out.x[o] = x;
-                out.y[o] = y;
-                out.box[o] = box;
-                out.mode[o] = nmode;
-                out.sign[o] = nsign;
-            } else {
-                atomicCAS(err, 0, E_LIMIT);
-            }
-            --todo;
-            if (nsign != sign) {  // two more attempts of the parent
-                todo += 2;
-                ++flips;
-            }
-            if (++made >= BRANCH_CAP) {
-                atomicCAS(err, 0, E_LIMIT);
-                todo = 0;
-            }
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(0xffffffffu, flips, o);
-    if (lane == 0 && flips) atomicAdd(nflips, flips);
-}
-
-// RTA scattering: with probability 1 - exp(-w dt) a particle is resampled
-// from the C w distribution.
-__global__ void be_scatter_rta(PArr P, long long n, const double* w, double dt, const float* rprob,
-                               const int* ralt, int nmodes, unsigned long long key) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int mode = P.mode[i];
-        Philox g;
-        g.init(key, (uint64_t)i);
-        const double u = g.uniform();
-        if (u < 1. - exp(-__ldg(w + mode) * dt)) {
-            const int j = int(mulhi32(g.next32(), uint32_t(nmodes)));
-            const float acc = float(g.next32() >> 8) * 0x1p-24f;
-            P.mode[i] = acc < __ldg(rprob + j) ? j : __ldg(ralt + j);
-        }
-    }
-}
-
 __global__ void be_hist(PArr P, long long n, int* H, int nmodes) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
@@ -714,8 +574,8 @@ __global__ void be_hist(PArr P, long long n, int* H, int nmodes) {
 // visit the particles in the order of a random affine permutation
 // t -> (a t + b) mod n (a coprime to n), so the ranks, and with them the
 // survivors, do not follow the order of the particle list.
-__global__ void be_cancel(PArr P, long long n, const int* H, int* cnt, int nmodes, const int* reservoir,
-                          unsigned long long pa, unsigned long long pb) {
+__device__ __forceinline__ void cancel_body(PArr P, long long n, const int* H, int* cnt, int nmodes,
+                                            const int* reservoir, unsigned long long pa, unsigned long long pb) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
          t += (long long)gridDim.x * blockDim.x) {
         const long long i = (long long)((unsigned __int128)(pa % (unsigned long long)n) * (unsigned long long)t %
@@ -751,6 +611,402 @@ __global__ void be_props(const int* H, int nmodes, const double* vx, const doubl
     }
     if (threadIdx.x == 0)
         for (int q = 0; q < 3; ++q) out[3 * box + q] = red[q][0];
+}
+
+// ------------------------------------------------ device-resident step
+// Counters of the step loop, kept on the device between kernels.
+enum { DC_NP = 0, DC_NOUT, DC_WORK, DC_FLIPS, DC_PSTEPS, DC_NGEN, DC_COUNT = 8 };
+
+// A source planned on the device: where its particles start in the
+// particle arrays and how many there are.
+struct SrcSpan {
+    unsigned long long base, total;
+};
+
+// Propagator scattering with sign branching (Scattering,
+// src/beyondRTA_MC2d.cpp:1073-1210): every scattering attempt of a parent
+// draws its next mode from the parent's column (an alias table over |P|
+// with the signs in the alias word, or, for an interpolated propagator, the
+// signed CDF probed as propagator_H::lower_bound does) and emits one
+// outgoing particle; when the drawn sign differs from the parent's, the
+// reference puts two copies of the parent back into the queue, and each
+// copy makes an attempt of its own.  The copies are identical to the
+// parent, so a thread keeps only the number of attempts its parent still
+// owes and makes them in place, with fresh draws.  BRANCH_CAP bounds the
+// attempts of one parent (a supercritical propagator never stops).
+constexpr unsigned BRANCH_CAP = 1u << 20;
+
+// One step of the particles [0, *n_in) of `in`, fused: advection by the
+// step (advect = 1; particles born in this step were advected when they were
+// made), then the scattering of the survivors -- RTA (ScatteringRTA,
+// src/beyondRTA_MC2d.cpp:983-1062, a resampling with probability
+// 1 - exp(-w dt)) or the propagator with sign branching as above -- and the
+// histogram H[box][mode] += sign of every outgoing particle, appended to
+// `out` warp by warp.  Persistent warps: a lane whose parent owes no more
+// attempts takes the next parent from a counter; a parent absorbed during
+// its advection owes none.  Each particle is read once and each outgoing
+// particle written once.
+__global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long long* n_in, PArr out,
+                                                  unsigned long long* dc, long long ocap, int advect,
+                                                  AdvectArgs aa, int rta, const PAlias* pal, const double* pcdf,
+                                                  int nm, const double* w, const float* rprob, const int* ralt,
+                                                  int nmodes, unsigned long long skey, int* H, int* err) {
+    const long long n = (long long)*n_in;
+    const int lane = threadIdx.x & 31;
+    if (advect && blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(dc + DC_PSTEPS, (unsigned long long)n);
+    unsigned long long flips = 0;
+    int mode = 0, sign = 1, box = 0, col = 0;
+    double x = 0., y = 0.;
+    unsigned todo = 0, made = 0;
+    bool done = false, valid = false;
+    Philox g;
+    g.init(skey, 0);
+    for (;;) {
+        const unsigned idle = __ballot_sync(0xffffffffu, todo == 0 && !done);
+        if (idle) {
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader) base = atomicAdd(dc + DC_WORK, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (todo == 0 && !done) {
+                const long long i = (long long)base + __popc(idle & ((1u << lane) - 1u));
+                if (i < n) {
+                    mode = in.mode[i];
+                    if (mode >= 0) {
+                        sign = in.sign[i];
+                        box = in.box[i];
+                        x = in.x[i];
+                        y = in.y[i];
+                        bool alive = true;
+                        if (advect) {
+                            if (aa.general) {
+                                BePol pol;
+                                pol.g.init(aa.gkey, (uint64_t)i);
+                                int e = 0;
+                                alive = advect_general(aa.T, pol, aa.Eb, x, y, box, mode, sign, aa.dt, e);
+                                if (e && aa.err) atomicCAS(aa.err, 0, e);
+                            } else {
+                                alive = advect_one(aa.G, aa.boxcell, aa.mv, aa.boxwall, aa.Eb, x, y, box, mode,
+                                                   sign, aa.dt);
+                            }
+                        }
+                        if (alive) {
+                            col = mode - 3;
+                            valid = rta ? true : (col >= 0 && col < nm);
+                            if (!valid) atomicCAS(err, 0, E_VALUE);
+                            g.init(skey, (uint64_t)i);
+                            todo = 1;
+                            made = 0;
+                        }
+                    }
+                } else {
+                    done = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, done)) break;
+        const bool act = todo > 0;
+        int nmode = mode, nsign = sign;
+        if (act && rta) {
+            const double u = g.uniform();
+            if (u < 1. - exp(-__ldg(w + mode) * aa.dt)) {
+                const int j = int(mulhi32(g.next32(), uint32_t(nmodes)));
+                const float acc = float(g.next32() >> 8) * 0x1p-24f;
+                nmode = acc < __ldg(rprob + j) ? j : __ldg(ralt + j);
+            }
+        } else if (act && valid && pcdf) {
+            const double* c = pcdf + (long long)col * nm;
+            const int im = lower_bound_abs(c, nm, g.uniform());
+            nmode = im + 3;
+            nsign = __ldg(c + im) > 0. ? sign : -sign;
+        } else if (act && valid) {
+            const int j = int(mulhi32(g.next32(), uint32_t(nm)));
+            const float acc = float(g.next32() >> 8) * 0x1p-24f;
+            const PAlias e = pal[(long long)col * nm + j];
+            const bool keep = acc < e.prob;
+            const int slot = keep ? j : int(e.alt & 0x3fffffffu);
+            const bool neg = keep ? (e.alt >> 31) != 0u : ((e.alt >> 30) & 1u) != 0u;
+            nmode = slot + 3;
+            nsign = neg ? -sign : sign;
+        }
+        const unsigned m1 = __ballot_sync(0xffffffffu, act);
+        unsigned long long wo = 0;
+        if (lane == 0 && m1) wo = atomicAdd(dc + DC_NOUT, (unsigned long long)__popc(m1));
+        wo = __shfl_sync(0xffffffffu, wo, 0);
+        if (act) {
+            const long long o = (long long)wo + __popc(m1 & ((1u << lane) - 1u));
+            if (o < ocap) {
+                out.x[o] = x;
+                out.y[o] = y;
+                out.box[o] = box;
+                out.mode[o] = nmode;
+                out.sign[o] = nsign;
+                atomicAdd(H + (long long)box * nmodes + nmode, nsign);
+            } else {
+                atomicCAS(err, 0, E_LIMIT);
+            }
+            --todo;
+            if (!rta && nsign != sign) {
+                todo += 2;
+                ++flips;
+            }
+            if (++made >= BRANCH_CAP) {
+                atomicCAS(err, 0, E_LIMIT);
+                todo = 0;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(0xffffffffu, flips, o);
+    if (lane == 0 && flips) atomicAdd(dc + DC_FLIPS, flips);
+}
+
+// Exclusive scan of cnt[0..n) into descs[k].first, by one warp; returns the
+// total.
+__device__ unsigned long long warp_scan_first(const long long* cnt, int n, GenDesc* descs) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long carry = 0;
+    for (int b = 0; b < n; b += 32) {
+        const int k = b + lane;
+        unsigned long long v = k < n ? (unsigned long long)cnt[k] : 0ull;
+        unsigned long long incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (k < n) descs[k].first = (long long)(carry + incl - v);
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    return carry;
+}
+
+// Claim `total` slots of the step's new particles at A[DC_NGEN..), within
+// the capacity (a source that would overflow it sets BTE_ERR_LIMIT and
+// makes nothing).
+__device__ void claim_span(unsigned long long total, unsigned long long* dc, SrcSpan* span, long long cap,
+                           int* err) {
+    const unsigned long long base = dc[DC_NGEN];
+    if ((long long)(base + total) > cap) {
+        atomicCAS(err, 0, E_LIMIT);
+        total = 0;
+    }
+    span->base = base;
+    span->total = total;
+    dc[DC_NGEN] = base + total;
+}
+
+// Particle numbers of the gradient and isothermal-wall sources of one step:
+// Ntogenerate's stochastic rounding (src/sampling.cpp:166-183, :243-260) of
+// the expected numbers genf[k], from one Philox block per source.  One warp.
+__global__ void be_plan_sources(GenDesc* descs, const double* genf, long long* cnt, int ngen,
+                                unsigned long long key, unsigned long long* dc, SrcSpan* span, long long cap,
+                                int* err) {
+    if (threadIdx.x >= 32) return;
+    for (int k = threadIdx.x; k < ngen; k += 32) {
+        Philox q;
+        q.init(key, (uint64_t)k);
+        const double gen = genf[k];
+        long long c = (long long)gen;
+        if (q.uniform() <= gen - floor(gen)) ++c;
+        cnt[k] = c;
+    }
+    __syncwarp();
+    const unsigned long long total = warp_scan_first(cnt, ngen, descs);
+    if (threadIdx.x == 0) claim_span(total, dc, span, cap, err);
+}
+
+// A void border's adiabatic re-emission, tabulated per run: its segment,
+// the inward normal, its box and the box's Teq, its length and the spline
+// J(T) -> T of its wall (-1: not re-emitting: reservoirs, periodic boxes).
+struct AdiBorder {
+    double x0, y0, dx, dy, nx, ny, Teq, len;
+    int box, spline, pad0, pad1;
+};
+
+// Natural cubic splines on the device (the host's Spline1D, the reference's
+// CubicSpline1D src/interpolation.cpp:20-103): per spline `nk` intervals of
+// coefficients a, b, c, d from x0, with the right ends xs for the search.
+struct SplineDev {
+    const double *a, *b, *c, *d, *x0, *xs;
+    int nk;
+};
+
+__device__ __forceinline__ double spline_eval(const SplineDev& S, int id, double x) {
+    const long long o = (long long)id * S.nk;
+    int lo = 0, cnt = S.nk;  // lower_bound over xs
+    while (cnt > 0) {
+        const int st = cnt >> 1;
+        if (S.xs[o + lo + st] < x) {
+            lo += st + 1;
+            cnt -= st + 1;
+        } else {
+            cnt = st;
+        }
+    }
+    const int idx = lo >= S.nk ? S.nk - 1 : lo;
+    const double dx = x - S.x0[o + idx];
+    return S.a[o + idx] + dx * (S.b[o + idx] + dx * (S.c[o + idx] + S.d[o + idx] * dx));
+}
+
+// The adiabatic walls of one step (src/beyondRTA_MC2d.cpp:294-350): each
+// re-emitting border re-emits |Eborder| particles at the temperature whose
+// isothermal flux carries its absorbed energy (spline of J), one
+// distribution request per border; Eborder starts again from zero.  One
+// warp.
+__global__ void be_plan_adiabatic(int* Eb, const AdiBorder* ab, int nborders, SplineDev S, double Eeff, double dtstep,
+                                  double thickness, WallReq* req, long long* cnt, GenDesc* descs,
+                                  unsigned long long* dc, SrcSpan* span, long long cap, int* err) {
+    if (threadIdx.x >= 32) return;
+    for (int k = threadIdx.x; k < nborders; k += 32) {
+        const int E = Eb[k];
+        Eb[k] = 0;
+        const AdiBorder A = ab[k];
+        long long c = 0;
+        GenDesc d{};
+        d.cdf = k;
+        d.box = A.box >= 0 ? A.box : 0;
+        if (A.spline >= 0 && E != 0) {
+            const double Jb = Eeff * E / dtstep / (A.len * thickness);
+            const double Tb = spline_eval(S, A.spline, Jb);
+            req[k] = WallReq{A.nx, A.ny, Tb, A.Teq};
+            d.x0 = A.x0;
+            d.y0 = A.y0;
+            d.dx = A.dx;
+            d.dy = A.dy;
+            d.sign = (Tb - A.Teq) >= 0 ? 1 : -1;
+            c = (long long)(fabs((double)E) + 1.0e-6);
+        }
+        cnt[k] = c;
+        d.first = 0;
+        descs[k] = d;
+    }
+    __syncwarp();
+    const unsigned long long total = warp_scan_first(cnt, nborders, descs);
+    if (threadIdx.x == 0) claim_span(total, dc, span, cap, err);
+}
+
+// New particles of one planned source at A[span.base + k), k < span.total,
+// each advected for a random part of the step as it is made (the sources
+// of steps 2-4 of the reference's loop); an absorbed one keeps mode -1.
+__global__ void be_generate_dev(PArr P, const SrcSpan* span, const GenDesc* gens, int ngen, const float* aprob,
+                                const int* aalt, const signed char* asign, const double* cdfs,
+                                const double* cdftot, int nmodes, unsigned long long key, const GBox* boxes,
+                                const V2* hull, AdvectArgs aa) {
+    const SrcSpan sp = *span;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < (long long)sp.total;
+         k += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = ngen;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (gens[mid].first <= k) lo = mid; else hi = mid;
+        }
+        const GenDesc gd = gens[lo];
+        Philox g;
+        g.init(key, (uint64_t)k);
+        double x, y;
+        bool placed = true;
+        if (gd.rect == 2) {
+            const GBox& Bx = boxes[gd.box];
+            placed = false;
+            for (int tries = 0; tries < 100000 && !placed; ++tries) {
+                x = gd.x0 + g.uniform() * gd.dx;
+                y = gd.y0 + g.uniform() * gd.dy;
+                placed = inside_hull(hull + Bx.hull_off, Bx.nhull, v2(x, y));
+            }
+        } else if (gd.rect) {
+            x = gd.x0 + g.uniform() * gd.dx;
+            y = gd.y0 + g.uniform() * gd.dy;
+        } else {
+            const double u = g.uniform();
+            x = gd.x0 + u * gd.dx;
+            y = gd.y0 + u * gd.dy;
+        }
+        int mode;
+        if (gd.cdf >= 0) {
+            const double* row = cdfs + (long long)gd.cdf * nmodes;
+            mode = cdftot[gd.cdf] > 0. ? lower_bound_d(row, nmodes, g.uniform()) : -1;
+            if (mode >= nmodes) mode = nmodes - 1;
+            if (!placed) mode = -1;
+        } else {
+            const float* pr = aprob + gd.alias_off;
+            const int* al = aalt + gd.alias_off;
+            const int j = int(mulhi32(g.next32(), uint32_t(nmodes)));
+            const float acc = float(g.next32() >> 8) * 0x1p-24f;
+            mode = acc < __ldg(pr + j) ? j : __ldg(al + j);
+        }
+        int box = gd.box;
+        const int sign = (gd.msign && mode >= 0) ? int(__ldg(asign + gd.alias_off + mode)) : gd.sign;
+        const long long i = (long long)sp.base + k;
+        if (mode >= 0) {  // a random part of the step
+            Philox h;
+            h.init(aa.key, (uint64_t)i);
+            const double dt = aa.dt * h.uniform();
+            bool alive;
+            if (aa.general) {
+                BePol pol;
+                pol.g.init(aa.gkey, (uint64_t)i);
+                int e = 0;
+                alive = advect_general(aa.T, pol, aa.Eb, x, y, box, mode, sign, dt, e);
+                if (e && aa.err) atomicCAS(aa.err, 0, e);
+            } else {
+                alive = advect_one(aa.G, aa.boxcell, aa.mv, aa.boxwall, aa.Eb, x, y, box, mode, sign, dt);
+            }
+            if (!alive) mode = -1;
+        }
+        P.x[i] = x;
+        P.y[i] = y;
+        P.box[i] = box;
+        P.mode[i] = mode;
+        P.sign[i] = sign;
+    }
+}
+
+// The wall-CDF passes over every border, for the borders the step planned
+// (cnt > 0); rows of the others are left as they are.
+__global__ void __launch_bounds__(256) be_wall_cdf1_dev(const double* om, const double* vx, const double* vy,
+                                                        const double* ne, double Te_ref, int n, const WallReq* req,
+                                                        const long long* cnt, double* cdf, double* chunk_tot) {
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    if (cnt[blockIdx.x / nch] == 0) return;
+    wall_cdf1_body(om, vx, vy, ne, Te_ref, n, req, cdf, chunk_tot);
+}
+__global__ void __launch_bounds__(256) be_wall_cdf2_dev(int n, const long long* cnt, const double* chunk_tot,
+                                                        double* cdf, double* tot) {
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    if (cnt[blockIdx.x / nch] == 0) return;
+    wall_cdf2_body(n, chunk_tot, cdf, tot);
+}
+
+// Cancellation on the device over [0, *n_in) with the random affine
+// visiting order drawn from `key` (a coprime to n).
+__device__ __forceinline__ unsigned long long gcd_u64(unsigned long long a, unsigned long long b) {
+    while (b) {
+        const unsigned long long t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+__global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, const int* H, int* cnt, int nmodes,
+                              const int* reservoir, unsigned long long key) {
+    const long long n = (long long)*n_in;
+    if (n <= 0) return;
+    Philox q;
+    q.init(key, 0);
+    unsigned long long pa = ((unsigned long long)q.next32() << 32 | q.next32()) | 1ull;
+    const unsigned long long pb = (unsigned long long)q.next32() << 32 | q.next32();
+    while (gcd_u64((unsigned long long)n, pa % (unsigned long long)n) != 1ull) pa += 2;
+    cancel_body(P, n, H, cnt, nmodes, reservoir, pa, pb);
+}
+
+// Compaction of [0, *n_in) with the survivors counted into *count.
+__global__ void be_compact_dev(PArr in, const unsigned long long* n_in, PArr out, unsigned long long* count) {
+    compact_body(in, (long long)*n_in, out, count);
+}
+
+// dc[to] = dc[from]; record[step] = dc[DC_NP] after it.
+__global__ void be_counters(unsigned long long* dc, int to, int from, long long* record, int step) {
+    if (to >= 0) dc[to] = dc[from];
+    if (record) record[step] = (long long)dc[DC_NP];
 }
 
 PArr arr(DBuf& x, DBuf& y, DBuf& m, DBuf& b, DBuf& s, long long off = 0) {
@@ -950,6 +1206,12 @@ double wall_pmf(const bte::HostModes& m, bte::V2 n, double Tw, double Te, std::v
     return 1.0e+12 * 1.054571726e-34 * s;
 }
 
+[[noreturn]] void throw_step_error(int e) {
+    throw Error(bte_status(e), e == BTE_ERR_LIMIT      ? "particle capacity or step cap exceeded"
+                               : e == BTE_ERR_GEOMETRY ? "geometry error in the advection"
+                                                       : "particle without a propagator column");
+}
+
 }  // namespace
 
 extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_berta_result* out) {
@@ -1024,7 +1286,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         B.d_H.alloc(std::size_t(nbx) * n * sizeof(int));
         B.d_cnt.alloc(std::size_t(nbx) * n * sizeof(int));
         B.d_props.alloc(std::size_t(nbx) * 3 * sizeof(double));
-        B.d_counts.alloc(4 * sizeof(unsigned long long));
         c->d_err.alloc(4 * sizeof(int));
         ck(cudaMemsetAsync(c->d_err.p, 0, 4 * sizeof(int), s), "memset");
         std::vector<int> hres(g.reservoir.begin(), g.reservoir.end());
@@ -1067,7 +1328,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             A.mv = c->d_mv.as<ModeVel>();
             return A;
         }();
-        auto* counts = B.d_counts.as<unsigned long long>();
         int* err = c->d_err.as<int>();
         // convex-box tables for geometries that are not a grid (or have
         // periodic boxes)
@@ -1078,7 +1338,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         std::vector<int> aalt;
         std::vector<GenDesc> descs;
         B.d_gens.alloc(std::size_t(std::max({nborders, nbx, int(iso.walls.size())}) + 1) * sizeof(GenDesc));
-        std::vector<WallReq> reqs;
         // a source spread over box b: its grid cell, or its bounding box with
         // rejection (geometry_2d::get_random_point)
         auto box_desc = [&](int b) {
@@ -1151,17 +1410,14 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         // generate the sources in `descs` at A[base..): alias rows from
         // aprob/aalt (uploaded here) or from a table already on the device
         // (rprob/ralt, with per-mode signs rsign), CDF rows from B.d_cdf
-        auto generate = [&](long long base, long long total, long long step, int phase, bool advect,
-                            const float* rprob = nullptr, const int* ralt = nullptr,
-                            const signed char* rsign = nullptr) {
+        // the initial deviation's particles (descs, alias rows aprob/aalt) at A[base..)
+        auto generate = [&](long long base, long long total, long long step, int phase) {
             if (total <= 0) return;
             if (base + total > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded: raise capacity");
-            // one staging buffer per phase (initial, gradient, isothermal, adiabatic)
-            const int slot = phase == 0 ? 0 : phase == 8 ? 1 : phase == 2 ? 2 : 3;
-            upload_pinned(B.d_gens, B.h_gens[slot], descs, s);
-            const float* dprob = rprob;
-            const int* dalt = ralt;
-            if (!rprob && !aprob.empty()) {
+            upload_pinned(B.d_gens, B.h_gens[0], descs, s);
+            const float* dprob = nullptr;
+            const int* dalt = nullptr;
+            if (!aprob.empty()) {
                 B.d_alias.alloc(aprob.size() * sizeof(float) + aalt.size() * sizeof(int));
                 ck(cudaMemcpyAsync(B.d_alias.p, aprob.data(), aprob.size() * sizeof(float), cudaMemcpyHostToDevice, s), "h2d");
                 int* a2 = reinterpret_cast<int*>(B.d_alias.as<char>() + aprob.size() * sizeof(float));
@@ -1171,35 +1427,9 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             PArr A = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
             be_generate<<<launch_blocks(total, c->nsm), 256, 0, s>>>(
-                A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), dprob, dalt, rsign,
+                A, base, total, B.d_gens.as<GenDesc>(), int(descs.size()), dprob, dalt, nullptr,
                 B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n, mix_key(p->seed, step, phase),
                 c->d_boxes.as<GBox>(), c->d_hull.as<V2>());
-            if (advect) {
-                AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt,
-                              mix_key(p->seed, step, phase + 1), 1,
-                              general, mix_key(p->seed, step, phase + 17), err, TT};
-                be_advect<<<launch_blocks(total, c->nsm), 256, 0, s>>>(A, base, base + total, aa);
-            }
-        };
-        auto read_count = [&](int k) {
-            unsigned long long v = 0;
-            ck(cudaMemcpyAsync(&v, counts + k, sizeof v, cudaMemcpyDeviceToHost, s), "d2h");
-            sync(c);
-            return (long long)v;
-        };
-        auto compact = [&](long long nn) {
-            ck(cudaMemsetAsync(counts, 0, sizeof(unsigned long long), s), "memset");
-            if (nn > 0)
-                be_compact<<<launch_blocks(nn, c->nsm), 256, 0, s>>>(
-                    arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), nn,
-                    arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), counts);
-            const long long m2 = read_count(0);
-            std::swap(B.a_x.p, B.b_x.p);
-            std::swap(B.a_y.p, B.b_y.p);
-            std::swap(B.a_mode.p, B.b_mode.p);
-            std::swap(B.a_box.p, B.b_box.p);
-            std::swap(B.a_sign.p, B.b_sign.p);
-            return m2;
         };
         std::vector<double> hprops(std::size_t(nbx) * 3);
         std::vector<double> vol(static_cast<std::size_t>(nbx));
@@ -1249,226 +1479,254 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 descs.push_back(d);
                 first += cnt;
             }
-            generate(0, first, -1, 0, false);
+            generate(0, first, -1, 0);
             np = first;
         }
         props(np, 0);
-        const PArr A0 = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
-        (void)A0;
         long long psteps = 0, branchings = 0;
+        // ---- the step loop, resident on the device: particle numbers stay in
+        // device counters, the sources are planned on the device, and the
+        // step's properties are recorded there; the host synchronises only
+        // when a per-step hook asks for each step's histogram
+        int nsteps = 0;
+        for (double t = 0.; t <= p->maxtime; t += p->dt) ++nsteps;
+        B.d_dc.alloc(DC_COUNT * sizeof(unsigned long long));
+        auto* dc = B.d_dc.as<unsigned long long>();
+        B.d_span.alloc(3 * sizeof(SrcSpan));
+        SrcSpan* span = B.d_span.as<SrcSpan>();
+        {
+            std::vector<unsigned long long> h0(DC_COUNT, 0ull);
+            h0[DC_NP] = (unsigned long long)np;
+            B.d_dc.upload(h0, s);
+        }
+        B.d_phist.alloc(std::size_t(nsteps + 1) * std::size_t(nbx) * 3 * sizeof(double));
+        B.d_nhist.alloc(std::size_t(nsteps + 1) * sizeof(long long));
+        // sources with fixed descriptors: gradient boxes and isothermal walls,
+        // with the expected particle numbers of a step
+        std::vector<GenDesc> gdesc, idesc;
+        std::vector<double> ggenf, igenf;
+        for (std::size_t k = 0; k < grad.box.size(); ++k) {
+            GenDesc d = box_desc(grad.box[k]);
+            d.alias_off = (long long)k * n;
+            d.msign = 1;
+            gdesc.push_back(d);
+            ggenf.push_back(p->dt * grad.energy[k] / p->Eeff);
+        }
+        for (std::size_t k = 0; k < iso.walls.size(); ++k) {
+            const WallGenerator& W = iso.walls[k];
+            const double Lb = norm(sub(W.sb, W.sa));
+            const double spf = Lb * g.thickness / (m.V * g.thickness / m.c);
+            const double cumulsum = std::fabs(W.flux) * double(m.nq) * vuc;
+            GenDesc d{};
+            d.x0 = W.p1.x;
+            d.y0 = W.p1.y;
+            d.dx = W.nd.x;
+            d.dy = W.nd.y;
+            d.box = W.box;
+            d.sign = W.sign;
+            d.cdf = -1;
+            d.alias_off = (long long)k * n;
+            idesc.push_back(d);
+            igenf.push_back(p->dt * spf * cumulsum / (p->Eeff * double(m.nq)));
+        }
+        const int ngd = int(gdesc.size()), nid = int(idesc.size());
+        if (ngd) {
+            B.d_gdesc.upload(gdesc, s);
+            B.d_ggenf.upload(ggenf, s);
+            B.d_gcnt.alloc(std::size_t(ngd) * sizeof(long long));
+        }
+        if (nid) {
+            B.d_idesc.upload(idesc, s);
+            B.d_igenf.upload(igenf, s);
+            B.d_icnt.alloc(std::size_t(nid) * sizeof(long long));
+        }
+        // adiabatic re-emission per void border: segment, inward normal, Teq
+        // and the J(T) -> T spline of its wall (one per normal and Teq)
+        std::vector<AdiBorder> adi(static_cast<std::size_t>(nborders));
+        std::vector<double> sa, sb, sc, sd, sx0, sxs;
+        std::map<std::tuple<double, double, double>, int> spline_of;
+        int spl_nk = 0;
+        std::vector<double> pmf;
+        for (int gb = 0; gb < nborders; ++gb) {
+            AdiBorder& A = adi[std::size_t(gb)];
+            const int b = border_box[std::size_t(gb)];
+            const GBorder& br = g.borders[std::size_t(gb)];
+            A.x0 = br.p1.x;
+            A.y0 = br.p1.y;
+            A.dx = br.nd.x;
+            A.dy = br.nd.y;
+            A.nx = -br.np.x;
+            A.ny = -br.np.y;
+            A.len = norm(sub(br.p2, br.p1));
+            A.box = b;
+            A.spline = -1;
+            if (b < 0 || g.reservoir[std::size_t(b)] || g.tto[std::size_t(b)] >= 0) continue;
+            const double Teq = g.Teq[std::size_t(b)];
+            A.Teq = Teq;
+            const auto key = std::make_tuple(A.nx, A.ny, Teq);
+            auto it = spline_of.find(key);
+            if (it == spline_of.end()) {
+                std::vector<double> J(100), Tv(100);
+                for (int t = 0; t < 100; ++t) {
+                    const double T = 10.0 + 10.0 * t;
+                    Tv[std::size_t(t)] = T;
+                    const double cs = wall_pmf(m, v2(A.nx, A.ny), T, Teq, pmf);
+                    J[std::size_t(t)] = ((T - Teq) >= 0 ? 1 : -1) * (cs / (double(m.nq) * vuc));
+                }
+                Spline1D sp;
+                sp.build(J, Tv);
+                spl_nk = int(sp.a.size());
+                sa.insert(sa.end(), sp.a.begin(), sp.a.end());
+                sb.insert(sb.end(), sp.b.begin(), sp.b.end());
+                sc.insert(sc.end(), sp.c.begin(), sp.c.end());
+                sd.insert(sd.end(), sp.d.begin(), sp.d.end());
+                sx0.insert(sx0.end(), sp.x0.begin(), sp.x0.end());
+                sxs.insert(sxs.end(), sp.xs.begin(), sp.xs.end());
+                it = spline_of.emplace(key, int(spline_of.size())).first;
+            }
+            A.spline = it->second;
+        }
+        B.d_adi.upload(adi, s);
+        B.d_adesc.alloc(std::size_t(nborders) * sizeof(GenDesc));
+        B.d_acnt.alloc(std::size_t(nborders) * sizeof(long long));
+        SplineDev SP{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, spl_nk};
+        if (!sa.empty()) {
+            B.d_sa.upload(sa, s);
+            B.d_sb.upload(sb, s);
+            B.d_sc.upload(sc, s);
+            B.d_sd.upload(sd, s);
+            B.d_sx0.upload(sx0, s);
+            B.d_sxs.upload(sxs, s);
+            SP = SplineDev{B.d_sa.as<double>(), B.d_sb.as<double>(), B.d_sc.as<double>(), B.d_sd.as<double>(),
+                           B.d_sx0.as<double>(), B.d_sxs.as<double>(), spl_nk};
+        }
+        const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+        const unsigned pblocks = unsigned(c->nsm) * 8u;  // persistent grids of the step kernels
+        const PAlias* pal = p->rta ? nullptr : B.d_palias.as<PAlias>();
+        const double* pcdf = (!p->rta && B.sel_lirp) ? B.d_pcdf.as<double>() : nullptr;
         int istep = 0;
         double time = 0.;
         // phase timing (the reference's timer buckets): events at the phase
-        // borders of every step, read after the step's last sync
+        // borders of every step, read at the end
         enum { PH_ADV, PH_CANCEL, PH_GEN, PH_HIST, PH_PROPS, PH_READ, PH_SAVE, PH_SCAT };
         double phase[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        cudaEvent_t pe[7];
-        for (auto& e : pe) ck(cudaEventCreate(&e), "cudaEventCreate");
+        std::vector<cudaEvent_t> pev(std::size_t(nsteps) * 7, nullptr);
         struct EvGuard {
-            cudaEvent_t* e;
+            std::vector<cudaEvent_t>* e;
             ~EvGuard() {
-                for (int i = 0; i < 7; ++i) cudaEventDestroy(e[i]);
+                for (auto ev : *e)
+                    if (ev) cudaEventDestroy(ev);
             }
-        } pe_guard{pe};
+        } pe_guard{&pev};
+        for (auto& e : pev) ck(cudaEventCreate(&e), "cudaEventCreate");
         phase[PH_READ] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-        std::vector<int> hE(static_cast<std::size_t>(nborders));
         std::vector<int> hH;
-        std::vector<double> pmf;
         const int cancel_every = p->cancel_every > 0 ? p->cancel_every : 4;
-        while (time <= p->maxtime) {
-            ck(cudaEventRecord(pe[0], s), "event");
-            // 1. advection
-            if (np > 0) {
-                AdvectArgs aa{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0,
-                              general, mix_key(p->seed, istep, 31), err, TT};
-                be_advect<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
-                                                                    0, np, aa);
+        const std::size_t hbytes = std::size_t(nbx) * n * sizeof(int);
+        auto swap_ab = [&] {
+            std::swap(B.a_x.p, B.b_x.p);
+            std::swap(B.a_y.p, B.b_y.p);
+            std::swap(B.a_mode.p, B.b_mode.p);
+            std::swap(B.a_box.p, B.b_box.p);
+            std::swap(B.a_sign.p, B.b_sign.p);
+        };
+        while (time <= p->maxtime && istep < nsteps) {
+            cudaEvent_t* ev = pev.data() + std::size_t(istep) * 7;
+            ck(cudaEventRecord(ev[0], s), "event");
+            // 1 + 6 + 7 for the particles of the last step: advection,
+            // scattering and histogram in one pass, into B
+            ck(cudaMemsetAsync(B.d_H.p, 0, hbytes, s), "memset");
+            ck(cudaMemsetAsync(dc + DC_NOUT, 0, 2 * sizeof(unsigned long long), s), "memset");
+            const AdvectArgs a_step{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0,
+                                    general, mix_key(p->seed, istep, 31), err, TT};
+            be_advance<<<pblocks, 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP,
+                                               arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc, cap, 1, a_step,
+                                               p->rta, pal, pcdf, B.nm, c->d_w.as<double>(),
+                                               c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
+                                               mix_key(p->seed, istep, 64), B.d_H.as<int>(), err);
+            ck(cudaEventRecord(ev[1], s), "event");
+            // 2-4 the step's sources, made at A[0..) (A is free now) and each
+            // advected for a random part of the step as it is made
+            ck(cudaMemsetAsync(dc + DC_NGEN, 0, sizeof(unsigned long long), s), "memset");
+            const PArr A = arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign);
+            auto gen_args = [&](int ph) {
+                return AdvectArgs{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt,
+                                  mix_key(p->seed, istep, ph + 1), 1, general, mix_key(p->seed, istep, ph + 17), err,
+                                  TT};
+            };
+            if (ngd) {
+                be_plan_sources<<<1, 32, 0, s>>>(B.d_gdesc.as<GenDesc>(), B.d_ggenf.as<double>(), B.d_gcnt.as<long long>(),
+                                                 ngd, mix_key(p->seed, istep, 40), dc, span + 0, cap, err);
+                be_generate_dev<<<pblocks, 256, 0, s>>>(A, span + 0, B.d_gdesc.as<GenDesc>(), ngd, B.d_gprob.as<float>(),
+                                                        B.d_galt.as<int>(), B.d_gsign.as<signed char>(),
+                                                        B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n,
+                                                        mix_key(p->seed, istep, 8), c->d_boxes.as<GBox>(),
+                                                        c->d_hull.as<V2>(), gen_args(8));
             }
-            psteps += np;
-            ck(cudaEventRecord(pe[1], s), "event");
-            // 2. gradient source term: Ntogenerate(dt, vol, Eeff) per box
-            if (!grad.box.empty()) {
-                descs.clear();
-                long long nnew = 0;
-                for (std::size_t k = 0; k < grad.box.size(); ++k) {
-                    const long long cnt = (long long)n_to_generate(p->dt * grad.energy[k] / p->Eeff, rng);
-                    if (cnt == 0) continue;
-                    GenDesc d = box_desc(grad.box[k]);
-                    d.alias_off = (long long)k * n;
-                    d.msign = 1;
-                    d.first = nnew;
-                    descs.push_back(d);
-                    nnew += cnt;
-                }
-                generate(np, nnew, istep, 8, true, B.d_gprob.as<float>(), B.d_galt.as<int>(),
-                         B.d_gsign.as<signed char>());
-                np += nnew;
+            if (nid) {
+                be_plan_sources<<<1, 32, 0, s>>>(B.d_idesc.as<GenDesc>(), B.d_igenf.as<double>(), B.d_icnt.as<long long>(),
+                                                 nid, mix_key(p->seed, istep, 41), dc, span + 1, cap, err);
+                be_generate_dev<<<pblocks, 256, 0, s>>>(A, span + 1, B.d_idesc.as<GenDesc>(), nid, B.d_isoprob.as<float>(),
+                                                        B.d_isoalt.as<int>(), nullptr, B.d_cdf.as<double>(),
+                                                        B.d_cdftot.as<double>(), n, mix_key(p->seed, istep, 2),
+                                                        c->d_boxes.as<GBox>(), c->d_hull.as<V2>(), gen_args(2));
             }
-            // 3. isothermal walls
-            descs.clear();
-            aprob.clear();
-            aalt.clear();
-            long long nnew = 0;
-            for (std::size_t k = 0; k < iso.walls.size(); ++k) {
-                const WallGenerator& W = iso.walls[k];
-                const double Lb = norm(sub(W.sb, W.sa));
-                const double spf = Lb * g.thickness / (m.V * g.thickness / m.c);
-                const double cumulsum = std::fabs(W.flux) * double(m.nq) * vuc;
-                const long long cnt = (long long)n_to_generate(p->dt * spf * cumulsum / (p->Eeff * double(m.nq)), rng);
-                if (cnt == 0) continue;
-                GenDesc d{};
-                d.x0 = W.p1.x;
-                d.y0 = W.p1.y;
-                d.dx = W.nd.x;
-                d.dy = W.nd.y;
-                d.box = W.box;
-                d.sign = W.sign;
-                d.rect = 0;
-                d.cdf = -1;
-                d.alias_off = (long long)k * n;
-                d.first = nnew;
-                descs.push_back(d);
-                nnew += cnt;
-            }
-            generate(np, nnew, istep, 2, true, B.d_isoprob.as<float>(), B.d_isoalt.as<int>());
-            np += nnew;
-            // 4. adiabatic diffuse walls: |Eborder| at the spline temperature
-            ck(cudaMemcpyAsync(hE.data(), B.d_Eb.p, hE.size() * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
-            sync(c);
-            ck(cudaMemsetAsync(B.d_Eb.p, 0, hE.size() * sizeof(int), s), "memset");
-            descs.clear();
-            aprob.clear();
-            aalt.clear();
-            reqs.clear();
-            nnew = 0;
-            for (int gb = 0; gb < nborders; ++gb) {
-                const int E = hE[std::size_t(gb)];
-                if (E == 0) continue;
-                const int b = border_box[std::size_t(gb)];
-                if (b < 0 || g.reservoir[std::size_t(b)] || g.tto[std::size_t(b)] >= 0) continue;
-                const GBorder& br = g.borders[std::size_t(gb)];
-                const V2 nwall = v2(-br.np.x, -br.np.y);
-                const double Teq = g.Teq[std::size_t(b)];
-                if (!B.spl_ok[std::size_t(gb)]) {
-                    std::vector<double> J(100), Tv(100);
-                    for (int t = 0; t < 100; ++t) {
-                        const double T = 10.0 + 10.0 * t;
-                        Tv[std::size_t(t)] = T;
-                        const double cs = wall_pmf(m, nwall, T, Teq, pmf);
-                        J[std::size_t(t)] = ((T - Teq) >= 0 ? 1 : -1) * (cs / (double(m.nq) * vuc));
-                    }
-                    B.spl[std::size_t(gb)].build(J, Tv);
-                    B.spl_ok[std::size_t(gb)] = 1;
-                }
-                const double len = norm(sub(br.p2, br.p1));
-                const double Jb = p->Eeff * E / p->dt / (len * g.thickness);
-                const double Tb = B.spl[std::size_t(gb)].interp(Jb);
-                GenDesc d{};
-                d.x0 = br.p1.x;
-                d.y0 = br.p1.y;
-                d.dx = br.nd.x;
-                d.dy = br.nd.y;
-                d.box = b;
-                d.sign = (Tb - Teq) >= 0 ? 1 : -1;
-                d.rect = 0;
-                d.cdf = int(reqs.size());
-                d.alias_off = 0;
-                d.first = nnew;
-                descs.push_back(d);
-                reqs.push_back(WallReq{nwall.x, nwall.y, Tb, Teq});
-                nnew += (long long)(std::abs(E) + 1.0e-6);
-            }
-            if (!reqs.empty()) {
-                // the re-emission distributions at the border temperatures,
-                // built on the device (one block per border)
-                upload_pinned(B.d_req, B.h_req, reqs, s);
-                const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
-                be_wall_cdf1<<<unsigned(reqs.size()) * unsigned(nch), 256, 0, s>>>(
+            if (nborders > 0) {
+                be_plan_adiabatic<<<1, 32, 0, s>>>(B.d_Eb.as<int>(), B.d_adi.as<AdiBorder>(), nborders, SP, p->Eeff,
+                                                   p->dt, g.thickness, B.d_req.as<WallReq>(), B.d_acnt.as<long long>(),
+                                                   B.d_adesc.as<GenDesc>(), dc, span + 2, cap, err);
+                be_wall_cdf1_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
                     B.d_om.as<double>(), B.d_vx.as<double>(), B.d_vy.as<double>(), B.d_ne.as<double>(), p->T0, n,
-                    B.d_req.as<WallReq>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
-                be_wall_cdf2<<<unsigned(reqs.size()) * unsigned(nch), 256, 0, s>>>(
-                    n, B.d_ctot.as<double>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
+                    B.d_req.as<WallReq>(), B.d_acnt.as<long long>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
+                be_wall_cdf2_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
+                    n, B.d_acnt.as<long long>(), B.d_ctot.as<double>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
+                be_generate_dev<<<pblocks, 256, 0, s>>>(A, span + 2, B.d_adesc.as<GenDesc>(), nborders, nullptr, nullptr,
+                                                        nullptr, B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n,
+                                                        mix_key(p->seed, istep, 4), c->d_boxes.as<GBox>(),
+                                                        c->d_hull.as<V2>(), gen_args(4));
             }
-            generate(np, nnew, istep, 4, true);
-            np += nnew;
-            ck(cudaEventRecord(pe[2], s), "event");
-            // 5. delete absorbed particles
-            np = compact(np);
-            // 6. scattering
-            if (p->rta) {
-                if (np > 0)
-                    be_scatter_rta<<<launch_blocks(np, c->nsm), 256, 0, s>>>(
-                        arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np, c->d_w.as<double>(), p->dt,
-                        c->d_rprob.as<float>(), c->d_ralt.as<int>(), n, mix_key(p->seed, istep, 6));
-            } else if (np > 0) {
-                // counts: [0] outgoing particles, [1] sign flips, [2] parents taken
-                ck(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), s), "memset");
-                long long sblocks = (np + 255) / 256;
-                if (sblocks > 8ll * c->nsm) sblocks = 8ll * c->nsm;
-                be_scatter<<<unsigned(sblocks), 256, 0, s>>>(
-                    arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), np,
-                    arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), counts, cap, counts + 1, counts + 2,
-                    B.d_palias.as<PAlias>(), B.sel_lirp ? B.d_pcdf.as<double>() : nullptr, B.nm,
-                    mix_key(p->seed, istep, 64), err);
-                unsigned long long hcnt[2] = {0, 0};
-                ck(cudaMemcpyAsync(hcnt, counts, sizeof hcnt, cudaMemcpyDeviceToHost, s), "d2h");
-                sync(c);
-                branchings += (long long)hcnt[1];
-                np = (long long)hcnt[0];
-                if (np > cap) throw Error(BTE_ERR_LIMIT, "particle capacity exceeded in scattering");
-                std::swap(B.a_x.p, B.b_x.p);
-                std::swap(B.a_y.p, B.b_y.p);
-                std::swap(B.a_mode.p, B.b_mode.p);
-                std::swap(B.a_box.p, B.b_box.p);
-                std::swap(B.a_sign.p, B.b_sign.p);
+            ck(cudaEventRecord(ev[2], s), "event");
+            // 5-7 for the new particles: the absorbed ones dropped, the others
+            // scattered and counted in the histogram, appended to B
+            ck(cudaMemsetAsync(dc + DC_WORK, 0, sizeof(unsigned long long), s), "memset");
+            be_advance<<<pblocks, 256, 0, s>>>(A, dc + DC_NGEN, arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc,
+                                               cap, 0, a_step, p->rta, pal, pcdf, B.nm, c->d_w.as<double>(),
+                                               c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
+                                               mix_key(p->seed, istep, 65), B.d_H.as<int>(), err);
+            ck(cudaEventRecord(ev[3], s), "event");
+            ck(cudaEventRecord(ev[4], s), "event");  // the histogram is made in the passes above
+            // 8. cancellation every cancel_every steps: B -> A; otherwise B is the population
+            if (istep % cancel_every == 0) {
+                ck(cudaMemsetAsync(B.d_cnt.p, 0, hbytes, s), "memset");
+                be_cancel_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
+                                                      B.d_H.as<int>(), B.d_cnt.as<int>(), n, d_res.as<int>(),
+                                                      mix_key(p->seed, istep, 77));
+                ck(cudaMemsetAsync(dc + DC_NP, 0, sizeof(unsigned long long), s), "memset");
+                be_compact_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
+                                                       arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP);
+            } else {
+                be_counters<<<1, 1, 0, s>>>(dc, DC_NP, DC_NOUT, nullptr, 0);
+                swap_ab();
             }
-            ck(cudaEventRecord(pe[3], s), "event");
-            // 7.-9. histogram, cancellation, properties
-            ck(cudaMemsetAsync(B.d_H.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
-            if (np > 0)
-                be_hist<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
-                                                                  np, B.d_H.as<int>(), n);
-            ck(cudaEventRecord(pe[4], s), "event");
-            if (istep % cancel_every == 0 && np > 0) {
-                ck(cudaMemsetAsync(B.d_cnt.p, 0, std::size_t(nbx) * n * sizeof(int), s), "memset");
-                // random affine permutation of the visiting order (a coprime to np)
-                unsigned long long pa = rng.next() | 1ull, pb = rng.next();
-                while (std::gcd((unsigned long long)np, pa % (unsigned long long)np) != 1ull) pa += 2;
-                be_cancel<<<launch_blocks(np, c->nsm), 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
-                                                                    np, B.d_H.as<int>(), B.d_cnt.as<int>(), n,
-                                                                    d_res.as<int>(), pa, pb);
-                np = compact(np);
-            }
-            ck(cudaEventRecord(pe[5], s), "event");
+            ck(cudaEventRecord(ev[5], s), "event");
+            // 9. properties of the step (calculate_prop), recorded on the device
             be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),
-                                          B.d_props.as<double>());
-            int herr[4];
-            ck(cudaMemcpyAsync(hprops.data(), B.d_props.p, hprops.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "d2h");
-            ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
-            ck(cudaEventRecord(pe[6], s), "event");
-            sync(c);
-            {
-                const int bucket[6] = {PH_ADV, PH_GEN, PH_SCAT, PH_HIST, PH_CANCEL, PH_PROPS};
-                for (int k = 0; k < 6; ++k) {
-                    float ms = 0.f;
-                    if (cudaEventElapsedTime(&ms, pe[k], pe[k + 1]) == cudaSuccess) phase[bucket[k]] += ms;
-                }
-            }
-            for (int b = 0; b < nbx; ++b) {
-                const double f1 = p->Eeff / vol[std::size_t(b)] * 1.0e+27;
-                const double f2 = p->Eeff / vol[std::size_t(b)] * 1.0e+30;
-                const std::size_t sidx = std::size_t(istep) + 1;
-                if (out->ed) out->ed[sidx * nbx + b] = f1 * hprops[3 * std::size_t(b)];
-                if (out->flux) {
-                    out->flux[(sidx * nbx + b) * 2] = f2 * hprops[3 * std::size_t(b) + 1];
-                    out->flux[(sidx * nbx + b) * 2 + 1] = f2 * hprops[3 * std::size_t(b) + 2];
-                }
-            }
-            if (out->nparticles) out->nparticles[istep + 1] = np;
+                                          B.d_phist.as<double>() + std::size_t(istep + 1) * nbx * 3);
+            be_counters<<<1, 1, 0, s>>>(dc, -1, 0, B.d_nhist.as<long long>(), istep + 1);
+            ck(cudaGetLastError(), "step launch");
+            ck(cudaEventRecord(ev[6], s), "event");
             if (p->on_step) {
                 hH.resize(std::size_t(nbx) * n);
-                ck(cudaMemcpyAsync(hH.data(), B.d_H.p, hH.size() * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
+                int herr[4];
+                long long hnp = 0;
+                ck(cudaMemcpyAsync(hH.data(), B.d_H.p, hbytes, cudaMemcpyDeviceToHost, s), "d2h");
+                ck(cudaMemcpyAsync(hprops.data(), B.d_phist.as<double>() + std::size_t(istep + 1) * nbx * 3,
+                                   hprops.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "d2h");
+                ck(cudaMemcpyAsync(&hnp, B.d_nhist.as<long long>() + istep + 1, sizeof hnp, cudaMemcpyDeviceToHost, s),
+                   "d2h");
+                ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
                 sync(c);
+                if (herr[0] != 0) throw_step_error(herr[0]);
                 std::vector<double> ed(static_cast<std::size_t>(nbx)), fl(std::size_t(nbx) * 2);
                 for (int b = 0; b < nbx; ++b) {
                     ed[std::size_t(b)] = p->Eeff / vol[std::size_t(b)] * 1.0e+27 * hprops[3 * std::size_t(b)];
@@ -1476,15 +1734,47 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                     fl[2 * std::size_t(b) + 1] = p->Eeff / vol[std::size_t(b)] * 1.0e+30 * hprops[3 * std::size_t(b) + 2];
                 }
                 const auto t_save = std::chrono::steady_clock::now();
-                p->on_step(p->user, istep + 1, time + p->dt, np, hH.data(), nbx, n, ed.data(), fl.data());
+                p->on_step(p->user, istep + 1, time + p->dt, hnp, hH.data(), nbx, n, ed.data(), fl.data());
                 phase[PH_SAVE] += 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t_save).count();
             }
-            if (herr[0] != 0)
-                throw Error(bte_status(herr[0]), herr[0] == BTE_ERR_LIMIT      ? "particle capacity or step cap exceeded"
-                                                 : herr[0] == BTE_ERR_GEOMETRY ? "geometry error in the advection"
-                                                                               : "particle without a propagator column");
             istep++;
             time += p->dt;
+        }
+        // the records of every step
+        {
+            int herr[4];
+            std::vector<double> ph(std::size_t(nsteps + 1) * nbx * 3);
+            std::vector<long long> nh(std::size_t(nsteps + 1));
+            std::vector<unsigned long long> hdc(DC_COUNT);
+            ck(cudaMemcpyAsync(ph.data(), B.d_phist.p, ph.size() * sizeof(double), cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(nh.data(), B.d_nhist.p, nh.size() * sizeof(long long), cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(hdc.data(), dc, DC_COUNT * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s), "d2h");
+            ck(cudaMemcpyAsync(herr, err, sizeof herr, cudaMemcpyDeviceToHost, s), "d2h");
+            sync(c);
+            if (herr[0] != 0) throw_step_error(herr[0]);
+            for (int st = 1; st <= istep; ++st) {
+                for (int b = 0; b < nbx; ++b) {
+                    const double f1 = p->Eeff / vol[std::size_t(b)] * 1.0e+27;
+                    const double f2 = p->Eeff / vol[std::size_t(b)] * 1.0e+30;
+                    const std::size_t q = (std::size_t(st) * nbx + std::size_t(b)) * 3;
+                    if (out->ed) out->ed[std::size_t(st) * nbx + b] = f1 * ph[q];
+                    if (out->flux) {
+                        out->flux[(std::size_t(st) * nbx + b) * 2] = f2 * ph[q + 1];
+                        out->flux[(std::size_t(st) * nbx + b) * 2 + 1] = f2 * ph[q + 2];
+                    }
+                }
+                if (out->nparticles) out->nparticles[st] = nh[std::size_t(st)];
+            }
+            psteps = (long long)hdc[DC_PSTEPS];
+            branchings = (long long)hdc[DC_FLIPS];
+            const int bucket[6] = {PH_ADV, PH_GEN, PH_SCAT, PH_HIST, PH_CANCEL, PH_PROPS};
+            for (int st = 0; st < istep; ++st)
+                for (int k = 0; k < 6; ++k) {
+                    float pms = 0.f;
+                    if (cudaEventElapsedTime(&pms, pev[std::size_t(st) * 7 + k], pev[std::size_t(st) * 7 + k + 1]) ==
+                        cudaSuccess)
+                        phase[bucket[k]] += pms;
+                }
         }
         ck(cudaEventRecord(c->ev1, s), "event");
         sync(c);

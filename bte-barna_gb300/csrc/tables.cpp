@@ -646,6 +646,11 @@ Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool
 
 GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry& g, double gx,
                                          double gy) {
+    return build_gradient_generators_boxes(m, g, std::vector<V2>(g.boxes.size(), v2(gx, gy)));
+}
+
+GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeometry& g,
+                                               const std::vector<V2>& grad) {
     GradGenerators R;
     const std::size_t n = m.n();
     const double vuc = m.V * g.thickness / m.c;
@@ -653,6 +658,10 @@ GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry&
     std::vector<signed char> sg(n);
     for (std::size_t s = 0; s < g.boxes.size(); ++s) {
         if (g.reservoir[s] || g.tto[s] >= 0) continue;
+        const double gx = grad[s].x, gy = grad[s].y;
+        // a box without a gradient has no source (source_term_gradient,
+        // src/beyondRTA_MC2d.cpp:626-628)
+        if (almost_equal(std::hypot(gx, gy), 0.)) continue;
         const double T = g.Teq[s];
         for (std::size_t k = 0; k < n; ++k) {
             const double vgradT = -(gx * m.vx[k] + gy * m.vy[k] + 0. * m.vz[k]);
@@ -683,6 +692,63 @@ GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry&
     }
     R.total_energy = wnorm;
     return R;
+}
+
+std::vector<V2> calculate_gradientT(const HostGeometry& g) {
+    std::vector<V2> out(g.boxes.size(), v2(0., 0.));
+    for (std::size_t s = 0; s < g.boxes.size(); ++s) {
+        if (g.reservoir[s] || g.tto[s] >= 0) continue;
+        const GBox& B = g.boxes[s];
+        // normal equations of the rows h_i = c_i - c_0, d_i = T_i - T_0 over
+        // the neighbours that are neither reservoirs nor periodic
+        double a = 0., b = 0., cc = 0., r0 = 0., r1 = 0.;
+        std::vector<int> seen;
+        for (int i = 0; i < B.ncontacts; ++i) {
+            const int o = g.contacts[std::size_t(B.contact_off + i)].id;
+            if (g.reservoir[std::size_t(o)] || g.tto[std::size_t(o)] >= 0) continue;
+            if (std::find(seen.begin(), seen.end(), o) != seen.end()) continue;
+            seen.push_back(o);
+            const double hx = g.boxes[std::size_t(o)].center.x - B.center.x;
+            const double hy = g.boxes[std::size_t(o)].center.y - B.center.y;
+            const double d = g.Teq[std::size_t(o)] - g.Teq[s];
+            a += hx * hx;
+            b += hx * hy;
+            cc += hy * hy;
+            r0 += hx * d;
+            r1 += hy * d;
+        }
+        if (seen.empty()) continue;
+        // minimum-norm least squares: the pseudo-inverse of H^T H through its
+        // eigenpairs, eigenvalues below 1e-12 of the largest taken as zero
+        // (neighbours on one line leave the orthogonal component at 0)
+        const double mid = 0.5 * (a + cc), rad = std::hypot(0.5 * (a - cc), b);
+        const double lam[2] = {mid + rad, mid - rad};
+        double gx = 0., gy = 0.;
+        for (int e = 0; e < 2; ++e) {
+            if (!(lam[e] > 1e-12 * lam[0])) continue;
+            double vx, vy;
+            if (b != 0.) {
+                vx = b;
+                vy = lam[e] - a;
+                if (std::hypot(vx, vy) == 0.) {
+                    vx = lam[e] - cc;
+                    vy = b;
+                }
+            } else {
+                const bool first = (a >= cc) == (e == 0);
+                vx = first ? 1. : 0.;
+                vy = first ? 0. : 1.;
+            }
+            const double nv = std::hypot(vx, vy);
+            vx /= nv;
+            vy /= nv;
+            const double proj = (vx * r0 + vy * r1) / lam[e];
+            gx += vx * proj;
+            gy += vy * proj;
+        }
+        out[s] = v2(gx, gy);
+    }
+    return out;
 }
 
 Generators build_initial_generators(const HostModes& m, const HostGeometry& g) {

@@ -127,6 +127,16 @@ struct GradGenerators {
 };
 GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry& g, double gx,
                                          double gy);
+// Nabla_T sources with a gradient per box (grad[box], K/nm); boxes without
+// a gradient get no source.
+GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeometry& g,
+                                               const std::vector<V2>& grad);
+// calculate_gradientT (src/geometry_2d.cpp:524-575): per box that is neither
+// a reservoir nor periodic, the least-squares gradient of Teq from the
+// centres of its neighbours of that kind, the minimum-norm one when they are
+// collinear (the reference solves with Eigen's complete orthogonal
+// decomposition); zero for every other box, K/nm.
+std::vector<V2> calculate_gradientT(const HostGeometry& g);
 // Distributions of the initial deviation per box (no particle counts).
 Generators build_initial_generators(const HostModes& m, const HostGeometry& g);
 // Particle counts per box for N particles (Ntogenerate stochastic rounding):
