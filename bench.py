@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--extra-seconds", type=float, default=30.0,
                     help="time cap of each arm of those summaries")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--berta-eeff", type=float, default=0.0,
+                    help="c2: this Eeff (J) instead of the calibration towards 1e7 particles alive; "
+                         "the line then lists the particles alive at every step of the first timed run")
     return ap.parse_args()
 
 
@@ -175,6 +178,26 @@ def profile_figures():
     return {}
 
 
+# be_advance: a particle read is x, y (FP64), mode, box, sign (int32): 28 B;
+# a particle written is the same 28 B plus the propagator column entry (or
+# resampling alias entry) drawn for it, 8 B.  The histogram's atomics hit
+# a 1.3 MB array that stays in L2.
+BE_IN_BYTES = 28
+BE_OUT_BYTES = 36
+
+
+def berta_profile_figures():
+    """ncu figures of be_advance from the committed capture summary: DRAM
+    bytes of one existing-particle launch per particle it read."""
+    p = os.path.join(REPO, "profiles", "be_advance_c2.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except (ValueError, OSError):
+            return {}
+    return {}
+
+
 # ----------------------------------------------------------------- CPU leg
 def cpu_sample(c, seconds, nthreads, seed=7, offset=0):
     """Time the restatement on a bounded slice of the workload's particles."""
@@ -246,8 +269,8 @@ def run_berta(args, rank, world, local):
     eng.load_propagator(P, 300.0)
     build_s = time.perf_counter() - t0
     dt, maxtime, target = 1.0, 99.0, 10_000_000
-    E = 1e-21
-    for _ in range(8):  # about 1 / Eeff, less where cancellation bites: iterate
+    E = args.berta_eeff if args.berta_eeff > 0 else 1e-21
+    for _ in range(0 if args.berta_eeff > 0 else 8):  # about 1 / Eeff, less where cancellation bites: iterate
         r = eng.berta_run(dt, maxtime, E, seed=7)
         n_end = int(r["nparticles"][-1])
         if n_end < 10_000:
@@ -267,6 +290,10 @@ def run_berta(args, rank, world, local):
     kern_ms = 0.0
     e2e_s = 0.0
     alive = []
+    adv_ms = 0.0
+    adv_bytes = 0.0
+    adv_in = 0
+    by_step = None
     for k in range(args.steps):
         flush.fill_(float(k))
         torch.cuda.synchronize()
@@ -276,10 +303,22 @@ def run_berta(args, rank, world, local):
         ps += int(r["particle_steps"])
         kern_ms += float(r["kernel_ms"])
         alive.append(int(r["nparticles"][-1]))
+        # be_advance: the advection and scattering phases (two launches a step)
+        adv_ms += r["phase_ms"]["advection"] + r["phase_ms"]["scattering"]
+        adv_bytes += BE_IN_BYTES * r["advance_in"] + BE_OUT_BYTES * r["advance_out"]
+        adv_in += int(r["advance_in"])
+        if by_step is None:
+            by_step = [int(v) for v in r["nparticles"]]
     torch.cuda.synchronize()
     clk = clocks.stop()
     nbx = int(c["geom"]["nboxes"])
     nsteps = btegpu.berta_steps(dt, maxtime)
+    launches = 2 * nsteps * args.steps
+    peak, peak_kind = measured_peaks()
+    achieved = adv_bytes / (adv_ms * 1e-3) / 1e9
+    prof = berta_profile_figures()
+    traffic = (prof["dram_bytes_per_particle_in"] * adv_in / launches
+               if prof.get("dram_bytes_per_particle_in") else None)
     line = {
         "metric": "beRTA particle-steps/s", "value": ps / (kern_ms * 1e-3), "unit": "particle-steps/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -295,8 +334,16 @@ def run_berta(args, rank, world, local):
         "e2e": {"value": ps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": (nsteps + 1) * (nbx * 3 + 1) * 8},
         "kernel_ms_per_step": kern_ms / args.steps,
+        "roofline": {"bound": "hbm", "kernel": "be_advance", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind + " (copy burst)",
+                     "traffic": traffic,
+                     "algorithmic_bytes_per_launch": adv_bytes / launches,
+                     "launch_ms": adv_ms / launches,
+                     "per_unit": f"{BE_IN_BYTES} B per particle read + {BE_OUT_BYTES} B per particle written"},
         "clocks": clk,
     }
+    if args.berta_eeff > 0:
+        line["nparticles_by_step"] = by_step
     print(json.dumps(line))
     eng.close()
     return 0
@@ -319,6 +366,48 @@ class SweepStats:
 
     def mean(self, i):
         return float(np.mean(self.k[i])) if self.k[i] else float("nan")
+
+
+class AdaptiveShares:
+    """Particle allocation from measured variances, for runs whose launches
+    deal their particles to G replica groups.  A case starts with a fraction
+    of its budget; each round adds its (particles, variance of the round's
+    mean) and the particle-weighted kappa mean; the next round gives it what
+    its pooled per-particle variance still asks for, with margin, and at
+    least a quarter of what it has used (an estimate from few groups may say
+    a case is nearly there while it is not)."""
+
+    def __init__(self, budgets, first_frac, nmin, tol, groups):
+        n = len(budgets)
+        self.G = groups
+        self.tol = tol
+        self.nmin = nmin
+        self.need = np.maximum(np.asarray(budgets, float) * first_frac, nmin)
+        self.w_sum = np.zeros(n)
+        self.wk_sum = np.zeros(n)
+        self.rounds = [[] for _ in range(n)]
+        self.kappa = np.full(n, np.nan)
+        self.rel = np.full(n, np.inf)
+
+    def alloc(self, i):
+        return max(self.need[i], self.nmin)
+
+    def add(self, i, n_i, kg):
+        """Adds one round of case i (n_i particles, per-group kappa kg);
+        returns True once 3 sigma / kappa <= tol."""
+        kg = np.asarray(kg, float)
+        self.rounds[i].append((n_i, kg.var(ddof=1) / self.G))
+        self.w_sum[i] += n_i
+        self.wk_sum[i] += n_i * kg.mean()
+        self.kappa[i] = self.wk_sum[i] / self.w_sum[i]
+        var = sum((n / self.w_sum[i]) ** 2 * v for n, v in self.rounds[i])
+        self.rel[i] = 3.0 * np.sqrt(var) / abs(self.kappa[i])
+        if self.rel[i] <= self.tol:
+            return True
+        s2 = np.mean([v * n for n, v in self.rounds[i]])
+        total = 9.0 * s2 / (self.tol * self.kappa[i]) ** 2
+        self.need[i] = max(1.3 * (total - self.w_sum[i]), 0.25 * self.w_sum[i], self.nmin)
+        return False
 
 
 def run_sweep(args, rank, world, local):
@@ -356,7 +445,9 @@ def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
     replica groups, so batch means exist after one launch, and each round
     gives each case, through its particle share, what its measured variance
     still asks for (a fraction of a budget in the first round); converged cases
-    drop out.  Table construction is outside both clocks.  Returns the line."""
+    drop out.  Plain adaptive: each case alone in per-case launches with the
+    batched arm's groups and allocation.  Table construction is outside
+    these clocks.  Returns the line."""
     import torch
     import btegpu
     import synth
@@ -386,12 +477,7 @@ def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
     per = ncells + 2
     active = np.ones(nc, dtype=bool)
     nmin = 2000.0 * G
-    need = np.maximum(budgets * first_frac, nmin)              # first round: a fraction of a budget
-    w_sum = np.zeros(nc)                                       # particles so far per case
-    wk_sum = np.zeros(nc)                                      # particle-weighted kappa sum
-    rounds_i = [[] for _ in range(nc)]                         # (particles, variance of the round mean)
-    kap_b = np.full(nc, np.nan)
-    rel_b = np.full(nc, np.inf)
+    ab = AdaptiveShares(budgets, first_frac, nmin, tol, G)
     ev_b = 0
     reps_b = 0
     parts_b = 0
@@ -399,7 +485,7 @@ def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     while active.any() and time.perf_counter() - t0 < cap:
-        alloc = np.where(active, np.maximum(need, nmin), 0.0)
+        alloc = np.array([ab.alloc(i) if active[i] else 0.0 for i in range(nc)])
         N = int(alloc.sum())
         ta = time.perf_counter()
         eng.load_materials(rates, Ts, alloc / alloc.sum())
@@ -417,25 +503,9 @@ def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
                           round(1e3 * (tc - tb), 1), round(1e3 * (td - tc), 1)])
         for i in np.flatnonzero(active):
             sl = slice(per * i, per * i + ncells)
-            kg = np.array([synth.sweep_kappa(x["jx"], sl, length=L) for x in grs])
-            n_i = alloc[i]
-            rounds_i[i].append((n_i, kg.var(ddof=1) / G))
-            w_sum[i] += n_i
-            wk_sum[i] += n_i * kg.mean()
-            kap_b[i] = wk_sum[i] / w_sum[i]
-            var = sum((n / w_sum[i]) ** 2 * v for n, v in rounds_i[i])
-            rel_b[i] = 3.0 * np.sqrt(var) / abs(kap_b[i])
-            if rel_b[i] <= tol:
+            kg = [synth.sweep_kappa(x["jx"], sl, length=L) for x in grs]
+            if ab.add(i, alloc[i], kg):
                 active[i] = False
-                continue
-            # per-particle variance pooled over the rounds, and the
-            # particles still needed for 3 sigma / kappa <= tol
-            s2 = np.mean([v * n for n, v in rounds_i[i]])
-            total = 9.0 * s2 / (tol * kap_b[i]) ** 2
-            # a round costs host work whatever its size, so a case is topped
-            # up with margin, and by at least a quarter of what it has used
-            # (its estimate may say it is nearly there while it is not)
-            need[i] = max(1.3 * (total - w_sum[i]), 0.25 * w_sum[i], nmin)
     t_b = time.perf_counter() - t0
     conv_b = int((~active).sum())
     eng.set_groups(0)
@@ -476,6 +546,36 @@ def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
         reps_p += k
         if t_p >= cap:
             break
+    # ---- plain, adaptive: each case alone in per-case launches, with the
+    # batched arm's replica groups and allocation, so that the comparison
+    # shows what one launch over all cases adds to the allocation
+    ad = AdaptiveShares(budgets, first_frac, nmin, tol, G)
+    t_a = 0.0
+    ev_a = 0
+    reps_a = 0
+    parts_a = 0
+    conv_a = 0
+    for i, cs in cases_iter:
+        e = engs[cs["T"]]
+        e.load_geometry(synth.sweep_ribbon(cs["width"], cs["T"], length=L, ncells=ncells))
+        e.rta_run(cs["T"], dt, maxtime, 1000, seed=2)         # tables for this geometry
+        e.set_groups(G)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        while t_a + (time.perf_counter() - t1) < cap:
+            n_i = int(ad.alloc(i))
+            r = e.rta_run(cs["T"], dt, maxtime, n_i, seed=7000 + reps_a, raw=False)
+            grs = [e.group_result(k, r["jx"].shape, keys=("jx",)) for k in range(G)]
+            ev_a += int(r["events"])
+            parts_a += n_i
+            reps_a += 1
+            if ad.add(i, n_i, [synth.sweep_kappa(x["jx"], slice(0, ncells), length=L) for x in grs]):
+                conv_a += 1
+                break
+        t_a += time.perf_counter() - t1
+        e.set_groups(0)
+        if t_a >= cap:
+            break
     for e in engs.values():
         e.close()
 
@@ -509,6 +609,7 @@ def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
     t_setup_b = time.perf_counter() - t3
     eng.close()
     clk = clocks.stop()
+    kap_b, rel_b = ab.kappa, ab.rel
     worst_b = float(np.max(rel_b))
     line = {
         "metric": "seconds to 1% kappa_eff (3 sigma) over the 64-case sweep, batched",
@@ -527,6 +628,10 @@ def sweep_arms(local, tol, cap, first_frac=0.25, groups=8, plain=True):
                   "events": ev_p,
                   "events_per_s": ev_p / max(t_p, 1e-9)},
         "speedup_plain_over_batched": (t_p / t_b) if (conv_b == nc and conv_p == nc) else None,
+        "plain_adaptive": {"seconds": t_a, "launches": reps_a, "particles": parts_a, "cases_converged": conv_a,
+                           "events": ev_a, "events_per_s": ev_a / max(t_a, 1e-9),
+                           "worst_3sigma_rel": float(np.max(ad.rel)) if conv_a else None},
+        "speedup_plain_adaptive_over_batched": (t_a / t_b) if (conv_b == nc and conv_a == nc) else None,
         "with_table_setup": {"batched_seconds": t_b + t_setup_b, "batched_setup_s": t_setup_b,
                              "plain_fresh_contexts_seconds": t_f, "plain_fresh_cases_converged": conv_f,
                              "speedup": (t_f / (t_b + t_setup_b)) if (conv_b == nc and conv_f == nc)

@@ -96,7 +96,8 @@ class BertaResult(C.Structure):
     _fields_ = [("nboxes", C.c_int32), ("nsteps", C.c_int32), ("ed", C.POINTER(C.c_double)),
                 ("flux", C.POINTER(C.c_double)), ("nparticles", C.POINTER(C.c_int64)),
                 ("histogram", C.POINTER(C.c_int32)), ("particle_steps", C.c_int64),
-                ("branchings", C.c_int64), ("kernel_ms", C.c_double), ("phase_ms", C.c_double * 8)]
+                ("branchings", C.c_int64), ("kernel_ms", C.c_double), ("phase_ms", C.c_double * 8),
+                ("advance_in", C.c_int64), ("advance_out", C.c_int64)]
 
 # the reference's beRTA timer buckets, in the order of bte_berta_result.phase_ms
 BERTA_PHASES = ("advection", "cancelling", "generators", "histogram", "properties", "read_data",
@@ -414,7 +415,8 @@ def _engine_berta_run(self, dt, maxtime, Eeff, T0=300.0, seed=1, rta=False, canc
     self._check(self.lib.bte_berta_run(self.ctx, C.byref(p), C.byref(r)))
     return {"ed": ed, "flux": flux, "nparticles": npart, "H": H, "nsteps": r.nsteps,
             "particle_steps": r.particle_steps, "branchings": r.branchings, "kernel_ms": r.kernel_ms,
-            "phase_ms": dict(zip(BERTA_PHASES, list(r.phase_ms)))}
+            "phase_ms": dict(zip(BERTA_PHASES, list(r.phase_ms))),
+            "advance_in": r.advance_in, "advance_out": r.advance_out}
 
 
 def _engine_steady_run(self, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_energy=-42.0,

@@ -81,6 +81,19 @@ struct PAlias {
     unsigned alt;  // bits 0-29 slot, bit 30 alt negative, bit 31 keep negative
 };
 
+// The scattering table of one box (Scattering, src/beyondRTA_MC2d.cpp:
+// 1130-1165): the alias table of the propagator tabulated at the box's Teq,
+// or the signed CDFs c1, c2 of the two tabulated temperatures T1 < T2 that
+// the reference picks for it, interpolated at T = Teq on the fly as lirp
+// (src/collision_operator.cpp:918-929) interpolates them; all null for a
+// box where nothing scatters (reservoirs, periodic boxes).
+struct BoxProp {
+    const PAlias* alias;
+    const double* c1;
+    const double* c2;
+    double T, T1, T2;
+};
+
 // Page-locked staging for the per-step uploads: a copy from pageable memory
 // may wait for the stream's earlier work, a copy from here does not.  Each
 // upload site has its own buffer, written again only after a later sync.
@@ -121,12 +134,12 @@ struct BertaState {
     // each), host copies kept for the interpolation of lirp
     std::map<double, std::vector<double>> props;
     long long props_version = 0;
-    // what the device holds: the alias table of the propagator at sel_T, or
-    // (sel_lirp) the interpolated signed CDF at sel_T
-    double sel_T = 0;
-    bool sel_lirp = false;
-    long long sel_version = -1;
-    DBuf d_palias, d_pcdf;
+    // device tables per tabulated temperature, built when a box asks for
+    // them: the alias table (a box at that Teq) and the signed CDF (an end
+    // of an interpolation); dropped when the propagators change
+    std::map<double, DBuf> dev_alias, dev_cdf;
+    long long dev_version = -1;
+    DBuf d_boxprop;                         // BoxProp per box
     long long cap = 0;
     DBuf a_x, a_y, a_mode, a_box, a_sign;   // particles
     DBuf b_x, b_y, b_mode, b_box, b_sign;   // compaction / scattering output
@@ -544,16 +557,25 @@ __device__ __forceinline__ void compact_body(PArr in, long long n, PArr out, uns
     }
 }
 
-// propagator_H::lower_bound (include/collision_operator.hpp:263-269): the
-// first entry whose |value| is not below u, by std::lower_bound's own
-// probing, so that an interpolated column whose |values| are not monotone
+// Entry k of the column interpolated at T: c1 + (T - T1) (c2 - c1) / (T2 - T1),
+// rounded step by step as the host's interpolation of the whole table is.
+__device__ __forceinline__ double lirp_at(const double* c1, const double* c2, int k, double T, double T1, double T2) {
+    const double a = __ldg(c1 + k), b = __ldg(c2 + k);
+    return __dadd_rn(a, __ddiv_rn(__dmul_rn(__dsub_rn(T, T1), __dsub_rn(b, a)), __dsub_rn(T2, T1)));
+}
+
+// propagator_H::lower_bound (include/collision_operator.hpp:263-269) over
+// the column interpolated at T: the first entry whose |value| is not below
+// u, by std::lower_bound's own probing (each probe interpolated when it is
+// read), so that an interpolated column whose |values| are not monotone
 // gives the same index as in the reference; clamped to the last entry.
-__device__ __forceinline__ int lower_bound_abs(const double* a, int n, double u) {
+__device__ __forceinline__ int lower_bound_abs_lirp(const double* c1, const double* c2, int n, double u, double T,
+                                                    double T1, double T2) {
     int lo = 0, cnt = n;
     while (cnt > 0) {
         const int step = cnt >> 1;
         const int it = lo + step;
-        if (fabs(__ldg(a + it)) < fabs(u)) {
+        if (fabs(lirp_at(c1, c2, it, T, T1, T2)) < fabs(u)) {
             lo = it + 1;
             cnt -= step + 1;
         } else {
@@ -615,7 +637,9 @@ __global__ void be_props(const int* H, int nmodes, const double* vx, const doubl
 
 // ------------------------------------------------ device-resident step
 // Counters of the step loop, kept on the device between kernels.
-enum { DC_NP = 0, DC_NOUT, DC_WORK, DC_FLIPS, DC_PSTEPS, DC_NGEN, DC_COUNT = 8 };
+// DC_IN and DC_OUTT sum the particles read and written by be_advance over
+// the run (the algorithmic traffic of its roofline).
+enum { DC_NP = 0, DC_NOUT, DC_WORK, DC_FLIPS, DC_PSTEPS, DC_NGEN, DC_IN, DC_OUTT, DC_COUNT = 8 };
 
 // A source planned on the device: where its particles start in the
 // particle arrays and how many there are.
@@ -648,12 +672,15 @@ constexpr unsigned BRANCH_CAP = 1u << 20;
 // particle written once.
 __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long long* n_in, PArr out,
                                                   unsigned long long* dc, long long ocap, int advect,
-                                                  AdvectArgs aa, int rta, const PAlias* pal, const double* pcdf,
+                                                  AdvectArgs aa, int rta, const PAlias* pal, const BoxProp* bprop,
                                                   int nm, const double* w, const float* rprob, const int* ralt,
                                                   int nmodes, unsigned long long skey, int* H, int* err) {
     const long long n = (long long)*n_in;
     const int lane = threadIdx.x & 31;
-    if (advect && blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(dc + DC_PSTEPS, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) {
+        if (advect) atomicAdd(dc + DC_PSTEPS, (unsigned long long)n);
+        atomicAdd(dc + DC_IN, (unsigned long long)n);
+    }
     unsigned long long flips = 0;
     int mode = 0, sign = 1, box = 0, col = 0;
     double x = 0., y = 0.;
@@ -714,20 +741,29 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
                 const float acc = float(g.next32() >> 8) * 0x1p-24f;
                 nmode = acc < __ldg(rprob + j) ? j : __ldg(ralt + j);
             }
-        } else if (act && valid && pcdf) {
-            const double* c = pcdf + (long long)col * nm;
-            const int im = lower_bound_abs(c, nm, g.uniform());
-            nmode = im + 3;
-            nsign = __ldg(c + im) > 0. ? sign : -sign;
         } else if (act && valid) {
-            const int j = int(mulhi32(g.next32(), uint32_t(nm)));
-            const float acc = float(g.next32() >> 8) * 0x1p-24f;
-            const PAlias e = pal[(long long)col * nm + j];
-            const bool keep = acc < e.prob;
-            const int slot = keep ? j : int(e.alt & 0x3fffffffu);
-            const bool neg = keep ? (e.alt >> 31) != 0u : ((e.alt >> 30) & 1u) != 0u;
-            nmode = slot + 3;
-            nsign = neg ? -sign : sign;
+            // one table for every box (pal), or the box's own
+            const PAlias* tab = pal ? pal : bprop[box].alias;
+            if (tab) {
+                const int j = int(mulhi32(g.next32(), uint32_t(nm)));
+                const float acc = float(g.next32() >> 8) * 0x1p-24f;
+                const PAlias e = tab[(long long)col * nm + j];
+                const bool keep = acc < e.prob;
+                const int slot = keep ? j : int(e.alt & 0x3fffffffu);
+                const bool neg = keep ? (e.alt >> 31) != 0u : ((e.alt >> 30) & 1u) != 0u;
+                nmode = slot + 3;
+                nsign = neg ? -sign : sign;
+            } else {
+                const BoxProp bp = bprop[box];
+                if (bp.c1) {
+                    const long long off = (long long)col * nm;
+                    const int im = lower_bound_abs_lirp(bp.c1 + off, bp.c2 + off, nm, g.uniform(), bp.T, bp.T1, bp.T2);
+                    nmode = im + 3;
+                    nsign = lirp_at(bp.c1 + off, bp.c2 + off, im, bp.T, bp.T1, bp.T2) > 0. ? sign : -sign;
+                } else {
+                    atomicCAS(err, 0, E_VALUE);  // a particle where nothing scatters
+                }
+            }
         }
         const unsigned m1 = __ballot_sync(0xffffffffu, act);
         unsigned long long wo = 0;
@@ -1006,7 +1042,10 @@ __global__ void be_compact_dev(PArr in, const unsigned long long* n_in, PArr out
 // dc[to] = dc[from]; record[step] = dc[DC_NP] after it.
 __global__ void be_counters(unsigned long long* dc, int to, int from, long long* record, int step) {
     if (to >= 0) dc[to] = dc[from];
-    if (record) record[step] = (long long)dc[DC_NP];
+    if (record) {  // the end of a step: its particles alive, and the outputs of its be_advance launches
+        record[step] = (long long)dc[DC_NP];
+        dc[DC_OUTT] += dc[DC_NOUT];
+    }
 }
 
 PArr arr(DBuf& x, DBuf& y, DBuf& m, DBuf& b, DBuf& s, long long off = 0) {
@@ -1132,55 +1171,86 @@ std::vector<double> signed_cumm(const std::vector<double>& P, int nm) {
     return c;
 }
 
-// The device tables of the propagator at Teq = T0 (Scattering,
-// src/beyondRTA_MC2d.cpp:1130-1165): the tabulated one when T0 is in the
-// table, sampled through per-column alias tables; otherwise lirp
-// (src/collision_operator.cpp:918-929) between the first tabulated
-// temperature above T0 and the next one -- both above T0, as the reference
-// picks them -- sampled through the interpolated signed CDF.
-void select_propagator(bte_ctx* c, bte::BertaState& B, double T0) {
+// The alias table of a propagator over |P| per column, with the signs of
+// the slot and of its alias in the alias word.
+std::vector<bte::PAlias> propagator_alias(const std::vector<double>& P, int nm) {
     using namespace bte;
-    if (B.sel_version == B.props_version && B.sel_T == T0) return;
-    const int nm = B.nm;
     const std::size_t nn = std::size_t(nm) * std::size_t(nm);
-    auto it = B.props.find(T0);
-    if (it != B.props.end()) {
-        const std::vector<double>& P = it->second;
-        std::vector<PAlias> tab(nn);
-        std::vector<double> w(static_cast<std::size_t>(nm));
-        std::vector<Alias> al(static_cast<std::size_t>(nm));
-        for (int j = 0; j < nm; ++j) {
-            const double* col = P.data() + std::size_t(j) * nm;
-            for (int i = 0; i < nm; ++i) w[std::size_t(i)] = std::fabs(col[i]);
-            alias_table(w.data(), nm, al.data());
-            for (int i = 0; i < nm; ++i) {
-                PAlias e;
-                e.prob = al[std::size_t(i)].prob;
-                const int alt = al[std::size_t(i)].alt;
-                e.alt = unsigned(alt) | (col[alt] < 0. ? (1u << 30) : 0u) | (col[i] < 0. ? (1u << 31) : 0u);
-                tab[std::size_t(j) * nm + std::size_t(i)] = e;
-            }
+    std::vector<PAlias> tab(nn);
+    std::vector<double> w(static_cast<std::size_t>(nm));
+    std::vector<Alias> al(static_cast<std::size_t>(nm));
+    for (int j = 0; j < nm; ++j) {
+        const double* col = P.data() + std::size_t(j) * nm;
+        for (int i = 0; i < nm; ++i) w[std::size_t(i)] = std::fabs(col[i]);
+        alias_table(w.data(), nm, al.data());
+        for (int i = 0; i < nm; ++i) {
+            PAlias e;
+            e.prob = al[std::size_t(i)].prob;
+            const int alt = al[std::size_t(i)].alt;
+            e.alt = unsigned(alt) | (col[alt] < 0. ? (1u << 30) : 0u) | (col[i] < 0. ? (1u << 31) : 0u);
+            tab[std::size_t(j) * nm + std::size_t(i)] = e;
         }
-        B.d_palias.upload(tab, c->stream);
-        B.sel_lirp = false;
-    } else {
-        auto m1 = B.props.lower_bound(T0);
-        const double Tlow = B.props.begin()->first;
-        if (m1 == B.props.end() || std::next(m1) == B.props.end() || T0 < Tlow)
-            throw Error(BTE_ERR_INPUT,
-                        "Extrapolation is not allowed: limit Tref between the min and max temperatures "
-                        "used in the propagator calculation");
-        const auto m2 = std::next(m1);
-        const double T1 = m1->first, T2 = m2->first;
-        const std::vector<double> c1 = signed_cumm(m1->second, nm), c2 = signed_cumm(m2->second, nm);
-        std::vector<double> pint(nn);
-        for (std::size_t i = 0; i < nn; ++i) pint[i] = c1[i] + (T0 - T1) * (c2[i] - c1[i]) / (T2 - T1);
-        B.d_pcdf.upload(pint, c->stream);
-        B.sel_lirp = true;
     }
+    return tab;
+}
+
+// The scattering table of every box at its Teq (Scattering,
+// src/beyondRTA_MC2d.cpp:1130-1165): the tabulated propagator when Teq is in
+// the table, sampled through per-column alias tables; otherwise lirp
+// (src/collision_operator.cpp:918-929) between the first tabulated
+// temperature above Teq and the next one -- both above Teq, as the
+// reference picks them -- sampled through the signed CDFs interpolated on
+// the fly.  Uploads the per-box BoxProp records; returns the alias table
+// every scattering box uses when they all use the same one, else null.
+const bte::PAlias* select_box_propagators(bte_ctx* c, bte::BertaState& B, const bte::HostGeometry& g) {
+    using namespace bte;
+    if (B.dev_version != B.props_version) {
+        B.dev_alias.clear();
+        B.dev_cdf.clear();
+        B.dev_version = B.props_version;
+    }
+    const int nm = B.nm;
+    auto alias_of = [&](double T) -> const PAlias* {
+        DBuf& d = B.dev_alias[T];
+        if (!d.p) d.upload(propagator_alias(B.props.at(T), nm), c->stream);
+        return d.as<PAlias>();
+    };
+    auto cdf_of = [&](double T) -> const double* {
+        DBuf& d = B.dev_cdf[T];
+        if (!d.p) d.upload(signed_cumm(B.props.at(T), nm), c->stream);
+        return d.as<double>();
+    };
+    const std::size_t nbx = g.boxes.size();
+    std::vector<BoxProp> bp(nbx, BoxProp{nullptr, nullptr, nullptr, 0., 0., 0.});
+    const PAlias* uniform = nullptr;
+    bool same = true, any = false;
+    const double Tlow = B.props.begin()->first;
+    for (std::size_t b = 0; b < nbx; ++b) {
+        if (g.reservoir[b] || g.tto[b] >= 0) continue;
+        const double Teq = g.Teq[b];
+        BoxProp& r = bp[b];
+        r.T = Teq;
+        if (B.props.count(Teq)) {
+            r.alias = alias_of(Teq);
+        } else {
+            const auto m1 = B.props.lower_bound(Teq);
+            if (m1 == B.props.end() || std::next(m1) == B.props.end() || Teq < Tlow)
+                throw Error(BTE_ERR_INPUT,
+                            "Extrapolation is not allowed: limit Tref between the min and max temperatures "
+                            "used in the propagator calculation");
+            const auto m2 = std::next(m1);
+            r.T1 = m1->first;
+            r.T2 = m2->first;
+            r.c1 = cdf_of(r.T1);
+            r.c2 = cdf_of(r.T2);
+        }
+        if (!any) uniform = r.alias;
+        else if (r.alias != uniform) same = false;
+        any = true;
+    }
+    B.d_boxprop.upload(bp, c->stream);
     sync(c);
-    B.sel_T = T0;
-    B.sel_version = B.props_version;
+    return same ? uniform : nullptr;
 }
 
 std::size_t n_to_generate(double gen, bte::Pcg64& rng) {
@@ -1231,18 +1301,19 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         const HostModes& m = c->modes;
         const HostGeometry& g = c->geom;
         if (c->nmat > 0) throw Error(BTE_ERR_INPUT, "materials are for transient batched runs");
-        // one temperature for the scattering tables: every box that is
-        // neither a reservoir nor periodic at T0, so the gradients of the
-        // boxes' Teq (calculate_gradientT, src/geometry_2d.cpp:524-575) are
-        // zero and only a homogeneous <gradient> adds a source term
-        for (std::size_t b = 0; b < g.boxes.size(); ++b)
-            if (!g.reservoir[b] && g.tto[b] < 0 && g.Teq[b] != p->T0)
-                throw Error(BTE_ERR_INPUT, "every box needs Teq = T0 (one scattering temperature per run)");
+        // RTA scattering uses the mode table's rates, given at T0 only: every
+        // box that scatters needs Teq = T0.  With the propagator each box
+        // scatters at its own Teq.
+        if (p->rta)
+            for (std::size_t b = 0; b < g.boxes.size(); ++b)
+                if (!g.reservoir[b] && g.tto[b] < 0 && g.Teq[b] != p->T0)
+                    throw Error(BTE_ERR_INPUT, "RTA scattering needs Teq = T0 in every box (rates at T0 only)");
         if (p->gradient_mode != 0 && p->gradient_mode != 1) throw Error(BTE_ERR_INPUT, "bad gradient_mode");
         if (p->gradient_mode == 1 && !(std::isfinite(p->gradient[0]) && std::isfinite(p->gradient[1])))
             throw Error(BTE_ERR_INPUT, "gradient must be finite");
+        const PAlias* pal = nullptr;
         if (p->rta) ensure_resample(c, p->T0);
-        else select_propagator(c, *c->berta, p->T0);
+        else pal = select_box_propagators(c, *c->berta, g);
         if (!c->berta) c->berta = new BertaState();
         BertaState& B = *c->berta;
         const int n = int(m.n());
@@ -1369,13 +1440,17 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             d.cdf = -1;
             return d;
         };
-        // the gradient source term: a homogeneous <gradient> on every box
-        // that is neither a reservoir nor periodic (the gradients of the
-        // boxes' Teq are zero here); Nabla_T rows at each box's Teq, built
-        // once as the reference's static generators are
-        GradGenerators grad;
-        if (p->gradient_mode == 1 && !almost_equal(std::hypot(p->gradient[0], p->gradient[1]), 0.)) {
-            grad = build_gradient_generators(m, g, p->gradient[0], p->gradient[1]);
+        // the gradient source term (source_term_gradient,
+        // src/beyondRTA_MC2d.cpp:597-676): a homogeneous <gradient> on every
+        // box that is neither a reservoir nor periodic, or the least-squares
+        // gradients of the boxes' Teq (calculate_gradientT, the reference's
+        // default, src/beyondRTA_MC2d.cpp:1441-1458); Nabla_T rows at each
+        // box's Teq for the boxes with a gradient, built once as the
+        // reference's static generators are
+        GradGenerators grad = p->gradient_mode == 1
+                                  ? build_gradient_generators(m, g, p->gradient[0], p->gradient[1])
+                                  : build_gradient_generators_boxes(m, g, calculate_gradientT(g));
+        if (!grad.box.empty()) {
             std::vector<float> gp(grad.alias.size());
             std::vector<int> ga(grad.alias.size());
             for (std::size_t i = 0; i < grad.alias.size(); ++i) {
@@ -1483,7 +1558,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             np = first;
         }
         props(np, 0);
-        long long psteps = 0, branchings = 0;
+        long long psteps = 0, branchings = 0, adv_in = 0, adv_out = 0;
         // ---- the step loop, resident on the device: particle numbers stay in
         // device counters, the sources are planned on the device, and the
         // step's properties are recorded there; the host synchronises only
@@ -1602,8 +1677,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         }
         const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
         const unsigned pblocks = unsigned(c->nsm) * 8u;  // persistent grids of the step kernels
-        const PAlias* pal = p->rta ? nullptr : B.d_palias.as<PAlias>();
-        const double* pcdf = (!p->rta && B.sel_lirp) ? B.d_pcdf.as<double>() : nullptr;
+        const BoxProp* bprop = p->rta ? nullptr : B.d_boxprop.as<BoxProp>();
         int istep = 0;
         double time = 0.;
         // phase timing (the reference's timer buckets): events at the phase
@@ -1641,7 +1715,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                                     general, mix_key(p->seed, istep, 31), err, TT};
             be_advance<<<pblocks, 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP,
                                                arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc, cap, 1, a_step,
-                                               p->rta, pal, pcdf, B.nm, c->d_w.as<double>(),
+                                               p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
                                                c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
                                                mix_key(p->seed, istep, 64), B.d_H.as<int>(), err);
             ck(cudaEventRecord(ev[1], s), "event");
@@ -1690,7 +1764,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             // scattered and counted in the histogram, appended to B
             ck(cudaMemsetAsync(dc + DC_WORK, 0, sizeof(unsigned long long), s), "memset");
             be_advance<<<pblocks, 256, 0, s>>>(A, dc + DC_NGEN, arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc,
-                                               cap, 0, a_step, p->rta, pal, pcdf, B.nm, c->d_w.as<double>(),
+                                               cap, 0, a_step, p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
                                                c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
                                                mix_key(p->seed, istep, 65), B.d_H.as<int>(), err);
             ck(cudaEventRecord(ev[3], s), "event");
@@ -1767,6 +1841,8 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             psteps = (long long)hdc[DC_PSTEPS];
             branchings = (long long)hdc[DC_FLIPS];
+            adv_in = (long long)hdc[DC_IN];
+            adv_out = (long long)hdc[DC_OUTT];
             const int bucket[6] = {PH_ADV, PH_GEN, PH_SCAT, PH_HIST, PH_CANCEL, PH_PROPS};
             for (int st = 0; st < istep; ++st)
                 for (int k = 0; k < 6; ++k) {
@@ -1786,6 +1862,8 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         out->nsteps = istep;
         out->particle_steps = psteps;
         out->branchings = branchings;
+        out->advance_in = adv_in;
+        out->advance_out = adv_out;
         out->kernel_ms = ms;
         for (int k = 0; k < 8; ++k) out->phase_ms[k] = phase[k];
         return BTE_OK;

@@ -696,59 +696,71 @@ GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeo
 
 std::vector<V2> calculate_gradientT(const HostGeometry& g) {
     std::vector<V2> out(g.boxes.size(), v2(0., 0.));
+    std::vector<double> hx, hy, d;
     for (std::size_t s = 0; s < g.boxes.size(); ++s) {
         if (g.reservoir[s] || g.tto[s] >= 0) continue;
         const GBox& B = g.boxes[s];
-        // normal equations of the rows h_i = c_i - c_0, d_i = T_i - T_0 over
-        // the neighbours that are neither reservoirs nor periodic
-        double a = 0., b = 0., cc = 0., r0 = 0., r1 = 0.;
-        std::vector<int> seen;
+        // rows h_i = c_i - c_0, d_i = T_i - T_0 over the neighbours that are
+        // neither reservoirs nor periodic (contacts are unique per neighbour)
+        hx.clear();
+        hy.clear();
+        d.clear();
         for (int i = 0; i < B.ncontacts; ++i) {
             const int o = g.contacts[std::size_t(B.contact_off + i)].id;
             if (g.reservoir[std::size_t(o)] || g.tto[std::size_t(o)] >= 0) continue;
-            if (std::find(seen.begin(), seen.end(), o) != seen.end()) continue;
-            seen.push_back(o);
-            const double hx = g.boxes[std::size_t(o)].center.x - B.center.x;
-            const double hy = g.boxes[std::size_t(o)].center.y - B.center.y;
-            const double d = g.Teq[std::size_t(o)] - g.Teq[s];
-            a += hx * hx;
-            b += hx * hy;
-            cc += hy * hy;
-            r0 += hx * d;
-            r1 += hy * d;
+            hx.push_back(g.boxes[std::size_t(o)].center.x - B.center.x);
+            hy.push_back(g.boxes[std::size_t(o)].center.y - B.center.y);
+            d.push_back(g.Teq[std::size_t(o)] - g.Teq[s]);
         }
-        if (seen.empty()) continue;
-        // minimum-norm least squares: the pseudo-inverse of H^T H through its
-        // eigenpairs, eigenvalues below 1e-12 of the largest taken as zero
-        // (neighbours on one line leave the orthogonal component at 0)
-        const double mid = 0.5 * (a + cc), rad = std::hypot(0.5 * (a - cc), b);
-        const double lam[2] = {mid + rad, mid - rad};
-        double gx = 0., gy = 0.;
-        for (int e = 0; e < 2; ++e) {
-            if (!(lam[e] > 1e-12 * lam[0])) continue;
-            double vx, vy;
-            if (b != 0.) {
-                vx = b;
-                vy = lam[e] - a;
-                if (std::hypot(vx, vy) == 0.) {
-                    vx = lam[e] - cc;
-                    vy = b;
-                }
-            } else {
-                const bool first = (a >= cc) == (e == 0);
-                vx = first ? 1. : 0.;
-                vy = first ? 0. : 1.;
-            }
-            const double nv = std::hypot(vx, vy);
-            vx /= nv;
-            vy /= nv;
-            const double proj = (vx * r0 + vy * r1) / lam[e];
-            gx += vx * proj;
-            gy += vy * proj;
-        }
-        out[s] = v2(gx, gy);
+        out[s] = min_norm_lstsq2(hx, hy, d);
     }
     return out;
+}
+
+V2 min_norm_lstsq2(const std::vector<double>& hx, const std::vector<double>& hy, const std::vector<double>& d) {
+    // Minimum-norm least squares of [hx hy] g = d, as a complete orthogonal
+    // decomposition does it: QR with column pivoting (the column of larger
+    // norm first, Gram-Schmidt for the second), the rank from |R_ii| above
+    // diag_size * epsilon * |R_11|, and for rank 1 the minimum-norm
+    // solution along the first row of R.
+    const std::size_t m = hx.size();
+    if (m == 0) return v2(0., 0.);
+    double n0 = 0., n1 = 0.;
+    for (std::size_t i = 0; i < m; ++i) {
+        n0 += hx[i] * hx[i];
+        n1 += hy[i] * hy[i];
+    }
+    const bool swap = n1 > n0;
+    const std::vector<double>& c1 = swap ? hy : hx;
+    const std::vector<double>& c2 = swap ? hx : hy;
+    const double r11 = std::sqrt(swap ? n1 : n0);
+    if (!(r11 > 0.)) return v2(0., 0.);
+    std::vector<double> q1(m), q2(m);
+    double r12 = 0., b1 = 0.;
+    for (std::size_t i = 0; i < m; ++i) {
+        q1[i] = c1[i] / r11;
+        r12 += q1[i] * c2[i];
+        b1 += q1[i] * d[i];
+    }
+    double r22s = 0.;
+    for (std::size_t i = 0; i < m; ++i) {
+        q2[i] = c2[i] - r12 * q1[i];
+        r22s += q2[i] * q2[i];
+    }
+    const double r22 = std::sqrt(r22s);
+    const double diag = double(std::min<std::size_t>(m, 2));
+    double x1, x2;
+    if (m >= 2 && r22 > diag * std::numeric_limits<double>::epsilon() * r11) {
+        double b2 = 0.;
+        for (std::size_t i = 0; i < m; ++i) b2 += (q2[i] / r22) * d[i];
+        x2 = b2 / r22;
+        x1 = (b1 - r12 * x2) / r11;
+    } else {
+        const double t = b1 / (r11 * r11 + r12 * r12);
+        x1 = r11 * t;
+        x2 = r12 * t;
+    }
+    return swap ? v2(x2, x1) : v2(x1, x2);
 }
 
 Generators build_initial_generators(const HostModes& m, const HostGeometry& g) {

@@ -137,6 +137,9 @@ GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeo
 // collinear (the reference solves with Eigen's complete orthogonal
 // decomposition); zero for every other box, K/nm.
 std::vector<V2> calculate_gradientT(const HostGeometry& g);
+// The minimum-norm least-squares solution g of rows (hx_i, hy_i) . g = d_i
+// (zero without rows).
+V2 min_norm_lstsq2(const std::vector<double>& hx, const std::vector<double>& hy, const std::vector<double>& d);
 // Distributions of the initial deviation per box (no particle counts).
 Generators build_initial_generators(const HostModes& m, const HostGeometry& g);
 // Particle counts per box for N particles (Ntogenerate stochastic rounding):

@@ -187,7 +187,11 @@ typedef struct bte_berta_params {
     double dt;               /* time step, ps                                    */
     double maxtime;          /* the loop runs while time <= maxtime              */
     double Eeff;             /* energy per particle, J (<Eeff Ed=...>)          */
-    double T0;               /* equilibrium temperature of the boxes, K          */
+    double T0;               /* temperature of the mode table's rates, K: with
+                                rta = 1 every box that scatters needs Teq = T0;
+                                with the propagator each box scatters at its own
+                                Teq (the tabulated propagator, or lirp between
+                                the two tabulated temperatures above it)      */
     uint64_t seed;
     int32_t mode;            /* BTE_MODE_PRODUCTION                              */
     int32_t rta;             /* 1: RTA scattering (<RTA/>), 0: propagator        */
@@ -196,7 +200,9 @@ typedef struct bte_berta_params {
                                 src/beyondRTA_MC2d.cpp:597-676):
                                 0: gradients from the boxes' Teq
                                    (calculate_gradientT, the reference's
-                                   default; zero while every box has Teq = T0)
+                                   default: the minimum-norm least-squares
+                                   gradient over each box's neighbours; zero
+                                   where they share its Teq)
                                 1: the homogeneous <gradient x y> below on
                                    every box that is neither a reservoir nor
                                    periodic                                 */
@@ -223,6 +229,9 @@ typedef struct bte_berta_result {
                                 generators, histogram, properties, read_data, saving,
                                 scattering; device time per step phase, host time
                                 for read_data (set-up) and saving (on_step)     */
+    int64_t advance_in;      /* out: particles read by the fused step kernel, summed
+                                over its launches (existing and new particles)  */
+    int64_t advance_out;     /* out: particles it wrote (outgoing after scattering) */
 } bte_berta_result;
 
 /* Parameters of a steady-state run of a periodic structure under an applied

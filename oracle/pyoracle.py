@@ -108,8 +108,22 @@ def load():
     lib.oracle_kat_bounce.restype = C.c_int
     lib.oracle_kat_prop_cumm.argtypes = [dp, C.c_int, C.c_int, dp]
     lib.oracle_kat_lirp.argtypes = [dp, dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp]
+    lib.oracle_kat_gradientT.argtypes = [mtp, C.POINTER(_bt.Geometry), dp]
+    lib.oracle_kat_gradientT.restype = C.c_int
     _lib = lib
     return lib
+
+
+def gradient_T(modes, geom):
+    """calculate_gradientT of the restatement: [box, 2] K/nm."""
+    lib = load()
+    ms, k1 = _bt.mode_struct(modes)
+    gs, k2 = _bt.geom_struct(geom)
+    out = np.zeros((int(geom["nboxes"]), 2))
+    st = lib.oracle_kat_gradientT(C.byref(ms), C.byref(gs), out.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    return out
 
 
 def timegrid(dt, maxtime):

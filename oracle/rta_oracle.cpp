@@ -45,6 +45,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <numeric>
 #include <stdexcept>
@@ -1267,6 +1268,107 @@ inline std::vector<GradGen> build_gradient(const Sim& S, double gx, double gy) {
     return out;
 }
 
+// Nabla_T sources with one gradient per box (source_term_gradient,
+// src/beyondRTA_MC2d.cpp:626-647): a box whose gradient is zero
+// (almost_equal on its norm) has none.
+inline std::vector<GradGen> build_gradient_boxes(const Sim& S, const std::vector<V2>& grad) {
+    const Modes& m = S.m;
+    const double vuc = m.V * S.thickness / m.c;
+    std::vector<GradGen> out;
+    for (auto& s : S.sys) {
+        if (s.reservoir || s.periodic) continue;
+        const V2 g = grad[s.id];
+        if (almost_equal(std::sqrt(g.x * g.x + g.y * g.y), 0.)) continue;
+        GradGen G;
+        G.box = s.id;
+        std::vector<double> pmf;
+        double cumulsum = nabla_t_pmf(m, g.x, g.y, s.Teq, pmf, G.sign);
+        double vol = s.area * S.thickness / vuc;
+        G.energy = dist_energy(vol, cumulsum, double(m.nq));
+        G.vol = vol;
+        G.cumulsum = cumulsum;
+        G.cdf = fill_cumulative(pmf);
+        out.push_back(std::move(G));
+    }
+    return out;
+}
+
+// calculate_gradientT, src/geometry_2d.cpp:524-575: for each box that is
+// neither a reservoir nor periodic, the rows h_i = c_i - c_0 and
+// d_i = Teq_i - Teq_0 over its contacts of that kind, and the
+// minimum-norm least-squares solution of h g = d, which the reference gets
+// from Eigen's CompleteOrthogonalDecomposition: Householder QR with column
+// pivoting, the rank from |R_ii| > min(rows, 2) eps |R_11|, and, for rank 1,
+// the minimum-norm solution along R's first row.
+inline V2 cod_solve(std::vector<std::array<double, 2>> h, std::vector<double> d) {
+    const std::size_t m = h.size();
+    if (m == 0) return V2{0., 0.};
+    double nrm[2] = {0., 0.};
+    for (auto& r : h) {
+        nrm[0] += r[0] * r[0];
+        nrm[1] += r[1] * r[1];
+    }
+    const int p0 = nrm[1] > nrm[0] ? 1 : 0, p1 = 1 - p0;
+    // Householder reflection of column p0 onto e1, applied to both columns and d
+    auto reflect = [&](std::size_t k, int col) -> double {
+        double sig = 0.;
+        for (std::size_t i = k; i < m; ++i) sig += h[i][col] * h[i][col];
+        const double alpha = -std::copysign(std::sqrt(sig), h[k][col]);
+        if (sig == 0.) return 0.;
+        std::vector<double> v(m, 0.);
+        for (std::size_t i = k; i < m; ++i) v[i] = h[i][col];
+        v[k] -= alpha;
+        double vv = 0.;
+        for (std::size_t i = k; i < m; ++i) vv += v[i] * v[i];
+        if (vv == 0.) return alpha;
+        for (int c = 0; c < 2; ++c) {
+            double t = 0.;
+            for (std::size_t i = k; i < m; ++i) t += v[i] * h[i][c];
+            t = 2. * t / vv;
+            for (std::size_t i = k; i < m; ++i) h[i][c] -= t * v[i];
+        }
+        double t = 0.;
+        for (std::size_t i = k; i < m; ++i) t += v[i] * d[i];
+        t = 2. * t / vv;
+        for (std::size_t i = k; i < m; ++i) d[i] -= t * v[i];
+        return alpha;
+    };
+    const double r11 = reflect(0, p0);
+    if (r11 == 0.) return V2{0., 0.};
+    const double r12 = h[0][p1];
+    double r22 = 0.;
+    if (m >= 2) r22 = reflect(1, p1);
+    const double thr = double(std::min<std::size_t>(m, 2)) * std::numeric_limits<double>::epsilon() * std::fabs(r11);
+    double x[2];
+    if (m >= 2 && std::fabs(r22) > thr) {
+        x[p1] = d[1] / r22;
+        x[p0] = (d[0] - r12 * x[p1]) / r11;
+    } else {
+        // rank 1: the solutions of r11 x0 + r12 x1 = d0; the one of least norm
+        const double t = d[0] / (r11 * r11 + r12 * r12);
+        x[p0] = r11 * t;
+        x[p1] = r12 * t;
+    }
+    return V2{x[0], x[1]};
+}
+
+inline std::vector<V2> calculate_gradientT(const Sim& S) {
+    std::vector<V2> out(S.sys.size(), V2{0., 0.});
+    for (auto& s : S.sys) {
+        if (s.reservoir || s.periodic) continue;
+        std::vector<std::array<double, 2>> h;
+        std::vector<double> d;
+        for (auto& [c, b] : s.contacts) {
+            const Box& o = S.sys[c];
+            if (o.reservoir || o.periodic) continue;
+            h.push_back({o.center.x - s.center.x, o.center.y - s.center.y});
+            d.push_back(o.Teq - s.Teq);
+        }
+        out[s.id] = cod_solve(h, d);
+    }
+    return out;
+}
+
 struct SteadyGen {
     std::vector<GradGen> grad;
     std::vector<double> grad_cum;
@@ -1590,6 +1692,8 @@ struct BeRun {
     bool rta = false;
     int nm = 0;                       // propagator size (modes minus the 3 Gamma acoustic)
     std::vector<double> cumm;         // signed cumulative per column, column-major
+    std::vector<const double*> box_cumm;  // per box: the table it scatters with
+    std::vector<std::vector<double>> cumms; // the tables of the boxes' Teq
     std::vector<double> resample_cdf; // RTA resampling at T (BE_derivative_distribution)
     double dt = 0, maxtime = 0, Eeff = 0;
     std::vector<std::vector<int>> Eborder;   // per box, per border
@@ -1648,7 +1752,16 @@ inline void build_cumm(BeRun& R, const double* P) {
 }
 
 // propagator_H::get: lower_bound on |cumm| (abs_less), sign of the entry,
-// index + 3.
+// index + 3; `tab` is the table (column-major nm x nm signed CDFs).
+inline std::pair<int, std::size_t> prop_get_tab(const BeRun& R, const double* tab, std::size_t col, double u) {
+    const double* c = tab + col * std::size_t(R.nm);
+    const double* it = std::lower_bound(c, c + R.nm, u,
+                                        [](double a, double b) { return std::fabs(a) < std::fabs(b); });
+    std::size_t im = std::size_t(it - c);
+    if (im >= std::size_t(R.nm)) im = std::size_t(R.nm) - 1;
+    return {c[im] > 0. ? 1 : -1, im + 3};
+}
+
 inline std::pair<int, std::size_t> prop_get(const BeRun& R, std::size_t col, double u) {
     const double* c = &R.cumm[col * std::size_t(R.nm)];
     const double* it = std::lower_bound(c, c + R.nm, u,
@@ -2252,6 +2365,22 @@ void oracle_kat_lirp(const double* P1, const double* P2, int n, int col, double 
         out[i] = orc::lirp_value(A.cumm[o + std::size_t(i)], B.cumm[o + std::size_t(i)], T1, T2, Tx);
 }
 
+// calculate_gradientT (src/geometry_2d.cpp:524-575) of the geometry's
+// boxes: out[2 * box + {0, 1}], K/nm.
+int oracle_kat_gradientT(const bte_mode_table* mt, const bte_geometry* gm, double* out) {
+    try {
+        const orc::Sim S = build_sim(mt, gm);
+        const auto g = orc::calculate_gradientT(S);
+        for (std::size_t i = 0; i < g.size(); ++i) {
+            out[2 * i] = g[i].x;
+            out[2 * i + 1] = g[i].y;
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
 // Spectral locations for the following oracle_rta_run calls (nloc = 0: off).
 void oracle_set_spectral(int nloc, const int* boxes) {
     g_spec_boxes.assign(boxes, boxes + (nloc > 0 ? nloc : 0));
@@ -2788,23 +2917,40 @@ int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const
             const std::size_t nn = std::size_t(nmP) * std::size_t(nmP);
             std::map<double, const double*> tab;
             for (int i = 0; i < nprop; ++i) tab[Ts[i]] = P + std::size_t(i) * nn;
-            const auto hit = tab.find(bp->T0);
-            if (hit != tab.end()) {
-                orc::build_cumm(R, hit->second);
-            } else {
-                const auto m1 = tab.lower_bound(bp->T0);
-                if (m1 == tab.end() || std::next(m1) == tab.end() || bp->T0 < tab.begin()->first)
-                    return fail(BTE_ERR_INPUT, "Extrapolation is not allowed");
-                const auto m2 = std::next(m1);
-                orc::BeRun R2;
-                R2.nm = nmP;
-                orc::build_cumm(R, m1->second);
-                orc::build_cumm(R2, m2->second);
-                const double T1 = m1->first, T2 = m2->first;
-                for (std::size_t i = 0; i < nn; ++i)
-                    R.cumm[i] = orc::lirp_value(R.cumm[i], R2.cumm[i], T1, T2, bp->T0);
+            // the table of each box's Teq: the tabulated one, or lirp between
+            // the first tabulated temperature above Teq and the next one
+            std::map<double, std::size_t> of_T;
+            for (auto& s : S.sys) {
+                if (s.reservoir || s.periodic || of_T.count(s.Teq)) continue;
+                orc::BeRun R1;
+                R1.nm = nmP;
+                const auto hit = tab.find(s.Teq);
+                if (hit != tab.end()) {
+                    orc::build_cumm(R1, hit->second);
+                } else {
+                    const auto m1 = tab.lower_bound(s.Teq);
+                    if (m1 == tab.end() || std::next(m1) == tab.end() || s.Teq < tab.begin()->first)
+                        return fail(BTE_ERR_INPUT, "Extrapolation is not allowed");
+                    const auto m2 = std::next(m1);
+                    orc::BeRun R2;
+                    R2.nm = nmP;
+                    orc::build_cumm(R1, m1->second);
+                    orc::build_cumm(R2, m2->second);
+                    const double T1 = m1->first, T2 = m2->first;
+                    for (std::size_t i = 0; i < nn; ++i)
+                        R1.cumm[i] = orc::lirp_value(R1.cumm[i], R2.cumm[i], T1, T2, s.Teq);
+                }
+                of_T[s.Teq] = R.cumms.size();
+                R.cumms.push_back(std::move(R1.cumm));
             }
+            R.box_cumm.assign(nbx, nullptr);
+            for (auto& s : S.sys)
+                if (!s.reservoir && !s.periodic) R.box_cumm[s.id] = R.cumms[of_T.at(s.Teq)].data();
         } else {
+            // the mode table's rates are given at T0 only
+            for (auto& s : S.sys)
+                if (!s.reservoir && !s.periodic && s.Teq != bp->T0)
+                    return fail(BTE_ERR_INPUT, "RTA scattering needs Teq = T0 in every box");
             R.resample_cdf = orc::fill_cumulative(orc::be_derivative_pmf(m, m.w, bp->T0));
         }
         for (auto& b : S.sys) {
@@ -2877,11 +3023,16 @@ int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const
         };
         // gradient source term (source_term_gradient, src/beyondRTA_MC2d.cpp:
         // 597-676): the homogeneous <gradient> on every box that is neither a
-        // reservoir nor periodic; the generators are built once
+        // reservoir nor periodic, or (the default, :1441-1458) the gradients
+        // of the boxes' Teq from calculate_gradientT; the generators are
+        // built once
         std::vector<orc::GradGen> grad;
-        if (bp->gradient_mode == 1 &&
-            !orc::almost_equal(std::hypot(bp->gradient[0], bp->gradient[1]), 0.))
-            grad = orc::build_gradient(S, bp->gradient[0], bp->gradient[1]);
+        if (bp->gradient_mode == 1) {
+            if (!orc::almost_equal(std::hypot(bp->gradient[0], bp->gradient[1]), 0.))
+                grad = orc::build_gradient(S, bp->gradient[0], bp->gradient[1]);
+        } else {
+            grad = orc::build_gradient_boxes(S, orc::calculate_gradientT(S));
+        }
         while (time <= R.maxtime) {
             // 1. advection
             for (auto& p : parts) orc::be_evolve(R, p, orc::get_v(m, p.mode), R.dt, rng_);
@@ -2993,7 +3144,9 @@ int oracle_berta_run_tab(const bte_mode_table* mt, const bte_geometry* gm, const
                     for (auto& p : elements) {
                         if (p.mode < 3) throw orc::value_error("Gamma acoustic particle has no propagator column");
                         const double u = orc::canonical(rng_);
-                        auto sol = orc::prop_get(R, p.mode - 3, u);
+                        const double* t = R.box_cumm[p.box];
+                        if (!t) throw orc::value_error("particle where nothing scatters");
+                        auto sol = orc::prop_get_tab(R, t, p.mode - 3, u);
                         const int newsign = (p.sign * sol.first) < 0 ? -1 : 1;
                         orc::BeParticle s1 = p;
                         s1.mode = sol.second;

@@ -235,6 +235,34 @@ def test_berta_interpolated_propagator_agrees_with_restatement(engine):
         e2.close()
 
 
+def test_berta_box_temperatures_agree_with_restatement(engine):
+    """Cells at 299.6 ... 300.4 K with propagators tabulated at 299.0,
+    300.0, 300.2, 300.6 and 301.0 K: the cells at 300.0 and 300.2 K take
+    their tabulated propagators (one alias table each), the other three
+    interpolate (lirp drawn on the fly, between the two tabulated
+    temperatures above them); the default source term injects the Teq
+    profile's least-squares gradients.  Energy density and flux against
+    the restatement."""
+    from parity_stats import check
+    m, g, _ = _case()
+    g["Teq"][:5] = [299.6, 299.8, 300.0, 300.2, 300.4]
+    g["Tinit"][:5] = g["Teq"][:5]
+    tab = {T: synth.propagator(m, T=T) for T in (299.0, 300.0, 300.2, 300.6, 301.0)}
+    engine.load_modes(m)
+    engine.load_geometry(g)
+    for T, P in tab.items():
+        engine.load_propagator(P, T)
+    R = 6
+    kw = dict(dt=1.0, maxtime=30.0, Eeff=2e-23, T0=300.0)
+    names = [f"ed_cell{i}" for i in range(5)] + ["flux_x"]
+    gpu = np.array([_obs(engine.berta_run(seed=10 + i, **kw)) for i in range(R)])
+    cpu = np.array([_obs(pyoracle.berta_run(m, g, tab, seed=20 + i, **kw)) for i in range(R)])
+    check(gpu, cpu, names, "beRTA box temperatures")
+    # RTA scattering has the mode table's rates at T0 only
+    with pytest.raises(btegpu.BteError, match="Teq = T0"):
+        engine.berta_run(1.0, 5.0, 2e-23, T0=300.0, rta=True)
+
+
 def test_berta_phase_times(engine, built, tmp_path):
     """The reference's timer buckets: device time per step phase, which add
     up to no more than the device time of the loop; the CLI prints the
