@@ -352,6 +352,13 @@ struct GContact {
     int pad;
     V2 np;      // normal of the contact border seen from this box
 };
+// An interval (lo, hi) of r0.u for the translations out of one periodic box
+// in which the translated segment meets contact ci of the target box and
+// no other candidate.
+struct TransFast {
+    double lo, hi;
+    int ci, pad;
+};
 struct GBox {
     V2 center;
     double area;

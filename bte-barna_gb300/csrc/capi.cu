@@ -66,6 +66,15 @@ void ensure_static(bte_ctx* c) {
         c->d_cseg.upload(g.contact_seg, c->stream);
         c->d_transl.upload(g.translation, c->stream);
         c->d_boxmat.upload(g.mat, c->stream);
+        {
+            const bte::TranslationFast tf = bte::build_translation_fast(g);
+            c->have_tfast = !tf.iv.empty();
+            if (c->have_tfast) {
+                c->d_tfast.upload(tf.iv, c->stream);
+                c->d_tfast_rng.upload(tf.rng, c->stream);
+                c->d_tfast_u.upload(tf.u, c->stream);
+            }
+        }
         if (g.rect_grid) {
             c->d_gx.upload(g.gx, c->stream);
             c->d_gy.upload(g.gy, c->stream);
@@ -137,6 +146,20 @@ void ensure_static(bte_ctx* c) {
         std::vector<int> mir = bte::build_mirror(m, g);
         c->have_mirror = std::any_of(mir.begin(), mir.end(), [](int x) { return x >= 0; });
         c->d_mirror.upload(mir, c->stream);
+        // exit times of the convex-polygon path without a division: 1 / (n.v)
+        // per border normal and mode, -1 where such a border is not left
+        // (n.v <= 0); only for tables of at most 256 MB
+        const std::size_t n = m.n(), ncl = g.normals.size();
+        c->d_invden.release();
+        if (ncl > 0 && ncl * n * sizeof(double) <= (std::size_t(256) << 20)) {
+            std::vector<double> inv(ncl * n);
+            for (std::size_t k = 0; k < ncl; ++k)
+                for (std::size_t j = 0; j < n; ++j) {
+                    const double den = g.normals[k].x * m.vxc[j] + g.normals[k].y * m.vyc[j];
+                    inv[k * n + j] = den > 0. ? 1.0 / den : -1.0;
+                }
+            c->d_invden.upload(inv, c->stream);
+        }
         sync(c);
         c->lambert_dev = true;
         if (c->verbose)
@@ -826,6 +849,9 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         T.contacts = c->d_contacts.as<bte::GContact>();
         T.cseg = c->d_cseg.as<bte::V2>();
         T.translation = c->d_transl.as<bte::V2>();
+        T.tfast = c->have_tfast ? c->d_tfast.as<bte::TransFast>() : nullptr;
+        T.tfast_rng = c->d_tfast_rng.as<int2>();
+        T.tfast_u = c->d_tfast_u.as<bte::V2>();
         T.nclass = c->nclass;
         T.row_ptr = c->d_row_ptr.as<long long>();
         T.lcol = c->d_lcol.as<int>();
@@ -901,7 +927,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
                                      c->d_work.as<unsigned long long>(), c->nsm, c->stream);
         } else {
             const bte::PolyArgs A{c->d_pborders.as<bte::PolyBorder>(), c->d_ppieces.as<bte::PolyPiece>(),
-                                  c->d_mv.as<bte::ModeVel>()};
+                                  c->d_mv.as<bte::ModeVel>(), c->d_invden.as<double>()};
             if (!bte::launch_prod_poly(T, A, c->d_tally.as<double>(), counters, err,
                                        c->d_work.as<unsigned long long>(), c->nsm, c->stream))
                 throw Error(BTE_ERR_CUDA, "polygon kernel does not fit on the device");
@@ -1170,6 +1196,9 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
     T.contacts = c->d_contacts.as<GContact>();
     T.cseg = c->d_cseg.as<V2>();
     T.translation = c->d_transl.as<V2>();
+    T.tfast = c->have_tfast ? c->d_tfast.as<TransFast>() : nullptr;
+    T.tfast_rng = c->d_tfast_rng.as<int2>();
+    T.tfast_u = c->d_tfast_u.as<V2>();
     T.nclass = c->nclass;
     T.row_ptr = c->d_row_ptr.as<long long>();
     T.lcol = c->d_lcol.as<int>();
@@ -1247,6 +1276,9 @@ void fill_static_tables(bte_ctx* c, DevTables& T) {
     T.contacts = c->d_contacts.as<GContact>();
     T.cseg = c->d_cseg.as<V2>();
     T.translation = c->d_transl.as<V2>();
+    T.tfast = c->have_tfast ? c->d_tfast.as<TransFast>() : nullptr;
+    T.tfast_rng = c->d_tfast_rng.as<int2>();
+    T.tfast_u = c->d_tfast_u.as<V2>();
     T.nclass = c->nclass;
     T.row_ptr = c->d_row_ptr.as<long long>();
     T.lcol = c->d_lcol.as<int>();

@@ -75,6 +75,9 @@ struct bte_ctx {
     bool modes_dev = false, geom_dev = false, lambert_dev = false;
     bte::DBuf d_vxc, d_vyc, d_w, d_tau, d_mv;
     bte::DBuf d_boxes, d_hull, d_borders, d_contacts, d_cseg, d_transl;
+    bte::DBuf d_tfast, d_tfast_rng, d_tfast_u;  // translations without a search
+    bool have_tfast = false;
+    bte::DBuf d_invden;                           // 1 / (n.v) per normal class and mode
     bte::DBuf d_gx, d_gy, d_gcell, d_boxcell;
     bte::DBuf d_pborders, d_ppieces;  // convex-polygon path (geometries that are not a grid)
     bte::DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;

@@ -72,6 +72,9 @@ struct PolyArgs {
     const PolyBorder* pb;     // [global border index]
     const PolyPiece* pieces;
     const ModeVel* mv;
+    // 1 / (n.v) per border normal class and mode ([nclass][n], -1 where the
+    // flight does not leave through such a border); null: divide per pass
+    const double* inv_den;
 };
 
 // Adjoint passes of the grid kernel: the functional's weights per tally

@@ -50,6 +50,13 @@ struct DevTables {
     const GContact* contacts;
     const V2* cseg;         // [contact][2]: lengthened contact segment (sbl)
     const V2* translation;  // [box]: <Translate_to> vector of periodic boxes
+    // translations that need no search (build_translation_fast): per
+    // periodic box, the unit normal u of its translation and the intervals
+    // of r0.u in which the translated segment meets exactly one candidate
+    // contact; null: none
+    const TransFast* tfast;
+    const int2* tfast_rng;  // [box]: first interval, count
+    const V2* tfast_u;      // [box]
     int nclass;
     // Lambert rows
     const long long* row_ptr;
@@ -253,6 +260,29 @@ __device__ int translate(const DevTables& T, P& pol, int box, V2 r0, V2 v, int& 
     if (tib < 0 || tib >= T.nboxes || almost_equal(norm(tj), 0.)) return E_GEOM;
     const V2 p1 = add(r0, tj);
     const GBox& TB = T.boxes[tib];
+    if (FAST && T.tfast) {
+        // away from the ends of the contacts' intervals exactly one contact
+        // of the target box qualifies, and it is the one the segment
+        // crosses: the search below would find it alone and return the
+        // crossing point, with no draw
+        const int2 rg = T.tfast_rng[box];
+        if (rg.y > 0) {
+            const V2 uh = T.tfast_u[box];
+            const double u = uh.x * r0.x + uh.y * r0.y;
+            for (int k = 0; k < rg.y; ++k) {
+                const TransFast f = T.tfast[rg.x + k];
+                if (u > f.lo && u < f.hi) {
+                    V2 xin;
+                    if (seg_meet(r0, p1, T.cseg[2 * f.ci], T.cseg[2 * f.ci + 1], xin)) {
+                        nbox = T.contacts[f.ci].id;
+                        rf = xin;
+                        return 0;
+                    }
+                    break;
+                }
+            }
+        }
+    }
     V2 tp;
     bool found = false;
     for (int k = 0; k < TB.nborders && !found; ++k) {

@@ -1188,20 +1188,38 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         // num / den over the borders with den = n.v > 0, num = c - n.x >= 0
         const GBox& B = T.boxes[p.box];
         int best = -1;
-        double bnum = 0., bden = 1.;
-        for (int k = 0; k < B.nborders; ++k) {
-            const PolyBorder& L = A.pb[B.border_off + k];
-            const double den = L.nx * mv.vx + L.ny * mv.vy;
-            if (!(den > 0.)) continue;
-            double num = L.c - (L.nx * p.pos.x + L.ny * p.pos.y);
-            num = num > 0. ? num : 0.;
-            if (best < 0 || num * bden < bnum * den) {
-                best = k;
-                bnum = num;
-                bden = den;
+        double te = HUGE_VAL;
+        if (A.inv_den) {
+            // 1 / den from the table of the border's normal class: one
+            // multiplication per border, compared as integers (both >= 0)
+            const double* inv = A.inv_den + p.mode;
+            for (int k = 0; k < B.nborders; ++k) {
+                const PolyBorder& L = A.pb[B.border_off + k];
+                const double iv = __ldg(inv + (long long)L.cls * T.n);
+                double num = L.c - (L.nx * p.pos.x + L.ny * p.pos.y);
+                num = num > 0. ? num : 0.;
+                const double tk = num * iv;
+                if (iv > 0. && ob(tk) < ob(te)) {
+                    best = k;
+                    te = tk;
+                }
             }
+        } else {
+            double bnum = 0., bden = 1.;
+            for (int k = 0; k < B.nborders; ++k) {
+                const PolyBorder& L = A.pb[B.border_off + k];
+                const double den = L.nx * mv.vx + L.ny * mv.vy;
+                if (!(den > 0.)) continue;
+                double num = L.c - (L.nx * p.pos.x + L.ny * p.pos.y);
+                num = num > 0. ? num : 0.;
+                if (best < 0 || num * bden < bnum * den) {
+                    best = k;
+                    bnum = num;
+                    bden = den;
+                }
+            }
+            te = best >= 0 ? bnum / bden : HUGE_VAL;
         }
-        double te = best >= 0 ? bnum / bden : HUGE_VAL;
         // time bins that end before the flight end and the exit border are
         // closed here, without a pass each: advance to the bin end, flush
         // the pending tally, open the next bin (two FMAs per bin instead of

@@ -763,6 +763,72 @@ V2 min_norm_lstsq2(const std::vector<double>& hx, const std::vector<double>& hy,
     return swap ? v2(x2, x1) : v2(x1, x2);
 }
 
+TranslationFast build_translation_fast(const HostGeometry& g, double margin) {
+    TranslationFast R;
+    const std::size_t nbx = g.boxes.size();
+    R.rng.assign(nbx, IntPair{0, 0});
+    R.u.assign(nbx, v2(0., 0.));
+    for (std::size_t P = 0; P < nbx; ++P) {
+        const int tb = g.tto[P];
+        if (tb < 0) continue;
+        const V2 t = g.translation[P];
+        const double tn = std::hypot(t.x, t.y);
+        if (!(tn > 0.)) continue;
+        const V2 u = v2(-t.y / tn, t.x / tn);
+        // every candidate contact's interval of r.u, its ends widened by
+        // the margin (a point contact is an interval of zero length)
+        struct Span {
+            double lo, hi;
+            int ci;
+        };
+        std::vector<Span> sp;
+        const GBox& TB = g.boxes[std::size_t(tb)];
+        for (int i = 0; i < TB.ncontacts; ++i) {
+            const int ci = TB.contact_off + i;
+            const int id = g.contacts[std::size_t(ci)].id;
+            if (id == tb || g.tto[std::size_t(id)] >= 0 || g.reservoir[std::size_t(id)]) continue;
+            const V2 a = g.contact_seg[2 * std::size_t(ci)], b = g.contact_seg[2 * std::size_t(ci) + 1];
+            const double ua = u.x * a.x + u.y * a.y, ub = u.x * b.x + u.y * b.y;
+            sp.push_back(Span{std::min(ua, ub), std::max(ua, ub), ci});
+        }
+        // the parts of each interval farther than the margin from every
+        // candidate's ends and covered by no other candidate
+        std::vector<double> cut;
+        for (auto& s : sp) {
+            cut.push_back(s.lo - margin);
+            cut.push_back(s.lo + margin);
+            cut.push_back(s.hi - margin);
+            cut.push_back(s.hi + margin);
+        }
+        std::sort(cut.begin(), cut.end());
+        R.rng[P].x = int(R.iv.size());
+        R.u[P] = u;
+        for (std::size_t k = 0; k + 1 < cut.size(); ++k) {
+            const double lo = cut[k], hi = cut[k + 1];
+            if (!(hi > lo)) continue;
+            const double mid = 0.5 * (lo + hi);
+            int owner = -1, cover = 0;
+            bool near_end = false;
+            for (auto& s : sp) {
+                if (std::fabs(mid - s.lo) < margin || std::fabs(mid - s.hi) < margin) near_end = true;
+                if (mid > s.lo && mid < s.hi) {
+                    ++cover;
+                    owner = s.ci;
+                }
+            }
+            if (near_end || cover != 1) continue;
+            if (!R.iv.empty() && int(R.iv.size()) > R.rng[P].x && R.iv.back().ci == owner &&
+                R.iv.back().hi == lo) {
+                R.iv.back().hi = hi;  // the same contact on both sides of a cut
+                continue;
+            }
+            R.iv.push_back(TransFast{lo, hi, owner, 0});
+        }
+        R.rng[P].y = int(R.iv.size()) - R.rng[P].x;
+    }
+    return R;
+}
+
 Generators build_initial_generators(const HostModes& m, const HostGeometry& g) {
     Generators R;
     const std::size_t n = m.n();

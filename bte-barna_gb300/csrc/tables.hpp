@@ -54,6 +54,23 @@ struct HostGeometry {
     std::vector<int> gcell;        // [gnx * gny], i-major
 };
 
+// Translations that need no search (geometry_2d::translate,
+// include/geometry_2d.hpp:366-493): for each periodic box P with target TB
+// and translation t, the unit normal u of t and the intervals of r0.u
+// (r0 the entry point into P) in which the segment r0 -> r0 + 1.0005 t
+// can meet exactly one candidate contact of TB (neither TB itself, a
+// periodic box nor a reservoir), kept `margin` nm away from the ends of
+// every candidate's interval.  rng[box] = (first interval, count).
+struct IntPair {  // the layout of int2
+    int x, y;
+};
+struct TranslationFast {
+    std::vector<TransFast> iv;
+    std::vector<IntPair> rng;
+    std::vector<V2> u;
+};
+TranslationFast build_translation_fast(const HostGeometry& g, double margin = 1.0e-2);
+
 // Alias entry of a Lambert row: pick slot j, keep its mode with probability
 // prob, else take alt (Walker / Vose).
 struct AliasRow {
