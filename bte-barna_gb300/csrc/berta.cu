@@ -146,7 +146,7 @@ struct BertaState {
     DBuf d_H, d_cnt, d_Eb, d_props, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
-    DBuf d_ne, d_ctot;                      // n(omega, T0) per mode; wall-CDF chunk sums
+    DBuf d_ctot;                            // wall-CDF chunk sums
     Pinned h_gens[1];                       // staging: descriptors of the initial particles
     // device-resident step loop: counters, planned sources, per-step records
     DBuf d_dc, d_span, d_gdesc, d_ggenf, d_gcnt, d_idesc, d_igenf, d_icnt, d_adi, d_adesc, d_acnt;
@@ -412,15 +412,33 @@ __device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& 
 // Isothermal_wall_distribution (src/sampling.cpp:189-269) of each request:
 // pmf_k = v_n omega_k |n(omega_k, Tw) - n(omega_k, Te)| for v_n > 0, turned
 // into a CDF row; tot[r] keeps the sum.  Each request's row is split into
-// chunks of WCDF_CHUNK modes, one block each, so that every SM's FP64 units
-// take part.  ne[k] = n(omega_k, Te_ref) is precomputed: a request at that
-// Te needs one exponential per mode instead of two.
+// chunks of WCDF_CHUNK modes, one block each.
+//
+// The pmf is evaluated in FP32 and summed in FP64: with x = hbar omega / kT,
+// n_w - n_e = expm1(x_e - x_w) / (expm1(x_e) (-expm1(-x_w))), which has no
+// cancellation when Tw is close to Te; when |x_e - x_w| >= 1/2 the plain
+// difference 1/expm1(x_w) - 1/expm1(x_e) loses nothing either.  Entries
+// above 1e-6 of the row's largest are within 4e-6 relative of the FP64
+// value, all entries above 1e-30 of it within 1e-5 (the rounding of x to
+// FP32 at x ~ 60), and the FP64 units do one addition per mode instead of
+// two exponentials and two divisions.
 constexpr int WCDF_CHUNK = 1024;
 
+__device__ __forceinline__ float wall_pmf_f(float w, float vn, float ce, float q, float rr) {
+    const float xe = ce * w;   // x_e
+    const float xw = xe * q;   // x_w = x_e Te / Tw
+    const float d = xe * rr;   // x_e - x_w = x_e (Tw - Te) / Tw
+    float diff;
+    if (fabsf(d) < 0.5f)
+        diff = xe < 80.f ? expm1f(d) / (expm1f(xe) * -expm1f(-xw)) : 0.f;
+    else
+        diff = 1.f / expm1f(xw) - 1.f / expm1f(xe);
+    return vn * w * fabsf(diff);
+}
+
 // pass 1: the chunk's running sums in place and its total
-__device__ __forceinline__ void wall_cdf1_body(const double* om, const double* vx, const double* vy,
-                                               const double* ne, double Te_ref, int n, const WallReq* req,
-                                               double* cdf, double* chunk_tot) {
+__device__ __forceinline__ void wall_cdf1_body(const float* om, const float* vx, const float* vy, int n,
+                                               const WallReq* req, double* cdf, double* chunk_tot) {
     __shared__ double part[256];
     const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
     const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
@@ -430,18 +448,14 @@ __device__ __forceinline__ void wall_cdf1_body(const double* om, const double* v
     const int seg = (c1 - c0 + blockDim.x - 1) / blockDim.x;
     const int k0 = c0 + threadIdx.x * seg, k1 = min(c1, k0 + seg);
     constexpr double pre = 1e12 * 1.054571726e-34 / 1.3806488e-23;
-    const bool pre_e = R.Te == Te_ref;
+    const float ce = float(pre / R.Te), q = float(R.Te / R.Tw), rr = float((R.Tw - R.Te) / R.Tw);
+    const float nx = float(R.nx), ny = float(R.ny);
     double acc = 0.;
     for (int k = k0; k < k1; ++k) {
-        const double w = om[k];
-        const double vn = R.nx * vx[k] + R.ny * vy[k];
-        double p = 0.;
-        if (vn > 0. && !almost_equal(0., w)) {
-            const double nw = 1. / (exp(pre * w / R.Tw) - 1.);
-            const double nE = pre_e ? ne[k] : 1. / (exp(pre * w / R.Te) - 1.);
-            p = vn * w * fabs(nw - nE);
-        }
-        acc += p;
+        const float w = __ldg(om + k);  // 0 where almost_equal(0, omega)
+        const float vn = nx * __ldg(vx + k) + ny * __ldg(vy + k);
+        const float p = (vn > 0.f && w != 0.f) ? wall_pmf_f(w, vn, ce, q, rr) : 0.f;
+        acc += double(p);
         row[k] = acc;  // running sum within the thread's segment
     }
     part[threadIdx.x] = acc;
@@ -536,24 +550,50 @@ __global__ void be_generate(PArr P, long long base, long long n, const GenDesc* 
 }
 
 // Append the live particles of [0, n) to `out` (warp-aggregated).
+// Compaction of [0, n): each block takes tiles of 4 x blockDim particles,
+// counts its survivors with warp ballots and claims their places with one
+// atomic per tile (the order inside a tile is kept).
+constexpr int COMPACT_ITEMS = 4;
 __device__ __forceinline__ void compact_body(PArr in, long long n, PArr out, unsigned long long* count) {
-    const int lane = threadIdx.x & 31;
-    for (long long base = blockIdx.x * (long long)blockDim.x; base < n;
-         base += (long long)gridDim.x * blockDim.x) {
-        const long long i = base + threadIdx.x;
-        const bool live = i < n && in.mode[i] >= 0;
-        const unsigned m = __ballot_sync(0xffffffffu, live);
-        unsigned long long w = 0;
-        if (lane == 0 && m) w = atomicAdd(count, (unsigned long long)__popc(m));
-        w = __shfl_sync(0xffffffffu, w, 0);
-        if (live) {
-            const long long o = (long long)w + __popc(m & ((1u << lane) - 1u));
-            out.x[o] = in.x[i];
-            out.y[o] = in.y[i];
-            out.mode[o] = in.mode[i];
-            out.box[o] = in.box[i];
-            out.sign[o] = in.sign[i];
+    __shared__ unsigned wcnt[COMPACT_ITEMS][32];
+    __shared__ unsigned long long tile_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const long long tile = (long long)COMPACT_ITEMS * blockDim.x;
+    for (long long base = blockIdx.x * tile; base < n; base += (long long)gridDim.x * tile) {
+        bool live[COMPACT_ITEMS];
+        unsigned m[COMPACT_ITEMS];
+#pragma unroll
+        for (int k = 0; k < COMPACT_ITEMS; ++k) {
+            const long long i = base + (long long)k * blockDim.x + threadIdx.x;
+            live[k] = i < n && in.mode[i] >= 0;
+            m[k] = __ballot_sync(0xffffffffu, live[k]);
+            if (lane == 0) wcnt[k][warp] = __popc(m[k]);
         }
+        __syncthreads();
+        if (threadIdx.x == 0) {  // exclusive offsets of (item, warp) in tile order
+            unsigned tot = 0;
+            for (int k = 0; k < COMPACT_ITEMS; ++k)
+                for (int w = 0; w < nw; ++w) {
+                    const unsigned c = wcnt[k][w];
+                    wcnt[k][w] = tot;
+                    tot += c;
+                }
+            tile_base = tot ? atomicAdd(count, (unsigned long long)tot) : 0ull;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < COMPACT_ITEMS; ++k) {
+            if (live[k]) {
+                const long long i = base + (long long)k * blockDim.x + threadIdx.x;
+                const long long o = (long long)(tile_base + wcnt[k][warp]) + __popc(m[k] & ((1u << lane) - 1u));
+                out.x[o] = in.x[i];
+                out.y[o] = in.y[i];
+                out.mode[o] = in.mode[i];
+                out.box[o] = in.box[i];
+                out.sign[o] = in.sign[i];
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -592,16 +632,24 @@ __global__ void be_hist(PArr P, long long n, int* H, int nmodes) {
 }
 
 // Cancellation: a particle survives when its sign is the sign of H at its
-// (box, mode) and its rank among those particles is below |H|.  Threads
-// visit the particles in the order of a random affine permutation
-// t -> (a t + b) mod n (a coprime to n), so the ranks, and with them the
-// survivors, do not follow the order of the particle list.
+// (box, mode) and its rank among those particles is below |H|.  Warps visit
+// the particles in chunks of 32 consecutive ones: chunk c in the order of a
+// random affine permutation w -> (a w + b) mod nchunks (a coprime to
+// nchunks), and the lanes the chunk's particles in the order of a random
+// XOR mask of the chunk, so the ranks, and with them the survivors, do not
+// follow the order of the particle list, while every read stays coalesced.
 __device__ __forceinline__ void cancel_body(PArr P, long long n, const int* H, int* cnt, int nmodes,
-                                            const int* reservoir, unsigned long long pa, unsigned long long pb) {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long i = (long long)((unsigned __int128)(pa % (unsigned long long)n) * (unsigned long long)t %
-                                        (unsigned long long)n + pb % (unsigned long long)n) % n;
+                                            const int* reservoir, unsigned long long pa, unsigned long long pb,
+                                            unsigned mkey) {
+    const unsigned long long nch = (unsigned long long)((n + 31) >> 5);
+    const int lane = threadIdx.x & 31;
+    const unsigned long long gw = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    for (unsigned long long w = gw; w < nch; w += nwarps) {
+        const unsigned long long c = (pa * w + pb) % nch;
+        const unsigned mask = ((unsigned)c * 0x9E3779B1u + mkey) >> 27;
+        const long long i = (long long)(c << 5) + (long long)((unsigned)lane ^ mask);
+        if (i >= n) continue;
         const long long key = (long long)P.box[i] * nmodes + P.mode[i];
         const int h = H[key];
         const int s = P.sign[i];
@@ -998,12 +1046,12 @@ __global__ void be_generate_dev(PArr P, const SrcSpan* span, const GenDesc* gens
 
 // The wall-CDF passes over every border, for the borders the step planned
 // (cnt > 0); rows of the others are left as they are.
-__global__ void __launch_bounds__(256) be_wall_cdf1_dev(const double* om, const double* vx, const double* vy,
-                                                        const double* ne, double Te_ref, int n, const WallReq* req,
-                                                        const long long* cnt, double* cdf, double* chunk_tot) {
+__global__ void __launch_bounds__(256) be_wall_cdf1_dev(const float* om, const float* vx, const float* vy, int n,
+                                                        const WallReq* req, const long long* cnt, double* cdf,
+                                                        double* chunk_tot) {
     const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
     if (cnt[blockIdx.x / nch] == 0) return;
-    wall_cdf1_body(om, vx, vy, ne, Te_ref, n, req, cdf, chunk_tot);
+    wall_cdf1_body(om, vx, vy, n, req, cdf, chunk_tot);
 }
 __global__ void __launch_bounds__(256) be_wall_cdf2_dev(int n, const long long* cnt, const double* chunk_tot,
                                                         double* cdf, double* tot) {
@@ -1026,12 +1074,24 @@ __global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, const int*
                               const int* reservoir, unsigned long long key) {
     const long long n = (long long)*n_in;
     if (n <= 0) return;
-    Philox q;
-    q.init(key, 0);
-    unsigned long long pa = ((unsigned long long)q.next32() << 32 | q.next32()) | 1ull;
-    const unsigned long long pb = (unsigned long long)q.next32() << 32 | q.next32();
-    while (gcd_u64((unsigned long long)n, pa % (unsigned long long)n) != 1ull) pa += 2;
-    cancel_body(P, n, H, cnt, nmodes, reservoir, pa, pb);
+    // the permutation's a, b and the XOR key, drawn by one thread per block
+    __shared__ unsigned long long s_ab[2];
+    __shared__ unsigned s_mkey;
+    if (threadIdx.x == 0) {
+        const unsigned long long nch = (unsigned long long)((n + 31) >> 5);
+        Philox q;
+        q.init(key, 0);
+        unsigned long long pa = ((unsigned long long)q.next32() << 32 | q.next32()) % nch;
+        const unsigned long long pb = ((unsigned long long)q.next32() << 32 | q.next32()) % nch;
+        if (pa == 0) pa = 1;
+        for (int t = 0; t < 64 && gcd_u64(nch, pa) != 1ull; ++t) pa = pa + 1 < nch ? pa + 1 : 1;
+        if (gcd_u64(nch, pa) != 1ull) pa = 1;  // 1 is coprime to every nch
+        s_ab[0] = pa;
+        s_ab[1] = pb;
+        s_mkey = q.next32();
+    }
+    __syncthreads();
+    cancel_body(P, n, H, cnt, nmodes, reservoir, s_ab[0], s_ab[1], s_mkey);
 }
 
 // Compaction of [0, *n_in) with the survivors counted into *count.
@@ -1472,15 +1532,17 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             B.d_isoprob.upload(ip, s);
             B.d_isoalt.upload(ia, s);
-            B.d_om.upload(m.omega, s);
-            B.d_vx.upload(m.vx, s);
-            B.d_vy.upload(m.vy, s);
-            // n(omega, T0) of every mode for the adiabatic re-emission rows
-            std::vector<double> ne(m.omega.size(), 0.);
-            const double pre = 1e12 * 1.054571726e-34 / 1.3806488e-23;
-            for (std::size_t k = 0; k < ne.size(); ++k)
-                if (m.omega[k] > 0.) ne[k] = 1. / (std::exp(pre * m.omega[k] / p->T0) - 1.);
-            B.d_ne.upload(ne, s);
+            // FP32 copies for the adiabatic walls' pmf (omega = 0 where
+            // almost_equal(0, omega): those modes take no part)
+            std::vector<float> omf(m.omega.size()), vxf(m.omega.size()), vyf(m.omega.size());
+            for (std::size_t k = 0; k < omf.size(); ++k) {
+                omf[k] = almost_equal(0., m.omega[k]) ? 0.f : float(m.omega[k]);
+                vxf[k] = float(m.vx[k]);
+                vyf[k] = float(m.vy[k]);
+            }
+            B.d_om.upload(omf, s);
+            B.d_vx.upload(vxf, s);
+            B.d_vy.upload(vyf, s);
         }
         // generate the sources in `descs` at A[base..): alias rows from
         // aprob/aalt (uploaded here) or from a table already on the device
@@ -1750,8 +1812,8 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                                                    p->dt, g.thickness, B.d_req.as<WallReq>(), B.d_acnt.as<long long>(),
                                                    B.d_adesc.as<GenDesc>(), dc, span + 2, cap, err);
                 be_wall_cdf1_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
-                    B.d_om.as<double>(), B.d_vx.as<double>(), B.d_vy.as<double>(), B.d_ne.as<double>(), p->T0, n,
-                    B.d_req.as<WallReq>(), B.d_acnt.as<long long>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
+                    B.d_om.as<float>(), B.d_vx.as<float>(), B.d_vy.as<float>(), n, B.d_req.as<WallReq>(),
+                    B.d_acnt.as<long long>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
                 be_wall_cdf2_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
                     n, B.d_acnt.as<long long>(), B.d_ctot.as<double>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
                 be_generate_dev<<<pblocks, 256, 0, s>>>(A, span + 2, B.d_adesc.as<GenDesc>(), nborders, nullptr, nullptr,
