@@ -124,7 +124,7 @@ void ensure_static(bte_ctx* c) {
                         double s0 = (cb.p1.x - P.px) * P.ux + (cb.p1.y - P.py) * P.uy;
                         double s1 = (cb.p2.x - P.px) * P.ux + (cb.p2.y - P.py) * P.uy;
                         if (s0 > s1) std::swap(s0, s1);
-                        pieces.push_back(bte::PolyPiece{s0, s1, gc.id, 0});
+                        pieces.push_back(bte::PolyPiece{s0 - 1.0e-9, s1 + 1.0e-9, gc.id, 0});
                     }
                     P.npieces = int(pieces.size()) - P.piece_off;
                 }
@@ -132,6 +132,31 @@ void ensure_static(bte_ctx* c) {
             if (pieces.empty()) pieces.push_back(bte::PolyPiece{0., 0., -1, 0});
             c->d_pborders.upload(pb, c->stream);
             c->d_ppieces.upload(pieces, c->stream);
+            // axis-aligned rectangles: four borders with normals +x, -x, +y, -y
+            std::vector<bte::PolyRect> rect(g.boxes.size());
+            for (std::size_t a = 0; a < g.boxes.size(); ++a) {
+                const bte::GBox& bx = g.boxes[a];
+                bte::PolyRect R{0., 0., 0., 0., -1, -1, -1, -1};
+                int k4[4] = {-1, -1, -1, -1};
+                double c4[4] = {0., 0., 0., 0.};
+                bool ok = bx.nborders == 4;
+                for (int k = 0; ok && k < 4; ++k) {
+                    const bte::PolyBorder& P = pb[std::size_t(bx.border_off + k)];
+                    const int side = P.nx == 1. && P.ny == 0. ? 0 : P.nx == -1. && P.ny == 0. ? 1
+                                   : P.nx == 0. && P.ny == 1. ? 2 : P.nx == 0. && P.ny == -1. ? 3 : -1;
+                    if (side < 0 || k4[side] >= 0) ok = false;
+                    else {
+                        k4[side] = k;
+                        c4[side] = P.c;
+                    }
+                }
+                if (ok) {
+                    R = bte::PolyRect{-c4[1], c4[0], -c4[3], c4[2], k4[0], k4[1], k4[2], k4[3]};
+                    if (!(R.x0 < R.x1 && R.y0 < R.y1)) R.kx1 = -1;
+                }
+                rect[a] = R;
+            }
+            c->d_prect.upload(rect, c->stream);
         }
         sync(c);
         c->geom_dev = true;
@@ -927,7 +952,8 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
                                      c->d_work.as<unsigned long long>(), c->nsm, c->stream);
         } else {
             const bte::PolyArgs A{c->d_pborders.as<bte::PolyBorder>(), c->d_ppieces.as<bte::PolyPiece>(),
-                                  c->d_mv.as<bte::ModeVel>(), c->d_invden.as<double>()};
+                                  c->d_mv.as<bte::ModeVel>(), c->d_invden.as<double>(),
+                                  c->d_prect.as<bte::PolyRect>()};
             if (!bte::launch_prod_poly(T, A, c->d_tally.as<double>(), counters, err,
                                        c->d_work.as<unsigned long long>(), c->nsm, c->stream))
                 throw Error(BTE_ERR_CUDA, "polygon kernel does not fit on the device");

@@ -78,6 +78,7 @@ struct bte_ctx {
     bte::DBuf d_tfast, d_tfast_rng, d_tfast_u;  // translations without a search
     bool have_tfast = false;
     bte::DBuf d_invden;                           // 1 / (n.v) per normal class and mode
+    bte::DBuf d_prect;                            // PolyRect per box
     bte::DBuf d_gx, d_gy, d_gcell, d_boxcell;
     bte::DBuf d_pborders, d_ppieces;  // convex-polygon path (geometries that are not a grid)
     bte::DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;

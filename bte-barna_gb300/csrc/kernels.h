@@ -65,8 +65,15 @@ struct PolyBorder {
     int piece_off, npieces, cls, pad;
 };
 struct PolyPiece {
-    double s0, s1;
+    double s0, s1;  // the interval of s, widened by 1e-9 at both ends
     int box, pad;
+};
+// An axis-aligned rectangular box of the polygon path: its lines and the
+// box's own indices of its +x, -x, +y, -y borders (kx1 = -1: not such a
+// box, the general border search applies).
+struct PolyRect {
+    double x0, x1, y0, y1;
+    int kx1, kx0, ky1, ky0;
 };
 struct PolyArgs {
     const PolyBorder* pb;     // [global border index]
@@ -75,6 +82,7 @@ struct PolyArgs {
     // 1 / (n.v) per border normal class and mode ([nclass][n], -1 where the
     // flight does not leave through such a border); null: divide per pass
     const double* inv_den;
+    const PolyRect* rect;     // [box] or null
 };
 
 // Adjoint passes of the grid kernel: the functional's weights per tally

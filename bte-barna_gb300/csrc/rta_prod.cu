@@ -1189,7 +1189,26 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         const GBox& B = T.boxes[p.box];
         int best = -1;
         double te = HUGE_VAL;
-        if (A.inv_den) {
+        // an axis-aligned rectangle: the cell-line test of the grid kernel,
+        // the line ahead in x and in y (a zero velocity component has
+        // 1/v = +inf and never exits), the nearer one first on ties
+        PolyRect R;
+        R.kx1 = -1;
+        if (A.rect) R = A.rect[p.box];
+        const bool rectb = R.kx1 >= 0;
+        bool xfirst = false;
+        double xw = 0., yw = 0.;
+        if (rectb) {
+            const bool upx = ob(mv.ivx) >= 0, upy = ob(mv.ivy) >= 0;
+            xw = upx ? R.x1 : R.x0;
+            yw = upy ? R.y1 : R.y0;
+            long long bx = ob((xw - p.pos.x) * mv.ivx), by = ob((yw - p.pos.y) * mv.ivy);
+            bx = bx > 0 ? bx : 0;
+            by = by > 0 ? by : 0;
+            xfirst = bx <= by;
+            best = xfirst ? (upx ? R.kx1 : R.kx0) : (upy ? R.ky1 : R.ky0);
+            te = obd(xfirst ? bx : by);
+        } else if (A.inv_den) {
             // 1 / den from the table of the border's normal class: one
             // multiplication per border, compared as integers (both >= 0)
             const double* inv = A.inv_den + p.mode;
@@ -1270,13 +1289,24 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
             const PolyBorder& L = A.pb[B.border_off + best];
             cls = L.cls;
             // onto the border line
-            const double off = L.nx * nx + L.ny * ny - L.c;
-            nx -= off * L.nx;
-            ny -= off * L.ny;
-            const double sx = (nx - L.px) * L.ux + (ny - L.py) * L.uy;
+            double sx;
+            if (rectb) {
+                if (xfirst) {
+                    nx = xw;
+                    sx = (ny - L.py) * L.uy;
+                } else {
+                    ny = yw;
+                    sx = (nx - L.px) * L.ux;
+                }
+            } else {
+                const double off = L.nx * nx + L.ny * ny - L.c;
+                nx -= off * L.nx;
+                ny -= off * L.ny;
+                sx = (nx - L.px) * L.ux + (ny - L.py) * L.uy;
+            }
             for (int j = 0; j < L.npieces; ++j) {
                 const PolyPiece pc = A.pieces[L.piece_off + j];
-                if (sx >= pc.s0 - 1.0e-9 && sx <= pc.s1 + 1.0e-9) {
+                if (sx >= pc.s0 && sx <= pc.s1) {
                     target = pc.box;
                     break;
                 }
@@ -1482,7 +1512,7 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
             const double sx = (nx - L.px) * L.ux + (ny - L.py) * L.uy;
             for (int j = 0; j < L.npieces; ++j) {
                 const PolyPiece pc = PA.pieces[L.piece_off + j];
-                if (sx >= pc.s0 - 1.0e-9 && sx <= pc.s1 + 1.0e-9) {
+                if (sx >= pc.s0 && sx <= pc.s1) {
                     target = pc.box;
                     break;
                 }

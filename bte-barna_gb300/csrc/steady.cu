@@ -282,7 +282,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         A.work = S.work.as<unsigned long long>();
 
         const PolyArgs PA{c->d_pborders.as<PolyBorder>(), c->d_ppieces.as<PolyPiece>(), c->d_mv.as<ModeVel>(),
-                          nullptr};
+                          nullptr, nullptr};
         const int max_gen = p->max_generations > 0 ? p->max_generations : 100000;
         std::vector<double> oldv(size_t(3) * nbx, 0.), cur(size_t(3) * nbx, 0.);
         std::vector<unsigned long long> hex, hphi(static_cast<size_t>(nbx));
