@@ -32,13 +32,15 @@ PUBLIC_SYMBOLS = ["bte_create", "bte_destroy", "bte_last_error", "bte_load_modes
                   "bte_load_geometry", "bte_rta_run", "bte_set_tuning", "bte_query_sizes",
                   "bte_version", "bte_rta_run_noalloc", "bte_load_propagator", "bte_berta_run",
                   "bte_steady_run", "bte_load_materials", "bte_rta_adjoint", "bte_set_spectral",
-                  "bte_get_spectral", "bte_set_groups", "bte_get_group_result"]
+                  "bte_get_spectral", "bte_set_groups", "bte_get_group_result", "bte_load_mode_tables",
+                  "bte_interface_table"]
 
 
 class BteError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
         self.code = code
+
 
 
 class DeviceOpts(C.Structure):
@@ -77,7 +79,8 @@ class RtaResult(C.Structure):
                 ("energy_rate", C.c_double), ("events", C.c_int64), ("wall_hits", C.c_int64),
                 ("crossings", C.c_int64), ("absorbed", C.c_int64),
                 ("specular_hits", C.c_int64), ("tally_updates", C.c_int64),
-                ("kernel_ms", C.c_double), ("translations", C.c_int64)]
+                ("kernel_ms", C.c_double), ("translations", C.c_int64),
+                ("interface_hits", C.c_int64), ("interface_transmissions", C.c_int64)]
 
 
 class Propagator(C.Structure):
@@ -282,6 +285,12 @@ def load_library(path: str = LIB_PATH):
     lib.bte_load_materials.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]
     lib.bte_load_materials.restype = C.c_int
+    lib.bte_load_mode_tables.argtypes = [vp, C.c_int32, C.POINTER(ModeTable)]
+    lib.bte_load_mode_tables.restype = C.c_int
+    lib.bte_interface_table.argtypes = [C.POINTER(ModeTable), C.POINTER(ModeTable), C.c_double, C.c_double,
+                                        C.c_double, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+    lib.bte_interface_table.restype = C.c_int
     lib.bte_set_spectral.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32]
     lib.bte_set_spectral.restype = C.c_int
     lib.bte_get_spectral.argtypes = [vp, C.POINTER(SpectralResult)]
@@ -350,6 +359,19 @@ class Engine:
         self._check(self.lib.bte_load_modes(self.ctx, C.byref(s)))
         self._keep["modes"] = keep
 
+    def load_mode_tables(self, tables):
+        """Several crystals: mode table k for the boxes of material k
+        (geometry "material"), diffuse mismatch at their contacts."""
+        arr = (ModeTable * len(tables))()
+        keep = []
+        for i, t in enumerate(tables):
+            s, k = mode_struct(t)
+            arr[i] = s
+            keep.append(k)
+        self._check(self.lib.bte_load_mode_tables(self.ctx, len(tables), arr))
+        self._keep["modes"] = {"omega": np.concatenate([np.asarray(t["omega"], float) for t in tables])}
+        self._keep["crystals"] = (arr, keep)
+
     def load_geometry(self, g: dict):
         s, keep = geom_struct(g)
         self._check(self.lib.bte_load_geometry(self.ctx, C.byref(s)))
@@ -380,7 +402,8 @@ class Engine:
             r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
         self._check(self.lib.bte_rta_run(self.ctx, C.byref(p), C.byref(r)))
         for k in ("Eeff", "energy_rate", "events", "wall_hits", "crossings", "absorbed",
-                  "specular_hits", "tally_updates", "kernel_ms", "translations"):
+                  "specular_hits", "tally_updates", "kernel_ms", "translations", "interface_hits",
+                  "interface_transmissions"):
             out[k] = getattr(r, k)
         return out
 
@@ -521,6 +544,37 @@ Engine.steady_run = _engine_steady_run
 Engine.load_propagator = _engine_load_propagator
 Engine.berta_run = _engine_berta_run
 
+
+def interface_table(A: dict, B: dict, normal, thickness: float, Tref: float):
+    """The engine's diffuse mismatch table from mode table A to B (host
+    code, no device): per incident mode of A, arrays (side out, mode out,
+    cumulative)."""
+    lib = load_library()
+    sa, ka = mode_struct(A)
+    sb, kb = mode_struct(B)
+    na = int(np.asarray(A["omega"]).size)
+    first = np.zeros(na + 1, dtype=np.int64)
+    ne = np.zeros(1, dtype=np.int64)
+    args = (C.byref(sa), C.byref(sb), float(normal[0]), float(normal[1]), float(thickness), float(Tref))
+    lp = C.POINTER(C.c_int64)
+    st = lib.bte_interface_table(*args, first.ctypes.data_as(lp), ne.ctypes.data_as(lp), None, None, None)
+    if st != 0:
+        raise BteError(st, _host_error(lib))
+    side = np.zeros(int(ne[0]), dtype=np.int32)
+    mode = np.zeros(int(ne[0]), dtype=np.int32)
+    cum = np.zeros(int(ne[0]))
+    st = lib.bte_interface_table(*args, first.ctypes.data_as(lp), ne.ctypes.data_as(lp),
+                                 side.ctypes.data_as(C.POINTER(C.c_int32)), mode.ctypes.data_as(C.POINTER(C.c_int32)),
+                                 cum.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise BteError(st, _host_error(lib))
+    return [(side[first[i]:first[i + 1]], mode[first[i]:first[i + 1]], cum[first[i]:first[i + 1]]) for i in range(na)]
+
+
+def _host_error(lib) -> str:
+    buf = C.create_string_buffer(512)
+    lib.bte_last_error(None, buf, 512)
+    return buf.value.decode()
 
 def debug_geometry(g: dict) -> np.ndarray:
     lib = load_library()

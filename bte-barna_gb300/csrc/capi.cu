@@ -6,7 +6,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <tuple>
 #include <string>
 #include <thread>
 #include <vector>
@@ -124,14 +126,17 @@ void ensure_static(bte_ctx* c) {
                         double s0 = (cb.p1.x - P.px) * P.ux + (cb.p1.y - P.py) * P.uy;
                         double s1 = (cb.p2.x - P.px) * P.ux + (cb.p2.y - P.py) * P.uy;
                         if (s0 > s1) std::swap(s0, s1);
-                        pieces.push_back(bte::PolyPiece{s0 - 1.0e-9, s1 + 1.0e-9, gc.id, 0});
+                        pieces.push_back(bte::PolyPiece{s0 - 1.0e-9, s1 + 1.0e-9, gc.id, -1});
                     }
                     P.npieces = int(pieces.size()) - P.piece_off;
                 }
             }
-            if (pieces.empty()) pieces.push_back(bte::PolyPiece{0., 0., -1, 0});
+            if (pieces.empty()) pieces.push_back(bte::PolyPiece{0., 0., -1, -1});
             c->d_pborders.upload(pb, c->stream);
             c->d_ppieces.upload(pieces, c->stream);
+            c->pieces_host = pieces;
+            c->pborders_host = pb;
+            c->dmm_dev = false;
             // axis-aligned rectangles: four borders with normals +x, -x, +y, -y
             std::vector<bte::PolyRect> rect(g.boxes.size());
             for (std::size_t a = 0; a < g.boxes.size(); ++a) {
@@ -162,13 +167,26 @@ void ensure_static(bte_ctx* c) {
         c->geom_dev = true;
     }
     if (!c->lambert_dev) {
-        bte::LambertTable L = bte::build_lambert(m, g, hw_threads());
+        bte::LambertTable L;
+        std::vector<int> mir;
+        if (c->ncrys > 0) {  // each crystal's rows over its own modes, then offset
+            std::vector<bte::LambertTable> Ls;
+            std::vector<std::vector<int>> ms;
+            for (const bte::HostModes& cm : c->crys) {
+                Ls.push_back(bte::build_lambert(cm, g, hw_threads()));
+                ms.push_back(bte::build_mirror(cm, g));
+            }
+            L = bte::merge_lambert(Ls, c->crys, c->crys_off);
+            mir = bte::merge_mirror(ms, c->crys, c->crys_off, L.nclass);
+        } else {
+            L = bte::build_lambert(m, g, hw_threads());
+            mir = bte::build_mirror(m, g);
+        }
         c->nclass = L.nclass;
         c->d_row_ptr.upload(L.row_ptr, c->stream);
         c->d_lcol.upload(L.col, c->stream);
         c->d_lcdf.upload(L.cdf, c->stream);
         c->d_lalias.upload(L.alias, c->stream);
-        std::vector<int> mir = bte::build_mirror(m, g);
         c->have_mirror = std::any_of(mir.begin(), mir.end(), [](int x) { return x >= 0; });
         c->d_mirror.upload(mir, c->stream);
         // exit times of the convex-polygon path without a division: 1 / (n.v)
@@ -189,6 +207,65 @@ void ensure_static(bte_ctx* c) {
         c->lambert_dev = true;
         if (c->verbose)
             std::printf("#Diffusive table: %d wall normals, %zu entries\n", L.nclass, L.col.size());
+    }
+    if (c->ncrys > 0 && !c->dmm_dev) {
+        // one mismatch table per (crystal A, crystal B, contact normal) over
+        // the contacts from a box that is neither a reservoir nor periodic to
+        // a box of another crystal, at the Teq of the first such box
+        std::map<std::tuple<int, int, double, double>, int> tab_of;
+        std::vector<long long> rows;
+        std::vector<bte::DmmEnt> ents;
+        const std::size_t ntot = m.n();
+        for (std::size_t a = 0; a < g.boxes.size(); ++a) {
+            if (g.reservoir[a] || g.tto[a] >= 0) continue;
+            const bte::GBox& B = g.boxes[a];
+            for (int i = 0; i < B.ncontacts; ++i) {
+                const std::size_t ci = std::size_t(B.contact_off + i);
+                const int b = g.contacts[ci].id;
+                const int ma = g.mat[a], mb = g.mat[std::size_t(b)];
+                if (ma == mb) continue;
+                const bte::V2 nw = g.contact_borders[ci].np;
+                const auto key = std::make_tuple(ma, mb, nw.x, nw.y);
+                if (tab_of.count(key)) continue;
+                const bte::HostModes& A = c->crys[std::size_t(ma)];
+                const bte::HostModes& Bm = c->crys[std::size_t(mb)];
+                const bte::DmmTable D = bte::build_dmm_table(
+                    A, c->crys_off[std::size_t(ma)], Bm, c->crys_off[std::size_t(mb)], ntot, nw,
+                    A.V * g.thickness / A.c, Bm.V * g.thickness / Bm.c, g.Teq[a], hw_threads());
+                tab_of[key] = int(tab_of.size());
+                const long long base = (long long)ents.size();
+                for (std::size_t K = 0; K <= ntot; ++K) rows.push_back(base + D.row[K]);
+                for (std::size_t e = 0; e < D.out.size(); ++e) ents.push_back(bte::DmmEnt{D.cum[e], D.out[e], D.side[e]});
+            }
+        }
+        // each piece that leads into another crystal names its table
+        std::vector<bte::PolyPiece>& pcs = c->pieces_host;
+        for (std::size_t a = 0; a < g.boxes.size(); ++a) {
+            if (g.reservoir[a] || g.tto[a] >= 0) continue;
+            const bte::GBox& B = g.boxes[a];
+            for (int i = 0; i < B.ncontacts; ++i) {
+                const std::size_t ci = std::size_t(B.contact_off + i);
+                const int b = g.contacts[ci].id;
+                if (g.mat[a] == g.mat[std::size_t(b)]) continue;
+                const bte::V2 nw = g.contact_borders[ci].np;
+                const int t = tab_of.at(std::make_tuple(g.mat[a], g.mat[std::size_t(b)], nw.x, nw.y));
+                for (int k = 0; k < B.nborders; ++k) {
+                    const bte::PolyBorder& P = c->pborders_host[std::size_t(B.border_off + k)];
+                    for (int j = 0; j < P.npieces; ++j) {
+                        bte::PolyPiece& pc = pcs[std::size_t(P.piece_off + j)];
+                        if (pc.box == b) pc.pad = t;
+                    }
+                }
+            }
+        }
+        if (rows.empty()) rows.push_back(0);
+        if (ents.empty()) ents.push_back(bte::DmmEnt{0., 0, 0});
+        c->d_dmm_row.upload(rows, c->stream);
+        c->d_dmm_ent.upload(ents, c->stream);
+        c->d_ppieces.upload(pcs, c->stream);
+        c->ndmm = int(tab_of.size());
+        sync(c);
+        c->dmm_dev = true;
     }
 }
 
@@ -272,7 +349,18 @@ void ensure_generators(bte_ctx* c, const bte_rta_params* p) {
         }
         return;
     }
-    if (p->source == BTE_SOURCE_WALLS) {
+    if (c->ncrys > 0) {
+        // each crystal's generators, rows over the concatenated modes
+        std::vector<bte::Generators> G;
+        for (int k = 0; k < c->ncrys; ++k) {
+            const bte::GenEmbed e{k, c->crys_off[std::size_t(k)], c->modes.n()};
+            G.push_back(p->source == BTE_SOURCE_WALLS
+                            ? bte::build_wall_generators(c->crys[std::size_t(k)], c->geom, false, &e)
+                            : bte::build_initial_generators(c->crys[std::size_t(k)], c->geom, &e));
+        }
+        c->gens = bte::merge_generators(G, p->source == BTE_SOURCE_WALLS, true);
+        if (p->source == BTE_SOURCE_INITIAL) c->gen_Eeff = bte::initial_counts(c->gens, p->nparticles, p->seed);
+    } else if (p->source == BTE_SOURCE_WALLS) {
         c->gens = bte::build_wall_generators(c->modes, c->geom);
         apply_shares(c, false);
     } else {
@@ -341,11 +429,22 @@ void prepare_run(bte_ctx* c, const bte_rta_params* p) {
     if (!c->have_modes || !c->have_geom)
         throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
     ck(cudaSetDevice(c->device), "cudaSetDevice");
+    if (c->ncrys > 0) {
+        // crystals joined by mismatch interfaces: the production polygon
+        // kernel only, every crystal at the run's T0
+        if (p->mode != BTE_MODE_PRODUCTION) throw Error(BTE_ERR_INPUT, "several crystals need the production mode");
+        if (p->flags & BTE_FLAG_GENERAL) throw Error(BTE_ERR_INPUT, "several crystals run on the polygon kernel");
+        if (!c->spec_boxes.empty()) throw Error(BTE_ERR_INPUT, "spectral outputs need one crystal");
+        if (c->mat_T0.empty() || c->mat_T0[0] != p->T0) {
+            c->mat_T0.assign(std::size_t(c->ncrys), p->T0);
+            c->resample_T0 = -1;
+        }
+    }
     for (std::size_t b = 0; b < c->geom.boxes.size(); ++b) {
         if (c->geom.mat[b] >= std::max(c->nmat, 1))
             throw Error(BTE_ERR_INPUT, "box material without loaded rates (bte_load_materials)");
         const double T0b = bte::box_T0(c, int(b), p->T0);
-        if (c->nmat > 0) {  // a particle keeps its material: materials must not touch
+        if (c->nmat > 0 && c->ncrys == 0) {  // a particle keeps its material: materials must not touch
             const bte::GBox& B = c->geom.boxes[b];
             for (int i = 0; i < B.ncontacts; ++i) {
                 const int o = c->geom.contacts[std::size_t(B.contact_off + i)].id;
@@ -425,20 +524,23 @@ void rta_post(bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, double Ee
             for (std::size_t k = 0; k < nk; ++k) v[k] /= step;
         });
     }
-    const double vcorr = g.thickness / m.c;
     if (out->temperature) {
-        // C_v per material, cached while the tables and temperatures stay
+        // C_v per material (per crystal: over its own modes, q points and
+        // cell), cached while the tables and temperatures stay
         std::vector<double> T0s(std::size_t(std::max(c->nmat, 1)));
         for (std::size_t k = 0; k < T0s.size(); ++k) T0s[k] = c->nmat > 0 ? c->mat_T0[k] : p->T0;
         if (c->cv_version != c->tables_version || c->cv_T0s != T0s) {
             c->cv_cache.resize(T0s.size());
-            for (std::size_t k = 0; k < T0s.size(); ++k) c->cv_cache[k] = bte::calc_cv(m, T0s[k]);
+            for (std::size_t k = 0; k < T0s.size(); ++k)
+                c->cv_cache[k] = bte::calc_cv(c->ncrys > 0 ? c->crys[k] : m, T0s[k]);
             c->cv_T0s = T0s;
             c->cv_version = c->tables_version;
         }
         const std::vector<double>& cvm = c->cv_cache;
         for (int ir = 0; ir < nbx; ++ir) {
-            const double cv = cvm[std::size_t(c->nmat > 0 ? g.mat[std::size_t(ir)] : 0)];
+            const std::size_t mk = std::size_t(c->nmat > 0 ? g.mat[std::size_t(ir)] : 0);
+            const double cv = cvm[mk];
+            const double vcorr = g.thickness / (c->ncrys > 0 ? c->crys[mk].c : m.c);
             const double T0b = bte::box_T0(c, ir, p->T0);
             for (int i = 0; i < nbins; ++i) {
                 const std::size_t k = std::size_t(ir) * nbins + i;
@@ -532,6 +634,10 @@ bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
         c->have_modes = true;
         c->tables_version++;
         bte::reset_propagators(c);
+        c->ncrys = 0;
+        c->crys.clear();
+        c->crys_off.clear();
+        c->dmm_dev = false;
         c->nmat = 0;  // materials are rate sets over one table
         c->mat_w.clear();
         c->mat_T0.clear();
@@ -562,6 +668,7 @@ bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
         c->have_geom = true;
         c->tables_version++;
         c->geom_dev = false;
+        c->dmm_dev = false;
         if (!same_normals) c->lambert_dev = false;
         c->gen_key_source = -1;
         return BTE_OK;
@@ -570,11 +677,80 @@ bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
     }
 }
 
+bte_status bte_load_mode_tables(bte_ctx* c, int32_t ntables, const bte_mode_table* tables) {
+    if (!c) return BTE_ERR_INPUT;
+    c->group_valid = false;
+    try {
+        if (ntables < 1 || !tables) throw Error(BTE_ERR_INPUT, "no mode tables");
+        ck(cudaSetDevice(c->device), "cudaSetDevice");
+        std::vector<bte::HostModes> crys;
+        for (int k = 0; k < ntables; ++k) crys.push_back(bte::build_modes(&tables[k]));
+        std::vector<std::size_t> off;
+        bte::HostModes all = bte::concat_modes(crys, off);
+        if (all.n() > (std::size_t(1) << 30)) throw Error(BTE_ERR_INPUT, "too many modes");
+        // the materials machinery with one rate set per crystal, each masked
+        // to its crystal's modes (zero rate, so zero weight, elsewhere)
+        const std::size_t n = all.n();
+        std::vector<double> mw(std::size_t(ntables) * n, 0.);
+        for (int k = 0; k < ntables; ++k)
+            for (std::size_t j = 0; j < crys[std::size_t(k)].n(); ++j)
+                mw[std::size_t(k) * n + off[std::size_t(k)] + j] = crys[std::size_t(k)].w[j];
+        c->modes = std::move(all);
+        c->crys = std::move(crys);
+        c->crys_off = std::move(off);
+        c->ncrys = ntables;
+        c->have_modes = true;
+        c->tables_version++;
+        bte::reset_propagators(c);
+        c->nmat = ntables;
+        c->mat_w = std::move(mw);
+        c->mat_T0.clear();  // set to each run's T0
+        c->mat_share.clear();
+        c->modes_dev = false;
+        c->lambert_dev = false;
+        c->dmm_dev = false;
+        c->resample_T0 = -1;
+        c->gen_key_source = -1;
+        return BTE_OK;
+    } catch (const Error& e) {
+        return fail(c, e);
+    }
+}
+
+bte_status bte_interface_table(const bte_mode_table* A, const bte_mode_table* B, double nx, double ny,
+                               double thickness, double Tref, int64_t* first, int64_t* nentries, int32_t* side,
+                               int32_t* mode, double* cum) {
+    try {
+        if (!A || !B || !first || !nentries || !(thickness > 0.) || !(Tref > 0.)) return BTE_ERR_INPUT;
+        const bte::HostModes a = bte::build_modes(A), b = bte::build_modes(B);
+        const std::size_t na = a.n();
+        const bte::DmmTable D = bte::build_dmm_table(a, 0, b, na, na + b.n(), bte::v2(nx, ny),
+                                                     a.V * thickness / a.c, b.V * thickness / b.c, Tref,
+                                                     hw_threads());
+        for (std::size_t i = 0; i <= na; ++i) first[i] = D.row[i];
+        *nentries = (int64_t)D.out.size();
+        if (side && mode && cum)
+            for (std::size_t e = 0; e < D.out.size(); ++e) {
+                side[e] = D.side[e];
+                mode[e] = D.side[e] == 0 ? D.out[e] : int32_t(std::size_t(D.out[e]) - na);
+                cum[e] = D.cum[e];
+            }
+        return BTE_OK;
+    } catch (const Error& e) {
+        g_create_error = e.what();
+        return e.code;
+    } catch (const std::exception& e) {
+        g_create_error = e.what();
+        return BTE_ERR_INPUT;
+    }
+}
+
 bte_status bte_load_materials(bte_ctx* c, int32_t nmat, const double* w, const double* T0,
                               const double* share) {
     if (!c) return BTE_ERR_INPUT;
     c->group_valid = false;
     try {
+        if (c->ncrys > 0) throw Error(BTE_ERR_STATE, "rate sets are for one mode table; crystals carry their own rates");
         if (nmat < 0 || (nmat > 0 && (!w || !T0))) throw Error(BTE_ERR_INPUT, "bad material arrays");
         if (share && nmat > 0) {
             double sum = 0.;
@@ -929,7 +1105,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         ck(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
         if (replay) {
             bte::launch_replay(T, c->d_tally.as<unsigned long long>(), counters, err, c->nsm, c->stream);
-        } else if (g.rect_grid) {
+        } else if (g.rect_grid && c->ncrys == 0) {
             bte::GridArgs A{};
             A.G.nx = g.gnx;
             A.G.ny = g.gny;
@@ -953,7 +1129,9 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         } else {
             const bte::PolyArgs A{c->d_pborders.as<bte::PolyBorder>(), c->d_ppieces.as<bte::PolyPiece>(),
                                   c->d_mv.as<bte::ModeVel>(), c->d_invden.as<double>(),
-                                  c->d_prect.as<bte::PolyRect>()};
+                                  c->d_prect.as<bte::PolyRect>(),
+                                  c->ncrys > 0 ? c->d_dmm_row.as<long long>() : nullptr,
+                                  c->ncrys > 0 ? c->d_dmm_ent.as<bte::DmmEnt>() : nullptr};
             if (!bte::launch_prod_poly(T, A, c->d_tally.as<double>(), counters, err,
                                        c->d_work.as<unsigned long long>(), c->nsm, c->stream))
                 throw Error(BTE_ERR_CUDA, "polygon kernel does not fit on the device");
@@ -1055,6 +1233,8 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         out->specular_hits = (int64_t)hc[4];
         out->tally_updates = (int64_t)hc[7];
         out->translations = (int64_t)hc[8];
+        out->interface_hits = (int64_t)hc[11];
+        out->interface_transmissions = (int64_t)hc[12];
         if (out->gz) std::copy(gz.begin(), gz.end(), out->gz);
         if (out->gz_jx) std::copy(jx.begin(), jx.end(), out->gz_jx);
         if (out->gz_jy) std::copy(jy.begin(), jy.end(), out->gz_jy);

@@ -8,7 +8,9 @@
 // [t_mid, box0, box1, ...] (src/RTA_MC2D.cpp:2437-2471).  `nthreads` is
 // accepted and ignored.  The material database is the engine's binary mode
 // table (magic BTEMODE1); almaBTE HDF5 files need libhdf5, which this build
-// does not link.  Extensions live in an <engine .../> element:
+// does not link.  Several <material>s (boxes name theirs in <MaterialID>)
+// run as crystals joined by diffuse mismatch interfaces, all of one
+// thickness.  Extensions live in an <engine .../> element:
 //   mode="replay|production" seed="N" specularity="p" source="walls|initial"
 #include <chrono>
 #include <cmath>
@@ -169,6 +171,9 @@ int main(int argc, char** argv) {
         const std::string base = dir_of(input);
         std::string gfile, dbfile;
         double dt = 0, maxtime = 0, thickness = 0, T0 = -1, p = 0;
+        // every <material name database thickness T0> (src/RTA_MC2D.cpp:1886-1923)
+        std::vector<std::string> mnames, mfiles;
+        std::vector<double> mthick;
         long long N = 0;
         double grad[2] = {0., 0.}, eps_energy = -42.0, eps_flux = -42.0;
         std::vector<int32_t> spec_boxes;
@@ -185,6 +190,9 @@ int main(int argc, char** argv) {
                 dbfile = k->get("database");
                 thickness = std::stod(k->get("thickness"));
                 T0 = std::stod(k->get("T0"));
+                mnames.push_back(k->has("name") ? k->get("name") : "");
+                mfiles.push_back(dbfile);
+                mthick.push_back(thickness);
             }
             if (k->name == "particles") N = std::stoll(k->get("N"));
             if (k->name == "ballistic") ballistic = 1;
@@ -215,7 +223,7 @@ int main(int argc, char** argv) {
         }
         // geometry
         auto groot = read_xml(resolve(base, gfile));
-        std::vector<int32_t> npts, res, tto;
+        std::vector<int32_t> npts, res, tto, bmat;
         std::vector<double> verts, teq, tinit, transl;
         bool any_periodic = false;
         for (auto& b : groot->kids) {
@@ -236,6 +244,16 @@ int main(int argc, char** argv) {
             teq.push_back(te);
             tinit.push_back(ic && ic->has("Tinit") ? std::stod(ic->get("Tinit")) : te);
             res.push_back(b->child("Reservoir") ? 1 : 0);
+            // <MaterialID name=...>: the box's crystal among the <material>s
+            const Node* mid = b->child("MaterialID");
+            int mk = 0;
+            if (mid && mnames.size() > 1) {
+                mk = -1;
+                for (std::size_t i = 0; i < mnames.size(); ++i)
+                    if (mnames[i] == mid->get("name")) mk = int(i);
+                if (mk < 0) throw std::runtime_error("box material " + mid->get("name") + " is not a <material>");
+            }
+            bmat.push_back(mk);
             // <Translate_to id="j"> tx ty [tz] </Translate_to>, src/geometry_2d.cpp:467-475
             const Node* tr = b->child("Translate_to");
             tto.push_back(tr ? std::stoi(tr->get("id")) : -1);
@@ -248,6 +266,9 @@ int main(int argc, char** argv) {
             transl.push_back(tx);
             transl.push_back(ty);
         }
+        if (mnames.size() > 1)
+            for (double t : mthick)
+                if (t != mthick[0]) throw std::runtime_error("materials of different thickness are not supported");
         ModesFile mf = read_modes(resolve(base, dbfile));
         bte_ctx* ctx = nullptr;
         bte_device_opts opts{0, 1};
@@ -267,7 +288,29 @@ int main(int argc, char** argv) {
         mt.dq = mf.dq;
         mt.V = mf.V;
         mt.c_lat = mf.c;
-        check(ctx, bte_load_modes(ctx, &mt), "load modes");
+        // several crystals: one mode table per <material>, diffuse mismatch
+        // at their contacts
+        std::vector<ModesFile> mfs;
+        std::vector<bte_mode_table> mts;
+        if (mnames.size() > 1) {
+            for (auto& f : mfiles) mfs.push_back(read_modes(resolve(base, f)));
+            for (auto& x : mfs) {
+                bte_mode_table t{};
+                t.nq = x.head[0];
+                t.nb = x.head[1];
+                for (int i = 0; i < 3; ++i) t.grid[i] = x.head[2 + i];
+                t.omega = x.omega.data();
+                t.vg = x.vg.data();
+                t.w = x.w.data();
+                t.dq = x.dq;
+                t.V = x.V;
+                t.c_lat = x.c;
+                mts.push_back(t);
+            }
+            check(ctx, bte_load_mode_tables(ctx, int32_t(mts.size()), mts.data()), "load mode tables");
+        } else {
+            check(ctx, bte_load_modes(ctx, &mt), "load modes");
+        }
         bte_geometry gm{};
         gm.nboxes = int32_t(npts.size());
         gm.npoints = npts.data();
@@ -276,6 +319,7 @@ int main(int argc, char** argv) {
         gm.Tinit = tinit.data();
         gm.reservoir = res.data();
         gm.thickness = thickness;
+        if (mnames.size() > 1) gm.material = bmat.data();
         if (any_periodic) {
             gm.translate_to = tto.data();
             gm.translation = transl.data();

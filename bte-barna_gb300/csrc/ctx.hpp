@@ -79,6 +79,17 @@ struct bte_ctx {
     bool have_tfast = false;
     bte::DBuf d_invden;                           // 1 / (n.v) per normal class and mode
     bte::DBuf d_prect;                            // PolyRect per box
+    // several crystals (bte_load_mode_tables): their own mode tables, the
+    // concatenation in `modes` (global mode off[k] + j), the rate sets of the
+    // materials machinery masked to each crystal, mismatch tables per interface
+    int ncrys = 0;
+    std::vector<bte::HostModes> crys;
+    std::vector<std::size_t> crys_off;
+    std::vector<bte::PolyPiece> pieces_host;      // the polygon path's pieces (pads: mismatch tables)
+    std::vector<bte::PolyBorder> pborders_host;
+    bool dmm_dev = false;
+    int ndmm = 0;
+    bte::DBuf d_dmm_row, d_dmm_ent;
     bte::DBuf d_gx, d_gy, d_gcell, d_boxcell;
     bte::DBuf d_pborders, d_ppieces;  // convex-polygon path (geometries that are not a grid)
     bte::DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;

@@ -66,7 +66,13 @@ struct PolyBorder {
 };
 struct PolyPiece {
     double s0, s1;  // the interval of s, widened by 1e-9 at both ends
-    int box, pad;
+    int box, pad;   // pad: the mismatch table of the contact (-1: same crystal)
+};
+// One entry of a diffuse mismatch table: cumulative probability, global
+// mode out, side out (0: back into the incident box, 1: into the other).
+struct DmmEnt {
+    double cum;
+    int out, side;
 };
 // An axis-aligned rectangular box of the polygon path: its lines and the
 // box's own indices of its +x, -x, +y, -y borders (kx1 = -1: not such a
@@ -83,6 +89,11 @@ struct PolyArgs {
     // flight does not leave through such a border); null: divide per pass
     const double* inv_den;
     const PolyRect* rect;     // [box] or null
+    // diffuse mismatch interfaces between crystals: a piece whose pad is
+    // t >= 0 leads through table t; its rows for global mode K are
+    // dmm_row[t * (n + 1) + K .. + 1] into dmm_ent
+    const long long* dmm_row;
+    const DmmEnt* dmm_ent;
 };
 
 // Adjoint passes of the grid kernel: the functional's weights per tally

@@ -102,7 +102,7 @@ struct DevTables {
 
 struct Counters {
     unsigned long long events, wall_hits, crossings, absorbed, specular, nudges, quirks, tallies,
-        translations, scattered, lost;
+        translations, scattered, lost, ifc_hits, ifc_trans;
 };
 
 // How a steady-state flight ends (periodic / gradient branch).

@@ -26,12 +26,13 @@ __device__ __forceinline__ void record_error(int* err, int e, long long pid) {
 
 // Warp-reduced counters: the first NC of (events, wall hits, crossings,
 // absorbed, specular, nudges, quirks, tally updates, translations,
-// steady-state scatters, steady-state drops).
+// steady-state scatters, steady-state drops, interface hits, interface
+// transmissions).
 template <int NC = 11>
 __device__ __forceinline__ void flush_counters_p(const Counters& c, unsigned long long* out) {
-    unsigned long long v[11] = {c.events, c.wall_hits, c.crossings, c.absorbed,
+    unsigned long long v[13] = {c.events, c.wall_hits, c.crossings, c.absorbed,
                                 c.specular, c.nudges, c.quirks, c.tallies, c.translations,
-                                c.scattered, c.lost};
+                                c.scattered, c.lost, c.ifc_hits, c.ifc_trans};
 #pragma unroll
     for (int i = 0; i < NC; ++i) {
         unsigned long long x = v[i];
@@ -1284,7 +1285,7 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         dt -= seg;
         if (bin_end) r1 = 0.;
         // what lies across the exit border
-        int target = -1, cls = 0;
+        int target = -1, cls = 0, dmm_t = -1;
         if (wall) {
             const PolyBorder& L = A.pb[B.border_off + best];
             cls = L.cls;
@@ -1308,9 +1309,42 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
                 const PolyPiece pc = A.pieces[L.piece_off + j];
                 if (sx >= pc.s0 && sx <= pc.s1) {
                     target = pc.box;
+                    dmm_t = pc.pad;
                     break;
                 }
             }
+        }
+        // a contact between crystals (change_material_diffuse,
+        // src/RTA_MC2D.cpp:871-964): the interface's table re-emits the
+        // particle on either side (Diffuse_mismatch_distribution::reemit,
+        // src/sampling.cpp:831-902: p uniform between the first and the last
+        // cumulative value of the incident mode's entries, the first entry
+        // not below p); the flight ends there.  Without entries the particle
+        // crosses in its mode, as the reference's 'X'.
+        const bool iface = wall && target >= 0 && dmm_t >= 0 && A.dmm_row;
+        bool dmm_back = false;
+        int dmm_mode = -1;
+        if (iface) {
+            const long long* row = A.dmm_row + (long long)dmm_t * (T.n + 1);
+            const long long e0 = __ldg(row + p.mode), e1 = __ldg(row + p.mode + 1);
+            if (e1 > e0) {
+                const double lo = A.dmm_ent[e0].cum, hi = A.dmm_ent[e1 - 1].cum;
+                const double u = double((((unsigned long long)rr.y << 32) | rr.z) >> 11) * 0x1p-53;
+                const double pp = u * (hi - lo) + lo;
+                long long a = e0, b = e1 - 1;
+                while (a < b) {
+                    const long long mid = (a + b) >> 1;
+                    if (A.dmm_ent[mid].cum >= pp) b = mid;
+                    else a = mid + 1;
+                }
+                const DmmEnt en = A.dmm_ent[a];
+                dmm_mode = en.out;
+                dmm_back = en.side == 0;
+            } else {
+                c.quirks++;
+            }
+            c.ifc_hits++;
+            if (!dmm_back) c.ifc_trans++;
         }
         if (T.spec_loc) {
             const int loc = __ldg(T.spec_loc + p.box);
@@ -1322,7 +1356,7 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         const double d0 = pd.r0 - r1, d1 = nx - pd.x0, d2 = ny - pd.y0;
         rb = r1;
         p.pos = v2(nx, ny);
-        const bool cross = wall && target >= 0;
+        const bool cross = wall && target >= 0 && !dmm_back;
         const bool absorbed = cross && T.boxes[target].reservoir;
         const bool periodic = cross && !absorbed && T.boxes[target].tto >= 0;
         const bool move = cross && !absorbed;
@@ -1364,7 +1398,10 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
             c.crossings++;
         }
         if (move || bin_end) pd.start(p.box * T.nbins + bin, rb, p.pos.x, p.pos.y);
-        if (reflect || flight_end) {
+        if (iface) {  // a new flight in the re-emitted mode
+            if (dmm_mode >= 0) p.mode = dmm_mode;
+            if (!new_flight(rr.x)) continue;
+        } else if (reflect || flight_end) {
             const int k = p.mode;
             int nm = k;
             if (reflect || !T.ballistic) {
@@ -1408,7 +1445,7 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         }
     }
     c.tallies = pd.flushes;
-    flush_counters_p(c, counters);
+    flush_counters_p<13>(c, counters);
 }
 
 bool launch_prod_poly(const DevTables& T, const PolyArgs& A, double* tally, unsigned long long* counters,

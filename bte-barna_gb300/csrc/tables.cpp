@@ -580,20 +580,35 @@ LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthrea
     return L;
 }
 
-Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required) {
+// pmf (the crystal's n modes) placed at e->off in a row of e->n, zeros
+// elsewhere; the row itself without an embedding
+static const std::vector<double>& embed_row(const std::vector<double>& pmf, const GenEmbed* e,
+                                            std::vector<double>& row) {
+    if (!e) return pmf;
+    row.assign(e->n, 0.);
+    std::copy(pmf.begin(), pmf.end(), row.begin() + std::ptrdiff_t(e->off));
+    return row;
+}
+
+Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required, const GenEmbed* e) {
     Generators R;
     const std::size_t n = m.n();
     const double vuc = m.V * g.thickness / m.c;
     const int nbx = int(g.boxes.size());
-    std::vector<double> pmf(n);
+    std::vector<double> pmf(n), row;
     for (int s = 0; s < nbx; ++s) {
         if (!g.reservoir[std::size_t(s)]) continue;
+        if (e && g.mat[std::size_t(s)] != e->mat) continue;  // another crystal's reservoir
         const GBox& rb = g.boxes[std::size_t(s)];
         for (int ci = 0; ci < rb.ncontacts; ++ci) {
             const int c = g.contacts[std::size_t(rb.contact_off + ci)].id;
             if (g.reservoir[std::size_t(c)] || g.tto[std::size_t(c)] >= 0) continue;
             const GBorder& b = g.contact_borders[std::size_t(rb.contact_off + ci)];
             if (almost_equal(norm(sub(b.p2, b.p1)), 0.)) continue;
+            // Isothermal_walls, src/beyondRTA_MC2d.cpp:484-487 (and
+            // Init_generator): a reservoir injects into its own material only
+            if (e && g.mat[std::size_t(c)] != e->mat)
+                throw Error(BTE_ERR_INPUT, "Injection from material A to B is not allowed");
             const double Tw = g.Teq[std::size_t(s)], Te = g.Teq[std::size_t(c)];
             if (almost_equal(Tw, Te)) continue;
             for (std::size_t k = 0; k < n; ++k) {
@@ -614,10 +629,11 @@ Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool
             W.sa = b.p1;
             W.sb = b.p2;
             W.flux = W.sign * (cumulsum / (double(m.nq) * vuc));
-            auto cdf = fill_cumulative(pmf);
+            const std::vector<double>& rw = embed_row(pmf, e, row);
+            auto cdf = fill_cumulative(rw);
             R.cdf.insert(R.cdf.end(), cdf.begin(), cdf.end());
-            std::vector<Alias> al(n);
-            alias_table(pmf.data(), int(n), al.data());
+            std::vector<Alias> al(rw.size());
+            alias_table(rw.data(), int(rw.size()), al.data());
             R.alias.insert(R.alias.end(), al.begin(), al.end());
             R.walls.push_back(W);
         }
@@ -829,13 +845,14 @@ TranslationFast build_translation_fast(const HostGeometry& g, double margin) {
     return R;
 }
 
-Generators build_initial_generators(const HostModes& m, const HostGeometry& g) {
+Generators build_initial_generators(const HostModes& m, const HostGeometry& g, const GenEmbed* e) {
     Generators R;
     const std::size_t n = m.n();
     const double vuc = m.V * g.thickness / m.c;
-    std::vector<double> pmf(n);
+    std::vector<double> pmf(n), row;
     for (std::size_t s = 0; s < g.boxes.size(); ++s) {
         if (g.reservoir[s] || g.tto[s] >= 0) continue;
+        if (e && g.mat[s] != e->mat) continue;
         const double Tr = g.Tinit[s], Te = g.Teq[s];
         if (almost_equal(Te, Tr)) continue;
         if (Tr <= 0 || Te <= 0) throw Error(BTE_ERR_VALUE, "Invalid temperature value");
@@ -850,15 +867,16 @@ Generators build_initial_generators(const HostModes& m, const HostGeometry& g) {
         R.init_box.push_back(int(s));
         R.init_sign.push_back((Tr - Te) >= 0 ? 1 : -1);
         R.init_energy.push_back(vol * cumulsum / double(m.nq));
-        auto cdf = fill_cumulative(pmf);
+        const std::vector<double>& rw = embed_row(pmf, e, row);
+        auto cdf = fill_cumulative(rw);
         R.cdf.insert(R.cdf.end(), cdf.begin(), cdf.end());
-        std::vector<Alias> al(n);
-        alias_table(pmf.data(), int(n), al.data());
+        std::vector<Alias> al(rw.size());
+        alias_table(rw.data(), int(rw.size()), al.data());
         R.alias.insert(R.alias.end(), al.begin(), al.end());
     }
-    if (R.init_box.empty()) throw Error(BTE_ERR_INPUT, "no box with Tinit different from Teq");
+    if (R.init_box.empty() && !e) throw Error(BTE_ERR_INPUT, "no box with Tinit different from Teq");
     double total = 0;
-    for (double e : R.init_energy) total += e;
+    for (double x : R.init_energy) total += x;
     R.total_energy = total;
     return R;
 }
@@ -911,6 +929,254 @@ std::vector<int> build_mirror(const HostModes& m, const HostGeometry& g) {
         }
     }
     return mir;
+}
+
+
+HostModes concat_modes(const std::vector<HostModes>& crys, std::vector<std::size_t>& off) {
+    HostModes all;
+    off.clear();
+    std::size_t n = 0;
+    for (const HostModes& m : crys) {
+        off.push_back(n);
+        n += m.n();
+        using Field = std::vector<double> HostModes::*;
+        for (Field pr : {&HostModes::omega, &HostModes::vx, &HostModes::vy, &HostModes::vz, &HostModes::w,
+                         &HostModes::vxc, &HostModes::vyc})
+            (all.*pr).insert((all.*pr).end(), (m.*pr).begin(), (m.*pr).end());
+    }
+    // one "q point" per mode: the concatenation has no q grid (no mirror
+    // images, no spectral q mesh); the cell of crystal 0 stands in where a
+    // per-table constant is read, which the crystal paths never do
+    all.nq = int(n);
+    all.nb = 1;
+    if (!crys.empty()) {
+        all.V = crys[0].V;
+        all.c = crys[0].c;
+    }
+    return all;
+}
+
+LambertTable merge_lambert(const std::vector<LambertTable>& L, const std::vector<HostModes>& crys,
+                           const std::vector<std::size_t>& off) {
+    LambertTable R;
+    if (L.empty()) return R;
+    R.nclass = L[0].nclass;
+    std::size_t n = 0;
+    for (const HostModes& m : crys) n += m.n();
+    R.row_ptr.assign(std::size_t(R.nclass) * (n + 1), 0);
+    for (int c = 0; c < R.nclass; ++c) {
+        long long* rp = &R.row_ptr[std::size_t(c) * (n + 1)];
+        for (std::size_t k = 0; k < crys.size(); ++k) {
+            const std::size_t nk = crys[k].n(), o = off[k];
+            const long long* lp = &L[k].row_ptr[std::size_t(c) * (nk + 1)];
+            for (std::size_t j = 0; j < nk; ++j) {
+                rp[o + j] = (long long)R.col.size();
+                for (long long e = lp[j]; e < lp[j + 1]; ++e) {
+                    R.col.push_back(L[k].col[std::size_t(e)] + int(o));
+                    R.cdf.push_back(L[k].cdf[std::size_t(e)]);
+                    AliasRow a = L[k].alias[std::size_t(e)];
+                    a.keep += int(o);
+                    a.alt += int(o);
+                    R.alias.push_back(a);
+                }
+            }
+        }
+        rp[n] = (long long)R.col.size();
+    }
+    return R;
+}
+
+std::vector<int> merge_mirror(const std::vector<std::vector<int>>& mir, const std::vector<HostModes>& crys,
+                              const std::vector<std::size_t>& off, int nclass) {
+    std::size_t n = 0;
+    for (const HostModes& m : crys) n += m.n();
+    std::vector<int> R(std::size_t(nclass) * n, -1);
+    for (std::size_t k = 0; k < crys.size(); ++k) {
+        const std::size_t nk = crys[k].n();
+        for (int c = 0; c < nclass; ++c)
+            for (std::size_t j = 0; j < nk; ++j) {
+                const int v = mir[k][std::size_t(c) * nk + j];
+                R[std::size_t(c) * n + off[k] + j] = v >= 0 ? v + int(off[k]) : -1;
+            }
+    }
+    return R;
+}
+
+Generators merge_generators(std::vector<Generators>& G, bool walls, bool required) {
+    Generators R;
+    for (Generators& g : G) {
+        if (walls) R.walls.insert(R.walls.end(), g.walls.begin(), g.walls.end());
+        R.init_box.insert(R.init_box.end(), g.init_box.begin(), g.init_box.end());
+        R.init_sign.insert(R.init_sign.end(), g.init_sign.begin(), g.init_sign.end());
+        R.init_energy.insert(R.init_energy.end(), g.init_energy.begin(), g.init_energy.end());
+        R.cdf.insert(R.cdf.end(), g.cdf.begin(), g.cdf.end());
+        R.alias.insert(R.alias.end(), g.alias.begin(), g.alias.end());
+        R.total_energy += g.total_energy;
+    }
+    if (walls) {
+        if (R.walls.empty() && required)
+            throw Error(BTE_ERR_INPUT, "no isothermal wall generator (no reservoir with a different Teq)");
+        double total = 0.;
+        for (auto& W : R.walls) total += W.energy;
+        double cum = 0.;
+        for (auto& W : R.walls) {
+            cum += W.energy / total;
+            R.wall_cum.push_back(cum);
+        }
+        R.total_energy = total;
+    } else if (R.init_box.empty()) {
+        throw Error(BTE_ERR_INPUT, "no box with Tinit different from Teq");
+    }
+    return R;
+}
+
+DmmTable build_dmm_table(const HostModes& A, std::size_t offA, const HostModes& B, std::size_t offB,
+                         std::size_t n_total, V2 nrm, double VA, double VB, double Tref, int nthreads) {
+    const double nn = std::sqrt(nrm.x * nrm.x + nrm.y * nrm.y);
+    if (!(nn > 0.)) throw Error(BTE_ERR_VALUE, "invalid normal vector");
+    const double ux = nrm.x / nn, uy = nrm.y / nn, uz = 0. / nn;
+    constexpr double scalebroad = 0.1;
+    // every mode of A then of B, q-major: side, index in its crystal, v.n,
+    // C = C(omega, Tref) / (kB nq V), and its Gaussian_for_DOS
+    // (include/dos.hpp:49-63): mu, sigma, the window (lbound, ubound)
+    struct M {
+        int side;
+        std::size_t j;
+        double vn, C, mu, sigma, lo, hi;
+        bool has;
+    };
+    std::vector<M> all;
+    const HostModes* cr[2] = {&A, &B};
+    const double V[2] = {VA, VB};
+    for (int s = 0; s < 2; ++s) {
+        const HostModes& m = *cr[s];
+        for (std::size_t k = 0; k < m.n(); ++k) {
+            M x;
+            x.side = s;
+            x.j = k;
+            x.vn = ux * m.vx[k] + uy * m.vy[k] + uz * m.vz[k];
+            x.C = bose_einstein_kernel(m.omega[k], Tref) / (kB * double(m.nq) * V[s]);
+            double r[3];
+            for (int a = 0; a < 3; ++a)
+                r[a] = m.vx[k] * m.dq[0 + 3 * a] + m.vy[k] * m.dq[1 + 3 * a] + m.vz[k] * m.dq[2 + 3 * a];
+            x.mu = m.omega[k];
+            x.sigma = scalebroad * (std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) / std::sqrt(12.));
+            x.lo = x.mu - nsigma * x.sigma < 0. ? 0. : x.mu - nsigma * x.sigma;
+            x.hi = x.mu + nsigma * x.sigma;
+            x.has = !(x.mu == 0. || x.sigma == 0.);
+            all.push_back(x);
+        }
+    }
+    const double root_two_pi = std::sqrt(2. * PI);
+    auto pdf = [&](const M& c, double t) {
+        if (!c.has) return 0.;
+        double e = t - c.mu;
+        e *= -e;
+        e /= 2 * c.sigma * c.sigma;
+        double v = std::exp(e);
+        v /= c.sigma * root_two_pi;
+        return v;
+    };
+    auto emission = [](const M& c) { return (c.side == 0 && c.vn < 0.) || (c.side == 1 && c.vn > 0.); };
+    // the candidates by mu, for windows: a candidate is compatible with
+    // target t when lo < t < hi, and hi - lo <= 2 nsigma sigma_max
+    std::vector<int> byw;
+    double smax = 0.;
+    for (std::size_t i = 0; i < all.size(); ++i)
+        if (emission(all[i])) {
+            byw.push_back(int(i));
+            smax = std::max(smax, all[i].sigma);
+        }
+    std::sort(byw.begin(), byw.end(), [&](int a, int b) {
+        return all[std::size_t(a)].mu < all[std::size_t(b)].mu ||
+               (all[std::size_t(a)].mu == all[std::size_t(b)].mu && a < b);
+    });
+    std::vector<double> mus(byw.size());
+    for (std::size_t i = 0; i < byw.size(); ++i) mus[i] = all[std::size_t(byw[i])].mu;
+    // side A's incident lists (v.n > 0), entries in the order of `all`
+    const std::size_t nA = A.n();
+    std::vector<std::vector<int>> lst(nA);
+    std::vector<std::vector<double>> raw(nA);
+    auto work = [&](std::size_t lo, std::size_t hi) {
+        std::vector<int> cand;
+        for (std::size_t j = lo; j < hi; ++j) {
+            const M& mi = all[j];
+            if (!(mi.vn > 0.)) continue;
+            const double t = mi.mu;
+            const double half = nsigma * smax * (1. + 1e-9) + 1e-300;
+            auto a = std::lower_bound(mus.begin(), mus.end(), t - half);
+            auto b = std::upper_bound(mus.begin(), mus.end(), t + half);
+            cand.clear();
+            for (auto it = a; it != b; ++it) {
+                const int ci = byw[std::size_t(it - mus.begin())];
+                const M& c = all[std::size_t(ci)];
+                if (t > c.lo && t < c.hi) cand.push_back(ci);
+            }
+            std::sort(cand.begin(), cand.end());  // the order of `all`
+            for (int ci : cand) {
+                const M& c = all[std::size_t(ci)];
+                lst[j].push_back(ci);
+                raw[j].push_back(c.C * std::fabs(c.vn) * 1.0 * pdf(c, t));
+            }
+        }
+    };
+    if (nthreads < 1) nthreads = 1;
+    {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nthreads; ++t)
+            th.emplace_back(work, nA * std::size_t(t) / std::size_t(nthreads),
+                            nA * std::size_t(t + 1) / std::size_t(nthreads));
+        for (auto& t : th) t.join();
+    }
+    double total = 0.;
+    for (std::size_t j = 0; j < nA; ++j)
+        for (double r : raw[j]) total += r;
+    // incident modes without a transition: the reflection of the closest
+    // frequency, recorded with the side of the last mode scanned (always B,
+    // as the reference's side_out variable ends the scan)
+    const int fix_side = all.back().side;
+    for (std::size_t j = 0; j < nA; ++j) {
+        const M& mi = all[j];
+        if (!(mi.vn > 0.) || !lst[j].empty()) continue;
+        long long best = -1;
+        double dmin = 1e300;
+        for (std::size_t ci = 0; ci < all.size(); ++ci) {
+            const M& c = all[ci];
+            if (c.side != 0 || !emission(c)) continue;
+            const double d = std::fabs(c.mu - mi.mu);
+            if (d < dmin) {
+                best = (long long)ci;
+                dmin = d;
+            }
+        }
+        if (best < 0) throw Error(BTE_ERR_VALUE, "no matching mode was found for some incident mode");
+        const M& c = all[std::size_t(best)];
+        if (c.j >= (fix_side == 0 ? A.n() : B.n()))
+            throw Error(BTE_ERR_VALUE, "a reflection index beyond the other material's table");
+        lst[j].push_back(-1 - int(best));  // marks the side quirk
+        const double r = c.C * std::fabs(c.vn) * 1.0;
+        raw[j].push_back(r);
+        total += r;
+    }
+    DmmTable T;
+    T.row.assign(n_total + 1, 0);
+    double pc = 0.;
+    for (std::size_t K = 0; K < n_total; ++K) {
+        T.row[K] = (long long)T.out.size();
+        if (K < offA || K >= offA + nA) continue;
+        const std::size_t j = K - offA;
+        for (std::size_t e = 0; e < lst[j].size(); ++e) {
+            const int ci = lst[j][e];
+            const M& c = all[std::size_t(ci >= 0 ? ci : -1 - ci)];
+            const int side = ci >= 0 ? c.side : fix_side;
+            pc += raw[j][e] / total;
+            T.out.push_back(int((side == 0 ? offA : offB) + c.j));
+            T.side.push_back(side);
+            T.cum.push_back(pc);
+        }
+    }
+    T.row[n_total] = (long long)T.out.size();
+    return T;
 }
 
 }  // namespace bte

@@ -128,7 +128,16 @@ void build_resample(const HostModes& m, double T0, std::vector<double>& cdf,
 // Lambert table rows per (wall-normal class, incoming mode).
 LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthreads);
 
-Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required = true);
+// A crystal's generators inside the concatenated mode space of several
+// crystals: only the reservoirs (walls) or boxes (initial deviation) of
+// material `mat`, their rows `n` long with the crystal's modes from `off`
+// and zeros elsewhere.
+struct GenEmbed {
+    int mat;
+    std::size_t off, n;
+};
+Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required = true,
+                                 const GenEmbed* e = nullptr);
 
 // Temperature-gradient sources of the steady state: one Nabla_T_distribution
 // per box that is neither a reservoir nor periodic (src/sampling.cpp:118-187,
@@ -158,7 +167,7 @@ std::vector<V2> calculate_gradientT(const HostGeometry& g);
 // (zero without rows).
 V2 min_norm_lstsq2(const std::vector<double>& hx, const std::vector<double>& hy, const std::vector<double>& d);
 // Distributions of the initial deviation per box (no particle counts).
-Generators build_initial_generators(const HostModes& m, const HostGeometry& g);
+Generators build_initial_generators(const HostModes& m, const HostGeometry& g, const GenEmbed* e = nullptr);
 // Particle counts per box for N particles (Ntogenerate stochastic rounding):
 // fills init_first and returns Eeff.
 double initial_counts(Generators& G, int64_t nparticles, uint64_t seed);
@@ -182,5 +191,33 @@ struct Spline1D {
 double calc_cv(const HostModes& m, double T);
 double bose_einstein(double omega, double T);
 double bose_einstein_kernel(double omega, double T);
+
+// ---- several crystals (one mode table per material, joined by diffuse
+// mismatch interfaces).  Their modes are concatenated: global mode
+// off[k] + j is mode j of crystal k.
+HostModes concat_modes(const std::vector<HostModes>& crys, std::vector<std::size_t>& off);
+// The crystals' Lambert tables (each built on its own modes) as one table
+// over the global modes; rows keep their crystal's modes.
+LambertTable merge_lambert(const std::vector<LambertTable>& L, const std::vector<HostModes>& crys,
+                           const std::vector<std::size_t>& off);
+std::vector<int> merge_mirror(const std::vector<std::vector<int>>& mir, const std::vector<HostModes>& crys,
+                              const std::vector<std::size_t>& off, int nclass);
+// Generators of each crystal (embedded rows) as one set: walls in crystal
+// order, the wall weights over all of them.
+Generators merge_generators(std::vector<Generators>& G, bool walls, bool required);
+
+// The diffuse mismatch table of the interface from crystal A (modes at
+// offset offA) to crystal B (offB), normal n from A to B, cells' volumes VA,
+// VB (scaled to the thickness), broadening factor 0.1, at Tref
+// (Diffuse_mismatch_distribution, src/sampling.cpp:437-830, side A lists):
+// for global incident mode K, entries [row[K], row[K + 1]) of (global mode
+// out, side out: 0 = A, 1 = B, cumulative).
+struct DmmTable {
+    std::vector<long long> row;  // n_total + 1
+    std::vector<int> out, side;
+    std::vector<double> cum;
+};
+DmmTable build_dmm_table(const HostModes& A, std::size_t offA, const HostModes& B, std::size_t offB,
+                         std::size_t n_total, V2 n, double VA, double VB, double Tref, int nthreads);
 
 }  // namespace bte

@@ -430,14 +430,16 @@ def _pack(boxes, Teq, Tinit, res, thickness):
 
 
 def write_geometry_xml(path: str, geom: dict, material: str = "synthetic") -> None:
-    """Geometry XML in the schema of read_geometry_XML (src/geometry_2d.cpp:408-522)."""
+    """Geometry XML in the schema of read_geometry_XML (src/geometry_2d.cpp:408-522).
+    With a "material" array, box b's MaterialID is `material` + its index."""
     lines = ["<Geometry>", f'    <number_of_boxes Ngeom="{geom["nboxes"]}"/>']
     off = 0
     for i in range(geom["nboxes"]):
         n = int(geom["npoints"][i])
         lines.append("    <Box>")
         lines.append(f'        <BoxID id="{i}"/>')
-        lines.append(f'        <MaterialID name="{material}"/>')
+        mname = material + str(int(geom["material"][i])) if geom.get("material") is not None else material
+        lines.append(f'        <MaterialID name="{mname}"/>')
         lines.append(f'        <Vertices dim="2" npoints="{n}">')
         for k in range(n):
             x, y = geom["vertices"][2 * (off + k)], geom["vertices"][2 * (off + k) + 1]

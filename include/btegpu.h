@@ -162,6 +162,9 @@ typedef struct bte_rta_result {
     int64_t tally_updates;   /* (box, time-bin) contributions made               */
     double kernel_ms;        /* device time of the particle loop                 */
     int64_t translations;    /* jumps through periodic boxes                     */
+    int64_t interface_hits;  /* arrivals at contacts between crystals (diffuse
+                                mismatch re-emissions)                        */
+    int64_t interface_transmissions; /* of those, re-emitted into the other crystal */
 } bte_rta_result;
 
 /* Propagator exp(B dt) of one material at one temperature over the modes
@@ -335,6 +338,32 @@ bte_status bte_load_geometry(bte_ctx* ctx, const bte_geometry* geom);
  * its boxes.  NULL keeps the energy-weighted choice and one Eeff. */
 bte_status bte_load_materials(bte_ctx* ctx, int32_t nmat, const double* w, const double* T0,
                               const double* share);
+
+/* Several crystals, each with its own mode table (and rates), in one
+ * geometry: box b is in crystal bte_geometry.material[b].  Particles that
+ * reach a contact between crystals are re-emitted by the diffuse mismatch
+ * model (Diffuse_mismatch_distribution, src/sampling.cpp:437-902, as
+ * change_material_diffuse uses it, src/RTA_MC2D.cpp:871-964): one table per
+ * (crystal, other crystal, contact normal), built at the Teq of the first
+ * box that meets it.  Replaces bte_load_modes and any rate sets of
+ * bte_load_materials; reservoirs inject into their own crystal only
+ * (BTE_ERR_INPUT "Injection from material A to B is not allowed").
+ * Production transient runs on the convex-polygon kernel; the layer
+ * coupling of LDMM is not available (it needs the modes' eigenvectors and a
+ * layer description the mode tables do not carry). */
+bte_status bte_load_mode_tables(bte_ctx* ctx, int32_t ntables, const bte_mode_table* tables);
+
+/* The diffuse mismatch table of the interface from table A to table B
+ * (normal (nx, ny) pointing from A to B, material thickness, Tref), built on
+ * the host (no device needed): for incident mode i of A (v.n > 0), entries
+ * [first[i], first[i+1]) of (side out: 0 = A, 1 = B; mode out in that
+ * side's table; cumulative probability over A's incident modes).  first
+ * has nq*nb of A + 1 values; with side, mode or cum NULL only first and
+ * *nentries are filled.  The reference records the closest-frequency
+ * reflection of an incident mode without a transition with side B; kept. */
+bte_status bte_interface_table(const bte_mode_table* A, const bte_mode_table* B, double nx, double ny,
+                               double thickness, double Tref, int64_t* first, int64_t* nentries,
+                               int32_t* side, int32_t* mode, double* cum);
 
 /* Run the RTA particle loop for one run and fill `out` (replaces one
  * iteration of the run loop of src/RTA_MC2D.cpp:2188-2543: generation,

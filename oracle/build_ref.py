@@ -8,7 +8,9 @@
    against an anchor so that a moved line fails loudly), into
    oracle/_ref/snip/, compiles oracle/ref_pins.cpp against them into
    oracle/_ref/ref_pins, runs it on a seeded synthetic mode table and
-   writes tests/golden/ref_pins.json: the flight-path functions.
+   writes tests/golden/ref_pins.json: the flight-path functions; and on
+   two smaller tables, tests/golden/ref_pins_dmm.json: the diffuse
+   mismatch model between materials.
 
 Only this script reads the reference tree, and only where it exists (the
 build container); oracle/_ref/ is not committed, the fixtures it writes are,
@@ -57,6 +59,9 @@ SNIPPETS = [
     ("rta_process_segment_transient.inc", "src/RTA_MC2D.cpp", 699, "void process_segment(std::size_t ibox,", 699),
     ("rta_process_segment_periodic.inc", "src/RTA_MC2D.cpp", 784, "void process_segment(std::size_t ibox,", 784),
     ("rta_get_v.inc", "src/RTA_MC2D.cpp", 843, "inline Eigen::Vector2d get_v(", 843),
+    ("dos_gaussian.inc", "include/dos.hpp", 28, "class Gaussian_for_DOS {", 28),
+    ("sampling_hpp_dmm.inc", "include/sampling.hpp", 324, "class layer_coupling {", 402),
+    ("sampling_cpp_dmm.inc", "src/sampling.cpp", 366, "double layer_coupling::get_injection_rate(", 831),
 ]
 
 
@@ -116,11 +121,11 @@ def extract_snippets(reference: str, out_dir: str) -> None:
             f.write(f'#line {first} "{rel}"\n{body}\n')
 
 
-def _write_table(path: str) -> None:
-    """The seeded synthetic mode table of the pins: 6x6 q points x 6 branches."""
+def _write_table(path: str, n: int = 6, config: int = 100) -> None:
+    """The seeded synthetic mode table of the pins: n x n q points x 6 branches."""
     sys.path.insert(0, os.path.join(REPO, "bte-barna_gb300"))
     import synth
-    m = synth.mode_table(6, 3, 3, 300.0, config=100)
+    m = synth.mode_table(n, 3, 3, 300.0, config=config)
     n = int(m["nq"]) * int(m["nb"])
     with open(path, "w") as f:
         f.write(f"{m['nq']} {m['nb']}\n")
@@ -150,13 +155,20 @@ def build_pins(reference: str) -> str:
     return exe
 
 
-def run_pins(exe: str) -> dict:
+def run_pins(exe: str):
+    """The pins' JSON and the diffuse mismatch pins' JSON (two 4x4 x 6
+    tables of different seeds)."""
     out_dir = os.path.dirname(exe)
     table = os.path.join(out_dir, "pins_table.txt")
     _write_table(table)
-    subprocess.run([exe, table, out_dir], check=True, capture_output=True, text=True)
+    ta, tb = os.path.join(out_dir, "pins_dmm_a.txt"), os.path.join(out_dir, "pins_dmm_b.txt")
+    _write_table(ta, 4, 100)
+    _write_table(tb, 4, 101)
+    subprocess.run([exe, table, out_dir, ta, tb], check=True, capture_output=True, text=True)
     with open(os.path.join(out_dir, "ref_pins.json")) as f:
-        return json.load(f)
+        pins = json.load(f)
+    with open(os.path.join(out_dir, "ref_pins_dmm.json")) as f:
+        return pins, json.load(f)
 
 
 def reference_tree():
@@ -192,9 +204,9 @@ def main() -> int:
     exe = build(args.reference)
     text = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
     data = json.loads(text)
-    pins = run_pins(build_pins(args.reference))
+    pins, dmm = run_pins(build_pins(args.reference))
     if not args.no_write:
-        for name, d in (("ref_kat.json", data), ("ref_pins.json", pins)):
+        for name, d in (("ref_kat.json", data), ("ref_pins.json", pins), ("ref_pins_dmm.json", dmm)):
             path = os.path.join(REPO, "tests", "golden", name)
             with open(path, "w") as f:
                 json.dump(d, f, indent=1 if name == "ref_kat.json" else None)

@@ -110,6 +110,15 @@ def load():
     lib.oracle_kat_lirp.argtypes = [dp, dp, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp]
     lib.oracle_kat_gradientT.argtypes = [mtp, C.POINTER(_bt.Geometry), dp]
     lib.oracle_kat_gradientT.restype = C.c_int
+    lib.oracle_rta_run_multi.argtypes = [mtp, C.c_int, C.POINTER(_bt.Geometry), C.POINTER(_bt.RtaParams), C.c_int,
+                                         C.POINTER(_bt.RtaResult), lp]
+    lib.oracle_rta_run_multi.restype = C.c_int
+    lib.oracle_kat_dmm.argtypes = [mtp, mtp, C.c_double, C.c_double, C.c_double, C.c_double, lp, lp, lp,
+                                   ip, lp, dp]
+    lib.oracle_kat_dmm.restype = C.c_int
+    lib.oracle_kat_dmm_reemit.argtypes = [mtp, mtp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                          C.c_uint64, C.c_int, lp, ip, lp]
+    lib.oracle_kat_dmm_reemit.restype = C.c_int
     _lib = lib
     return lib
 
@@ -414,6 +423,93 @@ def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, 
                specular_hits=int(r.specular_hits), translations=int(r.translations),
                loop_seconds=float(cnt[6]) * 1e-6)
     return out
+
+
+def rta_run_multi(tables, geom, T0, dt, maxtime, N, seed=1, nthreads=8, source=None, specularity=0.0,
+                  ballistic=False, begin=0, end=0):
+    """A geometry of several materials with their own mode tables (box b in
+    material geom["material"][b]), diffuse mismatch at their contacts."""
+    if source is None:
+        source = _bt.SOURCE_WALLS
+    lib = load()
+    keep = []
+    arr = (_bt.ModeTable * len(tables))()
+    for i, t in enumerate(tables):
+        ms, k = _bt.mode_struct(t)
+        arr[i] = ms
+        keep.append(k)
+    gs, k2 = _bt.geom_struct(geom)
+    p = _bt.params_struct(T0, dt, maxtime, N, seed, _bt.MODE_PRODUCTION, source, ballistic, specularity, begin, end)
+    nbins = int(np.floor(maxtime / dt + 1e-6))
+    shape = (int(geom["nboxes"]), nbins)
+    out = {k: np.zeros(shape) for k in ("gz", "gz_jx", "gz_jy", "temperature", "jx", "jy")}
+    r = _bt.RtaResult()
+    for k in out:
+        setattr(r, k, out[k].ctypes.data_as(C.POINTER(C.c_double)))
+    cnt = np.zeros(9, dtype=np.int64)
+    st = lib.oracle_rta_run_multi(arr, len(tables), C.byref(gs), C.byref(p), int(nthreads), C.byref(r),
+                                  cnt.ctypes.data_as(C.POINTER(C.c_longlong)))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    out.update(Eeff=r.Eeff, energy_rate=r.energy_rate, events=int(cnt[0]), wall_hits=int(cnt[1]),
+               crossings=int(cnt[2]), absorbed=int(cnt[3]), nudges=int(cnt[4]), quirks=int(cnt[5]),
+               loop_seconds=float(cnt[6]) * 1e-6, interface_hits=int(cnt[7]),
+               interface_transmissions=int(cnt[8]))
+    return out
+
+
+def dmm_table(A, B, normal, thickness, Tref):
+    """The restatement's diffuse mismatch table of mode tables A and B
+    (normal from A to B): per side s a list over incident modes of arrays
+    (side_out, mode_out, cumulative)."""
+    lib = load()
+    ma, k1 = _bt.mode_struct(A)
+    mb, k2 = _bt.mode_struct(B)
+    ne = np.zeros(2, dtype=np.int64)
+    lp_ = C.POINTER(C.c_longlong)
+    args = (C.byref(ma), C.byref(mb), float(normal[0]), float(normal[1]), float(thickness), float(Tref))
+    st = lib.oracle_kat_dmm(*args, ne.ctypes.data_as(lp_), None, None, None, None, None)
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    nA, nB = int(A["omega"].size), int(B["omega"].size)
+    fa = np.zeros(nA + 1, dtype=np.int64)
+    fb = np.zeros(nB + 1, dtype=np.int64)
+    tot = int(ne.sum())
+    side = np.zeros(tot, dtype=np.int32)
+    idx = np.zeros(tot, dtype=np.int64)
+    cum = np.zeros(tot)
+    st = lib.oracle_kat_dmm(*args, ne.ctypes.data_as(lp_), fa.ctypes.data_as(lp_), fb.ctypes.data_as(lp_),
+                            side.ctypes.data_as(C.POINTER(C.c_int)), idx.ctypes.data_as(lp_),
+                            cum.ctypes.data_as(C.POINTER(C.c_double)))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    out = []
+    base = 0
+    for f, n in ((fa, nA), (fb, nB)):
+        lists = [(side[base + f[i]:base + f[i + 1]], idx[base + f[i]:base + f[i + 1]], cum[base + f[i]:base + f[i + 1]])
+                 for i in range(n)]
+        out.append(lists)
+        base += int(f[n])
+    return out
+
+
+def dmm_reemit(A, B, normal, thickness, Tref, seed, stream, idx_in):
+    """Draws of the restatement's diffuse mismatch re-emission, incident
+    modes idx_in of side A in turn from one pcg64(seed, stream): (side out,
+    mode out) per draw."""
+    lib = load()
+    ma, k1 = _bt.mode_struct(A)
+    mb, k2 = _bt.mode_struct(B)
+    ii = np.ascontiguousarray(idx_in, dtype=np.int64)
+    side = np.zeros(ii.size, dtype=np.int32)
+    io = np.zeros(ii.size, dtype=np.int64)
+    lp_ = C.POINTER(C.c_longlong)
+    st = lib.oracle_kat_dmm_reemit(C.byref(ma), C.byref(mb), float(normal[0]), float(normal[1]), float(thickness),
+                                   float(Tref), int(seed), int(stream), int(ii.size), ii.ctypes.data_as(lp_),
+                                   side.ctypes.data_as(C.POINTER(C.c_int)), io.ctypes.data_as(lp_))
+    if st != 0:
+        raise _bt.BteError(st, lib.oracle_last_error().decode())
+    return side, io
 
 
 def geometry_dump(g: dict) -> np.ndarray:

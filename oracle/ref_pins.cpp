@@ -117,10 +117,13 @@ namespace alma {
 #include "particle_sign.inc"
 #include "calc_percentiles_log.inc"
 
-// One q point of the stand-in grid: omega (nb) and group velocities (3 x nb).
+// One q point of the stand-in grid: omega (nb) and group velocities (3 x nb)
+// (wfs: eigenvectors, read only by the layer-coupling branch of the
+// mismatch model, which the pins do not take).
 struct Spectrum_at_point {
     Eigen::ArrayXd omega;
     Eigen::ArrayXXd vg;
+    Eigen::MatrixXcd wfs;
 };
 
 // Stand-in for alma::Gamma_grid with trivial symmetry.
@@ -140,6 +143,22 @@ public:
 
 #include "sampling_hpp.inc"
 #include "sampling_cpp.inc"
+
+// Stand-ins of Crystal_structure (the cell volume and lattice vectors) and of
+// D_particle (its mode indices) for the diffuse mismatch model.
+struct Crystal_structure {
+    double V = 0;
+    Eigen::Matrix3d lattvec = Eigen::Matrix3d::Identity();
+};
+struct D_particle {
+    std::size_t q = 0, alpha = 0;
+};
+#include "dos_gaussian.inc"
+// the lookup tables of the mismatch model are private: the pins read them
+#define private public
+#include "sampling_hpp_dmm.inc"
+#undef private
+#include "sampling_cpp_dmm.inc"
 
 #include "collision_error_bound.inc"
 void Arnoldi_algorithm(const Eigen::MatrixXd& A, const Eigen::VectorXd& b, int n, Eigen::MatrixXd& B,
@@ -604,5 +623,74 @@ int main(int argc, char** argv) {
         << ", \"V\": " << num(tab.V) << ", \"c_lat\": " << num(tab.c) << "}";
     std::ofstream out(scratch + "/ref_pins.json");
     out << "{" << J.o.str() << "\n}\n";
+    if (argc > 3) {  // the diffuse mismatch model between the tables of argv[3] and argv[4]
+        const Table ta = read_table(argv[3]), tb = read_table(argv[4]);
+        auto ga = make_grid(ta), gb = make_grid(tb);
+        alma::Crystal_structure ca, cb;
+        ca.V = ta.V;
+        ca.lattvec(2, 2) = ta.c;
+        cb.V = tb.V;
+        cb.lattvec(2, 2) = tb.c;
+        Json D;
+        const double normals[][2] = {{1.0, 0.0}, {0.6, -0.8}};
+        const double thick = 0.335, Tref = 300.0;
+        D.key("cases");
+        D.o << "[";
+        for (int c = 0; c < 2; ++c) {
+            Eigen::Vector3d nw(normals[c][0], normals[c][1], 0.);
+            pcg64 rng(20261204ull, 900ull + unsigned(c));
+            alma::Diffuse_mismatch_distribution dm(*ga, ca, *gb, cb, nw, 0.1, rng, Tref, thick, thick);
+            std::string L;
+            for (int side = 0; side < 2; ++side) {
+                const auto& look = side == 0 ? dm.lookup_incidentA : dm.lookup_incidentB;
+                std::string s = "[";
+                for (std::size_t i = 0; i < look.size(); ++i) {
+                    s += (i ? ", [" : "[");
+                    for (std::size_t j = 0; j < look[i].size(); ++j)
+                        s += std::string(j ? ", " : "") + "[" + std::to_string(std::get<0>(look[i][j]) == 'A' ? 0 : 1) +
+                             ", " + std::to_string(std::get<1>(look[i][j])) + ", " + num(std::get<2>(look[i][j])) + "]";
+                    s += "]";
+                }
+                L += std::string(side ? ", \"B\": " : "\"A\": ") + s + "]";
+            }
+            // draws of reemit from the object's own pcg64 (a copy of rng
+            // taken at construction): incident modes of A, 8 draws each
+            std::string R = "[";
+            int cnt = 0;
+            for (std::size_t i = 0; i < dm.lookup_incidentA.size() && cnt < 12; ++i) {
+                if (dm.lookup_incidentA[i].size() < 3) continue;
+                for (int d = 0; d < 8; ++d) {
+                    alma::D_particle p;
+                    p.q = i / ta.nb;
+                    p.alpha = i % ta.nb;
+                    const char side = dm.reemit('A', p);
+                    R += std::string(cnt || d ? ", " : "") + "[" + std::to_string(i) + ", " +
+                         std::to_string(side == 'A' ? 0 : 1) + ", " + std::to_string(p.q) + ", " +
+                         std::to_string(p.alpha) + "]";
+                }
+                ++cnt;
+            }
+            R += "]";
+            D.o << (c ? ", " : "") << "{\"normal\": [" << num(normals[c][0]) << ", " << num(normals[c][1])
+                << "], \"seed\": 20261204, \"stream\": " << (900 + c) << ", " << L << ", \"reemit\": " << R << "}";
+        }
+        D.o << "]";
+        D.key("thickness");
+        D.o << num(thick);
+        D.key("Tref");
+        D.o << num(Tref);
+        D.key("scalebroad");
+        D.o << num(0.1);
+        for (int t = 0; t < 2; ++t) {
+            const Table& tt = t == 0 ? ta : tb;
+            D.key(t == 0 ? "modes_A" : "modes_B");
+            D.o << "{\"nq\": " << tt.nq << ", \"nb\": " << tt.nb << ", \"omega\": " << arr(tt.omega)
+                << ", \"vg\": " << arr(tt.vg) << ", \"w\": " << arr(tt.w) << ", \"dq\": " << arr(tt.dq)
+                << ", \"V\": " << num(tt.V) << ", \"c_lat\": " << num(tt.c) << "}";
+        }
+        std::ofstream od(scratch + "/ref_pins_dmm.json");
+        od << "{" << D.o.str() << "\n}\n";
+        if (!od) return 1;
+    }
     return out ? 0 : 1;
 }

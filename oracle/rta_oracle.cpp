@@ -47,6 +47,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <tuple>
 #include <numeric>
 #include <stdexcept>
 #include <string>
@@ -726,14 +727,17 @@ inline std::size_t bounce(const Sim& S, V2 npout, std::size_t imode, Pcg64& rng)
 
 // Generators of Init_generator, src/RTA_MC2D.cpp:289-418, in the order
 // (reservoir id, injection box id).
-inline void build_generators(Sim& S, double /*T0*/, bool required = true) {
+inline void build_generators(Sim& S, double /*T0*/, bool required = true, int only_mat = -1) {
     S.gens.clear();
     const Modes& m = S.m;
     const double vuc = m.V * S.thickness / m.c;
     for (auto& s : S.sys) {
         if (!s.reservoir) continue;
+        if (only_mat >= 0 && s.mat != only_mat) continue;  // another material's reservoir
         for (auto& [c, bv] : s.contacts) {
             if (S.sys[c].reservoir || S.sys[c].periodic) continue;
+            if (only_mat >= 0 && S.sys[c].mat != s.mat && !almost_equal(norm(bv[0].p2 - bv[0].p1), 0.))
+                throw input_error("Injection from material A to B is not allowed");
             const Border& b = bv[0];
             if (almost_equal(norm(b.p2 - b.p1), 0.)) continue;
             if (almost_equal(s.Teq, S.sys[c].Teq)) continue;
@@ -794,6 +798,7 @@ struct Tally {
     std::vector<int64_t> scnt;  // steady: signed segments per [loc][mode]
     int64_t events = 0, wall_hits = 0, crossings = 0, absorbed = 0, nudges = 0,
             quirks = 0, specular = 0, translations = 0;
+    int64_t interface_hits = 0, interface_transmissions = 0;  // diffuse mismatch
     void init(std::size_t nbx, std::size_t nbn) {
         nboxes = nbx;
         nbins = nbn;
@@ -950,9 +955,232 @@ inline std::pair<std::size_t, V2> translate(const Sim& S, std::size_t ib, V2 r0,
     throw geometry_error("Error in Translation");
 }
 
+// ---- Diffuse mismatch interfaces between materials
+// (Diffuse_mismatch_distribution, src/sampling.cpp:437-880, without the
+// layer coupling of LDMM; change_material_diffuse, src/RTA_MC2D.cpp:871-964).
+
+// Gaussian_for_DOS (include/dos.hpp:28-82) of mode k: mu = omega, sigma =
+// scalebroad * base_sigma(v) (include/qpoint_grid.hpp:179-181), the
+// compatibility window [lbound, ubound] of nsigma sigmas (lbound 0 when it
+// would be negative); no distribution when mu or sigma is 0.
+struct DosGauss {
+    double mu = 0, sigma = 0, lbound = 0, ubound = 0;
+    bool has = false;
+};
+inline DosGauss dos_gauss(const Modes& m, std::size_t k, double scalebroad) {
+    const double v[3] = {m.vx[k], m.vy[k], m.vz[k]};
+    double r[3];
+    for (int j = 0; j < 3; ++j) r[j] = v[0] * m.dq[0 + 3 * j] + v[1] * m.dq[1 + 3 * j] + v[2] * m.dq[2 + 3 * j];
+    DosGauss g;
+    g.mu = m.omega[k];
+    g.sigma = scalebroad * (std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) / std::sqrt(12.));
+    const bool truncated = g.mu - nsigma * g.sigma < 0.;
+    g.lbound = truncated ? 0. : g.mu - nsigma * g.sigma;
+    g.ubound = g.mu + nsigma * g.sigma;
+    g.has = !(g.mu == 0. || g.sigma == 0.);
+    return g;
+}
+// boost::math::pdf of the normal distribution, in its own order of operations
+inline double dos_pdf(const DosGauss& g, double x) {
+    if (!g.has) return 0.;
+    double e = x - g.mu;
+    e *= -e;
+    e /= 2 * g.sigma * g.sigma;
+    double pdf = std::exp(e);
+    pdf /= g.sigma * std::sqrt(2. * PI);
+    return pdf;
+}
+
+// One interface: per incident mode of side A (0) or B (1), its lookup
+// entries (side out, mode index out, cumulative probability), the
+// cumulative running over all incident modes of that side.
+struct DmmEntry {
+    int side;
+    std::size_t idx;
+    double cum;
+};
+struct Dmm {
+    std::size_t nb[2] = {0, 0};
+    std::vector<std::vector<DmmEntry>> in[2];
+};
+
+// The Diffuse_mismatch_distribution constructor: normal n points from A to
+// B; V[s] are the cells' volumes scaled to the thickness.
+inline Dmm build_dmm(const Modes& A, const Modes& B, double VA, double VB, V2 n, double scalebroad, double Tref) {
+    const double nn = std::sqrt(n.x * n.x + n.y * n.y);
+    if (nn == 0.) throw value_error("invalid normal vector");
+    const double ux = n.x / nn, uy = n.y / nn, uz = 0. / nn;
+    struct Mode {
+        int side;
+        std::size_t branch, q;
+        double vn, C;
+        DosGauss g;
+    };
+    const Modes* M[2] = {&A, &B};
+    const double V[2] = {VA, VB};
+    std::vector<Mode> all;
+    all.reserve(A.n() + B.n());
+    for (int s = 0; s < 2; ++s) {
+        const Modes& m = *M[s];
+        for (std::size_t q = 0; q < std::size_t(m.nq); ++q)
+            for (std::size_t b = 0; b < std::size_t(m.nb); ++b) {
+                const std::size_t k = q * std::size_t(m.nb) + b;
+                Mode md;
+                md.side = s;
+                md.branch = b;
+                md.q = q;
+                md.vn = ux * m.vx[k] + uy * m.vy[k] + uz * m.vz[k];
+                md.C = bose_einstein_kernel(m.omega[k], Tref) / (kB * double(m.nq) * V[s]);
+                md.g = dos_gauss(m, k, scalebroad);
+                all.push_back(md);
+            }
+    }
+    Dmm D;
+    D.nb[0] = std::size_t(A.nb);
+    D.nb[1] = std::size_t(B.nb);
+    D.in[0].assign(A.n(), {});
+    D.in[1].assign(B.n(), {});
+    std::vector<std::vector<double>> raw[2];
+    raw[0].assign(A.n(), {});
+    raw[1].assign(B.n(), {});
+    auto incident = [](const Mode& md) { return (md.side == 0 && md.vn > 0.) || (md.side == 1 && md.vn < 0.); };
+    auto emission = [](const Mode& md) { return (md.side == 0 && md.vn < 0.) || (md.side == 1 && md.vn > 0.); };
+    // every allowed transition, per incident mode (independent lists,
+    // filled on several threads; the totals are summed below in the
+    // reference's order)
+    auto work = [&](std::size_t lo, std::size_t hi) {
+        for (std::size_t li = lo; li < hi; ++li) {
+            const Mode& mi = all[li];
+            if (!incident(mi)) continue;
+            const std::size_t idx_in = mi.branch + mi.q * D.nb[mi.side];
+            const double target = mi.g.mu;
+            auto& lst = D.in[mi.side][idx_in];
+            auto& rw = raw[mi.side][idx_in];
+            for (const Mode& c : all) {
+                if (!(emission(c) && target > c.g.lbound && target < c.g.ubound)) continue;
+                const double r = c.C * std::fabs(c.vn) * 1.0 * dos_pdf(c.g, target);
+                lst.push_back(DmmEntry{c.side, c.branch + c.q * D.nb[c.side], 0.});
+                rw.push_back(r);
+            }
+        }
+    };
+    {
+        const std::size_t nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> th;
+        for (std::size_t t = 0; t < nt; ++t)
+            th.emplace_back(work, all.size() * t / nt, all.size() * (t + 1) / nt);
+        for (auto& t : th) t.join();
+    }
+    double total[2] = {0., 0.};
+    for (const Mode& mi : all) {
+        if (!incident(mi)) continue;
+        for (double r : raw[mi.side][mi.branch + mi.q * D.nb[mi.side]]) total[mi.side] += r;
+    }
+    // incident modes without a transition: the reflection of the closest
+    // frequency.  The reference records it with the side of the last mode
+    // it scanned (its side_out variable is assigned for every candidate),
+    // which is always B: an incident mode of A leaves into B with the index
+    // of A's reflection read in B's table.  Kept.
+    const int fix_side = all.empty() ? 0 : all.back().side;
+    for (const Mode& mi : all) {
+        if (!incident(mi)) continue;
+        const std::size_t idx_in = mi.branch + mi.q * D.nb[mi.side];
+        if (!D.in[mi.side][idx_in].empty()) continue;
+        const double target = mi.g.mu;
+        long long best = -1;
+        double dmin = 1e300;
+        for (std::size_t ci = 0; ci < all.size(); ++ci) {
+            const Mode& c = all[ci];
+            if (c.side != mi.side || !emission(c)) continue;
+            const double d = std::fabs(c.g.mu - target);
+            if (d < dmin) {
+                best = (long long)ci;
+                dmin = d;
+            }
+        }
+        if (best < 0) throw value_error("no matching mode was found for some incident mode");
+        const Mode& c = all[std::size_t(best)];
+        const double r = c.C * std::fabs(c.vn) * 1.0;
+        const std::size_t io = c.branch + c.q * D.nb[c.side];
+        if (io >= (fix_side == 0 ? A.n() : B.n()))
+            throw value_error("a reflection index beyond the other material's table");
+        D.in[mi.side][idx_in].push_back(DmmEntry{fix_side, io, 0.});
+        raw[mi.side][idx_in].push_back(r);
+        total[mi.side] += r;
+    }
+    // cumulative probabilities over the incident modes in index order
+    for (int s = 0; s < 2; ++s) {
+        double pc = 0.;
+        for (std::size_t i = 0; i < D.in[s].size(); ++i)
+            for (std::size_t j = 0; j < D.in[s][i].size(); ++j) {
+                pc += raw[s][i][j] / total[s];
+                D.in[s][i][j].cum = pc;
+            }
+    }
+    return D;
+}
+
+// Diffuse_mismatch_distribution::reemit (src/sampling.cpp:831-880): p
+// uniform between the first and the last cumulative value of the incident
+// mode's entries, the first entry whose value is not below p.  Returns the
+// side out (-1: no entry, the reference's 'X').
+inline int dmm_reemit(const Dmm& D, int side_in, std::size_t idx_in, Pcg64& rng, std::size_t& idx_out) {
+    const auto& L = D.in[side_in][idx_in];
+    if (L.empty()) return -1;
+    const double lo = L.front().cum, hi = L.back().cum;
+    const double p = canonical(rng) * (hi - lo) + lo;
+    for (const DmmEntry& e : L)
+        if (e.cum >= p) {
+            idx_out = e.idx;
+            return e.side;
+        }
+    idx_out = L.back().idx;  // p above the last value by rounding
+    return L.back().side;
+}
+
+// The interfaces of a multi-material geometry, keyed by (material A,
+// material B, contact normal from A to B).
+struct DmmSet {
+    std::map<std::tuple<int, int, double, double>, Dmm> tab;
+    std::vector<const Modes*> modes;  // per material
+};
+
+// change_material_diffuse (src/RTA_MC2D.cpp:871-964): the particle meets
+// the contact with box inew of another material; the interface of (its
+// material, inew's, the contact normal) re-emits it on either side; the
+// flight ends there (dt = 0).  An incident mode without entries (the
+// reference's 'X') crosses with its mode unchanged, as there.
+inline void dmm_cross(const Sim& S, const DmmSet& M, Particle& p, std::size_t inew, double& dt, Pcg64& rng,
+                      Tally& T) {
+    const Box& a = S.sys[p.box];
+    V2 nw = {0., 0.};
+    for (auto& [c, bb] : a.contacts)
+        if (c == inew) {
+            nw.x += bb[0].np.x;
+            nw.y += bb[0].np.y;
+        }
+    const auto it = M.tab.find(std::make_tuple(a.mat, S.sys[inew].mat, nw.x, nw.y));
+    if (it == M.tab.end()) throw geometry_error("interface without a mismatch table");
+    const Dmm& D = it->second;
+    std::size_t idx_out = 0;
+    const int side = dmm_reemit(D, 0, p.alpha + p.q * D.nb[0], rng, idx_out);
+    if (side >= 0) {
+        p.q = idx_out / D.nb[side];
+        p.alpha = idx_out % D.nb[side];
+    } else {
+        T.quirks++;
+    }
+    T.interface_hits++;
+    if (side != 0) {
+        p.box = inew;
+        T.interface_transmissions++;
+    }
+    dt = 0.;
+}
+
 // evolparticle (transient, one material), src/RTA_MC2D.cpp:990-1386.
 inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng,
-                         Tally& T, const Opts& o) {
+                         Tally& T, const Opts& o, const DmmSet* dmm = nullptr) {
     const std::size_t nb = S.m.nb;
     V2 opos = p.pos;
     const Box& box = S.sys[p.box];
@@ -1072,6 +1300,10 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
         p.pos = rnew;
         process_segment(S, T, p.box, p.t, p.t + tf, p.sign, v, p.q * nb + p.alpha);
         p.t += tf;
+        if (dmm && S.sys[pboxes[0]].mat != S.sys[p.box].mat) {
+            dmm_cross(S, *dmm, p, pboxes[0], dt, rng, T);
+            return;
+        }
         p.box = pboxes[0];
         T.crossings++;
         return;
@@ -1091,6 +1323,10 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
         } else {
             newid = pbox2[std::size_t(uniform_int(rng, 0, int(pbox2.size()) - 1))];
         }
+        if (dmm && S.sys[newid].mat != S.sys[p.box].mat) {
+            dmm_cross(S, *dmm, p, newid, dt, rng, T);
+            return;
+        }
         p.box = newid;
         T.crossings++;
         return;
@@ -1098,14 +1334,20 @@ inline void evolparticle(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng
 }
 
 // One particle of Init_generator (walls), src/RTA_MC2D.cpp:421-511.
+inline Particle generate_at(const Sim& S, const WallGen& G, Pcg64& rng);
 inline Particle generate(const Sim& S, Pcg64& rng) {
-    const std::size_t nb = S.m.nb;
     double selectGenR = canonical(rng);
     (void)selectGenR;  // ExGen = {1, 1} without a gradient: always walls
     double whereGenR = canonical(rng);
     auto it = std::lower_bound(S.gen_cum.begin(), S.gen_cum.end(), whereGenR);
     if (it == S.gen_cum.end()) --it;
-    const WallGen& G = S.gens[std::size_t(it - S.gen_cum.begin())];
+    return generate_at(S, S.gens[std::size_t(it - S.gen_cum.begin())], rng);
+}
+
+// The rest of one particle of Init_generator from wall generator G: a point
+// on its border, its mode.
+inline Particle generate_at(const Sim& S, const WallGen& G, Pcg64& rng) {
+    const std::size_t nb = S.m.nb;
     V2 ppos;
     for (int tries = 0;; ++tries) {
         if (tries > 1000) throw limit_error("border point rejection loop");
@@ -1224,6 +1466,151 @@ inline void run_particle(const Sim& S, std::size_t pid, uint64_t seed, double ma
     }
 }
 
+
+// ============================================================ several materials
+// Geometries whose boxes hold different crystals (one mode table per
+// material, box b in material gm->material[b]), joined by diffuse mismatch
+// interfaces.  Each material keeps its own Sim (modes, Lambert rows,
+// post-scattering CDF, wall generators) over the shared boxes; a particle
+// uses the Sim of its box's material, and its mode indexes that material's
+// table.
+struct MultiSim {
+    std::vector<Sim> mats;
+    DmmSet dmm;
+    std::vector<std::pair<int, std::size_t>> gref;  // wall generators: (material, index)
+    std::vector<double> gcum;
+    double energy = 0, Eeff = 0;
+    // initial deviation: the boxes in ascending order, their material's CDF
+    std::vector<std::size_t> init_box;
+    std::vector<int> init_sign;
+    std::vector<std::vector<double>> init_cdf;
+    std::vector<long long> init_first;
+};
+
+// The interface tables of every contact between boxes of different
+// materials that are neither reservoirs nor periodic, each built at the
+// Teq of the first box (in box order) that meets it; the reference builds
+// each on first use, at the Teq of the box the first particle comes from.
+inline void build_interfaces(MultiSim& M, double scalebroad = 0.1) {
+    const Sim& S0 = M.mats[0];
+    for (auto& a : S0.sys) {
+        if (a.reservoir || a.periodic) continue;
+        for (auto& [c, bv] : a.contacts) {
+            const Box& b = S0.sys[c];
+            if (b.mat == a.mat || b.reservoir || b.periodic) continue;
+            V2 nw = {0., 0.};
+            nw.x += bv[0].np.x;
+            nw.y += bv[0].np.y;
+            const auto key = std::make_tuple(a.mat, b.mat, nw.x, nw.y);
+            if (M.dmm.tab.count(key)) continue;
+            const Modes& A = M.mats[std::size_t(a.mat)].m;
+            const Modes& B = M.mats[std::size_t(b.mat)].m;
+            const double VA = A.V * S0.thickness / A.c, VB = B.V * S0.thickness / B.c;
+            M.dmm.tab.emplace(key, build_dmm(A, B, VA, VB, nw, scalebroad, a.Teq));
+        }
+    }
+}
+
+inline Particle generate_multi(const MultiSim& M, Pcg64& rng) {
+    double selectGenR = canonical(rng);
+    (void)selectGenR;
+    double whereGenR = canonical(rng);
+    auto it = std::lower_bound(M.gcum.begin(), M.gcum.end(), whereGenR);
+    if (it == M.gcum.end()) --it;
+    const auto& gr = M.gref[std::size_t(it - M.gcum.begin())];
+    const Sim& S = M.mats[std::size_t(gr.first)];
+    Particle p = generate_at(S, S.gens[gr.second], rng);
+    p.mat = 0;  // rates and resampling come from the material's own Sim
+    return p;
+}
+
+inline Particle generate_initial_multi(const MultiSim& M, std::size_t pid, Pcg64& rng) {
+    auto it = std::upper_bound(M.init_first.begin(), M.init_first.end(), (long long)pid);
+    const std::size_t g = std::size_t(it - M.init_first.begin()) - 1;
+    const Sim& S = M.mats[std::size_t(M.mats[0].sys[M.init_box[g]].mat)];
+    const Box& B = S.sys[M.init_box[g]];
+    double x0 = B.hull[0].x, x1 = B.hull[0].x, y0 = B.hull[0].y, y1 = B.hull[0].y;
+    for (auto& h : B.hull) {
+        x0 = std::min(x0, h.x);
+        x1 = std::max(x1, h.x);
+        y0 = std::min(y0, h.y);
+        y1 = std::max(y1, h.y);
+    }
+    V2 r;
+    for (int tries = 0;; ++tries) {
+        if (tries > 100000) throw limit_error("random point rejection loop");
+        r.x = x0 + canonical(rng) * (x1 - x0);
+        r.y = y0 + canonical(rng) * (y1 - y0);
+        if (B.inside(r)) break;
+    }
+    const std::size_t pos = lower_bound_idx(M.init_cdf[g], canonical(rng));
+    Particle p;
+    p.pos = r;
+    p.q = pos / S.m.nb;
+    p.alpha = pos % S.m.nb;
+    p.sign = M.init_sign[g];
+    p.t = 0.;
+    p.box = M.init_box[g];
+    p.mat = 0;
+    return p;
+}
+
+inline void build_initial_multi(MultiSim& M, int64_t nparticles, uint64_t seed) {
+    std::vector<double> pmf, energy;
+    for (auto& s : M.mats[0].sys) {
+        if (s.reservoir || s.periodic) continue;
+        if (almost_equal(s.Teq, s.Treal)) continue;
+        if (s.Treal <= 0 || s.Teq <= 0) throw value_error("Invalid temperature value");
+        const Sim& S = M.mats[std::size_t(s.mat)];
+        const double vuc = S.m.V * S.thickness / S.m.c;
+        const double cumulsum = out_tref_pmf(S.m, s.Treal, s.Teq, pmf);
+        M.init_box.push_back(s.id);
+        M.init_sign.push_back((s.Treal - s.Teq) >= 0 ? 1 : -1);
+        M.init_cdf.push_back(fill_cumulative(pmf));
+        energy.push_back(dist_energy(s.area * S.thickness / vuc, cumulsum, double(S.m.nq)));
+    }
+    if (M.init_box.empty()) throw input_error("no box with Tinit different from Teq");
+    double total = 0;
+    for (double e : energy) total += e;
+    M.energy = total;
+    M.Eeff = total / double(nparticles);
+    long long first = 0;
+    for (std::size_t b = 0; b < M.init_box.size(); ++b) {
+        M.init_first.push_back(first);
+        const double gen = energy[b] / M.Eeff;
+        long long np = (long long)gen;
+        Pcg64 r(seed, (uint64_t(1) << 63) + uint64_t(M.init_box[b]));
+        if (canonical(r) <= gen - std::floor(gen)) np++;
+        first += np;
+    }
+    M.init_first.push_back(first);
+}
+
+inline void run_particle_multi(const MultiSim& M, std::size_t pid, uint64_t seed, double maxtime, Tally& T,
+                               const Opts& o) {
+    Pcg64 rng(seed, pid);
+    Particle p = M.init_first.empty() ? generate_multi(M, rng) : generate_initial_multi(M, pid, rng);
+    double time = 0.;
+    long long nev = 0;
+    while (time < maxtime) {
+        if (++nev > (1ll << 26)) throw limit_error("free flights per particle cap");
+        const Sim& S = M.mats[std::size_t(M.mats[0].sys[p.box].mat)];
+        const std::size_t k = p.q * std::size_t(S.m.nb) + p.alpha;
+        V2 v = get_v(S.m, k);
+        double dt_ = random_dt(S.m.w[k], rng, o.log_impl);
+        T.events++;
+        if (time + dt_ > maxtime) dt_ = maxtime - time + 1.0e-8;
+        int guard = 0;
+        while (!almost_equal(dt_, 0.)) {
+            if (++guard > 1000000) throw limit_error("flight step cap");
+            // a crossing into another material ends the flight, so the Sim
+            // stays the particle's material's for the whole loop
+            evolparticle(S, p, v, dt_, rng, T, o, &M.dmm);
+        }
+        if (p.q == 0 && p.alpha == 0) break;
+        time = p.t;
+    }
+}
 
 // ============================================================ steady state
 // The periodic / gradient branch of RTAMC2D (src/RTA_MC2D.cpp:2544-2842):
@@ -2623,6 +3010,245 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
         return fail(BTE_ERR_LIMIT, e.what());
     } catch (const std::exception& e) {
         return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
+// A transient run of a geometry of nmat materials with their own mode
+// tables mts[m] (box b in gm->material[b]), diffuse mismatch at the
+// contacts between materials; production semantics (per-particle pcg64
+// streams as oracle_rta_run, the interfaces draw from the particle's
+// stream).  counters: events, wall_hits, crossings, absorbed, nudges,
+// quirks, loop microseconds, interface hits, interface transmissions.
+int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry* gm, const bte_rta_params* rp,
+                         int nthreads, bte_rta_result* out, int64_t* counters) {
+    try {
+        if (nmat < 1 || !gm->material) return fail(BTE_ERR_INPUT, "materials need mode tables and box materials");
+        orc::MultiSim M;
+        for (int k = 0; k < nmat; ++k) M.mats.push_back(build_sim(&mts[k], gm));
+        for (auto& b : M.mats[0].sys)
+            if (b.mat < 0 || b.mat >= nmat) return fail(BTE_ERR_INPUT, "box material out of range");
+        std::size_t ntime = std::size_t(std::floor(rp->maxtime / rp->dt + 1.0e-6)) + 1;
+        double maxtime = double(ntime - 1) * rp->dt;
+        const double step = maxtime / double(ntime - 1);
+        for (auto& S : M.mats) {
+            S.timegrid.resize(ntime);
+            for (std::size_t i = 0; i < ntime; ++i) S.timegrid[i] = (i == ntime - 1) ? maxtime : double(i) * step;
+            S.resample_cdf = orc::fill_cumulative(orc::be_derivative_pmf(S.m, S.m.w, rp->T0));
+            orc::build_lambert(S);
+        }
+        orc::build_interfaces(M);
+        int64_t total_particles = rp->nparticles;
+        if (rp->source == BTE_SOURCE_WALLS) {
+            std::vector<double> e;
+            for (int k = 0; k < nmat; ++k) {
+                orc::Sim& S = M.mats[std::size_t(k)];
+                orc::build_generators(S, rp->T0, false, k);
+                for (std::size_t i = 0; i < S.gens.size(); ++i) {
+                    M.gref.push_back({k, i});
+                    e.push_back(std::fabs(S.gens[i].flux) * orc::norm(S.gens[i].b.p2 - S.gens[i].b.p1) * S.thickness);
+                }
+            }
+            if (M.gref.empty()) return fail(BTE_ERR_INPUT, "no isothermal wall generator (no reservoir with a different Teq)");
+            double total = 0.;
+            for (double x : e) total += x;
+            double cum = 0.;
+            for (double x : e) {
+                cum += x / total;
+                M.gcum.push_back(cum);
+            }
+            M.energy = total;
+            M.Eeff = total / double(rp->nparticles);
+        } else {
+            orc::build_initial_multi(M, rp->nparticles, rp->seed);
+            total_particles = M.init_first.back();
+        }
+        orc::Opts o;
+        o.ballistic = rp->ballistic != 0;
+        o.specularity = rp->specularity;
+        const std::size_t nbx = M.mats[0].sys.size(), nbn = ntime - 1;
+        int64_t begin = rp->particle_begin,
+                end = rp->particle_end > 0 ? std::min<int64_t>(rp->particle_end, total_particles) : total_particles;
+        if (end < begin) end = begin;
+        if (nthreads < 1) nthreads = 1;
+        std::vector<orc::Tally> tl(static_cast<std::size_t>(nthreads));
+        std::vector<std::string> errs(static_cast<std::size_t>(nthreads));
+        std::vector<int> codes(static_cast<std::size_t>(nthreads), 0);
+        auto work = [&](int tid) {
+            orc::Tally& T = tl[std::size_t(tid)];
+            T.init(nbx, nbn);
+            const int64_t n = end - begin;
+            const int64_t lo = begin + n * tid / nthreads, hi = begin + n * (tid + 1) / nthreads;
+            try {
+                for (int64_t i = lo; i < hi; ++i) orc::run_particle_multi(M, std::size_t(i), rp->seed, maxtime, T, o);
+            } catch (const orc::value_error& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_VALUE;
+            } catch (const orc::limit_error& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_LIMIT;
+            } catch (const orc::input_error& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_INPUT;
+            } catch (const std::exception& e) {
+                errs[std::size_t(tid)] = e.what();
+                codes[std::size_t(tid)] = BTE_ERR_GEOMETRY;
+            }
+        };
+        const auto loop_start = std::chrono::steady_clock::now();
+        {
+            std::vector<std::thread> th;
+            for (int t = 0; t < nthreads; ++t) th.emplace_back(work, t);
+            for (auto& t : th) t.join();
+        }
+        const double loop_us =
+            std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - loop_start).count();
+        for (std::size_t t = 0; t < errs.size(); ++t)
+            if (!errs[t].empty()) return fail(codes[t], errs[t].c_str());
+        orc::Tally T = std::move(tl[0]);
+        for (std::size_t t = 1; t < tl.size(); ++t) {
+            for (std::size_t k = 0; k < T.gz.size(); ++k) {
+                T.gz[k] += tl[t].gz[k];
+                T.jx[k] += tl[t].jx[k];
+                T.jy[k] += tl[t].jy[k];
+            }
+            T.events += tl[t].events;
+            T.wall_hits += tl[t].wall_hits;
+            T.crossings += tl[t].crossings;
+            T.absorbed += tl[t].absorbed;
+            T.nudges += tl[t].nudges;
+            T.quirks += tl[t].quirks;
+            T.specular += tl[t].specular;
+            T.translations += tl[t].translations;
+            T.interface_hits += tl[t].interface_hits;
+            T.interface_transmissions += tl[t].interface_transmissions;
+        }
+        out->nboxes = int32_t(nbx);
+        out->nbins = int32_t(nbn);
+        out->Eeff = M.Eeff;
+        out->energy_rate = M.energy;
+        out->events = T.events;
+        out->wall_hits = T.wall_hits;
+        out->crossings = T.crossings;
+        out->absorbed = T.absorbed;
+        out->specular_hits = T.specular;
+        out->tally_updates = 0;
+        out->translations = T.translations;
+        if (counters) {
+            counters[0] = T.events; counters[1] = T.wall_hits; counters[2] = T.crossings;
+            counters[3] = T.absorbed; counters[4] = T.nudges; counters[5] = T.quirks;
+            counters[6] = int64_t(loop_us);
+            counters[7] = T.interface_hits; counters[8] = T.interface_transmissions;
+        }
+        if (out->gz) std::copy(T.gz.begin(), T.gz.end(), out->gz);
+        if (out->gz_jx) std::copy(T.jx.begin(), T.jx.end(), out->gz_jx);
+        if (out->gz_jy) std::copy(T.jy.begin(), T.jy.end(), out->gz_jy);
+        // post-processing (src/RTA_MC2D.cpp:2336-2435), each box with its
+        // material's heat capacity and out-of-plane lattice vector
+        const orc::Sim& S0 = M.mats[0];
+        std::vector<double> gz = T.gz, jx = T.jx, jy = T.jy;
+        for (std::size_t ir = 0; ir < nbx; ++ir) {
+            const double vbox = S0.sys[ir].area * S0.thickness;
+            for (std::size_t i = 0; i < nbn; ++i) {
+                gz[ir * nbn + i] = gz[ir * nbn + i] / vbox * M.Eeff;
+                jx[ir * nbn + i] = jx[ir * nbn + i] / vbox * (M.Eeff * 1e12 * 1e9 * 1e9);
+                jy[ir * nbn + i] = jy[ir * nbn + i] / vbox * (M.Eeff * 1e12 * 1e9 * 1e9);
+            }
+        }
+        if (rp->source == BTE_SOURCE_WALLS) {
+            for (std::size_t ir = 0; ir < nbx; ++ir)
+                for (std::size_t i = 1; i < nbn; ++i) {
+                    gz[ir * nbn + i] += gz[ir * nbn + i - 1];
+                    jx[ir * nbn + i] += jx[ir * nbn + i - 1];
+                    jy[ir * nbn + i] += jy[ir * nbn + i - 1];
+                }
+        } else {
+            for (std::size_t k = 0; k < gz.size(); ++k) {
+                gz[k] /= step;
+                jx[k] /= step;
+                jy[k] /= step;
+            }
+        }
+        if (out->temperature)
+            for (std::size_t ir = 0; ir < nbx; ++ir) {
+                const orc::Modes& m = M.mats[std::size_t(S0.sys[ir].mat)].m;
+                double cv = 0.;
+                for (std::size_t k = 0; k < m.n(); ++k) cv += orc::bose_einstein_kernel(m.omega[k], rp->T0);
+                cv = cv * orc::kB / double(m.nq) / m.V;
+                const double vcorr = S0.thickness / m.c;
+                for (std::size_t i = 0; i < nbn; ++i)
+                    out->temperature[ir * nbn + i] = gz[ir * nbn + i] / (cv / vcorr) + rp->T0;
+            }
+        if (out->jx) std::copy(jx.begin(), jx.end(), out->jx);
+        if (out->jy) std::copy(jy.begin(), jy.end(), out->jy);
+        return 0;
+    } catch (const orc::input_error& e) {
+        return fail(BTE_ERR_INPUT, e.what());
+    } catch (const orc::value_error& e) {
+        return fail(BTE_ERR_VALUE, e.what());
+    } catch (const orc::limit_error& e) {
+        return fail(BTE_ERR_LIMIT, e.what());
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
+// reemit draws of the interface of tables A and B (as oracle_kat_dmm) from
+// one pcg64(seed, stream), incident modes idx_in[i] of side A in turn.
+int oracle_kat_dmm_reemit(const bte_mode_table* A, const bte_mode_table* B, double nx, double ny, double thickness,
+                          double Tref, uint64_t seed, uint64_t stream, int n, const long long* idx_in, int* side_out,
+                          long long* idx_out) {
+    try {
+        const orc::Modes a = modes_from(A), b = modes_from(B);
+        const orc::Dmm D = orc::build_dmm(a, b, a.V * thickness / a.c, b.V * thickness / b.c, orc::V2{nx, ny}, 0.1,
+                                          Tref);
+        orc::Pcg64 rng(seed, stream);
+        for (int i = 0; i < n; ++i) {
+            std::size_t io = 0;
+            side_out[i] = orc::dmm_reemit(D, 0, std::size_t(idx_in[i]), rng, io);
+            idx_out[i] = (long long)io;
+        }
+        return 0;
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_INPUT, e.what());
+    }
+}
+
+// One interface table (the Diffuse_mismatch_distribution of tables A and B,
+// normal (nx, ny) from A to B, thickness t, Tref): for incident mode i of
+// side s (0 = A, 1 = B) its entries [first[s][i], first[s][i+1]) of
+// (side out, mode out, cumulative).  Call with null outputs for the sizes
+// (nentries[2]), then with arrays of those sizes.
+int oracle_kat_dmm(const bte_mode_table* A, const bte_mode_table* B, double nx, double ny, double thickness,
+                   double Tref, long long* nentries, long long* firstA, long long* firstB, int* side, long long* idx,
+                   double* cum) {
+    try {
+        const orc::Modes a = modes_from(A), b = modes_from(B);
+        const orc::Dmm D = orc::build_dmm(a, b, a.V * thickness / a.c, b.V * thickness / b.c, orc::V2{nx, ny}, 0.1,
+                                          Tref);
+        long long k = 0;
+        for (int s = 0; s < 2; ++s) {
+            long long* first = s == 0 ? firstA : firstB;
+            long long cnt = 0;
+            for (std::size_t i = 0; i < D.in[s].size(); ++i) {
+                if (first) first[i] = cnt;
+                for (const auto& e : D.in[s][i]) {
+                    if (side) {
+                        side[k] = e.side;
+                        idx[k] = (long long)e.idx;
+                        cum[k] = e.cum;
+                    }
+                    ++k;
+                    ++cnt;
+                }
+            }
+            if (first) first[D.in[s].size()] = cnt;
+            nentries[s] = cnt;
+        }
+        return 0;
+    } catch (const orc::value_error& e) {
+        return fail(BTE_ERR_VALUE, e.what());
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_INPUT, e.what());
     }
 }
 

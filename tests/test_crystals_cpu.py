@@ -1,0 +1,92 @@
+"""Several crystals joined by diffuse mismatch interfaces (RTAMC2D with boxes
+of different materials: change_material_diffuse, src/RTA_MC2D.cpp:871-964,
+Diffuse_mismatch_distribution, src/sampling.cpp:437-902), on the CPU:
+
+- the engine's interface tables (host code of libbtegpu.so, through
+  bte_interface_table) equal the restatement's entry for entry, whose
+  tables tests/test_dmm_pins.py holds to the reference's own code;
+- the restatement's multi-crystal run reduces to its one-table run draw for
+  draw when there is one crystal;
+- with an initial deviation in a closed geometry every particle spends each
+  whole bin in some box, across interfaces included;
+- a reservoir may inject into its own crystal only."""
+import numpy as np
+import pytest
+
+import btegpu
+import pyoracle
+import synth
+
+
+def _tables():
+    return synth.mode_table(8, 3, 3, 300.0, config=100), synth.mode_table(8, 3, 3, 300.0, config=101)
+
+
+def _same(e, o):
+    return all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+               for a, b in zip(e, o))
+
+
+@pytest.mark.parametrize("normal", [(1.0, 0.0), (0.0, -1.0), (0.6, -0.8)])
+def test_engine_interface_tables_equal_the_restatement(built, normal):
+    A, B = _tables()
+    e = btegpu.interface_table(A, B, normal, 0.335, 300.0)
+    o = pyoracle.dmm_table(A, B, normal, 0.335, 300.0)[0]
+    assert len(e) == len(o) and _same(e, o)
+    assert sum(len(x[0]) for x in e) > 0
+    # tables of different sizes (window search over the other crystal)
+    A2, B2 = synth.mode_table(12, 3, 3, 300.0, config=100), synth.mode_table(8, 3, 3, 250.0, config=102)
+    assert _same(btegpu.interface_table(A2, B2, normal, 0.335, 280.0),
+                 pyoracle.dmm_table(A2, B2, normal, 0.335, 280.0)[0])
+
+
+def _two_crystal_ribbon():
+    g = synth.ribbon_geometry(200.0, 50.0, 10, T_hot=301.0, T_cold=299.0)
+    g["material"] = np.array([0] * 5 + [1] * 5 + [0, 1], dtype=np.int32)
+    return g
+
+
+def _closed_two_crystals():
+    """A 200 nm x 50 nm block of 10 x 2 cells closed by void walls, crystal 0
+    left of x = 100 nm (initially 0.5 K hot), crystal 1 right of it."""
+    g = synth.grid_geometry(200.0, 50.0, 10, 2)
+    v = np.asarray(g["vertices"], float).reshape(-1, 4, 2).mean(axis=1)
+    g["material"] = (v[:, 0] > 100.0).astype(np.int32)
+    g["Tinit"] = np.where(g["material"] == 0, 300.5, 300.0)
+    return g
+
+
+def test_one_crystal_repeats_the_single_table_run():
+    A, _ = _tables()
+    g = synth.ribbon_geometry(200.0, 50.0, 10)
+    g["material"] = np.zeros(12, dtype=np.int32)
+    case = {"modes": A, "geom": g, "T0": 300.0, "dt": 10.0, "maxtime": 300.0, "N": 4000}
+    a = pyoracle.rta_run(case, seed=5, nthreads=4)
+    b = pyoracle.rta_run_multi([A], g, 300.0, 10.0, 300.0, 4000, seed=5, nthreads=4)
+    assert np.array_equal(a["gz"], b["gz"]) and a["events"] == b["events"]
+    assert np.array_equal(a["temperature"], b["temperature"])
+    assert b["interface_hits"] == 0
+
+
+def test_two_crystals_conserve_particle_time():
+    """Without reservoirs no particle is lost: each bin's tally sums to the
+    particles times the bin width, while particles cross and bounce back at
+    the interface."""
+    A, B = _tables()
+    g = _closed_two_crystals()
+    r = pyoracle.rta_run_multi([A, B], g, 300.0, 10.0, 200.0, 20000, seed=7, nthreads=8,
+                               source=btegpu.SOURCE_INITIAL)
+    assert r["interface_hits"] > 0 and 0 < r["interface_transmissions"] < r["interface_hits"]
+    assert r["absorbed"] == 0
+    per_bin = r["gz"].sum(axis=0)
+    n = per_bin[0] / 10.0
+    assert n > 0 and abs(n - round(n)) < 1e-6
+    assert np.allclose(per_bin, per_bin[0], rtol=1e-9, atol=0)
+
+
+def test_reservoir_injects_into_its_own_crystal_only():
+    A, B = _tables()
+    g = _two_crystal_ribbon()
+    g["material"][10] = 1  # the hot reservoir (touching cell 0 of crystal 0) in crystal 1
+    with pytest.raises(btegpu.BteError, match="Injection from material A to B"):
+        pyoracle.rta_run_multi([A, B], g, 300.0, 10.0, 100.0, 1000, seed=1, nthreads=2)

@@ -1,0 +1,109 @@
+"""GPU parity of several crystals joined by diffuse mismatch interfaces
+(bte_load_mode_tables; change_material_diffuse, src/RTA_MC2D.cpp:871-964,
+Diffuse_mismatch_distribution::reemit, src/sampling.cpp:831-902): the
+polygon kernel's re-emissions against the restatement, particle time
+conserved across interfaces, and the modes this path does not take."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import btegpu
+import pyoracle
+import synth
+from parity_stats import check
+
+pytestmark = pytest.mark.gpu
+
+
+def _tables():
+    return synth.mode_table(8, 3, 3, 300.0, config=100), synth.mode_table(8, 3, 3, 300.0, config=101)
+
+
+def _ribbon():
+    """Ten 20 nm cells between a 301 K and a 299 K reservoir; cells 0-4 and
+    the hot reservoir in crystal 0, cells 5-9 and the cold one in crystal 1."""
+    g = synth.ribbon_geometry(200.0, 50.0, 10, T_hot=301.0, T_cold=299.0)
+    g["material"] = np.array([0] * 5 + [1] * 5 + [0, 1], dtype=np.int32)
+    return g
+
+
+def test_two_crystal_ribbon_agrees_with_restatement(engine):
+    A, B = _tables()
+    g = _ribbon()
+    engine.load_mode_tables([A, B])
+    engine.load_geometry(g)
+    kw = dict(T0=300.0, dt=10.0, maxtime=300.0)
+    N = 20000
+    names = ([f"T_cell{i}_late" for i in range(10)] + [f"T_cell{i}_early" for i in range(10)]
+             + ["jx_late", "transmitted"])
+
+    def obs(r):
+        T = r["temperature"][:10] - 300.0
+        return np.concatenate([T[:, -10:].mean(axis=1) * 10, T[:, 3:8].mean(axis=1) * 10,
+                               [r["jx"][:10, -10:].mean() * 1e-7,
+                                r["interface_transmissions"] / max(r["interface_hits"], 1)]])
+    R = 6
+    gpu = []
+    for i in range(R):
+        r = engine.rta_run(N=N, seed=100 + i, **kw)
+        assert r["interface_hits"] > 0
+        gpu.append(obs(r))
+    cpu = [obs(pyoracle.rta_run_multi([A, B], g, N=N, seed=200 + i, nthreads=16, **kw)) for i in range(R)]
+    check(np.array(gpu), np.array(cpu), names, "two crystals")
+    # the interface resists: a temperature step between cells 4 and 5
+    Tl = np.array(gpu)[:, :10].mean(0)
+    assert Tl[4] - Tl[5] > 2.0 * max(Tl[3] - Tl[4], Tl[5] - Tl[6])
+
+
+def test_two_crystals_conserve_particle_time(engine):
+    A, B = _tables()
+    g = synth.grid_geometry(200.0, 50.0, 10, 2)
+    v = np.asarray(g["vertices"], float).reshape(-1, 4, 2).mean(axis=1)
+    g["material"] = (v[:, 0] > 100.0).astype(np.int32)
+    g["Tinit"] = np.where(g["material"] == 0, 300.5, 300.0)
+    engine.load_mode_tables([A, B])
+    engine.load_geometry(g)
+    r = engine.rta_run(300.0, 10.0, 200.0, 20000, seed=9, source=btegpu.SOURCE_INITIAL, raw=True)
+    assert r["interface_hits"] > 0 and 0 < r["interface_transmissions"] < r["interface_hits"]
+    assert r["absorbed"] == 0
+    per_bin = r["gz"].sum(axis=0)
+    n = per_bin[0] / 10.0
+    assert n > 0 and abs(n - round(n)) < 1e-6
+    assert np.allclose(per_bin, per_bin[0], rtol=1e-9, atol=0)
+
+
+def test_crystals_take_the_production_polygon_path_only(engine):
+    A, B = _tables()
+    engine.load_mode_tables([A, B])
+    engine.load_geometry(_ribbon())
+    with pytest.raises(btegpu.BteError, match="production"):
+        engine.rta_run(300.0, 10.0, 100.0, 1000, mode=btegpu.MODE_REPLAY)
+    with pytest.raises(btegpu.BteError, match="polygon"):
+        engine.rta_run(300.0, 10.0, 100.0, 1000, flags=btegpu.FLAG_GENERAL)
+    with pytest.raises(btegpu.BteError, match="rate sets"):
+        engine.load_materials([A["w"]], [300.0])
+
+
+def test_rtamc2d_cli_reads_several_materials(built, tmp_path):
+    """rtamc2d_gpu with two <material>s and boxes naming theirs in
+    <MaterialID> runs the crystals path: the CSV's late temperatures step
+    down at the interface."""
+    A, B = _tables()
+    g = _ribbon()
+    synth.write_geometry_xml(str(tmp_path / "beam.xml"), g, material="mat")
+    synth.write_modes_file(str(tmp_path / "a.bin"), A)
+    synth.write_modes_file(str(tmp_path / "b.bin"), B)
+    (tmp_path / "input.xml").write_text(
+        '<RTA_MC2d>\n  <geometry file="beam.xml"/>\n  <time dt="10" maxtime="200"/>\n'
+        '  <material name="mat0" database="a.bin" thickness="0.335" T0="300.0"/>\n'
+        '  <material name="mat1" database="b.bin" thickness="0.335" T0="300.0"/>\n'
+        '  <particles N="20000"/>\n  <engine seed="5"/>\n</RTA_MC2d>\n')
+    exe = os.path.join(os.path.dirname(built), "rtamc2d_gpu")
+    r = subprocess.run([exe, "input.xml", "4", "1"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    T = np.loadtxt(tmp_path / "temperature_300K_run_0.csv", delimiter=",")
+    assert T.shape == (20, 1 + g["nboxes"])
+    late = T[-5:, 1:11].mean(axis=0)
+    assert late[4] - late[5] > 2.0 * max(late[3] - late[4], late[5] - late[6])
