@@ -141,7 +141,7 @@ void ensure_static(bte_ctx* c) {
             std::vector<bte::PolyRect> rect(g.boxes.size());
             for (std::size_t a = 0; a < g.boxes.size(); ++a) {
                 const bte::GBox& bx = g.boxes[a];
-                bte::PolyRect R{0., 0., 0., 0., -1, -1, -1, -1};
+                bte::PolyRect R{0., 0., 0., 0., -1, -1, -1, -1, -2, -2, -2, -2, 0, 0, 0, 0, 0, 0, 0, 0};
                 int k4[4] = {-1, -1, -1, -1};
                 double c4[4] = {0., 0., 0., 0.};
                 bool ok = bx.nborders == 4;
@@ -156,8 +156,47 @@ void ensure_static(bte_ctx* c) {
                     }
                 }
                 if (ok) {
-                    R = bte::PolyRect{-c4[1], c4[0], -c4[3], c4[2], k4[0], k4[1], k4[2], k4[3]};
+                    R.x0 = -c4[1];
+                    R.x1 = c4[0];
+                    R.y0 = -c4[3];
+                    R.y1 = c4[2];
+                    R.kx1 = k4[0];
+                    R.kx0 = k4[1];
+                    R.ky1 = k4[2];
+                    R.ky0 = k4[3];
                     if (!(R.x0 < R.x1 && R.y0 < R.y1)) R.kx1 = -1;
+                    // what lies across each whole side
+                    int nbs[4], fls[4], cls[4];
+                    for (int sd = 0; sd < 4; ++sd) {
+                        const bte::PolyBorder& P = pb[std::size_t(bx.border_off + k4[sd])];
+                        const double len = sd < 2 ? R.y1 - R.y0 : R.x1 - R.x0;
+                        cls[sd] = P.cls;
+                        fls[sd] = 0;
+                        if (P.npieces == 0) {
+                            nbs[sd] = -1;
+                        } else if (P.npieces == 1 && pieces[std::size_t(P.piece_off)].s0 <= 0. &&
+                                   pieces[std::size_t(P.piece_off)].s1 >= len) {
+                            const int nb = pieces[std::size_t(P.piece_off)].box;
+                            nbs[sd] = nb;
+                            fls[sd] = (g.reservoir[std::size_t(nb)] ? 1 : 0) | (g.tto[std::size_t(nb)] >= 0 ? 2 : 0);
+                            // a contact between crystals takes the piece lookup (its table)
+                            if (g.mat[std::size_t(nb)] != g.mat[a]) nbs[sd] = -2;
+                        } else {
+                            nbs[sd] = -2;
+                        }
+                    }
+                    R.nx1 = nbs[0];
+                    R.nx0 = nbs[1];
+                    R.ny1 = nbs[2];
+                    R.ny0 = nbs[3];
+                    R.fx1 = fls[0];
+                    R.fx0 = fls[1];
+                    R.fy1 = fls[2];
+                    R.fy0 = fls[3];
+                    R.cx1 = cls[0];
+                    R.cx0 = cls[1];
+                    R.cy1 = cls[2];
+                    R.cy0 = cls[3];
                 }
                 rect[a] = R;
             }

@@ -76,10 +76,16 @@ struct DmmEnt {
 };
 // An axis-aligned rectangular box of the polygon path: its lines and the
 // box's own indices of its +x, -x, +y, -y borders (kx1 = -1: not such a
-// box, the general border search applies).
+// box, the general border search applies); across each side the
+// neighbour box when one piece covers the whole side (-1: a void side,
+// -2: look the side's pieces up), that box's flags (1: reservoir, 2:
+// periodic) and the side's wall class.
 struct PolyRect {
     double x0, x1, y0, y1;
     int kx1, kx0, ky1, ky0;
+    int nx1, nx0, ny1, ny0;
+    int fx1, fx0, fy1, fy0;
+    int cx1, cx0, cy1, cy0;
 };
 struct PolyArgs {
     const PolyBorder* pb;     // [global border index]

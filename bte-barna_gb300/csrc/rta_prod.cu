@@ -1199,6 +1199,7 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         const bool rectb = R.kx1 >= 0;
         bool xfirst = false;
         double xw = 0., yw = 0.;
+        int side_nb = -2, side_fl = 0, side_cls = 0;  // what lies across the exit side
         if (rectb) {
             const bool upx = ob(mv.ivx) >= 0, upy = ob(mv.ivy) >= 0;
             xw = upx ? R.x1 : R.x0;
@@ -1208,6 +1209,9 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
             by = by > 0 ? by : 0;
             xfirst = bx <= by;
             best = xfirst ? (upx ? R.kx1 : R.kx0) : (upy ? R.ky1 : R.ky0);
+            side_nb = xfirst ? (upx ? R.nx1 : R.nx0) : (upy ? R.ny1 : R.ny0);
+            side_fl = xfirst ? (upx ? R.fx1 : R.fx0) : (upy ? R.fy1 : R.fy0);
+            side_cls = xfirst ? (upx ? R.cx1 : R.cx0) : (upy ? R.cy1 : R.cy0);
             te = obd(xfirst ? bx : by);
         } else if (A.inv_den) {
             // 1 / den from the table of the border's normal class: one
@@ -1285,8 +1289,15 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         dt -= seg;
         if (bin_end) r1 = 0.;
         // what lies across the exit border
-        int target = -1, cls = 0, dmm_t = -1;
-        if (wall) {
+        int target = -1, cls = 0, dmm_t = -1, tflags = 0;
+        if (wall && rectb && side_nb != -2) {
+            // a side that is void or one neighbour: no piece lookup
+            if (xfirst) nx = xw;
+            else ny = yw;
+            target = side_nb;
+            tflags = side_fl;
+            cls = side_cls;
+        } else if (wall) {
             const PolyBorder& L = A.pb[B.border_off + best];
             cls = L.cls;
             // onto the border line
@@ -1313,6 +1324,7 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
                     break;
                 }
             }
+            if (target >= 0) tflags = (T.boxes[target].reservoir ? 1 : 0) | (T.boxes[target].tto >= 0 ? 2 : 0);
         }
         // a contact between crystals (change_material_diffuse,
         // src/RTA_MC2D.cpp:871-964): the interface's table re-emits the
@@ -1357,8 +1369,8 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         rb = r1;
         p.pos = v2(nx, ny);
         const bool cross = wall && target >= 0 && !dmm_back;
-        const bool absorbed = cross && T.boxes[target].reservoir;
-        const bool periodic = cross && !absorbed && T.boxes[target].tto >= 0;
+        const bool absorbed = cross && (tflags & 1);
+        const bool periodic = cross && !absorbed && (tflags & 2);
         const bool move = cross && !absorbed;
         const bool reflect = wall && target < 0;
         const bool last = bin_end && bin == last_bin;
