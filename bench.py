@@ -819,6 +819,8 @@ def time_to_1pct(local, cap):
             "plain_launches": sw["plain"]["launches"], "plain_particles": sw["plain"]["particles"],
             "kappa_batched_vs_plain_max_z": sw["kappa_batched_vs_plain_max_z"],
             "speedup_plain_over_batched": sw["speedup_plain_over_batched"],
+            "plain_adaptive_s": sw["plain_adaptive"]["seconds"],
+            "speedup_plain_adaptive_over_batched": sw["speedup_plain_adaptive_over_batched"],
             "with_table_setup": sw["with_table_setup"], "clocks": sw["clocks"]}
     except Exception as e:  # the summaries must not hide the headline line
         out["sweep"] = {"failed": str(e)}

@@ -781,6 +781,11 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
         }
         if (__all_sync(0xffffffffu, done)) break;
         const bool act = todo > 0;
+        // the warp's output places, claimed before the draws so that the
+        // atomic's round trip overlaps the propagator read
+        const unsigned m1 = __ballot_sync(0xffffffffu, act);
+        unsigned long long wo = 0;
+        if (lane == 0 && m1) wo = atomicAdd(dc + DC_NOUT, (unsigned long long)__popc(m1));
         int nmode = mode, nsign = sign;
         if (act && rta) {
             const double u = g.uniform();
@@ -813,9 +818,6 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
                 }
             }
         }
-        const unsigned m1 = __ballot_sync(0xffffffffu, act);
-        unsigned long long wo = 0;
-        if (lane == 0 && m1) wo = atomicAdd(dc + DC_NOUT, (unsigned long long)__popc(m1));
         wo = __shfl_sync(0xffffffffu, wo, 0);
         if (act) {
             const long long o = (long long)wo + __popc(m1 & ((1u << lane) - 1u));

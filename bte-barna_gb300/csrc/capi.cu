@@ -141,7 +141,7 @@ void ensure_static(bte_ctx* c) {
             std::vector<bte::PolyRect> rect(g.boxes.size());
             for (std::size_t a = 0; a < g.boxes.size(); ++a) {
                 const bte::GBox& bx = g.boxes[a];
-                bte::PolyRect R{0., 0., 0., 0., -1, -1, -1, -1, -2, -2, -2, -2, 0, 0, 0, 0, 0, 0, 0, 0};
+                bte::PolyRect R{0., 0., 0., 0., -1, -1, -1, -1, -2, -2, -2, -2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
                 int k4[4] = {-1, -1, -1, -1};
                 double c4[4] = {0., 0., 0., 0.};
                 bool ok = bx.nborders == 4;
@@ -197,6 +197,22 @@ void ensure_static(bte_ctx* c) {
                     R.cx0 = cls[1];
                     R.cy1 = cls[2];
                     R.cy0 = cls[3];
+                    // a strip spanning the period: the periodic box across
+                    // one side translates by the box's extent onto the
+                    // periodic box across the other side, whose whole side
+                    // this box is (geometry_2d::translate lands there)
+                    auto self_periodic = [&](int hi, int lo, double ext, bool along_x) {
+                        if (hi < 0 || lo < 0 || !(fls[along_x ? 0 : 2] & 2) || !(fls[along_x ? 1 : 3] & 2)) return 0;
+                        const bte::V2 th = g.translation[std::size_t(hi)], tl = g.translation[std::size_t(lo)];
+                        const bool ok = g.tto[std::size_t(hi)] == lo && g.tto[std::size_t(lo)] == hi &&
+                                        (along_x ? (th.x == -ext && th.y == 0. && tl.x == ext && tl.y == 0.)
+                                                 : (th.y == -ext && th.x == 0. && tl.y == ext && tl.x == 0.));
+                        return ok ? 1 : 0;
+                    };
+                    if (R.kx1 >= 0) {
+                        R.perx = self_periodic(R.nx1, R.nx0, R.x1 - R.x0, true);
+                        R.pery = self_periodic(R.ny1, R.ny0, R.y1 - R.y0, false);
+                    }
                 }
                 rect[a] = R;
             }

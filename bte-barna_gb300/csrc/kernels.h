@@ -86,6 +86,10 @@ struct PolyRect {
     int nx1, nx0, ny1, ny0;
     int fx1, fx0, fy1, fy0;
     int cx1, cx0, cy1, cy0;
+    // 1: the box's +x and -x sides lead through periodic boxes that
+    // translate by its width back into the box itself (a strip spanning
+    // the period in x); likewise in y
+    int perx, pery;
 };
 struct PolyArgs {
     const PolyBorder* pb;     // [global border index]

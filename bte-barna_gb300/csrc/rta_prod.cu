@@ -1207,6 +1207,10 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
             long long bx = ob((xw - p.pos.x) * mv.ivx), by = ob((yw - p.pos.y) * mv.ivy);
             bx = bx > 0 ? bx : 0;
             by = by > 0 ? by : 0;
+            // a strip spanning the period never exits through those sides:
+            // its flight wraps (below) instead of translating side by side
+            if (R.perx) bx = ob(HUGE_VAL);
+            if (R.pery) by = ob(HUGE_VAL);
             xfirst = bx <= by;
             best = xfirst ? (upx ? R.kx1 : R.kx0) : (upy ? R.ky1 : R.ky0);
             side_nb = xfirst ? (upx ? R.nx1 : R.nx0) : (upy ? R.ny1 : R.ny0);
@@ -1288,6 +1292,23 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
         double ny = fma(seg, mv.vy, p.pos.y);
         dt -= seg;
         if (bin_end) r1 = 0.;
+        if (rectb && (R.perx | R.pery)) {
+            // the translations the flight made in a strip spanning the
+            // period: back into the box by whole periods, the pending
+            // tally's start shifted alike (its displacement is the flight's)
+            if (R.perx && (nx >= R.x1 || nx < R.x0)) {
+                const double W = R.x1 - R.x0, k = floor((nx - R.x0) / W);
+                nx -= k * W;
+                pd.x0 -= k * W;
+                c.translations += (unsigned long long)fabs(k);
+            }
+            if (R.pery && (ny >= R.y1 || ny < R.y0)) {
+                const double H = R.y1 - R.y0, k = floor((ny - R.y0) / H);
+                ny -= k * H;
+                pd.y0 -= k * H;
+                c.translations += (unsigned long long)fabs(k);
+            }
+        }
         // what lies across the exit border
         int target = -1, cls = 0, dmm_t = -1, tflags = 0;
         if (wall && rectb && side_nb != -2) {
