@@ -76,8 +76,8 @@ def workload(name):
         c["dt"], c["maxtime"], c["N"] = 10.0, 1000.0, 10_000_000
         c["label"] = ("periodic bar, convex-polygon kernel: 32x32 q x 6 branches (6144 modes), "
                       "20nm x 40nm bar of 10 strips between periodic side boxes, 302/300K "
-                      "reservoirs below and above, 100 bins of 10ps, N=1e7")
-        c["per_step"] = 2_000_000
+                      "reservoirs below and above, 100 bins of 10ps, N=1e7, a step is the whole run")
+        c["per_step"] = 10_000_000
     else:
         c = synth.config0()
         c["label"] = ("plain RTA ribbon: 32x32 q x 6 branches (6144 modes), 1um x 100nm, 50 cells, "

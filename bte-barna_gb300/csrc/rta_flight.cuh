@@ -100,8 +100,11 @@ struct DevTables {
     long long group_stride;
 };
 
+// One thread's counts over one launch (32 bits: a thread would need over
+// 4e9 flight events in a launch to wrap one), warp-reduced into the
+// launch's 64-bit counters at its end.
 struct Counters {
-    unsigned long long events, wall_hits, crossings, absorbed, specular, nudges, quirks, tallies,
+    unsigned events, wall_hits, crossings, absorbed, specular, nudges, quirks, tallies,
         translations, scattered, lost, ifc_hits, ifc_trans;
 };
 

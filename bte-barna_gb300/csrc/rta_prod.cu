@@ -1300,13 +1300,13 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
                 const double W = R.x1 - R.x0, k = floor((nx - R.x0) / W);
                 nx -= k * W;
                 pd.x0 -= k * W;
-                c.translations += (unsigned long long)fabs(k);
+                c.translations += (unsigned)fabs(k);
             }
             if (R.pery && (ny >= R.y1 || ny < R.y0)) {
                 const double H = R.y1 - R.y0, k = floor((ny - R.y0) / H);
                 ny -= k * H;
                 pd.y0 -= k * H;
-                c.translations += (unsigned long long)fabs(k);
+                c.translations += (unsigned)fabs(k);
             }
         }
         // what lies across the exit border
