@@ -10,7 +10,8 @@
    oracle/_ref/ref_pins, runs it on a seeded synthetic mode table and
    writes tests/golden/ref_pins.json: the flight-path functions; and on
    two smaller tables, tests/golden/ref_pins_dmm.json: the diffuse
-   mismatch model between materials.
+   mismatch model between materials, with calculate_gradientT on two
+   seeded geometries.
 
 Only this script reads the reference tree, and only where it exists (the
 build container); oracle/_ref/ is not committed, the fixtures it writes are,
@@ -62,6 +63,8 @@ SNIPPETS = [
     ("dos_gaussian.inc", "include/dos.hpp", 28, "class Gaussian_for_DOS {", 28),
     ("sampling_hpp_dmm.inc", "include/sampling.hpp", 324, "class layer_coupling {", 402),
     ("sampling_cpp_dmm.inc", "src/sampling.cpp", 366, "double layer_coupling::get_injection_rate(", 831),
+    ("geometry_calculate_gradientT.inc", "src/geometry_2d.cpp", 524,
+     "Eigen::MatrixXd calculate_gradientT(std::vector<alma::geometry_2d>& sys) {", 524),
 ]
 
 
@@ -155,20 +158,67 @@ def build_pins(reference: str) -> str:
     return exe
 
 
+def gradient_geometries():
+    """The boxes of the calculate_gradientT pins: a 20 x 10 grid with a
+    staircase pore and seeded random Teq (4 to 8 neighbours per cell, corner
+    contacts included), and a ribbon of 6 cells with reservoirs (collinear
+    neighbours).  Returns [(geometry dict, [(centre, contacts)] per box)]."""
+    sys.path.insert(0, os.path.join(REPO, "bte-barna_gb300"))
+    import numpy as np
+    import synth
+    out = []
+    g = synth.grid_geometry(400.0, 200.0, 20, 10, pore_center=(200.0, 100.0), pore_diameter=80.0)
+    g["Teq"] = 300.0 + np.random.default_rng(20261204).normal(0.0, 0.5, g["nboxes"])
+    out.append(g)
+    r = synth.ribbon_geometry(240.0, 50.0, 6)
+    r["Teq"][:6] = [299.6, 299.8, 300.1, 300.2, 300.6, 300.7]
+    out.append(r)
+    res = []
+    for g in out:
+        v = np.asarray(g["vertices"], float).reshape(-1, 4, 2)
+        lo, hi = v.min(axis=1), v.max(axis=1)
+        c = 0.5 * (lo + hi)
+        n = len(v)
+        boxes = []
+        for a in range(n):
+            nb = [b for b in range(n) if b != a
+                  and lo[b, 0] <= hi[a, 0] + 1e-9 and lo[a, 0] <= hi[b, 0] + 1e-9
+                  and lo[b, 1] <= hi[a, 1] + 1e-9 and lo[a, 1] <= hi[b, 1] + 1e-9]
+            boxes.append((c[a], nb))
+        res.append((g, boxes))
+    return res
+
+
+def _write_gradient_file(path: str, g: dict, boxes) -> None:
+    with open(path, "w") as f:
+        f.write(f"{len(boxes)}\n")
+        for i, (c, nb) in enumerate(boxes):
+            f.write(f"{i} {int(g['reservoir'][i])} 0 {float(g['Teq'][i])!r} {float(c[0])!r} {float(c[1])!r} "
+                    f"{len(nb)} " + " ".join(str(b) for b in nb) + "\n")
+
+
 def run_pins(exe: str):
-    """The pins' JSON and the diffuse mismatch pins' JSON (two 4x4 x 6
-    tables of different seeds)."""
+    """The pins' JSON, the diffuse mismatch pins' JSON (two 4x4 x 6 tables of
+    different seeds) and the calculate_gradientT pins' JSON."""
     out_dir = os.path.dirname(exe)
     table = os.path.join(out_dir, "pins_table.txt")
     _write_table(table)
     ta, tb = os.path.join(out_dir, "pins_dmm_a.txt"), os.path.join(out_dir, "pins_dmm_b.txt")
     _write_table(ta, 4, 100)
     _write_table(tb, 4, 101)
-    subprocess.run([exe, table, out_dir, ta, tb], check=True, capture_output=True, text=True)
+    grads = []
+    for k, (g, boxes) in enumerate(gradient_geometries()):
+        gf = os.path.join(out_dir, f"pins_grad_{k}.txt")
+        _write_gradient_file(gf, g, boxes)
+        subprocess.run([exe, table, out_dir, ta, tb, gf], check=True, capture_output=True, text=True)
+        with open(os.path.join(out_dir, "ref_pins_grad.json")) as f:
+            grads.append({"Teq": [float(x) for x in g["Teq"]], **json.load(f)})
     with open(os.path.join(out_dir, "ref_pins.json")) as f:
         pins = json.load(f)
     with open(os.path.join(out_dir, "ref_pins_dmm.json")) as f:
-        return pins, json.load(f)
+        dmm = json.load(f)
+    dmm["gradientT"] = grads
+    return pins, dmm
 
 
 def reference_tree():

@@ -170,6 +170,22 @@ void build_P(Eigen::MatrixXd& A, Eigen::MatrixXd& P, double t, boost::mpi::commu
 #include "collision_arnoldi.inc"
 #include "collision_propagator_H_methods.inc"
 #include "collision_save_load_build_P.inc"
+
+// Stand-in of geometry_2d for calculate_gradientT: the flags, Teq, centre,
+// id and contact map (keyed by neighbour id) it reads.
+struct geom2d_border {};
+class geometry_2d {
+public:
+    double Teq = -1.;
+    bool reservoir = false, periodic = false;
+    Eigen::Vector2d center = Eigen::Vector2d::Zero();
+    std::size_t id = 0;
+    std::map<std::size_t, std::vector<geom2d_border>> contacts;
+    Eigen::Vector2d get_center() const { return center; }
+    std::size_t get_id() { return id; }
+    std::map<std::size_t, std::vector<geom2d_border>>& get_contacts() { return contacts; }
+};
+#include "geometry_calculate_gradientT.inc"
 }  // namespace alma
 
 #include "rta_gamma_pdf.inc"
@@ -623,6 +639,35 @@ int main(int argc, char** argv) {
         << ", \"V\": " << num(tab.V) << ", \"c_lat\": " << num(tab.c) << "}";
     std::ofstream out(scratch + "/ref_pins.json");
     out << "{" << J.o.str() << "\n}\n";
+    if (argc > 5) {  // calculate_gradientT on the boxes of argv[5]
+        std::ifstream in(argv[5]);
+        std::size_t nb = 0;
+        in >> nb;
+        std::vector<alma::geometry_2d> sys(nb);
+        for (std::size_t i = 0; i < nb; ++i) {
+            int res = 0, per = 0;
+            std::size_t nc = 0;
+            in >> sys[i].id >> res >> per >> sys[i].Teq >> sys[i].center(0) >> sys[i].center(1) >> nc;
+            sys[i].reservoir = res != 0;
+            sys[i].periodic = per != 0;
+            for (std::size_t k = 0; k < nc; ++k) {
+                std::size_t c = 0;
+                in >> c;
+                sys[i].contacts[c] = {alma::geom2d_border{}};
+            }
+        }
+        if (!in) {
+            std::fprintf(stderr, "bad gradient geometry file %s\n", argv[5]);
+            return 2;
+        }
+        const Eigen::MatrixXd G = alma::calculate_gradientT(sys);
+        std::ofstream og(scratch + "/ref_pins_grad.json");
+        og << "{\"gradients\": [";
+        for (std::size_t i = 0; i < nb; ++i)
+            og << (i ? ", [" : "[") << num(G(0, Eigen::Index(i))) << ", " << num(G(1, Eigen::Index(i))) << "]";
+        og << "]}\n";
+        if (!og) return 1;
+    }
     if (argc > 3) {  // the diffuse mismatch model between the tables of argv[3] and argv[4]
         const Table ta = read_table(argv[3]), tb = read_table(argv[4]);
         auto ga = make_grid(ta), gb = make_grid(tb);
