@@ -137,11 +137,13 @@ class SteadyResult(C.Structure):
                 ("log", C.POINTER(C.c_double)), ("Eeff", C.c_double), ("energy_rate", C.c_double),
                 ("events", C.c_int64), ("wall_hits", C.c_int64), ("crossings", C.c_int64),
                 ("absorbed", C.c_int64), ("translations", C.c_int64), ("scattered", C.c_int64),
-                ("births", C.c_int64), ("lost", C.c_int64), ("kernel_ms", C.c_double)]
+                ("births", C.c_int64), ("lost", C.c_int64), ("kernel_ms", C.c_double),
+                ("interface_hits", C.c_int64), ("interface_transmissions", C.c_int64)]
 
 
 STEADY_KEYS = ("generations", "converged", "Eeff", "energy_rate", "events", "wall_hits", "crossings",
-               "absorbed", "translations", "scattered", "births", "lost", "kernel_ms")
+               "absorbed", "translations", "scattered", "births", "lost", "kernel_ms", "interface_hits",
+               "interface_transmissions")
 
 
 def steady_call(fn, nboxes, T0, gradient, N, seed=1, mode=MODE_PRODUCTION, eps_energy=-42.0,

@@ -1500,10 +1500,12 @@ bool launch_prod_poly(const DevTables& T, const PolyArgs& A, double* tally, unsi
 // border lines (one box visit per pass, tallied at its end as the reference's
 // periodic process_segment does) until it scatters inside a box (phi +=
 // sign), reaches a void wall (redrawn and carried over), enters a reservoir
-// (absorbed) or a periodic box (translated, the flight goes on).
+// (absorbed) or a periodic box (translated, the flight goes on).  With
+// crystals (PA.dmm_row), a contact between crystals re-emits the particle
+// and carries it over as a void wall does.
 __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A, PolyArgs PA, double* tally,
                                                        unsigned long long* counters, int* err) {
-    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int lane = threadIdx.x & 31;
     ProdPolicy pol;
     pol.g.init(0, 0);
@@ -1537,6 +1539,32 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
                     } else {
                         active = true;
                         nseg = 0;
+                        if (PA.dmm_row) {
+                            // carried over across an interface into a
+                            // reservoir (absorbed) or a periodic box
+                            // (translated), as the next evolparticle call
+                            // does (src/RTA_MC2D.cpp:1449-1467)
+                            const GBox& B0 = T.boxes[p.box];
+                            if (B0.reservoir) {
+                                c.absorbed++;
+                                steady_emit(A, slot, FATE_ABSORBED, p);
+                                active = false;
+                            } else if (B0.tto >= 0) {
+                                V2 rf;
+                                int nb = p.box;
+                                const int e2 = translate<ProdPolicy, true>(T, pol, p.box, p.pos, v, nb, rf);
+                                if (e2) {
+                                    record_error(err, e2, slot);
+                                    A.flag[slot] = 0;
+                                    active = false;
+                                } else {
+                                    p.pos = rf;
+                                    p.box = nb;
+                                    p.mo = mat_off(T, nb);
+                                    c.translations++;
+                                }
+                            }
+                        }
                     }
                 } else {
                     done = true;
@@ -1572,7 +1600,7 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
         double nx = fma(seg, v.x, p.pos.x);
         double ny = fma(seg, v.y, p.pos.y);
         dt -= seg;
-        int target = -1, cls = 0;
+        int target = -1, cls = 0, dmm_t = -1;
         if (wall) {
             const PolyBorder& L = PA.pb[B.border_off + best];
             cls = L.cls;
@@ -1584,6 +1612,7 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
                 const PolyPiece pc = PA.pieces[L.piece_off + j];
                 if (sx >= pc.s0 && sx <= pc.s1) {
                     target = pc.box;
+                    dmm_t = pc.pad;
                     break;
                 }
             }
@@ -1613,6 +1642,38 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
             p.mode = nm;
             c.wall_hits++;
             fate = FATE_BOUNCE;
+        } else if (dmm_t >= 0 && PA.dmm_row) {
+            // a contact between crystals (change_material_diffuse in the
+            // periodic evolparticle, src/RTA_MC2D.cpp:1672-1689, 1751-1779):
+            // the interface's table re-emits the particle on either side
+            // (Diffuse_mismatch_distribution::reemit, src/sampling.cpp:
+            // 831-902) and it joins the next generation; an incident mode
+            // without entries crosses in its mode, as the reference's 'X'
+            const long long* row = PA.dmm_row + (long long)dmm_t * (T.n + 1);
+            const long long e0 = __ldg(row + p.mode), e1 = __ldg(row + p.mode + 1);
+            bool across = true;
+            if (e1 > e0) {
+                const double lo = PA.dmm_ent[e0].cum, hi = PA.dmm_ent[e1 - 1].cum;
+                const double pp = pol.u() * (hi - lo) + lo;
+                long long a = e0, b = e1 - 1;
+                while (a < b) {
+                    const long long mid = (a + b) >> 1;
+                    if (PA.dmm_ent[mid].cum >= pp) b = mid;
+                    else a = mid + 1;
+                }
+                const DmmEnt en = PA.dmm_ent[a];
+                p.mode = en.out;
+                across = en.side != 0;
+            } else {
+                c.quirks++;
+            }
+            c.ifc_hits++;
+            if (across) {
+                c.ifc_trans++;
+                p.box = target;
+                p.mo = mat_off(T, target);
+            }
+            fate = FATE_BOUNCE;
         } else if (T.boxes[target].reservoir) {
             c.absorbed++;
             fate = FATE_ABSORBED;
@@ -1640,7 +1701,7 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
         }
     }
     c.tallies += pol.ntally;
-    flush_counters_p(c, counters);
+    flush_counters_p<13>(c, counters);
 }
 
 bool launch_steady_poly(const DevTables& T, const SteadyArgs& A, const PolyArgs& PA, double* tally,

@@ -136,7 +136,8 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         using namespace bte;
         if (!c->have_modes || !c->have_geom)
             throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
-        if (c->nmat > 0) throw Error(BTE_ERR_INPUT, "materials are for transient batched runs");
+        const bool crystals = c->ncrys > 0;
+        if (c->nmat > 0 && !crystals) throw Error(BTE_ERR_INPUT, "materials are for transient batched runs");
         if (!(p->T0 > 0.) || !std::isfinite(p->T0)) throw Error(BTE_ERR_INPUT, "T0 must be > 0");
         if (p->nparticles < 1 || p->nparticles > 0x7fffffffll)
             throw Error(BTE_ERR_INPUT, "nparticles must be in [1, 2^31)");
@@ -153,6 +154,17 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
                 throw Error(BTE_ERR_INPUT, "Tref in xml is different from provided T0");
         if (!(p->specularity >= 0. && p->specularity <= 1.))
             throw Error(BTE_ERR_INPUT, "specularity must be in [0, 1]");
+        if (crystals) {
+            // crystals joined by mismatch interfaces: the production polygon
+            // kernel, every crystal at T0
+            if (p->mode != BTE_MODE_PRODUCTION) throw Error(BTE_ERR_INPUT, "several crystals need the production mode");
+            if (p->flags & BTE_FLAG_GENERAL) throw Error(BTE_ERR_INPUT, "several crystals run on the polygon kernel");
+            if (!c->spec_boxes.empty()) throw Error(BTE_ERR_INPUT, "spectral outputs need one crystal");
+            if (c->mat_T0.empty() || c->mat_T0[0] != p->T0) {
+                c->mat_T0.assign(std::size_t(c->ncrys), p->T0);
+                c->resample_T0 = -1;
+            }
+        }
         ensure_static(c);
         if (p->specularity > 0. && !c->have_mirror)
             throw Error(BTE_ERR_INPUT, "specular walls need an axis-aligned q grid with mirror images");
@@ -166,8 +178,25 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         cudaStream_t st = c->stream;
 
         // generators (Init_generator with a gradient, src/RTA_MC2D.cpp:289-447)
-        Generators W = build_wall_generators(m, g, false);
-        GradGenerators G = build_gradient_generators(m, g, gx, gy);
+        Generators W;
+        GradGenerators G;
+        if (crystals) {
+            // each crystal's sources over its own boxes, rows over the
+            // concatenated modes (Init_generator takes each box's material)
+            std::vector<Generators> Ws;
+            std::vector<GradGenerators> Gs;
+            const std::vector<V2> grad(g.boxes.size(), v2(gx, gy));
+            for (int k = 0; k < c->ncrys; ++k) {
+                const GenEmbed e{k, c->crys_off[std::size_t(k)], m.n()};
+                Ws.push_back(build_wall_generators(c->crys[std::size_t(k)], g, false, &e));
+                Gs.push_back(build_gradient_generators_boxes(c->crys[std::size_t(k)], g, grad, &e));
+            }
+            W = merge_generators(Ws, true, false);
+            G = merge_gradient_generators(Gs);
+        } else {
+            W = build_wall_generators(m, g, false);
+            G = build_gradient_generators(m, g, gx, gy);
+        }
         double E0 = 0.;
         for (auto& w : W.walls) E0 += w.energy;
         const double E1 = G.total_energy;
@@ -282,7 +311,9 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         A.work = S.work.as<unsigned long long>();
 
         const PolyArgs PA{c->d_pborders.as<PolyBorder>(), c->d_ppieces.as<PolyPiece>(), c->d_mv.as<ModeVel>(),
-                          nullptr, nullptr};
+                          nullptr, nullptr,
+                          crystals ? c->d_dmm_row.as<long long>() : nullptr,
+                          crystals ? c->d_dmm_ent.as<DmmEnt>() : nullptr};
         const int max_gen = p->max_generations > 0 ? p->max_generations : 100000;
         std::vector<double> oldv(size_t(3) * nbx, 0.), cur(size_t(3) * nbx, 0.);
         std::vector<unsigned long long> hex, hphi(static_cast<size_t>(nbx));
@@ -452,11 +483,24 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         out->lost = (int64_t)hc[10];
         out->births = births_total;
         out->kernel_ms = kms;
+        out->interface_hits = (int64_t)hc[11];
+        out->interface_transmissions = (int64_t)hc[12];
         if (out->exact && replay) std::memcpy(out->exact, hex.data(), size_t(nbx) * 6 * sizeof(long long));
-        // post-processing, src/RTA_MC2D.cpp:2698-2731
-        const double vcorr = g.thickness / m.c;
-        const double cv = calc_cv(m, p->T0);
+        // post-processing, src/RTA_MC2D.cpp:2698-2731: C_v and vcorr of each
+        // box's crystal
+        std::vector<double> cvs, vcorrs;
+        if (crystals) {
+            for (int k = 0; k < c->ncrys; ++k) {
+                cvs.push_back(calc_cv(c->crys[std::size_t(k)], p->T0));
+                vcorrs.push_back(g.thickness / c->crys[std::size_t(k)].c);
+            }
+        } else {
+            cvs.push_back(calc_cv(m, p->T0));
+            vcorrs.push_back(g.thickness / m.c);
+        }
         for (int b = 0; b < nbx; ++b) {
+            const std::size_t mk = crystals ? std::size_t(g.mat[std::size_t(b)]) : 0;
+            const double cv = cvs[mk], vcorr = vcorrs[mk];
             const double vbox = g.boxes[size_t(b)].area * g.thickness;
             const double z = cur[size_t(b)], zx = cur[size_t(nbx) + b], zy = cur[size_t(2) * nbx + b];
             if (out->gz) out->gz[b] = z;

@@ -21,6 +21,7 @@
 #include <map>
 #include <numeric>
 #include <thread>
+#include <tuple>
 
 namespace bte {
 
@@ -666,14 +667,15 @@ GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry&
 }
 
 GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeometry& g,
-                                               const std::vector<V2>& grad) {
+                                               const std::vector<V2>& grad, const GenEmbed* e) {
     GradGenerators R;
     const std::size_t n = m.n();
     const double vuc = m.V * g.thickness / m.c;
-    std::vector<double> pmf(n);
+    std::vector<double> pmf(n), row;
     std::vector<signed char> sg(n);
     for (std::size_t s = 0; s < g.boxes.size(); ++s) {
         if (g.reservoir[s] || g.tto[s] >= 0) continue;
+        if (e && g.mat[s] != e->mat) continue;  // another crystal's box
         const double gx = grad[s].x, gy = grad[s].y;
         // a box without a gradient has no source (source_term_gradient,
         // src/beyondRTA_MC2d.cpp:626-628)
@@ -693,12 +695,46 @@ GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeo
         const double vol = g.boxes[s].area * g.thickness / vuc;
         R.box.push_back(int(s));
         R.energy.push_back(vol * cumulsum / double(m.nq));
-        auto cdf = fill_cumulative(pmf);
+        const std::vector<double>& rw = embed_row(pmf, e, row);
+        auto cdf = fill_cumulative(rw);
         R.cdf.insert(R.cdf.end(), cdf.begin(), cdf.end());
-        std::vector<Alias> al(n);
-        alias_table(pmf.data(), int(n), al.data());
+        std::vector<Alias> al(rw.size());
+        alias_table(rw.data(), int(rw.size()), al.data());
         R.alias.insert(R.alias.end(), al.begin(), al.end());
-        R.sign.insert(R.sign.end(), sg.begin(), sg.end());
+        if (e) {  // modes outside the crystal are never drawn
+            std::vector<signed char> srow(e->n, 1);
+            std::copy(sg.begin(), sg.end(), srow.begin() + std::ptrdiff_t(e->off));
+            R.sign.insert(R.sign.end(), srow.begin(), srow.end());
+        } else {
+            R.sign.insert(R.sign.end(), sg.begin(), sg.end());
+        }
+    }
+    const double wnorm = std::accumulate(R.energy.begin(), R.energy.end(), 0.);
+    double cum = 0;
+    for (double w : R.energy) {
+        cum += w / wnorm;
+        R.cum.push_back(cum);
+    }
+    R.total_energy = wnorm;
+    return R;
+}
+
+GradGenerators merge_gradient_generators(const std::vector<GradGenerators>& G) {
+    // (box, crystal, index) in ascending box order
+    std::vector<std::tuple<int, std::size_t, std::size_t>> order;
+    for (std::size_t k = 0; k < G.size(); ++k)
+        for (std::size_t i = 0; i < G[k].box.size(); ++i) order.emplace_back(G[k].box[i], k, i);
+    std::sort(order.begin(), order.end());
+    GradGenerators R;
+    for (auto& [b, k, i] : order) {
+        const GradGenerators& S = G[k];
+        const std::size_t n = S.cdf.size() / S.box.size();
+        R.box.push_back(b);
+        R.energy.push_back(S.energy[i]);
+        R.cdf.insert(R.cdf.end(), S.cdf.begin() + std::ptrdiff_t(i * n), S.cdf.begin() + std::ptrdiff_t((i + 1) * n));
+        R.alias.insert(R.alias.end(), S.alias.begin() + std::ptrdiff_t(i * n),
+                       S.alias.begin() + std::ptrdiff_t((i + 1) * n));
+        R.sign.insert(R.sign.end(), S.sign.begin() + std::ptrdiff_t(i * n), S.sign.begin() + std::ptrdiff_t((i + 1) * n));
     }
     const double wnorm = std::accumulate(R.energy.begin(), R.energy.end(), 0.);
     double cum = 0;

@@ -154,9 +154,13 @@ struct GradGenerators {
 GradGenerators build_gradient_generators(const HostModes& m, const HostGeometry& g, double gx,
                                          double gy);
 // Nabla_T sources with a gradient per box (grad[box], K/nm); boxes without
-// a gradient get no source.
+// a gradient get no source.  With an embedding: only the boxes of crystal
+// e->mat, rows over the concatenated modes (the crystal's at e->off).
 GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeometry& g,
-                                               const std::vector<V2>& grad);
+                                               const std::vector<V2>& grad, const GenEmbed* e = nullptr);
+// Several crystals' gradient sources as one set in ascending box order,
+// the box weights renormalised over all of them.
+GradGenerators merge_gradient_generators(const std::vector<GradGenerators>& G);
 // calculate_gradientT (src/geometry_2d.cpp:524-575): per box that is neither
 // a reservoir nor periodic, the least-squares gradient of Teq from the
 // centres of its neighbours of that kind, the minimum-norm one when they are

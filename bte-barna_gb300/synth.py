@@ -154,6 +154,47 @@ def periodic_bar_geometry(width: float = 20.0, length: float = 40.0, nstrips: in
     return g
 
 
+def layered_bar_geometry(width: float = 20.0, length: float = 40.0, nstrips: int = 10, split: int = 5,
+                         T_hot: float = 302.0, T_cold: float = 300.0, T0: float = 300.0,
+                         thickness: float = C_LAT, side: float = 1.5, cap: float = 2.0) -> dict:
+    """The periodic bar of periodic_bar_geometry made of two crystals: strips
+    0..split-1 and the hot reservoir below in crystal 0, the other strips and
+    the cold reservoir above in crystal 1 (geom["material"]).  Each crystal
+    has its own pair of periodic side boxes (right -> left by -width and
+    back), so a flight leaving one side re-enters its own crystal."""
+    boxes, Teq, res, mat = [], [], [], []
+    dy = length / nstrips
+    ys = split * dy
+    for j in range(nstrips):
+        boxes.append(_rect(0.0, j * dy, width, (j + 1) * dy))
+        Teq.append(T0)
+        res.append(0)
+        mat.append(0 if j < split else 1)
+    base = len(boxes)
+    for k, (y0, y1) in enumerate(((0.0, ys), (ys, length))):
+        boxes.append(_rect(width, y0, width + side, y1))   # right of crystal k
+        boxes.append(_rect(-side, y0, 0.0, y1))            # left of crystal k
+        Teq += [T0, T0]
+        res += [0, 0]
+        mat += [k, k]
+    boxes.append(_rect(-side, -cap, width + side, 0.0))
+    boxes.append(_rect(-side, length, width + side, length + cap))
+    Teq += [T_hot, T_cold]
+    res += [1, 1]
+    mat += [0, 1]
+    g = _pack(boxes, Teq, list(Teq), res, thickness)
+    tto = np.full(len(boxes), -1, dtype=np.int32)
+    tr = np.zeros((len(boxes), 2))
+    for k in range(2):
+        right, left = base + 2 * k, base + 2 * k + 1
+        tto[right], tr[right] = left, (-width, 0.0)
+        tto[left], tr[left] = right, (width, 0.0)
+    g["translate_to"] = tto
+    g["translation"] = tr
+    g["material"] = np.array(mat, dtype=np.int32)
+    return g
+
+
 def periodic_cell_geometry(lx: float = 40.0, ly: float = 40.0, nx: int = 2, ny: int = 2,
                            T0: float = 300.0, thickness: float = C_LAT, side: float = 1.0) -> dict:
     """An nx x ny block of cells closed on all four sides by periodic boxes

@@ -282,6 +282,9 @@ typedef struct bte_steady_result {
     int64_t births;          /* particles created from phi                      */
     int64_t lost;            /* flights dropped at a crossing with no time left */
     double kernel_ms;        /* device time of the generation kernels           */
+    int64_t interface_hits;  /* contacts met between crystals (re-emitted and
+                                carried over, as void-wall reflections)        */
+    int64_t interface_transmissions; /* of which re-emitted across          */
 } bte_steady_result;
 
 /* Tuning knobs of the production kernels (project-written autotuner picks

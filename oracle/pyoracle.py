@@ -70,6 +70,9 @@ def load():
     lib.oracle_steady_run.argtypes = [C.POINTER(_bt.ModeTable), C.POINTER(_bt.Geometry),
                                       C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult)]
     lib.oracle_steady_run.restype = C.c_int
+    lib.oracle_steady_run_multi.argtypes = [C.POINTER(_bt.ModeTable), C.c_int, C.POINTER(_bt.Geometry),
+                                            C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult)]
+    lib.oracle_steady_run_multi.restype = C.c_int
     lib.oracle_pcg64.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
     lib.oracle_log.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_longlong, C.c_int]
@@ -172,6 +175,28 @@ def steady_run(case: dict, gradient, N=None, seed=1, nthreads=8, eps_energy=-42.
     return _bt.steady_call(call, int(case["geom"]["nboxes"]), case["T0"], gradient, N, seed,
                            _bt.MODE_REPLAY, eps_energy, eps_flux, max_generations,
                            specularity=specularity)
+
+
+def steady_run_multi(tables, geom, T0, gradient, N, seed=1, nthreads=8, eps_energy=-42.0, eps_flux=-42.0,
+                     max_generations=0, specularity=0.0):
+    """Steady state of a geometry of several crystals with their own mode
+    tables (box b in crystal geom["material"][b]), diffuse mismatch at their
+    contacts."""
+    lib = load()
+    keep = []
+    arr = (_bt.ModeTable * len(tables))()
+    for i, t in enumerate(tables):
+        ms, k = _bt.mode_struct(t)
+        arr[i] = ms
+        keep.append(k)
+    gs, k2 = _bt.geom_struct(geom)
+
+    def call(p, r):
+        st = lib.oracle_steady_run_multi(arr, len(tables), C.byref(gs), C.byref(p), int(nthreads), C.byref(r))
+        if st != 0:
+            raise _bt.BteError(st, lib.oracle_last_error().decode())
+    return _bt.steady_call(call, int(geom["nboxes"]), T0, gradient, N, seed, _bt.MODE_REPLAY, eps_energy,
+                           eps_flux, max_generations, specularity=specularity)
 
 
 def set_spectral(boxes):

@@ -1487,17 +1487,18 @@ struct MultiSim {
     std::vector<long long> init_first;
 };
 
-// The interface tables of every contact between boxes of different
-// materials that are neither reservoirs nor periodic, each built at the
-// Teq of the first box (in box order) that meets it; the reference builds
-// each on first use, at the Teq of the box the first particle comes from.
+// The interface tables of every contact from a box that is neither a
+// reservoir nor periodic to a box of another material (a reservoir or a
+// periodic box included), each built at the Teq of the first box (in box
+// order) that meets it; the reference builds each on first use, at the Teq
+// of the box the first particle comes from.
 inline void build_interfaces(MultiSim& M, double scalebroad = 0.1) {
     const Sim& S0 = M.mats[0];
     for (auto& a : S0.sys) {
         if (a.reservoir || a.periodic) continue;
         for (auto& [c, bv] : a.contacts) {
             const Box& b = S0.sys[c];
-            if (b.mat == a.mat || b.reservoir || b.periodic) continue;
+            if (b.mat == a.mat) continue;
             V2 nw = {0., 0.};
             nw.x += bv[0].np.x;
             nw.y += bv[0].np.y;
@@ -1628,6 +1629,7 @@ inline uint64_t steady_stream(uint64_t gen, uint64_t slot) { return (gen << 40) 
 // Nabla_T_distribution, src/sampling.cpp:118-187, per interior box.
 struct GradGen {
     std::size_t box;
+    int mat = 0;      // the material whose modes cdf runs over
     std::vector<double> cdf;
     std::vector<int> sign;
     double energy;    // get_energy(vol) = vol cumulsum / nq
@@ -1635,14 +1637,16 @@ struct GradGen {
     double cumulsum;
 };
 
-inline std::vector<GradGen> build_gradient(const Sim& S, double gx, double gy) {
+inline std::vector<GradGen> build_gradient(const Sim& S, double gx, double gy, int only_mat = -1) {
     const Modes& m = S.m;
     const double vuc = m.V * S.thickness / m.c;
     std::vector<GradGen> out;
     for (auto& s : S.sys) {
         if (s.reservoir || s.periodic) continue;
+        if (only_mat >= 0 && s.mat != only_mat) continue;  // another material's box
         GradGen G;
         G.box = s.id;
+        G.mat = only_mat >= 0 ? only_mat : 0;
         std::vector<double> pmf;
         double cumulsum = nabla_t_pmf(m, gx, gy, s.Teq, pmf, G.sign);
         double vol = s.area * S.thickness / vuc;
@@ -1756,7 +1760,11 @@ inline std::vector<V2> calculate_gradientT(const Sim& S) {
     return out;
 }
 
+// The sources of generation 0: wall generators (material, index into that
+// material's gens) with their cumulative weights, and gradient generators.
 struct SteadyGen {
+    std::vector<std::pair<int, std::size_t>> wall;
+    std::vector<double> wall_cum;
     std::vector<GradGen> grad;
     std::vector<double> grad_cum;
     double exg0 = 0, exg1 = 0;
@@ -1791,9 +1799,13 @@ inline void process_segment_steady(Tally& T, std::size_t ibox, int sign, double 
 
 enum Fate { F_LOST = 0, F_SCATTER = 1, F_BOUNCE = 2, F_ABSORBED = 3 };
 
-// evolparticle (periodic), src/RTA_MC2D.cpp:1406-1799, one material.
+// evolparticle (periodic), src/RTA_MC2D.cpp:1406-1799, in the material of
+// the particle's box (S); with `dmm`, a crossing into a box of another
+// material is change_material_diffuse (:1672-1689, :1751-1779): re-emitted
+// at the interface and carried into the next generation, as a void-wall
+// reflection is.
 inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg64& rng, Tally& T,
-                                Fate& fate, double specularity = 0.) {
+                                Fate& fate, double specularity = 0., const DmmSet* dmm = nullptr) {
     const std::size_t nb = S.m.nb;
     V2 opos = p.pos;
     const Box& box = S.sys[p.box];
@@ -1906,6 +1918,11 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
         p.pos = rnew;
         p.t += tf;
         process_segment_steady(T, p.box, p.sign, tf, v, p.q * nb + p.alpha);
+        if (dmm && S.sys[pboxes[0]].mat != S.sys[p.box].mat) {
+            dmm_cross(S, *dmm, p, pboxes[0], dt, rng, T);
+            fate = F_BOUNCE;
+            return;
+        }
         p.box = pboxes[0];
         T.crossings++;
         return;
@@ -1925,15 +1942,20 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
         } else {
             newid = pbox2[std::size_t(uniform_int(rng, 0, int(pbox2.size()) - 1))];
         }
+        if (dmm && S.sys[newid].mat != S.sys[p.box].mat) {
+            dmm_cross(S, *dmm, p, newid, dt, rng, T);
+            fate = F_BOUNCE;
+            return;
+        }
         p.box = newid;
         T.crossings++;
         return;
     }
 }
 
-inline int steady_gen_type(const Sim& S, const SteadyGen& SG, double u) {
+inline int steady_gen_type(const SteadyGen& SG, double u) {
     int id = u <= SG.exg0 ? 0 : 1;  // lower_bound over ExGen
-    if (id == 0 && S.gens.empty()) id = 1;
+    if (id == 0 && SG.wall.empty()) id = 1;
     if (id == 1 && SG.grad.empty()) id = 0;
     return id;
 }
@@ -1957,14 +1979,18 @@ inline V2 random_point(const Box& B, Pcg64& rng) {
 
 // Generation-0 particle of slot s (Init_generator with a gradient); `rank`
 // counts the gradient-generated slots before s (gsign alternates from -).
-inline Particle steady_generate0(const Sim& S, const SteadyGen& SG, uint64_t rank, Pcg64& rng) {
+// mats: one Sim per material; a generator's mode indexes its material's
+// table.
+inline Particle steady_generate0(const std::vector<Sim>& mats, const SteadyGen& SG, uint64_t rank, Pcg64& rng) {
     double selectGenR = canonical(rng);
-    if (steady_gen_type(S, SG, selectGenR) == 0) {
+    if (steady_gen_type(SG, selectGenR) == 0) {
         // case 0 of Init_generator after the generator-type draw
         double whereGenR = canonical(rng);
-        auto it = std::lower_bound(S.gen_cum.begin(), S.gen_cum.end(), whereGenR);
-        if (it == S.gen_cum.end()) --it;
-        const WallGen& G = S.gens[std::size_t(it - S.gen_cum.begin())];
+        auto it = std::lower_bound(SG.wall_cum.begin(), SG.wall_cum.end(), whereGenR);
+        if (it == SG.wall_cum.end()) --it;
+        const auto& ref = SG.wall[std::size_t(it - SG.wall_cum.begin())];
+        const Sim& S = mats[std::size_t(ref.first)];
+        const WallGen& G = S.gens[ref.second];
         V2 ppos;
         for (int tries = 0;; ++tries) {
             if (tries > 1000) throw limit_error("border point rejection loop");
@@ -1990,6 +2016,7 @@ inline Particle steady_generate0(const Sim& S, const SteadyGen& SG, uint64_t ran
     auto it = std::lower_bound(SG.grad_cum.begin(), SG.grad_cum.end(), whereGenR);
     if (it == SG.grad_cum.end()) --it;
     const GradGen& G = SG.grad[std::size_t(it - SG.grad_cum.begin())];
+    const Sim& S = mats[std::size_t(G.mat)];
     V2 ppos = random_point(S.sys[G.box], rng);
     const int want = (rank & 1u) ? 1 : -1;
     std::size_t pos = 0;
@@ -3252,24 +3279,54 @@ int oracle_kat_dmm(const bte_mode_table* A, const bte_mode_table* B, double nx, 
     }
 }
 
-// One steady-state run of a periodic structure under a gradient (the
-// restatement above) on `nthreads` host threads; fills `out` as
-// bte_steady_run does.  Tallies are exact 128-bit sums, turned into doubles
-// for the convergence test and the outputs.
-int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_steady_params* sp,
-                      int nthreads, bte_steady_result* out) {
+namespace {
+// The steady run over one Sim per material (mats[0] alone: the single
+// table, every box in it; several: box b in material sys[b].mat, the
+// interfaces in dmm).
+int steady_core(std::vector<orc::Sim>& mats, const orc::DmmSet* dmm, const bte_steady_params* sp, int nthreads,
+                bte_steady_result* out) {
     try {
-        orc::Sim S = build_sim(mt, gm);
+        const bool multi = mats.size() > 1;
+        const orc::Sim& S = mats[0];  // the boxes (shared by every material's Sim)
+        auto mat_of = [&](std::size_t b) -> std::size_t { return multi ? std::size_t(S.sys[b].mat) : 0; };
         const double gx = sp->gradient[0], gy = sp->gradient[1];
         if (orc::almost_equal(std::sqrt(gx * gx + gy * gy), 0.))
             return fail(BTE_ERR_INPUT, "the steady state needs a non-zero temperature gradient");
-        const std::size_t n = S.m.n(), nbx = S.sys.size(), nb = std::size_t(S.m.nb);
-        S.resample_cdf = orc::fill_cumulative(orc::be_derivative_pmf(S.m, S.m.w, sp->T0));
-        orc::build_lambert(S);
-        orc::build_generators(S, sp->T0, false);
-        const double E0 = S.gens.empty() ? 0. : S.energy;
+        const std::size_t nbx = S.sys.size();
         orc::SteadyGen SG;
-        SG.grad = orc::build_gradient(S, gx, gy);
+        double E0 = 0.;
+        for (std::size_t k = 0; k < mats.size(); ++k) {
+            orc::Sim& Sk = mats[k];
+            Sk.resample_cdf = orc::fill_cumulative(orc::be_derivative_pmf(Sk.m, Sk.m.w, sp->T0));
+            orc::build_lambert(Sk);
+            orc::build_generators(Sk, sp->T0, false, multi ? int(k) : -1);
+            if (!multi) {
+                E0 = Sk.gens.empty() ? 0. : Sk.energy;
+                for (std::size_t i = 0; i < Sk.gens.size(); ++i) SG.wall.push_back({0, i});
+                SG.wall_cum = Sk.gen_cum;
+            } else {
+                for (std::size_t i = 0; i < Sk.gens.size(); ++i) SG.wall.push_back({int(k), i});
+            }
+            std::vector<orc::GradGen> gk = orc::build_gradient(Sk, gx, gy, multi ? int(k) : -1);
+            for (auto& G : gk) SG.grad.push_back(std::move(G));
+        }
+        if (multi) {
+            // wall weights |flux| L thickness over every material's
+            // generators; gradient sources in ascending box order
+            std::vector<double> e;
+            for (auto& r : SG.wall) {
+                const orc::WallGen& G = mats[std::size_t(r.first)].gens[r.second];
+                e.push_back(std::fabs(G.flux) * orc::norm(G.b.p2 - G.b.p1) * S.thickness);
+            }
+            for (double x : e) E0 += x;
+            double c = 0.;
+            for (double x : e) {
+                c += x / E0;
+                SG.wall_cum.push_back(c);
+            }
+            std::stable_sort(SG.grad.begin(), SG.grad.end(),
+                             [](const orc::GradGen& a, const orc::GradGen& b) { return a.box < b.box; });
+        }
         std::vector<double> ge;
         for (auto& G : SG.grad) ge.push_back(G.energy);
         const double E1 = std::accumulate(ge.begin(), ge.end(), 0.);
@@ -3300,7 +3357,7 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
         std::vector<int> bsign;
         std::vector<int64_t> bfirst;
         int64_t nbirth = 0, births_total = 0;
-        int64_t ev = 0, wh = 0, cr = 0, ab = 0, tr = 0, sc = 0, lost = 0;
+        int64_t ev = 0, wh = 0, cr = 0, ab = 0, tr = 0, sc = 0, lost = 0, ih = 0, it_ = 0;
         int gen = 0, converged = 0;
         for (;;) {
             const int64_t nin = gen == 0 ? 0 : int64_t(carry.size());
@@ -3312,7 +3369,7 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
                 for (int64_t sl = 0; sl < nslots; ++sl) {
                     orc::Pcg64 r(sp->seed, orc::steady_stream(0, uint64_t(sl)));
                     rank[std::size_t(sl)] = c;
-                    if (orc::steady_gen_type(S, SG, orc::canonical(r)) == 1) c++;
+                    if (orc::steady_gen_type(SG, orc::canonical(r)) == 1) c++;
                 }
             }
             std::vector<orc::Particle> outp(static_cast<std::size_t>(nslots));
@@ -3326,7 +3383,7 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
                 T.init(nbx, 1);
                 if (nspec > 0) {
                     T.loc = &locs;
-                    T.nmodes = S.m.n();
+                    T.nmodes = S.m.n();  // one material
                     T.spec.assign(nspec, 0);
                     T.scnt.assign(nspec, 0);
                 }
@@ -3338,24 +3395,28 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
                         orc::Pcg64 rng(sp->seed, orc::steady_stream(uint64_t(gen), uint64_t(sl)));
                         orc::Particle p;
                         if (gen == 0) {
-                            p = orc::steady_generate0(S, SG, rank[std::size_t(sl)], rng);
+                            p = orc::steady_generate0(mats, SG, rank[std::size_t(sl)], rng);
                         } else if (sl < nin) {
                             p = carry[std::size_t(sl)];
                         } else {
                             const int64_t k = sl - nin;
                             auto it = std::upper_bound(bfirst.begin(), bfirst.end(), k);
                             const std::size_t j = std::size_t(it - bfirst.begin()) - 1;
+                            const orc::Sim& Sb = mats[mat_of(bbox[j])];
                             p.pos = orc::random_point(S.sys[bbox[j]], rng);
-                            const std::size_t pos = orc::lower_bound_idx(S.resample_cdf, orc::canonical(rng));
-                            p.q = pos / nb;
-                            p.alpha = pos % nb;
+                            const std::size_t pos = orc::lower_bound_idx(Sb.resample_cdf, orc::canonical(rng));
+                            p.q = pos / std::size_t(Sb.m.nb);
+                            p.alpha = pos % std::size_t(Sb.m.nb);
                             p.sign = bsign[j];
                             p.box = bbox[j];
                         }
                         p.t = 0.;
-                        const std::size_t k = p.q * nb + p.alpha;
-                        const orc::V2 v = orc::get_v(S.m, k);
-                        const double w = S.m.w[k];
+                        // the flight in the material of the particle's box
+                        // (material_w0[mat], :2580-2595)
+                        const orc::Sim& Sp = mats[mat_of(p.box)];
+                        const std::size_t k = p.q * std::size_t(Sp.m.nb) + p.alpha;
+                        const orc::V2 v = orc::get_v(Sp.m, k);
+                        const double w = Sp.m.w[k];
                         if (w == 0.) throw orc::value_error("invalid scattering rate");
                         double dt = -orc::bte_log(orc::canonical(rng)) / w;
                         T.events++;
@@ -3363,7 +3424,7 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
                         int guard = 0;
                         while (!orc::almost_equal(dt, 0.)) {
                             if (++guard > 1000000) throw orc::limit_error("flight step cap");
-                            orc::evolparticle_steady(S, p, v, dt, rng, T, f, sp->specularity);
+                            orc::evolparticle_steady(Sp, p, v, dt, rng, T, f, sp->specularity, dmm);
                         }
                         fate[std::size_t(sl)] = char(f);
                         if (f == orc::F_SCATTER) phi[p.box] += p.sign;
@@ -3401,6 +3462,8 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
                 cr += T.crossings;
                 ab += T.absorbed;
                 tr += T.translations;
+                ih += T.interface_hits;
+                it_ += T.interface_transmissions;
             }
             for (auto& ph : phis)
                 for (std::size_t b = 0; b < nbx; ++b) phi[b] += ph[b];
@@ -3474,11 +3537,17 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
                 out->exact[2 * k] = int64_t(uint64_t(u >> 64));
                 out->exact[2 * k + 1] = int64_t(uint64_t(u));
             }
-        // post-processing, src/RTA_MC2D.cpp:2698-2731
-        double cv = 0.;
-        for (std::size_t k = 0; k < n; ++k) cv += orc::bose_einstein_kernel(S.m.omega[k], sp->T0);
-        cv *= orc::kB / double(S.m.nq) / S.m.V;
-        const double vcorr = S.thickness / S.m.c;
+        out->interface_hits = ih;
+        out->interface_transmissions = it_;
+        // post-processing, src/RTA_MC2D.cpp:2698-2731: C_v and vcorr of
+        // each box's material
+        std::vector<double> cvs, vcorrs;
+        for (auto& Sk : mats) {
+            double cv = 0.;
+            for (std::size_t k = 0; k < Sk.m.n(); ++k) cv += orc::bose_einstein_kernel(Sk.m.omega[k], sp->T0);
+            cvs.push_back(cv * orc::kB / double(Sk.m.nq) / Sk.m.V);
+            vcorrs.push_back(S.thickness / Sk.m.c);
+        }
         for (std::size_t b = 0; b < nbx; ++b) {
             const double vbox = S.sys[b].area * S.thickness;
             const double z = cur[b], zx = cur[nbx + b], zy = cur[2 * nbx + b];
@@ -3486,7 +3555,8 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
             if (out->gz_jx) out->gz_jx[b] = zx;
             if (out->gz_jy) out->gz_jy[b] = zy;
             const double ed = z / vbox * Eeff;
-            if (out->temperature) out->temperature[b] = ed / (cv / vcorr) + sp->T0;
+            const std::size_t mk = mat_of(b);
+            if (out->temperature) out->temperature[b] = ed / (cvs[mk] / vcorrs[mk]) + sp->T0;
             if (out->jx) out->jx[b] = zx / vbox * (Eeff * 1e12 * 1e9 * 1e9);
             if (out->jy) out->jy[b] = zy / vbox * (Eeff * 1e12 * 1e9 * 1e9);
         }
@@ -3497,6 +3567,47 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
         return fail(BTE_ERR_VALUE, e.what());
     } catch (const orc::limit_error& e) {
         return fail(BTE_ERR_LIMIT, e.what());
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+}  // namespace
+
+// One steady-state run of a periodic structure under a gradient (the
+// restatement above) on `nthreads` host threads; fills `out` as
+// bte_steady_run does.  Tallies are exact 128-bit sums, turned into doubles
+// for the convergence test and the outputs.
+int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bte_steady_params* sp,
+                      int nthreads, bte_steady_result* out) {
+    try {
+        std::vector<orc::Sim> mats;
+        mats.push_back(build_sim(mt, gm));
+        return steady_core(mats, nullptr, sp, nthreads, out);
+    } catch (const std::exception& e) {
+        return fail(BTE_ERR_GEOMETRY, e.what());
+    }
+}
+
+// The steady state of a geometry of nmat crystals with their own mode
+// tables mts[m] (box b in gm->material[b]), diffuse mismatch at the contacts
+// between them (change_material_diffuse in the periodic evolparticle,
+// src/RTA_MC2D.cpp:1672-1689, 1751-1779: the re-emitted particle is carried
+// into the next generation).
+int oracle_steady_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry* gm,
+                            const bte_steady_params* sp, int nthreads, bte_steady_result* out) {
+    try {
+        if (nmat < 1 || !gm->material) return fail(BTE_ERR_INPUT, "materials need mode tables and box materials");
+        if (!g_spec_boxes.empty()) return fail(BTE_ERR_INPUT, "spectral outputs need one crystal");
+        orc::MultiSim M;
+        for (int k = 0; k < nmat; ++k) M.mats.push_back(build_sim(&mts[k], gm));
+        for (auto& b : M.mats[0].sys)
+            if (b.mat < 0 || b.mat >= nmat) return fail(BTE_ERR_INPUT, "box material out of range");
+        orc::build_interfaces(M);
+        if (nmat == 1) {
+            // one crystal: box materials are all 0, the single-table run
+            return steady_core(M.mats, nullptr, sp, nthreads, out);
+        }
+        return steady_core(M.mats, &M.dmm, sp, nthreads, out);
     } catch (const std::exception& e) {
         return fail(BTE_ERR_GEOMETRY, e.what());
     }

@@ -90,3 +90,47 @@ def test_reservoir_injects_into_its_own_crystal_only():
     g["material"][10] = 1  # the hot reservoir (touching cell 0 of crystal 0) in crystal 1
     with pytest.raises(btegpu.BteError, match="Injection from material A to B"):
         pyoracle.rta_run_multi([A, B], g, 300.0, 10.0, 100.0, 1000, seed=1, nthreads=2)
+
+
+# ---------------------------------------------------------------- steady state
+# The periodic evolparticle meets a contact between crystals with
+# change_material_diffuse and pushes the re-emitted particle into the next
+# generation (src/RTA_MC2D.cpp:1672-1689, 1751-1779).
+
+
+def test_steady_one_crystal_repeats_the_single_table_run():
+    A, _ = _tables()
+    g = synth.periodic_bar_geometry()
+    g["material"] = np.zeros(g["nboxes"], dtype=np.int32)
+    a = pyoracle.steady_run({"modes": A, "geom": g, "T0": 300.0, "N": 3000}, (0.0, -0.01), seed=2)
+    b = pyoracle.steady_run_multi([A], g, 300.0, (0.0, -0.01), 3000, seed=2)
+    assert np.array_equal(a["exact"], b["exact"]) and np.array_equal(a["log"], b["log"])
+    assert a["events"] == b["events"] and b["interface_hits"] == 0
+
+
+def test_steady_two_crystals_bookkeeping_and_threads():
+    """Every flight ends one way (an interface re-emission carries the
+    particle over like a wall reflection); the run does not depend on the
+    thread count."""
+    A, B = _tables()
+    g = synth.layered_bar_geometry()
+    a = pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), 3000, seed=3, nthreads=1)
+    b = pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), 3000, seed=3, nthreads=8)
+    assert np.array_equal(a["exact"], b["exact"]) and a["generations"] == b["generations"]
+    assert 0 < a["interface_transmissions"] < a["interface_hits"]
+    assert a["events"] == a["scattered"] + a["absorbed"] + a["lost"] + a["wall_hits"] + a["interface_hits"]
+    assert a["events"] == 3000 + a["births"] + a["interface_hits"]
+
+
+def test_steady_two_crystals_step_at_the_interface_and_flux_continuity():
+    """The interface resists: the temperature steps between strips 4 and 5
+    while the flux along the bar stays the same on both sides."""
+    A, B = _tables()
+    g = synth.layered_bar_geometry()
+    R = [pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), 4000, seed=10 + i, nthreads=8)
+         for i in range(4)]
+    T = np.mean([r["temperature"][:10] for r in R], axis=0)
+    assert T[4] - T[5] > 3.0 * max(abs(T[3] - T[4]), abs(T[5] - T[6]))
+    jy = np.array([[r["jy"][:5].mean(), r["jy"][5:10].mean()] for r in R])
+    d = jy[:, 0] - jy[:, 1]
+    assert abs(d.mean()) < 4.5 * d.std(ddof=1) / np.sqrt(len(d)) + 1e-3 * abs(jy.mean())

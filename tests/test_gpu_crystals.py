@@ -1,8 +1,9 @@
 """GPU parity of several crystals joined by diffuse mismatch interfaces
 (bte_load_mode_tables; change_material_diffuse, src/RTA_MC2D.cpp:871-964,
 Diffuse_mismatch_distribution::reemit, src/sampling.cpp:831-902): the
-polygon kernel's re-emissions against the restatement, particle time
-conserved across interfaces, and the modes this path does not take."""
+polygon kernel's re-emissions against the restatement in transient runs and
+in the periodic steady state, particle time conserved across interfaces,
+and the modes this path does not take."""
 import os
 import subprocess
 
@@ -84,6 +85,38 @@ def test_crystals_take_the_production_polygon_path_only(engine):
         engine.rta_run(300.0, 10.0, 100.0, 1000, flags=btegpu.FLAG_GENERAL)
     with pytest.raises(btegpu.BteError, match="rate sets"):
         engine.load_materials([A["w"]], [300.0])
+
+
+def test_two_crystal_steady_state_agrees_with_restatement(engine):
+    """Steady state of the layered periodic bar (strips 0-4 in crystal 0,
+    5-9 in crystal 1): the polygon kernel's interface re-emissions, carried
+    into the next generation, against the restatement."""
+    A, B = _tables()
+    g = synth.layered_bar_geometry()
+    engine.load_mode_tables([A, B])
+    engine.load_geometry(g)
+    N, R = 4000, 12
+    # per crystal (the strips of one crystal move together), plus the
+    # interface's own counts
+    names = ["T_crystal0", "T_crystal1", "jy_crystal0", "jy_crystal1", "transmitted", "hits_per_N"]
+
+    def obs(r):
+        T = r["temperature"][:10] - 300.0
+        return np.array([T[:5].mean(), T[5:].mean(), r["jy"][:5].mean() * 1e-8, r["jy"][5:10].mean() * 1e-8,
+                         r["interface_transmissions"] / max(r["interface_hits"], 1), r["interface_hits"] / N])
+    gpu = []
+    for i in range(R):
+        r = engine.steady_run(300.0, (0.0, -0.01), N, seed=300 + i)
+        assert r["interface_hits"] > 0
+        assert r["events"] == N + r["births"] + r["interface_hits"]
+        gpu.append(obs(r))
+    cpu = [obs(pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), N, seed=400 + i, nthreads=16))
+           for i in range(R)]
+    check(np.array(gpu), np.array(cpu), names, "two-crystal steady state")
+    with pytest.raises(btegpu.BteError, match="production"):
+        engine.steady_run(300.0, (0.0, -0.01), N, seed=1, mode=btegpu.MODE_REPLAY)
+    with pytest.raises(btegpu.BteError, match="polygon"):
+        engine.steady_run(300.0, (0.0, -0.01), N, seed=1, flags=btegpu.FLAG_GENERAL)
 
 
 def test_rtamc2d_cli_reads_several_materials(built, tmp_path):
