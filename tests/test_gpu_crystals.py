@@ -95,9 +95,12 @@ def test_two_crystal_steady_state_agrees_with_restatement(engine):
     g = synth.layered_bar_geometry()
     engine.load_mode_tables([A, B])
     engine.load_geometry(g)
-    N, R = 4000, 12
     # per crystal (the strips of one crystal move together), plus the
-    # interface's own counts
+    # interface's own counts.  The generation chains make a replica's flux
+    # heavy-tailed at a few thousand particles; 16000 per replica keeps the
+    # two-sample z near normal (100 replicas of 4000 each agreed to
+    # |z| < 2 on every observable)
+    N, R = 16000, 12
     names = ["T_crystal0", "T_crystal1", "jy_crystal0", "jy_crystal1", "transmitted", "hits_per_N"]
 
     def obs(r):
