@@ -650,7 +650,9 @@ __device__ __forceinline__ void cancel_body(PArr P, long long n, const int* H, i
         const unsigned mask = ((unsigned)c * 0x9E3779B1u + mkey) >> 27;
         const long long i = (long long)(c << 5) + (long long)((unsigned)lane ^ mask);
         if (i >= n) continue;
-        const long long key = (long long)P.box[i] * nmodes + P.mode[i];
+        const int mi = P.mode[i];
+        if (mi < 0) continue;  // a hole
+        const long long key = (long long)P.box[i] * nmodes + mi;
         const int h = H[key];
         const int s = P.sign[i];
         bool keep = !reservoir[P.box[i]] && h != 0 && ((s < 0) == (h < 0));
@@ -687,7 +689,10 @@ __global__ void be_props(const int* H, int nmodes, const double* vx, const doubl
 // Counters of the step loop, kept on the device between kernels.
 // DC_IN and DC_OUTT sum the particles read and written by be_advance over
 // the run (the algorithmic traffic of its roofline).
-enum { DC_NP = 0, DC_NOUT, DC_WORK, DC_FLIPS, DC_PSTEPS, DC_NGEN, DC_IN, DC_OUTT, DC_COUNT = 8 };
+// DC_NP: the places of the population (holes included, see be_advance);
+// DC_LIVE: its particles; DC_WRIT: the particles be_advance wrote in the
+// step.
+enum { DC_NP = 0, DC_NOUT, DC_WORK, DC_FLIPS, DC_PSTEPS, DC_NGEN, DC_IN, DC_OUTT, DC_WRIT, DC_LIVE, DC_COUNT = 10 };
 
 // A source planned on the device: where its particles start in the
 // particle arrays and how many there are.
@@ -715,46 +720,63 @@ constexpr unsigned BRANCH_CAP = 1u << 20;
 // 1 - exp(-w dt)) or the propagator with sign branching as above -- and the
 // histogram H[box][mode] += sign of every outgoing particle, appended to
 // `out` warp by warp.  Persistent warps: a lane whose parent owes no more
-// attempts takes the next parent from a counter; a parent absorbed during
-// its advection owes none.  Each particle is read once and each outgoing
-// particle written once.
-__global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long long* n_in, PArr out,
-                                                  unsigned long long* dc, long long ocap, int advect,
+// attempts takes the next parent; a parent absorbed during its advection
+// owes none.  Each particle is read once and each outgoing particle written
+// once.  A warp claims its parents and its output places from the two
+// global counters in chunks (BE_IN_CHUNK, BE_OUT_CHUNK), not once per pass:
+// every warp of the device adds to the same two words, and their atomics,
+// serialised at one L2 slice each, bounded the kernel.  The output places
+// a warp claimed and did not fill are holes (mode -1), which every reader
+// of the population skips and the next compaction drops; `n_in` counts
+// places, DC_LIVE and DC_WRIT particles.
+constexpr unsigned BE_IN_CHUNK = 128, BE_OUT_CHUNK = 64;
+// ADV: 0 no advection (particles made in this step), 1 advection on a
+// grid of cells, 2 advection across any convex boxes; one kernel each, so
+// that the grid variant carries none of the general walk's registers.
+template <int ADV>
+__global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, const unsigned long long* n_in, PArr out,
+                                                  unsigned long long* dc, long long ocap,
                                                   AdvectArgs aa, int rta, const PAlias* pal, const BoxProp* bprop,
                                                   int nm, const double* w, const float* rprob, const int* ralt,
                                                   int nmodes, unsigned long long skey, int* H, int* err) {
-    const long long n = (long long)*n_in;
+    constexpr bool advect = ADV != 0;
+    const long long n = min((long long)*n_in, ocap);  // places (both buffers hold ocap)
     const int lane = threadIdx.x & 31;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) {
-        if (advect) atomicAdd(dc + DC_PSTEPS, (unsigned long long)n);
-        atomicAdd(dc + DC_IN, (unsigned long long)n);
-    }
-    unsigned long long flips = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned long long flips = 0, nread = 0, written = 0;
     int mode = 0, sign = 1, box = 0, col = 0;
     double x = 0., y = 0.;
     unsigned todo = 0, made = 0;
     bool done = false, valid = false;
+    // the warp's claimed parents [qb, qe) and output places [ob, oe)
+    unsigned long long qb = 0, qe = 0, ob = 0, oe = 0;
     Philox g;
     g.init(skey, 0);
     for (;;) {
         const unsigned idle = __ballot_sync(0xffffffffu, todo == 0 && !done);
         if (idle) {
-            unsigned long long base = 0;
-            const int leader = __ffs(idle) - 1;
-            if (lane == leader) base = atomicAdd(dc + DC_WORK, (unsigned long long)__popc(idle));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (todo == 0 && !done) {
-                const long long i = (long long)base + __popc(idle & ((1u << lane) - 1u));
+            if (qb >= qe) {
+                unsigned long long b = 0;
+                if (lane == 0) b = atomicAdd(dc + DC_WORK, (unsigned long long)BE_IN_CHUNK);
+                b = __shfl_sync(0xffffffffu, b, 0);
+                qb = b;
+                qe = b + BE_IN_CHUNK;
+            }
+            const unsigned rank = __popc(idle & lt);
+            const unsigned long long avail = qe - qb;
+            if (todo == 0 && !done && rank < avail) {  // the others wait for the next pass
+                const long long i = (long long)(qb + rank);
                 if (i < n) {
                     mode = in.mode[i];
                     if (mode >= 0) {
+                        ++nread;
                         sign = in.sign[i];
                         box = in.box[i];
                         x = in.x[i];
                         y = in.y[i];
                         bool alive = true;
                         if (advect) {
-                            if (aa.general) {
+                            if (ADV == 2) {
                                 BePol pol;
                                 pol.g.init(aa.gkey, (uint64_t)i);
                                 int e = 0;
@@ -778,14 +800,24 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
                     done = true;
                 }
             }
+            qb += min((unsigned long long)__popc(idle), avail);
         }
         if (__all_sync(0xffffffffu, done)) break;
         const bool act = todo > 0;
-        // the warp's output places, claimed before the draws so that the
-        // atomic's round trip overlaps the propagator read
+        // the pass's output places, from the warp's chunk (a new chunk when
+        // it cannot hold them all: the rest of the old one become holes)
         const unsigned m1 = __ballot_sync(0xffffffffu, act);
-        unsigned long long wo = 0;
-        if (lane == 0 && m1) wo = atomicAdd(dc + DC_NOUT, (unsigned long long)__popc(m1));
+        const unsigned need = __popc(m1);
+        if (need > oe - ob) {
+            for (unsigned long long k = ob + lane; k < oe && k < (unsigned long long)ocap; k += 32) out.mode[k] = -1;
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(dc + DC_NOUT, (unsigned long long)BE_OUT_CHUNK);
+            b = __shfl_sync(0xffffffffu, b, 0);
+            ob = b;
+            oe = b + BE_OUT_CHUNK;
+        }
+        const unsigned long long wo = ob;
+        ob += need;
         int nmode = mode, nsign = sign;
         if (act && rta) {
             const double u = g.uniform();
@@ -818,9 +850,8 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
                 }
             }
         }
-        wo = __shfl_sync(0xffffffffu, wo, 0);
         if (act) {
-            const long long o = (long long)wo + __popc(m1 & ((1u << lane) - 1u));
+            const long long o = (long long)wo + __popc(m1 & lt);
             if (o < ocap) {
                 out.x[o] = x;
                 out.y[o] = y;
@@ -828,6 +859,7 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
                 out.mode[o] = nmode;
                 out.sign[o] = nsign;
                 atomicAdd(H + (long long)box * nmodes + nmode, nsign);
+                ++written;
             } else {
                 atomicCAS(err, 0, E_LIMIT);
             }
@@ -842,8 +874,20 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
             }
         }
     }
-    for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(0xffffffffu, flips, o);
-    if (lane == 0 && flips) atomicAdd(dc + DC_FLIPS, flips);
+    for (unsigned long long k = ob + lane; k < oe && k < (unsigned long long)ocap; k += 32) out.mode[k] = -1;
+    for (int o = 16; o > 0; o >>= 1) {
+        flips += __shfl_down_sync(0xffffffffu, flips, o);
+        nread += __shfl_down_sync(0xffffffffu, nread, o);
+        written += __shfl_down_sync(0xffffffffu, written, o);
+    }
+    if (lane == 0) {
+        if (flips) atomicAdd(dc + DC_FLIPS, flips);
+        if (nread) {
+            if (advect) atomicAdd(dc + DC_PSTEPS, nread);
+            atomicAdd(dc + DC_IN, nread);
+        }
+        if (written) atomicAdd(dc + DC_WRIT, written);
+    }
 }
 
 // Exclusive scan of cnt[0..n) into descs[k].first, by one warp; returns the
@@ -1072,9 +1116,9 @@ __device__ __forceinline__ unsigned long long gcd_u64(unsigned long long a, unsi
     }
     return a;
 }
-__global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, const int* H, int* cnt, int nmodes,
-                              const int* reservoir, unsigned long long key) {
-    const long long n = (long long)*n_in;
+__global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, long long cap, const int* H, int* cnt,
+                              int nmodes, const int* reservoir, unsigned long long key) {
+    const long long n = min((long long)*n_in, cap);
     if (n <= 0) return;
     // the permutation's a, b and the XOR key, drawn by one thread per block
     __shared__ unsigned long long s_ab[2];
@@ -1097,16 +1141,18 @@ __global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, const int*
 }
 
 // Compaction of [0, *n_in) with the survivors counted into *count.
-__global__ void be_compact_dev(PArr in, const unsigned long long* n_in, PArr out, unsigned long long* count) {
-    compact_body(in, (long long)*n_in, out, count);
+__global__ void be_compact_dev(PArr in, const unsigned long long* n_in, long long cap, PArr out,
+                               unsigned long long* count) {
+    compact_body(in, min((long long)*n_in, cap), out, count);
 }
 
-// dc[to] = dc[from]; record[step] = dc[DC_NP] after it.
-__global__ void be_counters(unsigned long long* dc, int to, int from, long long* record, int step) {
+// dc[to] = dc[from]; dc[DC_LIVE] = dc[live]; then record[step] = dc[DC_LIVE].
+__global__ void be_counters(unsigned long long* dc, int to, int from, int live, long long* record, int step) {
     if (to >= 0) dc[to] = dc[from];
+    if (live >= 0) dc[DC_LIVE] = dc[live];
     if (record) {  // the end of a step: its particles alive, and the outputs of its be_advance launches
-        record[step] = (long long)dc[DC_NP];
-        dc[DC_OUTT] += dc[DC_NOUT];
+        record[step] = (long long)dc[DC_LIVE];
+        dc[DC_OUTT] += dc[DC_WRIT];
     }
 }
 
@@ -1636,6 +1682,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         {
             std::vector<unsigned long long> h0(DC_COUNT, 0ull);
             h0[DC_NP] = (unsigned long long)np;
+            h0[DC_LIVE] = (unsigned long long)np;
             B.d_dc.upload(h0, s);
         }
         B.d_phist.alloc(std::size_t(nsteps + 1) * std::size_t(nbx) * 3 * sizeof(double));
@@ -1741,6 +1788,17 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         }
         const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
         const unsigned pblocks = unsigned(c->nsm) * 8u;  // persistent grids of the step kernels
+        // be_advance: the resident blocks only (each warp claims output
+        // places in chunks, so a warp that starts late would leave holes)
+        unsigned ablocks0 = 0, ablocks1 = 0;
+        {
+            int o0 = 0, o1 = 0;
+            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o0, be_advance<0>, 256, 0), "occupancy");
+            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, general ? be_advance<2> : be_advance<1>, 256, 0),
+               "occupancy");
+            ablocks0 = unsigned(c->nsm) * unsigned(std::max(o0, 1));
+            ablocks1 = unsigned(c->nsm) * unsigned(std::max(o1, 1));
+        }
         const BoxProp* bprop = p->rta ? nullptr : B.d_boxprop.as<BoxProp>();
         int istep = 0;
         double time = 0.;
@@ -1775,13 +1833,14 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             // scattering and histogram in one pass, into B
             ck(cudaMemsetAsync(B.d_H.p, 0, hbytes, s), "memset");
             ck(cudaMemsetAsync(dc + DC_NOUT, 0, 2 * sizeof(unsigned long long), s), "memset");
+            ck(cudaMemsetAsync(dc + DC_WRIT, 0, sizeof(unsigned long long), s), "memset");
             const AdvectArgs a_step{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0,
                                     general, mix_key(p->seed, istep, 31), err, TT};
-            be_advance<<<pblocks, 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP,
-                                               arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc, cap, 1, a_step,
-                                               p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
-                                               c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
-                                               mix_key(p->seed, istep, 64), B.d_H.as<int>(), err);
+            (general ? be_advance<2> : be_advance<1>)<<<ablocks1, 256, 0, s>>>(
+                arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP,
+                arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc, cap, a_step, p->rta, pal, bprop, B.nm,
+                c->d_w.as<double>(), c->d_rprob.as<float>(), c->d_ralt.as<int>(), n, mix_key(p->seed, istep, 64),
+                B.d_H.as<int>(), err);
             ck(cudaEventRecord(ev[1], s), "event");
             // 2-4 the step's sources, made at A[0..) (A is free now) and each
             // advected for a random part of the step as it is made
@@ -1827,30 +1886,33 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             // 5-7 for the new particles: the absorbed ones dropped, the others
             // scattered and counted in the histogram, appended to B
             ck(cudaMemsetAsync(dc + DC_WORK, 0, sizeof(unsigned long long), s), "memset");
-            be_advance<<<pblocks, 256, 0, s>>>(A, dc + DC_NGEN, arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc,
-                                               cap, 0, a_step, p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
-                                               c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
-                                               mix_key(p->seed, istep, 65), B.d_H.as<int>(), err);
+            be_advance<0><<<ablocks0, 256, 0, s>>>(A, dc + DC_NGEN, arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign),
+                                                  dc, cap, a_step, p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
+                                                  c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
+                                                  mix_key(p->seed, istep, 65), B.d_H.as<int>(), err);
             ck(cudaEventRecord(ev[3], s), "event");
             ck(cudaEventRecord(ev[4], s), "event");  // the histogram is made in the passes above
             // 8. cancellation every cancel_every steps: B -> A; otherwise B is the population
             if (istep % cancel_every == 0) {
                 ck(cudaMemsetAsync(B.d_cnt.p, 0, hbytes, s), "memset");
                 be_cancel_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
-                                                      B.d_H.as<int>(), B.d_cnt.as<int>(), n, d_res.as<int>(),
+                                                      cap, B.d_H.as<int>(), B.d_cnt.as<int>(), n, d_res.as<int>(),
                                                       mix_key(p->seed, istep, 77));
                 ck(cudaMemsetAsync(dc + DC_NP, 0, sizeof(unsigned long long), s), "memset");
                 be_compact_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
-                                                       arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP);
+                                                       cap, arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
+                                                       dc + DC_NP);
             } else {
-                be_counters<<<1, 1, 0, s>>>(dc, DC_NP, DC_NOUT, nullptr, 0);
+                be_counters<<<1, 1, 0, s>>>(dc, DC_NP, DC_NOUT, DC_WRIT, nullptr, 0);
                 swap_ab();
             }
             ck(cudaEventRecord(ev[5], s), "event");
             // 9. properties of the step (calculate_prop), recorded on the device
             be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),
                                           B.d_phist.as<double>() + std::size_t(istep + 1) * nbx * 3);
-            be_counters<<<1, 1, 0, s>>>(dc, -1, 0, B.d_nhist.as<long long>(), istep + 1);
+            // after a compaction the population has no holes: its places are its particles
+            be_counters<<<1, 1, 0, s>>>(dc, -1, 0, istep % cancel_every == 0 ? DC_NP : -1,
+                                        B.d_nhist.as<long long>(), istep + 1);
             ck(cudaGetLastError(), "step launch");
             ck(cudaEventRecord(ev[6], s), "event");
             if (p->on_step) {
