@@ -293,6 +293,7 @@ def run_berta(args, rank, world, local):
     adv_ms = 0.0
     adv_bytes = 0.0
     adv_in = 0
+    phase_sum = {}
     by_step = None
     for k in range(args.steps):
         flush.fill_(float(k))
@@ -307,6 +308,8 @@ def run_berta(args, rank, world, local):
         adv_ms += r["phase_ms"]["advection"] + r["phase_ms"]["scattering"]
         adv_bytes += BE_IN_BYTES * r["advance_in"] + BE_OUT_BYTES * r["advance_out"]
         adv_in += int(r["advance_in"])
+        for ph, v in r["phase_ms"].items():
+            phase_sum[ph] = phase_sum.get(ph, 0.0) + v
         if by_step is None:
             by_step = [int(v) for v in r["nparticles"]]
     torch.cuda.synchronize()
@@ -334,6 +337,9 @@ def run_berta(args, rank, world, local):
         "e2e": {"value": ps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": (nsteps + 1) * (nbx * 3 + 1) * 8},
         "kernel_ms_per_step": kern_ms / args.steps,
+        # device time of the reference's timer buckets per 100-step run
+        # (CUDA events at the phase borders of every step)
+        "phase_ms_per_step": {ph: v / args.steps for ph, v in phase_sum.items()},
         "roofline": {"bound": "hbm", "kernel": "be_advance", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind + " (copy burst)",
                      "traffic": traffic,

@@ -155,6 +155,10 @@ struct BertaState {
     std::vector<Spline1D> spl;
     std::vector<char> spl_ok;
     long long spl_version = -1;   // tables the splines were built for
+    // the adiabatic borders' records and J(T) -> T splines on the device
+    long long adi_version = -1;   // tables they were built for
+    int adi_nk = 0;
+    bool adi_splines = false;
 };
 
 void reset_propagators(bte_ctx* c) {
@@ -439,7 +443,7 @@ __device__ __forceinline__ float wall_pmf_f(float w, float vn, float ce, float q
 // pass 1: the chunk's running sums in place and its total
 __device__ __forceinline__ void wall_cdf1_body(const float* om, const float* vx, const float* vy, int n,
                                                const WallReq* req, double* cdf, double* chunk_tot) {
-    __shared__ double part[256];
+    __shared__ double part[64];
     const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
     const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
     const WallReq R = req[r];
@@ -458,19 +462,27 @@ __device__ __forceinline__ void wall_cdf1_body(const float* om, const float* vx,
         acc += double(p);
         row[k] = acc;  // running sum within the thread's segment
     }
-    part[threadIdx.x] = acc;
+    // exclusive offsets of the threads' segments: a shuffle scan in each
+    // warp, then over the warps' totals
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    double incl = acc;
+    for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) part[warp] = incl;
     __syncthreads();
-    if (threadIdx.x == 0) {  // exclusive offsets of the segments
-        double sum = 0.;
-        for (int t = 0; t < blockDim.x; ++t) {
-            const double v = part[t];
-            part[t] = sum;
-            sum += v;
+    if (warp == 0) {
+        double w = lane < nwarps ? part[lane] : 0.;
+        for (int o = 1; o < 32; o <<= 1) {
+            const double t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
         }
-        chunk_tot[blockIdx.x] = sum;
+        if (lane < nwarps) part[32 + lane] = w;  // inclusive totals of the warps
+        if (lane == nwarps - 1) chunk_tot[blockIdx.x] = w;
     }
     __syncthreads();
-    const double off = part[threadIdx.x];
+    const double off = (incl - acc) + (warp > 0 ? part[32 + warp - 1] : 0.);
     for (int k = k0; k < k1; ++k) row[k] += off;
 }
 
@@ -1639,36 +1651,8 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             if (out->nparticles) out->nparticles[sidx] = nn;
         };
-        ck(cudaEventRecord(c->ev0, s), "event");
-        // initial deviation (init_particles, src/beyondRTA_MC2d.cpp:211-269)
-        long long np = 0;
-        descs.clear();
-        aprob.clear();
-        aalt.clear();
-        if (have_ini) {
-            long long first = 0;
-            for (std::size_t k = 0; k < ini.init_box.size(); ++k) {
-                const long long cnt = (long long)n_to_generate(ini.init_energy[k] / p->Eeff, rng);
-                if (cnt == 0) continue;
-                const int b = ini.init_box[k];
-                GenDesc d = box_desc(b);
-                d.sign = ini.init_sign[k];
-                d.cdf = -1;
-                const long long off = (long long)aprob.size();
-                for (std::size_t q = 0; q < std::size_t(n); ++q) {
-                    aprob.push_back(ini.alias[k * std::size_t(n) + q].prob);
-                    aalt.push_back(ini.alias[k * std::size_t(n) + q].alt);
-                }
-                d.alias_off = off;
-                d.first = first;
-                descs.push_back(d);
-                first += cnt;
-            }
-            generate(0, first, -1, 0);
-            np = first;
-        }
-        props(np, 0);
-        long long psteps = 0, branchings = 0, adv_in = 0, adv_out = 0;
+        // everything the host prepares for the run comes before ev0, so that
+        // the device time of the run holds no host work
         // ---- the step loop, resident on the device: particle numbers stay in
         // device counters, the sources are planned on the device, and the
         // step's properties are recorded there; the host synchronises only
@@ -1679,12 +1663,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         auto* dc = B.d_dc.as<unsigned long long>();
         B.d_span.alloc(3 * sizeof(SrcSpan));
         SrcSpan* span = B.d_span.as<SrcSpan>();
-        {
-            std::vector<unsigned long long> h0(DC_COUNT, 0ull);
-            h0[DC_NP] = (unsigned long long)np;
-            h0[DC_LIVE] = (unsigned long long)np;
-            B.d_dc.upload(h0, s);
-        }
         B.d_phist.alloc(std::size_t(nsteps + 1) * std::size_t(nbx) * 3 * sizeof(double));
         B.d_nhist.alloc(std::size_t(nsteps + 1) * sizeof(long long));
         // sources with fixed descriptors: gradient boxes and isothermal walls,
@@ -1728,12 +1706,15 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         }
         // adiabatic re-emission per void border: segment, inward normal, Teq
         // and the J(T) -> T spline of its wall (one per normal and Teq)
-        std::vector<AdiBorder> adi(static_cast<std::size_t>(nborders));
+        // (built once per mode table and geometry: 100 wall pmfs over every
+        // mode per spline, the host's largest cost of a run)
+        const bool adi_cached = B.adi_version == c->tables_version;
+        std::vector<AdiBorder> adi(static_cast<std::size_t>(adi_cached ? 0 : nborders));
         std::vector<double> sa, sb, sc, sd, sx0, sxs;
         std::map<std::tuple<double, double, double>, int> spline_of;
-        int spl_nk = 0;
+        int spl_nk = adi_cached ? B.adi_nk : 0;
         std::vector<double> pmf;
-        for (int gb = 0; gb < nborders; ++gb) {
+        for (int gb = 0; gb < (adi_cached ? 0 : nborders); ++gb) {
             AdiBorder& A = adi[std::size_t(gb)];
             const int b = border_box[std::size_t(gb)];
             const GBorder& br = g.borders[std::size_t(gb)];
@@ -1772,20 +1753,26 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             A.spline = it->second;
         }
-        B.d_adi.upload(adi, s);
+        if (!adi_cached) {
+            B.d_adi.upload(adi, s);
+            B.adi_splines = !sa.empty();
+            if (B.adi_splines) {
+                B.d_sa.upload(sa, s);
+                B.d_sb.upload(sb, s);
+                B.d_sc.upload(sc, s);
+                B.d_sd.upload(sd, s);
+                B.d_sx0.upload(sx0, s);
+                B.d_sxs.upload(sxs, s);
+            }
+            B.adi_nk = spl_nk;
+            B.adi_version = c->tables_version;
+        }
         B.d_adesc.alloc(std::size_t(nborders) * sizeof(GenDesc));
         B.d_acnt.alloc(std::size_t(nborders) * sizeof(long long));
         SplineDev SP{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, spl_nk};
-        if (!sa.empty()) {
-            B.d_sa.upload(sa, s);
-            B.d_sb.upload(sb, s);
-            B.d_sc.upload(sc, s);
-            B.d_sd.upload(sd, s);
-            B.d_sx0.upload(sx0, s);
-            B.d_sxs.upload(sxs, s);
+        if (B.adi_splines)
             SP = SplineDev{B.d_sa.as<double>(), B.d_sb.as<double>(), B.d_sc.as<double>(), B.d_sd.as<double>(),
                            B.d_sx0.as<double>(), B.d_sxs.as<double>(), spl_nk};
-        }
         const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
         const unsigned pblocks = unsigned(c->nsm) * 8u;  // persistent grids of the step kernels
         // be_advance: the resident blocks only (each warp claims output
@@ -1815,6 +1802,42 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
         } pe_guard{&pev};
         for (auto& e : pev) ck(cudaEventCreate(&e), "cudaEventCreate");
+        ck(cudaEventRecord(c->ev0, s), "event");
+        // initial deviation (init_particles, src/beyondRTA_MC2d.cpp:211-269)
+        long long np = 0;
+        descs.clear();
+        aprob.clear();
+        aalt.clear();
+        if (have_ini) {
+            long long first = 0;
+            for (std::size_t k = 0; k < ini.init_box.size(); ++k) {
+                const long long cnt = (long long)n_to_generate(ini.init_energy[k] / p->Eeff, rng);
+                if (cnt == 0) continue;
+                const int b = ini.init_box[k];
+                GenDesc d = box_desc(b);
+                d.sign = ini.init_sign[k];
+                d.cdf = -1;
+                const long long off = (long long)aprob.size();
+                for (std::size_t q = 0; q < std::size_t(n); ++q) {
+                    aprob.push_back(ini.alias[k * std::size_t(n) + q].prob);
+                    aalt.push_back(ini.alias[k * std::size_t(n) + q].alt);
+                }
+                d.alias_off = off;
+                d.first = first;
+                descs.push_back(d);
+                first += cnt;
+            }
+            generate(0, first, -1, 0);
+            np = first;
+        }
+        props(np, 0);
+        long long psteps = 0, branchings = 0, adv_in = 0, adv_out = 0;
+        {
+            std::vector<unsigned long long> h0(DC_COUNT, 0ull);
+            h0[DC_NP] = (unsigned long long)np;
+            h0[DC_LIVE] = (unsigned long long)np;
+            B.d_dc.upload(h0, s);
+        }
         phase[PH_READ] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         std::vector<int> hH;
         const int cancel_every = p->cancel_every > 0 ? p->cancel_every : 4;
