@@ -14,7 +14,7 @@
 //                                           be_plan_sources, be_generate_dev
 //   4 adiabatic diffuse re-emission of |Eborder| at the wall temperature from
 //     the J(T) cubic spline (adiabatic_diffuse_walls :281-435)
-//                  be_plan_adiabatic, be_wall_cdf1/2_dev, be_generate_dev
+//                  be_plan_adiabatic, be_wall_cdf_dev, be_generate_dev
 //   5 deletion of the absorbed particles, 6 propagator scattering with sign
 //     branching (Scattering :1073-1210, propagator_H::get
 //     src/collision_operator.cpp:892-903), each parent's branching attempts
@@ -146,7 +146,6 @@ struct BertaState {
     DBuf d_H, d_cnt, d_Eb, d_props, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
-    DBuf d_ctot;                            // wall-CDF chunk sums
     Pinned h_gens[1];                       // staging: descriptors of the initial particles
     // device-resident step loop: counters, planned sources, per-step records
     DBuf d_dc, d_span, d_gdesc, d_ggenf, d_gcnt, d_idesc, d_igenf, d_icnt, d_adi, d_adesc, d_acnt;
@@ -415,8 +414,10 @@ __device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& 
 
 // Isothermal_wall_distribution (src/sampling.cpp:189-269) of each request:
 // pmf_k = v_n omega_k |n(omega_k, Tw) - n(omega_k, Te)| for v_n > 0, turned
-// into a CDF row; tot[r] keeps the sum.  Each request's row is split into
-// chunks of WCDF_CHUNK modes, one block each.
+// into a CDF row; tot[r] keeps the sum.  One block of WCDF_THREADS threads
+// per request: each thread sums a segment of the row in FP64, a shuffle
+// scan gives the segments' offsets and the row's total, and each thread
+// normalises its own segment.
 //
 // The pmf is evaluated in FP32 and summed in FP64: with x = hbar omega / kT,
 // n_w - n_e = expm1(x_e - x_w) / (expm1(x_e) (-expm1(-x_w))), which has no
@@ -426,7 +427,7 @@ __device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& 
 // value, all entries above 1e-30 of it within 1e-5 (the rounding of x to
 // FP32 at x ~ 60), and the FP64 units do one addition per mode instead of
 // two exponentials and two divisions.
-constexpr int WCDF_CHUNK = 1024;
+constexpr int WCDF_THREADS = 1024;
 
 __device__ __forceinline__ float wall_pmf_f(float w, float vn, float ce, float q, float rr) {
     const float xe = ce * w;   // x_e
@@ -440,17 +441,14 @@ __device__ __forceinline__ float wall_pmf_f(float w, float vn, float ce, float q
     return vn * w * fabsf(diff);
 }
 
-// pass 1: the chunk's running sums in place and its total
-__device__ __forceinline__ void wall_cdf1_body(const float* om, const float* vx, const float* vy, int n,
-                                               const WallReq* req, double* cdf, double* chunk_tot) {
-    __shared__ double part[64];
-    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
-    const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
+__device__ __forceinline__ void wall_cdf_body(const float* om, const float* vx, const float* vy, int n,
+                                              const WallReq* req, double* cdf, double* tot) {
+    __shared__ double wsum[32];
+    const int r = blockIdx.x;
     const WallReq R = req[r];
     double* row = cdf + (long long)r * n;
-    const int c0 = ch * WCDF_CHUNK, c1 = min(n, c0 + WCDF_CHUNK);
-    const int seg = (c1 - c0 + blockDim.x - 1) / blockDim.x;
-    const int k0 = c0 + threadIdx.x * seg, k1 = min(c1, k0 + seg);
+    const int seg = (n + int(blockDim.x) - 1) / int(blockDim.x);
+    const int k0 = min(n, int(threadIdx.x) * seg), k1 = min(n, k0 + seg);
     constexpr double pre = 1e12 * 1.054571726e-34 / 1.3806488e-23;
     const float ce = float(pre / R.Te), q = float(R.Te / R.Tw), rr = float((R.Tw - R.Te) / R.Tw);
     const float nx = float(R.nx), ny = float(R.ny);
@@ -462,45 +460,30 @@ __device__ __forceinline__ void wall_cdf1_body(const float* om, const float* vx,
         acc += double(p);
         row[k] = acc;  // running sum within the thread's segment
     }
-    // exclusive offsets of the threads' segments: a shuffle scan in each
-    // warp, then over the warps' totals
+    // offsets of the segments: a shuffle scan in each warp, then over the
+    // warps' totals
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     double incl = acc;
     for (int o = 1; o < 32; o <<= 1) {
         const double t = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= o) incl += t;
     }
-    if (lane == 31) part[warp] = incl;
+    if (lane == 31) wsum[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        double w = lane < nwarps ? part[lane] : 0.;
+        double w = lane < nwarps ? wsum[lane] : 0.;
         for (int o = 1; o < 32; o <<= 1) {
             const double t = __shfl_up_sync(0xffffffffu, w, o);
             if (lane >= o) w += t;
         }
-        if (lane < nwarps) part[32 + lane] = w;  // inclusive totals of the warps
-        if (lane == nwarps - 1) chunk_tot[blockIdx.x] = w;
+        if (lane < nwarps) wsum[lane] = w;  // inclusive totals of the warps
     }
     __syncthreads();
-    const double off = (incl - acc) + (warp > 0 ? part[32 + warp - 1] : 0.);
-    for (int k = k0; k < k1; ++k) row[k] += off;
-}
-
-// pass 2: offsets of the chunks, normalisation, the request's total
-__device__ __forceinline__ void wall_cdf2_body(int n, const double* chunk_tot, double* cdf, double* tot) {
-    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
-    const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
-    double off = 0., total = 0.;
-    for (int c = 0; c < nch; ++c) {
-        const double v = chunk_tot[(long long)r * nch + c];
-        if (c < ch) off += v;
-        total += v;
-    }
-    if (ch == 0 && threadIdx.x == 0) tot[r] = total;
+    const double total = wsum[nwarps - 1];
+    if (threadIdx.x == 0) tot[r] = total;
     if (!(total > 0.)) return;
-    double* row = cdf + (long long)r * n;
-    const int c0 = ch * WCDF_CHUNK, c1 = min(n, c0 + WCDF_CHUNK);
-    for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) row[k] = (row[k] + off) / total;
+    const double off = (incl - acc) + (warp > 0 ? wsum[warp - 1] : 0.);
+    for (int k = k0; k < k1; ++k) row[k] = (row[k] + off) / total;
 }
 
 // New particles [base, base + n) from the step's sources.
@@ -1104,18 +1087,11 @@ __global__ void be_generate_dev(PArr P, const SrcSpan* span, const GenDesc* gens
 
 // The wall-CDF passes over every border, for the borders the step planned
 // (cnt > 0); rows of the others are left as they are.
-__global__ void __launch_bounds__(256) be_wall_cdf1_dev(const float* om, const float* vx, const float* vy, int n,
-                                                        const WallReq* req, const long long* cnt, double* cdf,
-                                                        double* chunk_tot) {
-    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
-    if (cnt[blockIdx.x / nch] == 0) return;
-    wall_cdf1_body(om, vx, vy, n, req, cdf, chunk_tot);
-}
-__global__ void __launch_bounds__(256) be_wall_cdf2_dev(int n, const long long* cnt, const double* chunk_tot,
-                                                        double* cdf, double* tot) {
-    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
-    if (cnt[blockIdx.x / nch] == 0) return;
-    wall_cdf2_body(n, chunk_tot, cdf, tot);
+__global__ void __launch_bounds__(WCDF_THREADS) be_wall_cdf_dev(const float* om, const float* vx, const float* vy,
+                                                                 int n, const WallReq* req, const long long* cnt,
+                                                                 double* cdf, double* tot) {
+    if (cnt[blockIdx.x] == 0) return;
+    wall_cdf_body(om, vx, vy, n, req, cdf, tot);
 }
 
 // Cancellation on the device over [0, *n_in) with the random affine
@@ -1465,7 +1441,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         B.d_req.alloc(std::size_t(nborders) * sizeof(WallReq));
         B.d_cdf.alloc(std::size_t(nborders) * std::size_t(m.n()) * sizeof(double));
         B.d_cdftot.alloc(std::size_t(nborders) * sizeof(double));
-        B.d_ctot.alloc(std::size_t(nborders) * ((m.n() + WCDF_CHUNK - 1) / WCDF_CHUNK) * sizeof(double));
         ck(cudaMemsetAsync(B.d_Eb.p, 0, std::size_t(nborders) * sizeof(int), s), "memset");
         if (int(B.spl.size()) != nborders || B.spl_version != c->tables_version) {
             B.spl.assign(std::size_t(nborders), Spline1D());
@@ -1773,7 +1748,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         if (B.adi_splines)
             SP = SplineDev{B.d_sa.as<double>(), B.d_sb.as<double>(), B.d_sc.as<double>(), B.d_sd.as<double>(),
                            B.d_sx0.as<double>(), B.d_sxs.as<double>(), spl_nk};
-        const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
         const unsigned pblocks = unsigned(c->nsm) * 8u;  // persistent grids of the step kernels
         // be_advance: the resident blocks only (each warp claims output
         // places in chunks, so a warp that starts late would leave holes)
@@ -1895,11 +1869,9 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 be_plan_adiabatic<<<1, 32, 0, s>>>(B.d_Eb.as<int>(), B.d_adi.as<AdiBorder>(), nborders, SP, p->Eeff,
                                                    p->dt, g.thickness, B.d_req.as<WallReq>(), B.d_acnt.as<long long>(),
                                                    B.d_adesc.as<GenDesc>(), dc, span + 2, cap, err);
-                be_wall_cdf1_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
+                be_wall_cdf_dev<<<unsigned(nborders), WCDF_THREADS, 0, s>>>(
                     B.d_om.as<float>(), B.d_vx.as<float>(), B.d_vy.as<float>(), n, B.d_req.as<WallReq>(),
-                    B.d_acnt.as<long long>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
-                be_wall_cdf2_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
-                    n, B.d_acnt.as<long long>(), B.d_ctot.as<double>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
+                    B.d_acnt.as<long long>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
                 be_generate_dev<<<pblocks, 256, 0, s>>>(A, span + 2, B.d_adesc.as<GenDesc>(), nborders, nullptr, nullptr,
                                                         nullptr, B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n,
                                                         mix_key(p->seed, istep, 4), c->d_boxes.as<GBox>(),
