@@ -1,13 +1,17 @@
 """GPU tests of the beyond-RTA (beRTAMC2D) step loop against the CPU
-restatement: per-step energy density and flux agree within 4.5 sigma over
-independent replicas, for propagator scattering (with sign branching) and
-for the RTA alternative."""
+restatement: per-step energy density and flux agree over independent
+replicas (parity_stats: the count of observables above 3 sigma at a 1 %
+false-alarm rate, and 4.5 sigma for the family), for propagator scattering
+(with sign branching) and for the RTA alternative.  The device loop's
+particle order follows its warps' claims, so its runs are not repeatable
+draw for draw; every replica is an independent sample."""
 import numpy as np
 import pytest
 
 import btegpu
 import pyoracle
 import synth
+from parity_stats import check
 
 pytestmark = pytest.mark.gpu
 
@@ -32,14 +36,11 @@ def test_berta_agrees_with_restatement(engine, rta):
     engine.load_modes(m)
     engine.load_geometry(g)
     engine.load_propagator(P)
-    R = 5
+    R = 8
     kw = dict(dt=1.0, maxtime=40.0, Eeff=2e-23, rta=rta)
     gpu = np.array([_obs(engine.berta_run(seed=10 + i, **kw)) for i in range(R)])
     cpu = np.array([_obs(pyoracle.berta_run(m, g, P, seed=20 + i, **kw)) for i in range(R)])
-    d = gpu.mean(0) - cpu.mean(0)
-    se = np.sqrt(gpu.var(0, ddof=1) / R + cpu.var(0, ddof=1) / R)
-    z = np.abs(d) / np.maximum(se, 1e-300)
-    assert z.max() < 4.5, (z, gpu.mean(0), cpu.mean(0))
+    check(gpu, cpu, [f"ed_box{i}" for i in range(5)] + ["flux_x"], f"beRTA ribbon rta={rta}")
 
 
 def test_berta_counts_and_branching(engine):
@@ -98,14 +99,11 @@ def test_berta_periodic_bar_agrees_with_restatement(engine, rta):
     engine.load_modes(m)
     engine.load_geometry(g)
     engine.load_propagator(P)
-    R = 5
+    R = 8
     kw = dict(dt=1.0, maxtime=40.0, Eeff=1e-23, rta=rta)
     gpu = np.array([_bar_obs(engine.berta_run(seed=10 + i, **kw)) for i in range(R)])
     cpu = np.array([_bar_obs(pyoracle.berta_run(m, g, P, seed=20 + i, **kw)) for i in range(R)])
-    d = gpu.mean(0) - cpu.mean(0)
-    se = np.sqrt(gpu.var(0, ddof=1) / R + cpu.var(0, ddof=1) / R)
-    z = np.abs(d) / np.maximum(se, 1e-300)
-    assert z.max() < 4.5, (z, gpu.mean(0), cpu.mean(0))
+    check(gpu, cpu, [f"ed_strip{i}" for i in range(10)] + ["flux_y"], f"beRTA periodic bar rta={rta}")
 
 
 def test_berta_gradient_source_gives_bulk_kappa(engine):
@@ -138,10 +136,7 @@ def test_berta_gradient_with_propagator_agrees_with_restatement(engine):
         return np.concatenate([f, [r["nparticles"][-1] * 1e-3]])
     gpu = np.array([obs(engine.berta_run(seed=10 + i, **kw)) for i in range(R)])
     cpu = np.array([obs(pyoracle.berta_run(m, g, P, seed=20 + i, **kw)) for i in range(R)])
-    d = gpu.mean(0) - cpu.mean(0)
-    se = np.sqrt(gpu.var(0, ddof=1) / R + cpu.var(0, ddof=1) / R)
-    z = np.abs(d) / np.maximum(se, 1e-300)
-    assert z.max() < 4.5, (z, gpu.mean(0), cpu.mean(0))
+    check(gpu, cpu, ["flux_x", "flux_y", "particles_end"], "beRTA gradient with propagator")
 
 
 def test_bertamc2d_cli_gradient_on_periodic_block(built, tmp_path):
@@ -214,14 +209,11 @@ def test_berta_interpolated_propagator_agrees_with_restatement(engine):
     engine.load_geometry(g)
     for T, P in tab.items():
         engine.load_propagator(P, T)
-    R = 6
+    R = 8
     kw = dict(dt=1.0, maxtime=30.0, Eeff=2e-23, T0=300.0)
     gpu = np.array([_obs(engine.berta_run(seed=10 + i, **kw)) for i in range(R)])
     cpu = np.array([_obs(pyoracle.berta_run(m, g, tab, seed=20 + i, **kw)) for i in range(R)])
-    d = gpu.mean(0) - cpu.mean(0)
-    se = np.sqrt(gpu.var(0, ddof=1) / R + cpu.var(0, ddof=1) / R)
-    z = np.abs(d) / np.maximum(se, 1e-300)
-    assert z.max() < 4.5, (z, gpu.mean(0), cpu.mean(0))
+    check(gpu, cpu, [f"ed_box{i}" for i in range(5)] + ["flux_x"], "beRTA interpolated propagator")
     # with 290 and 305 only, 300 K has one tabulated temperature above it
     e2 = btegpu.Engine(0)
     try:
