@@ -313,10 +313,29 @@ void ensure_static(bte_ctx* c) {
                 }
             }
         }
+        // the same tables per contact, for the evolparticle-faithful kernels
+        std::vector<int> cdmm(g.contacts.size(), -1);
+        for (std::size_t a = 0; a < g.boxes.size(); ++a) {
+            if (g.reservoir[a] || g.tto[a] >= 0) continue;
+            const bte::GBox& B = g.boxes[a];
+            for (int i = 0; i < B.ncontacts; ++i) {
+                const std::size_t ci = std::size_t(B.contact_off + i);
+                const int b = g.contacts[ci].id;
+                if (g.mat[a] == g.mat[std::size_t(b)]) continue;
+                const bte::V2 nw = g.contact_borders[ci].np;
+                cdmm[ci] = tab_of.at(std::make_tuple(g.mat[a], g.mat[std::size_t(b)], nw.x, nw.y));
+            }
+        }
+        std::vector<int> coff;
+        for (int k = 0; k <= c->ncrys; ++k)
+            coff.push_back(k < c->ncrys ? int(c->crys_off[std::size_t(k)]) : int(m.n()));
+        if (cdmm.empty()) cdmm.push_back(-1);
         if (rows.empty()) rows.push_back(0);
         if (ents.empty()) ents.push_back(bte::DmmEnt{0., 0, 0});
         c->d_dmm_row.upload(rows, c->stream);
         c->d_dmm_ent.upload(ents, c->stream);
+        c->d_cdmm.upload(cdmm, c->stream);
+        c->d_crysoff.upload(coff, c->stream);
         c->d_ppieces.upload(pcs, c->stream);
         c->ndmm = int(tab_of.size());
         sync(c);
@@ -485,10 +504,7 @@ void prepare_run(bte_ctx* c, const bte_rta_params* p) {
         throw Error(BTE_ERR_STATE, "load the mode table and the geometry before running");
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     if (c->ncrys > 0) {
-        // crystals joined by mismatch interfaces: the production polygon
-        // kernel only, every crystal at the run's T0
-        if (p->mode != BTE_MODE_PRODUCTION) throw Error(BTE_ERR_INPUT, "several crystals need the production mode");
-        if (p->flags & BTE_FLAG_GENERAL) throw Error(BTE_ERR_INPUT, "several crystals run on the polygon kernel");
+        // crystals joined by mismatch interfaces: every crystal at the run's T0
         if (!c->spec_boxes.empty()) throw Error(BTE_ERR_INPUT, "spectral outputs need one crystal");
         if (c->mat_T0.empty() || c->mat_T0[0] != p->T0) {
             c->mat_T0.assign(std::size_t(c->ncrys), p->T0);
@@ -1115,6 +1131,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         T.lalias = c->d_lalias.as<int4>();
         T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
         T.box_mat = c->nmat > 0 ? c->d_boxmat.as<int>() : nullptr;
+        bte::set_crystal_tables(c, T);
         T.ntime = int(ntime);
         T.timegrid = c->d_time.as<double>();
         T.maxtime = maxtime;
@@ -1467,6 +1484,7 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
     T.lalias = c->d_lalias.as<int4>();
     T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
     T.box_mat = c->nmat > 0 ? c->d_boxmat.as<int>() : nullptr;
+    set_crystal_tables(c, T);
     T.ntime = r->ntime;
     T.timegrid = nullptr;  // set by the caller
     T.maxtime = r->maxtime;
@@ -1547,6 +1565,17 @@ void fill_static_tables(bte_ctx* c, DevTables& T) {
     T.lalias = c->d_lalias.as<int4>();
     T.mirror = c->have_mirror ? c->d_mirror.as<int>() : nullptr;
     T.box_mat = c->nmat > 0 ? c->d_boxmat.as<int>() : nullptr;
+    set_crystal_tables(c, T);
+}
+
+// The interface tables of crystals joined by mismatch interfaces (null
+// with one crystal).
+void set_crystal_tables(const bte_ctx* c, DevTables& T) {
+    const bool crys = c->ncrys > 0 && c->dmm_dev;
+    T.contact_dmm = crys ? c->d_cdmm.as<int>() : nullptr;
+    T.dmm_row = crys ? c->d_dmm_row.as<long long>() : nullptr;
+    T.dmm_ent = crys ? c->d_dmm_ent.as<DmmEnt>() : nullptr;
+    T.crys_off = crys ? c->d_crysoff.as<int>() : nullptr;
 }
 
 double box_T0(const bte_ctx* c, int b, double T0) {

@@ -90,6 +90,7 @@ struct bte_ctx {
     bool dmm_dev = false;
     int ndmm = 0;
     bte::DBuf d_dmm_row, d_dmm_ent;
+    bte::DBuf d_cdmm, d_crysoff;  // per contact its interface table (-1: none); crystals' first modes
     bte::DBuf d_gx, d_gy, d_gcell, d_boxcell;
     bte::DBuf d_pborders, d_ppieces;  // convex-polygon path (geometries that are not a grid)
     bte::DBuf d_row_ptr, d_lcol, d_lcdf, d_lalias, d_mirror;
@@ -163,6 +164,8 @@ void prepare_run(bte_ctx* c, const bte_rta_params* p);
 bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r, std::string* why);
 // Mode, geometry and Lambert tables of a context into the kernel tables.
 void fill_static_tables(bte_ctx* c, DevTables& T);
+// The interface tables of several crystals into the kernel tables.
+void set_crystal_tables(const bte_ctx* c, DevTables& T);
 // The ntime points of the time grid (src/RTA_MC2D.cpp:2118-2124: i * step,
 // the last exactly maxtime) followed by the ntime - 1 bin widths, the
 // layout DevTables::timegrid points to.

@@ -68,12 +68,6 @@ struct PolyPiece {
     double s0, s1;  // the interval of s, widened by 1e-9 at both ends
     int box, pad;   // pad: the mismatch table of the contact (-1: same crystal)
 };
-// One entry of a diffuse mismatch table: cumulative probability, global
-// mode out, side out (0: back into the incident box, 1: into the other).
-struct DmmEnt {
-    double cum;
-    int out, side;
-};
 // An axis-aligned rectangular box of the polygon path: its lines and the
 // box's own indices of its +x, -x, +y, -y borders (kx1 = -1: not such a
 // box, the general border search applies); across each side the

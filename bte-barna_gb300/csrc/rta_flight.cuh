@@ -31,6 +31,13 @@ struct WallGenDev {
     int box, sign;
 };
 
+// One entry of a diffuse mismatch table: cumulative probability, global
+// mode out, side out (0: back into the incident box, 1: into the other).
+struct DmmEnt {
+    double cum;
+    int out, side;
+};
+
 struct DevTables {
     // modes
     int n, nb;
@@ -98,6 +105,15 @@ struct DevTables {
     // <= 1: one tally)
     int ngroups;
     long long group_stride;
+    // crystals joined by mismatch interfaces (null: one crystal): per
+    // contact the interface table of (its box's crystal, the neighbour's,
+    // the contact normal), -1 within a crystal; the tables' rows
+    // [table][n + 1] into their entries; each crystal's first global mode
+    // (ncrys + 1 values)
+    const int* contact_dmm;
+    const long long* dmm_row;
+    const DmmEnt* dmm_ent;
+    const int* crys_off;
 };
 
 // One thread's counts over one launch (32 bits: a thread would need over
@@ -218,6 +234,63 @@ __device__ __forceinline__ int contact_index(const DevTables& T, int box, int te
     for (int i = 0; i < B.ncontacts; ++i)
         if (T.contacts[B.contact_off + i].id == test) return B.contact_off + i;
     return -1;
+}
+
+// The interface table between `box` and its neighbour `inew`, or -1 (one
+// crystal, the same crystal, or no contact).
+__device__ __forceinline__ int dmm_table(const DevTables& T, int box, int inew) {
+    if (!T.contact_dmm) return -1;
+    const int ci = contact_index(T, box, inew);
+    return ci >= 0 ? T.contact_dmm[ci] : -1;
+}
+
+// Mode k of the incident crystal `ma` read in crystal `mb` by its index
+// within its crystal (the reference keeps (q, alpha) across an interface
+// without a transition), or -1 beyond mb's table.
+__device__ __forceinline__ int dmm_same_index(const DevTables& T, int k, int ma, int mb) {
+    const int local = k - T.crys_off[ma];
+    return local < T.crys_off[mb + 1] - T.crys_off[mb] ? T.crys_off[mb] + local : -1;
+}
+
+// change_material_diffuse (src/RTA_MC2D.cpp:871-964): the particle meets
+// its box's contact with box `inew` of another crystal; the interface's
+// table re-emits it on either side (Diffuse_mismatch_distribution::reemit,
+// src/sampling.cpp:831-902: p uniform between the first and the last
+// cumulative value of the incident mode's entries, the first entry not
+// below p) and the flight ends (dt = 0).  An incident mode without entries
+// (the reference's 'X') crosses with its index kept within the crystal.
+template <class P>
+__device__ int dmm_cross(const DevTables& T, P& pol, Particle& p, int inew, int table, double& dt, Counters& c) {
+    const long long* row = T.dmm_row + (long long)table * (T.n + 1);
+    const long long e0 = row[p.mode], e1 = row[p.mode + 1];
+    c.ifc_hits++;
+    if (e1 > e0) {
+        const double lo = T.dmm_ent[e0].cum, hi = T.dmm_ent[e1 - 1].cum;
+        const double pp = pol.u() * (hi - lo) + lo;
+        long long a = e0, b = e1 - 1;
+        while (a < b) {
+            const long long mid = (a + b) >> 1;
+            if (T.dmm_ent[mid].cum >= pp) b = mid;
+            else a = mid + 1;
+        }
+        const DmmEnt en = T.dmm_ent[a];
+        p.mode = en.out;
+        if (en.side != 0) {
+            p.box = inew;
+            p.mo = mat_off(T, inew);
+            c.ifc_trans++;
+        }
+    } else {
+        c.quirks++;
+        const int k = dmm_same_index(T, p.mode, T.box_mat[p.box], T.box_mat[inew]);
+        if (k < 0) return E_VALUE;
+        p.mode = k;
+        p.box = inew;
+        p.mo = mat_off(T, inew);
+        c.ifc_trans++;
+    }
+    dt = 0.;
+    return 0;
 }
 
 template <class P>
@@ -525,6 +598,12 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
         int e = seg_tally<STEADY>(T, pol, p, tf, v);
         if (e) return e;
         p.t += tf;
+        const int tab = dmm_table(T, p.box, pboxes[0]);
+        if (tab >= 0) {  // another crystal (:1282, :1690)
+            e = dmm_cross(T, pol, p, pboxes[0], tab, dt, c);
+            if (STEADY) fate = FATE_BOUNCE;  // pushed into the next generation
+            return e;
+        }
         p.box = pboxes[0];
         c.crossings++;
         return 0;
@@ -545,6 +624,12 @@ __device__ int evolparticle(const DevTables& T, P& pol, Particle& p, V2 v, doubl
             if (T.boxes[newid].tto < 0) p.pos = add(p.pos, divs(scal(1.0e-6, d), norm(d)));
         } else {
             newid = pbox2[pol.choose(n2)];
+        }
+        const int tab = dmm_table(T, p.box, newid);
+        if (tab >= 0) {  // another crystal (:1355-1366, :1762-1776)
+            e = dmm_cross(T, pol, p, newid, tab, dt, c);
+            if (STEADY) fate = FATE_BOUNCE;
+            return e;
         }
         p.box = newid;
         c.crossings++;

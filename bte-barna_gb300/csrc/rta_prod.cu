@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(128) rta_prod_general(DevTables T, double* tal
         }
     }
     c.tallies += pol.ntally;
-    flush_counters_p(c, counters);
+    flush_counters_p<13>(c, counters);
 }
 
 // Generation 0: 1 per slot whose first draw picks a gradient generator.
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(128) rta_steady_prod(DevTables T, SteadyArgs A
         }
     }
     c.tallies += pol.ntally;
-    flush_counters_p(c, counters);
+    flush_counters_p<13>(c, counters);
 }
 
 void launch_steady_prod(const DevTables& T, const SteadyArgs& A, double* tally,
@@ -1373,8 +1373,15 @@ __global__ void __launch_bounds__(256) rta_prod_poly(DevTables T, PolyArgs A, do
                 const DmmEnt en = A.dmm_ent[a];
                 dmm_mode = en.out;
                 dmm_back = en.side == 0;
-            } else {
+            } else {  // no entries: across with the index kept within the crystal
                 c.quirks++;
+                dmm_mode = dmm_same_index(T, p.mode, T.box_mat[p.box], T.box_mat[target]);
+                if (dmm_mode < 0) {
+                    record_error(err, E_VALUE, pid);
+                    active = false;
+                    done = true;
+                    continue;
+                }
             }
             c.ifc_hits++;
             if (!dmm_back) c.ifc_trans++;
@@ -1664,8 +1671,16 @@ __global__ void __launch_bounds__(128) rta_steady_poly(DevTables T, SteadyArgs A
                 const DmmEnt en = PA.dmm_ent[a];
                 p.mode = en.out;
                 across = en.side != 0;
-            } else {
+            } else {  // no entries: across with the index kept within the crystal
                 c.quirks++;
+                const int k = dmm_same_index(T, p.mode, T.box_mat[p.box], T.box_mat[target]);
+                if (k < 0) {
+                    record_error(err, E_VALUE, slot);
+                    A.flag[slot] = 0;
+                    active = false;
+                    continue;
+                }
+                p.mode = k;
             }
             c.ifc_hits++;
             if (across) {

@@ -105,11 +105,11 @@ struct ReplayPolicy {
 };
 
 __device__ __forceinline__ void flush_counters(const Counters& c, unsigned long long* out) {
-    unsigned long long v[11] = {c.events, c.wall_hits, c.crossings, c.absorbed,
+    unsigned long long v[13] = {c.events, c.wall_hits, c.crossings, c.absorbed,
                                 c.specular, c.nudges, c.quirks, c.tallies, c.translations,
-                                c.scattered, c.lost};
+                                c.scattered, c.lost, c.ifc_hits, c.ifc_trans};
 #pragma unroll
-    for (int i = 0; i < 11; ++i) {
+    for (int i = 0; i < 13; ++i) {
         unsigned long long x = v[i];
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + i, x);

@@ -155,10 +155,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         if (!(p->specularity >= 0. && p->specularity <= 1.))
             throw Error(BTE_ERR_INPUT, "specularity must be in [0, 1]");
         if (crystals) {
-            // crystals joined by mismatch interfaces: the production polygon
-            // kernel, every crystal at T0
-            if (p->mode != BTE_MODE_PRODUCTION) throw Error(BTE_ERR_INPUT, "several crystals need the production mode");
-            if (p->flags & BTE_FLAG_GENERAL) throw Error(BTE_ERR_INPUT, "several crystals run on the polygon kernel");
+            // crystals joined by mismatch interfaces, every crystal at T0
             if (!c->spec_boxes.empty()) throw Error(BTE_ERR_INPUT, "spectral outputs need one crystal");
             if (c->mat_T0.empty() || c->mat_T0[0] != p->T0) {
                 c->mat_T0.assign(std::size_t(c->ncrys), p->T0);

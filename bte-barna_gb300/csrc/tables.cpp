@@ -1062,6 +1062,26 @@ Generators merge_generators(std::vector<Generators>& G, bool walls, bool require
         R.total_energy = total;
     } else if (R.init_box.empty()) {
         throw Error(BTE_ERR_INPUT, "no box with Tinit different from Teq");
+    } else {
+        // the initial deviation's boxes in ascending box order, as one
+        // crystal's are, and their energy summed in that order
+        const std::size_t nb = R.init_box.size(), n = R.cdf.size() / nb;
+        std::vector<std::size_t> ord(nb);
+        std::iota(ord.begin(), ord.end(), std::size_t(0));
+        std::stable_sort(ord.begin(), ord.end(),
+                         [&](std::size_t a, std::size_t b) { return R.init_box[a] < R.init_box[b]; });
+        Generators S;
+        S.total_energy = 0.;
+        for (std::size_t i : ord) {
+            S.init_box.push_back(R.init_box[i]);
+            S.init_sign.push_back(R.init_sign[i]);
+            S.init_energy.push_back(R.init_energy[i]);
+            S.cdf.insert(S.cdf.end(), R.cdf.begin() + std::ptrdiff_t(i * n), R.cdf.begin() + std::ptrdiff_t((i + 1) * n));
+            S.alias.insert(S.alias.end(), R.alias.begin() + std::ptrdiff_t(i * n),
+                           R.alias.begin() + std::ptrdiff_t((i + 1) * n));
+            S.total_energy += R.init_energy[i];
+        }
+        return S;
     }
     return R;
 }

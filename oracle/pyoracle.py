@@ -471,6 +471,8 @@ def rta_run_multi(tables, geom, T0, dt, maxtime, N, seed=1, nthreads=8, source=N
     r = _bt.RtaResult()
     for k in out:
         setattr(r, k, out[k].ctypes.data_as(C.POINTER(C.c_double)))
+    out["exact"] = np.zeros(shape + (3, 2), dtype=np.int64)
+    r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
     cnt = np.zeros(9, dtype=np.int64)
     st = lib.oracle_rta_run_multi(arr, len(tables), C.byref(gs), C.byref(p), int(nthreads), C.byref(r),
                                   cnt.ctypes.data_as(C.POINTER(C.c_longlong)))

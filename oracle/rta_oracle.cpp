@@ -3138,6 +3138,7 @@ int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry
                 T.jx[k] += tl[t].jx[k];
                 T.jy[k] += tl[t].jy[k];
             }
+            for (std::size_t k = 0; k < T.ex.size(); ++k) T.ex[k] += tl[t].ex[k];
             T.events += tl[t].events;
             T.wall_hits += tl[t].wall_hits;
             T.crossings += tl[t].crossings;
@@ -3149,6 +3150,13 @@ int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry
             T.interface_hits += tl[t].interface_hits;
             T.interface_transmissions += tl[t].interface_transmissions;
         }
+        // the exact 128-bit sums, as the replay kernels keep them
+        if (out->exact)
+            for (std::size_t k = 0; k < T.ex.size(); ++k) {
+                unsigned __int128 u = (unsigned __int128)T.ex[k];
+                out->exact[2 * k] = int64_t(uint64_t(u >> 64));
+                out->exact[2 * k + 1] = int64_t(uint64_t(u));
+            }
         out->nboxes = int32_t(nbx);
         out->nbins = int32_t(nbn);
         out->Eeff = M.Eeff;

@@ -1,9 +1,10 @@
 """GPU parity of several crystals joined by diffuse mismatch interfaces
 (bte_load_mode_tables; change_material_diffuse, src/RTA_MC2D.cpp:871-964,
-Diffuse_mismatch_distribution::reemit, src/sampling.cpp:831-902): the
-polygon kernel's re-emissions against the restatement in transient runs and
-in the periodic steady state, particle time conserved across interfaces,
-and the modes this path does not take."""
+Diffuse_mismatch_distribution::reemit, src/sampling.cpp:831-902): replay
+mode bit for bit against the restatement (transient runs from walls and
+from an initial deviation, and the periodic steady state), the production
+polygon kernel and the evolparticle-faithful kernel statistically, particle
+time conserved across interfaces, and the outputs crystals do not take."""
 import os
 import subprocess
 
@@ -75,16 +76,71 @@ def test_two_crystals_conserve_particle_time(engine):
     assert np.allclose(per_bin, per_bin[0], rtol=1e-9, atol=0)
 
 
-def test_crystals_take_the_production_polygon_path_only(engine):
+def _closed_block():
+    g = synth.grid_geometry(200.0, 50.0, 10, 2)
+    v = np.asarray(g["vertices"], float).reshape(-1, 4, 2).mean(axis=1)
+    g["material"] = (v[:, 0] > 100.0).astype(np.int32)
+    g["Tinit"] = np.where(g["material"] == 0, 300.5, 300.0)
+    return g
+
+
+@pytest.mark.parametrize("source", ["walls", "initial"])
+def test_two_crystals_replay_is_bit_exact(engine, source):
+    """Replay mode (pcg64 streams, CDF inversion, the interface drawing its
+    re-emission from the particle's stream as the restatement does)
+    reproduces the restatement's multi-crystal run draw for draw: identical
+    128-bit tallies and counters, on the ribbon with reservoirs in each
+    crystal and on the closed block with an initial deviation."""
+    A, B = _tables()
+    if source == "walls":
+        g, src, N = _ribbon(), btegpu.SOURCE_WALLS, 4000
+    else:
+        g, src, N = _closed_block(), btegpu.SOURCE_INITIAL, 4000
+    engine.load_mode_tables([A, B])
+    engine.load_geometry(g)
+    kw = dict(T0=300.0, dt=10.0, maxtime=200.0)
+    r = engine.rta_run(N=N, seed=5, mode=btegpu.MODE_REPLAY, source=src, exact=True, **kw)
+    o = pyoracle.rta_run_multi([A, B], g, N=N, seed=5, nthreads=16, source=src, **kw)
+    assert r["interface_hits"] > 0 and 0 < r["interface_transmissions"] < r["interface_hits"]
+    for k in ("events", "wall_hits", "crossings", "absorbed", "interface_hits", "interface_transmissions"):
+        assert r[k] == o[k], (k, r[k], o[k])
+    assert np.array_equal(r["exact"], o["exact"])
+    assert r["Eeff"] == o["Eeff"]
+
+
+def test_two_crystals_general_kernel_agrees_with_restatement(engine):
+    """The evolparticle-faithful production kernel (BTE_FLAG_GENERAL) with
+    the interfaces: the ribbon's temperatures and transmitted fraction
+    against the restatement."""
+    A, B = _tables()
+    g = _ribbon()
+    engine.load_mode_tables([A, B])
+    engine.load_geometry(g)
+    kw = dict(T0=300.0, dt=10.0, maxtime=300.0)
+    N, R = 20000, 6
+    names = [f"T_cell{i}_late" for i in range(10)] + ["transmitted"]
+
+    def obs(r):
+        T = r["temperature"][:10] - 300.0
+        return np.concatenate([T[:, -10:].mean(axis=1) * 10,
+                               [r["interface_transmissions"] / max(r["interface_hits"], 1)]])
+    gpu = [obs(engine.rta_run(N=N, seed=300 + i, flags=btegpu.FLAG_GENERAL, **kw)) for i in range(R)]
+    cpu = [obs(pyoracle.rta_run_multi([A, B], g, N=N, seed=400 + i, nthreads=16, **kw)) for i in range(R)]
+    check(np.array(gpu), np.array(cpu), names, "two crystals, evolparticle-faithful kernel")
+
+
+def test_crystals_refuse_rate_sets_and_spectral_outputs(engine):
     A, B = _tables()
     engine.load_mode_tables([A, B])
     engine.load_geometry(_ribbon())
-    with pytest.raises(btegpu.BteError, match="production"):
-        engine.rta_run(300.0, 10.0, 100.0, 1000, mode=btegpu.MODE_REPLAY)
-    with pytest.raises(btegpu.BteError, match="polygon"):
-        engine.rta_run(300.0, 10.0, 100.0, 1000, flags=btegpu.FLAG_GENERAL)
     with pytest.raises(btegpu.BteError, match="rate sets"):
         engine.load_materials([A["w"]], [300.0])
+    engine.set_spectral([0], 10)
+    try:
+        with pytest.raises(btegpu.BteError, match="spectral"):
+            engine.rta_run(300.0, 10.0, 100.0, 1000)
+    finally:
+        engine.set_spectral([], 0)
 
 
 def test_two_crystal_steady_state_agrees_with_restatement(engine):
@@ -116,10 +172,30 @@ def test_two_crystal_steady_state_agrees_with_restatement(engine):
     cpu = [obs(pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), N, seed=400 + i, nthreads=16))
            for i in range(R)]
     check(np.array(gpu), np.array(cpu), names, "two-crystal steady state")
-    with pytest.raises(btegpu.BteError, match="production"):
-        engine.steady_run(300.0, (0.0, -0.01), N, seed=1, mode=btegpu.MODE_REPLAY)
-    with pytest.raises(btegpu.BteError, match="polygon"):
-        engine.steady_run(300.0, (0.0, -0.01), N, seed=1, flags=btegpu.FLAG_GENERAL)
+    # the evolparticle-faithful kernel with the same interfaces
+    gen = [obs(engine.steady_run(300.0, (0.0, -0.01), N, seed=500 + i, flags=btegpu.FLAG_GENERAL))
+           for i in range(R)]
+    check(np.array(gen), np.array(cpu), names, "two-crystal steady state, evolparticle-faithful kernel")
+
+
+def test_two_crystal_steady_replay_is_bit_exact(engine):
+    """The steady state of the layered bar in replay mode against the
+    restatement's steady run over several materials: every generation, its
+    128-bit tallies and the counters, interface re-emissions included."""
+    A, B = _tables()
+    g = synth.layered_bar_geometry()
+    engine.load_mode_tables([A, B])
+    engine.load_geometry(g)
+    r = engine.steady_run(300.0, (0.0, -0.01), 3000, seed=6, mode=btegpu.MODE_REPLAY)
+    o = pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), 3000, seed=6, nthreads=16)
+    assert r["generations"] == o["generations"] > 1
+    assert r["interface_hits"] > 0
+    for k in ("events", "wall_hits", "crossings", "absorbed", "translations", "scattered", "births", "lost",
+              "interface_hits", "interface_transmissions"):
+        assert r[k] == o[k], (k, r[k], o[k])
+    assert np.array_equal(r["exact"], o["exact"])
+    assert np.array_equal(r["log"], o["log"])
+    assert r["Eeff"] == o["Eeff"]
 
 
 def test_rtamc2d_cli_reads_several_materials(built, tmp_path):
