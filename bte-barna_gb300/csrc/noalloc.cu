@@ -21,8 +21,9 @@
 //     depend on an earlier call, but calls that overlap on the GPU (on
 //     several streams or threads at once) race and must be serialised;
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (set-up, once per device); make that first call
-//     before any stream capture.  The address is kept for the life of the
+//     cudaGetSymbolAddress (set-up, once per device); every call
+//     synchronises its stream, so none can be recorded in a stream
+//     capture.  The address is kept for the life of the
 //     process and never looked up again, so a process that calls
 //     cudaDeviceReset must not use this entry point on that device after it.
 #include <cuda_runtime.h>

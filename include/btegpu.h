@@ -506,8 +506,8 @@ bte_status bte_get_group_result(bte_ctx* ctx, int32_t group, bte_rta_result* out
  * initial source the same N and seed); the boxes must tile an axis-aligned
  * grid and mode must be BTE_MODE_PRODUCTION.  The first call on a device
  * does the set-up: it looks up the scratch address once (kept until the
- * process exits, so not after a cudaDeviceReset); make that first call
- * before any stream capture. */
+ * process exits, so not after a cudaDeviceReset).  Since every call
+ * synchronises its stream, no call can be recorded in a stream capture. */
 bte_status bte_rta_run_noalloc(bte_ctx* ctx, const bte_rta_params* params,
                                double* d_tally, bte_rta_result* out);
 
