@@ -287,10 +287,10 @@ def load_library(path: str = LIB_PATH):
     lib.bte_load_materials.argtypes = [vp, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double)]
     lib.bte_load_materials.restype = C.c_int
-    lib.bte_load_mode_tables.argtypes = [vp, C.c_int32, C.POINTER(ModeTable)]
+    lib.bte_load_mode_tables.argtypes = [vp, C.c_int32, C.POINTER(ModeTable), C.POINTER(C.c_double)]
     lib.bte_load_mode_tables.restype = C.c_int
     lib.bte_interface_table.argtypes = [C.POINTER(ModeTable), C.POINTER(ModeTable), C.c_double, C.c_double,
-                                        C.c_double, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                        C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     lib.bte_interface_table.restype = C.c_int
     lib.bte_set_spectral.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32]
@@ -361,16 +361,22 @@ class Engine:
         self._check(self.lib.bte_load_modes(self.ctx, C.byref(s)))
         self._keep["modes"] = keep
 
-    def load_mode_tables(self, tables):
+    def load_mode_tables(self, tables, thickness=None):
         """Several crystals: mode table k for the boxes of material k
-        (geometry "material"), diffuse mismatch at their contacts."""
+        (geometry "material"), diffuse mismatch at their contacts.
+        `thickness`: each crystal's thickness in nm (None: the geometry's)."""
         arr = (ModeTable * len(tables))()
         keep = []
         for i, t in enumerate(tables):
             s, k = mode_struct(t)
             arr[i] = s
             keep.append(k)
-        self._check(self.lib.bte_load_mode_tables(self.ctx, len(tables), arr))
+        th = None if thickness is None else np.ascontiguousarray(np.asarray(thickness, dtype=float))
+        if th is not None and th.size != len(tables):
+            raise ValueError("one thickness per mode table")
+        self._check(self.lib.bte_load_mode_tables(self.ctx, len(tables), arr,
+                                                  _dptr(th) if th is not None else None))
+        keep.append(th)
         self._keep["modes"] = {"omega": np.concatenate([np.asarray(t["omega"], float) for t in tables])}
         self._keep["crystals"] = (arr, keep)
 
@@ -547,17 +553,19 @@ Engine.load_propagator = _engine_load_propagator
 Engine.berta_run = _engine_berta_run
 
 
-def interface_table(A: dict, B: dict, normal, thickness: float, Tref: float):
+def interface_table(A: dict, B: dict, normal, thickness, Tref: float):
     """The engine's diffuse mismatch table from mode table A to B (host
     code, no device): per incident mode of A, arrays (side out, mode out,
-    cumulative)."""
+    cumulative).  `thickness`: one value for both crystals' boxes, or the
+    pair (A's, B's)."""
     lib = load_library()
     sa, ka = mode_struct(A)
     sb, kb = mode_struct(B)
     na = int(np.asarray(A["omega"]).size)
     first = np.zeros(na + 1, dtype=np.int64)
     ne = np.zeros(1, dtype=np.int64)
-    args = (C.byref(sa), C.byref(sb), float(normal[0]), float(normal[1]), float(thickness), float(Tref))
+    ta, tb = (thickness, thickness) if np.isscalar(thickness) else thickness
+    args = (C.byref(sa), C.byref(sb), float(normal[0]), float(normal[1]), float(ta), float(tb), float(Tref))
     lp = C.POINTER(C.c_int64)
     st = lib.bte_interface_table(*args, first.ctypes.data_as(lp), ne.ctypes.data_as(lp), None, None, None)
     if st != 0:

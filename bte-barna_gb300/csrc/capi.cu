@@ -286,7 +286,8 @@ void ensure_static(bte_ctx* c) {
                 const bte::HostModes& Bm = c->crys[std::size_t(mb)];
                 const bte::DmmTable D = bte::build_dmm_table(
                     A, c->crys_off[std::size_t(ma)], Bm, c->crys_off[std::size_t(mb)], ntot, nw,
-                    A.V * g.thickness / A.c, Bm.V * g.thickness / Bm.c, g.Teq[a], hw_threads());
+                    A.V * bte::crystal_thickness(c, ma) / A.c, Bm.V * bte::crystal_thickness(c, mb) / Bm.c,
+                    g.Teq[a], hw_threads());
                 tab_of[key] = int(tab_of.size());
                 const long long base = (long long)ents.size();
                 for (std::size_t K = 0; K <= ntot; ++K) rows.push_back(base + D.row[K]);
@@ -427,7 +428,7 @@ void ensure_generators(bte_ctx* c, const bte_rta_params* p) {
         // each crystal's generators, rows over the concatenated modes
         std::vector<bte::Generators> G;
         for (int k = 0; k < c->ncrys; ++k) {
-            const bte::GenEmbed e{k, c->crys_off[std::size_t(k)], c->modes.n()};
+            const bte::GenEmbed e{k, c->crys_off[std::size_t(k)], c->modes.n(), bte::crystal_thickness(c, k)};
             G.push_back(p->source == BTE_SOURCE_WALLS
                             ? bte::build_wall_generators(c->crys[std::size_t(k)], c->geom, false, &e)
                             : bte::build_initial_generators(c->crys[std::size_t(k)], c->geom, &e));
@@ -556,7 +557,7 @@ void rta_post(bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, double Ee
     // post-processing, src/RTA_MC2D.cpp:2336-2435
     each([&](std::vector<double>& v) {
         for (int ir = 0; ir < nbx; ++ir) {
-            const double vbox = g.boxes[std::size_t(ir)].area * g.thickness;
+            const double vbox = g.boxes[std::size_t(ir)].area * bte::box_thickness(c, ir);
             for (int i = 0; i < nbins; ++i) v[std::size_t(ir) * nbins + i] /= vbox;
         }
     });
@@ -611,7 +612,7 @@ void rta_post(bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, double Ee
         for (int ir = 0; ir < nbx; ++ir) {
             const std::size_t mk = std::size_t(c->nmat > 0 ? g.mat[std::size_t(ir)] : 0);
             const double cv = cvm[mk];
-            const double vcorr = g.thickness / (c->ncrys > 0 ? c->crys[mk].c : m.c);
+            const double vcorr = bte::box_thickness(c, ir) / (c->ncrys > 0 ? c->crys[mk].c : m.c);
             const double T0b = bte::box_T0(c, ir, p->T0);
             for (int i = 0; i < nbins; ++i) {
                 const std::size_t k = std::size_t(ir) * nbins + i;
@@ -708,6 +709,7 @@ bte_status bte_load_modes(bte_ctx* c, const bte_mode_table* mt) {
         c->ncrys = 0;
         c->crys.clear();
         c->crys_off.clear();
+        c->crys_thick.clear();
         c->dmm_dev = false;
         c->nmat = 0;  // materials are rate sets over one table
         c->mat_w.clear();
@@ -748,11 +750,19 @@ bte_status bte_load_geometry(bte_ctx* c, const bte_geometry* g) {
     }
 }
 
-bte_status bte_load_mode_tables(bte_ctx* c, int32_t ntables, const bte_mode_table* tables) {
+bte_status bte_load_mode_tables(bte_ctx* c, int32_t ntables, const bte_mode_table* tables,
+                                const double* thickness) {
     if (!c) return BTE_ERR_INPUT;
     c->group_valid = false;
     try {
         if (ntables < 1 || !tables) throw Error(BTE_ERR_INPUT, "no mode tables");
+        std::vector<double> th;
+        if (thickness)
+            for (int k = 0; k < ntables; ++k) {
+                if (!(thickness[k] > 0.) || !std::isfinite(thickness[k]))
+                    throw Error(BTE_ERR_INPUT, "crystal thickness must be > 0");
+                th.push_back(thickness[k]);
+            }
         ck(cudaSetDevice(c->device), "cudaSetDevice");
         std::vector<bte::HostModes> crys;
         for (int k = 0; k < ntables; ++k) crys.push_back(bte::build_modes(&tables[k]));
@@ -769,6 +779,7 @@ bte_status bte_load_mode_tables(bte_ctx* c, int32_t ntables, const bte_mode_tabl
         c->modes = std::move(all);
         c->crys = std::move(crys);
         c->crys_off = std::move(off);
+        c->crys_thick = std::move(th);
         c->ncrys = ntables;
         c->have_modes = true;
         c->tables_version++;
@@ -789,14 +800,15 @@ bte_status bte_load_mode_tables(bte_ctx* c, int32_t ntables, const bte_mode_tabl
 }
 
 bte_status bte_interface_table(const bte_mode_table* A, const bte_mode_table* B, double nx, double ny,
-                               double thickness, double Tref, int64_t* first, int64_t* nentries, int32_t* side,
-                               int32_t* mode, double* cum) {
+                               double thickness_a, double thickness_b, double Tref, int64_t* first,
+                               int64_t* nentries, int32_t* side, int32_t* mode, double* cum) {
     try {
-        if (!A || !B || !first || !nentries || !(thickness > 0.) || !(Tref > 0.)) return BTE_ERR_INPUT;
+        if (!A || !B || !first || !nentries || !(thickness_a > 0.) || !(thickness_b > 0.) || !(Tref > 0.))
+            return BTE_ERR_INPUT;
         const bte::HostModes a = bte::build_modes(A), b = bte::build_modes(B);
         const std::size_t na = a.n();
         const bte::DmmTable D = bte::build_dmm_table(a, 0, b, na, na + b.n(), bte::v2(nx, ny),
-                                                     a.V * thickness / a.c, b.V * thickness / b.c, Tref,
+                                                     a.V * thickness_a / a.c, b.V * thickness_b / b.c, Tref,
                                                      hw_threads());
         for (std::size_t i = 0; i <= na; ++i) first[i] = D.row[i];
         *nentries = (int64_t)D.out.size();
@@ -1576,6 +1588,14 @@ void set_crystal_tables(const bte_ctx* c, DevTables& T) {
     T.dmm_row = crys ? c->d_dmm_row.as<long long>() : nullptr;
     T.dmm_ent = crys ? c->d_dmm_ent.as<DmmEnt>() : nullptr;
     T.crys_off = crys ? c->d_crysoff.as<int>() : nullptr;
+}
+
+double crystal_thickness(const bte_ctx* c, int k) {
+    return c->crys_thick.empty() ? c->geom.thickness : c->crys_thick[std::size_t(k)];
+}
+
+double box_thickness(const bte_ctx* c, int b) {
+    return c->ncrys > 0 ? crystal_thickness(c, c->geom.mat[std::size_t(b)]) : c->geom.thickness;
 }
 
 double box_T0(const bte_ctx* c, int b, double T0) {

@@ -266,9 +266,6 @@ int main(int argc, char** argv) {
             transl.push_back(tx);
             transl.push_back(ty);
         }
-        if (mnames.size() > 1)
-            for (double t : mthick)
-                if (t != mthick[0]) throw std::runtime_error("materials of different thickness are not supported");
         ModesFile mf = read_modes(resolve(base, dbfile));
         bte_ctx* ctx = nullptr;
         bte_device_opts opts{0, 1};
@@ -307,7 +304,8 @@ int main(int argc, char** argv) {
                 t.c_lat = x.c;
                 mts.push_back(t);
             }
-            check(ctx, bte_load_mode_tables(ctx, int32_t(mts.size()), mts.data()), "load mode tables");
+            // each crystal's boxes take its <material thickness> (thicknesses[box])
+            check(ctx, bte_load_mode_tables(ctx, int32_t(mts.size()), mts.data(), mthick.data()), "load mode tables");
         } else {
             check(ctx, bte_load_modes(ctx, &mt), "load modes");
         }

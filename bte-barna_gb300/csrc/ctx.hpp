@@ -83,6 +83,7 @@ struct bte_ctx {
     // concatenation in `modes` (global mode off[k] + j), the rate sets of the
     // materials machinery masked to each crystal, mismatch tables per interface
     int ncrys = 0;
+    std::vector<double> crys_thick;  // per crystal (empty: the geometry's thickness)
     std::vector<bte::HostModes> crys;
     std::vector<std::size_t> crys_off;
     std::vector<bte::PolyPiece> pieces_host;      // the polygon path's pieces (pads: mismatch tables)
@@ -166,6 +167,10 @@ bte_status prepared_grid_run(bte_ctx* c, const bte_rta_params* p, PreparedRun* r
 void fill_static_tables(bte_ctx* c, DevTables& T);
 // The interface tables of several crystals into the kernel tables.
 void set_crystal_tables(const bte_ctx* c, DevTables& T);
+// Thickness of crystal k's boxes (the geometry's without crystal values)
+// and of box b.
+double crystal_thickness(const bte_ctx* c, int k);
+double box_thickness(const bte_ctx* c, int b);
 // The ntime points of the time grid (src/RTA_MC2D.cpp:2118-2124: i * step,
 // the last exactly maxtime) followed by the ntime - 1 bin widths, the
 // layout DevTables::timegrid points to.

@@ -184,7 +184,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
             std::vector<GradGenerators> Gs;
             const std::vector<V2> grad(g.boxes.size(), v2(gx, gy));
             for (int k = 0; k < c->ncrys; ++k) {
-                const GenEmbed e{k, c->crys_off[std::size_t(k)], m.n()};
+                const GenEmbed e{k, c->crys_off[std::size_t(k)], m.n(), crystal_thickness(c, k)};
                 Ws.push_back(build_wall_generators(c->crys[std::size_t(k)], g, false, &e));
                 Gs.push_back(build_gradient_generators_boxes(c->crys[std::size_t(k)], g, grad, &e));
             }
@@ -489,7 +489,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         if (crystals) {
             for (int k = 0; k < c->ncrys; ++k) {
                 cvs.push_back(calc_cv(c->crys[std::size_t(k)], p->T0));
-                vcorrs.push_back(g.thickness / c->crys[std::size_t(k)].c);
+                vcorrs.push_back(crystal_thickness(c, k) / c->crys[std::size_t(k)].c);
             }
         } else {
             cvs.push_back(calc_cv(m, p->T0));
@@ -498,7 +498,7 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
         for (int b = 0; b < nbx; ++b) {
             const std::size_t mk = crystals ? std::size_t(g.mat[std::size_t(b)]) : 0;
             const double cv = cvs[mk], vcorr = vcorrs[mk];
-            const double vbox = g.boxes[size_t(b)].area * g.thickness;
+            const double vbox = g.boxes[size_t(b)].area * box_thickness(c, b);
             const double z = cur[size_t(b)], zx = cur[size_t(nbx) + b], zy = cur[size_t(2) * nbx + b];
             if (out->gz) out->gz[b] = z;
             if (out->gz_jx) out->gz_jx[b] = zx;

@@ -594,7 +594,8 @@ static const std::vector<double>& embed_row(const std::vector<double>& pmf, cons
 Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required, const GenEmbed* e) {
     Generators R;
     const std::size_t n = m.n();
-    const double vuc = m.V * g.thickness / m.c;
+    const double th = e && e->thickness > 0. ? e->thickness : g.thickness;
+    const double vuc = m.V * th / m.c;
     const int nbx = int(g.boxes.size());
     std::vector<double> pmf(n), row;
     for (int s = 0; s < nbx; ++s) {
@@ -647,7 +648,7 @@ Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool
     double total = 0;
     for (auto& W : R.walls) {
         const double Lb = norm(sub(W.sb, W.sa));
-        W.energy = std::fabs(W.flux) * Lb * g.thickness;
+        W.energy = std::fabs(W.flux) * Lb * th;
         total += W.energy;
         ws.push_back(W.energy);
     }
@@ -670,7 +671,8 @@ GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeo
                                                const std::vector<V2>& grad, const GenEmbed* e) {
     GradGenerators R;
     const std::size_t n = m.n();
-    const double vuc = m.V * g.thickness / m.c;
+    const double th = e && e->thickness > 0. ? e->thickness : g.thickness;
+    const double vuc = m.V * th / m.c;
     std::vector<double> pmf(n), row;
     std::vector<signed char> sg(n);
     for (std::size_t s = 0; s < g.boxes.size(); ++s) {
@@ -692,7 +694,7 @@ GradGenerators build_gradient_generators_boxes(const HostModes& m, const HostGeo
             }
         }
         const double cumulsum = kB * std::accumulate(pmf.begin(), pmf.end(), 0.);
-        const double vol = g.boxes[s].area * g.thickness / vuc;
+        const double vol = g.boxes[s].area * th / vuc;
         R.box.push_back(int(s));
         R.energy.push_back(vol * cumulsum / double(m.nq));
         const std::vector<double>& rw = embed_row(pmf, e, row);
@@ -884,7 +886,8 @@ TranslationFast build_translation_fast(const HostGeometry& g, double margin) {
 Generators build_initial_generators(const HostModes& m, const HostGeometry& g, const GenEmbed* e) {
     Generators R;
     const std::size_t n = m.n();
-    const double vuc = m.V * g.thickness / m.c;
+    const double th = e && e->thickness > 0. ? e->thickness : g.thickness;
+    const double vuc = m.V * th / m.c;
     std::vector<double> pmf(n), row;
     for (std::size_t s = 0; s < g.boxes.size(); ++s) {
         if (g.reservoir[s] || g.tto[s] >= 0) continue;
@@ -899,7 +902,7 @@ Generators build_initial_generators(const HostModes& m, const HostGeometry& g, c
                          : om * std::fabs(bose_einstein(om, Tr) - bose_einstein(om, Te));
         }
         const double cumulsum = 1.0e+12 * hbar * std::accumulate(pmf.begin(), pmf.end(), 0.);
-        const double vol = g.boxes[s].area * g.thickness / vuc;
+        const double vol = g.boxes[s].area * th / vuc;
         R.init_box.push_back(int(s));
         R.init_sign.push_back((Tr - Te) >= 0 ? 1 : -1);
         R.init_energy.push_back(vol * cumulsum / double(m.nq));

@@ -135,6 +135,7 @@ LambertTable build_lambert(const HostModes& m, const HostGeometry& g, int nthrea
 struct GenEmbed {
     int mat;
     std::size_t off, n;
+    double thickness = 0.;  // of the crystal's boxes (0: the geometry's)
 };
 Generators build_wall_generators(const HostModes& m, const HostGeometry& g, bool required = true,
                                  const GenEmbed* e = nullptr);

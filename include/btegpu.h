@@ -351,13 +351,18 @@ bte_status bte_load_materials(bte_ctx* ctx, int32_t nmat, const double* w, const
  * box that meets it.  Replaces bte_load_modes and any rate sets of
  * bte_load_materials; reservoirs inject into their own crystal only
  * (BTE_ERR_INPUT "Injection from material A to B is not allowed").
- * Production transient runs on the convex-polygon kernel; the layer
- * coupling of LDMM is not available (it needs the modes' eigenvectors and a
- * layer description the mode tables do not carry). */
-bte_status bte_load_mode_tables(bte_ctx* ctx, int32_t ntables, const bte_mode_table* tables);
+ * thickness: each crystal's <material thickness> (nm), the thickness of
+ * its boxes (the reference's thicknesses[box]); NULL: the geometry's
+ * thickness for every crystal.  Transient and steady runs, replay and
+ * production; the layer coupling of LDMM is not available (it needs the
+ * modes' eigenvectors and a layer description the mode tables do not
+ * carry). */
+bte_status bte_load_mode_tables(bte_ctx* ctx, int32_t ntables, const bte_mode_table* tables,
+                                const double* thickness);
 
 /* The diffuse mismatch table of the interface from table A to table B
- * (normal (nx, ny) pointing from A to B, material thickness, Tref), built on
+ * (normal (nx, ny) pointing from A to B, the thicknesses of A's and B's
+ * boxes, Tref), built on
  * the host (no device needed): for incident mode i of A (v.n > 0), entries
  * [first[i], first[i+1]) of (side out: 0 = A, 1 = B; mode out in that
  * side's table; cumulative probability over A's incident modes).  first
@@ -365,8 +370,8 @@ bte_status bte_load_mode_tables(bte_ctx* ctx, int32_t ntables, const bte_mode_ta
  * *nentries are filled.  The reference records the closest-frequency
  * reflection of an incident mode without a transition with side B; kept. */
 bte_status bte_interface_table(const bte_mode_table* A, const bte_mode_table* B, double nx, double ny,
-                               double thickness, double Tref, int64_t* first, int64_t* nentries,
-                               int32_t* side, int32_t* mode, double* cum);
+                               double thickness_a, double thickness_b, double Tref, int64_t* first,
+                               int64_t* nentries, int32_t* side, int32_t* mode, double* cum);
 
 /* Run the RTA particle loop for one run and fill `out` (replaces one
  * iteration of the run loop of src/RTA_MC2D.cpp:2188-2543: generation,

@@ -71,7 +71,8 @@ def load():
                                       C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult)]
     lib.oracle_steady_run.restype = C.c_int
     lib.oracle_steady_run_multi.argtypes = [C.POINTER(_bt.ModeTable), C.c_int, C.POINTER(_bt.Geometry),
-                                            C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult)]
+                                            C.POINTER(_bt.SteadyParams), C.c_int, C.POINTER(_bt.SteadyResult),
+                                            C.POINTER(C.c_double)]
     lib.oracle_steady_run_multi.restype = C.c_int
     lib.oracle_pcg64.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int]
@@ -114,7 +115,7 @@ def load():
     lib.oracle_kat_gradientT.argtypes = [mtp, C.POINTER(_bt.Geometry), dp]
     lib.oracle_kat_gradientT.restype = C.c_int
     lib.oracle_rta_run_multi.argtypes = [mtp, C.c_int, C.POINTER(_bt.Geometry), C.POINTER(_bt.RtaParams), C.c_int,
-                                         C.POINTER(_bt.RtaResult), lp]
+                                         C.POINTER(_bt.RtaResult), lp, dp]
     lib.oracle_rta_run_multi.restype = C.c_int
     lib.oracle_kat_dmm.argtypes = [mtp, mtp, C.c_double, C.c_double, C.c_double, C.c_double, lp, lp, lp,
                                    ip, lp, dp]
@@ -178,7 +179,7 @@ def steady_run(case: dict, gradient, N=None, seed=1, nthreads=8, eps_energy=-42.
 
 
 def steady_run_multi(tables, geom, T0, gradient, N, seed=1, nthreads=8, eps_energy=-42.0, eps_flux=-42.0,
-                     max_generations=0, specularity=0.0):
+                     max_generations=0, specularity=0.0, thickness=None):
     """Steady state of a geometry of several crystals with their own mode
     tables (box b in crystal geom["material"][b]), diffuse mismatch at their
     contacts."""
@@ -191,8 +192,11 @@ def steady_run_multi(tables, geom, T0, gradient, N, seed=1, nthreads=8, eps_ener
         keep.append(k)
     gs, k2 = _bt.geom_struct(geom)
 
+    th, thp = _thickness_arg(thickness, len(tables))
+
     def call(p, r):
-        st = lib.oracle_steady_run_multi(arr, len(tables), C.byref(gs), C.byref(p), int(nthreads), C.byref(r))
+        st = lib.oracle_steady_run_multi(arr, len(tables), C.byref(gs), C.byref(p), int(nthreads), C.byref(r),
+                                         thp)
         if st != 0:
             raise _bt.BteError(st, lib.oracle_last_error().decode())
     return _bt.steady_call(call, int(geom["nboxes"]), T0, gradient, N, seed, _bt.MODE_REPLAY, eps_energy,
@@ -450,10 +454,20 @@ def rta_run(case: dict, N=None, seed=1, nthreads=1, log_impl=0, begin=0, end=0, 
     return out
 
 
+def _thickness_arg(thickness, n):
+    if thickness is None:
+        return None, None
+    th = np.ascontiguousarray(np.asarray(thickness, dtype=float))
+    if th.size != n:
+        raise ValueError("one thickness per mode table")
+    return th, th.ctypes.data_as(C.POINTER(C.c_double))
+
+
 def rta_run_multi(tables, geom, T0, dt, maxtime, N, seed=1, nthreads=8, source=None, specularity=0.0,
-                  ballistic=False, begin=0, end=0):
+                  ballistic=False, begin=0, end=0, thickness=None):
     """A geometry of several materials with their own mode tables (box b in
-    material geom["material"][b]), diffuse mismatch at their contacts."""
+    material geom["material"][b]), diffuse mismatch at their contacts.
+    `thickness`: each material's thickness (None: the geometry's)."""
     if source is None:
         source = _bt.SOURCE_WALLS
     lib = load()
@@ -474,8 +488,9 @@ def rta_run_multi(tables, geom, T0, dt, maxtime, N, seed=1, nthreads=8, source=N
     out["exact"] = np.zeros(shape + (3, 2), dtype=np.int64)
     r.exact = out["exact"].ctypes.data_as(C.POINTER(C.c_int64))
     cnt = np.zeros(9, dtype=np.int64)
+    th, thp = _thickness_arg(thickness, len(tables))
     st = lib.oracle_rta_run_multi(arr, len(tables), C.byref(gs), C.byref(p), int(nthreads), C.byref(r),
-                                  cnt.ctypes.data_as(C.POINTER(C.c_longlong)))
+                                  cnt.ctypes.data_as(C.POINTER(C.c_longlong)), thp)
     if st != 0:
         raise _bt.BteError(st, lib.oracle_last_error().decode())
     out.update(Eeff=r.Eeff, energy_rate=r.energy_rate, events=int(cnt[0]), wall_hits=int(cnt[1]),

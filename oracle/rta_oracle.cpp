@@ -1506,7 +1506,8 @@ inline void build_interfaces(MultiSim& M, double scalebroad = 0.1) {
             if (M.dmm.tab.count(key)) continue;
             const Modes& A = M.mats[std::size_t(a.mat)].m;
             const Modes& B = M.mats[std::size_t(b.mat)].m;
-            const double VA = A.V * S0.thickness / A.c, VB = B.V * S0.thickness / B.c;
+            const double VA = A.V * M.mats[std::size_t(a.mat)].thickness / A.c;
+            const double VB = B.V * M.mats[std::size_t(b.mat)].thickness / B.c;
             M.dmm.tab.emplace(key, build_dmm(A, B, VA, VB, nw, scalebroad, a.Teq));
         }
     }
@@ -3047,11 +3048,13 @@ int oracle_rta_run_mat(const bte_mode_table* mt, const bte_geometry* gm, int nma
 // stream).  counters: events, wall_hits, crossings, absorbed, nudges,
 // quirks, loop microseconds, interface hits, interface transmissions.
 int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry* gm, const bte_rta_params* rp,
-                         int nthreads, bte_rta_result* out, int64_t* counters) {
+                         int nthreads, bte_rta_result* out, int64_t* counters, const double* thickness) {
     try {
         if (nmat < 1 || !gm->material) return fail(BTE_ERR_INPUT, "materials need mode tables and box materials");
         orc::MultiSim M;
         for (int k = 0; k < nmat; ++k) M.mats.push_back(build_sim(&mts[k], gm));
+        if (thickness)  // each material's boxes at its own thickness (thicknesses[box])
+            for (int k = 0; k < nmat; ++k) M.mats[std::size_t(k)].thickness = thickness[k];
         for (auto& b : M.mats[0].sys)
             if (b.mat < 0 || b.mat >= nmat) return fail(BTE_ERR_INPUT, "box material out of range");
         std::size_t ntime = std::size_t(std::floor(rp->maxtime / rp->dt + 1.0e-6)) + 1;
@@ -3182,7 +3185,7 @@ int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry
         const orc::Sim& S0 = M.mats[0];
         std::vector<double> gz = T.gz, jx = T.jx, jy = T.jy;
         for (std::size_t ir = 0; ir < nbx; ++ir) {
-            const double vbox = S0.sys[ir].area * S0.thickness;
+            const double vbox = S0.sys[ir].area * M.mats[std::size_t(S0.sys[ir].mat)].thickness;
             for (std::size_t i = 0; i < nbn; ++i) {
                 gz[ir * nbn + i] = gz[ir * nbn + i] / vbox * M.Eeff;
                 jx[ir * nbn + i] = jx[ir * nbn + i] / vbox * (M.Eeff * 1e12 * 1e9 * 1e9);
@@ -3209,7 +3212,7 @@ int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry
                 double cv = 0.;
                 for (std::size_t k = 0; k < m.n(); ++k) cv += orc::bose_einstein_kernel(m.omega[k], rp->T0);
                 cv = cv * orc::kB / double(m.nq) / m.V;
-                const double vcorr = S0.thickness / m.c;
+                const double vcorr = M.mats[std::size_t(S0.sys[ir].mat)].thickness / m.c;
                 for (std::size_t i = 0; i < nbn; ++i)
                     out->temperature[ir * nbn + i] = gz[ir * nbn + i] / (cv / vcorr) + rp->T0;
             }
@@ -3323,8 +3326,9 @@ int steady_core(std::vector<orc::Sim>& mats, const orc::DmmSet* dmm, const bte_s
             // generators; gradient sources in ascending box order
             std::vector<double> e;
             for (auto& r : SG.wall) {
-                const orc::WallGen& G = mats[std::size_t(r.first)].gens[r.second];
-                e.push_back(std::fabs(G.flux) * orc::norm(G.b.p2 - G.b.p1) * S.thickness);
+                const orc::Sim& Sr = mats[std::size_t(r.first)];
+                const orc::WallGen& G = Sr.gens[r.second];
+                e.push_back(std::fabs(G.flux) * orc::norm(G.b.p2 - G.b.p1) * Sr.thickness);
             }
             for (double x : e) E0 += x;
             double c = 0.;
@@ -3554,10 +3558,10 @@ int steady_core(std::vector<orc::Sim>& mats, const orc::DmmSet* dmm, const bte_s
             double cv = 0.;
             for (std::size_t k = 0; k < Sk.m.n(); ++k) cv += orc::bose_einstein_kernel(Sk.m.omega[k], sp->T0);
             cvs.push_back(cv * orc::kB / double(Sk.m.nq) / Sk.m.V);
-            vcorrs.push_back(S.thickness / Sk.m.c);
+            vcorrs.push_back(Sk.thickness / Sk.m.c);
         }
         for (std::size_t b = 0; b < nbx; ++b) {
-            const double vbox = S.sys[b].area * S.thickness;
+            const double vbox = S.sys[b].area * mats[mat_of(b)].thickness;
             const double z = cur[b], zx = cur[nbx + b], zy = cur[2 * nbx + b];
             if (out->gz) out->gz[b] = z;
             if (out->gz_jx) out->gz_jx[b] = zx;
@@ -3602,12 +3606,15 @@ int oracle_steady_run(const bte_mode_table* mt, const bte_geometry* gm, const bt
 // src/RTA_MC2D.cpp:1672-1689, 1751-1779: the re-emitted particle is carried
 // into the next generation).
 int oracle_steady_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry* gm,
-                            const bte_steady_params* sp, int nthreads, bte_steady_result* out) {
+                            const bte_steady_params* sp, int nthreads, bte_steady_result* out,
+                            const double* thickness) {
     try {
         if (nmat < 1 || !gm->material) return fail(BTE_ERR_INPUT, "materials need mode tables and box materials");
         if (!g_spec_boxes.empty()) return fail(BTE_ERR_INPUT, "spectral outputs need one crystal");
         orc::MultiSim M;
         for (int k = 0; k < nmat; ++k) M.mats.push_back(build_sim(&mts[k], gm));
+        if (thickness)
+            for (int k = 0; k < nmat; ++k) M.mats[std::size_t(k)].thickness = thickness[k];
         for (auto& b : M.mats[0].sys)
             if (b.mat < 0 || b.mat >= nmat) return fail(BTE_ERR_INPUT, "box material out of range");
         orc::build_interfaces(M);

@@ -40,6 +40,37 @@ def test_engine_interface_tables_equal_the_restatement(built, normal):
                  pyoracle.dmm_table(A2, B2, normal, 0.335, 280.0)[0])
 
 
+def test_interface_table_takes_each_crystals_thickness(built):
+    """The cell volume of a side enters its table as V thickness / c, so
+    B's boxes twice as thick give the table of B with twice its cell
+    volume."""
+    A, B = _tables()
+    B2 = dict(B)
+    B2["V"] = 2.0 * B["V"]
+    for normal in ((1.0, 0.0), (0.6, -0.8)):
+        a = btegpu.interface_table(A, B, normal, (0.335, 0.67), 300.0)
+        b = btegpu.interface_table(A, B2, normal, 0.335, 300.0)
+        assert _same(a, b)
+        assert not _same(a, btegpu.interface_table(A, B, normal, 0.335, 300.0))
+
+
+def test_restatement_thickness_per_material():
+    """Each material's boxes at its own thickness: equal thicknesses repeat
+    the run without them draw for draw; another thickness for one crystal
+    changes the interface tables (and the boxes' volumes)."""
+    A, B = _tables()
+    g = _two_crystal_ribbon()
+    kw = dict(T0=300.0, dt=10.0, maxtime=100.0, N=3000, seed=4, nthreads=4)
+    a = pyoracle.rta_run_multi([A, B], g, **kw)
+    b = pyoracle.rta_run_multi([A, B], g, thickness=[0.335, 0.335], **kw)
+    assert np.array_equal(a["exact"], b["exact"]) and a["Eeff"] == b["Eeff"]
+    c = pyoracle.rta_run_multi([A, B], g, thickness=[0.335, 0.67], **kw)
+    # a wall's energy |flux| L t does not depend on t (the flux goes as
+    # 1 / t through the unit-cell volume); the interface's tables do
+    assert c["Eeff"] == a["Eeff"]
+    assert not np.array_equal(a["exact"], c["exact"])
+
+
 def _two_crystal_ribbon():
     g = synth.ribbon_geometry(200.0, 50.0, 10, T_hot=301.0, T_cold=299.0)
     g["material"] = np.array([0] * 5 + [1] * 5 + [0, 1], dtype=np.int32)

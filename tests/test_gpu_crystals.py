@@ -84,8 +84,9 @@ def _closed_block():
     return g
 
 
-@pytest.mark.parametrize("source", ["walls", "initial"])
-def test_two_crystals_replay_is_bit_exact(engine, source):
+@pytest.mark.parametrize("source,thickness", [("walls", None), ("initial", None), ("walls", (0.335, 0.5)),
+                                              ("initial", (0.6, 0.335))])
+def test_two_crystals_replay_is_bit_exact(engine, source, thickness):
     """Replay mode (pcg64 streams, CDF inversion, the interface drawing its
     re-emission from the particle's stream as the restatement does)
     reproduces the restatement's multi-crystal run draw for draw: identical
@@ -96,16 +97,20 @@ def test_two_crystals_replay_is_bit_exact(engine, source):
         g, src, N = _ribbon(), btegpu.SOURCE_WALLS, 4000
     else:
         g, src, N = _closed_block(), btegpu.SOURCE_INITIAL, 4000
-    engine.load_mode_tables([A, B])
+    engine.load_mode_tables([A, B], thickness=thickness)
     engine.load_geometry(g)
     kw = dict(T0=300.0, dt=10.0, maxtime=200.0)
     r = engine.rta_run(N=N, seed=5, mode=btegpu.MODE_REPLAY, source=src, exact=True, **kw)
-    o = pyoracle.rta_run_multi([A, B], g, N=N, seed=5, nthreads=16, source=src, **kw)
+    o = pyoracle.rta_run_multi([A, B], g, N=N, seed=5, nthreads=16, source=src, thickness=thickness, **kw)
     assert r["interface_hits"] > 0 and 0 < r["interface_transmissions"] < r["interface_hits"]
     for k in ("events", "wall_hits", "crossings", "absorbed", "interface_hits", "interface_transmissions"):
         assert r[k] == o[k], (k, r[k], o[k])
     assert np.array_equal(r["exact"], o["exact"])
     assert r["Eeff"] == o["Eeff"]
+    # the outputs: each box's volume and C_v correction at its crystal's thickness
+    rr = engine.rta_run(N=N, seed=5, mode=btegpu.MODE_REPLAY, source=src, **kw)
+    assert np.allclose(rr["temperature"], o["temperature"], rtol=0, atol=1e-12 * 300.0)
+    assert np.allclose(rr["jx"], o["jx"], rtol=1e-12, atol=1e-12 * np.abs(o["jx"]).max())
 
 
 def test_two_crystals_general_kernel_agrees_with_restatement(engine):
@@ -179,15 +184,17 @@ def test_two_crystal_steady_state_agrees_with_restatement(engine):
 
 
 def test_two_crystal_steady_replay_is_bit_exact(engine):
-    """The steady state of the layered bar in replay mode against the
-    restatement's steady run over several materials: every generation, its
-    128-bit tallies and the counters, interface re-emissions included."""
+    """The steady state of the layered bar (its crystals 0.335 and 0.45 nm
+    thick) in replay mode against the restatement's steady run over several
+    materials: every generation, its 128-bit tallies and the counters,
+    interface re-emissions included, and the temperatures."""
     A, B = _tables()
     g = synth.layered_bar_geometry()
-    engine.load_mode_tables([A, B])
+    engine.load_mode_tables([A, B], thickness=(0.335, 0.45))
     engine.load_geometry(g)
     r = engine.steady_run(300.0, (0.0, -0.01), 3000, seed=6, mode=btegpu.MODE_REPLAY)
-    o = pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), 3000, seed=6, nthreads=16)
+    o = pyoracle.steady_run_multi([A, B], g, 300.0, (0.0, -0.01), 3000, seed=6, nthreads=16,
+                                  thickness=(0.335, 0.45))
     assert r["generations"] == o["generations"] > 1
     assert r["interface_hits"] > 0
     for k in ("events", "wall_hits", "crossings", "absorbed", "translations", "scattered", "births", "lost",
@@ -196,12 +203,13 @@ def test_two_crystal_steady_replay_is_bit_exact(engine):
     assert np.array_equal(r["exact"], o["exact"])
     assert np.array_equal(r["log"], o["log"])
     assert r["Eeff"] == o["Eeff"]
+    assert np.abs(r["temperature"] - o["temperature"]).max() <= 1e-12 * 300.0
 
 
 def test_rtamc2d_cli_reads_several_materials(built, tmp_path):
-    """rtamc2d_gpu with two <material>s and boxes naming theirs in
-    <MaterialID> runs the crystals path: the CSV's late temperatures step
-    down at the interface."""
+    """rtamc2d_gpu with two <material>s of different thickness and boxes
+    naming theirs in <MaterialID> runs the crystals path: the CSV's late
+    temperatures step down at the interface."""
     A, B = _tables()
     g = _ribbon()
     synth.write_geometry_xml(str(tmp_path / "beam.xml"), g, material="mat")
@@ -210,7 +218,7 @@ def test_rtamc2d_cli_reads_several_materials(built, tmp_path):
     (tmp_path / "input.xml").write_text(
         '<RTA_MC2d>\n  <geometry file="beam.xml"/>\n  <time dt="10" maxtime="200"/>\n'
         '  <material name="mat0" database="a.bin" thickness="0.335" T0="300.0"/>\n'
-        '  <material name="mat1" database="b.bin" thickness="0.335" T0="300.0"/>\n'
+        '  <material name="mat1" database="b.bin" thickness="0.5" T0="300.0"/>\n'
         '  <particles N="20000"/>\n  <engine seed="5"/>\n</RTA_MC2d>\n')
     exe = os.path.join(os.path.dirname(built), "rtamc2d_gpu")
     r = subprocess.run([exe, "input.xml", "4", "1"], cwd=tmp_path, capture_output=True, text=True)
