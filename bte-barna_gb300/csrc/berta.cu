@@ -252,7 +252,6 @@ struct AdvectArgs {
 // Draws of the geometric choices of one particle's advection.
 struct BePol {
     Philox g;
-    __device__ double u() { return g.uniform(); }
     __device__ int choose(int n) { return uniform_below(g, uint32_t(n)); }
 };
 
