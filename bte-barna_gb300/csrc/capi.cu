@@ -506,7 +506,6 @@ void prepare_run(bte_ctx* c, const bte_rta_params* p) {
     ck(cudaSetDevice(c->device), "cudaSetDevice");
     if (c->ncrys > 0) {
         // crystals joined by mismatch interfaces: every crystal at the run's T0
-        if (!c->spec_boxes.empty()) throw Error(BTE_ERR_INPUT, "spectral outputs need one crystal");
         if (c->mat_T0.empty() || c->mat_T0[0] != p->T0) {
             c->mat_T0.assign(std::size_t(c->ncrys), p->T0);
             c->resample_T0 = -1;
@@ -899,59 +898,78 @@ bte_status bte_get_spectral(bte_ctx* c, bte_spectral_result* out) {
     if (!c || !out) return BTE_ERR_INPUT;
     try {
         if (!c->spec_valid) throw Error(BTE_ERR_STATE, "no run with spectral locations yet");
-        const bte::HostModes& m = c->modes;
         const bte::HostGeometry& g = c->geom;
-        const std::size_t n = m.n(), nb = std::size_t(m.nb), nq = std::size_t(m.nq);
+        const std::size_t n = c->modes.n();  // global modes (the crystals' one after the other)
         const std::size_t nloc = c->spec_boxes.size(), nbins = std::size_t(c->spec_nbins);
         const std::size_t nw = std::size_t(c->spec_nomega);
+        // each location's crystal (the reference takes the location's
+        // material's grid, :1987-2048): its modes and their first global index
+        auto crystal_of = [&](std::size_t l) -> int {
+            return c->ncrys > 0 ? g.mat[std::size_t(c->spec_boxes[l])] : -1;
+        };
+        auto modes_of = [&](int k) -> const bte::HostModes& {
+            return k >= 0 ? c->crys[std::size_t(k)] : c->modes;
+        };
+        const bte::HostModes& m0 = modes_of(nloc > 0 ? crystal_of(0) : -1);
+        const std::size_t nq = std::size_t(m0.nq);
+        for (std::size_t l = 1; l < nloc; ++l) {
+            const bte::HostModes& ml = modes_of(crystal_of(l));
+            if (ml.nq != m0.nq || ml.grid[0] != m0.grid[0] || ml.grid[1] != m0.grid[1])
+                throw Error(BTE_ERR_INPUT, "spectral locations in crystals of different q grids");
+        }
         out->nloc = int32_t(nloc);
         out->nbins = int32_t(nbins);
         out->nomega = int32_t(nw);
         out->nq = int32_t(nq);
-        // omega ticks: LinSpaced(nomega, 0, max omega) + delta/2 (:2041-2045)
-        double maxw = 0.;
-        for (double w : m.omega) maxw = std::max(maxw, w);
-        std::vector<double> grid(nw);
-        for (std::size_t i = 0; i < nw; ++i)
-            grid[i] = (nw > 1 ? maxw * double(i) / double(nw - 1) : 0.) + 0.5 * maxw / double(nw);
-        if (out->omega)
-            for (std::size_t l = 0; l < nloc; ++l) std::copy(grid.begin(), grid.end(), out->omega + l * nw);
-        // Gamma pdf of every mode over the ticks, shape k = w^2 / sigma,
-        // scale theta = sigma / w (gamma_pdf, :61-63), kept where it is not
-        // negligible
-        const std::vector<double> sig = bte::mode_sigmas(m);
-        std::vector<std::vector<std::pair<int, double>>> gw(n);
-        for (std::size_t k = 0; k < n; ++k) {
-            const double w = m.omega[k];
-            if (!(w > 0.)) continue;
-            const double kk = w * w / sig[k], th = sig[k] / w;
-            const double lg = std::lgamma(kk);
-            for (std::size_t i = 0; i < nw; ++i) {
-                const double x = grid[i] / th;
-                const double lp = (kk - 1.0) * std::log(x) - x - lg - std::log(th);
-                if (lp > -700.) {
-                    const double pdf = std::exp(lp);
-                    if (pdf > 0.) gw[k].emplace_back(int(i), pdf);
-                }
-            }
-        }
-        const double vcorr = g.thickness / m.c;
         const double hbar = 1.054571726e-34;
         for (std::size_t l = 0; l < nloc; ++l) {
+            const int kc = crystal_of(l);
+            const bte::HostModes& m = modes_of(kc);
+            const std::size_t off = kc >= 0 ? c->crys_off[std::size_t(kc)] : 0, nk = m.n();
+            const std::size_t nb = std::size_t(m.nb);
+            // omega ticks of the location's crystal: LinSpaced(nomega, 0,
+            // max omega) + delta/2 (:2041-2045)
+            double maxw = 0.;
+            for (double w : m.omega) maxw = std::max(maxw, w);
+            std::vector<double> grid(nw);
+            for (std::size_t i = 0; i < nw; ++i)
+                grid[i] = (nw > 1 ? maxw * double(i) / double(nw - 1) : 0.) + 0.5 * maxw / double(nw);
+            if (out->omega) std::copy(grid.begin(), grid.end(), out->omega + l * nw);
+            // Gamma pdf of every mode over the ticks, shape k = w^2 / sigma,
+            // scale theta = sigma / w (gamma_pdf, :61-63), kept where it is not
+            // negligible
+            const std::vector<double> sig = bte::mode_sigmas(m);
+            std::vector<std::vector<std::pair<int, double>>> gw(nk);
+            for (std::size_t k = 0; k < nk; ++k) {
+                const double w = m.omega[k];
+                if (!(w > 0.)) continue;
+                const double kk = w * w / sig[k], th = sig[k] / w;
+                const double lg = std::lgamma(kk);
+                for (std::size_t i = 0; i < nw; ++i) {
+                    const double x = grid[i] / th;
+                    const double lp = (kk - 1.0) * std::log(x) - x - lg - std::log(th);
+                    if (lp > -700.) {
+                        const double pdf = std::exp(lp);
+                        if (pdf > 0.) gw[k].emplace_back(int(i), pdf);
+                    }
+                }
+            }
             const int box = c->spec_boxes[l];
-            const double vbox = g.boxes[std::size_t(box)].area * g.thickness;
+            const double tb = bte::box_thickness(c, box);
+            const double vcorr = tb / m.c;
+            const double vbox = g.boxes[std::size_t(box)].area * tb;
             const double T0b = bte::box_T0(c, box, c->spec_T0);
             const double cv = bte::calc_cv(m, T0b);
             const double Eeff = c->spec_Eeff;
             std::vector<double> dT(nbins * nw, 0.), jx(nbins * nw, 0.), jy(nbins * nw, 0.), fq(nbins * nq, 0.);
             const bool steady = c->spec_steady;
             for (std::size_t b = 0; b < nbins; ++b) {
-                const double* Tm = c->spec_raw.data() + (l * nbins + b) * n;
-                for (std::size_t k = 0; k < n; ++k) {
+                const double* Tm = c->spec_raw.data() + (l * nbins + b) * n + off;
+                for (std::size_t k = 0; k < nk; ++k) {
                     const double t = Tm[k];
                     // fd_qmesh: time / omega (transient, :757), sign / omega
                     // per segment (steady, :829)
-                    const double f = steady ? double(c->spec_cnt[l * n + k]) : t;
+                    const double f = steady ? double(c->spec_cnt[l * n + off + k]) : t;
                     if (f != 0. && m.omega[k] > 0.) fq[b * nq + k / nb] += f / m.omega[k];
                     if (t == 0.) continue;
                     for (auto& [i, wgt] : gw[k]) {
@@ -989,6 +1007,7 @@ bte_status bte_get_spectral(bte_ctx* c, bte_spectral_result* out) {
         if (out->q1bz) {
             // q points in Cartesian coordinates, reduced coordinates wrapped
             // to [-1/2, 1/2) (a Gamma-centred n1 x n2 grid, iq = i n2 + j)
+            const bte::HostModes& m = m0;
             const int n1 = m.grid[0] > 0 ? m.grid[0] : 1, n2 = m.grid[1] > 0 ? m.grid[1] : 1;
             for (std::size_t iq = 0; iq < nq; ++iq) {
                 const int i = int(iq) / n2, j = int(iq) % n2;

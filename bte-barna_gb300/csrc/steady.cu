@@ -156,7 +156,6 @@ bte_status bte_steady_run(bte_ctx* c, const bte_steady_params* p, bte_steady_res
             throw Error(BTE_ERR_INPUT, "specularity must be in [0, 1]");
         if (crystals) {
             // crystals joined by mismatch interfaces, every crystal at T0
-            if (!c->spec_boxes.empty()) throw Error(BTE_ERR_INPUT, "spectral outputs need one crystal");
             if (c->mat_T0.empty() || c->mat_T0[0] != p->T0) {
                 c->mat_T0.assign(std::size_t(c->ncrys), p->T0);
                 c->resample_T0 = -1;

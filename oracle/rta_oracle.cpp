@@ -605,6 +605,9 @@ struct Sim {
     Modes m;
     std::vector<Box> sys;
     double thickness = 0;
+    // first global mode of this material's table (several materials: their
+    // tables one after the other, as the spectral tallies index them)
+    std::size_t mode_off = 0;
     // run state
     std::vector<double> timegrid;
     std::vector<double> resample_cdf;
@@ -844,7 +847,7 @@ inline void process_segment(const Sim& S, Tally& T, std::size_t ibox, double t0,
         T.ex[3 * k + 2] += quant(v.y * contr);
         // per-mode time at a spectral location (the gamma weights, v and
         // 1/omega of the reference's sd tallies are linear in it)
-        if (lc >= 0) T.spec[(std::size_t(lc) * T.nbins + i) * T.nmodes + mode] += quant(contr);
+        if (lc >= 0) T.spec[(std::size_t(lc) * T.nbins + i) * T.nmodes + S.mode_off + mode] += quant(contr);
     }
 }
 
@@ -1829,7 +1832,7 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
     if (box.inside(rnew)) {
         p.pos = rnew;
         p.t += dt;
-        process_segment_steady(T, p.box, p.sign, dt, v, p.q * nb + p.alpha);  // evalphi: phi += sign
+        process_segment_steady(T, p.box, p.sign, dt, v, S.mode_off + p.q * nb + p.alpha);  // evalphi: phi += sign
         dt = 0.;
         fate = F_SCATTER;
         return;
@@ -1861,7 +1864,7 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
             pboxes.push_back(test);
     }
     if (pboxes.empty()) {
-        process_segment_steady(T, p.box, p.sign, tf, v, p.q * nb + p.alpha);
+        process_segment_steady(T, p.box, p.sign, tf, v, S.mode_off + p.q * nb + p.alpha);
         p.t += tf;
         std::vector<std::size_t> ids;
         for (auto& g : S.sys)
@@ -1918,7 +1921,7 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
     } else if (pboxes.size() == 1) {
         p.pos = rnew;
         p.t += tf;
-        process_segment_steady(T, p.box, p.sign, tf, v, p.q * nb + p.alpha);
+        process_segment_steady(T, p.box, p.sign, tf, v, S.mode_off + p.q * nb + p.alpha);
         if (dmm && S.sys[pboxes[0]].mat != S.sys[p.box].mat) {
             dmm_cross(S, *dmm, p, pboxes[0], dt, rng, T);
             fate = F_BOUNCE;
@@ -1928,7 +1931,7 @@ inline void evolparticle_steady(const Sim& S, Particle& p, V2 v, double& dt, Pcg
         T.crossings++;
         return;
     } else {
-        process_segment_steady(T, p.box, p.sign, tf, v, p.q * nb + p.alpha);
+        process_segment_steady(T, p.box, p.sign, tf, v, S.mode_off + p.q * nb + p.alpha);
         p.t += tf;
         p.pos = rnew;
         std::vector<std::size_t> pbox2;
@@ -3067,6 +3070,11 @@ int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry
             orc::build_lambert(S);
         }
         orc::build_interfaces(M);
+        std::size_t ntot = 0;  // the materials' modes one after the other
+        for (auto& S : M.mats) {
+            S.mode_off = ntot;
+            ntot += S.m.n();
+        }
         int64_t total_particles = rp->nparticles;
         if (rp->source == BTE_SOURCE_WALLS) {
             std::vector<double> e;
@@ -3103,9 +3111,16 @@ int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry
         std::vector<orc::Tally> tl(static_cast<std::size_t>(nthreads));
         std::vector<std::string> errs(static_cast<std::size_t>(nthreads));
         std::vector<int> codes(static_cast<std::size_t>(nthreads), 0);
+        std::vector<int> locs(nbx, -1);
+        for (std::size_t q = 0; q < g_spec_boxes.size(); ++q) locs[std::size_t(g_spec_boxes[q])] = int(q);
         auto work = [&](int tid) {
             orc::Tally& T = tl[std::size_t(tid)];
             T.init(nbx, nbn);
+            if (!g_spec_boxes.empty()) {
+                T.loc = &locs;
+                T.nmodes = ntot;
+                T.spec.assign(g_spec_boxes.size() * nbn * ntot, 0);
+            }
             const int64_t n = end - begin;
             const int64_t lo = begin + n * tid / nthreads, hi = begin + n * (tid + 1) / nthreads;
             try {
@@ -3152,7 +3167,9 @@ int oracle_rta_run_multi(const bte_mode_table* mts, int nmat, const bte_geometry
             T.translations += tl[t].translations;
             T.interface_hits += tl[t].interface_hits;
             T.interface_transmissions += tl[t].interface_transmissions;
+            for (std::size_t k = 0; k < T.spec.size(); ++k) T.spec[k] += tl[t].spec[k];
         }
+        g_spec_last = T.spec;
         // the exact 128-bit sums, as the replay kernels keep them
         if (out->exact)
             for (std::size_t k = 0; k < T.ex.size(); ++k) {
@@ -3361,7 +3378,12 @@ int steady_core(std::vector<orc::Sim>& mats, const orc::DmmSet* dmm, const bte_s
         // spectral locations: per-mode time and segment counts over all generations
         std::vector<int> locs(nbx, -1);
         for (std::size_t i = 0; i < g_spec_boxes.size(); ++i) locs[std::size_t(g_spec_boxes[i])] = int(i);
-        const std::size_t nspec = g_spec_boxes.size() * S.m.n();
+        std::size_t ntot = 0;  // the materials' modes one after the other
+        for (auto& Sk : mats) {
+            Sk.mode_off = ntot;
+            ntot += Sk.m.n();
+        }
+        const std::size_t nspec = g_spec_boxes.size() * ntot;
         std::vector<__int128> spec_tot(nspec, 0);
         std::vector<int64_t> cnt_tot(nspec, 0);
         std::vector<orc::Particle> carry;
@@ -3395,7 +3417,7 @@ int steady_core(std::vector<orc::Sim>& mats, const orc::DmmSet* dmm, const bte_s
                 T.init(nbx, 1);
                 if (nspec > 0) {
                     T.loc = &locs;
-                    T.nmodes = S.m.n();  // one material
+                    T.nmodes = ntot;
                     T.spec.assign(nspec, 0);
                     T.scnt.assign(nspec, 0);
                 }
@@ -3610,7 +3632,6 @@ int oracle_steady_run_multi(const bte_mode_table* mts, int nmat, const bte_geome
                             const double* thickness) {
     try {
         if (nmat < 1 || !gm->material) return fail(BTE_ERR_INPUT, "materials need mode tables and box materials");
-        if (!g_spec_boxes.empty()) return fail(BTE_ERR_INPUT, "spectral outputs need one crystal");
         orc::MultiSim M;
         for (int k = 0; k < nmat; ++k) M.mats.push_back(build_sim(&mts[k], gm));
         if (thickness)

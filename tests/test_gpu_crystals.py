@@ -134,16 +134,20 @@ def test_two_crystals_general_kernel_agrees_with_restatement(engine):
     check(np.array(gpu), np.array(cpu), names, "two crystals, evolparticle-faithful kernel")
 
 
-def test_crystals_refuse_rate_sets_and_spectral_outputs(engine):
-    A, B = _tables()
+def test_crystals_refuse_rate_sets_and_mixed_q_grids_in_spectral_outputs(engine):
+    """Rate sets are for one mode table; spectral locations in crystals of
+    different q grids have no common fd_q layout."""
+    A, _ = _tables()
+    B = synth.mode_table(12, 3, 3, 300.0, config=102)
     engine.load_mode_tables([A, B])
     engine.load_geometry(_ribbon())
     with pytest.raises(btegpu.BteError, match="rate sets"):
         engine.load_materials([A["w"]], [300.0])
-    engine.set_spectral([0], 10)
+    engine.set_spectral([2, 7], 10)
     try:
-        with pytest.raises(btegpu.BteError, match="spectral"):
-            engine.rta_run(300.0, 10.0, 100.0, 1000)
+        r = engine.rta_run(300.0, 10.0, 100.0, 1000)
+        with pytest.raises(btegpu.BteError, match="different q grids"):
+            engine.get_spectral(r["gz"].shape[1])
     finally:
         engine.set_spectral([], 0)
 
@@ -227,3 +231,44 @@ def test_rtamc2d_cli_reads_several_materials(built, tmp_path):
     assert T.shape == (20, 1 + g["nboxes"])
     late = T[-5:, 1:11].mean(axis=0)
     assert late[4] - late[5] > 2.0 * max(late[3] - late[4], late[5] - late[6])
+
+
+def test_two_crystal_spectral_outputs(engine):
+    """Spectral decomposition at a box of each crystal (crystals 0.335 and
+    0.5 nm thick): replay's per-mode time tally equals the restatement's
+    over the concatenated modes, and each location's outputs use its own
+    crystal's modes, omega ticks, broadening, volume and heat capacity."""
+    A, B = _tables()
+    g = _ribbon()
+    th = (0.335, 0.5)
+    engine.load_mode_tables([A, B], thickness=th)
+    engine.load_geometry(g)
+    kw = dict(T0=300.0, dt=10.0, maxtime=200.0)
+    locs, nw = [2, 7], 200
+    engine.set_spectral(locs, nomega=nw)
+    try:
+        r = engine.rta_run(N=4000, seed=8, mode=btegpu.MODE_REPLAY, **kw)
+        nbins = r["gz"].shape[1]
+        sp = engine.get_spectral(nbins)
+    finally:
+        engine.set_spectral([])
+    nA, nB = A["omega"].size, B["omega"].size
+    pyoracle.set_spectral(locs)
+    try:
+        pyoracle.rta_run_multi([A, B], g, N=4000, seed=8, nthreads=8, thickness=th, **kw)
+        _, val = pyoracle.spectral_raw((2, nbins, nA + nB))
+    finally:
+        pyoracle.set_spectral([])
+    assert np.array_equal(sp["raw"], val)
+    assert np.abs(val[0, :, nA:]).max() == 0 and np.abs(val[1, :, :nA]).max() == 0
+    for l, (tab, off) in enumerate(((A, 0), (B, nA))):
+        raw = sp["raw"][l:l + 1, :, off:off + tab["omega"].size]
+        grid, dT, jx, jy, fq = pyoracle.spectral_post(tab, raw, nw)
+        assert np.allclose(sp["omega"][l], grid, rtol=1e-14)
+        # dT per tick and the box temperature share the factor Eeff / V_box / (C_v / vcorr)
+        c = (r["temperature"][locs[l], -1] - 300.0) / raw[0].sum()
+        assert np.allclose(sp["dT_omega"][l], c * dT[0], rtol=1e-9, atol=1e-12 * np.abs(sp["dT_omega"][l]).max())
+        for mine, ref in ((sp["jx_omega"][l], jx[0]), (sp["jy_omega"][l], jy[0]), (sp["fd_q"][l], fq[0])):
+            i = np.argmax(np.abs(ref))
+            k = mine.flat[i] / ref.flat[i]
+            assert np.allclose(mine, k * ref, rtol=1e-9, atol=1e-12 * np.abs(mine).max())
