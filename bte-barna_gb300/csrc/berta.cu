@@ -97,25 +97,6 @@ struct BoxProp {
 // Page-locked staging for the per-step uploads: a copy from pageable memory
 // may wait for the stream's earlier work, a copy from here does not.  Each
 // upload site has its own buffer, written again only after a later sync.
-struct Pinned {
-    void* p = nullptr;
-    size_t bytes = 0;
-    Pinned() = default;
-    Pinned(const Pinned&) = delete;
-    Pinned& operator=(const Pinned&) = delete;
-    ~Pinned() {
-        if (p) cudaFreeHost(p);
-    }
-    void reserve(size_t n) {
-        if (bytes >= n) return;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        bytes = 0;
-        ck(cudaMallocHost(&p, n), "cudaMallocHost");
-        bytes = n;
-    }
-};
-
 template <class T>
 void upload_pinned(DBuf& d, Pinned& h, const std::vector<T>& v, cudaStream_t s) {
     const size_t bytes = v.size() * sizeof(T);

@@ -542,7 +542,7 @@ namespace bte {
 // the flux factor, the time integration of a walls source (or bin averages
 // of an initial deviation) and T = gz / (C_v / vcorr) + T0.
 void rta_post(bte_ctx* c, const bte_rta_params* p, int nbx, int nbins, double Eeff, double step,
-              std::vector<double> gz, std::vector<double> jx, std::vector<double> jy, bte_rta_result* out) {
+              std::vector<double>& gz, std::vector<double>& jx, std::vector<double>& jy, bte_rta_result* out) {
     const bte::HostModes& m = c->modes;
     const bte::HostGeometry& g = c->geom;
     const std::size_t nk = std::size_t(nbx) * std::size_t(nbins);
@@ -1068,8 +1068,8 @@ bte_status bte_get_group_result(bte_ctx* c, int32_t group, bte_rta_result* out) 
         if (out->gz) std::copy(gz.begin(), gz.end(), out->gz);
         if (out->gz_jx) std::copy(jx.begin(), jx.end(), out->gz_jx);
         if (out->gz_jy) std::copy(jy.begin(), jy.end(), out->gz_jy);
-        bte::rta_post(c, &c->group_params, c->group_nbx, c->group_nbins, c->group_Eeff, c->group_step,
-                      std::move(gz), std::move(jx), std::move(jy), out);
+        bte::rta_post(c, &c->group_params, c->group_nbx, c->group_nbins, c->group_Eeff, c->group_step, gz, jx, jy,
+                      out);
         return BTE_OK;
     } catch (const std::exception& e) {
         c->err = e.what();
@@ -1244,13 +1244,14 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         std::vector<unsigned long long> hc(16);
         int herr[4];
         std::vector<unsigned long long> hex;
-        std::vector<double> htal;
+        const double* htal = nullptr;  // the production tally, in the page-locked readback buffer
         if (replay) {
             hex.resize(nk * 6);
             ck(cudaMemcpyAsync(hex.data(), c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
         } else {
-            htal.resize(nk * 3 * std::size_t(ngroups));
-            ck(cudaMemcpyAsync(htal.data(), c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
+            c->h_tally.reserve(tally_bytes);
+            htal = static_cast<const double*>(c->h_tally.p);
+            ck(cudaMemcpyAsync(c->h_tally.p, c->d_tally.p, tally_bytes, cudaMemcpyDeviceToHost, c->stream), "d2h");
         }
         ck(cudaMemcpyAsync(hc.data(), counters, 16 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream), "d2h");
         ck(cudaMemcpyAsync(herr, err, 4 * sizeof(int), cudaMemcpyDeviceToHost, c->stream), "d2h");
@@ -1290,13 +1291,14 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
                                                       : "geometry error");
             throw Error(bte_status(herr[0]), msg);
         }
+        std::vector<double> sum;
         if (ngroups > 1) {
             // keep the groups; the run's outputs are their sum, in group order
-            c->group_raw = htal;
-            std::vector<double> sum(nk * 3, 0.);
+            c->group_raw.assign(htal, htal + nk * 3 * std::size_t(ngroups));
+            sum.assign(nk * 3, 0.);
             for (int gi = 0; gi < ngroups; ++gi)
                 for (std::size_t k = 0; k < nk * 3; ++k) sum[k] += htal[std::size_t(gi) * nk * 3 + k];
-            htal.swap(sum);
+            htal = sum.data();
             c->group_n = ngroups;
             c->group_nbx = nbx;
             c->group_nbins = nbins;
@@ -1306,7 +1308,12 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
             c->group_valid = true;
         }
         // raw tallies
-        std::vector<double> gz(nk), jx(nk), jy(nk);
+        std::vector<double>& gz = c->post_gz;
+        std::vector<double>& jx = c->post_jx;
+        std::vector<double>& jy = c->post_jy;
+        gz.resize(nk);
+        jx.resize(nk);
+        jy.resize(nk);
         if (replay) {
             for (std::size_t k = 0; k < nk; ++k) {
                 double* dst[3] = {&gz[k], &jx[k], &jy[k]};
@@ -1341,7 +1348,7 @@ bte_status bte_rta_run(bte_ctx* c, const bte_rta_params* p, bte_rta_result* out)
         if (out->gz) std::copy(gz.begin(), gz.end(), out->gz);
         if (out->gz_jx) std::copy(jx.begin(), jx.end(), out->gz_jx);
         if (out->gz_jy) std::copy(jy.begin(), jy.end(), out->gz_jy);
-        bte::rta_post(c, p, nbx, nbins, Eeff, step, std::move(gz), std::move(jx), std::move(jy), out);
+        bte::rta_post(c, p, nbx, nbins, Eeff, step, gz, jx, jy, out);
         return BTE_OK;
     } catch (const Error& e) {
         return fail(c, e);

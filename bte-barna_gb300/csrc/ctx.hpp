@@ -47,6 +47,28 @@ struct DBuf {
     T* as() const { return static_cast<T*>(p); }
 };
 
+// Page-locked host memory, grown as needed and kept: device copies from or
+// into it run at full bus speed and need no staging.
+struct Pinned {
+    void* p = nullptr;
+    size_t bytes = 0;
+    Pinned() = default;
+    Pinned(const Pinned&) = delete;
+    Pinned& operator=(const Pinned&) = delete;
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+    void reserve(size_t n) {
+        if (bytes >= n) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        ck(cudaMallocHost(&p, n), "cudaMallocHost");
+        bytes = n;
+    }
+};
+
+
 inline int hw_threads() {
     unsigned n = std::thread::hardware_concurrency();
     return n ? int(n < 64u ? n : 64u) : 4;
@@ -138,6 +160,10 @@ struct bte_ctx {
     double group_Eeff = 0., group_step = 0.;
     bte_rta_params group_params{};
     std::vector<double> group_raw;
+    // the production tally's readback (page-locked) and the raw tallies
+    // handed to the post-processing, kept across runs
+    bte::Pinned h_tally;
+    std::vector<double> post_gz, post_jx, post_jy;
     // run buffers
     bte::DBuf d_time, d_tally, d_counters, d_err, d_work;
     std::vector<double> h_time;
