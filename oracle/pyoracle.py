@@ -496,7 +496,7 @@ def rta_run_multi(tables, geom, T0, dt, maxtime, N, seed=1, nthreads=8, source=N
     out.update(Eeff=r.Eeff, energy_rate=r.energy_rate, events=int(cnt[0]), wall_hits=int(cnt[1]),
                crossings=int(cnt[2]), absorbed=int(cnt[3]), nudges=int(cnt[4]), quirks=int(cnt[5]),
                loop_seconds=float(cnt[6]) * 1e-6, interface_hits=int(cnt[7]),
-               interface_transmissions=int(cnt[8]))
+               interface_transmissions=int(cnt[8]), translations=int(r.translations))
     return out
 
 
