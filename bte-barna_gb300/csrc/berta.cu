@@ -715,6 +715,9 @@ __global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, con
                                                   int nm, const double* w, const float* rprob, const int* ralt,
                                                   int nmodes, unsigned long long skey, int* H, int* err) {
     constexpr bool advect = ADV != 0;
+    // the step's new particles are a few per warp: smaller claims spread
+    // them over more warps
+    constexpr unsigned in_chunk = ADV == 0 ? 32u : BE_IN_CHUNK;
     const long long n = min((long long)*n_in, ocap);  // places (both buffers hold ocap)
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
@@ -732,10 +735,10 @@ __global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, con
         if (idle) {
             if (qb >= qe) {
                 unsigned long long b = 0;
-                if (lane == 0) b = atomicAdd(dc + DC_WORK, (unsigned long long)BE_IN_CHUNK);
+                if (lane == 0) b = atomicAdd(dc + DC_WORK, (unsigned long long)in_chunk);
                 b = __shfl_sync(0xffffffffu, b, 0);
                 qb = b;
-                qe = b + BE_IN_CHUNK;
+                qe = b + in_chunk;
             }
             const unsigned rank = __popc(idle & lt);
             const unsigned long long avail = qe - qb;
