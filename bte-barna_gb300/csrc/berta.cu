@@ -14,7 +14,7 @@
 //                                           be_plan_sources, be_generate_dev
 //   4 adiabatic diffuse re-emission of |Eborder| at the wall temperature from
 //     the J(T) cubic spline (adiabatic_diffuse_walls :281-435)
-//                  be_plan_adiabatic, be_wall_cdf_dev, be_generate_dev
+//                  be_plan_adiabatic, be_wall_cdf1/2_dev, be_generate_dev
 //   5 deletion of the absorbed particles, 6 propagator scattering with sign
 //     branching (Scattering :1073-1210, propagator_H::get
 //     src/collision_operator.cpp:892-903), each parent's branching attempts
@@ -127,6 +127,7 @@ struct BertaState {
     DBuf d_H, d_cnt, d_Eb, d_props, d_boxwall, d_gens, d_alias, d_rvx, d_rvy;
     DBuf d_om, d_vx, d_vy, d_req, d_cdf, d_cdftot, d_isoprob, d_isoalt;
     DBuf d_gprob, d_galt, d_gsign;          // gradient source rows
+    DBuf d_ctot;                            // wall-CDF chunk sums
     Pinned h_gens[1];                       // staging: descriptors of the initial particles
     // device-resident step loop: counters, planned sources, per-step records
     DBuf d_dc, d_span, d_gdesc, d_ggenf, d_gcnt, d_idesc, d_igenf, d_icnt, d_adi, d_adesc, d_acnt;
@@ -135,10 +136,6 @@ struct BertaState {
     std::vector<Spline1D> spl;
     std::vector<char> spl_ok;
     long long spl_version = -1;   // tables the splines were built for
-    // the adiabatic borders' records and J(T) -> T splines on the device
-    long long adi_version = -1;   // tables they were built for
-    int adi_nk = 0;
-    bool adi_splines = false;
 };
 
 void reset_propagators(bte_ctx* c) {
@@ -233,6 +230,7 @@ struct AdvectArgs {
 // Draws of the geometric choices of one particle's advection.
 struct BePol {
     Philox g;
+    __device__ double u() { return g.uniform(); }
     __device__ int choose(int n) { return uniform_below(g, uint32_t(n)); }
 };
 
@@ -394,10 +392,8 @@ __device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& 
 
 // Isothermal_wall_distribution (src/sampling.cpp:189-269) of each request:
 // pmf_k = v_n omega_k |n(omega_k, Tw) - n(omega_k, Te)| for v_n > 0, turned
-// into a CDF row; tot[r] keeps the sum.  One block of WCDF_THREADS threads
-// per request: each thread sums a segment of the row in FP64, a shuffle
-// scan gives the segments' offsets and the row's total, and each thread
-// normalises its own segment.
+// into a CDF row; tot[r] keeps the sum.  Each request's row is split into
+// chunks of WCDF_CHUNK modes, one block each.
 //
 // The pmf is evaluated in FP32 and summed in FP64: with x = hbar omega / kT,
 // n_w - n_e = expm1(x_e - x_w) / (expm1(x_e) (-expm1(-x_w))), which has no
@@ -407,7 +403,7 @@ __device__ bool advect_general(const DevTables& T, BePol& pol, int* Eb, double& 
 // value, all entries above 1e-30 of it within 1e-5 (the rounding of x to
 // FP32 at x ~ 60), and the FP64 units do one addition per mode instead of
 // two exponentials and two divisions.
-constexpr int WCDF_THREADS = 1024;
+constexpr int WCDF_CHUNK = 1024;
 
 __device__ __forceinline__ float wall_pmf_f(float w, float vn, float ce, float q, float rr) {
     const float xe = ce * w;   // x_e
@@ -421,14 +417,17 @@ __device__ __forceinline__ float wall_pmf_f(float w, float vn, float ce, float q
     return vn * w * fabsf(diff);
 }
 
-__device__ __forceinline__ void wall_cdf_body(const float* om, const float* vx, const float* vy, int n,
-                                              const WallReq* req, double* cdf, double* tot) {
-    __shared__ double wsum[32];
-    const int r = blockIdx.x;
+// pass 1: the chunk's running sums in place and its total
+__device__ __forceinline__ void wall_cdf1_body(const float* om, const float* vx, const float* vy, int n,
+                                               const WallReq* req, double* cdf, double* chunk_tot) {
+    __shared__ double part[256];
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
     const WallReq R = req[r];
     double* row = cdf + (long long)r * n;
-    const int seg = (n + int(blockDim.x) - 1) / int(blockDim.x);
-    const int k0 = min(n, int(threadIdx.x) * seg), k1 = min(n, k0 + seg);
+    const int c0 = ch * WCDF_CHUNK, c1 = min(n, c0 + WCDF_CHUNK);
+    const int seg = (c1 - c0 + blockDim.x - 1) / blockDim.x;
+    const int k0 = c0 + threadIdx.x * seg, k1 = min(c1, k0 + seg);
     constexpr double pre = 1e12 * 1.054571726e-34 / 1.3806488e-23;
     const float ce = float(pre / R.Te), q = float(R.Te / R.Tw), rr = float((R.Tw - R.Te) / R.Tw);
     const float nx = float(R.nx), ny = float(R.ny);
@@ -440,30 +439,37 @@ __device__ __forceinline__ void wall_cdf_body(const float* om, const float* vx, 
         acc += double(p);
         row[k] = acc;  // running sum within the thread's segment
     }
-    // offsets of the segments: a shuffle scan in each warp, then over the
-    // warps' totals
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    double incl = acc;
-    for (int o = 1; o < 32; o <<= 1) {
-        const double t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    if (lane == 31) wsum[warp] = incl;
+    part[threadIdx.x] = acc;
     __syncthreads();
-    if (warp == 0) {
-        double w = lane < nwarps ? wsum[lane] : 0.;
-        for (int o = 1; o < 32; o <<= 1) {
-            const double t = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += t;
+    if (threadIdx.x == 0) {  // exclusive offsets of the segments
+        double sum = 0.;
+        for (int t = 0; t < blockDim.x; ++t) {
+            const double v = part[t];
+            part[t] = sum;
+            sum += v;
         }
-        if (lane < nwarps) wsum[lane] = w;  // inclusive totals of the warps
+        chunk_tot[blockIdx.x] = sum;
     }
     __syncthreads();
-    const double total = wsum[nwarps - 1];
-    if (threadIdx.x == 0) tot[r] = total;
+    const double off = part[threadIdx.x];
+    for (int k = k0; k < k1; ++k) row[k] += off;
+}
+
+// pass 2: offsets of the chunks, normalisation, the request's total
+__device__ __forceinline__ void wall_cdf2_body(int n, const double* chunk_tot, double* cdf, double* tot) {
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    const int r = blockIdx.x / nch, ch = blockIdx.x % nch;
+    double off = 0., total = 0.;
+    for (int c = 0; c < nch; ++c) {
+        const double v = chunk_tot[(long long)r * nch + c];
+        if (c < ch) off += v;
+        total += v;
+    }
+    if (ch == 0 && threadIdx.x == 0) tot[r] = total;
     if (!(total > 0.)) return;
-    const double off = (incl - acc) + (warp > 0 ? wsum[warp - 1] : 0.);
-    for (int k = k0; k < k1; ++k) row[k] = (row[k] + off) / total;
+    double* row = cdf + (long long)r * n;
+    const int c0 = ch * WCDF_CHUNK, c1 = min(n, c0 + WCDF_CHUNK);
+    for (int k = c0 + threadIdx.x; k < c1; k += blockDim.x) row[k] = (row[k] + off) / total;
 }
 
 // New particles [base, base + n) from the step's sources.
@@ -625,9 +631,7 @@ __device__ __forceinline__ void cancel_body(PArr P, long long n, const int* H, i
         const unsigned mask = ((unsigned)c * 0x9E3779B1u + mkey) >> 27;
         const long long i = (long long)(c << 5) + (long long)((unsigned)lane ^ mask);
         if (i >= n) continue;
-        const int mi = P.mode[i];
-        if (mi < 0) continue;  // a hole
-        const long long key = (long long)P.box[i] * nmodes + mi;
+        const long long key = (long long)P.box[i] * nmodes + P.mode[i];
         const int h = H[key];
         const int s = P.sign[i];
         bool keep = !reservoir[P.box[i]] && h != 0 && ((s < 0) == (h < 0));
@@ -664,10 +668,7 @@ __global__ void be_props(const int* H, int nmodes, const double* vx, const doubl
 // Counters of the step loop, kept on the device between kernels.
 // DC_IN and DC_OUTT sum the particles read and written by be_advance over
 // the run (the algorithmic traffic of its roofline).
-// DC_NP: the places of the population (holes included, see be_advance);
-// DC_LIVE: its particles; DC_WRIT: the particles be_advance wrote in the
-// step.
-enum { DC_NP = 0, DC_NOUT, DC_WORK, DC_FLIPS, DC_PSTEPS, DC_NGEN, DC_IN, DC_OUTT, DC_WRIT, DC_LIVE, DC_COUNT = 10 };
+enum { DC_NP = 0, DC_NOUT, DC_WORK, DC_FLIPS, DC_PSTEPS, DC_NGEN, DC_IN, DC_OUTT, DC_COUNT = 8 };
 
 // A source planned on the device: where its particles start in the
 // particle arrays and how many there are.
@@ -695,66 +696,46 @@ constexpr unsigned BRANCH_CAP = 1u << 20;
 // 1 - exp(-w dt)) or the propagator with sign branching as above -- and the
 // histogram H[box][mode] += sign of every outgoing particle, appended to
 // `out` warp by warp.  Persistent warps: a lane whose parent owes no more
-// attempts takes the next parent; a parent absorbed during its advection
-// owes none.  Each particle is read once and each outgoing particle written
-// once.  A warp claims its parents and its output places from the two
-// global counters in chunks (BE_IN_CHUNK, BE_OUT_CHUNK), not once per pass:
-// every warp of the device adds to the same two words, and their atomics,
-// serialised at one L2 slice each, bounded the kernel.  The output places
-// a warp claimed and did not fill are holes (mode -1), which every reader
-// of the population skips and the next compaction drops; `n_in` counts
-// places, DC_LIVE and DC_WRIT particles.
-constexpr unsigned BE_IN_CHUNK = 128, BE_OUT_CHUNK = 64;
-// ADV: 0 no advection (particles made in this step), 1 advection on a
-// grid of cells, 2 advection across any convex boxes; one kernel each, so
-// that the grid variant carries none of the general walk's registers.
-template <int ADV>
-__global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, const unsigned long long* n_in, PArr out,
-                                                  unsigned long long* dc, long long ocap,
+// attempts takes the next parent from a counter; a parent absorbed during
+// its advection owes none.  Each particle is read once and each outgoing
+// particle written once.
+__global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long long* n_in, PArr out,
+                                                  unsigned long long* dc, long long ocap, int advect,
                                                   AdvectArgs aa, int rta, const PAlias* pal, const BoxProp* bprop,
                                                   int nm, const double* w, const float* rprob, const int* ralt,
                                                   int nmodes, unsigned long long skey, int* H, int* err) {
-    constexpr bool advect = ADV != 0;
-    // the step's new particles are a few per warp: smaller claims spread
-    // them over more warps
-    constexpr unsigned in_chunk = ADV == 0 ? 32u : BE_IN_CHUNK;
-    const long long n = min((long long)*n_in, ocap);  // places (both buffers hold ocap)
+    const long long n = (long long)*n_in;
     const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    unsigned long long flips = 0, nread = 0, written = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) {
+        if (advect) atomicAdd(dc + DC_PSTEPS, (unsigned long long)n);
+        atomicAdd(dc + DC_IN, (unsigned long long)n);
+    }
+    unsigned long long flips = 0;
     int mode = 0, sign = 1, box = 0, col = 0;
     double x = 0., y = 0.;
     unsigned todo = 0, made = 0;
     bool done = false, valid = false;
-    // the warp's claimed parents [qb, qe) and output places [ob, oe)
-    unsigned long long qb = 0, qe = 0, ob = 0, oe = 0;
     Philox g;
     g.init(skey, 0);
     for (;;) {
         const unsigned idle = __ballot_sync(0xffffffffu, todo == 0 && !done);
         if (idle) {
-            if (qb >= qe) {
-                unsigned long long b = 0;
-                if (lane == 0) b = atomicAdd(dc + DC_WORK, (unsigned long long)in_chunk);
-                b = __shfl_sync(0xffffffffu, b, 0);
-                qb = b;
-                qe = b + in_chunk;
-            }
-            const unsigned rank = __popc(idle & lt);
-            const unsigned long long avail = qe - qb;
-            if (todo == 0 && !done && rank < avail) {  // the others wait for the next pass
-                const long long i = (long long)(qb + rank);
+            unsigned long long base = 0;
+            const int leader = __ffs(idle) - 1;
+            if (lane == leader) base = atomicAdd(dc + DC_WORK, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (todo == 0 && !done) {
+                const long long i = (long long)base + __popc(idle & ((1u << lane) - 1u));
                 if (i < n) {
                     mode = in.mode[i];
                     if (mode >= 0) {
-                        ++nread;
                         sign = in.sign[i];
                         box = in.box[i];
                         x = in.x[i];
                         y = in.y[i];
                         bool alive = true;
                         if (advect) {
-                            if (ADV == 2) {
+                            if (aa.general) {
                                 BePol pol;
                                 pol.g.init(aa.gkey, (uint64_t)i);
                                 int e = 0;
@@ -778,24 +759,14 @@ __global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, con
                     done = true;
                 }
             }
-            qb += min((unsigned long long)__popc(idle), avail);
         }
         if (__all_sync(0xffffffffu, done)) break;
         const bool act = todo > 0;
-        // the pass's output places, from the warp's chunk (a new chunk when
-        // it cannot hold them all: the rest of the old one become holes)
+        // the warp's output places, claimed before the draws so that the
+        // atomic's round trip overlaps the propagator read
         const unsigned m1 = __ballot_sync(0xffffffffu, act);
-        const unsigned need = __popc(m1);
-        if (need > oe - ob) {
-            for (unsigned long long k = ob + lane; k < oe && k < (unsigned long long)ocap; k += 32) out.mode[k] = -1;
-            unsigned long long b = 0;
-            if (lane == 0) b = atomicAdd(dc + DC_NOUT, (unsigned long long)BE_OUT_CHUNK);
-            b = __shfl_sync(0xffffffffu, b, 0);
-            ob = b;
-            oe = b + BE_OUT_CHUNK;
-        }
-        const unsigned long long wo = ob;
-        ob += need;
+        unsigned long long wo = 0;
+        if (lane == 0 && m1) wo = atomicAdd(dc + DC_NOUT, (unsigned long long)__popc(m1));
         int nmode = mode, nsign = sign;
         if (act && rta) {
             const double u = g.uniform();
@@ -828,8 +799,9 @@ __global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, con
                 }
             }
         }
+        wo = __shfl_sync(0xffffffffu, wo, 0);
         if (act) {
-            const long long o = (long long)wo + __popc(m1 & lt);
+            const long long o = (long long)wo + __popc(m1 & ((1u << lane) - 1u));
             if (o < ocap) {
                 out.x[o] = x;
                 out.y[o] = y;
@@ -837,7 +809,6 @@ __global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, con
                 out.mode[o] = nmode;
                 out.sign[o] = nsign;
                 atomicAdd(H + (long long)box * nmodes + nmode, nsign);
-                ++written;
             } else {
                 atomicCAS(err, 0, E_LIMIT);
             }
@@ -852,20 +823,8 @@ __global__ void __launch_bounds__(256, ADV == 2 ? 1 : 3) be_advance(PArr in, con
             }
         }
     }
-    for (unsigned long long k = ob + lane; k < oe && k < (unsigned long long)ocap; k += 32) out.mode[k] = -1;
-    for (int o = 16; o > 0; o >>= 1) {
-        flips += __shfl_down_sync(0xffffffffu, flips, o);
-        nread += __shfl_down_sync(0xffffffffu, nread, o);
-        written += __shfl_down_sync(0xffffffffu, written, o);
-    }
-    if (lane == 0) {
-        if (flips) atomicAdd(dc + DC_FLIPS, flips);
-        if (nread) {
-            if (advect) atomicAdd(dc + DC_PSTEPS, nread);
-            atomicAdd(dc + DC_IN, nread);
-        }
-        if (written) atomicAdd(dc + DC_WRIT, written);
-    }
+    for (int o = 16; o > 0; o >>= 1) flips += __shfl_down_sync(0xffffffffu, flips, o);
+    if (lane == 0 && flips) atomicAdd(dc + DC_FLIPS, flips);
 }
 
 // Exclusive scan of cnt[0..n) into descs[k].first, by one warp; returns the
@@ -1070,11 +1029,18 @@ __global__ void be_generate_dev(PArr P, const SrcSpan* span, const GenDesc* gens
 
 // The wall-CDF passes over every border, for the borders the step planned
 // (cnt > 0); rows of the others are left as they are.
-__global__ void __launch_bounds__(WCDF_THREADS) be_wall_cdf_dev(const float* om, const float* vx, const float* vy,
-                                                                 int n, const WallReq* req, const long long* cnt,
-                                                                 double* cdf, double* tot) {
-    if (cnt[blockIdx.x] == 0) return;
-    wall_cdf_body(om, vx, vy, n, req, cdf, tot);
+__global__ void __launch_bounds__(256) be_wall_cdf1_dev(const float* om, const float* vx, const float* vy, int n,
+                                                        const WallReq* req, const long long* cnt, double* cdf,
+                                                        double* chunk_tot) {
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    if (cnt[blockIdx.x / nch] == 0) return;
+    wall_cdf1_body(om, vx, vy, n, req, cdf, chunk_tot);
+}
+__global__ void __launch_bounds__(256) be_wall_cdf2_dev(int n, const long long* cnt, const double* chunk_tot,
+                                                        double* cdf, double* tot) {
+    const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+    if (cnt[blockIdx.x / nch] == 0) return;
+    wall_cdf2_body(n, chunk_tot, cdf, tot);
 }
 
 // Cancellation on the device over [0, *n_in) with the random affine
@@ -1087,9 +1053,9 @@ __device__ __forceinline__ unsigned long long gcd_u64(unsigned long long a, unsi
     }
     return a;
 }
-__global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, long long cap, const int* H, int* cnt,
-                              int nmodes, const int* reservoir, unsigned long long key) {
-    const long long n = min((long long)*n_in, cap);
+__global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, const int* H, int* cnt, int nmodes,
+                              const int* reservoir, unsigned long long key) {
+    const long long n = (long long)*n_in;
     if (n <= 0) return;
     // the permutation's a, b and the XOR key, drawn by one thread per block
     __shared__ unsigned long long s_ab[2];
@@ -1112,18 +1078,16 @@ __global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, long long 
 }
 
 // Compaction of [0, *n_in) with the survivors counted into *count.
-__global__ void be_compact_dev(PArr in, const unsigned long long* n_in, long long cap, PArr out,
-                               unsigned long long* count) {
-    compact_body(in, min((long long)*n_in, cap), out, count);
+__global__ void be_compact_dev(PArr in, const unsigned long long* n_in, PArr out, unsigned long long* count) {
+    compact_body(in, (long long)*n_in, out, count);
 }
 
-// dc[to] = dc[from]; dc[DC_LIVE] = dc[live]; then record[step] = dc[DC_LIVE].
-__global__ void be_counters(unsigned long long* dc, int to, int from, int live, long long* record, int step) {
+// dc[to] = dc[from]; record[step] = dc[DC_NP] after it.
+__global__ void be_counters(unsigned long long* dc, int to, int from, long long* record, int step) {
     if (to >= 0) dc[to] = dc[from];
-    if (live >= 0) dc[DC_LIVE] = dc[live];
     if (record) {  // the end of a step: its particles alive, and the outputs of its be_advance launches
-        record[step] = (long long)dc[DC_LIVE];
-        dc[DC_OUTT] += dc[DC_WRIT];
+        record[step] = (long long)dc[DC_NP];
+        dc[DC_OUTT] += dc[DC_NOUT];
     }
 }
 
@@ -1424,6 +1388,7 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         B.d_req.alloc(std::size_t(nborders) * sizeof(WallReq));
         B.d_cdf.alloc(std::size_t(nborders) * std::size_t(m.n()) * sizeof(double));
         B.d_cdftot.alloc(std::size_t(nborders) * sizeof(double));
+        B.d_ctot.alloc(std::size_t(nborders) * ((m.n() + WCDF_CHUNK - 1) / WCDF_CHUNK) * sizeof(double));
         ck(cudaMemsetAsync(B.d_Eb.p, 0, std::size_t(nborders) * sizeof(int), s), "memset");
         if (int(B.spl.size()) != nborders || B.spl_version != c->tables_version) {
             B.spl.assign(std::size_t(nborders), Spline1D());
@@ -1609,8 +1574,36 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             if (out->nparticles) out->nparticles[sidx] = nn;
         };
-        // everything the host prepares for the run comes before ev0, so that
-        // the device time of the run holds no host work
+        ck(cudaEventRecord(c->ev0, s), "event");
+        // initial deviation (init_particles, src/beyondRTA_MC2d.cpp:211-269)
+        long long np = 0;
+        descs.clear();
+        aprob.clear();
+        aalt.clear();
+        if (have_ini) {
+            long long first = 0;
+            for (std::size_t k = 0; k < ini.init_box.size(); ++k) {
+                const long long cnt = (long long)n_to_generate(ini.init_energy[k] / p->Eeff, rng);
+                if (cnt == 0) continue;
+                const int b = ini.init_box[k];
+                GenDesc d = box_desc(b);
+                d.sign = ini.init_sign[k];
+                d.cdf = -1;
+                const long long off = (long long)aprob.size();
+                for (std::size_t q = 0; q < std::size_t(n); ++q) {
+                    aprob.push_back(ini.alias[k * std::size_t(n) + q].prob);
+                    aalt.push_back(ini.alias[k * std::size_t(n) + q].alt);
+                }
+                d.alias_off = off;
+                d.first = first;
+                descs.push_back(d);
+                first += cnt;
+            }
+            generate(0, first, -1, 0);
+            np = first;
+        }
+        props(np, 0);
+        long long psteps = 0, branchings = 0, adv_in = 0, adv_out = 0;
         // ---- the step loop, resident on the device: particle numbers stay in
         // device counters, the sources are planned on the device, and the
         // step's properties are recorded there; the host synchronises only
@@ -1621,6 +1614,11 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         auto* dc = B.d_dc.as<unsigned long long>();
         B.d_span.alloc(3 * sizeof(SrcSpan));
         SrcSpan* span = B.d_span.as<SrcSpan>();
+        {
+            std::vector<unsigned long long> h0(DC_COUNT, 0ull);
+            h0[DC_NP] = (unsigned long long)np;
+            B.d_dc.upload(h0, s);
+        }
         B.d_phist.alloc(std::size_t(nsteps + 1) * std::size_t(nbx) * 3 * sizeof(double));
         B.d_nhist.alloc(std::size_t(nsteps + 1) * sizeof(long long));
         // sources with fixed descriptors: gradient boxes and isothermal walls,
@@ -1664,15 +1662,12 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
         }
         // adiabatic re-emission per void border: segment, inward normal, Teq
         // and the J(T) -> T spline of its wall (one per normal and Teq)
-        // (built once per mode table and geometry: 100 wall pmfs over every
-        // mode per spline, the host's largest cost of a run)
-        const bool adi_cached = B.adi_version == c->tables_version;
-        std::vector<AdiBorder> adi(static_cast<std::size_t>(adi_cached ? 0 : nborders));
+        std::vector<AdiBorder> adi(static_cast<std::size_t>(nborders));
         std::vector<double> sa, sb, sc, sd, sx0, sxs;
         std::map<std::tuple<double, double, double>, int> spline_of;
-        int spl_nk = adi_cached ? B.adi_nk : 0;
+        int spl_nk = 0;
         std::vector<double> pmf;
-        for (int gb = 0; gb < (adi_cached ? 0 : nborders); ++gb) {
+        for (int gb = 0; gb < nborders; ++gb) {
             AdiBorder& A = adi[std::size_t(gb)];
             const int b = border_box[std::size_t(gb)];
             const GBorder& br = g.borders[std::size_t(gb)];
@@ -1711,38 +1706,22 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
             A.spline = it->second;
         }
-        if (!adi_cached) {
-            B.d_adi.upload(adi, s);
-            B.adi_splines = !sa.empty();
-            if (B.adi_splines) {
-                B.d_sa.upload(sa, s);
-                B.d_sb.upload(sb, s);
-                B.d_sc.upload(sc, s);
-                B.d_sd.upload(sd, s);
-                B.d_sx0.upload(sx0, s);
-                B.d_sxs.upload(sxs, s);
-            }
-            B.adi_nk = spl_nk;
-            B.adi_version = c->tables_version;
-        }
+        B.d_adi.upload(adi, s);
         B.d_adesc.alloc(std::size_t(nborders) * sizeof(GenDesc));
         B.d_acnt.alloc(std::size_t(nborders) * sizeof(long long));
         SplineDev SP{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, spl_nk};
-        if (B.adi_splines)
+        if (!sa.empty()) {
+            B.d_sa.upload(sa, s);
+            B.d_sb.upload(sb, s);
+            B.d_sc.upload(sc, s);
+            B.d_sd.upload(sd, s);
+            B.d_sx0.upload(sx0, s);
+            B.d_sxs.upload(sxs, s);
             SP = SplineDev{B.d_sa.as<double>(), B.d_sb.as<double>(), B.d_sc.as<double>(), B.d_sd.as<double>(),
                            B.d_sx0.as<double>(), B.d_sxs.as<double>(), spl_nk};
-        const unsigned pblocks = unsigned(c->nsm) * 8u;  // persistent grids of the step kernels
-        // be_advance: the resident blocks only (each warp claims output
-        // places in chunks, so a warp that starts late would leave holes)
-        unsigned ablocks0 = 0, ablocks1 = 0;
-        {
-            int o0 = 0, o1 = 0;
-            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o0, be_advance<0>, 256, 0), "occupancy");
-            ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o1, general ? be_advance<2> : be_advance<1>, 256, 0),
-               "occupancy");
-            ablocks0 = unsigned(c->nsm) * unsigned(std::max(o0, 1));
-            ablocks1 = unsigned(c->nsm) * unsigned(std::max(o1, 1));
         }
+        const int nch = (n + WCDF_CHUNK - 1) / WCDF_CHUNK;
+        const unsigned pblocks = unsigned(c->nsm) * 8u;  // persistent grids of the step kernels
         const BoxProp* bprop = p->rta ? nullptr : B.d_boxprop.as<BoxProp>();
         int istep = 0;
         double time = 0.;
@@ -1759,42 +1738,6 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             }
         } pe_guard{&pev};
         for (auto& e : pev) ck(cudaEventCreate(&e), "cudaEventCreate");
-        ck(cudaEventRecord(c->ev0, s), "event");
-        // initial deviation (init_particles, src/beyondRTA_MC2d.cpp:211-269)
-        long long np = 0;
-        descs.clear();
-        aprob.clear();
-        aalt.clear();
-        if (have_ini) {
-            long long first = 0;
-            for (std::size_t k = 0; k < ini.init_box.size(); ++k) {
-                const long long cnt = (long long)n_to_generate(ini.init_energy[k] / p->Eeff, rng);
-                if (cnt == 0) continue;
-                const int b = ini.init_box[k];
-                GenDesc d = box_desc(b);
-                d.sign = ini.init_sign[k];
-                d.cdf = -1;
-                const long long off = (long long)aprob.size();
-                for (std::size_t q = 0; q < std::size_t(n); ++q) {
-                    aprob.push_back(ini.alias[k * std::size_t(n) + q].prob);
-                    aalt.push_back(ini.alias[k * std::size_t(n) + q].alt);
-                }
-                d.alias_off = off;
-                d.first = first;
-                descs.push_back(d);
-                first += cnt;
-            }
-            generate(0, first, -1, 0);
-            np = first;
-        }
-        props(np, 0);
-        long long psteps = 0, branchings = 0, adv_in = 0, adv_out = 0;
-        {
-            std::vector<unsigned long long> h0(DC_COUNT, 0ull);
-            h0[DC_NP] = (unsigned long long)np;
-            h0[DC_LIVE] = (unsigned long long)np;
-            B.d_dc.upload(h0, s);
-        }
         phase[PH_READ] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         std::vector<int> hH;
         const int cancel_every = p->cancel_every > 0 ? p->cancel_every : 4;
@@ -1813,14 +1756,13 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             // scattering and histogram in one pass, into B
             ck(cudaMemsetAsync(B.d_H.p, 0, hbytes, s), "memset");
             ck(cudaMemsetAsync(dc + DC_NOUT, 0, 2 * sizeof(unsigned long long), s), "memset");
-            ck(cudaMemsetAsync(dc + DC_WRIT, 0, sizeof(unsigned long long), s), "memset");
             const AdvectArgs a_step{GA.G, GA.boxcell, GA.mv, B.d_boxwall.as<int4>(), B.d_Eb.as<int>(), p->dt, 0ull, 0,
                                     general, mix_key(p->seed, istep, 31), err, TT};
-            (general ? be_advance<2> : be_advance<1>)<<<ablocks1, 256, 0, s>>>(
-                arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP,
-                arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc, cap, a_step, p->rta, pal, bprop, B.nm,
-                c->d_w.as<double>(), c->d_rprob.as<float>(), c->d_ralt.as<int>(), n, mix_key(p->seed, istep, 64),
-                B.d_H.as<int>(), err);
+            be_advance<<<pblocks, 256, 0, s>>>(arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP,
+                                               arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc, cap, 1, a_step,
+                                               p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
+                                               c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
+                                               mix_key(p->seed, istep, 64), B.d_H.as<int>(), err);
             ck(cudaEventRecord(ev[1], s), "event");
             // 2-4 the step's sources, made at A[0..) (A is free now) and each
             // advected for a random part of the step as it is made
@@ -1852,9 +1794,11 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
                 be_plan_adiabatic<<<1, 32, 0, s>>>(B.d_Eb.as<int>(), B.d_adi.as<AdiBorder>(), nborders, SP, p->Eeff,
                                                    p->dt, g.thickness, B.d_req.as<WallReq>(), B.d_acnt.as<long long>(),
                                                    B.d_adesc.as<GenDesc>(), dc, span + 2, cap, err);
-                be_wall_cdf_dev<<<unsigned(nborders), WCDF_THREADS, 0, s>>>(
+                be_wall_cdf1_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
                     B.d_om.as<float>(), B.d_vx.as<float>(), B.d_vy.as<float>(), n, B.d_req.as<WallReq>(),
-                    B.d_acnt.as<long long>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
+                    B.d_acnt.as<long long>(), B.d_cdf.as<double>(), B.d_ctot.as<double>());
+                be_wall_cdf2_dev<<<unsigned(nborders) * unsigned(nch), 256, 0, s>>>(
+                    n, B.d_acnt.as<long long>(), B.d_ctot.as<double>(), B.d_cdf.as<double>(), B.d_cdftot.as<double>());
                 be_generate_dev<<<pblocks, 256, 0, s>>>(A, span + 2, B.d_adesc.as<GenDesc>(), nborders, nullptr, nullptr,
                                                         nullptr, B.d_cdf.as<double>(), B.d_cdftot.as<double>(), n,
                                                         mix_key(p->seed, istep, 4), c->d_boxes.as<GBox>(),
@@ -1864,33 +1808,30 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             // 5-7 for the new particles: the absorbed ones dropped, the others
             // scattered and counted in the histogram, appended to B
             ck(cudaMemsetAsync(dc + DC_WORK, 0, sizeof(unsigned long long), s), "memset");
-            be_advance<0><<<ablocks0, 256, 0, s>>>(A, dc + DC_NGEN, arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign),
-                                                  dc, cap, a_step, p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
-                                                  c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
-                                                  mix_key(p->seed, istep, 65), B.d_H.as<int>(), err);
+            be_advance<<<pblocks, 256, 0, s>>>(A, dc + DC_NGEN, arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc,
+                                               cap, 0, a_step, p->rta, pal, bprop, B.nm, c->d_w.as<double>(),
+                                               c->d_rprob.as<float>(), c->d_ralt.as<int>(), n,
+                                               mix_key(p->seed, istep, 65), B.d_H.as<int>(), err);
             ck(cudaEventRecord(ev[3], s), "event");
             ck(cudaEventRecord(ev[4], s), "event");  // the histogram is made in the passes above
             // 8. cancellation every cancel_every steps: B -> A; otherwise B is the population
             if (istep % cancel_every == 0) {
                 ck(cudaMemsetAsync(B.d_cnt.p, 0, hbytes, s), "memset");
                 be_cancel_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
-                                                      cap, B.d_H.as<int>(), B.d_cnt.as<int>(), n, d_res.as<int>(),
+                                                      B.d_H.as<int>(), B.d_cnt.as<int>(), n, d_res.as<int>(),
                                                       mix_key(p->seed, istep, 77));
                 ck(cudaMemsetAsync(dc + DC_NP, 0, sizeof(unsigned long long), s), "memset");
                 be_compact_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
-                                                       cap, arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign),
-                                                       dc + DC_NP);
+                                                       arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP);
             } else {
-                be_counters<<<1, 1, 0, s>>>(dc, DC_NP, DC_NOUT, DC_WRIT, nullptr, 0);
+                be_counters<<<1, 1, 0, s>>>(dc, DC_NP, DC_NOUT, nullptr, 0);
                 swap_ab();
             }
             ck(cudaEventRecord(ev[5], s), "event");
             // 9. properties of the step (calculate_prop), recorded on the device
             be_props<<<nbx, 256, 0, s>>>(B.d_H.as<int>(), n, B.d_rvx.as<double>(), B.d_rvy.as<double>(),
                                           B.d_phist.as<double>() + std::size_t(istep + 1) * nbx * 3);
-            // after a compaction the population has no holes: its places are its particles
-            be_counters<<<1, 1, 0, s>>>(dc, -1, 0, istep % cancel_every == 0 ? DC_NP : -1,
-                                        B.d_nhist.as<long long>(), istep + 1);
+            be_counters<<<1, 1, 0, s>>>(dc, -1, 0, B.d_nhist.as<long long>(), istep + 1);
             ck(cudaGetLastError(), "step launch");
             ck(cudaEventRecord(ev[6], s), "event");
             if (p->on_step) {
