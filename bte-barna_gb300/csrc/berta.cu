@@ -704,7 +704,7 @@ __global__ void __launch_bounds__(256) be_advance(PArr in, const unsigned long l
                                                   AdvectArgs aa, int rta, const PAlias* pal, const BoxProp* bprop,
                                                   int nm, const double* w, const float* rprob, const int* ralt,
                                                   int nmodes, unsigned long long skey, int* H, int* err) {
-    const long long n = (long long)*n_in;
+    const long long n = min((long long)*n_in, ocap);  // places beyond the buffers (an overflow) are not read
     const int lane = threadIdx.x & 31;
     if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) {
         if (advect) atomicAdd(dc + DC_PSTEPS, (unsigned long long)n);
@@ -1053,9 +1053,10 @@ __device__ __forceinline__ unsigned long long gcd_u64(unsigned long long a, unsi
     }
     return a;
 }
-__global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, const int* H, int* cnt, int nmodes,
+__global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, long long cap, const int* H, int* cnt,
+                              int nmodes,
                               const int* reservoir, unsigned long long key) {
-    const long long n = (long long)*n_in;
+    const long long n = min((long long)*n_in, cap);
     if (n <= 0) return;
     // the permutation's a, b and the XOR key, drawn by one thread per block
     __shared__ unsigned long long s_ab[2];
@@ -1078,8 +1079,9 @@ __global__ void be_cancel_dev(PArr P, const unsigned long long* n_in, const int*
 }
 
 // Compaction of [0, *n_in) with the survivors counted into *count.
-__global__ void be_compact_dev(PArr in, const unsigned long long* n_in, PArr out, unsigned long long* count) {
-    compact_body(in, (long long)*n_in, out, count);
+__global__ void be_compact_dev(PArr in, const unsigned long long* n_in, long long cap, PArr out,
+                               unsigned long long* count) {
+    compact_body(in, min((long long)*n_in, cap), out, count);
 }
 
 // dc[to] = dc[from]; record[step] = dc[DC_NP] after it.
@@ -1817,11 +1819,11 @@ extern "C" bte_status bte_berta_run(bte_ctx* c, const bte_berta_params* p, bte_b
             // 8. cancellation every cancel_every steps: B -> A; otherwise B is the population
             if (istep % cancel_every == 0) {
                 ck(cudaMemsetAsync(B.d_cnt.p, 0, hbytes, s), "memset");
-                be_cancel_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
+                be_cancel_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT, cap,
                                                       B.d_H.as<int>(), B.d_cnt.as<int>(), n, d_res.as<int>(),
                                                       mix_key(p->seed, istep, 77));
                 ck(cudaMemsetAsync(dc + DC_NP, 0, sizeof(unsigned long long), s), "memset");
-                be_compact_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT,
+                be_compact_dev<<<pblocks, 256, 0, s>>>(arr(B.b_x, B.b_y, B.b_mode, B.b_box, B.b_sign), dc + DC_NOUT, cap,
                                                        arr(B.a_x, B.a_y, B.a_mode, B.a_box, B.a_sign), dc + DC_NP);
             } else {
                 be_counters<<<1, 1, 0, s>>>(dc, DC_NP, DC_NOUT, nullptr, 0);

@@ -271,3 +271,18 @@ def test_berta_phase_times(engine, built, tmp_path):
     assert device <= r["kernel_ms"] * 1.01 + 0.1
     assert ph["saving"] == 0.0  # no on_step hook here
 
+
+
+def test_berta_capacity_overflow_is_an_error_and_the_context_stays_usable(engine):
+    """A population larger than the particle buffers stops with
+    BTE_ERR_LIMIT at the end of the run (the step kernels read no place
+    beyond the buffers and drop what does not fit); the next run on the
+    same context with room enough is unaffected."""
+    m, g, P = _case()
+    engine.load_modes(m)
+    engine.load_geometry(g)
+    engine.load_propagator(P)
+    with pytest.raises(btegpu.BteError, match="capacity"):
+        engine.berta_run(1.0, 20.0, 2e-23, seed=3, capacity=300)
+    r = engine.berta_run(1.0, 20.0, 2e-23, seed=3)
+    assert r["nparticles"][-1] > 300 and np.isfinite(r["ed"]).all()
